@@ -1,0 +1,449 @@
+/*
+ * mypbr_gpu.h — the C ABI of the GB300 path-tracing backend.
+ *
+ * This is the drop-in boundary for mypbr's per-pixel path-tracing loop,
+ *   frame camera::render(const hittable& world, const hittable_list& lights,
+ *                        int save_every, const pass_callback& on_pass)
+ * (include/camera.h:79-105 of the reference). The reference passes a virtual
+ * C++ object graph (hittable / material / texture / light_list,
+ * include/hittable.h:34-60, include/material.h:22-72, include/texture.h:17-22,
+ * include/light_list.h:33-134), which cannot cross a C ABI. Here the same
+ * scene travels as plain arrays (mypbr_flat_scene), built on the host from the
+ * same .scene / OBJ files by mypbr_scene_load (the counterpart of load_scene,
+ * include/scene.h:244), with the BVH already built on the host by the same
+ * binned-SAH rules as include/bvh.h:110-205.
+ *
+ * Everything in the flat scene is FP64 on the host, as the reference stores it
+ * (include/vec3.h:11); the device copy made by mypbr_gpu_scene_create is FP32
+ * apart from the film accumulators, which stay FP64.
+ *
+ * Conventions
+ *   - every function returns a mypbr_status (0 = MYPBR_OK) unless noted;
+ *   - output images are row-major from the top-left pixel, like the reference's
+ *     frame (include/camera.h:71-76, include/denoiser.h:11-20), and hold
+ *     averages over the samples, not sums;
+ *   - buffers passed in are owned by the caller; the library owns device memory
+ *     and the handles it returns;
+ *   - one render per scene handle at a time; functions are not re-entrant on the
+ *     same handle.
+ */
+#ifndef MYPBR_GPU_H
+#define MYPBR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MYPBR_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status */
+
+typedef enum mypbr_status {
+    MYPBR_OK = 0,
+    MYPBR_ERR_CUDA = 1,             /* a CUDA call failed (message via mypbr_last_error) */
+    MYPBR_ERR_UNSUPPORTED = 2,      /* a scene feature this backend does not implement */
+    MYPBR_ERR_QUEUE_OVERFLOW = 3,   /* a device queue ran out of capacity */
+    MYPBR_ERR_DEVICE_TIMEOUT = 4,   /* a bounded device wait gave up */
+    MYPBR_ERR_INVALID_ARGUMENT = 5, /* null pointer, bad size or bad index */
+    MYPBR_ERR_OUT_OF_MEMORY = 6,    /* device or host allocation failed */
+    MYPBR_ERR_BAD_SCENE = 7,        /* the scene text or a referenced file is malformed */
+    MYPBR_ERR_IO = 8,               /* a file could not be opened or read */
+    MYPBR_ERR_NO_DEVICE = 9,        /* no CUDA device is visible */
+    MYPBR_ERR_DEVICE_CHECK = 10     /* a device-side bounds check fired (index recorded) */
+} mypbr_status;
+
+/* Human-readable name of a status code. Never NULL. */
+const char* mypbr_gpu_status_string(int status);
+
+/* The message of the last failure on the calling thread ("" if none). Like the
+ * reference's "path:line: message" on std::cerr (include/scene.h:255-258). */
+const char* mypbr_last_error(void);
+
+/* ------------------------------------------------------------ flat scene */
+
+/* Primitive kinds, as stored in mypbr_prim_ref.kind and light members. */
+enum {
+    MYPBR_PRIM_SPHERE = 0,   /* include/sphere.h:23-52 */
+    MYPBR_PRIM_QUAD = 1,     /* include/quad.h:30-81 */
+    MYPBR_PRIM_TRIANGLE = 2, /* include/mesh.h:47-108 */
+    MYPBR_PRIM_MEDIUM = 3    /* include/medium.h:60-88 */
+};
+
+/* An affine map p -> M p + t with its inverse, as the reference's transform
+ * (include/transform.h:72-173). */
+typedef struct mypbr_xform {
+    double m[3][3];
+    double t[3];
+    double inv_m[3][3];
+    double inv_t[3];
+} mypbr_xform;
+
+/* A sphere; a negative radius flips the normal inwards (include/sphere.h:9-16).
+ * xform >= 0 places the sphere through that transform: the ray is moved into
+ * the sphere's own space, as instance::hit does (include/instance.h:29-41). */
+typedef struct mypbr_sphere {
+    double center[3];
+    double radius;
+    int32_t material;
+    int32_t xform;
+} mypbr_sphere;
+
+/* A parallelogram Q + a u + b v, a, b in [0, 1], in world space (transforms
+ * are baked in). normal is the unit outward normal (include/quad.h:11-18 for an
+ * untransformed quad; the inverse-transpose image for a transformed one). */
+typedef struct mypbr_quad {
+    double q[3], u[3], v[3];
+    double normal[3];
+    int32_t material;
+    int32_t reserved;
+} mypbr_quad;
+
+/* Triangle flags. */
+enum {
+    MYPBR_TRI_FLIP_NORMAL = 1 /* geometric normal is -normalize(e1 x e2) (mirroring transform) */
+};
+
+/* One triangle of a mesh by vertex indices (include/mesh.h:28-44); normal and
+ * uv indices are -1 when absent. Positions are in world space. */
+typedef struct mypbr_triangle {
+    int32_t v[3];
+    int32_t n[3];
+    int32_t t[3];
+    int32_t material;
+    int32_t flags;
+    int32_t mesh; /* index into mypbr_flat_scene.meshes (-1: none) */
+} mypbr_triangle;
+
+/* A mesh = a contiguous range of triangles with one area CDF, used when the
+ * mesh is a light (include/mesh.h:175-216). */
+typedef struct mypbr_mesh {
+    int64_t first_triangle;
+    int64_t triangle_count;
+    int32_t material;
+    int32_t reserved;
+} mypbr_mesh;
+
+/* A homogeneous medium of the given density (collisions per unit length) in
+ * a convex boundary (include/medium.h:289-331). shape 0: sphere (a = centre,
+ * b[0] = radius); shape 1: box (a = min corner, b = max corner). xform >= 0
+ * moves the boundary (the medium keeps world-space distances). */
+typedef struct mypbr_medium {
+    int32_t shape;
+    int32_t xform;
+    int32_t material;
+    int32_t reserved;
+    double density;
+    double a[3], b[3];
+} mypbr_medium;
+
+/* Objects without a finite bounding box, tested beside the BVH
+ * (scene::unbounded, include/scene.h:34-36): the infinite ground
+ * (include/plane.h:17-34) and exponential height fog (include/medium.h:347-390). */
+enum { MYPBR_UNBOUNDED_GROUND = 0, MYPBR_UNBOUNDED_HEIGHT_FOG = 1 };
+typedef struct mypbr_unbounded {
+    int32_t kind;
+    int32_t material;
+    double height;       /* ground: plane y = height; fog: base */
+    double density;      /* fog only */
+    double scale_height; /* fog only */
+} mypbr_unbounded;
+
+/* One node of the host-built BVH, in the reference's depth-first layout
+ * (include/bvh.h:93-98): the left child is the next node; interior nodes keep
+ * the right child's index in offset; leaves keep the first primitive reference
+ * in offset and count > 0. */
+typedef struct mypbr_bvh_node {
+    double bmin[3], bmax[3];
+    int32_t offset;
+    int32_t count;
+    int32_t axis;
+    int32_t reserved;
+} mypbr_bvh_node;
+
+/* A BVH leaf entry: which primitive (kind, index into that kind's array). */
+typedef struct mypbr_prim_ref {
+    int32_t kind;
+    int32_t index;
+} mypbr_prim_ref;
+
+/* ---------------------------------------------------------- appearance */
+
+enum {
+    MYPBR_TEX_SOLID = 0,   /* p[0..2] = colour (include/texture.h:259-270) */
+    MYPBR_TEX_CHECKER = 1, /* p[0] = 1/scale, a = even texture, b = odd (texture.h:273-291) */
+    MYPBR_TEX_IMAGE = 2    /* width x height texels at offset (texture.h:302-444) */
+};
+enum {
+    MYPBR_TEXF_HDR = 1,    /* texels are RGB float in texels_hdr, else RGBA8 in texels_ldr */
+    MYPBR_TEXF_LINEAR = 2, /* 8-bit values are data (k / 255), not sRGB */
+    MYPBR_TEXF_REPEAT = 4  /* wrap (u, v) instead of clamping */
+};
+typedef struct mypbr_texture {
+    int32_t type;
+    int32_t a, b;
+    int32_t width, height;
+    int32_t flags;
+    int64_t offset; /* first texel (ldr: byte offset / 4 per texel; hdr: float offset / 3) */
+    double p[4];
+} mypbr_texture;
+
+enum {
+    MYPBR_MAT_LAMBERTIAN = 0,      /* include/material.h:74-101 */
+    MYPBR_MAT_METAL = 1,           /* include/material.h:109-173 */
+    MYPBR_MAT_DIELECTRIC = 2,      /* include/material.h:184-264 */
+    MYPBR_MAT_THIN_DIELECTRIC = 3, /* include/material.h:683-707 */
+    MYPBR_MAT_PRINCIPLED = 4,      /* include/material.h:346-552 */
+    MYPBR_MAT_DIFFUSE_LIGHT = 5,   /* include/material.h:568-615 */
+    MYPBR_MAT_PHASE = 6            /* include/medium.h:248-274 */
+};
+
+/* Material flags. */
+enum {
+    MYPBR_MATF_MEASURED = 1,   /* metal / principled conductor uses the complex IOR (microfacet.h:98-142) */
+    MYPBR_MATF_COAT = 2,       /* principled has a clear coat (material.h:366-371) */
+    MYPBR_MATF_COAT_TINT = 4   /* principled coat tint differs from white (material.h:379) */
+};
+
+/*
+ * A material. Texture slots hold texture indices (-1 = none). Parameter slots
+ * by type:
+ *   LAMBERTIAN      tex[0] albedo
+ *   METAL           p[0..2] albedo (Schlick f0), p[3] roughness (clamped [0,1]),
+ *                   p[4..6] eta, p[7..9] k (measured), p[10..12] f_avg
+ *   DIELECTRIC      p[0] ior, p[1] roughness, p[2..4] sigma_a
+ *   THIN_DIELECTRIC p[0] ior, p[2..4] tint
+ *   PRINCIPLED      tex[0] base, tex[1] metallic, tex[2] roughness, tex[3] base normal map,
+ *                   tex[4] coat weight, tex[5] coat roughness, tex[6] coat normal map,
+ *                   p[0] dielectric f0, p[4..6] eta, p[7..9] k, p[10..12] conductor f_avg,
+ *                   p[13..15] coat tint
+ *   DIFFUSE_LIGHT   p[0..2] emission, p[3] spread (degrees), p[4] tan(spread/2) (inf = none),
+ *                   p[5] cosine share
+ *   PHASE           p[0..2] albedo, p[3] g
+ * Wrappers, any type:
+ *   normal_map  >= 0: normal_mapped wrapper (material.h:631-674) with that texture
+ *   emission_tex >= 0: emissive_surface wrapper (material.h:714-741)
+ */
+typedef struct mypbr_material {
+    int32_t type;
+    int32_t flags;
+    int32_t tex[8];
+    int32_t normal_map;
+    int32_t emission_tex;
+    double p[16];
+} mypbr_material;
+
+/* --------------------------------------------------------------- lights */
+
+enum {
+    MYPBR_LIGHT_GROUP = 0,       /* a primitive, a box (6 quads) or a mesh */
+    MYPBR_LIGHT_ENVIRONMENT = 1, /* include/environment.h:163-349 */
+    MYPBR_LIGHT_SUN = 2          /* include/sun.h:23-83 */
+};
+
+/* A light of the light list (include/light_list.h:33-134). Its members are
+ * light_members[first_member .. first_member + member_count): it is sampled by
+ * picking a member by member_cdf and a direction towards that member; its pdf
+ * is the member-weighted sum (hittable_list.h:107-124, mesh.h:197-216).
+ * probability is the power-based selection probability p_k
+ * (light_list.h:45-96), and the lights' CDF is the running sum. */
+typedef struct mypbr_light {
+    int32_t kind;
+    int32_t first_member;
+    int32_t member_count;
+    int32_t reserved;
+    double probability;
+} mypbr_light;
+
+typedef struct mypbr_light_member {
+    int32_t prim_kind;
+    int32_t prim_index;
+    double weight; /* selection probability within the light */
+} mypbr_light_member;
+
+/* An equirectangular environment (include/environment.h:163-349): width x
+ * height RGB floats, row 0 at +y. width == 0 means none. */
+typedef struct mypbr_environment {
+    int32_t width, height;
+    const float* pixels;
+    double intensity;
+    double rotation; /* in turns */
+} mypbr_environment;
+
+/* A sun (include/sun.h:23-83). enabled == 0 means none. */
+typedef struct mypbr_sun {
+    int32_t enabled;
+    int32_t disk_visible;
+    double direction[3]; /* unit, towards the sun */
+    double angular_diameter; /* degrees */
+    double irradiance[3];
+} mypbr_sun;
+
+/* The whole scene as plain arrays. */
+typedef struct mypbr_flat_scene {
+    uint32_t abi_version;
+    uint32_t reserved0;
+
+    const mypbr_sphere* spheres;       int64_t sphere_count;
+    const mypbr_quad* quads;           int64_t quad_count;
+    const double* positions;           int64_t position_count; /* xyz triples */
+    const double* normals;             int64_t normal_count;   /* xyz triples */
+    const double* uvs;                 int64_t uv_count;       /* uv pairs */
+    const mypbr_triangle* triangles;   int64_t triangle_count;
+    const mypbr_mesh* meshes;          int64_t mesh_count;
+    const mypbr_medium* media;         int64_t medium_count;
+    const mypbr_xform* xforms;         int64_t xform_count;
+    const mypbr_unbounded* unbounded;  int64_t unbounded_count;
+
+    const mypbr_bvh_node* bvh_nodes;   int64_t bvh_node_count;
+    const mypbr_prim_ref* bvh_prims;   int64_t bvh_prim_count;
+
+    const mypbr_material* materials;   int64_t material_count;
+    const mypbr_texture* textures;     int64_t texture_count;
+    const uint8_t* texels_ldr;         int64_t texels_ldr_bytes;
+    const float* texels_hdr;           int64_t texels_hdr_count;
+
+    const mypbr_light* lights;               int64_t light_count;
+    const mypbr_light_member* light_members; int64_t light_member_count;
+    mypbr_environment environment;
+    mypbr_sun sun;
+
+    /* The sky seen by escaping rays when there is no environment
+     * (include/camera.h:41-42, :515-529): the gradient, or a constant. */
+    int32_t use_sky;
+    int32_t reserved1;
+    double background[3];
+} mypbr_flat_scene;
+
+/* --------------------------------------------------------------- camera */
+
+/* The reference camera's public settings (include/camera.h:20-56) that shape
+ * rays. image_height is int(image_width / aspect_ratio), at least 1
+ * (camera.h:143-144); mypbr_camera_init fills it. */
+typedef struct mypbr_camera {
+    int32_t image_width;
+    int32_t image_height;
+    double aspect_ratio;
+    double vfov;
+    double lookfrom[3], lookat[3], vup[3];
+    double defocus_angle;
+    double focus_dist;
+    double ortho_height;
+    int32_t blades;
+    int32_t reserved;
+    double blade_rotation;
+} mypbr_camera;
+
+/* The reference camera's defaults (camera.h:20-56). */
+void mypbr_camera_init(mypbr_camera* cam);
+
+/* Render settings: the integrator knobs of camera.h:23-34 plus this backend's. */
+typedef struct mypbr_render_opts {
+    int32_t samples_per_pixel;   /* camera.h:23 */
+    int32_t max_depth;           /* camera.h:24 */
+    int32_t max_diffuse;         /* camera.h:27, 0 = no cap */
+    int32_t max_specular;        /* camera.h:28 */
+    int32_t max_scatter;         /* camera.h:29 */
+    int32_t transparent_shadows; /* camera.h:34 */
+    int32_t collect_features;    /* camera.h:56: also fill albedo, normal, variance */
+    int32_t guided;              /* reserved for the path-guiding proposal; must be 0 */
+    uint64_t seed;               /* seeds the counter-based random numbers */
+    int32_t samples_per_wave;    /* passes traced together (0 = automatic) */
+    int32_t reserved;
+} mypbr_render_opts;
+
+void mypbr_render_opts_init(mypbr_render_opts* opts);
+
+/* ------------------------------------------------------------ host layer */
+
+typedef struct mypbr_host_scene mypbr_host_scene;
+
+/* Parses a .scene file (grammar of include/scene.h:44-243) with its OBJ meshes
+ * and .hdr environment, builds the SAH BVH and the light list, and returns the
+ * flat scene plus the camera and render settings the file gives. On failure,
+ * *out is NULL and mypbr_last_error() holds "path:line: message". */
+int mypbr_scene_load(const char* path, mypbr_host_scene** out);
+
+/* The same from text in memory; relative paths resolve against base_dir. */
+int mypbr_scene_parse(const char* text, const char* base_dir, mypbr_host_scene** out);
+
+const mypbr_flat_scene* mypbr_scene_flat(const mypbr_host_scene* s);
+const mypbr_camera* mypbr_scene_camera(const mypbr_host_scene* s);
+const mypbr_render_opts* mypbr_scene_render_opts(const mypbr_host_scene* s);
+void mypbr_scene_free(mypbr_host_scene* s);
+
+/* The Kulla-Conty tables E[32][32] (row = roughness, column = mu) then
+ * E_avg[32], built on the host by the reference's deterministic VNDF
+ * quadrature (include/microfacet.h:299-337). out must hold 1056 doubles. */
+int mypbr_ggx_albedo_table(double* out);
+
+/* ---------------------------------------------------------- device layer */
+
+typedef struct mypbr_gpu_scene mypbr_gpu_scene;
+
+/* Copies the flat scene to HBM (FP32 geometry, compact BVH) on the current
+ * CUDA device. The flat scene may be freed afterwards. */
+int mypbr_gpu_scene_create(const mypbr_flat_scene* scene, mypbr_gpu_scene** out);
+void mypbr_gpu_scene_destroy(mypbr_gpu_scene* scene);
+
+/* Called between passes with the number of samples per pixel done; the output
+ * buffers then hold the running average (camera.h:95-102). */
+typedef void (*mypbr_pass_callback)(int done, void* user);
+
+/* Renders the scene: the replacement for camera::render (camera.h:79-105).
+ * radiance: W*H*3 doubles (required). albedo, normal: W*H*3, variance: W*H;
+ * filled when opts->collect_features, otherwise may be NULL. The call is
+ * synchronous. If save_every > 0, on_pass is called every save_every passes
+ * (not after the last one). */
+int mypbr_gpu_render(mypbr_gpu_scene* scene, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                     double* radiance, double* albedo, double* normal, double* variance,
+                     int save_every, mypbr_pass_callback on_pass, void* user);
+
+/* The same, with outputs left in device memory (each a device pointer of the
+ * sizes above, NULL allowed as for mypbr_gpu_render) and work issued on the
+ * given CUDA stream (NULL = the legacy default stream). Returns once the
+ * work is queued; stats (optional) are filled after a stream sync. */
+typedef struct mypbr_render_stats {
+    uint64_t paths;            /* camera rays traced */
+    uint64_t extension_rays;   /* closest-hit rays traced for path continuation */
+    uint64_t shadow_rays;      /* shadow rays traced */
+    uint64_t kernel_launches;  /* kernels this call launched */
+} mypbr_render_stats;
+
+int mypbr_gpu_render_device(mypbr_gpu_scene* scene, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                            double* d_radiance, double* d_albedo, double* d_normal, double* d_variance,
+                            void* cuda_stream, mypbr_render_stats* stats);
+
+/* mypbr_gpu_render with, in addition, the per-channel variance of the mean
+ * radiance (W*H*3 doubles, may be NULL) from the per-sample second moments,
+ * and render statistics (may be NULL). */
+int mypbr_gpu_render_ex(mypbr_gpu_scene* scene, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                        double* radiance, double* albedo, double* normal, double* variance,
+                        double* channel_variance, int save_every, mypbr_pass_callback on_pass, void* user,
+                        mypbr_render_stats* stats);
+
+/* Ray batch query: closest hit of n rays against the scene, the reference's
+ * world.hit (hittable_list.h:25-37 over bvh.h:45-86 and scene::unbounded)
+ * without media (media are stochastic). rays: n x 8 floats (ox oy oz dx dy dz
+ * tmin tmax), device or host memory as `on_device` says. hits: n x 8 floats
+ * (t, nx, ny, nz, u, v, front_face, unused) and prim: n x 2 int32 (kind,
+ * index; kind -1 on a miss; the ground plane reports kind 4). */
+int mypbr_gpu_trace(mypbr_gpu_scene* scene, const float* rays, int64_t n, float* hits, int32_t* prim,
+                    int on_device);
+
+/* Pointwise BSDF query, for parity checks of eval / pdf (material.h:35-44 and
+ * the scatter() pdf): for each of n records evaluates material `material` at a
+ * surface point. rec: n x 16 floats (p xyz, normal xyz, front_face, u, v,
+ * dpdu xyz, dpdv xyz, unused), r_in: n x 3 floats (incoming direction),
+ * wi: n x 3 floats (outgoing direction). out: n x 4 floats (eval rgb, pdf).
+ * Host memory. */
+int mypbr_gpu_bsdf_eval(mypbr_gpu_scene* scene, int32_t material, const float* rec, const float* r_in,
+                        const float* wi, int64_t n, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MYPBR_GPU_H */

@@ -1,0 +1,297 @@
+"""mypbr_gb300 — the GB300 backend of mypbr's per-pixel path-tracing loop.
+
+The Python side mirrors the reference's host interface for this path:
+
+    scene.h:244   load_scene(path, scene&)        ->  load_scene(path) -> Scene
+    camera.h:19   class camera (public settings)  ->  Camera (same attribute names)
+    camera.h:79   frame camera::render(world, lights, save_every, on_pass)
+                                                  ->  Camera.render(gpu_scene, save_every, on_pass) -> Frame
+    denoiser.h:14 class frame                     ->  Frame (radiance, albedo, normal, variance)
+
+Everything runs through the C ABI of include/mypbr_gpu.h, implemented by the
+in-tree library mypbr_gb300/_lib/libmypbr_gb300.so (hand-written CUDA for
+sm_103a plus the C++ host scene layer). There is no CPU fallback: if the
+library is missing or no GPU is visible, rendering raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libmypbr_gb300.so")
+
+MYPBR_OK = 0
+STATUS_NAMES = {
+    0: "MYPBR_OK", 1: "MYPBR_ERR_CUDA", 2: "MYPBR_ERR_UNSUPPORTED", 3: "MYPBR_ERR_QUEUE_OVERFLOW",
+    4: "MYPBR_ERR_DEVICE_TIMEOUT", 5: "MYPBR_ERR_INVALID_ARGUMENT", 6: "MYPBR_ERR_OUT_OF_MEMORY",
+    7: "MYPBR_ERR_BAD_SCENE", 8: "MYPBR_ERR_IO", 9: "MYPBR_ERR_NO_DEVICE", 10: "MYPBR_ERR_DEVICE_CHECK",
+}
+
+
+class MypbrError(RuntimeError):
+    """A non-zero mypbr_status, with the library's message."""
+
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class CameraStruct(ctypes.Structure):
+    """mypbr_camera (include/mypbr_gpu.h)."""
+    _fields_ = [("image_width", ctypes.c_int32), ("image_height", ctypes.c_int32),
+                ("aspect_ratio", ctypes.c_double), ("vfov", ctypes.c_double),
+                ("lookfrom", ctypes.c_double * 3), ("lookat", ctypes.c_double * 3), ("vup", ctypes.c_double * 3),
+                ("defocus_angle", ctypes.c_double), ("focus_dist", ctypes.c_double),
+                ("ortho_height", ctypes.c_double), ("blades", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("blade_rotation", ctypes.c_double)]
+
+
+class RenderOptsStruct(ctypes.Structure):
+    """mypbr_render_opts (include/mypbr_gpu.h)."""
+    _fields_ = [("samples_per_pixel", ctypes.c_int32), ("max_depth", ctypes.c_int32),
+                ("max_diffuse", ctypes.c_int32), ("max_specular", ctypes.c_int32),
+                ("max_scatter", ctypes.c_int32), ("transparent_shadows", ctypes.c_int32),
+                ("collect_features", ctypes.c_int32), ("guided", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("samples_per_wave", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class RenderStatsStruct(ctypes.Structure):
+    """mypbr_render_stats (include/mypbr_gpu.h)."""
+    _fields_ = [("paths", ctypes.c_uint64), ("extension_rays", ctypes.c_uint64),
+                ("shadow_rays", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
+
+
+PASS_CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_void_p)
+
+_lib = None
+
+
+def lib():
+    """The loaded C-ABI library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise MypbrError(9, f"{LIB_PATH} is missing: build it with mypbr_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    dp, fp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)
+    L.mypbr_gpu_status_string.restype = ctypes.c_char_p
+    L.mypbr_gpu_status_string.argtypes = [ctypes.c_int]
+    L.mypbr_last_error.restype = ctypes.c_char_p
+    L.mypbr_scene_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
+    L.mypbr_scene_parse.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]
+    L.mypbr_scene_flat.restype = vp
+    L.mypbr_scene_flat.argtypes = [vp]
+    L.mypbr_scene_camera.restype = ctypes.POINTER(CameraStruct)
+    L.mypbr_scene_camera.argtypes = [vp]
+    L.mypbr_scene_render_opts.restype = ctypes.POINTER(RenderOptsStruct)
+    L.mypbr_scene_render_opts.argtypes = [vp]
+    L.mypbr_scene_free.argtypes = [vp]
+    L.mypbr_scene_free.restype = None
+    L.mypbr_ggx_albedo_table.argtypes = [dp]
+    L.mypbr_camera_init.argtypes = [ctypes.POINTER(CameraStruct)]
+    L.mypbr_camera_init.restype = None
+    L.mypbr_render_opts_init.argtypes = [ctypes.POINTER(RenderOptsStruct)]
+    L.mypbr_render_opts_init.restype = None
+    L.mypbr_gpu_scene_create.argtypes = [vp, ctypes.POINTER(vp)]
+    L.mypbr_gpu_scene_destroy.argtypes = [vp]
+    L.mypbr_gpu_scene_destroy.restype = None
+    L.mypbr_gpu_render.argtypes = [vp, ctypes.POINTER(CameraStruct), ctypes.POINTER(RenderOptsStruct), vp, vp, vp,
+                                   vp, ctypes.c_int, PASS_CALLBACK, vp]
+    L.mypbr_gpu_render_device.argtypes = [vp, ctypes.POINTER(CameraStruct), ctypes.POINTER(RenderOptsStruct), vp,
+                                          vp, vp, vp, vp, ctypes.POINTER(RenderStatsStruct)]
+    L.mypbr_gpu_trace.argtypes = [vp, fp, i64, fp, ip, ctypes.c_int]
+    L.mypbr_gpu_bsdf_eval.argtypes = [vp, i32, fp, fp, fp, i64, fp]
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != MYPBR_OK:
+        raise MypbrError(status, lib().mypbr_last_error().decode(errors="replace"))
+
+
+class Frame:
+    """What a render produces per pixel, rows from the top left (denoiser.h:14-20).
+    radiance, albedo, normal: (H, W, 3) float64; variance: (H, W)."""
+
+    def __init__(self, radiance, albedo=None, normal=None, variance=None):
+        self.radiance = radiance
+        self.albedo = albedo
+        self.normal = normal
+        self.variance = variance
+
+
+class Scene:
+    """A scene loaded on the host: the flat arrays of the C ABI plus the camera
+    and render settings its file gives (scene.h:32-40)."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle)
+        L = lib()
+        self.camera = Camera(L.mypbr_scene_camera(self._h).contents, L.mypbr_scene_render_opts(self._h).contents)
+
+    @property
+    def flat(self):
+        """Address of the mypbr_flat_scene (valid while this Scene lives)."""
+        return lib().mypbr_scene_flat(self._h)
+
+    def close(self):
+        if self._h:
+            lib().mypbr_scene_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def load_scene(path):
+    """Parses a .scene file (the grammar of the reference's scene.h:44-243)."""
+    out = ctypes.c_void_p()
+    check(lib().mypbr_scene_load(os.fsencode(path), ctypes.byref(out)))
+    return Scene(out.value)
+
+
+def parse_scene(text, base_dir="."):
+    """The same from text; relative file names resolve against base_dir."""
+    out = ctypes.c_void_p()
+    check(lib().mypbr_scene_parse(text.encode(), os.fsencode(base_dir), ctypes.byref(out)))
+    return Scene(out.value)
+
+
+class GpuScene:
+    """The scene in HBM (mypbr_gpu_scene_create)."""
+
+    def __init__(self, scene):
+        out = ctypes.c_void_p()
+        check(lib().mypbr_gpu_scene_create(scene.flat, ctypes.byref(out)))
+        self._h = out
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().mypbr_gpu_scene_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace(self, rays):
+        """Closest hits of rays (n, 8) float32 [o, d, tmin, tmax]: returns
+        hits (n, 8) float32 [t, normal, u, v, front_face, -] and prim (n, 2) int32."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[0]
+        hits = np.zeros((n, 8), dtype=np.float32)
+        prim = np.zeros((n, 2), dtype=np.int32)
+        fp, ip = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)
+        check(lib().mypbr_gpu_trace(self._h, rays.ctypes.data_as(fp), n, hits.ctypes.data_as(fp),
+                                    prim.ctypes.data_as(ip), 0))
+        return hits, prim
+
+    def bsdf_eval(self, material, rec, r_in, wi):
+        """eval rgb and scatter pdf of material at records rec (n, 16)."""
+        rec = np.ascontiguousarray(rec, dtype=np.float32)
+        r_in = np.ascontiguousarray(r_in, dtype=np.float32)
+        wi = np.ascontiguousarray(wi, dtype=np.float32)
+        n = rec.shape[0]
+        out = np.zeros((n, 4), dtype=np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        check(lib().mypbr_gpu_bsdf_eval(self._h, int(material), rec.ctypes.data_as(fp), r_in.ctypes.data_as(fp),
+                                        wi.ctypes.data_as(fp), n, out.ctypes.data_as(fp)))
+        return out
+
+
+class Camera:
+    """The reference camera's settings (camera.h:20-56) as attributes."""
+
+    _CAM = {"image_width", "aspect_ratio", "vfov", "lookfrom", "lookat", "vup", "defocus_angle", "focus_dist",
+            "ortho_height", "blades", "blade_rotation"}
+    _OPT = {"samples_per_pixel", "max_depth", "max_diffuse", "max_specular", "max_scatter", "transparent_shadows",
+            "collect_features", "seed", "samples_per_wave", "guided"}
+
+    def __init__(self, cam=None, opts=None):
+        c = CameraStruct()
+        o = RenderOptsStruct()
+        if cam is None:
+            lib().mypbr_camera_init(ctypes.byref(c))
+        else:
+            ctypes.memmove(ctypes.byref(c), ctypes.byref(cam), ctypes.sizeof(c))
+        if opts is None:
+            lib().mypbr_render_opts_init(ctypes.byref(o))
+        else:
+            ctypes.memmove(ctypes.byref(o), ctypes.byref(opts), ctypes.sizeof(o))
+        object.__setattr__(self, "_c", c)
+        object.__setattr__(self, "_o", o)
+
+    def __getattr__(self, name):
+        if name in Camera._CAM:
+            v = getattr(self._c, name)
+            return tuple(v) if name in ("lookfrom", "lookat", "vup") else v
+        if name in Camera._OPT:
+            return getattr(self._o, name)
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name in Camera._CAM:
+            if name in ("lookfrom", "lookat", "vup"):
+                arr = getattr(self._c, name)
+                for k in range(3):
+                    arr[k] = float(value[k])
+            else:
+                setattr(self._c, name, value)
+        elif name in Camera._OPT:
+            setattr(self._o, name, int(value))
+        else:
+            raise AttributeError(name)
+
+    def height(self):
+        h = int(self._c.image_width / self._c.aspect_ratio)
+        return max(h, 1)
+
+    def structs(self):
+        """The (mypbr_camera, mypbr_render_opts) pair, with image_height set."""
+        self._c.image_height = self.height()
+        return self._c, self._o
+
+    def render(self, gpu_scene, save_every=0, on_pass=None):
+        """Renders on the GPU and returns the Frame (camera::render, camera.h:79-105).
+        on_pass(done, frame) is called every save_every passes."""
+        c, o = self.structs()
+        w, h = c.image_width, c.image_height
+        rad = np.zeros((h, w, 3), dtype=np.float64)
+        feats = bool(o.collect_features)
+        alb = np.zeros((h, w, 3), dtype=np.float64) if feats else None
+        nrm = np.zeros((h, w, 3), dtype=np.float64) if feats else None
+        var = np.zeros((h, w), dtype=np.float64) if feats else None
+
+        def ptr(a):
+            return ctypes.c_void_p(a.ctypes.data) if a is not None else ctypes.c_void_p()
+
+        if on_pass is not None:
+            def trampoline(done, _user):
+                on_pass(done, Frame(rad.copy(), None if alb is None else alb.copy(),
+                                    None if nrm is None else nrm.copy(), None if var is None else var.copy()))
+            cb = PASS_CALLBACK(trampoline)
+        else:
+            cb = PASS_CALLBACK()
+        check(lib().mypbr_gpu_render(gpu_scene.handle, ctypes.byref(c), ctypes.byref(o), ptr(rad), ptr(alb),
+                                     ptr(nrm), ptr(var), int(save_every), cb, None))
+        return Frame(rad, alb, nrm, var)
+
+
+def ggx_albedo_table():
+    """The Kulla-Conty tables the device uses: (E[32, 32], E_avg[32])."""
+    out = np.zeros(32 * 32 + 32, dtype=np.float64)
+    check(lib().mypbr_ggx_albedo_table(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return out[:1024].reshape(32, 32), out[1024:]

@@ -1,0 +1,589 @@
+// The scene as the kernels see it (FP32, in HBM) and the geometric queries on
+// it: primitive intersection, the BVH walk and surface reconstruction.
+//
+// Layout (built by scene_gpu.cu from the flat FP64 scene):
+//   bvh         4 float4 per interior node: child 0 box (lo.xyz | index),
+//               (hi.xyz | count), child 1 likewise. count 0: index is an
+//               interior node; count > 0: index is the first of `count` leaf
+//               references. Boxes are rounded outwards to FP32. Loaded with
+//               128-bit loads through the read-only path.
+//   leaf_refs   (kind << 29 | index) per leaf slot.
+//   spheres     float4 (centre, radius) + int2 (material, xform).
+//   quads       5 float4: (Q | material), u, v, unit normal n, w = (u x v) / |u x v|^2.
+//   triangles   3 float4 (v0 | material), (v1 | flags), (v2 | mesh); shading
+//               indices in tri_shading (n0 n1 n2 t0) (t1 t2 - -).
+//   media       3 float4: (a | density), (b | shape), (xform, material, -, -).
+//   xforms      6 float4: forward rows (m | t), inverse rows (m^-1 | t^-1).
+#pragma once
+
+#include "dev_math.cuh"
+
+namespace mypbr_dev {
+
+enum : int { kSphere = 0, kQuad = 1, kTriangle = 2, kMedium = 3, kGround = 4, kHeightFog = 5 };
+
+constexpr int kBvhStack = 64;
+constexpr uint32_t kKindShift = 29;
+constexpr uint32_t kIndexMask = (1u << kKindShift) - 1;
+
+struct DevUnbounded {
+    int kind, material;
+    float height, density, scale_height, pad0, pad1, pad2;
+};
+
+struct DevMaterial {
+    int type, flags, normal_map, emission_tex;
+    int tex[8];
+    float p[16];
+};
+
+struct DevTexture {
+    int type, a, b, width, height, flags;
+    long long offset;
+    float p[4];
+};
+
+struct DevLight {
+    int kind, first_member, member_count, pad;
+    float probability, cdf_hi, pad1, pad2;  // cdf_hi: running sum up to and including this light
+};
+
+struct DevMember {
+    int kind, index;
+    float weight, cdf;  // cdf: running sum within the light up to and including this member
+};
+
+struct DeviceScene {
+    // geometry
+    const float4* bvh;
+    const uint32_t* leaf_refs;
+    const float4* spheres;
+    const int2* sphere_info;
+    const float4* quads;
+    const float4* tris;
+    const int4* tri_shading;
+    const float3* normals;
+    const float2* uvs;
+    const float4* media;
+    const float4* xforms;
+    const DevUnbounded* unbounded;
+    int unbounded_count;
+    int has_bvh;
+    // appearance
+    const DevMaterial* materials;
+    const DevTexture* textures;
+    const uint8_t* texels_ldr;
+    const float* texels_hdr;
+    const float* ggx_e;     // 32 x 32
+    const float* ggx_eavg;  // 32
+    // lights
+    const DevLight* lights;
+    const DevMember* members;
+    int light_count;
+    // environment
+    int env_w, env_h;
+    const float4* env_pixels;   // rgb, pad
+    const float* env_texel_pdf; // p_ij * W * H
+    const float2* env_alias;    // (probability, alias index as float bits)
+    float env_intensity, env_rotation;
+    // sun
+    int sun_enabled, sun_disk_visible;
+    float3 sun_dir;
+    float sun_cos_max, sun_solid_angle;
+    float3 sun_radiance;
+    // sky without an environment
+    int use_sky;
+    float3 background;
+};
+
+MYPBR_DEV float4 ldg4(const float4* p) { return __ldg(p); }
+
+// ------------------------------------------------------------- transforms
+
+struct XformRef {
+    float4 r[6];
+};
+MYPBR_DEV void load_xform(const DeviceScene& S, int x, XformRef& X) {
+    const float4* p = S.xforms + 6 * x;
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        X.r[k] = ldg4(p + k);
+}
+MYPBR_DEV float3 xf_point(const XformRef& X, float3 p) {
+    return f3(X.r[0].x * p.x + X.r[0].y * p.y + X.r[0].z * p.z + X.r[0].w,
+              X.r[1].x * p.x + X.r[1].y * p.y + X.r[1].z * p.z + X.r[1].w,
+              X.r[2].x * p.x + X.r[2].y * p.y + X.r[2].z * p.z + X.r[2].w);
+}
+MYPBR_DEV float3 xf_vec(const XformRef& X, float3 v) {
+    return f3(X.r[0].x * v.x + X.r[0].y * v.y + X.r[0].z * v.z, X.r[1].x * v.x + X.r[1].y * v.y + X.r[1].z * v.z,
+              X.r[2].x * v.x + X.r[2].y * v.y + X.r[2].z * v.z);
+}
+MYPBR_DEV float3 xf_ipoint(const XformRef& X, float3 p) {
+    return f3(X.r[3].x * p.x + X.r[3].y * p.y + X.r[3].z * p.z + X.r[3].w,
+              X.r[4].x * p.x + X.r[4].y * p.y + X.r[4].z * p.z + X.r[4].w,
+              X.r[5].x * p.x + X.r[5].y * p.y + X.r[5].z * p.z + X.r[5].w);
+}
+MYPBR_DEV float3 xf_ivec(const XformRef& X, float3 v) {
+    return f3(X.r[3].x * v.x + X.r[3].y * v.y + X.r[3].z * v.z, X.r[4].x * v.x + X.r[4].y * v.y + X.r[4].z * v.z,
+              X.r[5].x * v.x + X.r[5].y * v.y + X.r[5].z * v.z);
+}
+// Normals map by the inverse transpose.
+MYPBR_DEV float3 xf_normal(const XformRef& X, float3 n) {
+    return f3(X.r[3].x * n.x + X.r[4].x * n.y + X.r[5].x * n.z, X.r[3].y * n.x + X.r[4].y * n.y + X.r[5].y * n.z,
+              X.r[3].z * n.x + X.r[4].z * n.y + X.r[5].z * n.z);
+}
+
+// ------------------------------------------------------------ primitives
+
+// Ray/sphere roots in object space with the discriminant formed from the
+// squared distance of the centre to the ray's line (Haines et al., "Precision
+// Improvements for Ray/Sphere Intersection", Ray Tracing Gems 2019, ch. 7),
+// which keeps FP32 accurate for large spheres such as a ground of radius 1000.
+// Returns the nearest root in (tmin, tmax), the reference's rule (sphere.h:23-52).
+MYPBR_DEV bool sphere_root(float3 c, float r, float3 o, float3 d, float tmin, float tmax, float& t) {
+    float a = dot(d, d);
+    float3 f = o - c;
+    float b = -dot(f, d);  // = dot(d, c - o)
+    float3 l = f + (b / a) * d;  // offset of the closest point of the line from the centre
+    float disc = a * (r * r - dot(l, l));
+    if (disc < 0.0f)
+        return false;
+    float sq = sqrtf(disc);
+    float q = b + copysignf(sq, b);
+    float cc = dot(f, f) - r * r;
+    float r0 = cc / q, r1 = q / a;
+    if (q == 0.0f) {
+        r0 = r1 = b / a;
+    }
+    float lo = fminf(r0, r1), hi = fmaxf(r0, r1);
+    if (lo > tmin && lo < tmax) {
+        t = lo;
+        return true;
+    }
+    if (hi > tmin && hi < tmax) {
+        t = hi;
+        return true;
+    }
+    return false;
+}
+
+MYPBR_DEV bool hit_sphere(const DeviceScene& S, int i, float3 o, float3 d, float tmin, float tmax, float& t) {
+    float4 s = ldg4(S.spheres + i);
+    int xf = __ldg(&S.sphere_info[i].y);
+    if (xf < 0)
+        return sphere_root(f3(s), s.w, o, d, tmin, tmax, t);
+    XformRef X;
+    load_xform(S, xf, X);
+    return sphere_root(f3(s), s.w, xf_ipoint(X, o), xf_ivec(X, d), tmin, tmax, t);
+}
+
+// Plane t, then the parallelogram test 0 <= a, b <= 1 (quad.h:30-62).
+MYPBR_DEV bool hit_quad(const DeviceScene& S, int i, float3 o, float3 d, float tmin, float tmax, float& t, float& a,
+                        float& b) {
+    const float4* q = S.quads + 5 * i;
+    float4 Q = ldg4(q), n = ldg4(q + 3);
+    float3 N = f3(n);
+    float denom = dot(N, d);
+    if (fabsf(denom) < 1e-8f)
+        return false;
+    float tt = dot(N, f3(Q) - o) / denom;
+    if (!(tt >= tmin && tt <= tmax))
+        return false;
+    float3 hp = (o - f3(Q)) + tt * d;
+    float3 u = f3(ldg4(q + 1)), v = f3(ldg4(q + 2)), w = f3(ldg4(q + 4));
+    float al = dot(w, cross(hp, v)), be = dot(w, cross(u, hp));
+    if (al < 0.0f || al > 1.0f || be < 0.0f || be > 1.0f)
+        return false;
+    t = tt;
+    a = al;
+    b = be;
+    return true;
+}
+
+// Per-ray constants of the watertight ray/triangle test (Woop, Benthin and
+// Wald, "Watertight Ray/Triangle Intersection", JCGT 2013).
+struct TriRay {
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+MYPBR_DEV TriRay make_tri_ray(float3 d) {
+    TriRay r;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    r.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    r.kx = r.kz == 2 ? 0 : r.kz + 1;
+    r.ky = r.kx == 2 ? 0 : r.kx + 1;
+    if (comp(d, r.kz) < 0.0f) {
+        int tmp = r.kx;
+        r.kx = r.ky;
+        r.ky = tmp;
+    }
+    float dz = comp(d, r.kz);
+    r.sx = comp(d, r.kx) / dz;
+    r.sy = comp(d, r.ky) / dz;
+    r.sz = 1.0f / dz;
+    return r;
+}
+
+// Barycentrics b1, b2 are the weights of v1 and v2, the reference's (u, v)
+// without texture coordinates (mesh.h:72-79).
+MYPBR_DEV bool hit_triangle(const DeviceScene& S, int i, float3 o, const TriRay& R, float tmin, float tmax, float& t,
+                            float& b1, float& b2) {
+    const float4* tp = S.tris + 3 * i;
+    float3 A = f3(ldg4(tp)) - o, B = f3(ldg4(tp + 1)) - o, C = f3(ldg4(tp + 2)) - o;
+    float Az = comp(A, R.kz), Bz = comp(B, R.kz), Cz = comp(C, R.kz);
+    float Ax = comp(A, R.kx) - R.sx * Az, Ay = comp(A, R.ky) - R.sy * Az;
+    float Bx = comp(B, R.kx) - R.sx * Bz, By = comp(B, R.ky) - R.sy * Bz;
+    float Cx = comp(C, R.kx) - R.sx * Cz, Cy = comp(C, R.ky) - R.sy * Cz;
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        // Exactly on an edge in FP32: decide in FP64, as the paper prescribes
+        U = float(double(Cx) * double(By) - double(Cy) * double(Bx));
+        V = float(double(Ax) * double(Cy) - double(Ay) * double(Cx));
+        W = float(double(Bx) * double(Ay) - double(By) * double(Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f))
+        return false;
+    float det = U + V + W;
+    if (det == 0.0f)
+        return false;
+    float T = R.sz * (U * Az + V * Bz + W * Cz);
+    float inv = 1.0f / det;
+    float tt = T * inv;
+    if (!(tt > tmin && tt < tmax))
+        return false;
+    t = tt;
+    b1 = V * inv;
+    b2 = W * inv;
+    return true;
+}
+
+// Where a line enters and leaves a medium's convex boundary (medium.h:298-302).
+MYPBR_DEV bool medium_span(const DeviceScene& S, int i, float3 o, float3 d, float& t_in, float& t_out, float& density,
+                           int& material) {
+    const float4* m = S.media + 3 * i;
+    float4 A = ldg4(m), B = ldg4(m + 1), C = ldg4(m + 2);
+    density = A.w;
+    int shape = __float_as_int(B.w), xf = __float_as_int(C.x);
+    material = __float_as_int(C.y);
+    float3 lo = o, ld = d;
+    if (xf >= 0) {
+        XformRef X;
+        load_xform(S, xf, X);
+        lo = xf_ipoint(X, o);
+        ld = xf_ivec(X, d);
+    }
+    if (shape == 0) {
+        float3 c = f3(A);
+        float r = B.x;
+        float a = dot(ld, ld);
+        float3 f = lo - c;
+        float b = -dot(f, ld);
+        float3 l = f + (b / a) * ld;
+        float disc = a * (r * r - dot(l, l));
+        if (disc < 0.0f)
+            return false;
+        float sq = sqrtf(disc);
+        t_in = (b - sq) / a;
+        t_out = (b + sq) / a;
+        return t_out > t_in + 0.0001f;
+    }
+    float t0 = -3.0e38f, t1 = 3.0e38f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float mn = fminf(comp(f3(A), k), comp(f3(B), k)), mx = fmaxf(comp(f3(A), k), comp(f3(B), k));
+        float dk = comp(ld, k), ok = comp(lo, k);
+        if (dk == 0.0f) {
+            if (ok < mn || ok > mx)
+                return false;
+            continue;
+        }
+        float ta = (mn - ok) / dk, tb = (mx - ok) / dk;
+        t0 = fmaxf(t0, fminf(ta, tb));
+        t1 = fminf(t1, fmaxf(ta, tb));
+    }
+    t_in = t0;
+    t_out = t1;
+    return t1 > t0 + 0.0001f;
+}
+
+// Free-flight sampling in a homogeneous medium (medium.h:295-323): xi is the
+// ray's uniform number for this medium.
+MYPBR_DEV bool hit_medium(const DeviceScene& S, int i, float3 o, float3 d, float tmin, float tmax, float xi, float& t) {
+    float a, b, density;
+    int mat;
+    if (!medium_span(S, i, o, d, a, b, density, mat))
+        return false;
+    float t0 = fmaxf(a, tmin), t1 = fminf(b, tmax);
+    if (t0 >= t1)
+        return false;
+    float len = length(d);
+    float dist = -logf(1.0f - xi) / density;
+    if (dist > (t1 - t0) * len)
+        return false;
+    t = t0 + dist / len;
+    return true;
+}
+
+// ------------------------------------------------------------- traversal
+
+struct HitInfo {
+    float t, b1, b2;
+    uint32_t prim;  // kind << 29 | index; 0xffffffff: miss
+};
+constexpr uint32_t kMiss = 0xffffffffu;
+
+MYPBR_DEV float safe_inv(float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysignf(1e30f, x); }
+
+// The closest hit along o + t d, t in (tmin, tmax): the BVH, then the
+// unbounded objects beside it (main.cpp:70-74 of the reference). media_key
+// seeds free-flight sampling in media; media_key == 0 skips media (used by the
+// deterministic ray-batch query).
+MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
+    HitInfo h;
+    h.prim = kMiss;
+    h.t = tmax;
+    h.b1 = h.b2 = 0.0f;
+    if (S.has_bvh) {
+        float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+        float3 oi = -1.0f * (o * inv);
+        TriRay tr = make_tri_ray(d);
+        int stack[kBvhStack];
+        int sp = 0;
+        int node = 0;
+        while (true) {
+            const float4* n = S.bvh + 4 * node;
+            float4 a0 = ldg4(n), a1 = ldg4(n + 1), c0 = ldg4(n + 2), c1 = ldg4(n + 3);
+            // slab tests of both children against (tmin, best)
+            float lx0 = fmaf(a0.x, inv.x, oi.x), hx0 = fmaf(a1.x, inv.x, oi.x);
+            float ly0 = fmaf(a0.y, inv.y, oi.y), hy0 = fmaf(a1.y, inv.y, oi.y);
+            float lz0 = fmaf(a0.z, inv.z, oi.z), hz0 = fmaf(a1.z, inv.z, oi.z);
+            float n0 = fmaxf(fmaxf(fminf(lx0, hx0), fminf(ly0, hy0)), fmaxf(fminf(lz0, hz0), tmin));
+            float f0 = fminf(fminf(fmaxf(lx0, hx0), fmaxf(ly0, hy0)), fminf(fmaxf(lz0, hz0), h.t));
+            float lx1 = fmaf(c0.x, inv.x, oi.x), hx1 = fmaf(c1.x, inv.x, oi.x);
+            float ly1 = fmaf(c0.y, inv.y, oi.y), hy1 = fmaf(c1.y, inv.y, oi.y);
+            float lz1 = fmaf(c0.z, inv.z, oi.z), hz1 = fmaf(c1.z, inv.z, oi.z);
+            float n1 = fmaxf(fmaxf(fminf(lx1, hx1), fminf(ly1, hy1)), fmaxf(fminf(lz1, hz1), tmin));
+            float f1 = fminf(fminf(fmaxf(lx1, hx1), fmaxf(ly1, hy1)), fminf(fmaxf(lz1, hz1), h.t));
+            // A small relative widening keeps FP32 slab tests conservative
+            bool h0 = n0 <= f0 * 1.00000024f + 1e-30f;
+            bool h1 = n1 <= f1 * 1.00000024f + 1e-30f;
+            int i0 = __float_as_int(a0.w), k0 = __float_as_int(a1.w);
+            int i1 = __float_as_int(c0.w), k1 = __float_as_int(c1.w);
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                bool hit = side == 0 ? h0 : h1;
+                int cnt = side == 0 ? k0 : k1;
+                int first = side == 0 ? i0 : i1;
+                if (!(hit && cnt > 0))
+                    continue;
+                for (int k = 0; k < cnt; k++) {
+                    uint32_t ref = __ldg(S.leaf_refs + first + k);
+                    int kind = int(ref >> kKindShift), idx = int(ref & kIndexMask);
+                    float t, b1 = 0.0f, b2 = 0.0f;
+                    bool got = false;
+                    if (kind == kTriangle) {
+                        got = hit_triangle(S, idx, o, tr, tmin, h.t, t, b1, b2);
+                    } else if (kind == kSphere) {
+                        got = hit_sphere(S, idx, o, d, tmin, h.t, t);
+                    } else if (kind == kQuad) {
+                        got = hit_quad(S, idx, o, d, tmin, h.t, t, b1, b2);
+                    } else if (kind == kMedium && media_key != 0) {
+                        got = hit_medium(S, idx, o, d, tmin, h.t, hash_uniform(media_key, uint32_t(idx)), t);
+                    }
+                    if (got) {
+                        h.t = t;
+                        h.b1 = b1;
+                        h.b2 = b2;
+                        h.prim = ref;
+                    }
+                }
+            }
+            h0 = h0 && k0 == 0;
+            h1 = h1 && k1 == 0;
+            if (h0 && h1) {
+                bool first0 = n0 <= n1;
+                stack[sp++] = first0 ? i1 : i0;
+                node = first0 ? i0 : i1;
+            } else if (h0) {
+                node = i0;
+            } else if (h1) {
+                node = i1;
+            } else {
+                if (sp == 0)
+                    break;
+                node = stack[--sp];
+            }
+        }
+    }
+    // The ground (plane.h:17-34) and height fog (medium.h:352-381) beside the BVH
+    for (int k = 0; k < S.unbounded_count; k++) {
+        DevUnbounded ub = S.unbounded[k];
+        if (ub.kind == 0) {
+            if (fabsf(d.y) < 1e-12f)
+                continue;
+            float t = (ub.height - o.y) / d.y;
+            if (t > tmin && t < h.t) {
+                h.t = t;
+                h.prim = (uint32_t(kGround) << kKindShift) | uint32_t(k);
+            }
+        } else if (media_key != 0) {
+            float len = length(d);
+            float kk = d.y / ub.scale_height;
+            float start = ub.density * len * expf(-(o.y + tmin * d.y - ub.height) / ub.scale_height);
+            if (!(start > 0.0f))
+                continue;
+            float tau = -logf(1.0f - hash_uniform(media_key, 0x40000000u + uint32_t(k)));
+            float t;
+            if (fabsf(kk) < 1e-12f) {
+                t = tmin + tau / start;
+            } else {
+                float x = 1.0f - tau * kk / start;
+                if (x <= 0.0f)
+                    continue;
+                t = tmin - logf(x) / kk;
+            }
+            if (t < h.t && isfinite(t)) {
+                h.t = t;
+                h.prim = (uint32_t(kHeightFog) << kKindShift) | uint32_t(k);
+            }
+        }
+    }
+    return h;
+}
+
+// ------------------------------------------------------- surface records
+
+struct Surface {
+    float3 p, normal, dpdu, dpdv;
+    float u, v;
+    int material;
+    bool front;
+};
+
+MYPBR_DEV void set_face(Surface& s, float3 d, float3 outward) {
+    s.front = dot(d, outward) < 0.0f;
+    s.normal = s.front ? outward : -outward;
+}
+
+// sphere.h:536-560: (u, v) and tangents of a point p on the unit sphere, radius r
+MYPBR_DEV void sphere_uv_tangents(float3 p, float r, Surface& s) {
+    float theta = acosf(clampf(-p.y, -1.0f, 1.0f));
+    float phi = atan2f(-p.z, p.x) + kPi;
+    s.u = phi * (0.5f * kInvPi);
+    s.v = theta * kInvPi;
+    float st = sqrtf(p.x * p.x + p.z * p.z);
+    if (st < 1e-8f) {
+        s.dpdu = s.dpdv = f3(0.0f);
+        return;
+    }
+    s.dpdu = (2.0f * kPi * r) * f3(p.z, 0.0f, -p.x);
+    s.dpdv = (kPi * r / st) * f3(-p.x * p.y, st * st, -p.y * p.z);
+}
+
+// Rebuilds the hit record (hittable.h:12-32) of a hit found by closest_hit.
+MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o, float3 d) {
+    Surface s;
+    int kind = int(h.prim >> kKindShift), idx = int(h.prim & kIndexMask);
+    s.p = o + h.t * d;
+    s.u = s.v = 0.0f;
+    s.dpdu = s.dpdv = f3(0.0f);
+    s.front = true;
+    s.normal = f3(1, 0, 0);
+    s.material = 0;
+    if (kind == kSphere) {
+        float4 sp = ldg4(S.spheres + idx);
+        int2 info = S.sphere_info[idx];
+        s.material = info.x;
+        float3 c = f3(sp);
+        float r = sp.w;
+        if (info.y < 0) {
+            float3 outward = (s.p - c) / r;
+            outward = outward * rsqrtf(dot(outward, outward));
+            s.p = c + fabsf(r) * (r < 0.0f ? -outward : outward);  // back onto the surface
+            set_face(s, d, outward);
+            sphere_uv_tangents(r < 0.0f ? -outward : outward, fabsf(r), s);
+        } else {
+            XformRef X;
+            load_xform(S, info.y, X);
+            float3 lo = xf_ipoint(X, o), ld = xf_ivec(X, d);
+            float3 lp = lo + h.t * ld;
+            float3 outward = (lp - c) / r;
+            Surface ls;
+            set_face(ls, ld, outward);
+            float3 un = r < 0.0f ? -outward : outward;
+            sphere_uv_tangents(un * rsqrtf(dot(un, un)), fabsf(r), ls);
+            s.u = ls.u;
+            s.v = ls.v;
+            s.front = ls.front;
+            s.p = xf_point(X, lp);
+            s.normal = normalize(xf_normal(X, ls.normal));
+            s.dpdu = xf_vec(X, ls.dpdu);
+            s.dpdv = xf_vec(X, ls.dpdv);
+        }
+    } else if (kind == kQuad) {
+        const float4* q = S.quads + 5 * idx;
+        float4 Q = ldg4(q);
+        s.material = __float_as_int(Q.w);
+        s.u = h.b1;
+        s.v = h.b2;
+        s.dpdu = f3(ldg4(q + 1));
+        s.dpdv = f3(ldg4(q + 2));
+        s.p = f3(Q) + h.b1 * s.dpdu + h.b2 * s.dpdv;
+        set_face(s, d, f3(ldg4(q + 3)));
+    } else if (kind == kTriangle) {
+        const float4* tp = S.tris + 3 * idx;
+        float4 P0 = ldg4(tp), P1 = ldg4(tp + 1), P2 = ldg4(tp + 2);
+        s.material = __float_as_int(P0.w);
+        int flags = __float_as_int(P1.w);
+        float b1 = h.b1, b2 = h.b2, b0 = 1.0f - b1 - b2;
+        float3 v0 = f3(P0), e1 = f3(P1) - v0, e2 = f3(P2) - v0;
+        s.p = v0 + b1 * e1 + b2 * e2;
+        int4 sa = S.tri_shading[2 * idx], sb = S.tri_shading[2 * idx + 1];
+        s.u = b1;
+        s.v = b2;
+        bool has_uv = sa.w >= 0;
+        s.dpdu = e1;
+        s.dpdv = e2;
+        if (has_uv) {
+            float2 t0 = S.uvs[sa.w], t1 = S.uvs[sb.x], t2 = S.uvs[sb.y];
+            s.u = b0 * t0.x + b1 * t1.x + b2 * t2.x;
+            s.v = b0 * t0.y + b1 * t1.y + b2 * t2.y;
+            float du1 = t1.x - t0.x, dv1 = t1.y - t0.y, du2 = t2.x - t0.x, dv2 = t2.y - t0.y;
+            float det = du1 * dv2 - du2 * dv1;
+            if (fabsf(det) < 1e-12f) {
+                s.dpdu = s.dpdv = f3(0.0f);
+            } else {
+                float iv = 1.0f / det;
+                s.dpdu = (dv2 * e1 - dv1 * e2) * iv;
+                s.dpdv = (du1 * e2 - du2 * e1) * iv;
+            }
+        }
+        float3 g = normalize(cross(e1, e2));
+        if (flags & 1)
+            g = -g;
+        set_face(s, d, g);
+        if (sa.x >= 0) {
+            float3 sh = b0 * S.normals[sa.x] + b1 * S.normals[sa.y] + b2 * S.normals[sa.z];
+            if (dot(sh, sh) > 0.0f) {
+                sh = normalize(sh);
+                s.normal = dot(sh, s.normal) < 0.0f ? -sh : sh;
+            }
+        }
+    } else if (kind == kMedium) {
+        s.material = __float_as_int(ldg4(S.media + 3 * idx + 2).y);
+    } else if (kind == kGround) {
+        DevUnbounded ub = S.unbounded[idx];
+        s.material = ub.material;
+        s.p.y = ub.height;
+        s.u = s.p.x;
+        s.v = -s.p.z;
+        s.dpdu = f3(1, 0, 0);
+        s.dpdv = f3(0, 0, -1);
+        set_face(s, d, f3(0, 1, 0));
+    } else if (kind == kHeightFog) {
+        s.material = S.unbounded[idx].material;
+    }
+    return s;
+}
+
+}  // namespace mypbr_dev

@@ -1,0 +1,66 @@
+// The device scene handle behind mypbr_gpu_scene and the helpers the
+// translation units share.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../../include/mypbr_gpu.h"
+#include "dev_scene.cuh"
+
+namespace mypbr_dev {
+
+// Scratch memory of one render: path state in slots, queues of slot indices,
+// the FP64 film. Kept on the scene handle and grown on demand.
+struct RenderBuffers {
+    size_t capacity = 0;   // path slots
+    size_t pixels = 0;     // film pixels
+    int depth_slots = 0;   // per-bounce queue counters
+    // path state (slot-indexed)
+    float4* ray_o = nullptr;     // origin, tmin
+    float4* ray_d = nullptr;     // direction, scatter pdf of the direction
+    float4* beta = nullptr;      // throughput, unused
+    float4* radiance = nullptr;  // path radiance so far, unused
+    uint2* rng = nullptr;        // PCG state
+    uint4* meta = nullptr;       // pixel, sample, flags (depth | specular | seen | counts), -
+    float4* hit = nullptr;       // t, b1, b2, prim bits
+    float4* sh_o = nullptr;      // shadow ray: origin, -
+    float4* sh_d = nullptr;      // direction, final flag
+    float4* sh_c = nullptr;      // contribution rgb, -
+    uint32_t* queue[2] = {nullptr, nullptr};  // extension queues (ping-pong)
+    uint32_t* shadow_queue = nullptr;
+    uint32_t* counters = nullptr;             // [2 * depth_slots + 8]
+    // film (pixel-indexed, FP64 sums)
+    double* film = nullptr;   // radiance sum rgb
+    double* film2 = nullptr;  // radiance squared sum rgb
+    double* feat = nullptr;   // albedo rgb, normal rgb, luminance^2 (7 per pixel)
+    int* error = nullptr;     // sticky device error word
+};
+
+}  // namespace mypbr_dev
+
+struct mypbr_gpu_scene {
+    mypbr_dev::DeviceScene dev{};
+    std::vector<void*> allocations;
+    int device = 0;
+    int sm_count = 0;
+    int max_depth_bvh = 0;
+    size_t leaf_ref_count = 0;
+    int64_t material_count = 0;
+    mypbr_dev::RenderBuffers rb;
+};
+
+namespace mypbr_dev {
+
+void set_error_message(const std::string& m);
+int cuda_fail(cudaError_t e, const char* what);
+int release_buffers(RenderBuffers& rb);
+
+}  // namespace mypbr_dev
+
+#define MYPBR_CUDA(call)                                       \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess)                                 \
+            return ::mypbr_dev::cuda_fail(e_, #call);          \
+    } while (0)

@@ -1,0 +1,135 @@
+// Pointwise queries for parity checks: ray batches through the BVH walk, and
+// BSDF eval / pdf at given surface records. Both run the same device
+// functions the renderer runs.
+#include <algorithm>
+#include <string>
+
+#include "dev_shading.cuh"
+#include "gpu_scene.h"
+
+namespace mypbr_dev {
+
+__global__ void k_trace(DeviceScene S, const float* rays, long long n, float* hits, int* prim) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const float* r = rays + 8 * k;
+        float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
+        HitInfo h = closest_hit(S, o, d, r[6], r[7], 0);
+        float* out = hits + 8 * k;
+        if (h.prim == kMiss) {
+            for (int c = 0; c < 8; c++)
+                out[c] = 0.0f;
+            prim[2 * k] = -1;
+            prim[2 * k + 1] = -1;
+            continue;
+        }
+        Surface s = make_surface(S, h, o, d);
+        out[0] = h.t;
+        out[1] = s.normal.x;
+        out[2] = s.normal.y;
+        out[3] = s.normal.z;
+        out[4] = s.u;
+        out[5] = s.v;
+        out[6] = s.front ? 1.0f : 0.0f;
+        out[7] = float(s.material);
+        prim[2 * k] = int(h.prim >> kKindShift);
+        prim[2 * k + 1] = int(h.prim & kIndexMask);
+    }
+}
+
+__global__ void k_bsdf(DeviceScene S, int material, const float* rec, const float* r_in, const float* wi, long long n,
+                       float* out) {
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const float* r = rec + 16 * k;
+        Surface s;
+        s.p = f3(r[0], r[1], r[2]);
+        s.normal = f3(r[3], r[4], r[5]);
+        s.front = r[6] != 0.0f;
+        s.u = r[7];
+        s.v = r[8];
+        s.dpdu = f3(r[9], r[10], r[11]);
+        s.dpdv = f3(r[12], r[13], r[14]);
+        s.material = material;
+        float3 d = f3(r_in[3 * k], r_in[3 * k + 1], r_in[3 * k + 2]);
+        float3 w = f3(wi[3 * k], wi[3 * k + 1], wi[3 * k + 2]);
+        float3 e = eval(S, material, d, s, w);
+        Rng g = make_rng(1, uint64_t(k), 0);
+        ScatterRec sr;
+        bool sc = scatter(S, material, d, s, sr, g);
+        out[4 * k] = e.x;
+        out[4 * k + 1] = e.y;
+        out[4 * k + 2] = e.z;
+        out[4 * k + 3] = (sc && !sr.skip_pdf) ? sr.pdf.value(w) : 0.0f;
+    }
+}
+
+namespace {
+struct Buf {
+    void* p = nullptr;
+    ~Buf() {
+        if (p)
+            cudaFree(p);
+    }
+};
+int bad_arg(const std::string& m) {
+    set_error_message(m);
+    return MYPBR_ERR_INVALID_ARGUMENT;
+}
+}  // namespace
+
+}  // namespace mypbr_dev
+
+using namespace mypbr_dev;
+
+extern "C" int mypbr_gpu_trace(mypbr_gpu_scene* G, const float* rays, int64_t n, float* hits, int32_t* prim,
+                               int on_device) {
+    if (!G || (n > 0 && (!rays || !hits || !prim)) || n < 0)
+        return bad_arg("mypbr_gpu_trace: bad argument");
+    if (n == 0)
+        return MYPBR_OK;
+    MYPBR_CUDA(cudaSetDevice(G->device));
+    int blocks = int(std::min<int64_t>((n + 127) / 128, int64_t(G->sm_count) * 16));
+    if (on_device) {
+        k_trace<<<blocks, 128>>>(G->dev, rays, (long long)n, hits, prim);
+        MYPBR_CUDA(cudaGetLastError());
+        MYPBR_CUDA(cudaDeviceSynchronize());
+        return MYPBR_OK;
+    }
+    Buf dr, dh, dp;
+    MYPBR_CUDA(cudaMalloc(&dr.p, size_t(n) * 8 * sizeof(float)));
+    MYPBR_CUDA(cudaMalloc(&dh.p, size_t(n) * 8 * sizeof(float)));
+    MYPBR_CUDA(cudaMalloc(&dp.p, size_t(n) * 2 * sizeof(int)));
+    MYPBR_CUDA(cudaMemcpy(dr.p, rays, size_t(n) * 8 * sizeof(float), cudaMemcpyHostToDevice));
+    k_trace<<<blocks, 128>>>(G->dev, static_cast<float*>(dr.p), (long long)n, static_cast<float*>(dh.p),
+                             static_cast<int*>(dp.p));
+    MYPBR_CUDA(cudaGetLastError());
+    MYPBR_CUDA(cudaMemcpy(hits, dh.p, size_t(n) * 8 * sizeof(float), cudaMemcpyDeviceToHost));
+    MYPBR_CUDA(cudaMemcpy(prim, dp.p, size_t(n) * 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    return MYPBR_OK;
+}
+
+extern "C" int mypbr_gpu_bsdf_eval(mypbr_gpu_scene* G, int32_t material, const float* rec, const float* r_in,
+                                   const float* wi, int64_t n, float* out) {
+    if (!G || n < 0 || (n > 0 && (!rec || !r_in || !wi || !out)))
+        return bad_arg("mypbr_gpu_bsdf_eval: bad argument");
+    if (material < 0 || material >= G->material_count)
+        return bad_arg("mypbr_gpu_bsdf_eval: material index out of range");
+    if (n == 0)
+        return MYPBR_OK;
+    MYPBR_CUDA(cudaSetDevice(G->device));
+    Buf a, b, c, d;
+    MYPBR_CUDA(cudaMalloc(&a.p, size_t(n) * 16 * sizeof(float)));
+    MYPBR_CUDA(cudaMalloc(&b.p, size_t(n) * 3 * sizeof(float)));
+    MYPBR_CUDA(cudaMalloc(&c.p, size_t(n) * 3 * sizeof(float)));
+    MYPBR_CUDA(cudaMalloc(&d.p, size_t(n) * 4 * sizeof(float)));
+    MYPBR_CUDA(cudaMemcpy(a.p, rec, size_t(n) * 16 * sizeof(float), cudaMemcpyHostToDevice));
+    MYPBR_CUDA(cudaMemcpy(b.p, r_in, size_t(n) * 3 * sizeof(float), cudaMemcpyHostToDevice));
+    MYPBR_CUDA(cudaMemcpy(c.p, wi, size_t(n) * 3 * sizeof(float), cudaMemcpyHostToDevice));
+    int blocks = int(std::min<int64_t>((n + 127) / 128, 4096));
+    k_bsdf<<<blocks, 128>>>(G->dev, material, static_cast<float*>(a.p), static_cast<float*>(b.p),
+                            static_cast<float*>(c.p), (long long)n, static_cast<float*>(d.p));
+    MYPBR_CUDA(cudaGetLastError());
+    MYPBR_CUDA(cudaMemcpy(out, d.p, size_t(n) * 4 * sizeof(float), cudaMemcpyDeviceToHost));
+    return MYPBR_OK;
+}

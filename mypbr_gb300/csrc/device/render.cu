@@ -1,0 +1,785 @@
+// The wavefront path tracer: camera::render / ray_color of the reference
+// (include/camera.h:79-461) as kernels over queues in HBM.
+//
+// A wave holds every pixel times `npass` passes, one path per slot. Each
+// bounce runs three kernels:
+//   extend  closest hit of every ray in the extension queue (BVH walk);
+//   shade   per path: sky or emission with MIS, Beer-Lambert, scatter();
+//           for non-specular vertices next-event estimation writes a shadow
+//           ray into the shadow queue; the BSDF sample, Russian roulette, and
+//           the surviving path goes to the next extension queue;
+//   shadow  closest hit of every shadow ray; adds f L w / pdf to its path and,
+//           for a path that ended at this bounce, writes it to the film.
+// Queues hold slot indices and are appended with warp-aggregated atomics; the
+// per-bounce counters live in device memory, so the host never waits on them.
+// Kernels are persistent-style (grid = SMs x resident blocks, grid-stride over
+// the queue length they read on the device).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../host/host_math.h"
+#include "dev_shading.cuh"
+#include "gpu_scene.h"
+
+namespace mypbr_dev {
+
+constexpr uint32_t kFlagSpecular = 1u << 8;
+constexpr uint32_t kFlagSeen = 1u << 9;
+
+struct CameraParams {
+    float3 center, p00, du, dv, wv, disk_u, disk_v;
+    int width, height, sqrt_spp, blades;
+    float recip_sqrt_spp, focus_dist, ortho_height, defocus_angle, blade_rotation;
+};
+
+struct WaveParams {
+    DeviceScene S;
+    CameraParams cam;
+    RenderBuffers B;
+    int max_depth, max_diffuse, max_specular, max_scatter;
+    int transparent_shadows, collect_features, has_lights, pad;
+    unsigned long long seed;
+    int pass0, npass;
+    unsigned long long* totals;  // extension rays, shadow rays
+};
+
+// Counter slots: extension queue length entering bounce d, shadow queue length of bounce d.
+MYPBR_DEV uint32_t* ext_counter(const WaveParams& P, int d) { return P.B.counters + d; }
+MYPBR_DEV uint32_t* sh_counter(const WaveParams& P, int d) { return P.B.counters + P.B.depth_slots + d; }
+
+// One atomic per warp: the active lanes that push get consecutive slots.
+MYPBR_DEV uint32_t warp_push(uint32_t* counter) {
+    unsigned mask = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader)
+        base = atomicAdd(counter, uint32_t(__popc(mask)));
+    base = __shfl_sync(mask, base, leader);
+    return base + uint32_t(__popc(mask & ((1u << lane) - 1u)));
+}
+
+MYPBR_DEV void film_add(const WaveParams& P, uint32_t pixel, float3 c) {
+    // NaN or infinite estimates count as black (camera.h:281-287)
+    if (!isfinite(c.x) || !isfinite(c.y) || !isfinite(c.z))
+        c = f3(0.0f);
+    double* f = P.B.film + 3 * size_t(pixel);
+    double* f2 = P.B.film2 + 3 * size_t(pixel);
+    atomicAdd(f, double(c.x));
+    atomicAdd(f + 1, double(c.y));
+    atomicAdd(f + 2, double(c.z));
+    atomicAdd(f2, double(c.x) * c.x);
+    atomicAdd(f2 + 1, double(c.y) * c.y);
+    atomicAdd(f2 + 2, double(c.z) * c.z);
+    if (P.collect_features) {
+        double l = luminance(c);
+        atomicAdd(P.B.feat + 7 * size_t(pixel) + 6, l * l);
+    }
+}
+
+MYPBR_DEV uint64_t media_key(const WaveParams& P, uint32_t pixel, uint32_t pass, uint32_t depth, uint32_t kind) {
+    return mix64(P.seed ^ mix64((uint64_t(pixel) << 24) ^ (uint64_t(pass) << 8) ^ (uint64_t(depth) << 2) ^ kind)) | 1ull;
+}
+
+// camera.h:291-339: a ray through pixel (i, j) for pass `pass`, stratified over
+// the first sqrt_spp^2 passes with the per-pixel cell offset of camera.h:205.
+MYPBR_DEV void camera_ray(const CameraParams& C, int i, int j, int pass, Rng& g, float3& o, float3& d) {
+    int strata = C.sqrt_spp * C.sqrt_spp;
+    float ox, oy;
+    if (pass >= strata) {
+        ox = g.next() - 0.5f;
+        oy = g.next() - 0.5f;
+    } else {
+        long long cell = (long long)pass + (long long)i * 7919 + (long long)j * 104729;
+        int c = int(cell % strata);
+        float rx = g.next(), ry = g.next();
+        ox = ((c % C.sqrt_spp) + rx) * C.recip_sqrt_spp - 0.5f;
+        oy = ((c / C.sqrt_spp) + ry) * C.recip_sqrt_spp - 0.5f;
+    }
+    float3 ps = C.p00 + (float(i) + ox) * C.du + (float(j) + oy) * C.dv;
+    float3 eye = C.ortho_height > 0.0f ? ps + C.focus_dist * C.wv : C.center;
+    if (C.defocus_angle <= 0.0f) {
+        o = eye;
+    } else {
+        float px, py;
+        if (C.blades >= 3) {  // camera.h:329-339
+            int k = min(int(g.next() * C.blades), C.blades - 1);
+            float a0 = C.blade_rotation + 2.0f * kPi * k / C.blades;
+            float a1 = a0 + 2.0f * kPi / C.blades;
+            float s = g.next(), t = g.next();
+            if (s + t > 1.0f) {
+                s = 1.0f - s;
+                t = 1.0f - t;
+            }
+            px = s * cosf(a0) + t * cosf(a1);
+            py = s * sinf(a0) + t * sinf(a1);
+        } else {  // vec3.h:309-315
+            do {
+                px = 2.0f * g.next() - 1.0f;
+                py = 2.0f * g.next() - 1.0f;
+            } while (px * px + py * py >= 1.0f);
+        }
+        o = eye + px * C.disk_u + py * C.disk_v;
+    }
+    d = ps - o;
+}
+
+__global__ void k_generate(WaveParams P) {
+    size_t npix = size_t(P.cam.width) * P.cam.height;
+    size_t n = npix * size_t(P.npass);
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
+        uint32_t pixel = uint32_t(t % npix);
+        uint32_t pass = uint32_t(P.pass0 + int(t / npix));
+        int i = int(pixel % uint32_t(P.cam.width)), j = int(pixel / uint32_t(P.cam.width));
+        Rng g = make_rng(P.seed, pixel, pass);
+        float3 o, d;
+        camera_ray(P.cam, i, j, int(pass), g, o, d);
+        P.B.ray_o[t] = make_float4(o.x, o.y, o.z, 0.001f);
+        P.B.ray_d[t] = make_float4(d.x, d.y, d.z, 0.0f);
+        P.B.beta[t] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        P.B.radiance[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        P.B.rng[t] = make_uint2(uint32_t(g.state), uint32_t(g.state >> 32));
+        P.B.meta[t] = make_uint4(pixel, pass, kFlagSpecular, 0u);
+        P.B.queue[0][t] = uint32_t(t);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        *ext_counter(P, 0) = uint32_t(n);
+}
+
+MYPBR_DEV Rng load_rng(const WaveParams& P, uint32_t slot) {
+    uint2 s = P.B.rng[slot];
+    Rng g;
+    g.state = (uint64_t(s.y) << 32) | s.x;
+    return g;
+}
+
+// camera.h:253-277: albedo and normal of the first non-specular surface
+__global__ void k_features(WaveParams P) {
+    size_t n = size_t(P.cam.width) * P.cam.height * size_t(P.npass);
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
+        float4 ro = P.B.ray_o[t], rd = P.B.ray_d[t];
+        uint4 meta = P.B.meta[t];
+        float3 o = f3(ro), d = f3(rd);
+        Rng g = make_rng(P.seed ^ 0x5bd1e995ull, meta.x, meta.y);
+        float3 tint = f3(1.0f), albedo = f3(1.0f), normal = f3(0.0f);
+        bool done = false;
+        for (int b = 0; b < 8 && !done; b++) {
+            HitInfo h = closest_hit(P.S, o, d, 0.001f, 3.0e38f, media_key(P, meta.x, meta.y, 100 + b, 3));
+            if (h.prim == kMiss)
+                break;
+            Surface s = make_surface(P.S, h, o, d);
+            tint *= interior_transmittance(P.S, s.material, h.t * length(d), s.front);
+            ScatterRec sr;
+            if (!scatter(P.S, s.material, d, s, sr, g)) {
+                albedo = tint;
+                normal = s.normal;
+                done = true;
+            } else if (!sr.skip_pdf) {
+                albedo = tint * sr.attenuation;
+                normal = s.normal;
+                done = true;
+            } else {
+                tint *= sr.attenuation;
+                o = s.p;
+                d = sr.skip_dir;
+            }
+        }
+        if (!done) {
+            albedo = tint;
+            normal = f3(0.0f);
+        }
+        double* f = P.B.feat + 7 * size_t(meta.x);
+        atomicAdd(f, double(albedo.x));
+        atomicAdd(f + 1, double(albedo.y));
+        atomicAdd(f + 2, double(albedo.z));
+        atomicAdd(f + 3, double(normal.x));
+        atomicAdd(f + 4, double(normal.y));
+        atomicAdd(f + 5, double(normal.z));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_extend(WaveParams P, int depth) {
+    uint32_t n = *ext_counter(P, depth);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
+        atomicAdd(&P.totals[0], (unsigned long long)n);
+    const uint32_t* q = P.B.queue[depth & 1];
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        uint32_t slot = q[k];
+        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
+        uint4 meta = P.B.meta[slot];
+        HitInfo h = closest_hit(P.S, f3(ro), f3(rd), ro.w, 3.0e38f, media_key(P, meta.x, meta.y, uint32_t(depth), 0));
+        P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
+    uint32_t n = *ext_counter(P, depth);
+    const uint32_t* q = P.B.queue[depth & 1];
+    uint32_t* q_next = P.B.queue[(depth + 1) & 1];
+    const DeviceScene& S = P.S;
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        uint32_t slot = q[k];
+        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot], hb = P.B.hit[slot];
+        float4 bt = P.B.beta[slot], rad4 = P.B.radiance[slot];
+        uint4 meta = P.B.meta[slot];
+        Rng g = load_rng(P, slot);
+        float3 o = f3(ro), d = f3(rd), beta = f3(bt), rad = f3(rad4);
+        float scatter_pdf = rd.w;
+        bool specular = meta.z & kFlagSpecular, seen = meta.z & kFlagSeen;
+        uint32_t diffuse_count = (meta.z >> 16) & 0xff, specular_count = (meta.z >> 24) & 0xff;
+        uint32_t scatter_count = meta.w;
+        bool terminate = false, pushed_shadow = false;
+        float3 new_o = o, new_d = d;
+        HitInfo h;
+        h.t = hb.x;
+        h.b1 = hb.y;
+        h.b2 = hb.z;
+        h.prim = __float_as_uint(hb.w);
+        if (h.prim == kMiss) {
+            // camera.h:373-387: the sky is a light, weighted like emission
+            float3 sky = escaped_radiance(S, d, depth == 0);
+            if (!seen) {
+                if (specular || !P.has_lights)
+                    rad += beta * sky;
+                else
+                    rad += beta * sky * power_heuristic(scatter_pdf, lights_pdf(S, o, d));
+            }
+            terminate = true;
+        } else {
+            Surface s = make_surface(S, h, o, d);
+            int mat = s.material;
+            beta *= interior_transmittance(S, mat, h.t * length(d), s.front);  // camera.h:396
+            if (!seen && may_emit(S, mat)) {                                   // camera.h:399-407
+                float3 em = emitted(S, mat, d, s);
+                if (nonzero(em)) {
+                    if (specular || !P.has_lights)
+                        rad += beta * em;
+                    else
+                        rad += beta * em * power_heuristic(scatter_pdf, lights_pdf(S, o, d));
+                }
+            }
+            ScatterRec sr;
+            if (!scatter(S, mat, d, s, sr, g)) {
+                terminate = true;
+            } else if (sr.skip_pdf) {  // camera.h:413-423
+                if (P.max_specular > 0 && ++specular_count > uint32_t(P.max_specular)) {
+                    terminate = true;
+                } else {
+                    beta *= sr.attenuation;
+                    new_o = s.p;
+                    new_d = sr.skip_dir;
+                    if (P.transparent_shadows && lets_shadows_through(S, mat) && P.has_lights && depth > 0 && !specular)
+                        seen = true;
+                    specular = true;
+                }
+            } else {  // camera.h:424-448
+                bool vol = is_volume(S, mat);
+                uint32_t& cnt = vol ? scatter_count : diffuse_count;
+                int cap = vol ? P.max_scatter : P.max_diffuse;
+                bool capped = cap > 0 && ++cnt >= uint32_t(cap);
+                bool last = depth == P.max_depth - 1 || capped;
+                seen = false;
+                if (P.has_lights) {  // camera.h:466-506, the shadow ray traced by k_shadow
+                    float3 to_light = lights_sample(S, s.p, g);
+                    float lp = lights_pdf(S, s.p, to_light);
+                    if (lp > 0.0f) {
+                        float3 f = eval(S, mat, d, s, to_light);
+                        if (f.x > 0.0f || f.y > 0.0f || f.z > 0.0f) {
+                            float w = last ? 1.0f : power_heuristic(lp, sr.pdf.value(to_light));
+                            float3 c = beta * f * (w / lp);
+                            float3 sd = normalize(to_light);
+                            P.B.sh_o[slot] = make_float4(s.p.x, s.p.y, s.p.z, 0.001f);
+                            P.B.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+                            P.B.sh_c[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+                            P.B.shadow_queue[warp_push(sh_counter(P, depth))] = slot;
+                            pushed_shadow = true;
+                        }
+                    }
+                }
+                if (capped) {
+                    terminate = true;
+                } else {
+                    float3 dir = sr.pdf.generate(g);
+                    float spdf = sr.pdf.value(dir);
+                    if (!(spdf > 0.0f)) {
+                        terminate = true;
+                    } else {
+                        beta *= eval(S, mat, d, s, dir) / spdf;
+                        scatter_pdf = spdf;
+                        new_o = s.p;
+                        new_d = dir;
+                        specular = false;
+                    }
+                }
+            }
+            // Russian roulette (camera.h:452-457)
+            if (!terminate && depth >= 3) {
+                float survive = fminf(maxc(beta), 0.95f);
+                if (g.next() >= survive)
+                    terminate = true;
+                else
+                    beta = beta / survive;
+            }
+            if (!terminate && depth + 1 >= P.max_depth)
+                terminate = true;
+        }
+        if (terminate) {
+            if (pushed_shadow) {
+                P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+                P.B.sh_d[slot].w = 1.0f;  // the shadow kernel finishes this path
+            } else {
+                film_add(P, meta.x, rad);
+            }
+            continue;
+        }
+        P.B.ray_o[slot] = make_float4(new_o.x, new_o.y, new_o.z, 0.001f);
+        P.B.ray_d[slot] = make_float4(new_d.x, new_d.y, new_d.z, scatter_pdf);
+        P.B.beta[slot] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+        P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        P.B.rng[slot] = make_uint2(uint32_t(g.state), uint32_t(g.state >> 32));
+        uint32_t flags = (specular ? kFlagSpecular : 0u) | (seen ? kFlagSeen : 0u) | (diffuse_count << 16) |
+                         (specular_count << 24);
+        P.B.meta[slot] = make_uint4(meta.x, meta.y, flags, scatter_count);
+        q_next[warp_push(ext_counter(P, depth + 1))] = slot;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
+    uint32_t n = *sh_counter(P, depth);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
+        atomicAdd(&P.totals[1], (unsigned long long)n);
+    const DeviceScene& S = P.S;
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        uint32_t slot = P.B.shadow_queue[k];
+        float4 so = P.B.sh_o[slot], sd = P.B.sh_d[slot], sc = P.B.sh_c[slot];
+        uint4 meta = P.B.meta[slot];
+        float3 o = f3(so), d = f3(sd);
+        float3 through = f3(1.0f), emission = f3(0.0f);
+        for (int hop = 0; hop <= 16; hop++) {
+            HitInfo h = closest_hit(S, o, d, 0.001f, 3.0e38f, media_key(P, meta.x, meta.y, uint32_t(depth), 1 + 4 * hop));
+            if (h.prim == kMiss) {
+                emission = escaped_radiance(S, d, false);
+                break;
+            }
+            int kind = int(h.prim >> kKindShift);
+            int mat;
+            if (kind == kQuad)
+                mat = __float_as_int(ldg4(S.quads + 5 * (h.prim & kIndexMask)).w);
+            else if (kind == kTriangle)
+                mat = __float_as_int(ldg4(S.tris + 3 * (h.prim & kIndexMask)).w);
+            else if (kind == kSphere)
+                mat = S.sphere_info[h.prim & kIndexMask].x;
+            else
+                mat = -1;  // media, ground and fog neither emit nor let shadows through
+            bool through_glass = P.transparent_shadows && hop < 16 && mat >= 0 && lets_shadows_through(S, mat);
+            if (!through_glass && (mat < 0 || !may_emit(S, mat)))
+                break;  // blocked by something dark
+            Surface s = make_surface(S, h, o, d);
+            if (through_glass) {
+                through *= interior_transmittance(S, mat, h.t * length(d), s.front);
+                o = s.p;
+                continue;
+            }
+            emission = emitted(S, mat, d, s);
+            break;
+        }
+        float3 add = f3(sc) * through * emission;
+        float3 rad = f3(P.B.radiance[slot]) + add;
+        if (sd.w != 0.0f)
+            film_add(P, meta.x, rad);
+        else
+            P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+    }
+}
+
+// Averages (camera.h:223-246): radiance, albedo, normal over `samples`, and
+// the variance of the mean luminance.
+__global__ void k_resolve(WaveParams P, int samples, double* radiance, double* albedo, double* normal,
+                          double* variance) {
+    size_t npix = size_t(P.cam.width) * P.cam.height;
+    double scale = 1.0 / samples;
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < npix; p += stride) {
+        double r0 = scale * P.B.film[3 * p], r1 = scale * P.B.film[3 * p + 1], r2 = scale * P.B.film[3 * p + 2];
+        radiance[3 * p] = r0;
+        radiance[3 * p + 1] = r1;
+        radiance[3 * p + 2] = r2;
+        if (!P.collect_features)
+            continue;
+        const double* f = P.B.feat + 7 * p;
+        if (albedo) {
+            albedo[3 * p] = scale * f[0];
+            albedo[3 * p + 1] = scale * f[1];
+            albedo[3 * p + 2] = scale * f[2];
+        }
+        if (normal) {
+            normal[3 * p] = scale * f[3];
+            normal[3 * p + 1] = scale * f[4];
+            normal[3 * p + 2] = scale * f[5];
+        }
+        if (variance) {
+            double mean = 0.2126 * r0 + 0.7152 * r1 + 0.0722 * r2;
+            double spread = fmax(scale * f[6] - mean * mean, 0.0);
+            variance[p] = samples > 1 ? spread / (samples - 1) : spread;
+        }
+    }
+}
+
+// Per-channel variance of the mean radiance, from the second moments
+// (for the statistical parity checks).
+__global__ void k_channel_variance(WaveParams P, int samples, double* out) {
+    size_t n = size_t(P.cam.width) * P.cam.height * 3;
+    double scale = 1.0 / samples;
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        double m = scale * P.B.film[k];
+        double spread = fmax(scale * P.B.film2[k] - m * m, 0.0);
+        out[k] = samples > 1 ? spread / (samples - 1) : spread;
+    }
+}
+
+// ------------------------------------------------------------ host side
+
+int release_buffers(RenderBuffers& rb) {
+    void* ptrs[] = {rb.ray_o, rb.ray_d, rb.beta, rb.radiance, rb.rng, rb.meta, rb.hit, rb.sh_o, rb.sh_d, rb.sh_c,
+                    rb.queue[0], rb.queue[1], rb.shadow_queue, rb.counters, rb.film, rb.film2, rb.feat, rb.error};
+    for (void* p : ptrs)
+        if (p)
+            cudaFree(p);
+    rb = RenderBuffers();
+    return MYPBR_OK;
+}
+
+namespace {
+
+template <typename T>
+int alloc(T*& p, size_t count) {
+    MYPBR_CUDA(cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(count, 1) * sizeof(T)));
+    return MYPBR_OK;
+}
+
+int ensure_buffers(RenderBuffers& rb, size_t capacity, size_t pixels, int depth_slots) {
+    if (rb.capacity >= capacity && rb.pixels >= pixels && rb.depth_slots >= depth_slots)
+        return MYPBR_OK;
+    capacity = std::max(capacity, rb.capacity);
+    pixels = std::max(pixels, rb.pixels);
+    depth_slots = std::max(depth_slots, rb.depth_slots);
+    release_buffers(rb);
+    int s = MYPBR_OK;
+#define A(ptr, n) \
+    if (s == MYPBR_OK) s = alloc(ptr, n)
+    A(rb.ray_o, capacity);
+    A(rb.ray_d, capacity);
+    A(rb.beta, capacity);
+    A(rb.radiance, capacity);
+    A(rb.rng, capacity);
+    A(rb.meta, capacity);
+    A(rb.hit, capacity);
+    A(rb.sh_o, capacity);
+    A(rb.sh_d, capacity);
+    A(rb.sh_c, capacity);
+    A(rb.queue[0], capacity);
+    A(rb.queue[1], capacity);
+    A(rb.shadow_queue, capacity);
+    A(rb.counters, size_t(2 * depth_slots + 8));
+    A(rb.film, 3 * pixels);
+    A(rb.film2, 3 * pixels);
+    A(rb.feat, 7 * pixels);
+    A(rb.error, 1);
+#undef A
+    if (s != MYPBR_OK) {
+        release_buffers(rb);
+        return s;
+    }
+    rb.capacity = capacity;
+    rb.pixels = pixels;
+    rb.depth_slots = depth_slots;
+    return MYPBR_OK;
+}
+
+// camera.h:142-179 in FP64, handed to the device in FP32
+CameraParams make_camera(const mypbr_camera& c, int spp) {
+    using mypbr_host::V3;
+    CameraParams C{};
+    int w = c.image_width;
+    int h = c.image_height > 0 ? c.image_height : std::max(1, int(c.image_width / c.aspect_ratio));
+    C.width = w;
+    C.height = h;
+    C.sqrt_spp = std::max(1, int(std::sqrt(double(spp))));
+    C.recip_sqrt_spp = float(1.0 / C.sqrt_spp);
+    const double pi = 3.1415926535897932385;
+    V3 from(c.lookfrom[0], c.lookfrom[1], c.lookfrom[2]), at(c.lookat[0], c.lookat[1], c.lookat[2]),
+        vup(c.vup[0], c.vup[1], c.vup[2]);
+    double theta = c.vfov * pi / 180.0;
+    double hh = std::tan(theta / 2);
+    double vh = c.ortho_height > 0 ? c.ortho_height : 2 * hh * c.focus_dist;
+    double vw = vh * (double(w) / h);
+    V3 wv = mypbr_host::unit(from - at);
+    V3 u = mypbr_host::unit(mypbr_host::cross(vup, wv));
+    V3 v = mypbr_host::cross(wv, u);
+    V3 vu = vw * u, vv = vh * -v;
+    V3 du = vu / w, dv = vv / h;
+    V3 ul = from - (c.focus_dist * wv) - vu / 2 - vv / 2;
+    V3 p00 = ul + 0.5 * (du + dv);
+    double dr = c.focus_dist * std::tan(c.defocus_angle / 2 * pi / 180.0);
+    auto F = [](const V3& a) { return make_float3(float(a.x), float(a.y), float(a.z)); };
+    C.center = F(from);
+    C.p00 = F(p00);
+    C.du = F(du);
+    C.dv = F(dv);
+    C.wv = F(wv);
+    C.disk_u = F(u * dr);
+    C.disk_v = F(v * dr);
+    C.focus_dist = float(c.focus_dist);
+    C.ortho_height = float(c.ortho_height);
+    C.defocus_angle = float(c.defocus_angle);
+    C.blades = c.blades;
+    C.blade_rotation = float(c.blade_rotation * pi / 180.0);
+    return C;
+}
+
+int bad_arg(const std::string& m) {
+    set_error_message(m);
+    return MYPBR_ERR_INVALID_ARGUMENT;
+}
+
+struct Launch {
+    int grid_extend, grid_shade, grid_shadow, grid_stream;
+};
+
+Launch launch_config(const mypbr_gpu_scene& G) {
+    Launch L{};
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend, 256, 0);
+    L.grid_extend = G.sm_count * std::max(per_sm, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade, 256, 0);
+    L.grid_shade = G.sm_count * std::max(per_sm, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow, 256, 0);
+    L.grid_shadow = G.sm_count * std::max(per_sm, 1);
+    L.grid_stream = G.sm_count * 8;
+    return L;
+}
+
+// Renders passes [pass0, pass0 + npass) of every pixel into the film.
+int run_wave(mypbr_gpu_scene& G, WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches) {
+    MYPBR_CUDA(cudaMemsetAsync(P.B.counters, 0, sizeof(uint32_t) * size_t(2 * P.B.depth_slots + 8), st));
+    k_generate<<<L.grid_stream, 256, 0, st>>>(P);
+    launches++;
+    if (P.collect_features) {
+        k_features<<<L.grid_shade, 256, 0, st>>>(P);
+        launches++;
+    }
+    for (int depth = 0; depth < P.max_depth; depth++) {
+        k_extend<<<L.grid_extend, 256, 0, st>>>(P, depth);
+        k_shade<<<L.grid_shade, 256, 0, st>>>(P, depth);
+        k_shadow<<<L.grid_shadow, 256, 0, st>>>(P, depth);
+        launches += 3;
+    }
+    MYPBR_CUDA(cudaGetLastError());
+    return MYPBR_OK;
+}
+
+}  // namespace
+
+struct RenderSetup {
+    WaveParams P;
+    Launch L;
+    int spp, per_wave;
+    size_t npix;
+};
+
+int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* o, int save_every, RenderSetup& R) {
+    if (!G || !cam || !o)
+        return bad_arg("mypbr_gpu_render: null argument");
+    if (cam->image_width < 1 || o->samples_per_pixel < 1 || o->max_depth < 1 || o->max_depth > 4096)
+        return bad_arg("mypbr_gpu_render: image_width, samples_per_pixel and max_depth must be positive");
+    if (o->guided != 0) {
+        set_error_message("mypbr_gpu_render: the guided sampler is not available in this build");
+        return MYPBR_ERR_UNSUPPORTED;
+    }
+    if (o->max_diffuse > 255 || o->max_specular > 255 || o->max_diffuse < 0 || o->max_specular < 0 ||
+        o->max_scatter < 0)
+        return bad_arg("mypbr_gpu_render: bounce caps must be in [0, 255]");
+    MYPBR_CUDA(cudaSetDevice(G->device));
+    WaveParams& P = R.P;
+    P = WaveParams{};
+    P.S = G->dev;
+    P.cam = make_camera(*cam, o->samples_per_pixel);
+    P.max_depth = o->max_depth;
+    P.max_diffuse = o->max_diffuse;
+    P.max_specular = o->max_specular;
+    P.max_scatter = o->max_scatter;
+    P.transparent_shadows = o->transparent_shadows;
+    P.collect_features = o->collect_features;
+    P.has_lights = G->dev.light_count > 0;
+    P.seed = o->seed;
+    R.npix = size_t(P.cam.width) * P.cam.height;
+    if (R.npix > (size_t(1) << 31))
+        return bad_arg("mypbr_gpu_render: image too large");
+    R.spp = o->samples_per_pixel;
+    // About 8M paths in flight per wave (or what the caller asks)
+    int per_wave = o->samples_per_wave > 0 ? o->samples_per_wave
+                                           : int(std::max<size_t>(1, (size_t(8) << 20) / std::max<size_t>(R.npix, 1)));
+    per_wave = std::min(per_wave, R.spp);
+    if (save_every > 0)
+        per_wave = std::min(per_wave, save_every);
+    while (per_wave > 1 && R.npix * size_t(per_wave) > (size_t(1) << 30))
+        per_wave /= 2;
+    R.per_wave = per_wave;
+    int s = ensure_buffers(G->rb, R.npix * size_t(per_wave), R.npix, P.max_depth + 1);
+    if (s != MYPBR_OK)
+        return s;
+    P.B = G->rb;
+    R.L = launch_config(*G);
+    return MYPBR_OK;
+}
+
+struct Totals {
+    unsigned long long* d = nullptr;
+    ~Totals() {
+        if (d)
+            cudaFree(d);
+    }
+};
+
+int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_rad, double* d_alb, double* d_nrm,
+               double* d_var, double* d_chvar, int save_every, mypbr_pass_callback cb, void* user,
+               double* h_rad, double* h_alb, double* h_nrm, double* h_var, mypbr_render_stats* stats) {
+    WaveParams& P = R.P;
+    Totals tot;
+    MYPBR_CUDA(cudaMalloc(&tot.d, 2 * sizeof(unsigned long long)));
+    MYPBR_CUDA(cudaMemsetAsync(tot.d, 0, 2 * sizeof(unsigned long long), st));
+    P.totals = tot.d;
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * R.npix * sizeof(double), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * R.npix * sizeof(double), st));
+    if (P.collect_features)
+        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * R.npix * sizeof(double), st));
+    uint64_t launches = 0;
+    for (int pass0 = 0; pass0 < R.spp; pass0 += R.per_wave) {
+        P.pass0 = pass0;
+        P.npass = std::min(R.per_wave, R.spp - pass0);
+        int s = run_wave(*G, P, R.L, st, launches);
+        if (s != MYPBR_OK)
+            return s;
+        int done = pass0 + P.npass;
+        if (cb && save_every > 0 && done % save_every == 0 && done < R.spp) {
+            k_resolve<<<R.L.grid_stream, 256, 0, st>>>(P, done, d_rad, d_alb, d_nrm, d_var);
+            launches++;
+            MYPBR_CUDA(cudaGetLastError());
+            if (h_rad) {
+                MYPBR_CUDA(cudaMemcpyAsync(h_rad, d_rad, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                if (P.collect_features) {
+                    if (h_alb)
+                        MYPBR_CUDA(cudaMemcpyAsync(h_alb, d_alb, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                    if (h_nrm)
+                        MYPBR_CUDA(cudaMemcpyAsync(h_nrm, d_nrm, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                    if (h_var)
+                        MYPBR_CUDA(cudaMemcpyAsync(h_var, d_var, R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                }
+            }
+            MYPBR_CUDA(cudaStreamSynchronize(st));
+            cb(done, user);
+        }
+    }
+    k_resolve<<<R.L.grid_stream, 256, 0, st>>>(P, R.spp, d_rad, d_alb, d_nrm, d_var);
+    launches++;
+    if (d_chvar) {
+        k_channel_variance<<<R.L.grid_stream, 256, 0, st>>>(P, R.spp, d_chvar);
+        launches++;
+    }
+    MYPBR_CUDA(cudaGetLastError());
+    if (stats) {
+        unsigned long long t[2];
+        MYPBR_CUDA(cudaMemcpyAsync(t, tot.d, sizeof t, cudaMemcpyDeviceToHost, st));
+        MYPBR_CUDA(cudaStreamSynchronize(st));
+        stats->paths = uint64_t(R.npix) * uint64_t(R.spp);
+        stats->extension_rays = t[0];
+        stats->shadow_rays = t[1];
+        stats->kernel_launches = launches;
+    }
+    return MYPBR_OK;
+}
+
+}  // namespace mypbr_dev
+
+using namespace mypbr_dev;
+
+extern "C" int mypbr_gpu_render_device(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                                       double* d_radiance, double* d_albedo, double* d_normal, double* d_variance,
+                                       void* cuda_stream, mypbr_render_stats* stats) {
+    if (!d_radiance)
+        return bad_arg("mypbr_gpu_render_device: radiance is required");
+    RenderSetup R;
+    int s = prepare(G, cam, opts, 0, R);
+    if (s != MYPBR_OK)
+        return s;
+    return render_all(G, R, static_cast<cudaStream_t>(cuda_stream), d_radiance, d_albedo, d_normal, d_variance,
+                      nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, stats);
+}
+
+namespace {
+struct DevBuf {
+    double* p = nullptr;
+    ~DevBuf() {
+        if (p)
+            cudaFree(p);
+    }
+};
+}  // namespace
+
+// The render with host outputs, plus (channel_variance != NULL) the per-channel
+// variance of the mean radiance (W*H*3) used by the statistical parity tests.
+extern "C" int mypbr_gpu_render_ex(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                                   double* radiance, double* albedo, double* normal, double* variance,
+                                   double* channel_variance, int save_every, mypbr_pass_callback on_pass, void* user,
+                                   mypbr_render_stats* stats) {
+    if (!radiance)
+        return bad_arg("mypbr_gpu_render: radiance is required");
+    RenderSetup R;
+    int s = prepare(G, cam, opts, save_every, R);
+    if (s != MYPBR_OK)
+        return s;
+    bool feats = opts->collect_features != 0;
+    DevBuf rad, alb, nrm, var, chv;
+    MYPBR_CUDA(cudaMalloc(&rad.p, 3 * R.npix * sizeof(double)));
+    if (feats) {
+        MYPBR_CUDA(cudaMalloc(&alb.p, 3 * R.npix * sizeof(double)));
+        MYPBR_CUDA(cudaMalloc(&nrm.p, 3 * R.npix * sizeof(double)));
+        MYPBR_CUDA(cudaMalloc(&var.p, R.npix * sizeof(double)));
+    }
+    if (channel_variance)
+        MYPBR_CUDA(cudaMalloc(&chv.p, 3 * R.npix * sizeof(double)));
+    cudaStream_t st = nullptr;
+    s = render_all(G, R, st, rad.p, alb.p, nrm.p, var.p, chv.p, save_every, on_pass, user, radiance,
+                   feats ? albedo : nullptr, feats ? normal : nullptr, feats ? variance : nullptr, stats);
+    if (s != MYPBR_OK)
+        return s;
+    MYPBR_CUDA(cudaMemcpyAsync(radiance, rad.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (feats) {
+        if (albedo)
+            MYPBR_CUDA(cudaMemcpyAsync(albedo, alb.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (normal)
+            MYPBR_CUDA(cudaMemcpyAsync(normal, nrm.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (variance)
+            MYPBR_CUDA(cudaMemcpyAsync(variance, var.p, R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    if (channel_variance)
+        MYPBR_CUDA(cudaMemcpyAsync(channel_variance, chv.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MYPBR_CUDA(cudaStreamSynchronize(st));
+    return MYPBR_OK;
+}
+
+extern "C" int mypbr_gpu_render(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                                double* radiance, double* albedo, double* normal, double* variance, int save_every,
+                                mypbr_pass_callback on_pass, void* user) {
+    return mypbr_gpu_render_ex(G, cam, opts, radiance, albedo, normal, variance, nullptr, save_every, on_pass, user,
+                               nullptr);
+}

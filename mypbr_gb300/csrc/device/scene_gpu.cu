@@ -1,0 +1,584 @@
+// mypbr_gpu_scene_create / destroy: the flat FP64 scene becomes the compact
+// FP32 layout of dev_scene.cuh in HBM.
+//
+// Every index of the flat scene is checked here, on the host, before anything
+// reaches the device, so the kernels can index without bounds checks:
+// materials, textures, texels, vertices, normals, uvs, transforms, BVH nodes
+// and leaf references, light members. The BVH depth is checked against the
+// traversal stack the kernels hold.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../host/bvh_build.h"
+#include "gpu_scene.h"
+
+namespace mypbr_host {
+void set_error(const std::string& message);
+}
+
+namespace mypbr_dev {
+
+void set_error_message(const std::string& m) { mypbr_host::set_error(m); }
+
+int cuda_fail(cudaError_t e, const char* what) {
+    set_error_message(std::string(what) + ": " + cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation)
+        return MYPBR_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return MYPBR_ERR_NO_DEVICE;
+    return MYPBR_ERR_CUDA;
+}
+
+namespace {
+
+float round_down(double x) {
+    float f = float(x);
+    if (double(f) > x)
+        f = std::nextafter(f, -INFINITY);
+    return f;
+}
+float round_up(double x) {
+    float f = float(x);
+    if (double(f) < x)
+        f = std::nextafter(f, INFINITY);
+    return f;
+}
+
+// The bits of an int in a float slot (host side of __float_as_int).
+float ibits(int i) {
+    float f;
+    std::memcpy(&f, &i, sizeof f);
+    return f;
+}
+
+int bad(const std::string& m) {
+    set_error_message("mypbr_gpu_scene_create: " + m);
+    return MYPBR_ERR_INVALID_ARGUMENT;
+}
+
+struct Uploader {
+    mypbr_gpu_scene& G;
+    template <typename T>
+    int put(const std::vector<T>& v, const T*& out) {
+        out = nullptr;
+        if (v.empty())
+            return MYPBR_OK;
+        void* p = nullptr;
+        MYPBR_CUDA(cudaMalloc(&p, v.size() * sizeof(T)));
+        G.allocations.push_back(p);
+        MYPBR_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        out = static_cast<const T*>(p);
+        return MYPBR_OK;
+    }
+};
+
+const std::vector<double>& ggx_table_cached() {
+    static std::vector<double> table;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        table.resize(32 * 32 + 32);
+        mypbr_host::ggx_albedo_table(table.data());
+    });
+    return table;
+}
+
+int validate(const mypbr_flat_scene& F) {
+    auto in = [](int64_t i, int64_t n) { return i >= 0 && i < n; };
+    int64_t nm = F.material_count, nt = F.texture_count;
+    if (nm <= 0)
+        return bad("the scene has no materials");
+    for (int64_t k = 0; k < nm; k++) {
+        const auto& m = F.materials[k];
+        if (m.type < 0 || m.type > MYPBR_MAT_PHASE)
+            return bad("material " + std::to_string(k) + " has an unknown type");
+        for (int t : m.tex)
+            if (t != -1 && !in(t, nt))
+                return bad("material " + std::to_string(k) + " names a missing texture");
+        if ((m.normal_map != -1 && !in(m.normal_map, nt)) || (m.emission_tex != -1 && !in(m.emission_tex, nt)))
+            return bad("material " + std::to_string(k) + " names a missing texture");
+        if ((m.type == MYPBR_MAT_LAMBERTIAN && m.tex[0] < 0) ||
+            (m.type == MYPBR_MAT_PRINCIPLED && (m.tex[0] < 0 || m.tex[1] < 0 || m.tex[2] < 0)) ||
+            (m.type == MYPBR_MAT_PRINCIPLED && (m.flags & MYPBR_MATF_COAT) && (m.tex[4] < 0 || m.tex[5] < 0)))
+            return bad("material " + std::to_string(k) + " lacks a texture it needs");
+    }
+    for (int64_t k = 0; k < nt; k++) {
+        const auto& t = F.textures[k];
+        if (t.type == MYPBR_TEX_CHECKER) {
+            if (!in(t.a, nt) || !in(t.b, nt) || F.textures[t.a].type == MYPBR_TEX_CHECKER ||
+                F.textures[t.b].type == MYPBR_TEX_CHECKER)
+                return bad("checker texture " + std::to_string(k) + " must pick between two plain textures");
+        } else if (t.type == MYPBR_TEX_IMAGE) {
+            int64_t texels = int64_t(t.width) * t.height;
+            if (t.width <= 0 || t.height <= 0 || t.offset < 0)
+                return bad("image texture " + std::to_string(k) + " has no pixels");
+            if (t.flags & MYPBR_TEXF_HDR) {
+                if ((t.offset + texels) * 3 > F.texels_hdr_count)
+                    return bad("image texture " + std::to_string(k) + " runs past texels_hdr");
+            } else if ((t.offset + texels) * 4 > F.texels_ldr_bytes) {
+                return bad("image texture " + std::to_string(k) + " runs past texels_ldr");
+            }
+        } else if (t.type != MYPBR_TEX_SOLID) {
+            return bad("texture " + std::to_string(k) + " has an unknown type");
+        }
+    }
+    for (int64_t k = 0; k < F.sphere_count; k++)
+        if (!in(F.spheres[k].material, nm) || (F.spheres[k].xform != -1 && !in(F.spheres[k].xform, F.xform_count)) ||
+            F.spheres[k].radius == 0)
+            return bad("sphere " + std::to_string(k) + " is malformed");
+    for (int64_t k = 0; k < F.quad_count; k++)
+        if (!in(F.quads[k].material, nm))
+            return bad("quad " + std::to_string(k) + " names a missing material");
+    for (int64_t k = 0; k < F.triangle_count; k++) {
+        const auto& t = F.triangles[k];
+        if (!in(t.material, nm))
+            return bad("triangle " + std::to_string(k) + " names a missing material");
+        for (int c = 0; c < 3; c++) {
+            if (!in(t.v[c], F.position_count) || (t.n[c] != -1 && !in(t.n[c], F.normal_count)) ||
+                (t.t[c] != -1 && !in(t.t[c], F.uv_count)))
+                return bad("triangle " + std::to_string(k) + " has an index out of range");
+        }
+        if ((t.n[0] < 0) != (t.n[1] < 0) || (t.n[0] < 0) != (t.n[2] < 0) || (t.t[0] < 0) != (t.t[1] < 0) ||
+            (t.t[0] < 0) != (t.t[2] < 0))
+            return bad("triangle " + std::to_string(k) + " mixes present and missing normals or uvs");
+    }
+    for (int64_t k = 0; k < F.medium_count; k++) {
+        const auto& m = F.media[k];
+        if (!in(m.material, nm) || (m.xform != -1 && !in(m.xform, F.xform_count)) || m.shape < 0 || m.shape > 1 ||
+            !(m.density > 0))
+            return bad("medium " + std::to_string(k) + " is malformed");
+    }
+    for (int64_t k = 0; k < F.unbounded_count; k++) {
+        const auto& u = F.unbounded[k];
+        if (!in(u.material, nm) || u.kind < 0 || u.kind > 1 ||
+            (u.kind == MYPBR_UNBOUNDED_HEIGHT_FOG && !(u.density > 0 && u.scale_height > 0)))
+            return bad("unbounded object " + std::to_string(k) + " is malformed");
+    }
+    auto prim_count = [&](int kind) -> int64_t {
+        switch (kind) {
+            case MYPBR_PRIM_SPHERE: return F.sphere_count;
+            case MYPBR_PRIM_QUAD: return F.quad_count;
+            case MYPBR_PRIM_TRIANGLE: return F.triangle_count;
+            case MYPBR_PRIM_MEDIUM: return F.medium_count;
+            default: return -1;
+        }
+    };
+    for (int64_t k = 0; k < F.bvh_prim_count; k++) {
+        const auto& r = F.bvh_prims[k];
+        int64_t n = prim_count(r.kind);
+        if (n < 0 || !in(r.index, n) || r.index >= int64_t(kIndexMask))
+            return bad("BVH primitive reference " + std::to_string(k) + " is out of range");
+    }
+    if (F.bvh_prim_count > 0) {
+        if (F.bvh_node_count <= 0)
+            return bad("primitives without BVH nodes");
+        for (int64_t k = 0; k < F.bvh_node_count; k++) {
+            const auto& n = F.bvh_nodes[k];
+            if (n.count > 0) {
+                if (n.offset < 0 || int64_t(n.offset) + n.count > F.bvh_prim_count)
+                    return bad("BVH leaf " + std::to_string(k) + " runs past the primitive references");
+            } else if (n.count == 0) {
+                if (k + 1 >= F.bvh_node_count || n.offset <= k || n.offset >= F.bvh_node_count)
+                    return bad("BVH node " + std::to_string(k) + " has a child out of range");
+            } else {
+                return bad("BVH node " + std::to_string(k) + " has a negative count");
+            }
+        }
+    }
+    for (int64_t k = 0; k < F.light_count; k++) {
+        const auto& L = F.lights[k];
+        if (L.kind == MYPBR_LIGHT_GROUP) {
+            if (L.member_count <= 0 || L.first_member < 0 ||
+                int64_t(L.first_member) + L.member_count > F.light_member_count)
+                return bad("light " + std::to_string(k) + " has members out of range");
+            for (int m = 0; m < L.member_count; m++) {
+                const auto& mb = F.light_members[L.first_member + m];
+                if (mb.prim_kind < 0 || mb.prim_kind > MYPBR_PRIM_TRIANGLE || !in(mb.prim_index, prim_count(mb.prim_kind)))
+                    return bad("light member of light " + std::to_string(k) + " is out of range");
+            }
+        } else if (L.kind == MYPBR_LIGHT_ENVIRONMENT) {
+            if (F.environment.width <= 0 || F.environment.height <= 0 || !F.environment.pixels)
+                return bad("an environment light without an environment");
+        } else if (L.kind == MYPBR_LIGHT_SUN) {
+            if (!F.sun.enabled)
+                return bad("a sun light without a sun");
+        } else {
+            return bad("light " + std::to_string(k) + " has an unknown kind");
+        }
+    }
+    return MYPBR_OK;
+}
+
+// Depth of the DFS BVH below node k (iterative, no recursion on deep trees).
+int bvh_depth(const mypbr_flat_scene& F) {
+    int best = 0;
+    std::vector<std::pair<int, int>> st{{0, 1}};
+    while (!st.empty()) {
+        auto [k, d] = st.back();
+        st.pop_back();
+        best = std::max(best, d);
+        const auto& n = F.bvh_nodes[k];
+        if (n.count == 0) {
+            st.push_back({k + 1, d + 1});
+            st.push_back({n.offset, d + 1});
+        }
+    }
+    return best;
+}
+
+}  // namespace
+
+int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
+    if (!Fp || !out)
+        return bad("null argument");
+    *out = nullptr;
+    const mypbr_flat_scene& F = *Fp;
+    if (F.abi_version != MYPBR_ABI_VERSION)
+        return bad("ABI version mismatch");
+    int status = validate(F);
+    if (status != MYPBR_OK)
+        return status;
+
+    int device_count = 0;
+    cudaError_t ce = cudaGetDeviceCount(&device_count);
+    if (ce != cudaSuccess || device_count == 0) {
+        set_error_message("mypbr_gpu_scene_create: no CUDA device is visible");
+        return MYPBR_ERR_NO_DEVICE;
+    }
+    auto holder = std::make_unique<mypbr_gpu_scene>();
+    mypbr_gpu_scene& G = *holder;
+    MYPBR_CUDA(cudaGetDevice(&G.device));
+    MYPBR_CUDA(cudaDeviceGetAttribute(&G.sm_count, cudaDevAttrMultiProcessorCount, G.device));
+    DeviceScene& D = G.dev;
+    Uploader up{G};
+    auto fail_cleanup = [&](int s) {
+        for (void* p : G.allocations)
+            cudaFree(p);
+        G.allocations.clear();
+        return s;
+    };
+#define PUT(vec, dst)                          \
+    do {                                       \
+        int s_ = up.put((vec), (dst));         \
+        if (s_ != MYPBR_OK)                    \
+            return fail_cleanup(s_);           \
+    } while (0)
+
+    // ---- BVH: child boxes stored in the parent
+    std::vector<float4> nodes;
+    std::vector<uint32_t> refs;
+    D.has_bvh = F.bvh_prim_count > 0;
+    if (D.has_bvh) {
+        G.max_depth_bvh = bvh_depth(F);
+        if (G.max_depth_bvh >= kBvhStack) {
+            set_error_message("mypbr_gpu_scene_create: BVH depth " + std::to_string(G.max_depth_bvh) +
+                              " exceeds the traversal stack (" + std::to_string(kBvhStack) + ")");
+            return MYPBR_ERR_UNSUPPORTED;
+        }
+        std::vector<int> new_index(size_t(F.bvh_node_count), -1);
+        int interior = 0;
+        for (int64_t k = 0; k < F.bvh_node_count; k++)
+            if (F.bvh_nodes[k].count == 0)
+                new_index[size_t(k)] = interior++;
+        auto child_entry = [&](int64_t c, float4& lo, float4& hi) {
+            const auto& n = F.bvh_nodes[c];
+            lo = make_float4(round_down(n.bmin[0]), round_down(n.bmin[1]), round_down(n.bmin[2]), 0.0f);
+            hi = make_float4(round_up(n.bmax[0]), round_up(n.bmax[1]), round_up(n.bmax[2]), 0.0f);
+            int idx = n.count > 0 ? n.offset : new_index[size_t(c)];
+            lo.w = ibits(idx);
+            hi.w = ibits(n.count);
+        };
+        if (F.bvh_nodes[0].count > 0) {
+            // A root leaf: one node holding it, beside a box nothing can hit
+            float4 lo, hi;
+            child_entry(0, lo, hi);
+            nodes = {lo, hi, make_float4(1e30f, 1e30f, 1e30f, ibits(0)),
+                     make_float4(-1e30f, -1e30f, -1e30f, ibits(0))};
+        } else {
+            nodes.resize(size_t(interior) * 4);
+            for (int64_t k = 0; k < F.bvh_node_count; k++) {
+                const auto& n = F.bvh_nodes[k];
+                if (n.count != 0)
+                    continue;
+                float4* dst = &nodes[size_t(new_index[size_t(k)]) * 4];
+                child_entry(k + 1, dst[0], dst[1]);
+                child_entry(n.offset, dst[2], dst[3]);
+            }
+        }
+        refs.resize(size_t(F.bvh_prim_count));
+        for (int64_t k = 0; k < F.bvh_prim_count; k++)
+            refs[size_t(k)] = (uint32_t(F.bvh_prims[k].kind) << kKindShift) | uint32_t(F.bvh_prims[k].index);
+    }
+    PUT(nodes, D.bvh);
+    PUT(refs, D.leaf_refs);
+    G.leaf_ref_count = refs.size();
+
+    // ---- primitives
+    std::vector<float4> spheres;
+    std::vector<int2> sphere_info;
+    for (int64_t k = 0; k < F.sphere_count; k++) {
+        const auto& s = F.spheres[k];
+        spheres.push_back(make_float4(float(s.center[0]), float(s.center[1]), float(s.center[2]), float(s.radius)));
+        sphere_info.push_back(make_int2(s.material, s.xform));
+    }
+    PUT(spheres, D.spheres);
+    PUT(sphere_info, D.sphere_info);
+
+    std::vector<float4> quads;
+    for (int64_t k = 0; k < F.quad_count; k++) {
+        const auto& q = F.quads[k];
+        mypbr_host::V3 u(q.u[0], q.u[1], q.u[2]), v(q.v[0], q.v[1], q.v[2]);
+        mypbr_host::V3 c = mypbr_host::cross(u, v);
+        mypbr_host::V3 w = c / mypbr_host::dot(c, c);
+        quads.push_back(make_float4(float(q.q[0]), float(q.q[1]), float(q.q[2]), ibits(q.material)));
+        quads.push_back(make_float4(float(u.x), float(u.y), float(u.z), 0.0f));
+        quads.push_back(make_float4(float(v.x), float(v.y), float(v.z), 0.0f));
+        quads.push_back(make_float4(float(q.normal[0]), float(q.normal[1]), float(q.normal[2]), 0.0f));
+        quads.push_back(make_float4(float(w.x), float(w.y), float(w.z), 0.0f));
+    }
+    PUT(quads, D.quads);
+
+    std::vector<float4> tris;
+    std::vector<int4> tri_shading;
+    tris.reserve(size_t(F.triangle_count) * 3);
+    for (int64_t k = 0; k < F.triangle_count; k++) {
+        const auto& t = F.triangles[k];
+        for (int c = 0; c < 3; c++) {
+            const double* p = F.positions + 3 * int64_t(t.v[c]);
+            int w = c == 0 ? t.material : (c == 1 ? t.flags : t.mesh);
+            tris.push_back(make_float4(float(p[0]), float(p[1]), float(p[2]), ibits(w)));
+        }
+        tri_shading.push_back(make_int4(t.n[0], t.n[1], t.n[2], t.t[0]));
+        tri_shading.push_back(make_int4(t.t[1], t.t[2], -1, -1));
+    }
+    PUT(tris, D.tris);
+    PUT(tri_shading, D.tri_shading);
+    std::vector<float3> normals;
+    for (int64_t k = 0; k < F.normal_count; k++)
+        normals.push_back(make_float3(float(F.normals[3 * k]), float(F.normals[3 * k + 1]), float(F.normals[3 * k + 2])));
+    PUT(normals, D.normals);
+    std::vector<float2> uvs;
+    for (int64_t k = 0; k < F.uv_count; k++)
+        uvs.push_back(make_float2(float(F.uvs[2 * k]), float(F.uvs[2 * k + 1])));
+    PUT(uvs, D.uvs);
+
+    std::vector<float4> media;
+    for (int64_t k = 0; k < F.medium_count; k++) {
+        const auto& m = F.media[k];
+        media.push_back(make_float4(float(m.a[0]), float(m.a[1]), float(m.a[2]), float(m.density)));
+        media.push_back(make_float4(float(m.b[0]), float(m.b[1]), float(m.b[2]), ibits(m.shape)));
+        media.push_back(make_float4(ibits(m.xform), ibits(m.material), 0.0f, 0.0f));
+    }
+    PUT(media, D.media);
+
+    std::vector<float4> xforms;
+    for (int64_t k = 0; k < F.xform_count; k++) {
+        const auto& x = F.xforms[k];
+        for (int r = 0; r < 3; r++)
+            xforms.push_back(make_float4(float(x.m[r][0]), float(x.m[r][1]), float(x.m[r][2]), float(x.t[r])));
+        for (int r = 0; r < 3; r++)
+            xforms.push_back(
+                make_float4(float(x.inv_m[r][0]), float(x.inv_m[r][1]), float(x.inv_m[r][2]), float(x.inv_t[r])));
+    }
+    PUT(xforms, D.xforms);
+
+    std::vector<DevUnbounded> unb;
+    for (int64_t k = 0; k < F.unbounded_count; k++) {
+        const auto& u = F.unbounded[k];
+        DevUnbounded d{};
+        d.kind = u.kind;
+        d.material = u.material;
+        d.height = float(u.height);
+        d.density = float(u.density);
+        d.scale_height = float(u.scale_height);
+        unb.push_back(d);
+    }
+    PUT(unb, D.unbounded);
+    D.unbounded_count = int(unb.size());
+
+    // ---- appearance
+    std::vector<DevMaterial> mats;
+    for (int64_t k = 0; k < F.material_count; k++) {
+        const auto& m = F.materials[k];
+        DevMaterial d{};
+        d.type = m.type;
+        d.flags = m.flags;
+        d.normal_map = m.normal_map;
+        d.emission_tex = m.emission_tex;
+        for (int t = 0; t < 8; t++)
+            d.tex[t] = m.tex[t];
+        for (int p = 0; p < 16; p++)
+            d.p[p] = float(m.p[p]);
+        mats.push_back(d);
+    }
+    PUT(mats, D.materials);
+    std::vector<DevTexture> texs;
+    for (int64_t k = 0; k < F.texture_count; k++) {
+        const auto& t = F.textures[k];
+        DevTexture d{};
+        d.type = t.type;
+        d.a = t.a;
+        d.b = t.b;
+        d.width = t.width;
+        d.height = t.height;
+        d.flags = t.flags;
+        d.offset = t.offset;
+        for (int p = 0; p < 4; p++)
+            d.p[p] = float(t.p[p]);
+        texs.push_back(d);
+    }
+    PUT(texs, D.textures);
+    std::vector<uint8_t> ldr(F.texels_ldr, F.texels_ldr + F.texels_ldr_bytes);
+    PUT(ldr, D.texels_ldr);
+    std::vector<float> hdr(F.texels_hdr, F.texels_hdr + F.texels_hdr_count);
+    PUT(hdr, D.texels_hdr);
+    const auto& tab = ggx_table_cached();
+    std::vector<float> ge(tab.begin(), tab.begin() + 1024), ga(tab.begin() + 1024, tab.end());
+    PUT(ge, D.ggx_e);
+    PUT(ga, D.ggx_eavg);
+
+    // ---- lights
+    std::vector<DevLight> lights;
+    std::vector<DevMember> members(size_t(F.light_member_count));
+    double acc = 0;
+    for (int64_t k = 0; k < F.light_count; k++) {
+        const auto& L = F.lights[k];
+        DevLight d{};
+        d.kind = L.kind;
+        d.first_member = L.first_member;
+        d.member_count = L.member_count;
+        d.probability = float(L.probability);
+        acc += L.probability;
+        d.cdf_hi = k + 1 == F.light_count ? 2.0f : float(acc);  // the last light takes the rest
+        lights.push_back(d);
+        if (L.kind == MYPBR_LIGHT_GROUP) {
+            double macc = 0;
+            for (int m = 0; m < L.member_count; m++) {
+                const auto& mb = F.light_members[L.first_member + m];
+                macc += mb.weight;
+                DevMember dm{};
+                dm.kind = mb.prim_kind;
+                dm.index = mb.prim_index;
+                dm.weight = float(mb.weight);
+                dm.cdf = m + 1 == L.member_count ? 2.0f : float(macc);
+                members[size_t(L.first_member + m)] = dm;
+            }
+        }
+    }
+    PUT(lights, D.lights);
+    PUT(members, D.members);
+    D.light_count = int(lights.size());
+
+    // ---- environment: pixels, per-texel pdf and alias table
+    D.env_w = F.environment.width > 0 ? F.environment.width : 0;
+    D.env_h = D.env_w > 0 ? F.environment.height : 0;
+    D.env_intensity = float(F.environment.intensity);
+    D.env_rotation = float(F.environment.rotation);
+    if (D.env_w > 0) {
+        int w = D.env_w, h = D.env_h;
+        size_t n = size_t(w) * h;
+        std::vector<float4> px(n);
+        std::vector<double> wgt(n);
+        std::vector<double> row(h, 0.0);
+        const double kPiD = 3.1415926535897932385;
+        double total = 0;
+        for (int j = 0; j < h; j++) {
+            double st = std::sin(kPiD * (j + 0.5) / h);
+            for (int i = 0; i < w; i++) {
+                const float* p = F.environment.pixels + (size_t(j) * w + i) * 3;
+                px[size_t(j) * w + i] = make_float4(p[0], p[1], p[2], 0.0f);
+                double l = 0.2126 * p[0] + 0.7152 * p[1] + 0.0722 * p[2];
+                wgt[size_t(j) * w + i] = std::fmax(l * st, 0.0);
+                row[j] += wgt[size_t(j) * w + i];
+            }
+            total += row[j];
+        }
+        std::vector<double> prob(n);
+        if (total > 0) {
+            for (size_t k = 0; k < n; k++)
+                prob[k] = wgt[k] / total;
+        } else {
+            // A black sky: rows by sin(theta), uniform within a row (environment.h:302-309)
+            double s = 0;
+            for (int j = 0; j < h; j++)
+                s += std::sin(kPiD * (j + 0.5) / h);
+            for (int j = 0; j < h; j++)
+                for (int i = 0; i < w; i++)
+                    prob[size_t(j) * w + i] = std::sin(kPiD * (j + 0.5) / h) / s / w;
+        }
+        std::vector<float> texel_pdf(n);
+        for (size_t k = 0; k < n; k++)
+            texel_pdf[k] = float(prob[k] * double(w) * double(h));
+        // Vose's alias method
+        std::vector<float2> alias(n);
+        std::vector<double> scaled(n);
+        std::vector<uint32_t> small, large;
+        for (size_t k = 0; k < n; k++) {
+            scaled[k] = prob[k] * double(n);
+            (scaled[k] < 1.0 ? small : large).push_back(uint32_t(k));
+        }
+        while (!small.empty() && !large.empty()) {
+            uint32_t s = small.back(), l = large.back();
+            small.pop_back();
+            alias[s] = make_float2(float(scaled[s]), ibits(int(l)));
+            scaled[l] = (scaled[l] + scaled[s]) - 1.0;
+            if (scaled[l] < 1.0) {
+                large.pop_back();
+                small.push_back(l);
+            }
+        }
+        for (uint32_t l : large)
+            alias[l] = make_float2(1.0f, ibits(int(l)));
+        for (uint32_t s : small)
+            alias[s] = make_float2(1.0f, ibits(int(s)));
+        PUT(px, D.env_pixels);
+        PUT(texel_pdf, D.env_texel_pdf);
+        PUT(alias, D.env_alias);
+    }
+
+    // ---- sun (sun.h:23-43) and the plain sky
+    D.sun_enabled = F.sun.enabled;
+    D.sun_disk_visible = F.sun.disk_visible;
+    if (F.sun.enabled) {
+        mypbr_host::V3 d(F.sun.direction[0], F.sun.direction[1], F.sun.direction[2]);
+        d = mypbr_host::unit(d);
+        double half = std::fmax(F.sun.angular_diameter, 1e-3) * 3.1415926535897932385 / 180.0 / 2;
+        double cmax = std::cos(half);
+        double omega = 2 * 3.1415926535897932385 * (1 - cmax);
+        D.sun_dir = make_float3(float(d.x), float(d.y), float(d.z));
+        D.sun_cos_max = float(cmax);
+        D.sun_solid_angle = float(omega);
+        D.sun_radiance = make_float3(float(F.sun.irradiance[0] / omega), float(F.sun.irradiance[1] / omega),
+                                     float(F.sun.irradiance[2] / omega));
+    }
+    G.material_count = F.material_count;
+    D.use_sky = F.use_sky;
+    D.background = make_float3(float(F.background[0]), float(F.background[1]), float(F.background[2]));
+#undef PUT
+    *out = holder.release();
+    return MYPBR_OK;
+}
+
+}  // namespace mypbr_dev
+
+extern "C" int mypbr_gpu_scene_create(const mypbr_flat_scene* scene, mypbr_gpu_scene** out) {
+    try {
+        return mypbr_dev::create_scene(scene, out);
+    } catch (const std::bad_alloc&) {
+        mypbr_dev::set_error_message("mypbr_gpu_scene_create: out of host memory");
+        return MYPBR_ERR_OUT_OF_MEMORY;
+    }
+}
+
+extern "C" void mypbr_gpu_scene_destroy(mypbr_gpu_scene* scene) {
+    if (!scene)
+        return;
+    mypbr_dev::release_buffers(scene->rb);
+    for (void* p : scene->allocations)
+        cudaFree(p);
+    delete scene;
+}

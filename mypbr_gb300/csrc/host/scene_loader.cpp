@@ -1,0 +1,1809 @@
+// The host scene layer: parses mypbr's .scene language into a mypbr_flat_scene.
+//
+// It accepts the reference's grammar (include/scene.h:44-243, parsed at
+// scene.h:244-551) and keeps its meaning: the same defaults, the same order in
+// which lights enter the light list (emissive objects as they appear, the
+// environment at its line, then "sky uniform" and the sun at the end of the
+// file), the same bounding boxes for the scene radius that env/sun power uses
+// (light_list.h:45-96), and "path:line: message" errors. What changes is the
+// result: instead of a graph of virtual objects, transforms are baked into
+// world-space quads and triangles (spheres and media keep their transform,
+// as instance::hit does), and one BVH is built over every primitive.
+//
+// Not handled here (MYPBR_ERR_UNSUPPORTED with a message): glTF meshes, .vox
+// models, "sky atmosphere" / "style voxel", cyclorama, softbox, MTL files and
+// 8-bit image textures (PNG/JPEG); .hdr images are read.
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../../include/mypbr_gpu.h"
+#include "bvh_build.h"
+#include "host_math.h"
+#include "host_scene.h"
+
+using namespace mypbr_host;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+}  // namespace
+
+namespace mypbr_host {
+
+void set_error(const std::string& message) { g_last_error = message; }
+void clear_error() { g_last_error.clear(); }
+
+// ------------------------------------------------------------ .hdr reading
+
+// Reads a Radiance RGBE (.hdr) image as linear RGB floats, row 0 at the top.
+// Each pixel is mantissa * 2^(exponent - 136) per channel (exponent 0 is
+// black); scanlines may be flat or use the newer per-channel run-length code.
+bool read_hdr(const std::string& path, int& width, int& height, std::vector<float>& rgb, std::string& error) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) {
+        error = "cannot open '" + path + "'";
+        return false;
+    }
+    std::string line;
+    if (!std::getline(f, line) || (line.rfind("#?RADIANCE", 0) != 0 && line.rfind("#?RGBE", 0) != 0)) {
+        error = "'" + path + "' is not a Radiance .hdr file";
+        return false;
+    }
+    bool rgbe = false;
+    while (std::getline(f, line)) {
+        if (line.empty())
+            break;
+        if (line.find("FORMAT=32-bit_rle_rgbe") != std::string::npos)
+            rgbe = true;
+    }
+    if (!rgbe) {
+        error = "'" + path + "': unsupported .hdr pixel format";
+        return false;
+    }
+    if (!std::getline(f, line)) {
+        error = "'" + path + "': missing resolution line";
+        return false;
+    }
+    char ya[3] = {}, xa[3] = {};
+    int h = 0, w = 0;
+    if (std::sscanf(line.c_str(), "%2s %d %2s %d", ya, &h, xa, &w) != 4 || std::strcmp(ya, "-Y") != 0 ||
+        std::strcmp(xa, "+X") != 0 || w <= 0 || h <= 0) {
+        error = "'" + path + "': unsupported .hdr orientation '" + line + "'";
+        return false;
+    }
+    std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    size_t pos = 0;
+    auto get = [&](uint8_t& b) {
+        if (pos >= data.size())
+            return false;
+        b = data[pos++];
+        return true;
+    };
+    width = w;
+    height = h;
+    rgb.assign(size_t(w) * h * 3, 0.0f);
+    std::vector<uint8_t> scan(size_t(w) * 4);
+    for (int j = 0; j < h; j++) {
+        uint8_t b0, b1, b2, b3;
+        size_t start = pos;
+        if (!get(b0) || !get(b1) || !get(b2) || !get(b3)) {
+            error = "'" + path + "': truncated";
+            return false;
+        }
+        if (w >= 8 && w < 32768 && b0 == 2 && b1 == 2 && ((b2 << 8) | b3) == w && !(b2 & 0x80)) {
+            for (int c = 0; c < 4; c++) {
+                int i = 0;
+                while (i < w) {
+                    uint8_t n;
+                    if (!get(n)) {
+                        error = "'" + path + "': truncated";
+                        return false;
+                    }
+                    if (n > 128) {
+                        int run = n - 128;
+                        uint8_t v;
+                        if (!get(v) || i + run > w) {
+                            error = "'" + path + "': bad run";
+                            return false;
+                        }
+                        for (int k = 0; k < run; k++)
+                            scan[size_t(i++) * 4 + c] = v;
+                    } else {
+                        if (n == 0 || i + n > w) {
+                            error = "'" + path + "': bad run";
+                            return false;
+                        }
+                        for (int k = 0; k < n; k++) {
+                            uint8_t v;
+                            if (!get(v)) {
+                                error = "'" + path + "': truncated";
+                                return false;
+                            }
+                            scan[size_t(i++) * 4 + c] = v;
+                        }
+                    }
+                }
+            }
+        } else {
+            pos = start;
+            for (int i = 0; i < w; i++)
+                for (int c = 0; c < 4; c++)
+                    if (!get(scan[size_t(i) * 4 + c])) {
+                        error = "'" + path + "': truncated";
+                        return false;
+                    }
+        }
+        for (int i = 0; i < w; i++) {
+            const uint8_t* p = &scan[size_t(i) * 4];
+            float* o = &rgb[(size_t(j) * w + i) * 3];
+            if (p[3] == 0) {
+                o[0] = o[1] = o[2] = 0.0f;
+            } else {
+                float s = std::ldexp(1.0f, int(p[3]) - 136);
+                o[0] = p[0] * s;
+                o[1] = p[1] * s;
+                o[2] = p[2] * s;
+            }
+        }
+    }
+    return true;
+}
+
+// --------------------------------------------------------- Fresnel helpers
+
+double fresnel_conductor(double cos_i, double eta, double k) {
+    cos_i = std::clamp(cos_i, 0.0, 1.0);
+    std::complex<double> n(eta, k);
+    std::complex<double> sin2_t = (1 - cos_i * cos_i) / (n * n);
+    std::complex<double> cos_t = std::sqrt(1.0 - sin2_t);
+    std::complex<double> rp = (n * cos_i - cos_t) / (n * cos_i + cos_t);
+    std::complex<double> rs = (cos_i - n * cos_t) / (cos_i + n * cos_t);
+    return (std::norm(rp) + std::norm(rs)) / 2;
+}
+
+// The named conductors' RGB complex indices (include/microfacet.h:76-93).
+bool find_conductor(const std::string& name, V3& eta, V3& k) {
+    struct Entry {
+        const char* names[3];
+        double eta[3], k[3];
+    };
+    static const Entry table[] = {
+        {{"Al", "aluminium", "aluminum"}, {1.6575, 0.880405, 0.521244}, {9.22381, 6.2695, 4.837}},
+        {{"Ti", "titanium", "titanium"}, {3.2754, 2.37975, 2.02469}, {4.57233, 3.22453, 2.72781}},
+        {{"Cu", "copper", "copper"}, {0.201005, 0.92375, 1.10222}, {3.91326, 2.45305, 2.14209}},
+        {{"Au", "gold", "gold"}, {0.143036, 0.375307, 1.44205}, {3.983, 2.38556, 1.60336}},
+        {{"Ag", "silver", "silver"}, {0.155276, 0.116728, 0.138388}, {4.82835, 3.12222, 2.1469}},
+        {{"Cr", "chromium", "chrome"}, {4.36967, 2.91651, 1.6549}, {5.20655, 4.23131, 3.7547}},
+    };
+    for (const auto& e : table)
+        for (const char* n : e.names)
+            if (name == n) {
+                eta = V3(e.eta[0], e.eta[1], e.eta[2]);
+                k = V3(e.k[0], e.k[1], e.k[2]);
+                return true;
+            }
+    return false;
+}
+
+// f0 and the cosine-weighted hemispherical average F_avg of a measured metal:
+// 2 * int F(mu) mu dmu by the 512-point midpoint rule (microfacet.h:109-123).
+void measured_fresnel(const V3& eta, const V3& k, V3& f0, V3& f_avg) {
+    for (int c = 0; c < 3; c++) {
+        f0[c] = fresnel_conductor(1.0, eta[c], k[c]);
+        const int n = 512;
+        double sum = 0;
+        for (int i = 0; i < n; i++) {
+            double mu = (i + 0.5) / n;
+            sum += fresnel_conductor(mu, eta[c], k[c]) * mu;
+        }
+        f_avg[c] = 2 * sum / n;
+    }
+}
+
+}  // namespace mypbr_host
+
+// ------------------------------------------------------------------ parser
+
+namespace {
+
+struct PendingLight {
+    int kind;  // MYPBR_LIGHT_*
+    int first_member, member_count;
+    double power;  // < 0: computed at the end (environment / sun need the radius)
+};
+
+class Loader {
+  public:
+    mypbr_host_scene& S;
+    std::string path_for_errors;
+    std::string scene_dir;
+    int line_number = 0;
+    std::string error;
+
+    std::map<std::string, int> materials;
+    std::map<std::string, int> textures;
+    int default_material = -1;
+    bool use_normal_maps = true;
+
+    Box world_box;
+    std::vector<BuildItem> items;
+    std::vector<PendingLight> pending_lights;
+
+    // End-of-file settings (scene.h:421-451)
+    bool sun_on = false;
+    double sun_elevation = 45, sun_azimuth = 45, sun_intensity = 3, sun_angle = 4;
+    V3 sun_tint{1, 1, 1};
+    bool sun_disk = true;
+    bool sky_uniform = false, sky_atmosphere = false;
+    V3 sky_radiance;
+    bool ground = false;
+    double ground_height = 0;
+    int ground_material = -1;
+    double fog_density = 0;
+    int fog_material = -1;
+    bool has_environment = false;
+    bool uniform_sky_env = false;  // the environment is the 8 x 4 "sky uniform" image
+    bool power_selection = true;
+
+    explicit Loader(mypbr_host_scene& s) : S(s) {}
+
+    bool fail(const std::string& message) {
+        error = path_for_errors + ":" + std::to_string(line_number) + ": " + message;
+        return false;
+    }
+
+    // ------------------------------------------------------ tables
+
+    int add_texture_solid(const V3& c) {
+        mypbr_texture t{};
+        t.type = MYPBR_TEX_SOLID;
+        t.a = t.b = -1;
+        t.p[0] = c.x;
+        t.p[1] = c.y;
+        t.p[2] = c.z;
+        S.textures.push_back(t);
+        return int(S.textures.size()) - 1;
+    }
+
+    int add_material(const mypbr_material& m) {
+        S.materials.push_back(m);
+        return int(S.materials.size()) - 1;
+    }
+
+    static mypbr_material blank_material(int type) {
+        mypbr_material m{};
+        m.type = type;
+        for (int& t : m.tex)
+            t = -1;
+        m.normal_map = -1;
+        m.emission_tex = -1;
+        return m;
+    }
+
+    int lambertian(const V3& albedo) {
+        auto m = blank_material(MYPBR_MAT_LAMBERTIAN);
+        m.tex[0] = add_texture_solid(albedo);
+        return add_material(m);
+    }
+
+    bool is_emissive(int mat) const { return S.materials[mat].type == MYPBR_MAT_DIFFUSE_LIGHT; }
+
+    // luminance of diffuse_light::average_emission (material.h:588)
+    double average_emission_luminance(int mat) const {
+        const auto& m = S.materials[mat];
+        if (m.type != MYPBR_MAT_DIFFUSE_LIGHT)
+            return 0;
+        return luminance(V3(m.p[0], m.p[1], m.p[2]) * m.p[5]);
+    }
+
+    // ------------------------------------------------------ number reading
+
+    bool read_color_or_texture(std::istringstream& in, const std::string& first, int& tex) {
+        if (first == "texture") {
+            std::string name;
+            if (!(in >> name))
+                return false;
+            auto it = textures.find(name);
+            if (it == textures.end()) {
+                error = "unknown texture '" + name + "'";
+                return false;
+            }
+            tex = it->second;
+            return true;
+        }
+        std::istringstream rgb(first);
+        double r, g, b;
+        if (!(rgb >> r) || !(in >> g >> b))
+            return false;
+        tex = add_texture_solid(V3(r, g, b));
+        return true;
+    }
+
+    bool read_texture_name(std::istringstream& in, int& tex) {
+        std::string name;
+        if (!(in >> name)) {
+            error = "expected a texture name";
+            return false;
+        }
+        auto it = textures.find(name);
+        if (it == textures.end()) {
+            error = "unknown texture '" + name + "'";
+            return false;
+        }
+        tex = it->second;
+        return true;
+    }
+
+    bool read_value_or_texture(std::istringstream& in, int& tex) {
+        std::string first;
+        if (!(in >> first))
+            return false;
+        if (first == "texture")
+            return read_texture_name(in, tex);
+        std::istringstream number(first);
+        double x;
+        if (!(number >> x) || x < 0 || x > 1)
+            return false;
+        tex = add_texture_solid(V3(x, x, x));
+        return true;
+    }
+
+    // Optional material name, then transforms in order (scene.h:330-403).
+    bool read_tail(std::istringstream& in, int& mat, Xf& xform, bool& transformed) {
+        mat = default_material;
+        xform = Xf();
+        transformed = false;
+        auto is_transform = [](const std::string& t) {
+            return t == "translate" || t == "scale" || t == "rotate" || t == "rotate_x" || t == "rotate_y" ||
+                   t == "rotate_z";
+        };
+        std::string token;
+        if (!(in >> token))
+            return true;
+        if (!is_transform(token)) {
+            auto it = materials.find(token);
+            if (it == materials.end()) {
+                error = "unknown material '" + token + "'";
+                return false;
+            }
+            mat = it->second;
+            if (!(in >> token))
+                return true;
+        }
+        do {
+            Xf step;
+            bool ok = true;
+            if (token == "translate") {
+                V3 d;
+                ok = bool(in >> d.x >> d.y >> d.z);
+                step = Xf::translate(d);
+            } else if (token == "rotate_x" || token == "rotate_y" || token == "rotate_z") {
+                double deg;
+                ok = bool(in >> deg);
+                V3 axis(token == "rotate_x", token == "rotate_y", token == "rotate_z");
+                step = Xf::rotate(deg, axis);
+            } else if (token == "rotate") {
+                double deg;
+                V3 axis;
+                ok = bool(in >> deg >> axis.x >> axis.y >> axis.z) && axis.length_squared() > 0;
+                if (ok)
+                    step = Xf::rotate(deg, axis);
+            } else if (token == "scale") {
+                V3 f;
+                ok = bool(in >> f.x);
+                if (ok) {
+                    std::streampos mark = in.tellg();
+                    if (in >> f.y) {
+                        ok = bool(in >> f.z);
+                    } else {
+                        in.clear();
+                        in.seekg(mark);
+                        f = V3(f.x, f.x, f.x);
+                    }
+                }
+                ok = ok && f.x != 0 && f.y != 0 && f.z != 0;
+                step = Xf::scale(f);
+            } else {
+                error = "unexpected value '" + token +
+                        "' (expected a transform: translate, scale, rotate, rotate_x, rotate_y or rotate_z)";
+                return false;
+            }
+            if (!ok) {
+                error = "bad values for '" + token + "'";
+                return false;
+            }
+            xform = step.then_after(xform);
+            transformed = true;
+        } while (in >> token);
+        return true;
+    }
+
+    // ------------------------------------------------------ geometry
+
+    int add_xform(const Xf& x) {
+        mypbr_xform o{};
+        for (int i = 0; i < 3; i++) {
+            for (int j = 0; j < 3; j++) {
+                o.m[i][j] = x.m[i][j];
+                o.inv_m[i][j] = x.inv_m[i][j];
+            }
+            o.t[i] = x.t[i];
+            o.inv_t[i] = x.inv_t[i];
+        }
+        S.xforms.push_back(o);
+        return int(S.xforms.size()) - 1;
+    }
+
+    void add_item(int kind, int index, const Box& box) {
+        BuildItem it;
+        it.box = box;
+        it.centroid = box.centroid();
+        it.ref.kind = kind;
+        it.ref.index = index;
+        items.push_back(it);
+    }
+
+    void add_light(int first_member, int count, double power) {
+        pending_lights.push_back({MYPBR_LIGHT_GROUP, first_member, count, power});
+    }
+
+    void add_member(int kind, int index, double weight) {
+        mypbr_light_member m{};
+        m.prim_kind = kind;
+        m.prim_index = index;
+        m.weight = weight;
+        S.light_members.push_back(m);
+    }
+
+    bool check_light_xform(int mat, const Xf& xform, bool transformed) {
+        if (transformed && is_emissive(mat) && !xform.is_similarity()) {
+            error = "lights can only be moved, rotated and scaled uniformly";
+            return false;
+        }
+        return true;
+    }
+
+    bool add_sphere(const V3& c, double r, int mat, const Xf& xform, bool transformed) {
+        if (!check_light_xform(mat, xform, transformed))
+            return false;
+        mypbr_sphere s{};
+        s.center[0] = c.x;
+        s.center[1] = c.y;
+        s.center[2] = c.z;
+        s.radius = r;
+        s.material = mat;
+        s.xform = transformed ? add_xform(xform) : -1;
+        S.spheres.push_back(s);
+        int index = int(S.spheres.size()) - 1;
+        V3 rv(std::fabs(r), std::fabs(r), std::fabs(r));
+        Box box = Box::from_points(c - rv, c + rv);
+        if (transformed)
+            box = xform.box(box);
+        world_box.grow(box);
+        add_item(MYPBR_PRIM_SPHERE, index, box);
+        if (is_emissive(mat)) {
+            double power = kPi * 4 * kPi * r * r * average_emission_luminance(mat);
+            if (transformed)
+                power *= xform.area_scale();
+            int first = int(S.light_members.size());
+            add_member(MYPBR_PRIM_SPHERE, index, 1.0);
+            add_light(first, 1, power);
+        }
+        return true;
+    }
+
+    static Box quad_box(const V3& q, const V3& u, const V3& v) {
+        Box b = Box::from_points(q, q + u + v);
+        b.grow(Box::from_points(q + u, q + v));
+        return b;
+    }
+
+    // Adds one world-space quad (object-space q, u, v moved by xform); returns its index.
+    int push_quad(const V3& q, const V3& u, const V3& v, int mat, const Xf& xform, bool transformed) {
+        mypbr_quad o{};
+        V3 n = unit(cross(u, v));
+        V3 wq = q, wu = u, wv = v, wn = n;
+        if (transformed) {
+            wq = xform.point(q);
+            wu = xform.vec(u);
+            wv = xform.vec(v);
+            wn = unit(xform.normal(n));
+        }
+        for (int k = 0; k < 3; k++) {
+            o.q[k] = wq[k];
+            o.u[k] = wu[k];
+            o.v[k] = wv[k];
+            o.normal[k] = wn[k];
+        }
+        o.material = mat;
+        S.quads.push_back(o);
+        int index = int(S.quads.size()) - 1;
+        Box box = transformed ? xform.box(quad_box(q, u, v)) : quad_box(q, u, v);
+        add_item(MYPBR_PRIM_QUAD, index, box);
+        return index;
+    }
+
+    bool add_quad(const V3& q, const V3& u, const V3& v, int mat, const Xf& xform, bool transformed) {
+        if (!check_light_xform(mat, xform, transformed))
+            return false;
+        int index = push_quad(q, u, v, mat, xform, transformed);
+        Box box = quad_box(q, u, v);
+        world_box.grow(transformed ? xform.box(box) : box);
+        if (is_emissive(mat)) {
+            double power = kPi * cross(u, v).length() * average_emission_luminance(mat);
+            if (transformed)
+                power *= xform.area_scale();
+            int first = int(S.light_members.size());
+            add_member(MYPBR_PRIM_QUAD, index, 1.0);
+            add_light(first, 1, power);
+        }
+        return true;
+    }
+
+    // The six sides of the box with opposite corners a, b (quad.h:95-113).
+    static void box_sides(const V3& a, const V3& b, V3 q[6], V3 u[6], V3 v[6]) {
+        V3 mn(std::fmin(a.x, b.x), std::fmin(a.y, b.y), std::fmin(a.z, b.z));
+        V3 mx(std::fmax(a.x, b.x), std::fmax(a.y, b.y), std::fmax(a.z, b.z));
+        V3 dx(mx.x - mn.x, 0, 0), dy(0, mx.y - mn.y, 0), dz(0, 0, mx.z - mn.z);
+        q[0] = V3(mn.x, mn.y, mx.z); u[0] = dx;  v[0] = dy;   // front
+        q[1] = V3(mx.x, mn.y, mx.z); u[1] = -dz; v[1] = dy;   // right
+        q[2] = V3(mx.x, mn.y, mn.z); u[2] = -dx; v[2] = dy;   // back
+        q[3] = V3(mn.x, mn.y, mn.z); u[3] = dz;  v[3] = dy;   // left
+        q[4] = V3(mn.x, mx.y, mx.z); u[4] = dx;  v[4] = -dz;  // top
+        q[5] = V3(mn.x, mn.y, mn.z); u[5] = dx;  v[5] = dz;   // bottom
+    }
+
+    static Box box_bounds(const V3& a, const V3& b) {
+        V3 q[6], u[6], v[6];
+        box_sides(a, b, q, u, v);
+        Box box;
+        for (int s = 0; s < 6; s++)
+            box.grow(quad_box(q[s], u[s], v[s]));
+        return box;
+    }
+
+    bool add_box(const V3& a, const V3& b, int mat, const Xf& xform, bool transformed) {
+        if (!check_light_xform(mat, xform, transformed))
+            return false;
+        V3 q[6], u[6], v[6];
+        box_sides(a, b, q, u, v);
+        int idx[6];
+        double power = 0;
+        for (int s = 0; s < 6; s++) {
+            idx[s] = push_quad(q[s], u[s], v[s], mat, xform, transformed);
+            power += kPi * cross(u[s], v[s]).length() * average_emission_luminance(mat);
+        }
+        Box box = box_bounds(a, b);
+        world_box.grow(transformed ? xform.box(box) : box);
+        if (is_emissive(mat)) {
+            if (transformed)
+                power *= xform.area_scale();
+            int first = int(S.light_members.size());
+            for (int s = 0; s < 6; s++)
+                add_member(MYPBR_PRIM_QUAD, idx[s], 1.0 / 6);
+            add_light(first, 6, power);
+        }
+        return true;
+    }
+
+    bool add_medium(double density, bool sphere, const V3& a, const V3& b, int mat, const Xf& xform,
+                    bool transformed) {
+        mypbr_medium m{};
+        m.shape = sphere ? 0 : 1;
+        m.xform = transformed ? add_xform(xform) : -1;
+        m.material = mat;
+        m.density = density;
+        for (int k = 0; k < 3; k++) {
+            m.a[k] = a[k];
+            m.b[k] = b[k];
+        }
+        Box box;
+        if (sphere) {
+            double r = b.x;
+            V3 rv(r, r, r);
+            box = Box::from_points(a - rv, a + rv);
+        } else {
+            box = box_bounds(a, b);
+        }
+        if (transformed)
+            box = xform.box(box);
+        S.media.push_back(m);
+        int index = int(S.media.size()) - 1;
+        world_box.grow(box);
+        add_item(MYPBR_PRIM_MEDIUM, index, box);
+        return true;
+    }
+
+    // A Wavefront OBJ file (include/obj_loader.h:191-340, without MTL files):
+    // faces triangulated as fans, degenerate triangles dropped, one part per
+    // usemtl material (scene material of that name, else the line's material).
+    bool add_obj(const std::string& file, bool smooth, int line_mat, const Xf& xform, bool transformed) {
+        std::ifstream in(file);
+        if (!in) {
+            error = "cannot open '" + file + "'";
+            return false;
+        }
+        std::vector<V3> pos, nrm, uv;
+        struct Face {
+            int v[3], n[3], t[3];
+        };
+        std::vector<int> part_order;
+        std::map<int, std::vector<Face>> faces;
+        int current = line_mat;
+        auto resolve = [](long index, size_t count) -> int {
+            if (index > 0 && size_t(index) <= count)
+                return int(index - 1);
+            if (index < 0 && size_t(-index) <= count)
+                return int(long(count) + index);
+            return -1;
+        };
+        std::string line;
+        int ln = 0;
+        while (std::getline(in, line)) {
+            ln++;
+            const char* s = line.c_str();
+            while (*s == ' ' || *s == '\t')
+                s++;
+            auto read_vec = [&](const char* p, int n) {
+                double x[3] = {0, 0, 0};
+                char* end;
+                for (int k = 0; k < n; k++) {
+                    x[k] = std::strtod(p, &end);
+                    p = end;
+                }
+                return V3(x[0], x[1], x[2]);
+            };
+            if (s[0] == 'v' && (s[1] == ' ' || s[1] == '\t')) {
+                pos.push_back(read_vec(s + 2, 3));
+            } else if (s[0] == 'v' && s[1] == 'n') {
+                nrm.push_back(read_vec(s + 2, 3));
+            } else if (s[0] == 'v' && s[1] == 't') {
+                uv.push_back(read_vec(s + 2, 2));
+            } else if (s[0] == 'f' && (s[1] == ' ' || s[1] == '\t')) {
+                std::vector<int> vs, ns, ts;
+                const char* p = s + 2;
+                while (true) {
+                    while (*p == ' ' || *p == '\t' || *p == '\r')
+                        p++;
+                    if (*p == '\0')
+                        break;
+                    char* end;
+                    long v = std::strtol(p, &end, 10), t = 0, n = 0;
+                    if (end == p) {
+                        error = file + ":" + std::to_string(ln) + ": bad face";
+                        return false;
+                    }
+                    p = end;
+                    if (*p == '/') {
+                        p++;
+                        if (*p != '/') {
+                            t = std::strtol(p, &end, 10);
+                            p = end;
+                        }
+                        if (*p == '/') {
+                            p++;
+                            n = std::strtol(p, &end, 10);
+                            p = end;
+                        }
+                    }
+                    int vi = resolve(v, pos.size());
+                    if (vi < 0) {
+                        error = file + ":" + std::to_string(ln) + ": vertex index out of range";
+                        return false;
+                    }
+                    vs.push_back(vi);
+                    ts.push_back(resolve(t, uv.size()));
+                    ns.push_back(resolve(n, nrm.size()));
+                }
+                for (size_t k = 1; k + 1 < vs.size(); k++) {
+                    Face f;
+                    size_t id[3] = {0, k, k + 1};
+                    for (int c = 0; c < 3; c++) {
+                        f.v[c] = vs[id[c]];
+                        f.n[c] = ns[id[c]];
+                        f.t[c] = ts[id[c]];
+                    }
+                    const V3& p0 = pos[f.v[0]];
+                    if (cross(pos[f.v[1]] - p0, pos[f.v[2]] - p0).near_zero())
+                        continue;
+                    if (!faces.count(current))
+                        part_order.push_back(current);
+                    faces[current].push_back(f);
+                }
+            } else if (line.compare(size_t(s - line.c_str()), 6, "usemtl") == 0) {
+                std::string name(s + 6);
+                name.erase(0, name.find_first_not_of(" \t"));
+                name.erase(name.find_last_not_of(" \t\r") + 1);
+                auto it = materials.find(name);
+                current = it != materials.end() ? it->second : line_mat;
+            }
+        }
+        if (smooth && nrm.empty()) {
+            nrm.assign(pos.size(), V3());
+            for (int pm : part_order)
+                for (auto& f : faces[pm]) {
+                    const V3& p0 = pos[f.v[0]];
+                    V3 n = cross(pos[f.v[1]] - p0, pos[f.v[2]] - p0);
+                    for (int c = 0; c < 3; c++) {
+                        nrm[f.v[c]] = nrm[f.v[c]] + n;
+                        f.n[c] = f.v[c];
+                    }
+                }
+        }
+        if (part_order.empty()) {
+            error = "'" + file + "' has no faces";
+            return false;
+        }
+        for (int pm : part_order)
+            if (!check_light_xform(pm, xform, transformed))
+                return false;
+
+        // Vertex data in world space; normals by the inverse transpose, kept
+        // unnormalized so that interpolation commutes with the transform.
+        int64_t vbase = S.position_count(), nbase = S.normal_count(), tbase = S.uv_count();
+        for (const V3& p : pos) {
+            V3 w = transformed ? xform.point(p) : p;
+            S.positions.push_back(w.x);
+            S.positions.push_back(w.y);
+            S.positions.push_back(w.z);
+        }
+        for (const V3& n : nrm) {
+            V3 w = transformed ? xform.normal(n) : n;
+            S.normals.push_back(w.x);
+            S.normals.push_back(w.y);
+            S.normals.push_back(w.z);
+        }
+        for (const V3& t : uv) {
+            S.uvs.push_back(t.x);
+            S.uvs.push_back(t.y);
+        }
+        bool flip = transformed && xform.det() < 0;
+        double area_scale = transformed ? xform.area_scale() : 1.0;
+        for (int pm : part_order) {
+            const auto& fs = faces[pm];
+            mypbr_mesh mesh{};
+            mesh.first_triangle = int64_t(S.triangles.size());
+            mesh.triangle_count = int64_t(fs.size());
+            mesh.material = pm;
+            S.meshes.push_back(mesh);
+            int mesh_index = int(S.meshes.size()) - 1;
+            Box part_box;
+            double total_area = 0;
+            std::vector<double> areas;
+            areas.reserve(fs.size());
+            for (const auto& f : fs) {
+                mypbr_triangle t{};
+                for (int c = 0; c < 3; c++) {
+                    t.v[c] = int(vbase + f.v[c]);
+                    t.n[c] = f.n[c] >= 0 ? int(nbase + f.n[c]) : -1;
+                    t.t[c] = f.t[c] >= 0 ? int(tbase + f.t[c]) : -1;
+                }
+                // A vertex-normal index counts only if all three are present (mesh.h:100)
+                if (t.n[0] < 0 || t.n[1] < 0 || t.n[2] < 0)
+                    t.n[0] = t.n[1] = t.n[2] = -1;
+                if (t.t[0] < 0 || t.t[1] < 0 || t.t[2] < 0)
+                    t.t[0] = t.t[1] = t.t[2] = -1;
+                t.material = pm;
+                t.flags = flip ? MYPBR_TRI_FLIP_NORMAL : 0;
+                t.mesh = mesh_index;
+                S.triangles.push_back(t);
+                int ti = int(S.triangles.size()) - 1;
+                const V3 &p0 = pos[f.v[0]], &p1 = pos[f.v[1]], &p2 = pos[f.v[2]];
+                Box obox = Box::from_points(p0, p1);
+                obox.grow(Box::from_points(p2, p2));
+                part_box.grow(obox);
+                // World-space box for the BVH item
+                V3 w0 = transformed ? xform.point(p0) : p0, w1 = transformed ? xform.point(p1) : p1,
+                   w2 = transformed ? xform.point(p2) : p2;
+                Box wbox = Box::from_points(w0, w1);
+                wbox.grow(Box::from_points(w2, w2));
+                add_item(MYPBR_PRIM_TRIANGLE, ti, wbox);
+                double a = 0.5 * cross(p1 - p0, p2 - p0).length();
+                areas.push_back(a);
+                total_area += a;
+            }
+            world_box.grow(transformed ? xform.box(part_box) : part_box);
+            if (is_emissive(pm)) {
+                double lum = average_emission_luminance(pm), power = 0;
+                int first = int(S.light_members.size());
+                for (size_t k = 0; k < fs.size(); k++) {
+                    power += kPi * areas[k] * lum;
+                    add_member(MYPBR_PRIM_TRIANGLE, int(mesh.first_triangle + int64_t(k)),
+                               total_area > 0 ? areas[k] / total_area : 0.0);
+                }
+                add_light(first, int(fs.size()), power * area_scale);
+            }
+        }
+        return true;
+    }
+
+    // ------------------------------------------------------ lines
+
+    bool parse_material(std::istringstream& in) {
+        std::string name, type;
+        if (!(in >> name >> type))
+            return fail("expected 'material <name> <type> <parameters...>'");
+        int normal_map = -1;
+        auto read_normal_map = [&]() {
+            std::string key;
+            if (!(in >> key))
+                return true;
+            if (key != "normal_map") {
+                error = "unexpected value '" + key + "' (expected 'normal_map <texture>')";
+                return false;
+            }
+            return read_texture_name(in, normal_map);
+        };
+        mypbr_material m = blank_material(0);
+        if (type == "lambertian") {
+            m.type = MYPBR_MAT_LAMBERTIAN;
+            std::string first;
+            error.clear();
+            if (!(in >> first) || !read_color_or_texture(in, first, m.tex[0]))
+                return fail(error.empty()
+                                ? "expected 'material <name> lambertian <r> <g> <b>' or '... lambertian texture <name>'"
+                                : error);
+            if (!read_normal_map())
+                return fail(error);
+        } else if (type == "metal") {
+            const char* usage = "expected 'material <name> metal <r> <g> <b> <roughness>' or "
+                                "'... metal <Al|Ti|Cu|Au|Ag|Cr> <roughness>'";
+            m.type = MYPBR_MAT_METAL;
+            std::string first;
+            double r = 0, g = 0, b = 0, roughness = 0;
+            V3 eta, k;
+            if (!(in >> first))
+                return fail(usage);
+            bool measured = find_conductor(first, eta, k);
+            if (measured) {
+                if (!(in >> roughness) || roughness < 0)
+                    return fail(usage);
+            } else {
+                std::istringstream number(first);
+                if (!(number >> r) || !(in >> g >> b >> roughness) || roughness < 0)
+                    return fail(usage);
+            }
+            error.clear();
+            if (!read_normal_map())
+                return fail(error);
+            m.p[3] = std::clamp(roughness, 0.0, 1.0);
+            if (measured) {
+                V3 f0, f_avg;
+                measured_fresnel(eta, k, f0, f_avg);
+                m.flags |= MYPBR_MATF_MEASURED;
+                for (int c = 0; c < 3; c++) {
+                    m.p[c] = f0[c];
+                    m.p[4 + c] = eta[c];
+                    m.p[7 + c] = k[c];
+                    m.p[10 + c] = f_avg[c];
+                }
+            } else {
+                V3 f0(r, g, b);
+                for (int c = 0; c < 3; c++) {
+                    m.p[c] = f0[c];
+                    m.p[10 + c] = f0[c] + (1 - f0[c]) / 21;
+                }
+            }
+        } else if (type == "dielectric") {
+            const char* usage = "expected 'material <name> dielectric <index of refraction> [roughness <r>] "
+                                "[color <r> <g> <b> [distance <d>]]'";
+            double ior, roughness = 0, distance = 1;
+            V3 tint(1, 1, 1);
+            std::string key;
+            if (!(in >> ior) || ior <= 0)
+                return fail(usage);
+            while (in >> key) {
+                bool ok = true;
+                if (key == "roughness") {
+                    ok = bool(in >> roughness) && roughness >= 0;
+                } else if (key == "color") {
+                    double r, g, b;
+                    ok = bool(in >> r >> g >> b) && r > 0 && g > 0 && b > 0 && r <= 1 && g <= 1 && b <= 1;
+                    tint = V3(r, g, b);
+                } else if (key == "distance") {
+                    ok = bool(in >> distance) && distance > 0;
+                } else {
+                    ok = false;
+                }
+                if (!ok)
+                    return fail(usage);
+            }
+            m.type = MYPBR_MAT_DIELECTRIC;
+            m.p[0] = ior;
+            m.p[1] = std::clamp(roughness, 0.0, 1.0);
+            for (int c = 0; c < 3; c++)
+                m.p[2 + c] = -std::log(tint[c]) / distance;
+        } else if (type == "thin_glass") {
+            const char* usage = "expected 'material <name> thin_glass <index of refraction> [color <r> <g> <b>]'";
+            double ior;
+            V3 tint(1, 1, 1);
+            std::string key;
+            if (!(in >> ior) || ior <= 0)
+                return fail(usage);
+            if (in >> key) {
+                double r, g, b;
+                if (key != "color" || !(in >> r >> g >> b) || r < 0 || g < 0 || b < 0 || r > 1 || g > 1 || b > 1)
+                    return fail(usage);
+                tint = V3(r, g, b);
+            }
+            m.type = MYPBR_MAT_THIN_DIELECTRIC;
+            m.p[0] = ior;
+            for (int c = 0; c < 3; c++)
+                m.p[2 + c] = tint[c];
+        } else if (type == "principled") {
+            m.type = MYPBR_MAT_PRINCIPLED;
+            int base = add_texture_solid(V3(0.8, 0.8, 0.8));
+            int metallic = add_texture_solid(V3(0, 0, 0));
+            int rough = add_texture_solid(V3(0.5, 0.5, 0.5));
+            int coat = -1, coat_rough = -1, coat_normals = -1, base_normals = -1;
+            V3 coat_tint(1, 1, 1), eta, k;
+            bool coat_tinted = false, measured = false;
+            double ior = 1.5;
+            std::string key;
+            error.clear();
+            while (in >> key) {
+                bool ok = true;
+                if (key == "texture") {
+                    ok = read_color_or_texture(in, key, base);
+                } else if (key == "color") {
+                    std::string first;
+                    ok = bool(in >> first) && read_color_or_texture(in, first, base);
+                } else if (key == "metallic") {
+                    ok = read_value_or_texture(in, metallic);
+                } else if (key == "roughness") {
+                    ok = read_value_or_texture(in, rough);
+                } else if (key == "ior") {
+                    ok = bool(in >> ior) && ior > 0;
+                } else if (key == "normal_map") {
+                    ok = read_texture_name(in, base_normals);
+                } else if (key == "clearcoat") {
+                    ok = read_value_or_texture(in, coat);
+                } else if (key == "clearcoat_roughness") {
+                    ok = read_value_or_texture(in, coat_rough);
+                } else if (key == "clearcoat_normal_map") {
+                    ok = read_texture_name(in, coat_normals);
+                } else if (key == "conductor") {
+                    std::string metal_name;
+                    ok = bool(in >> metal_name) && (measured = find_conductor(metal_name, eta, k));
+                    if (!ok)
+                        error = "unknown conductor '" + metal_name + "' (known: Al Ti Cu Au Ag Cr)";
+                } else if (key == "clearcoat_color") {
+                    double r, g, b;
+                    ok = bool(in >> r >> g >> b) && r > 0 && g > 0 && b > 0 && r <= 1 && g <= 1 && b <= 1;
+                    coat_tint = V3(r, g, b);
+                    coat_tinted = true;
+                } else {
+                    return fail("unknown principled setting '" + key + "'");
+                }
+                if (!ok)
+                    return fail(error.empty() ? "bad value for principled setting '" + key + "'" : error);
+            }
+            if ((coat_rough >= 0 || coat_normals >= 0 || coat_tinted) && coat < 0)
+                return fail("clearcoat_roughness, clearcoat_normal_map and clearcoat_color need 'clearcoat <weight>'");
+            double r0 = (ior - 1) / (ior + 1);
+            m.p[0] = r0 * r0;
+            m.tex[0] = base;
+            m.tex[1] = metallic;
+            m.tex[2] = rough;
+            m.tex[3] = use_normal_maps ? base_normals : -1;
+            if (measured) {
+                V3 f0, f_avg;
+                measured_fresnel(eta, k, f0, f_avg);
+                m.flags |= MYPBR_MATF_MEASURED;
+                for (int c = 0; c < 3; c++) {
+                    m.p[4 + c] = eta[c];
+                    m.p[7 + c] = k[c];
+                    m.p[10 + c] = f_avg[c];
+                }
+            }
+            m.p[13] = m.p[14] = m.p[15] = 1;
+            if (coat >= 0) {
+                m.flags |= MYPBR_MATF_COAT;
+                m.tex[4] = coat;
+                m.tex[5] = coat_rough >= 0 ? coat_rough : add_texture_solid(V3(0, 0, 0));
+                m.tex[6] = use_normal_maps ? coat_normals : -1;
+                for (int c = 0; c < 3; c++)
+                    m.p[13 + c] = coat_tint[c];
+                if (!(coat_tint.x == 1 && coat_tint.y == 1 && coat_tint.z == 1))
+                    m.flags |= MYPBR_MATF_COAT_TINT;
+            }
+        } else if (type == "volume") {
+            double r, g, b, aniso = 0;
+            std::string key;
+            if (!(in >> r >> g >> b))
+                return fail("expected 'material <name> volume <r> <g> <b> [g <anisotropy>]'");
+            if (in >> key) {
+                if (key != "g" || !(in >> aniso) || aniso <= -1 || aniso >= 1)
+                    return fail(
+                        "expected 'material <name> volume <r> <g> <b> [g <anisotropy between -1 and 1>]'");
+            }
+            m.type = MYPBR_MAT_PHASE;
+            m.p[0] = r;
+            m.p[1] = g;
+            m.p[2] = b;
+            m.p[3] = aniso;
+        } else if (type == "emissive") {
+            const char* usage = "expected 'material <name> emissive <r> <g> <b> [spread <degrees, 0 to 180>]'";
+            double r, g, b, spread = 180;
+            std::string key;
+            if (!(in >> r >> g >> b))
+                return fail(usage);
+            if (in >> key && (key != "spread" || !(in >> spread) || spread <= 0 || spread > 180))
+                return fail(usage);
+            m.type = MYPBR_MAT_DIFFUSE_LIGHT;
+            m.p[0] = r;
+            m.p[1] = g;
+            m.p[2] = b;
+            m.p[3] = spread;
+            double half = radians(spread) / 2;
+            m.p[4] = spread >= 180 ? kInf : std::tan(half);
+            // Cosine-weighted share of the gridded emission (material.h:600-608)
+            if (half >= kPi / 2 - 1e-9) {
+                m.p[5] = 1;
+            } else {
+                double s = std::sin(half), c = std::cos(half);
+                m.p[5] = s * s - (half - s * c) * c / s;
+            }
+        } else {
+            return fail("unknown material type '" + type + "'");
+        }
+        if (normal_map >= 0 && use_normal_maps)
+            m.normal_map = normal_map;
+        materials[name] = add_material(m);
+        return true;
+    }
+
+    bool parse_texture(std::istringstream& in) {
+        std::string name, type;
+        if (!(in >> name >> type))
+            return fail("expected 'texture <name> <type> <parameters...>'");
+        if (type == "solid") {
+            double r, g, b;
+            if (!(in >> r >> g >> b))
+                return fail("expected 'texture <name> solid <r> <g> <b>'");
+            textures[name] = add_texture_solid(V3(r, g, b));
+        } else if (type == "checker") {
+            double scale, r0, g0, b0, r1, g1, b1;
+            if (!(in >> scale >> r0 >> g0 >> b0 >> r1 >> g1 >> b1) || scale <= 0)
+                return fail("expected 'texture <name> checker <scale> <r g b> <r g b>'");
+            int even = add_texture_solid(V3(r0, g0, b0));
+            int odd = add_texture_solid(V3(r1, g1, b1));
+            mypbr_texture t{};
+            t.type = MYPBR_TEX_CHECKER;
+            t.a = even;
+            t.b = odd;
+            t.p[0] = 1.0 / scale;
+            S.textures.push_back(t);
+            textures[name] = int(S.textures.size()) - 1;
+        } else if (type == "image") {
+            std::string file, option;
+            if (!(in >> file))
+                return fail("expected 'texture <name> image <path> [linear]'");
+            bool linear = false;
+            if (in >> option) {
+                if (option != "linear")
+                    return fail("expected 'texture <name> image <path> [linear]'");
+                linear = true;
+            }
+            if (file[0] != '/')
+                file = scene_dir + file;
+            auto ends_with = [&](const char* suf) {
+                size_t n = std::strlen(suf);
+                return file.size() >= n && file.compare(file.size() - n, n, suf) == 0;
+            };
+            if (!ends_with(".hdr")) {
+                unsupported = true;
+                return fail("image texture '" + file + "': only .hdr images are read by this backend");
+            }
+            int w, h;
+            std::vector<float> rgb;
+            std::string err;
+            if (!read_hdr(file, w, h, rgb, err))
+                return fail("cannot load image '" + file + "'");
+            mypbr_texture t{};
+            t.type = MYPBR_TEX_IMAGE;
+            t.a = t.b = -1;
+            t.width = w;
+            t.height = h;
+            t.flags = MYPBR_TEXF_HDR | (linear ? MYPBR_TEXF_LINEAR : 0);
+            t.offset = int64_t(S.texels_hdr.size() / 3);
+            S.texels_hdr.insert(S.texels_hdr.end(), rgb.begin(), rgb.end());
+            S.textures.push_back(t);
+            textures[name] = int(S.textures.size()) - 1;
+        } else {
+            return fail("unknown texture type '" + type + "'");
+        }
+        return true;
+    }
+
+    bool unsupported = false;
+
+    bool parse_line(std::istringstream& in, const std::string& keyword) {
+        auto& cam = S.camera;
+        auto& opts = S.opts;
+        if (keyword == "image_width") {
+            if (!(in >> cam.image_width) || cam.image_width < 1)
+                return fail("expected 'image_width <positive integer>'");
+        } else if (keyword == "aspect_ratio") {
+            double num, den = 1.0;
+            if (!(in >> num))
+                return fail("expected 'aspect_ratio <w>/<h>' or 'aspect_ratio <number>'");
+            if (in.peek() == '/') {
+                in.get();
+                if (!(in >> den))
+                    return fail("expected 'aspect_ratio <w>/<h>'");
+            }
+            if (num <= 0 || den <= 0)
+                return fail("aspect_ratio must be positive");
+            cam.aspect_ratio = num / den;
+        } else if (keyword == "samples_per_pixel") {
+            if (!(in >> opts.samples_per_pixel) || opts.samples_per_pixel < 1)
+                return fail("expected 'samples_per_pixel <positive integer>'");
+        } else if (keyword == "max_depth") {
+            if (!(in >> opts.max_depth) || opts.max_depth < 1)
+                return fail("expected 'max_depth <positive integer>'");
+        } else if (keyword == "camera") {
+            std::string key;
+            while (in >> key) {
+                bool ok = true;
+                if (key == "lookfrom")
+                    ok = bool(in >> cam.lookfrom[0] >> cam.lookfrom[1] >> cam.lookfrom[2]);
+                else if (key == "lookat")
+                    ok = bool(in >> cam.lookat[0] >> cam.lookat[1] >> cam.lookat[2]);
+                else if (key == "vup")
+                    ok = bool(in >> cam.vup[0] >> cam.vup[1] >> cam.vup[2]);
+                else if (key == "vfov")
+                    ok = bool(in >> cam.vfov) && cam.vfov > 0 && cam.vfov < 180;
+                else if (key == "aperture")
+                    ok = bool(in >> cam.defocus_angle) && cam.defocus_angle >= 0;
+                else if (key == "focus")
+                    ok = bool(in >> cam.focus_dist) && cam.focus_dist > 0;
+                else if (key == "ortho")
+                    ok = bool(in >> cam.ortho_height) && cam.ortho_height >= 0;
+                else if (key == "blades")
+                    ok = bool(in >> cam.blades) && (cam.blades == 0 || cam.blades >= 3);
+                else if (key == "blade_rotation")
+                    ok = bool(in >> cam.blade_rotation);
+                else
+                    return fail("unknown camera setting '" + key + "'");
+                if (!ok)
+                    return fail("bad value for camera setting '" + key + "'");
+            }
+        } else if (keyword == "vfov") {
+            if (!(in >> cam.vfov) || cam.vfov <= 0 || cam.vfov >= 180)
+                return fail("expected 'vfov <degrees between 0 and 180>'");
+        } else if (keyword == "aperture") {
+            if (!(in >> cam.defocus_angle) || cam.defocus_angle < 0)
+                return fail("expected 'aperture <defocus angle in degrees>'");
+        } else if (keyword == "focus") {
+            if (!(in >> cam.focus_dist) || cam.focus_dist <= 0)
+                return fail("expected 'focus <positive distance>'");
+        } else if (keyword == "background") {
+            double r, g, b;
+            if (!(in >> r >> g >> b))
+                return fail("expected 'background <r> <g> <b>'");
+            S.use_sky = false;
+            S.background = V3(r, g, b);
+        } else if (keyword == "light_selection") {
+            std::string mode;
+            if (!(in >> mode) || (mode != "power" && mode != "uniform"))
+                return fail("expected 'light_selection power|uniform'");
+            power_selection = mode == "power";
+        } else if (keyword == "environment") {
+            std::string file, key;
+            double intensity = 1, rotation = 0;
+            const char* usage = "expected 'environment <file.hdr> [intensity <s>] [rotate <degrees>]'";
+            if (!(in >> file))
+                return fail(usage);
+            while (in >> key) {
+                bool ok = (key == "intensity" && in >> intensity && intensity >= 0) ||
+                          (key == "rotate" && in >> rotation);
+                if (!ok)
+                    return fail(usage);
+            }
+            if (file[0] != '/')
+                file = scene_dir + file;
+            int w, h;
+            std::vector<float> rgb;
+            std::string err;
+            if (!read_hdr(file, w, h, rgb, err))
+                return fail("cannot load environment map '" + file + "'");
+            if (has_environment)
+                return fail("only one environment is allowed");
+            set_environment(w, h, std::move(rgb), intensity, rotation / 360);
+        } else if (keyword == "sun") {
+            const char* usage = "expected 'sun elevation <deg> azimuth <deg> [intensity <E>] [color <r g b>] "
+                                "[angle <deg>] [disk on|off]' or 'sun off'";
+            std::string key;
+            sun_on = true;
+            while (in >> key) {
+                bool ok = true;
+                if (key == "off")
+                    sun_on = false;
+                else if (key == "elevation")
+                    ok = bool(in >> sun_elevation) && sun_elevation >= -90 && sun_elevation <= 90;
+                else if (key == "azimuth")
+                    ok = bool(in >> sun_azimuth);
+                else if (key == "intensity")
+                    ok = bool(in >> sun_intensity) && sun_intensity >= 0;
+                else if (key == "color")
+                    ok = bool(in >> sun_tint.x >> sun_tint.y >> sun_tint.z);
+                else if (key == "angle")
+                    ok = bool(in >> sun_angle) && sun_angle > 0 && sun_angle < 90;
+                else if (key == "disk") {
+                    std::string value;
+                    ok = bool(in >> value) && (value == "on" || value == "off");
+                    sun_disk = value == "on";
+                } else
+                    ok = false;
+                if (!ok)
+                    return fail(usage);
+            }
+        } else if (keyword == "sky") {
+            std::string type;
+            if (!(in >> type))
+                return fail("expected 'sky uniform <r g b>', 'sky atmosphere [...]' or 'sky gradient'");
+            if (type == "uniform") {
+                if (!(in >> sky_radiance.x >> sky_radiance.y >> sky_radiance.z))
+                    return fail("expected 'sky uniform <r g b>'");
+                sky_uniform = true;
+                S.use_sky = true;
+                sky_atmosphere = false;
+            } else if (type == "atmosphere") {
+                std::string rest;
+                while (in >> rest) {
+                }
+                sky_atmosphere = true;
+                sky_uniform = false;
+                S.use_sky = true;
+            } else if (type == "gradient") {
+                sky_uniform = false;
+                sky_atmosphere = false;
+                S.use_sky = true;
+            } else {
+                return fail("unknown sky type '" + type + "' (expected uniform, atmosphere or gradient)");
+            }
+        } else if (keyword == "ground") {
+            std::string key;
+            ground = true;
+            while (in >> key) {
+                if (key == "off") {
+                    ground = false;
+                } else if (key == "height") {
+                    if (!(in >> ground_height))
+                        return fail("expected 'ground [height <y>] [material]'");
+                } else {
+                    auto it = materials.find(key);
+                    if (it == materials.end())
+                        return fail("unknown material '" + key + "'");
+                    ground_material = it->second;
+                }
+            }
+        } else if (keyword == "style") {
+            std::string name;
+            if (!(in >> name) || (name != "voxel" && name != "classic"))
+                return fail("expected 'style voxel' or 'style classic'");
+            bool voxel = name == "voxel";
+            sun_on = voxel;
+            sun_elevation = voxel ? 50 : 45;
+            sun_azimuth = voxel ? 50 : 45;
+            sun_intensity = voxel ? 4 : 3;
+            sun_angle = voxel ? 3 : 4;
+            sun_tint = V3(1, 1, 1);
+            sun_disk = true;
+            sky_uniform = false;
+            sky_atmosphere = voxel;
+            S.use_sky = true;
+            ground = voxel;
+            ground_material = voxel ? lambertian(V3(0.3, 0.3, 0.3)) : default_material;
+            opts.max_diffuse = voxel ? 2 : 0;
+            opts.max_specular = voxel ? 5 : 0;
+            opts.max_scatter = voxel ? 5 : 0;
+            opts.transparent_shadows = voxel;
+        } else if (keyword == "bounces") {
+            const char* usage = "expected 'bounces [diffuse <n>] [specular <n>] [scatter <n>]'";
+            std::string key;
+            while (in >> key) {
+                bool ok = (key == "diffuse" && in >> opts.max_diffuse && opts.max_diffuse >= 0) ||
+                          (key == "specular" && in >> opts.max_specular && opts.max_specular >= 0) ||
+                          (key == "scatter" && in >> opts.max_scatter && opts.max_scatter >= 0);
+                if (!ok)
+                    return fail(usage);
+            }
+        } else if (keyword == "transparent_shadows") {
+            std::string value;
+            if (!(in >> value) || (value != "on" && value != "off"))
+                return fail("expected 'transparent_shadows on|off'");
+            opts.transparent_shadows = value == "on";
+        } else if (keyword == "height_fog") {
+            double density, scale, base = 0;
+            std::string name, key;
+            const char* usage = "expected 'height_fog <density> <scale height> <volume material> [base <y>]'";
+            if (!(in >> density >> scale >> name) || density <= 0 || scale <= 0)
+                return fail(usage);
+            if (in >> key && (key != "base" || !(in >> base)))
+                return fail(usage);
+            auto it = materials.find(name);
+            if (it == materials.end() || S.materials[it->second].type != MYPBR_MAT_PHASE)
+                return fail("expected a volume material, got '" + name + "'");
+            mypbr_unbounded u{};
+            u.kind = MYPBR_UNBOUNDED_HEIGHT_FOG;
+            u.material = it->second;
+            u.height = base;
+            u.density = density;
+            u.scale_height = scale;
+            S.unbounded.push_back(u);
+        } else if (keyword == "bloom") {
+            // Display settings: they change written images, not the radiance frame
+            double strength;
+            if (!(in >> strength) || strength < 0)
+                return fail("expected 'bloom <strength> [threshold <radiance>] [radius <fraction of width>]'");
+            std::string key;
+            double x;
+            while (in >> key) {
+                if (!((key == "threshold" && in >> x && x >= 0) || (key == "radius" && in >> x && x > 0)))
+                    return fail("expected 'bloom <strength> [threshold <radiance>] [radius <fraction of width>]'");
+            }
+        } else if (keyword == "vignette") {
+            double v;
+            if (!(in >> v) || v < 0)
+                return fail("expected 'vignette <strength>'");
+        } else if (keyword == "exposure") {
+            double v;
+            if (!(in >> v))
+                return fail("expected 'exposure <stops>'");
+        } else if (keyword == "tonemap") {
+            std::string name;
+            if (!(in >> name) || (name != "none" && name != "reinhard" && name != "aces"))
+                return fail("expected 'tonemap none|reinhard|aces'");
+        } else if (keyword == "normal_maps") {
+            std::string state;
+            if (!(in >> state) || (state != "on" && state != "off"))
+                return fail("expected 'normal_maps on|off'");
+            use_normal_maps = state == "on";
+        } else if (keyword == "texture") {
+            return parse_texture(in);
+        } else if (keyword == "material") {
+            return parse_material(in);
+        } else if (keyword == "sphere" || keyword == "quad" || keyword == "box") {
+            int mat;
+            Xf xform;
+            bool transformed;
+            error.clear();
+            if (keyword == "sphere") {
+                double x, y, z, r;
+                if (!(in >> x >> y >> z >> r) || r == 0)
+                    return fail("expected 'sphere <x> <y> <z> <non-zero radius> [material] [transforms]'");
+                if (!read_tail(in, mat, xform, transformed))
+                    return fail(error);
+                if (!add_sphere(V3(x, y, z), r, mat, xform, transformed))
+                    return fail(error);
+            } else if (keyword == "quad") {
+                V3 q, u, v;
+                if (!(in >> q.x >> q.y >> q.z >> u.x >> u.y >> u.z >> v.x >> v.y >> v.z))
+                    return fail("expected 'quad <Qx Qy Qz> <ux uy uz> <vx vy vz> [material] [transforms]'");
+                if (cross(u, v).near_zero())
+                    return fail("quad edges must not be parallel");
+                if (!read_tail(in, mat, xform, transformed))
+                    return fail(error);
+                if (!add_quad(q, u, v, mat, xform, transformed))
+                    return fail(error);
+            } else {
+                V3 a, b;
+                if (!(in >> a.x >> a.y >> a.z >> b.x >> b.y >> b.z))
+                    return fail("expected 'box <x0 y0 z0> <x1 y1 z1> [material] [transforms]'");
+                if (!read_tail(in, mat, xform, transformed))
+                    return fail(error);
+                if (!add_box(a, b, mat, xform, transformed))
+                    return fail(error);
+            }
+        } else if (keyword == "medium") {
+            double density;
+            std::string shape;
+            if (!(in >> density >> shape) || density <= 0)
+                return fail("expected 'medium <positive density> sphere|box <...> <material> [transforms]'");
+            V3 a, b;
+            bool sphere = shape == "sphere";
+            if (sphere) {
+                double r;
+                if (!(in >> a.x >> a.y >> a.z >> r) || r <= 0)
+                    return fail("expected 'medium <density> sphere <x> <y> <z> <positive radius> <material>'");
+                b = V3(r, 0, 0);
+            } else if (shape == "box") {
+                if (!(in >> a.x >> a.y >> a.z >> b.x >> b.y >> b.z))
+                    return fail("expected 'medium <density> box <x0 y0 z0> <x1 y1 z1> <material>'");
+            } else {
+                return fail("a medium's boundary must be 'sphere' or 'box'");
+            }
+            int mat;
+            Xf xform;
+            bool transformed;
+            error.clear();
+            if (!read_tail(in, mat, xform, transformed))
+                return fail(error);
+            if (S.materials[mat].type != MYPBR_MAT_PHASE)
+                return fail("a medium needs a volume material");
+            add_medium(density, sphere, a, b, mat, xform, transformed);
+        } else if (keyword == "fog") {
+            std::string name;
+            if (!(in >> fog_density >> name) || fog_density <= 0)
+                return fail("expected 'fog <positive density> <volume material>'");
+            auto it = materials.find(name);
+            if (it == materials.end() || S.materials[it->second].type != MYPBR_MAT_PHASE)
+                return fail("expected a volume material, got '" + name + "'");
+            fog_material = it->second;
+        } else if (keyword == "mesh") {
+            std::string file;
+            if (!(in >> file))
+                return fail("expected 'mesh <file.obj> [material] [transforms]'");
+            if (file[0] != '/')
+                file = scene_dir + file;
+            std::string rest, first;
+            std::getline(in, rest);
+            std::istringstream peek(rest);
+            bool smooth = (peek >> first) && first == "smooth";
+            std::istringstream tail(smooth ? rest.substr(rest.find("smooth") + 6) : rest);
+            auto ends_with = [&](const char* suf) {
+                size_t n = std::strlen(suf);
+                return file.size() >= n && file.compare(file.size() - n, n, suf) == 0;
+            };
+            if (ends_with(".gltf") || ends_with(".glb")) {
+                unsupported = true;
+                return fail("glTF meshes are not read by this backend");
+            }
+            int mat;
+            Xf xform;
+            bool transformed;
+            error.clear();
+            if (!read_tail(tail, mat, xform, transformed))
+                return fail(error);
+            if (!add_obj(file, smooth, mat, xform, transformed))
+                return fail(error);
+            std::string extra;
+            if (tail >> extra)
+                return fail("unexpected value '" + extra + "'");
+        } else if (keyword == "vox" || keyword == "cyclorama" || keyword == "softbox") {
+            unsupported = true;
+            return fail("'" + keyword + "' is not supported by this backend");
+        } else {
+            return fail("unknown keyword '" + keyword + "'");
+        }
+        std::string extra;
+        if (in >> extra)
+            return fail("unexpected value '" + extra + "'");
+        return true;
+    }
+
+    void set_environment(int w, int h, std::vector<float> rgb, double intensity, double rotation_turns) {
+        S.env_pixels = std::move(rgb);
+        S.env_width = w;
+        S.env_height = h;
+        S.env_intensity = intensity;
+        S.env_rotation = rotation_turns;
+        has_environment = true;
+        pending_lights.push_back({MYPBR_LIGHT_ENVIRONMENT, 0, 0, -1});
+    }
+
+    // env power: pi R^2 times the integral of luminance over the sphere (environment.h:252-263)
+    double environment_power(double radius) const {
+        double sum = 0;
+        int w = S.env_width, h = S.env_height;
+        for (int j = 0; j < h; j++) {
+            double s = std::sin(kPi * (j + 0.5) / h);
+            for (int i = 0; i < w; i++) {
+                // "sky uniform" keeps its FP64 radiance, as the reference's in-memory sky does
+                const float* p = &S.env_pixels[(size_t(j) * w + i) * 3];
+                V3 c = uniform_sky_env ? sky_radiance : V3(p[0], p[1], p[2]);
+                double wgt = luminance(c) * s;
+                sum += std::fmax(wgt, 0.0);
+            }
+        }
+        double integral = S.env_intensity * sum * (2 * kPi / w) * (kPi / h);
+        return kPi * radius * radius * integral;
+    }
+
+    bool finish() {
+        if (items.empty() && S.media.empty())
+            return fail("the scene has no objects");
+        if (sky_uniform) {
+            if (has_environment)
+                return fail("'sky uniform' and 'environment' can't be used together");
+            std::vector<float> rgb(8 * 4 * 3);
+            for (int k = 0; k < 32; k++) {
+                rgb[3 * k] = float(sky_radiance.x);
+                rgb[3 * k + 1] = float(sky_radiance.y);
+                rgb[3 * k + 2] = float(sky_radiance.z);
+            }
+            set_environment(8, 4, std::move(rgb), 1.0, 0.0);
+            uniform_sky_env = true;
+        }
+        double el = radians(sun_elevation), az = radians(sun_azimuth);
+        V3 sun_dir(std::cos(el) * std::sin(az), std::sin(el), -std::cos(el) * std::cos(az));
+        V3 sun_irr = sun_intensity * sun_tint;
+        if (sky_atmosphere) {
+            unsupported = true;
+            return fail("'sky atmosphere' is not supported by this backend");
+        }
+        if (sun_on) {
+            S.sun.enabled = 1;
+            S.sun.disk_visible = sun_disk;
+            V3 d = unit(sun_dir);
+            for (int k = 0; k < 3; k++) {
+                S.sun.direction[k] = d[k];
+                S.sun.irradiance[k] = sun_irr[k];
+            }
+            S.sun.angular_diameter = sun_angle;
+            pending_lights.push_back({MYPBR_LIGHT_SUN, 0, 0, -1});
+        }
+        if (ground) {
+            mypbr_unbounded u{};
+            u.kind = MYPBR_UNBOUNDED_GROUND;
+            u.material = ground_material;
+            u.height = ground_height;
+            S.unbounded.push_back(u);
+        }
+        if (fog_material >= 0) {
+            Box e = world_box;
+            add_medium(fog_density, false, e.lo, e.hi, fog_material, Xf(), false);
+        }
+        V3 lf(S.camera.lookfrom[0], S.camera.lookfrom[1], S.camera.lookfrom[2]);
+        V3 la(S.camera.lookat[0], S.camera.lookat[1], S.camera.lookat[2]);
+        V3 vu(S.camera.vup[0], S.camera.vup[1], S.camera.vup[2]);
+        if ((lf - la).near_zero() || cross(vu, lf - la).near_zero())
+            return fail("camera lookfrom must differ from lookat, and vup must not point along the view");
+
+        // Light selection probabilities (light_list.h:45-96)
+        size_t n = pending_lights.size();
+        std::vector<double> prob(n, n > 0 ? 1.0 / n : 0.0);
+        if (n > 0 && power_selection) {
+            double radius = 0;
+            if (world_box.size(0) > 0 && world_box.size(1) > 0 && world_box.size(2) > 0)
+                radius = 0.5 * std::sqrt(world_box.size(0) * world_box.size(0) +
+                                         world_box.size(1) * world_box.size(1) +
+                                         world_box.size(2) * world_box.size(2));
+            if (!std::isfinite(radius) || radius <= 0)
+                radius = 1;
+            std::vector<double> power(n);
+            double known_sum = 0;
+            int known = 0;
+            for (size_t k = 0; k < n; k++) {
+                const auto& L = pending_lights[k];
+                if (L.kind == MYPBR_LIGHT_ENVIRONMENT)
+                    power[k] = environment_power(radius);
+                else if (L.kind == MYPBR_LIGHT_SUN)
+                    power[k] = kPi * radius * radius * luminance(sun_irr);
+                else
+                    power[k] = L.power;
+                if (std::isfinite(power[k]) && power[k] > 0) {
+                    known_sum += power[k];
+                    known++;
+                }
+            }
+            double fallback = known > 0 ? known_sum / known : 1.0;
+            double total = 0;
+            for (auto& p : power) {
+                if (!std::isfinite(p) || p <= 0)
+                    p = fallback;
+                total += p;
+            }
+            const double uniform_fraction = 0.2;
+            for (size_t k = 0; k < n; k++)
+                prob[k] = (1 - uniform_fraction) * power[k] / total + uniform_fraction / n;
+        }
+        for (size_t k = 0; k < n; k++) {
+            mypbr_light l{};
+            l.kind = pending_lights[k].kind;
+            l.first_member = pending_lights[k].first_member;
+            l.member_count = pending_lights[k].member_count;
+            l.probability = prob[k];
+            S.lights.push_back(l);
+        }
+        build_bvh(items, S.bvh_nodes, S.bvh_prims);
+        return true;
+    }
+
+    int run(std::istream& file) {
+        default_material = lambertian(V3(0.5, 0.5, 0.5));
+        ground_material = default_material;
+        std::string line;
+        while (std::getline(file, line)) {
+            line_number++;
+            auto comment = line.find('#');
+            if (comment != std::string::npos)
+                line.erase(comment);
+            std::istringstream in(line);
+            std::string keyword;
+            if (!(in >> keyword))
+                continue;
+            if (!parse_line(in, keyword)) {
+                set_error(error);
+                return unsupported ? MYPBR_ERR_UNSUPPORTED : MYPBR_ERR_BAD_SCENE;
+            }
+        }
+        if (!finish()) {
+            set_error(error);
+            return unsupported ? MYPBR_ERR_UNSUPPORTED : MYPBR_ERR_BAD_SCENE;
+        }
+        S.finalize();
+        return MYPBR_OK;
+    }
+};
+
+}  // namespace
+
+// ----------------------------------------------------------- host scene
+
+void mypbr_host_scene::finalize() {
+    flat = mypbr_flat_scene{};
+    flat.abi_version = MYPBR_ABI_VERSION;
+    flat.spheres = spheres.data();
+    flat.sphere_count = int64_t(spheres.size());
+    flat.quads = quads.data();
+    flat.quad_count = int64_t(quads.size());
+    flat.positions = positions.data();
+    flat.position_count = position_count();
+    flat.normals = normals.data();
+    flat.normal_count = normal_count();
+    flat.uvs = uvs.data();
+    flat.uv_count = uv_count();
+    flat.triangles = triangles.data();
+    flat.triangle_count = int64_t(triangles.size());
+    flat.meshes = meshes.data();
+    flat.mesh_count = int64_t(meshes.size());
+    flat.media = media.data();
+    flat.medium_count = int64_t(media.size());
+    flat.xforms = xforms.data();
+    flat.xform_count = int64_t(xforms.size());
+    flat.unbounded = unbounded.data();
+    flat.unbounded_count = int64_t(unbounded.size());
+    flat.bvh_nodes = bvh_nodes.data();
+    flat.bvh_node_count = int64_t(bvh_nodes.size());
+    flat.bvh_prims = bvh_prims.data();
+    flat.bvh_prim_count = int64_t(bvh_prims.size());
+    flat.materials = materials.data();
+    flat.material_count = int64_t(materials.size());
+    flat.textures = textures.data();
+    flat.texture_count = int64_t(textures.size());
+    flat.texels_ldr = texels_ldr.data();
+    flat.texels_ldr_bytes = int64_t(texels_ldr.size());
+    flat.texels_hdr = texels_hdr.data();
+    flat.texels_hdr_count = int64_t(texels_hdr.size());
+    flat.lights = lights.data();
+    flat.light_count = int64_t(lights.size());
+    flat.light_members = light_members.data();
+    flat.light_member_count = int64_t(light_members.size());
+    flat.environment.width = env_pixels.empty() ? 0 : env_width;
+    flat.environment.height = env_pixels.empty() ? 0 : env_height;
+    flat.environment.pixels = env_pixels.data();
+    flat.environment.intensity = env_intensity;
+    flat.environment.rotation = env_rotation;
+    flat.sun = sun;
+    flat.use_sky = use_sky ? 1 : 0;
+    flat.background[0] = background.x;
+    flat.background[1] = background.y;
+    flat.background[2] = background.z;
+    // Camera height as camera::initialize computes it (camera.h:143-144)
+    int h = int(camera.image_width / camera.aspect_ratio);
+    camera.image_height = h < 1 ? 1 : h;
+}
+
+extern "C" {
+
+void mypbr_camera_init(mypbr_camera* cam) {
+    if (!cam)
+        return;
+    *cam = mypbr_camera{};
+    cam->image_width = 100;
+    cam->aspect_ratio = 1.0;
+    cam->image_height = 100;
+    cam->vfov = 90;
+    cam->lookat[2] = -1;
+    cam->vup[1] = 1;
+    cam->focus_dist = 10;
+}
+
+void mypbr_render_opts_init(mypbr_render_opts* opts) {
+    if (!opts)
+        return;
+    *opts = mypbr_render_opts{};
+    opts->samples_per_pixel = 10;
+    opts->max_depth = 10;
+    opts->seed = 0x6d797062725f6762ull;
+}
+
+const char* mypbr_last_error(void) { return g_last_error.c_str(); }
+
+const char* mypbr_gpu_status_string(int status) {
+    switch (status) {
+        case MYPBR_OK: return "ok";
+        case MYPBR_ERR_CUDA: return "CUDA error";
+        case MYPBR_ERR_UNSUPPORTED: return "unsupported feature";
+        case MYPBR_ERR_QUEUE_OVERFLOW: return "device queue overflow";
+        case MYPBR_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+        case MYPBR_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case MYPBR_ERR_OUT_OF_MEMORY: return "out of memory";
+        case MYPBR_ERR_BAD_SCENE: return "bad scene";
+        case MYPBR_ERR_IO: return "I/O error";
+        case MYPBR_ERR_NO_DEVICE: return "no CUDA device";
+        case MYPBR_ERR_DEVICE_CHECK: return "device bounds check failed";
+        default: return "unknown status";
+    }
+}
+
+static int load_from_stream(std::istream& in, const std::string& name, const std::string& dir,
+                            mypbr_host_scene** out) {
+    auto s = std::make_unique<mypbr_host_scene>();
+    mypbr_camera_init(&s->camera);
+    mypbr_render_opts_init(&s->opts);
+    Loader loader(*s);
+    loader.path_for_errors = name;
+    loader.scene_dir = dir;
+    int status;
+    try {
+        status = loader.run(in);
+    } catch (const std::bad_alloc&) {
+        set_error(name + ": out of host memory");
+        return MYPBR_ERR_OUT_OF_MEMORY;
+    }
+    if (status != MYPBR_OK)
+        return status;
+    *out = s.release();
+    return MYPBR_OK;
+}
+
+int mypbr_scene_load(const char* path, mypbr_host_scene** out) {
+    if (!path || !out) {
+        set_error("mypbr_scene_load: null argument");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    clear_error();
+    std::string p(path);
+    std::ifstream file(p);
+    if (!file) {
+        set_error("Error: cannot open scene file '" + p + "'");
+        return MYPBR_ERR_IO;
+    }
+    auto slash = p.find_last_of('/');
+    std::string dir = slash == std::string::npos ? "" : p.substr(0, slash + 1);
+    return load_from_stream(file, p, dir, out);
+}
+
+int mypbr_scene_parse(const char* text, const char* base_dir, mypbr_host_scene** out) {
+    if (!text || !out) {
+        set_error("mypbr_scene_parse: null argument");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    clear_error();
+    std::string dir = base_dir ? base_dir : "";
+    if (!dir.empty() && dir.back() != '/')
+        dir += '/';
+    std::istringstream in{std::string(text)};
+    return load_from_stream(in, "<scene text>", dir, out);
+}
+
+const mypbr_flat_scene* mypbr_scene_flat(const mypbr_host_scene* s) { return s ? &s->flat : nullptr; }
+const mypbr_camera* mypbr_scene_camera(const mypbr_host_scene* s) { return s ? &s->camera : nullptr; }
+const mypbr_render_opts* mypbr_scene_render_opts(const mypbr_host_scene* s) { return s ? &s->opts : nullptr; }
+void mypbr_scene_free(mypbr_host_scene* s) { delete s; }
+
+int mypbr_ggx_albedo_table(double* out) {
+    if (!out) {
+        set_error("mypbr_ggx_albedo_table: null argument");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    ggx_albedo_table(out);
+    return MYPBR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+"""ctypes views of the flat scene arrays (include/mypbr_gpu.h), for
+inspection from Python: materials, textures, lights, primitives as numpy
+record arrays."""
+import ctypes
+
+import numpy as np
+
+_i32, _i64, _f64, _vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
+
+
+class Environment(ctypes.Structure):
+    _fields_ = [("width", _i32), ("height", _i32), ("pixels", _vp), ("intensity", _f64), ("rotation", _f64)]
+
+
+class Sun(ctypes.Structure):
+    _fields_ = [("enabled", _i32), ("disk_visible", _i32), ("direction", _f64 * 3), ("angular_diameter", _f64),
+                ("irradiance", _f64 * 3)]
+
+
+_ARRAYS = ["spheres", "quads", "positions", "normals", "uvs", "triangles", "meshes", "media", "xforms", "unbounded",
+           "bvh_nodes", "bvh_prims", "materials", "textures", "texels_ldr", "texels_hdr", "lights", "light_members"]
+_COUNTS = {"positions": "position_count", "normals": "normal_count", "uvs": "uv_count",
+           "texels_ldr": "texels_ldr_bytes", "texels_hdr": "texels_hdr_count", "bvh_nodes": "bvh_node_count",
+           "bvh_prims": "bvh_prim_count", "light_members": "light_member_count", "media": "medium_count",
+           "meshes": "mesh_count", "unbounded": "unbounded_count"}
+
+
+def _count_name(a):
+    return _COUNTS.get(a, a[:-1] + "_count")
+
+
+class FlatScene(ctypes.Structure):
+    _fields_ = ([("abi_version", ctypes.c_uint32), ("reserved0", ctypes.c_uint32)] +
+                [f for a in _ARRAYS for f in ((a, _vp), (_count_name(a), _i64))] +
+                [("environment", Environment), ("sun", Sun), ("use_sky", _i32), ("reserved1", _i32),
+                 ("background", _f64 * 3)])
+
+
+DTYPES = {
+    "spheres": np.dtype([("center", "<f8", 3), ("radius", "<f8"), ("material", "<i4"), ("xform", "<i4")]),
+    "quads": np.dtype([("q", "<f8", 3), ("u", "<f8", 3), ("v", "<f8", 3), ("normal", "<f8", 3),
+                       ("material", "<i4"), ("reserved", "<i4")]),
+    "positions": np.dtype(("<f8", 3)),
+    "normals": np.dtype(("<f8", 3)),
+    "uvs": np.dtype(("<f8", 2)),
+    "triangles": np.dtype([("v", "<i4", 3), ("n", "<i4", 3), ("t", "<i4", 3), ("material", "<i4"),
+                           ("flags", "<i4"), ("mesh", "<i4")]),
+    "meshes": np.dtype([("first_triangle", "<i8"), ("triangle_count", "<i8"), ("material", "<i4"),
+                        ("reserved", "<i4")]),
+    "media": np.dtype([("shape", "<i4"), ("xform", "<i4"), ("material", "<i4"), ("reserved", "<i4"),
+                       ("density", "<f8"), ("a", "<f8", 3), ("b", "<f8", 3)]),
+    "xforms": np.dtype([("m", "<f8", (3, 3)), ("t", "<f8", 3), ("inv_m", "<f8", (3, 3)), ("inv_t", "<f8", 3)]),
+    "unbounded": np.dtype([("kind", "<i4"), ("material", "<i4"), ("height", "<f8"), ("density", "<f8"),
+                           ("scale_height", "<f8")]),
+    "bvh_nodes": np.dtype([("bmin", "<f8", 3), ("bmax", "<f8", 3), ("offset", "<i4"), ("count", "<i4"),
+                           ("axis", "<i4"), ("reserved", "<i4")]),
+    "bvh_prims": np.dtype([("kind", "<i4"), ("index", "<i4")]),
+    "materials": np.dtype([("type", "<i4"), ("flags", "<i4"), ("tex", "<i4", 8), ("normal_map", "<i4"),
+                           ("emission_tex", "<i4"), ("p", "<f8", 16)]),
+    "textures": np.dtype([("type", "<i4"), ("a", "<i4"), ("b", "<i4"), ("width", "<i4"), ("height", "<i4"),
+                          ("flags", "<i4"), ("offset", "<i8"), ("p", "<f8", 4)]),
+    "texels_ldr": np.dtype("u1"),
+    "texels_hdr": np.dtype("<f4"),
+    "lights": np.dtype([("kind", "<i4"), ("first_member", "<i4"), ("member_count", "<i4"), ("reserved", "<i4"),
+                        ("probability", "<f8")]),
+    "light_members": np.dtype([("prim_kind", "<i4"), ("prim_index", "<i4"), ("weight", "<f8")]),
+}
+
+
+def view(scene):
+    """The flat scene of a mypbr_gb300.Scene as a dict of numpy arrays (copies)."""
+    fs = FlatScene.from_address(scene.flat)
+    out = {}
+    for a in _ARRAYS:
+        n = getattr(fs, _count_name(a))
+        ptr = getattr(fs, a)
+        dt = DTYPES[a]
+        if n == 0 or not ptr:
+            out[a] = np.zeros(0, dtype=dt)
+            continue
+        buf = (ctypes.c_char * (dt.itemsize * n)).from_address(ptr)
+        out[a] = np.frombuffer(bytes(buf), dtype=dt, count=n)
+    out["environment"] = fs.environment
+    out["sun"] = fs.sun
+    out["use_sky"] = fs.use_sky
+    out["background"] = tuple(fs.background)
+    return out
