@@ -1,0 +1,397 @@
+"""Benchmark: Mpaths/s of the wavefront path tracer on the 1000-sphere field.
+
+Workload (the headline configuration): a seeded field of 1000 spheres on a
+ground sphere (r = 1000 at y = -1000), centres uniform in [-11, 11] x [0.2, 1.2]
+x [-11, 11], radii lognormal(mu = -1.6, sigma = 0.3), 60% lambertian (albedo
+U[0,1]^3), 25% GGX metal (albedo U[0.5,1]^3, roughness U[0.02, 0.6]), 15%
+dielectric (ior 1.5), lit by a 1024 x 512 equirectangular sky (gradient plus a
+Gaussian sun lobe of angular radius 0.5 degrees and peak radiance 5e4)
+importance-sampled by alias table; 1920 x 1080, 256 spp, max depth 16. All
+inputs are synthetic and seeded; no dataset is involved.
+
+One step = one full render of that frame (530.8 M paths). `value` times the
+renders with the scene and the film resident in HBM (mypbr_gpu_render_device
+on the current stream, CUDA events); `e2e` times the C-ABI call a user makes
+with host buffers: mypbr_gpu_scene_create (uploads the flat scene) +
+mypbr_gpu_render (renders, copies the FP64 frame back) + destroy.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--spp S]
+
+--impl reference times the CPU implementation of the same path (the FP64
+restatement of the reference's camera::render in oracle/, on every host core)
+on a bounded sample of the same workload. With N > 1 (torchrun) every rank
+renders its own independent set of samples of the frame (weak scaling, no
+collective inside the timed region); rank 0 prints the JSON line.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WIDTH, HEIGHT = 1920, 1080
+METRIC = "Mpaths/s at 1080p"
+UNIT = "Mpaths/s"
+
+
+# ------------------------------------------------------------ the workload
+
+def write_hdr(path, rgb):
+    """Writes float RGB (H, W, 3) as a flat Radiance RGBE file."""
+    h, w, _ = rgb.shape
+    v = rgb.max(axis=2)
+    m, e = np.frexp(v)
+    scale = np.where(v > 1e-32, m * 256.0 / np.maximum(v, 1e-38), 0.0)
+    out = np.zeros((h, w, 4), dtype=np.uint8)
+    for c in range(3):
+        out[..., c] = np.clip(np.floor(rgb[..., c] * scale), 0, 255).astype(np.uint8)
+    out[..., 3] = np.where(v > 1e-32, e + 128, 0).astype(np.uint8)
+    with open(path, "wb") as f:
+        f.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
+        f.write(f"-Y {h} +X {w}\n".encode())
+        f.write(out.tobytes())
+
+
+def sky_image(w=1024, h=512):
+    """Sky gradient plus a Gaussian sun lobe (angular radius 0.5 deg, peak 5e4),
+    in the equirectangular layout of environment.h:334-348 (row 0 at +y)."""
+    j, i = np.meshgrid(np.arange(h) + 0.5, np.arange(w) + 0.5, indexing="ij")
+    theta = math.pi * j / h
+    phi = 2 * math.pi * (i / w - 0.5)
+    d = np.stack([np.sin(theta) * np.sin(phi), np.cos(theta), -np.sin(theta) * np.cos(phi)], axis=2)
+    up = np.clip(d[..., 1], 0, 1)
+    horizon = np.array([0.75, 0.85, 1.0])
+    zenith = np.array([0.15, 0.35, 0.85])
+    sky = horizon * (1 - up[..., None]) + zenith * up[..., None]
+    below = d[..., 1] < 0
+    sky[below] = np.array([0.12, 0.11, 0.10])
+    el, az = math.radians(35), math.radians(60)
+    sun = np.array([math.cos(el) * math.sin(az), math.sin(el), -math.cos(el) * math.cos(az)])
+    ang = np.arccos(np.clip((d * sun).sum(axis=2), -1, 1))
+    sigma = math.radians(0.5)
+    lobe = 5e4 * np.exp(-0.5 * (ang / sigma) ** 2)
+    return sky + lobe[..., None] * np.array([1.0, 0.95, 0.85])
+
+
+def sphere_field_scene(directory, seed=2, spp=256, width=WIDTH, height=HEIGHT, depth=16):
+    rng = np.random.default_rng(seed)
+    write_hdr(os.path.join(directory, "sky.hdr"), sky_image())
+    lines = [f"image_width {width}", f"aspect_ratio {width}/{height}", f"samples_per_pixel {spp}",
+             f"max_depth {depth}", "camera lookfrom 0 6 18  lookat 0 0 0  vup 0 1 0  vfov 35",
+             "environment sky.hdr", "material ground lambertian 0.5 0.5 0.5", "sphere 0 -1000 0 1000 ground"]
+    n = 1000
+    centers = np.stack([rng.uniform(-11, 11, n), rng.uniform(0.2, 1.2, n), rng.uniform(-11, 11, n)], axis=1)
+    radii = rng.lognormal(-1.6, 0.3, n)
+    kind = rng.uniform(size=n)
+    for k in range(n):
+        if kind[k] < 0.60:
+            a = rng.uniform(0, 1, 3)
+            lines.append(f"material m{k} lambertian {a[0]:.6f} {a[1]:.6f} {a[2]:.6f}")
+        elif kind[k] < 0.85:
+            a = rng.uniform(0.5, 1, 3)
+            lines.append(f"material m{k} metal {a[0]:.6f} {a[1]:.6f} {a[2]:.6f} {rng.uniform(0.02, 0.6):.6f}")
+        else:
+            lines.append(f"material m{k} dielectric 1.5")
+        c = centers[k]
+        lines.append(f"sphere {c[0]:.6f} {c[1]:.6f} {c[2]:.6f} {radii[k]:.6f} m{k}")
+    path = os.path.join(directory, "sphere_field.scene")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return path
+
+
+WORKLOAD = {"workload": "sphere_field_1000_hdri", "width": WIDTH, "height": HEIGHT, "spp": 256, "max_depth": 16,
+            "spheres": 1001, "environment": "1024x512 RGB float, alias-table sampled", "seed": 2,
+            "l2": "inputs (path state, queues, FP64 film) exceed L2; L2 also flushed between steps",
+            "guided": False}
+
+
+# ------------------------------------------------------------ helpers
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.close()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def flat_bytes(scene):
+    """Bytes of the flat scene arrays (what mypbr_gpu_scene_create copies)."""
+    from mypbr_gb300 import flat
+    v = flat.view(scene)
+    total = 0
+    for k, a in v.items():
+        if isinstance(a, np.ndarray):
+            total += a.nbytes
+    env = v["environment"]
+    total += env.width * env.height * 3 * 4
+    return total
+
+
+def oracle_render_timed(scene, spp, threads, rows=None):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    cam = scene.camera
+    cam.samples_per_pixel = spp
+    O = orc.OracleScene(scene)
+    t = time.perf_counter()
+    _, _, ex = O.render(cam, threads=threads, rows=rows)
+    return time.perf_counter() - t, ex
+
+
+def cpu_sample(scene, threads, budget_s):
+    """Times the oracle on a bounded sample of the workload: a band of rows of
+    the 1080p frame at the full 256 spp, sized from a short probe to take about
+    budget_s seconds. Returns (Mpaths/s, description)."""
+    probe_rows = 4
+    t1, ex1 = oracle_render_timed(scene, 256, threads, rows=(HEIGHT // 2 - probe_rows // 2, probe_rows))
+    rate = ex1["paths"] / t1
+    rows = int(max(probe_rows, min(HEIGHT, budget_s * rate / (WIDTH * 256))))
+    first = max(0, HEIGHT // 2 - rows // 2)
+    t, ex = oracle_render_timed(scene, 256, threads, rows=(first, rows))
+    return ex["paths"] / t / 1e6, f"rows {first}..{first + rows - 1} of 1920x1080 at 256 spp ({ex['paths']} paths, {t:.1f} s)"
+
+
+# ------------------------------------------------------------ arms
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import mypbr_gb300 as mp
+    threads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as d:
+        scene = mp.load_scene(sphere_field_scene(d, spp=256))
+        rates = []
+        desc = ""
+        for k in range(args.warmup + args.steps):
+            mpaths, desc = cpu_sample(scene, threads, args.reference_budget)
+            if k >= args.warmup:
+                rates.append(mpaths)
+    value = statistics.mean(rates)
+    ms_per_step = WIDTH * HEIGHT * 256 / (value * 1e6) * 1e3
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "config": WORKLOAD, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "per step: " + desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import mypbr_gb300 as mp
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    with tempfile.TemporaryDirectory() as d:
+        scene = mp.load_scene(sphere_field_scene(d, spp=args.spp))
+    cam = scene.camera
+    cam.samples_per_pixel = args.spp
+    cam.seed = 1000 + rank  # independent samples per rank
+    gpu = mp.GpuScene(scene)
+    L = mp.lib()
+    c, o = cam.structs()
+    w, h = c.image_width, c.image_height
+    rad = torch.zeros((h, w, 3), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # larger than the 129 MB L2
+    stream = torch.cuda.current_stream(dev)
+
+    def step(stats, timing):
+        o.timing = int(timing)
+        mp.check(L.mypbr_gpu_render_device(gpu.handle, ctypes.byref(c), ctypes.byref(o),
+                                           ctypes.c_void_p(rad.data_ptr()), None, None, None,
+                                           ctypes.c_void_p(stream.cuda_stream), ctypes.byref(stats)))
+
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        step(mp.RenderStatsStruct(), False)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times, launches = [], 0
+    totals = {"ext": 0, "sh": 0, "ms_extend": 0.0, "ms_shade": 0.0, "ms_shadow": 0.0, "ms_generate": 0.0,
+              "n_extend": 0, "n_shade": 0, "n_shadow": 0}
+    for _ in range(args.steps):
+        flush.fill_(1)
+        st = mp.RenderStatsStruct()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(st, True)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        launches += st.kernel_launches
+        totals["ext"] += st.extension_rays
+        totals["sh"] += st.shadow_rays
+        for k in ("ms_extend", "ms_shade", "ms_shadow", "ms_generate"):
+            totals[k] += getattr(st, k)
+        totals["n_extend"] += st.launches_extend
+        totals["n_shade"] += st.launches_shade
+        totals["n_shadow"] += st.launches_shadow
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = sum(times)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    paths_per_step = w * h * args.spp
+    value = world * paths_per_step * args.steps / (total_ms * 1e-3) / 1e6
+
+    # e2e through the C ABI with host buffers: upload, render, copy back
+    host = np.zeros((h, w, 3))
+    e2e_times = []
+    h2d = flat_bytes(scene)
+    o.timing = 0
+    for k in range(max(1, args.e2e_steps) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g2 = mp.GpuScene(scene)
+        mp.check(L.mypbr_gpu_render(g2.handle, ctypes.byref(c), ctypes.byref(o), ctypes.c_void_p(host.ctypes.data),
+                                    None, None, None, 0, mp.PASS_CALLBACK(), None))
+        g2.close()
+        dt = time.perf_counter() - t0
+        if k > 0:  # the first one warms the host-side allocations
+            e2e_times.append(dt)
+    e2e = world * paths_per_step / statistics.mean(e2e_times) / 1e6
+
+    if rank == 0:
+        # roofline of the dominant kernel, extend: algorithmic bytes per ray =
+        # ray record read (origin + tmin, direction + pdf: 32 B) + queue index
+        # (4 B) + hit record written (16 B)
+        ms_ext = totals["ms_extend"] / max(totals["n_extend"], 1)
+        bytes_per_ray = 52
+        ext_per_launch = totals["ext"] / max(totals["n_extend"], 1)
+        achieved = bytes_per_ray * ext_per_launch / (ms_ext * 1e-3) / 1e9 if ms_ext > 0 else 0.0
+        peak = None
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                peak = json.load(f)["hbm_gbs"]
+            peak_src = "measured"
+        except Exception:
+            peak, peak_src = 6800.0, "fallback"
+        shares = {k: totals[k] / total_ms for k in ("ms_extend", "ms_shade", "ms_shadow", "ms_generate")}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+                "config": dict(WORKLOAD, spp=args.spp, parallelism=f"samples x{world}"),
+                "gpu_launches": int(launches),
+                "rays": {"extension_per_path": totals["ext"] / (paths_per_step * args.steps),
+                         "shadow_per_path": totals["sh"] / (paths_per_step * args.steps),
+                         "mrays_per_s": world * (totals["ext"] + totals["sh"]) / (total_ms * 1e-3) / 1e6},
+                "kernel_time_share": shares,
+                "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
+                             "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": None,
+                             "peak_source": peak_src, "bytes_per_ray": bytes_per_ray,
+                             "avg_launch_ms": ms_ext, "rays_per_launch": ext_per_launch},
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(w * h * 3 * 8)},
+                "clocks": clk}
+        if world == 1 and not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            mpaths, desc = cpu_sample(scene, threads, args.cpu_budget)
+            line["cpu_baseline"] = {"value": mpaths, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--spp", type=int, default=256)
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
+    p.add_argument("--reference-budget", type=float, default=8.0, help="seconds per reference step")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    args = p.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

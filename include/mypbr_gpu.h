@@ -351,7 +351,9 @@ typedef struct mypbr_render_opts {
     int32_t guided;              /* reserved for the path-guiding proposal; must be 0 */
     uint64_t seed;               /* seeds the counter-based random numbers */
     int32_t samples_per_wave;    /* passes traced together (0 = automatic) */
-    int32_t reserved;
+    int32_t timing;              /* 1: time each kernel kind with CUDA events (stats) */
+    int32_t first_row;           /* render only rows [first_row, first_row + row_count) */
+    int32_t row_count;           /* 0 = every row; other rows of the outputs are left as they are */
 } mypbr_render_opts;
 
 void mypbr_render_opts_init(mypbr_render_opts* opts);
@@ -410,6 +412,9 @@ typedef struct mypbr_render_stats {
     uint64_t extension_rays;   /* closest-hit rays traced for path continuation */
     uint64_t shadow_rays;      /* shadow rays traced */
     uint64_t kernel_launches;  /* kernels this call launched */
+    /* with opts->timing: summed CUDA-event time per kernel kind, milliseconds */
+    double ms_generate, ms_extend, ms_shade, ms_shadow, ms_other;
+    uint64_t launches_extend, launches_shade, launches_shadow;
 } mypbr_render_stats;
 
 int mypbr_gpu_render_device(mypbr_gpu_scene* scene, const mypbr_camera* cam, const mypbr_render_opts* opts,

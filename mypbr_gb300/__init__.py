@@ -53,13 +53,21 @@ class RenderOptsStruct(ctypes.Structure):
                 ("max_diffuse", ctypes.c_int32), ("max_specular", ctypes.c_int32),
                 ("max_scatter", ctypes.c_int32), ("transparent_shadows", ctypes.c_int32),
                 ("collect_features", ctypes.c_int32), ("guided", ctypes.c_int32), ("seed", ctypes.c_uint64),
-                ("samples_per_wave", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("samples_per_wave", ctypes.c_int32), ("timing", ctypes.c_int32),
+                ("first_row", ctypes.c_int32), ("row_count", ctypes.c_int32)]
 
 
 class RenderStatsStruct(ctypes.Structure):
     """mypbr_render_stats (include/mypbr_gpu.h)."""
     _fields_ = [("paths", ctypes.c_uint64), ("extension_rays", ctypes.c_uint64),
-                ("shadow_rays", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
+                ("shadow_rays", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+                ("ms_generate", ctypes.c_double), ("ms_extend", ctypes.c_double), ("ms_shade", ctypes.c_double),
+                ("ms_shadow", ctypes.c_double), ("ms_other", ctypes.c_double),
+                ("launches_extend", ctypes.c_uint64), ("launches_shade", ctypes.c_uint64),
+                ("launches_shadow", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 PASS_CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_void_p)
@@ -102,6 +110,8 @@ def lib():
                                    vp, ctypes.c_int, PASS_CALLBACK, vp]
     L.mypbr_gpu_render_device.argtypes = [vp, ctypes.POINTER(CameraStruct), ctypes.POINTER(RenderOptsStruct), vp,
                                           vp, vp, vp, vp, ctypes.POINTER(RenderStatsStruct)]
+    L.mypbr_gpu_render_ex.argtypes = [vp, ctypes.POINTER(CameraStruct), ctypes.POINTER(RenderOptsStruct), vp, vp, vp,
+                                      vp, vp, ctypes.c_int, PASS_CALLBACK, vp, ctypes.POINTER(RenderStatsStruct)]
     L.mypbr_gpu_trace.argtypes = [vp, fp, i64, fp, ip, ctypes.c_int]
     L.mypbr_gpu_bsdf_eval.argtypes = [vp, i32, fp, fp, fp, i64, fp]
     _lib = L
@@ -218,7 +228,7 @@ class Camera:
     _CAM = {"image_width", "aspect_ratio", "vfov", "lookfrom", "lookat", "vup", "defocus_angle", "focus_dist",
             "ortho_height", "blades", "blade_rotation"}
     _OPT = {"samples_per_pixel", "max_depth", "max_diffuse", "max_specular", "max_scatter", "transparent_shadows",
-            "collect_features", "seed", "samples_per_wave", "guided"}
+            "collect_features", "seed", "samples_per_wave", "guided", "timing", "first_row", "row_count"}
 
     def __init__(self, cam=None, opts=None):
         c = CameraStruct()
@@ -288,6 +298,20 @@ class Camera:
         check(lib().mypbr_gpu_render(gpu_scene.handle, ctypes.byref(c), ctypes.byref(o), ptr(rad), ptr(alb),
                                      ptr(nrm), ptr(var), int(save_every), cb, None))
         return Frame(rad, alb, nrm, var)
+
+
+def render_ex(camera, gpu_scene):
+    """Renders and returns (radiance (H, W, 3), per-channel variance of the
+    mean (H, W, 3), stats dict) through mypbr_gpu_render_ex."""
+    c, o = camera.structs()
+    w, h = c.image_width, c.image_height
+    rad = np.zeros((h, w, 3))
+    chv = np.zeros((h, w, 3))
+    st = RenderStatsStruct()
+    check(lib().mypbr_gpu_render_ex(gpu_scene.handle, ctypes.byref(c), ctypes.byref(o),
+                                    ctypes.c_void_p(rad.ctypes.data), None, None, None,
+                                    ctypes.c_void_p(chv.ctypes.data), 0, PASS_CALLBACK(), None, ctypes.byref(st)))
+    return rad, chv, st.as_dict()
 
 
 def ggx_albedo_table():

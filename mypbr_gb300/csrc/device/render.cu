@@ -43,6 +43,7 @@ struct WaveParams {
     int transparent_shadows, collect_features, has_lights, pad;
     unsigned long long seed;
     int pass0, npass;
+    int first_row, band_rows;  // the rows rendered: [first_row, first_row + band_rows)
     unsigned long long* totals;  // extension rays, shadow rays
 };
 
@@ -128,11 +129,12 @@ MYPBR_DEV void camera_ray(const CameraParams& C, int i, int j, int pass, Rng& g,
 }
 
 __global__ void k_generate(WaveParams P) {
-    size_t npix = size_t(P.cam.width) * P.cam.height;
+    size_t npix = size_t(P.cam.width) * P.band_rows;
     size_t n = npix * size_t(P.npass);
     size_t stride = size_t(gridDim.x) * blockDim.x;
+    size_t first_pixel = size_t(P.first_row) * P.cam.width;
     for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
-        uint32_t pixel = uint32_t(t % npix);
+        uint32_t pixel = uint32_t(first_pixel + t % npix);
         uint32_t pass = uint32_t(P.pass0 + int(t / npix));
         int i = int(pixel % uint32_t(P.cam.width)), j = int(pixel / uint32_t(P.cam.width));
         Rng g = make_rng(P.seed, pixel, pass);
@@ -159,7 +161,7 @@ MYPBR_DEV Rng load_rng(const WaveParams& P, uint32_t slot) {
 
 // camera.h:253-277: albedo and normal of the first non-specular surface
 __global__ void k_features(WaveParams P) {
-    size_t n = size_t(P.cam.width) * P.cam.height * size_t(P.npass);
+    size_t n = size_t(P.cam.width) * P.band_rows * size_t(P.npass);
     size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
         float4 ro = P.B.ray_o[t], rd = P.B.ray_d[t];
@@ -404,10 +406,11 @@ __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
 // the variance of the mean luminance.
 __global__ void k_resolve(WaveParams P, int samples, double* radiance, double* albedo, double* normal,
                           double* variance) {
-    size_t npix = size_t(P.cam.width) * P.cam.height;
+    size_t first = size_t(P.first_row) * P.cam.width;
+    size_t end = first + size_t(P.cam.width) * P.band_rows;
     double scale = 1.0 / samples;
     size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < npix; p += stride) {
+    for (size_t p = first + size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < end; p += stride) {
         double r0 = scale * P.B.film[3 * p], r1 = scale * P.B.film[3 * p + 1], r2 = scale * P.B.film[3 * p + 2];
         radiance[3 * p] = r0;
         radiance[3 * p + 1] = r1;
@@ -436,10 +439,11 @@ __global__ void k_resolve(WaveParams P, int samples, double* radiance, double* a
 // Per-channel variance of the mean radiance, from the second moments
 // (for the statistical parity checks).
 __global__ void k_channel_variance(WaveParams P, int samples, double* out) {
-    size_t n = size_t(P.cam.width) * P.cam.height * 3;
+    size_t first = size_t(P.first_row) * P.cam.width * 3;
+    size_t end = first + size_t(P.cam.width) * P.band_rows * 3;
     double scale = 1.0 / samples;
     size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+    for (size_t k = first + size_t(blockIdx.x) * blockDim.x + threadIdx.x; k < end; k += stride) {
         double m = scale * P.B.film[k];
         double spread = fmax(scale * P.B.film2[k] - m * m, 0.0);
         out[k] = samples > 1 ? spread / (samples - 1) : spread;
@@ -568,19 +572,88 @@ Launch launch_config(const mypbr_gpu_scene& G) {
     return L;
 }
 
-// Renders passes [pass0, pass0 + npass) of every pixel into the film.
-int run_wave(mypbr_gpu_scene& G, WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches) {
+// CUDA events around each launch, summed per kernel kind after the render.
+struct KernelTimer {
+    bool on = false;
+    cudaStream_t st = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+    std::vector<int> kinds;  // 0 generate, 1 extend, 2 shade, 3 shadow, 4 other
+    size_t used = 0;
+    ~KernelTimer() {
+        for (auto& e : pool) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+    }
+    int begin(int kind) {
+        if (!on)
+            return MYPBR_OK;
+        if (used == pool.size()) {
+            cudaEvent_t a, b;
+            MYPBR_CUDA(cudaEventCreate(&a));
+            MYPBR_CUDA(cudaEventCreate(&b));
+            pool.push_back({a, b});
+            kinds.push_back(kind);
+        }
+        kinds[used] = kind;
+        MYPBR_CUDA(cudaEventRecord(pool[used].first, st));
+        return MYPBR_OK;
+    }
+    int end() {
+        if (!on)
+            return MYPBR_OK;
+        MYPBR_CUDA(cudaEventRecord(pool[used].second, st));
+        used++;
+        return MYPBR_OK;
+    }
+    int collect(mypbr_render_stats* s) {
+        if (!on || !s)
+            return MYPBR_OK;
+        double ms[5] = {0, 0, 0, 0, 0};
+        uint64_t cnt[5] = {0, 0, 0, 0, 0};
+        for (size_t k = 0; k < used; k++) {
+            MYPBR_CUDA(cudaEventSynchronize(pool[k].second));
+            float t = 0;
+            MYPBR_CUDA(cudaEventElapsedTime(&t, pool[k].first, pool[k].second));
+            ms[kinds[k]] += t;
+            cnt[kinds[k]]++;
+        }
+        s->ms_generate = ms[0];
+        s->ms_extend = ms[1];
+        s->ms_shade = ms[2];
+        s->ms_shadow = ms[3];
+        s->ms_other = ms[4];
+        s->launches_extend = cnt[1];
+        s->launches_shade = cnt[2];
+        s->launches_shadow = cnt[3];
+        return MYPBR_OK;
+    }
+};
+
+#define TIMED(kind, launch)                      \
+    do {                                         \
+        int s_ = T.begin(kind);                  \
+        if (s_ != MYPBR_OK)                      \
+            return s_;                           \
+        launch;                                  \
+        s_ = T.end();                            \
+        if (s_ != MYPBR_OK)                      \
+            return s_;                           \
+    } while (0)
+
+// Renders passes [pass0, pass0 + npass) of every pixel of the band into the film.
+int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T) {
     MYPBR_CUDA(cudaMemsetAsync(P.B.counters, 0, sizeof(uint32_t) * size_t(2 * P.B.depth_slots + 8), st));
-    k_generate<<<L.grid_stream, 256, 0, st>>>(P);
+    TIMED(0, (k_generate<<<L.grid_stream, 256, 0, st>>>(P)));
     launches++;
     if (P.collect_features) {
-        k_features<<<L.grid_shade, 256, 0, st>>>(P);
+        TIMED(4, (k_features<<<L.grid_shade, 256, 0, st>>>(P)));
         launches++;
     }
     for (int depth = 0; depth < P.max_depth; depth++) {
-        k_extend<<<L.grid_extend, 256, 0, st>>>(P, depth);
-        k_shade<<<L.grid_shade, 256, 0, st>>>(P, depth);
-        k_shadow<<<L.grid_shadow, 256, 0, st>>>(P, depth);
+        TIMED(1, (k_extend<<<L.grid_extend, 256, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        TIMED(3, (k_shadow<<<L.grid_shadow, 256, 0, st>>>(P, depth)));
         launches += 3;
     }
     MYPBR_CUDA(cudaGetLastError());
@@ -593,7 +666,8 @@ struct RenderSetup {
     WaveParams P;
     Launch L;
     int spp, per_wave;
-    size_t npix;
+    size_t npix;  // pixels of the band
+    bool timing;
 };
 
 int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* o, int save_every, RenderSetup& R) {
@@ -621,9 +695,14 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
     P.collect_features = o->collect_features;
     P.has_lights = G->dev.light_count > 0;
     P.seed = o->seed;
-    R.npix = size_t(P.cam.width) * P.cam.height;
-    if (R.npix > (size_t(1) << 31))
+    if (size_t(P.cam.width) * P.cam.height > (size_t(1) << 31))
         return bad_arg("mypbr_gpu_render: image too large");
+    P.first_row = o->first_row;
+    P.band_rows = o->row_count > 0 ? o->row_count : P.cam.height - o->first_row;
+    if (o->first_row < 0 || o->row_count < 0 || P.band_rows <= 0 || P.first_row + P.band_rows > P.cam.height)
+        return bad_arg("mypbr_gpu_render: first_row / row_count outside the image");
+    R.npix = size_t(P.cam.width) * P.band_rows;
+    R.timing = o->timing != 0;
     R.spp = o->samples_per_pixel;
     // About 8M paths in flight per wave (or what the caller asks)
     int per_wave = o->samples_per_wave > 0 ? o->samples_per_wave
@@ -634,7 +713,7 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
     while (per_wave > 1 && R.npix * size_t(per_wave) > (size_t(1) << 30))
         per_wave /= 2;
     R.per_wave = per_wave;
-    int s = ensure_buffers(G->rb, R.npix * size_t(per_wave), R.npix, P.max_depth + 1);
+    int s = ensure_buffers(G->rb, R.npix * size_t(per_wave), size_t(P.cam.width) * P.cam.height, P.max_depth + 1);
     if (s != MYPBR_OK)
         return s;
     P.B = G->rb;
@@ -658,15 +737,19 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
     MYPBR_CUDA(cudaMalloc(&tot.d, 2 * sizeof(unsigned long long)));
     MYPBR_CUDA(cudaMemsetAsync(tot.d, 0, 2 * sizeof(unsigned long long), st));
     P.totals = tot.d;
-    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * R.npix * sizeof(double), st));
-    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * R.npix * sizeof(double), st));
+    size_t full = size_t(P.cam.width) * P.cam.height;
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * full * sizeof(double), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * full * sizeof(double), st));
     if (P.collect_features)
-        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * R.npix * sizeof(double), st));
+        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * full * sizeof(double), st));
     uint64_t launches = 0;
+    KernelTimer T;
+    T.on = R.timing;
+    T.st = st;
     for (int pass0 = 0; pass0 < R.spp; pass0 += R.per_wave) {
         P.pass0 = pass0;
         P.npass = std::min(R.per_wave, R.spp - pass0);
-        int s = run_wave(*G, P, R.L, st, launches);
+        int s = run_wave(P, R.L, st, launches, T);
         if (s != MYPBR_OK)
             return s;
         int done = pass0 + P.npass;
@@ -675,14 +758,19 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
             launches++;
             MYPBR_CUDA(cudaGetLastError());
             if (h_rad) {
-                MYPBR_CUDA(cudaMemcpyAsync(h_rad, d_rad, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                size_t off = size_t(P.first_row) * P.cam.width;
+                MYPBR_CUDA(cudaMemcpyAsync(h_rad + 3 * off, d_rad + 3 * off, 3 * R.npix * sizeof(double),
+                                           cudaMemcpyDeviceToHost, st));
                 if (P.collect_features) {
                     if (h_alb)
-                        MYPBR_CUDA(cudaMemcpyAsync(h_alb, d_alb, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                        MYPBR_CUDA(cudaMemcpyAsync(h_alb + 3 * off, d_alb + 3 * off, 3 * R.npix * sizeof(double),
+                                                   cudaMemcpyDeviceToHost, st));
                     if (h_nrm)
-                        MYPBR_CUDA(cudaMemcpyAsync(h_nrm, d_nrm, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                        MYPBR_CUDA(cudaMemcpyAsync(h_nrm + 3 * off, d_nrm + 3 * off, 3 * R.npix * sizeof(double),
+                                                   cudaMemcpyDeviceToHost, st));
                     if (h_var)
-                        MYPBR_CUDA(cudaMemcpyAsync(h_var, d_var, R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+                        MYPBR_CUDA(cudaMemcpyAsync(h_var + off, d_var + off, R.npix * sizeof(double),
+                                                   cudaMemcpyDeviceToHost, st));
                 }
             }
             MYPBR_CUDA(cudaStreamSynchronize(st));
@@ -697,6 +785,7 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
     }
     MYPBR_CUDA(cudaGetLastError());
     if (stats) {
+        *stats = mypbr_render_stats{};
         unsigned long long t[2];
         MYPBR_CUDA(cudaMemcpyAsync(t, tot.d, sizeof t, cudaMemcpyDeviceToHost, st));
         MYPBR_CUDA(cudaStreamSynchronize(st));
@@ -704,6 +793,9 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
         stats->extension_rays = t[0];
         stats->shadow_rays = t[1];
         stats->kernel_launches = launches;
+        int s = T.collect(stats);
+        if (s != MYPBR_OK)
+            return s;
     }
     return MYPBR_OK;
 }
@@ -748,31 +840,39 @@ extern "C" int mypbr_gpu_render_ex(mypbr_gpu_scene* G, const mypbr_camera* cam, 
     if (s != MYPBR_OK)
         return s;
     bool feats = opts->collect_features != 0;
+    // Device outputs cover the whole image (kernels index by image pixel);
+    // only the band's rows come back.
+    size_t full = size_t(R.P.cam.width) * R.P.cam.height;
+    size_t off = size_t(R.P.first_row) * R.P.cam.width, n = R.npix;
     DevBuf rad, alb, nrm, var, chv;
-    MYPBR_CUDA(cudaMalloc(&rad.p, 3 * R.npix * sizeof(double)));
+    MYPBR_CUDA(cudaMalloc(&rad.p, 3 * full * sizeof(double)));
     if (feats) {
-        MYPBR_CUDA(cudaMalloc(&alb.p, 3 * R.npix * sizeof(double)));
-        MYPBR_CUDA(cudaMalloc(&nrm.p, 3 * R.npix * sizeof(double)));
-        MYPBR_CUDA(cudaMalloc(&var.p, R.npix * sizeof(double)));
+        MYPBR_CUDA(cudaMalloc(&alb.p, 3 * full * sizeof(double)));
+        MYPBR_CUDA(cudaMalloc(&nrm.p, 3 * full * sizeof(double)));
+        MYPBR_CUDA(cudaMalloc(&var.p, full * sizeof(double)));
     }
     if (channel_variance)
-        MYPBR_CUDA(cudaMalloc(&chv.p, 3 * R.npix * sizeof(double)));
+        MYPBR_CUDA(cudaMalloc(&chv.p, 3 * full * sizeof(double)));
     cudaStream_t st = nullptr;
     s = render_all(G, R, st, rad.p, alb.p, nrm.p, var.p, chv.p, save_every, on_pass, user, radiance,
                    feats ? albedo : nullptr, feats ? normal : nullptr, feats ? variance : nullptr, stats);
     if (s != MYPBR_OK)
         return s;
-    MYPBR_CUDA(cudaMemcpyAsync(radiance, rad.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+    auto back = [&](double* host, const double* dev, size_t per_pixel) {
+        return cudaMemcpyAsync(host + per_pixel * off, dev + per_pixel * off, per_pixel * n * sizeof(double),
+                               cudaMemcpyDeviceToHost, st);
+    };
+    MYPBR_CUDA(back(radiance, rad.p, 3));
     if (feats) {
         if (albedo)
-            MYPBR_CUDA(cudaMemcpyAsync(albedo, alb.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+            MYPBR_CUDA(back(albedo, alb.p, 3));
         if (normal)
-            MYPBR_CUDA(cudaMemcpyAsync(normal, nrm.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+            MYPBR_CUDA(back(normal, nrm.p, 3));
         if (variance)
-            MYPBR_CUDA(cudaMemcpyAsync(variance, var.p, R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+            MYPBR_CUDA(back(variance, var.p, 1));
     }
     if (channel_variance)
-        MYPBR_CUDA(cudaMemcpyAsync(channel_variance, chv.p, 3 * R.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MYPBR_CUDA(back(channel_variance, chv.p, 3));
     MYPBR_CUDA(cudaStreamSynchronize(st));
     return MYPBR_OK;
 }

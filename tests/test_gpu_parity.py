@@ -1,0 +1,225 @@
+"""The CUDA path against the oracle and the reference's goldens (GPU).
+
+(a) ray batches: hit/miss and primitive id identical to the FP64 oracle (which
+    matches the reference to 1e-12) away from edges and ties, t and normal to
+    1e-5 relative;
+(b) BSDF eval / pdf against the reference's values at 1e-5;
+(c) white furnace energy conservation to 1e-3;
+(d) full renders within 3 sigma of the reference's per-pixel means.
+Everything goes through the C ABI (mypbr_gb300 is a ctypes binding of it).
+"""
+import numpy as np
+import pytest
+
+import mypbr_gb300 as mp
+import oracle as orc
+from conftest import GOLDEN, scene_path
+from mypbr_gb300 import flat
+
+pytestmark = pytest.mark.gpu
+
+
+def load_golden(name):
+    return np.load(f"{GOLDEN}/{name}.npz")
+
+
+_GPU_SCENES = {}
+
+
+def gpu_scene(name):
+    if name not in _GPU_SCENES:
+        sc = mp.load_scene(scene_path(f"{name}.scene"))
+        _GPU_SCENES[name] = (sc, mp.GpuScene(sc))
+    return _GPU_SCENES[name]
+
+
+def stable_mask(O, rays, scale, trials=4, seed=0):
+    """Rays whose oracle result (hit/miss and primitive) does not change when
+    the origin moves by 1e-5 of the scene scale: the ones away from edges,
+    silhouettes and ties, where an FP32 answer must equal the FP64 one."""
+    rng = np.random.default_rng(seed)
+    _, base = O.trace(rays)
+    ok = np.ones(len(rays), dtype=bool)
+    for _ in range(trials):
+        r = rays.copy()
+        r[:, 0:3] += rng.normal(size=(len(r), 3)) * 1e-5 * scale
+        _, p = O.trace(r)
+        ok &= np.all(p == base, axis=1)
+    return ok
+
+
+@pytest.mark.parametrize("scene_name,golden,scale", [("hits_mix", "hits_mix", 10.0), ("cornell_c1", "hits_cornell", 555.0)])
+def test_trace_matches_oracle_and_reference(scene_name, golden, scale):
+    sc, G = gpu_scene(scene_name)
+    g = load_golden(golden)
+    n = len(g["hit"])
+    rays = np.zeros((n, 8))
+    rays[:, 0:3] = g["o"]
+    rays[:, 3:6] = g["d"]
+    rays[:, 6] = 0.001
+    rays[:, 7] = 3e38
+    O = orc.OracleScene(sc)
+    ohits, oprim = O.trace(rays)
+    assert np.array_equal(oprim[:, 0] >= 0, g["hit"] > 0)
+    hits, prim = G.trace(rays.astype(np.float32))
+    ok = stable_mask(O, rays, scale)
+    assert ok.mean() > 0.98, f"only {ok.mean():.4f} of the rays are away from edges"
+    np.testing.assert_array_equal(prim[ok], oprim[ok], err_msg="hit/miss or primitive id differs")
+    both = ok & (prim[:, 0] >= 0)
+    rel_t = np.abs(hits[both, 0] - ohits[both, 0]) / np.abs(ohits[both, 0])
+    assert rel_t.max() < 1e-5, rel_t.max()
+    dn = np.abs(hits[both, 1:4] - ohits[both, 1:4]).max()
+    assert dn < 1e-5, dn
+    np.testing.assert_array_equal(hits[both, 6], ohits[both, 6])
+
+
+def test_bsdf_matches_reference():
+    sc, G = gpu_scene("bsdf_probe")
+    b = load_golden("bsdf_probe")
+    mats = flat.view(sc)["spheres"]["material"]
+    n = len(b["sphere"])
+    rec = np.zeros((n, 16))
+    rec[:, 5] = 1.0
+    rec[:, 6] = 1 - b["face"]
+    rec[:, 7], rec[:, 8] = 0.25, 0.75
+    rec[:, 9], rec[:, 13] = 2.0, 3.0
+    for k in np.unique(b["sphere"]):
+        m = b["sphere"] == k
+        out = G.bsdf_eval(int(mats[k]), rec[m], -b["wo"][m], b["wi"][m])
+        ev, pdf = b["eval"][m], b["pdf"][m]
+        # 1e-5 relative, with an absolute floor at 1e-5 of the largest value of
+        # this material (FP32 cannot resolve relative differences of values
+        # 1e5 times smaller than the lobe's peak)
+        scale_e = max(np.abs(ev).max(), 1e-12)
+        scale_p = max(np.abs(pdf).max(), 1e-12)
+        np.testing.assert_allclose(out[:, :3], ev, rtol=1e-5, atol=1e-5 * scale_e, err_msg=f"material {k} eval")
+        np.testing.assert_allclose(out[:, 3], pdf, rtol=1e-5, atol=1e-5 * scale_p, err_msg=f"material {k} pdf")
+
+
+FURNACE = """
+image_width 32
+aspect_ratio 1
+samples_per_pixel {spp}
+max_depth 100
+background 1 1 1
+{extra}
+material m {material}
+sphere 0 0 -1 0.5 m
+"""
+
+
+@pytest.mark.parametrize("material,tol", [("lambertian 1 1 1", 1e-5), ("metal 1 1 1 0", 1e-5),
+                                          ("dielectric 1.5", 0.02), ("thin_glass 1.5", 0.02)])
+def test_white_furnace(material, tol):
+    """furnace_test.cpp:194-206: objects that neither absorb nor emit vanish in
+    a white background. Lambertian and mirror are exact in the reference (1e-6);
+    here in FP32 the bound is 1e-5, inside the benchmark spec's 1e-3."""
+    sc = mp.parse_scene(FURNACE.format(spp=64, extra="", material=material))
+    G = mp.GpuScene(sc)
+    f = sc.camera.render(G)
+    mean = f.radiance.mean()
+    worst = np.abs(f.radiance - 1).max()
+    assert abs(mean - 1) < tol and worst < 4 * tol, (mean, worst)
+
+
+def test_white_furnace_environment_nee():
+    """furnace_test.cpp:211-213: the white sky as an importance-sampled
+    environment light, with NEE and MIS."""
+    sc = mp.parse_scene(FURNACE.format(spp=256, extra="sky uniform 1 1 1", material="lambertian 1 1 1"))
+    G = mp.GpuScene(sc)
+    f = sc.camera.render(G)
+    assert abs(f.radiance.mean() - 1) < 1e-3
+    assert np.abs(f.radiance - 1).max() < 0.08
+
+
+@pytest.mark.parametrize("g", [0.0, 0.7])
+def test_white_medium_furnace(g):
+    text = f"""
+image_width 32
+aspect_ratio 1
+samples_per_pixel 256
+max_depth 100
+background 1 1 1
+material haze volume 1 1 1 g {g}
+medium 2.0 sphere 0 0 -1 0.5 haze
+"""
+    sc = mp.parse_scene(text)
+    f = sc.camera.render(mp.GpuScene(sc))
+    assert abs(f.radiance.mean() - 1) < 0.03
+
+
+@pytest.mark.parametrize("scaled", [False, True])
+def test_beer_lambert_slab(scaled):
+    """furnace_test.cpp:157-188: exp(-sigma_a d) through an index-1 slab, exact."""
+    d = 0.8
+    sigma = np.array([0.2, 1.0, 3.0])
+    tint = np.exp(-sigma * 1.0)
+    geo = ("box -50 -50 -1.4 50 50 -1 glass scale 2" if scaled else "box -100 -100 -2.8 100 100 -2 glass")
+    text = f"""
+image_width 8
+aspect_ratio 1
+samples_per_pixel 4
+max_depth 10
+background 1 1 1
+camera vfov 0.1
+material glass dielectric 1.0 color {tint[0]:.17g} {tint[1]:.17g} {tint[2]:.17g} distance 1
+{geo}
+"""
+    sc = mp.parse_scene(text)
+    f = sc.camera.render(mp.GpuScene(sc))
+    want = np.exp(-sigma * d)
+    assert np.abs(f.radiance - want).max() < 1e-5
+
+
+def render_gpu(name, width, spp, seed=7):
+    sc, G = gpu_scene(name)
+    cam = sc.camera
+    cam.image_width = width
+    cam.samples_per_pixel = spp
+    cam.seed = seed
+    rad, chv, _ = mp.render_ex(cam, G)
+    return rad, chv
+
+
+@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials"])
+def test_render_matches_reference(name):
+    g = load_golden(f"render_{name}")
+    rad, var = render_gpu(name, g["mean"].shape[1], 1024)
+    z = (rad - g["mean"]) / np.sqrt(var + g["var_of_mean"] + 1e-30)
+    n = rad.shape[0] * rad.shape[1]
+    tot_sigma = np.sqrt(var.sum(axis=(0, 1)) + g["var_of_mean"].sum(axis=(0, 1))) / n
+    tot_z = (rad.mean(axis=(0, 1)) - g["mean"].mean(axis=(0, 1))) / tot_sigma
+    assert np.mean(np.abs(z) > 3) < 0.02, np.mean(np.abs(z) > 3)
+    assert np.mean(np.abs(z) > 5) < 0.002
+    assert np.all(np.abs(tot_z) < 4), tot_z
+
+
+def test_render_matches_oracle_c1():
+    """Config 1 (Cornell, 256 x 256 at 64 spp in the benchmark) at a reduced
+    size: GPU vs oracle per-pixel within 3 sigma."""
+    rad, var = render_gpu("cornell_c1", 64, 256, seed=11)
+    sc, _ = gpu_scene("cornell_c1")
+    cam = sc.camera
+    cam.image_width = 64
+    cam.samples_per_pixel = 256
+    orad, ovar, _ = orc.OracleScene(sc).render(cam, threads=0)
+    z = (rad - orad) / np.sqrt(var + ovar + 1e-30)
+    assert np.mean(np.abs(z) > 3) < 0.02
+    assert abs(rad.mean() - orad.mean()) < 4 * np.sqrt((var.sum() + ovar.sum())) / rad.size
+
+
+def test_features_and_progressive_callback():
+    sc, G = gpu_scene("cornell_c1")
+    cam = sc.camera
+    cam.image_width = 32
+    cam.samples_per_pixel = 16
+    cam.collect_features = 1
+    seen = []
+    f = cam.render(G, save_every=4, on_pass=lambda done, fr: seen.append((done, fr.radiance.mean())))
+    assert [d for d, _ in seen] == [4, 8, 12]
+    assert f.albedo.shape == (32, 32, 3) and f.normal.shape == (32, 32, 3) and f.variance.shape == (32, 32)
+    # Cornell: every camera ray hits a lambertian surface; albedo within the wall colours
+    assert f.albedo.min() >= 0 and f.albedo.max() <= 0.75
+    assert np.all(np.linalg.norm(f.normal, axis=2) <= 1 + 1e-9)
+    assert np.all(f.variance >= 0)
+    cam.collect_features = 0
