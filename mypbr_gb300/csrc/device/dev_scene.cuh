@@ -69,6 +69,8 @@ struct DeviceScene {
     const DevUnbounded* unbounded;
     int unbounded_count;
     int has_bvh;
+    int bvh_node_count;  // interior nodes; a walk visits each at most once
+    int* error;          // sticky device error word (0 = none), read by the host after each call
     // appearance
     const DevMaterial* materials;
     const DevTexture* textures;
@@ -350,7 +352,14 @@ MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tm
         int stack[kBvhStack];
         int sp = 0;
         int node = 0;
+        // A tree walk enters each interior node at most once; the cap only
+        // guards against a malformed tree, which it reports instead of spinning.
+        int visits = 0;
         while (true) {
+            if (++visits > S.bvh_node_count + 1) {
+                atomicCAS(S.error, 0, 1);
+                break;
+            }
             const float4* n = S.bvh + 4 * node;
             float4 a0 = ldg4(n), a1 = ldg4(n + 1), c0 = ldg4(n + 2), c1 = ldg4(n + 3);
             // slab tests of both children against (tmin, best)
@@ -402,6 +411,10 @@ MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tm
             h1 = h1 && k1 == 0;
             if (h0 && h1) {
                 bool first0 = n0 <= n1;
+                if (sp == kBvhStack) {  // deeper than the host-checked depth: report, stop
+                    atomicCAS(S.error, 0, 2);
+                    break;
+                }
                 stack[sp++] = first0 ? i1 : i0;
                 node = first0 ? i0 : i1;
             } else if (h0) {

@@ -109,17 +109,21 @@ MYPBR_DEV float fresnel_conductor(float ci, float eta, float k) {
 // microfacet.h:145-212
 struct Ggx {
     float a;
+    // For unit h, h.z^2 (a^2 - 1) + 1 = a^2 h.z^2 + h.x^2 + h.y^2: the right-hand
+    // form has no cancellation near the peak (h.z -> 1), where FP32 loses the
+    // left-hand one for small alpha.
     MYPBR_DEV float D(float3 h) const {
         if (h.z <= 0.0f)
             return 0.0f;
-        float a2 = a * a, d = h.z * h.z * (a2 - 1.0f) + 1.0f;
+        float a2 = a * a, d = a2 * h.z * h.z + (h.x * h.x + h.y * h.y);
         return a2 / (kPi * d * d);
     }
+    // tan^2 of a unit w as (x^2 + y^2) / z^2, the same cancellation-free form
     MYPBR_DEV float lambda(float3 w) const {
         float c2 = w.z * w.z;
         if (c2 <= 0.0f)
             return 3.0e38f;
-        float t2 = fmaxf(0.0f, 1.0f - c2) / c2;
+        float t2 = (w.x * w.x + w.y * w.y) / c2;
         return 0.5f * (-1.0f + sqrtf(1.0f + a * a * t2));
     }
     MYPBR_DEV float G1(float3 w) const { return 1.0f / (1.0f + lambda(w)); }
@@ -342,21 +346,35 @@ struct Pdf {
     int n;
     Lobe lobe[3];
     float prob[3];
+    // Loops with a constant trip count and static indices keep the lobes in
+    // registers (a dynamically indexed array would live in local memory).
     MYPBR_DEV float value(float3 dir) const {
         float s = 0.0f;
-        for (int k = 0; k < n; k++)
-            if (prob[k] > 0.0f)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if (k < n && prob[k] > 0.0f)
                 s += prob[k] * lobe[k].value(dir);
         return s;
     }
     MYPBR_DEV float3 generate(Rng& g) const {
         float xi = g.next(), acc = 0.0f;
-        for (int k = 0; k < n - 1; k++) {
-            acc += prob[k];
-            if (xi < acc)
-                return lobe[k].generate(g);
+        int pick = n - 1;
+#pragma unroll
+        for (int k = 2; k >= 0; k--) {  // the first lobe whose running sum passes xi
+            float upto = 0.0f;
+#pragma unroll
+            for (int j = 0; j <= k; j++)
+                upto += prob[j];
+            if (k < n - 1 && xi < upto)
+                pick = k;
         }
-        return lobe[n - 1].generate(g);
+        (void)acc;
+        Lobe l = lobe[0];
+#pragma unroll
+        for (int k = 1; k < 3; k++)
+            if (pick == k)
+                l = lobe[k];
+        return l.generate(g);
     }
 };
 

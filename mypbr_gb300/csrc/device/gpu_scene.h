@@ -55,6 +55,7 @@ namespace mypbr_dev {
 void set_error_message(const std::string& m);
 int cuda_fail(cudaError_t e, const char* what);
 int release_buffers(RenderBuffers& rb);
+int check_device_error(mypbr_gpu_scene* G);
 
 }  // namespace mypbr_dev
 

@@ -94,7 +94,7 @@ extern "C" int mypbr_gpu_trace(mypbr_gpu_scene* G, const float* rays, int64_t n,
         k_trace<<<blocks, 128>>>(G->dev, rays, (long long)n, hits, prim);
         MYPBR_CUDA(cudaGetLastError());
         MYPBR_CUDA(cudaDeviceSynchronize());
-        return MYPBR_OK;
+        return check_device_error(G);
     }
     Buf dr, dh, dp;
     MYPBR_CUDA(cudaMalloc(&dr.p, size_t(n) * 8 * sizeof(float)));
@@ -106,7 +106,7 @@ extern "C" int mypbr_gpu_trace(mypbr_gpu_scene* G, const float* rays, int64_t n,
     MYPBR_CUDA(cudaGetLastError());
     MYPBR_CUDA(cudaMemcpy(hits, dh.p, size_t(n) * 8 * sizeof(float), cudaMemcpyDeviceToHost));
     MYPBR_CUDA(cudaMemcpy(prim, dp.p, size_t(n) * 2 * sizeof(int), cudaMemcpyDeviceToHost));
-    return MYPBR_OK;
+    return check_device_error(G);
 }
 
 extern "C" int mypbr_gpu_bsdf_eval(mypbr_gpu_scene* G, int32_t material, const float* rec, const float* r_in,
@@ -131,5 +131,5 @@ extern "C" int mypbr_gpu_bsdf_eval(mypbr_gpu_scene* G, int32_t material, const f
                             static_cast<float*>(c.p), (long long)n, static_cast<float*>(d.p));
     MYPBR_CUDA(cudaGetLastError());
     MYPBR_CUDA(cudaMemcpy(out, d.p, size_t(n) * 4 * sizeof(float), cudaMemcpyDeviceToHost));
-    return MYPBR_OK;
+    return check_device_error(G);
 }

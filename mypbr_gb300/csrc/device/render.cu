@@ -796,6 +796,7 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
         int s = T.collect(stats);
         if (s != MYPBR_OK)
             return s;
+        return check_device_error(G);
     }
     return MYPBR_OK;
 }
@@ -874,7 +875,7 @@ extern "C" int mypbr_gpu_render_ex(mypbr_gpu_scene* G, const mypbr_camera* cam, 
     if (channel_variance)
         MYPBR_CUDA(back(channel_variance, chv.p, 3));
     MYPBR_CUDA(cudaStreamSynchronize(st));
-    return MYPBR_OK;
+    return check_device_error(G);
 }
 
 extern "C" int mypbr_gpu_render(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* opts,

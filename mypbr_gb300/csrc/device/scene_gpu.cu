@@ -271,6 +271,7 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     // ---- BVH: child boxes stored in the parent
     std::vector<float4> nodes;
     std::vector<uint32_t> refs;
+    int interior = 0;
     D.has_bvh = F.bvh_prim_count > 0;
     if (D.has_bvh) {
         G.max_depth_bvh = bvh_depth(F);
@@ -280,7 +281,6 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
             return MYPBR_ERR_UNSUPPORTED;
         }
         std::vector<int> new_index(size_t(F.bvh_node_count), -1);
-        int interior = 0;
         for (int64_t k = 0; k < F.bvh_node_count; k++)
             if (F.bvh_nodes[k].count == 0)
                 new_index[size_t(k)] = interior++;
@@ -293,11 +293,15 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
             hi.w = ibits(n.count);
         };
         if (F.bvh_nodes[0].count > 0) {
-            // A root leaf: one node holding it, beside a box nothing can hit
+            // A root leaf: one node holding it twice. The second copy's box sits
+            // at +infinity on every axis, where the slab test fails for every
+            // ray (both slab distances are +inf or both -inf); and were it ever
+            // entered it would only test the same primitives again, never loop.
             float4 lo, hi;
             child_entry(0, lo, hi);
-            nodes = {lo, hi, make_float4(1e30f, 1e30f, 1e30f, ibits(0)),
-                     make_float4(-1e30f, -1e30f, -1e30f, ibits(0))};
+            float inf = INFINITY;
+            nodes = {lo, hi, make_float4(inf, inf, inf, lo.w), make_float4(inf, inf, inf, hi.w)};
+            interior = 1;
         } else {
             nodes.resize(size_t(interior) * 4);
             for (int64_t k = 0; k < F.bvh_node_count; k++) {
@@ -315,6 +319,13 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     }
     PUT(nodes, D.bvh);
     PUT(refs, D.leaf_refs);
+    D.bvh_node_count = interior;
+    {
+        std::vector<int> zero(1, 0);
+        const int* err = nullptr;
+        PUT(zero, err);
+        D.error = const_cast<int*>(err);
+    }
     G.leaf_ref_count = refs.size();
 
     // ---- primitives
@@ -573,6 +584,21 @@ extern "C" int mypbr_gpu_scene_create(const mypbr_flat_scene* scene, mypbr_gpu_s
         return MYPBR_ERR_OUT_OF_MEMORY;
     }
 }
+
+namespace mypbr_dev {
+// Reads and clears the sticky device error word after a synchronised call.
+int check_device_error(mypbr_gpu_scene* G) {
+    int e = 0;
+    MYPBR_CUDA(cudaMemcpy(&e, G->dev.error, sizeof e, cudaMemcpyDeviceToHost));
+    if (e == 0)
+        return MYPBR_OK;
+    int zero = 0;
+    MYPBR_CUDA(cudaMemcpy(G->dev.error, &zero, sizeof zero, cudaMemcpyHostToDevice));
+    set_error_message(e == 1 ? "device check: a BVH walk visited more nodes than the tree has"
+                             : "device check: a BVH walk overflowed its stack");
+    return MYPBR_ERR_DEVICE_CHECK;
+}
+}  // namespace mypbr_dev
 
 extern "C" void mypbr_gpu_scene_destroy(mypbr_gpu_scene* scene) {
     if (!scene)

@@ -61,13 +61,30 @@ def test_trace_matches_oracle_and_reference(scene_name, golden, scale):
     O = orc.OracleScene(sc)
     ohits, oprim = O.trace(rays)
     assert np.array_equal(oprim[:, 0] >= 0, g["hit"] > 0)
-    hits, prim = G.trace(rays.astype(np.float32))
+    # the device traces FP32 rays: the oracle answers for the same rounded rays
+    rays32 = rays.astype(np.float32)
+    rays = rays32.astype(np.float64)
+    ohits, oprim = O.trace(rays)
+    hits, prim = G.trace(rays32)
     ok = stable_mask(O, rays, scale)
+    # exact ties (coplanar surfaces such as a box bottom on the floor) have two
+    # correct answers: the oracle's BVH and brute-force walks then disagree
+    _, brute = O.trace(rays, brute_force=True)
+    ok &= np.all(brute == oprim, axis=1)
     assert ok.mean() > 0.98, f"only {ok.mean():.4f} of the rays are away from edges"
     np.testing.assert_array_equal(prim[ok], oprim[ok], err_msg="hit/miss or primitive id differs")
     both = ok & (prim[:, 0] >= 0)
+    # t to 1e-5 relative; where the hit is much closer than the coordinates are
+    # large, FP32 resolves t only to a few ulps of those coordinates, so the
+    # bound is 1e-5 t |d| or 4 ulps of the largest coordinate, whichever is larger
+    dlen = np.linalg.norm(rays[both, 3:6], axis=1)
+    dt = np.abs(hits[both, 0] - ohits[both, 0]) * dlen
+    coord = np.maximum(np.abs(rays[both, 0:3]).max(axis=1), scale)
+    bound = np.maximum(1e-5 * ohits[both, 0] * dlen, 4 * 2.0 ** -23 * coord)
+    worst = np.argsort(dt / bound)[-3:]
+    assert np.all(dt <= bound), (dt[worst], bound[worst], ohits[both][worst, 0])
     rel_t = np.abs(hits[both, 0] - ohits[both, 0]) / np.abs(ohits[both, 0])
-    assert rel_t.max() < 1e-5, rel_t.max()
+    assert np.median(rel_t) < 1e-6
     dn = np.abs(hits[both, 1:4] - ohits[both, 1:4]).max()
     assert dn < 1e-5, dn
     np.testing.assert_array_equal(hits[both, 6], ohits[both, 6])
@@ -83,17 +100,38 @@ def test_bsdf_matches_reference():
     rec[:, 6] = 1 - b["face"]
     rec[:, 7], rec[:, 8] = 0.25, 0.75
     rec[:, 9], rec[:, 13] = 2.0, 3.0
+    O = orc.OracleScene(sc)
+    rng = np.random.default_rng(5)
     for k in np.unique(b["sphere"]):
         m = b["sphere"] == k
-        out = G.bsdf_eval(int(mats[k]), rec[m], -b["wo"][m], b["wi"][m])
-        ev, pdf = b["eval"][m], b["pdf"][m]
-        # 1e-5 relative, with an absolute floor at 1e-5 of the largest value of
-        # this material (FP32 cannot resolve relative differences of values
-        # 1e5 times smaller than the lobe's peak)
+        mat = int(mats[k])
+        wo32 = (-b["wo"][m]).astype(np.float32).astype(np.float64)
+        wi32 = b["wi"][m].astype(np.float32).astype(np.float64)
+        out = G.bsdf_eval(mat, rec[m], wo32, wi32)
+        # The oracle at the same FP32-rounded directions matches the reference's
+        # values (pinned to 1e-12 on the unrounded grid in the CPU tests)
+        ref = O.bsdf(mat, rec[m], wo32, wi32)
+        ev, pdf = ref[:, :3], ref[:, 3]
+        np.testing.assert_allclose(O.bsdf(mat, rec[m], -b["wo"][m], b["wi"][m])[:, 3], b["pdf"][m], rtol=1e-12,
+                                   atol=1e-14)
+        # How far the FP64 answer itself moves when the directions move by one
+        # FP32 rounding: near a sharp lobe's peak that sensitivity, not the
+        # kernel, limits what FP32 can match
+        wiggle = np.zeros(len(wi32))
+        for _ in range(4):
+            d1 = wi32 * (1 + rng.choice([-1, 1], wi32.shape) * 2.0 ** -24)
+            d0 = wo32 * (1 + rng.choice([-1, 1], wo32.shape) * 2.0 ** -24)
+            wiggle = np.maximum(wiggle, np.abs(O.bsdf(mat, rec[m], d0, d1)[:, 3] - pdf))
         scale_e = max(np.abs(ev).max(), 1e-12)
         scale_p = max(np.abs(pdf).max(), 1e-12)
+        # 1e-5 relative, an absolute floor of 1e-5 of the material's largest
+        # value, or 8 times the FP32-rounding sensitivity, whichever is largest
         np.testing.assert_allclose(out[:, :3], ev, rtol=1e-5, atol=1e-5 * scale_e, err_msg=f"material {k} eval")
-        np.testing.assert_allclose(out[:, 3], pdf, rtol=1e-5, atol=1e-5 * scale_p, err_msg=f"material {k} pdf")
+        bound = np.maximum(np.maximum(1e-5 * np.abs(pdf), 1e-5 * scale_p), 8 * wiggle)
+        bad = np.abs(out[:, 3] - pdf) > bound
+        assert not bad.any(), (k, out[bad, 3], pdf[bad], wiggle[bad])
+        within_1e5 = np.abs(out[:, 3] - pdf) <= np.maximum(1e-5 * np.abs(pdf), 1e-5 * scale_p)
+        assert within_1e5.mean() > 0.99, (k, within_1e5.mean())
 
 
 FURNACE = """
@@ -218,8 +256,8 @@ def test_features_and_progressive_callback():
     f = cam.render(G, save_every=4, on_pass=lambda done, fr: seen.append((done, fr.radiance.mean())))
     assert [d for d, _ in seen] == [4, 8, 12]
     assert f.albedo.shape == (32, 32, 3) and f.normal.shape == (32, 32, 3) and f.variance.shape == (32, 32)
-    # Cornell: every camera ray hits a lambertian surface; albedo within the wall colours
-    assert f.albedo.min() >= 0 and f.albedo.max() <= 0.75
-    assert np.all(np.linalg.norm(f.normal, axis=2) <= 1 + 1e-9)
+    # albedo: a wall colour, or 1 where the camera ray escapes past the open front (camera.h:248-252)
+    assert f.albedo.min() >= 0 and f.albedo.max() <= 1.0 + 1e-12
+    assert np.all(np.linalg.norm(f.normal, axis=2) <= 1 + 1e-6)  # FP32 unit normals
     assert np.all(f.variance >= 0)
     cam.collect_features = 0
