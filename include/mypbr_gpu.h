@@ -429,6 +429,24 @@ int mypbr_gpu_render_ex(mypbr_gpu_scene* scene, const mypbr_camera* cam, const m
                         double* channel_variance, int save_every, mypbr_pass_callback on_pass, void* user,
                         mypbr_render_stats* stats);
 
+/* The render with no device allocation, for callers that may not allocate
+ * device memory while they render (a host that gives this library a fixed
+ * device-memory budget up front, or a per-frame callback where the
+ * synchronisation an allocation can cause would stall the frame). It has no
+ * counterpart in the reference. Every scratch buffer comes from one static
+ * 18 MiB device array in the library, present on every GPU that loads it until
+ * the library is unloaded; the scene comes from mypbr_gpu_scene_create and the
+ * outputs are caller-provided device buffers as for mypbr_gpu_render_device.
+ * Limits: at most 65,536 pixels in the rendered rows (256 x 256, say) and
+ * max_depth <= 1024; larger requests fail with MYPBR_ERR_INVALID_ARGUMENT.
+ * Calls share the array: it is cleared at the start of each call, and calls
+ * that overlap on the GPU race, so issue one at a time. The first call on a
+ * device looks up the array's address with that device current; make it
+ * before capturing any stream. Synchronous: returns when the frame is done. */
+int mypbr_gpu_render_noalloc(mypbr_gpu_scene* scene, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                             double* d_radiance, double* d_albedo, double* d_normal, double* d_variance,
+                             void* cuda_stream);
+
 /* Ray batch query: closest hit of n rays against the scene, the reference's
  * world.hit (hittable_list.h:25-37 over bvh.h:45-86 and scene::unbounded)
  * without media (media are stochastic). rays: n x 8 floats (ox oy oz dx dy dz

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -883,4 +884,171 @@ extern "C" int mypbr_gpu_render(mypbr_gpu_scene* G, const mypbr_camera* cam, con
                                 mypbr_pass_callback on_pass, void* user) {
     return mypbr_gpu_render_ex(G, cam, opts, radiance, albedo, normal, variance, nullptr, save_every, on_pass, user,
                                nullptr);
+}
+
+// ------------------------------------------------- render without allocation
+//
+// mypbr_gpu_render_noalloc: the same render, with every scratch buffer (path
+// state, queues, queue counters, FP64 film, ray totals) carved from one
+// file-scope device array instead of cudaMalloc. It serves callers that may
+// not allocate device memory while they render: a host application that hands
+// this library a fixed device-memory budget up front and forbids allocation
+// afterwards, or a per-frame callback of an interactive viewer in which the
+// device-wide synchronisation an allocation can cause would stall the frame.
+// The scene must already be on the device (mypbr_gpu_scene_create) and the
+// caller passes device output buffers.
+//
+// Limits: at most kNoAllocMaxPixels (65,536) pixels in the rendered rows,
+// max_depth at most kNoAllocMaxDepth. The array (kNoAllocBytes, 18 MiB) exists
+// on every GPU that loads this library, for as long as the library is loaded.
+// Every call reuses it and it keeps the previous call's contents, so the film
+// and counters are cleared at the start of each call; two calls whose work
+// overlaps on the GPU (different streams, or different host threads) race on
+// it and must not be issued. The first call on a device looks the array's
+// device address up (cudaGetSymbolAddress) with that device current; make that
+// first call before capturing any stream.
+
+namespace mypbr_dev {
+namespace {
+
+constexpr size_t kNoAllocMaxPixels = 65536;  // path slots and film pixels
+constexpr int kNoAllocMaxDepth = 1024;
+constexpr size_t kNoAllocAlign = 256;
+
+constexpr size_t align_up(size_t x) { return (x + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+constexpr size_t kSlotBytes = 9 * sizeof(float4) + sizeof(uint2) + 3 * sizeof(uint32_t);
+constexpr size_t kPixelBytes = (3 + 3 + 7) * sizeof(double);
+constexpr size_t kCounterBytes = (2 * (kNoAllocMaxDepth + 1) + 8) * sizeof(uint32_t);
+constexpr size_t kNoAllocNeed = 16 * kNoAllocAlign + kNoAllocMaxPixels * (kSlotBytes + kPixelBytes) + kCounterBytes +
+                                2 * sizeof(unsigned long long);
+constexpr size_t kNoAllocBytes = size_t(18) << 20;
+static_assert(kNoAllocNeed <= kNoAllocBytes, "scratch layout exceeds the static array");
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// The array's device address on the current device, looked up once per device.
+int noalloc_scratch(int device, unsigned char** out) {
+    if (device < 0 || device >= kMaxDevices)
+        return bad_arg("mypbr_gpu_render_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_ptr[device]);
+    return MYPBR_OK;
+}
+
+// Carves the render buffers out of the array (each start 256-byte aligned).
+RenderBuffers carve(unsigned char* base, unsigned long long** totals) {
+    RenderBuffers rb;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char* p = base + off;
+        off = align_up(off + bytes);
+        return p;
+    };
+    const size_t n = kNoAllocMaxPixels;
+    rb.ray_o = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.ray_d = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.beta = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.radiance = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.rng = reinterpret_cast<uint2*>(take(n * sizeof(uint2)));
+    rb.meta = reinterpret_cast<uint4*>(take(n * sizeof(uint4)));
+    rb.hit = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.sh_o = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.sh_d = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.sh_c = reinterpret_cast<float4*>(take(n * sizeof(float4)));
+    rb.queue[0] = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    rb.queue[1] = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    rb.shadow_queue = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    rb.counters = reinterpret_cast<uint32_t*>(take(kCounterBytes));
+    rb.film = reinterpret_cast<double*>(take(3 * n * sizeof(double)));
+    rb.film2 = reinterpret_cast<double*>(take(3 * n * sizeof(double)));
+    rb.feat = reinterpret_cast<double*>(take(7 * n * sizeof(double)));
+    *totals = reinterpret_cast<unsigned long long*>(take(2 * sizeof(unsigned long long)));
+    rb.capacity = n;
+    rb.pixels = n;
+    rb.depth_slots = kNoAllocMaxDepth + 1;
+    return rb;
+}
+
+}  // namespace
+}  // namespace mypbr_dev
+
+extern "C" int mypbr_gpu_render_noalloc(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* o,
+                                        double* d_radiance, double* d_albedo, double* d_normal, double* d_variance,
+                                        void* cuda_stream) {
+    if (!G || !cam || !o || !d_radiance)
+        return bad_arg("mypbr_gpu_render_noalloc: null argument");
+    if (cam->image_width < 1 || o->samples_per_pixel < 1 || o->max_depth < 1)
+        return bad_arg("mypbr_gpu_render_noalloc: image_width, samples_per_pixel and max_depth must be positive");
+    if (o->max_depth > kNoAllocMaxDepth)
+        return bad_arg("mypbr_gpu_render_noalloc: max_depth is limited to " + std::to_string(kNoAllocMaxDepth));
+    if (o->guided != 0) {
+        set_error_message("mypbr_gpu_render_noalloc: the guided sampler is not available in this build");
+        return MYPBR_ERR_UNSUPPORTED;
+    }
+    if (o->max_diffuse > 255 || o->max_specular > 255 || o->max_diffuse < 0 || o->max_specular < 0 ||
+        o->max_scatter < 0)
+        return bad_arg("mypbr_gpu_render_noalloc: bounce caps must be in [0, 255]");
+    MYPBR_CUDA(cudaSetDevice(G->device));
+    WaveParams P{};
+    P.S = G->dev;
+    P.cam = make_camera(*cam, o->samples_per_pixel);
+    size_t full = size_t(P.cam.width) * P.cam.height;
+    if (full > kNoAllocMaxPixels)
+        return bad_arg("mypbr_gpu_render_noalloc: " + std::to_string(P.cam.width) + " x " +
+                       std::to_string(P.cam.height) + " exceeds the " + std::to_string(kNoAllocMaxPixels) +
+                       "-pixel limit of the render without allocation");
+    P.first_row = o->first_row;
+    P.band_rows = o->row_count > 0 ? o->row_count : P.cam.height - o->first_row;
+    if (o->first_row < 0 || o->row_count < 0 || P.band_rows <= 0 || P.first_row + P.band_rows > P.cam.height)
+        return bad_arg("mypbr_gpu_render_noalloc: first_row / row_count outside the image");
+    P.max_depth = o->max_depth;
+    P.max_diffuse = o->max_diffuse;
+    P.max_specular = o->max_specular;
+    P.max_scatter = o->max_scatter;
+    P.transparent_shadows = o->transparent_shadows;
+    P.collect_features = o->collect_features;
+    P.has_lights = G->dev.light_count > 0;
+    P.seed = o->seed;
+    unsigned char* base = nullptr;
+    int s = noalloc_scratch(G->device, &base);
+    if (s != MYPBR_OK)
+        return s;
+    P.B = carve(base, &P.totals);
+    size_t npix = size_t(P.cam.width) * P.band_rows;
+    int spp = o->samples_per_pixel;
+    int per_wave = int(std::max<size_t>(1, kNoAllocMaxPixels / npix));
+    per_wave = std::min(per_wave, spp);
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    // The array keeps the last call's contents: clear what accumulates
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * full * sizeof(double), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * full * sizeof(double), st));
+    if (P.collect_features)
+        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * full * sizeof(double), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.totals, 0, 2 * sizeof(unsigned long long), st));
+    Launch L = launch_config(*G);
+    uint64_t launches = 0;
+    KernelTimer T;  // off: no events are created
+    T.st = st;
+    for (int pass0 = 0; pass0 < spp; pass0 += per_wave) {
+        P.pass0 = pass0;
+        P.npass = std::min(per_wave, spp - pass0);
+        s = run_wave(P, L, st, launches, T);
+        if (s != MYPBR_OK)
+            return s;
+    }
+    k_resolve<<<L.grid_stream, 256, 0, st>>>(P, spp, d_radiance, d_albedo, d_normal, d_variance);
+    MYPBR_CUDA(cudaGetLastError());
+    MYPBR_CUDA(cudaStreamSynchronize(st));
+    return check_device_error(G);
 }
