@@ -76,8 +76,8 @@ struct DeviceScene {
     const DevTexture* textures;
     const uint8_t* texels_ldr;
     const float* texels_hdr;
-    const float* ggx_e;     // 32 x 32
-    const float* ggx_eavg;  // 32
+    const float* ggx_e;     // 1 - E(mu, alpha), 32 x 32
+    const float* ggx_eavg;  // 1 - E_avg(alpha), 32
     // lights
     const DevLight* lights;
     const DevMember* members;

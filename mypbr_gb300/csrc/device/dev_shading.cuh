@@ -149,8 +149,12 @@ struct Ggx {
     }
 };
 
-// ggx_albedo_table (microfacet.h:276-293)
-MYPBR_DEV float table_E(const DeviceScene& S, float c, float alpha) {
+// ggx_albedo_table (microfacet.h:276-293). The device holds the complements
+// 1 - E and 1 - E_avg, computed in FP64 on the host: the compensation lobe
+// divides products of (1 - E) by (1 - E_avg), all near zero for smooth
+// surfaces, where forming 1 - E in FP32 would lose most digits. Bilinear
+// interpolation of 1 - E equals 1 minus the interpolated E.
+MYPBR_DEV float table_one_minus_E(const DeviceScene& S, float c, float alpha) {
     float x = clampf(c, 0.0f, 1.0f) * 31.0f, y = clampf(sqrtf(alpha), 0.0f, 1.0f) * 31.0f;
     int i = min(int(x), 30), j = min(int(y), 30);
     float tx = x - i, ty = y - j;
@@ -159,30 +163,32 @@ MYPBR_DEV float table_E(const DeviceScene& S, float c, float alpha) {
     float hi = (1.0f - tx) * e[(j + 1) * 32 + i] + tx * e[(j + 1) * 32 + i + 1];
     return (1.0f - ty) * lo + ty * hi;
 }
-MYPBR_DEV float table_Eavg(const DeviceScene& S, float alpha) {
+MYPBR_DEV float table_E(const DeviceScene& S, float c, float alpha) { return 1.0f - table_one_minus_E(S, c, alpha); }
+MYPBR_DEV float table_one_minus_Eavg(const DeviceScene& S, float alpha) {
     float y = clampf(sqrtf(alpha), 0.0f, 1.0f) * 31.0f;
     int j = min(int(y), 30);
     float ty = y - j;
     return (1.0f - ty) * S.ggx_eavg[j] + ty * S.ggx_eavg[j + 1];
 }
+MYPBR_DEV float table_Eavg(const DeviceScene& S, float alpha) { return 1.0f - table_one_minus_Eavg(S, alpha); }
 // microfacet.h:341-373
 MYPBR_DEV float ms_eval(const DeviceScene& S, float co, float ci, float alpha) {
     if (co <= 0.0f || ci <= 0.0f)
         return 0.0f;
-    float miss = 1.0f - table_Eavg(S, alpha);
+    float miss = table_one_minus_Eavg(S, alpha);
     if (miss < 1e-6f)
         return 0.0f;
-    return (1.0f - table_E(S, co, alpha)) * (1.0f - table_E(S, ci, alpha)) / (kPi * miss) * ci;
+    return table_one_minus_E(S, co, alpha) * table_one_minus_E(S, ci, alpha) / (kPi * miss) * ci;
 }
 MYPBR_DEV float ms_albedo(const DeviceScene& S, float co, float alpha) {
-    if (co <= 0.0f || 1.0f - table_Eavg(S, alpha) < 1e-6f)
+    if (co <= 0.0f || table_one_minus_Eavg(S, alpha) < 1e-6f)
         return 0.0f;
-    return 1.0f - table_E(S, co, alpha);
+    return table_one_minus_E(S, co, alpha);
 }
 MYPBR_DEV float3 ms_fresnel_avg(const DeviceScene& S, float3 fa, float alpha) {
-    float e = table_Eavg(S, alpha);
-    return f3(fa.x * fa.x * e / (1.0f - fa.x * (1.0f - e)), fa.y * fa.y * e / (1.0f - fa.y * (1.0f - e)),
-              fa.z * fa.z * e / (1.0f - fa.z * (1.0f - e)));
+    float m = table_one_minus_Eavg(S, alpha), e = 1.0f - m;
+    return f3(fa.x * fa.x * e / (1.0f - fa.x * m), fa.y * fa.y * e / (1.0f - fa.y * m),
+              fa.z * fa.z * e / (1.0f - fa.z * m));
 }
 MYPBR_DEV float3 ms_fresnel(const DeviceScene& S, float3 f0, float alpha) {
     return ms_fresnel_avg(S, f0 + (f3(1.0f) - f0) * (1.0f / 21.0f), alpha);

@@ -448,7 +448,12 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     std::vector<float> hdr(F.texels_hdr, F.texels_hdr + F.texels_hdr_count);
     PUT(hdr, D.texels_hdr);
     const auto& tab = ggx_table_cached();
-    std::vector<float> ge(tab.begin(), tab.begin() + 1024), ga(tab.begin() + 1024, tab.end());
+    // complements 1 - E and 1 - E_avg, formed in FP64 (see table_one_minus_E)
+    std::vector<float> ge(1024), ga(32);
+    for (int k = 0; k < 1024; k++)
+        ge[size_t(k)] = float(1.0 - tab[size_t(k)]);
+    for (int k = 0; k < 32; k++)
+        ga[size_t(k)] = float(1.0 - tab[size_t(1024 + k)]);
     PUT(ge, D.ggx_e);
     PUT(ga, D.ggx_eavg);
 
