@@ -70,6 +70,8 @@ struct DeviceScene {
     int unbounded_count;
     int has_bvh;
     int bvh_node_count;  // interior nodes; a walk visits each at most once
+    int has_media;       // media or height fog present (free-flight sampling needs keys)
+    const uint8_t* mat_class;  // shading class of each material
     int* error;          // sticky device error word (0 = none), read by the host after each call
     // appearance
     const DevMaterial* materials;

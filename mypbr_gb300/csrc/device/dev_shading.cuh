@@ -482,12 +482,14 @@ MYPBR_DEV float3 base_eval(const DeviceScene& S, const DevMaterial& m, const Pri
     return spec + ((1.0f - a.metallic) * tr * wi.z * kInvPi) * a.base;
 }
 
-// scatter() of the material itself (no normal-map wrapper)
+// scatter() of the material itself (no normal-map wrapper). ONLY >= 0 names
+// the material type at compile time, which leaves only that case in the code.
+template <int ONLY = -1>
 MYPBR_DEV bool scatter_inner(const DeviceScene& S, const DevMaterial& m, float3 r_dir, const Surface& rec,
                              ScatterRec& sr, Rng& g) {
     sr.skip_pdf = false;
     sr.pdf.n = 0;
-    switch (m.type) {
+    switch (ONLY >= 0 ? ONLY : m.type) {
         case kLambertian:  // material.h:79-85
             sr.attenuation = tex_value(S, m.tex[0], rec.u, rec.v, rec.p);
             sr.pdf.n = 1;
@@ -611,8 +613,9 @@ MYPBR_DEV bool scatter_inner(const DeviceScene& S, const DevMaterial& m, float3 
     }
 }
 
+template <int ONLY = -1>
 MYPBR_DEV float3 eval_inner(const DeviceScene& S, const DevMaterial& m, float3 r_dir, const Surface& rec, float3 dir) {
-    switch (m.type) {
+    switch (ONLY >= 0 ? ONLY : m.type) {
         case kLambertian: {  // material.h:88-97
             float c = dot(rec.normal, normalize(dir));
             return tex_value(S, m.tex[0], rec.u, rec.v, rec.p) * (c < 0.0f ? 0.0f : c * kInvPi);

@@ -16,25 +16,23 @@ struct RenderBuffers {
     size_t capacity = 0;   // path slots
     size_t pixels = 0;     // film pixels
     int depth_slots = 0;   // per-bounce queue counters
-    // path state (slot-indexed)
-    float4* ray_o = nullptr;     // origin, tmin
+    // path state (slot-indexed, 64 B)
+    float4* ray_o = nullptr;     // origin, path flags (bits)
     float4* ray_d = nullptr;     // direction, scatter pdf of the direction
-    float4* beta = nullptr;      // throughput, unused
-    float4* radiance = nullptr;  // path radiance so far, unused
-    uint2* rng = nullptr;        // PCG state
-    uint4* meta = nullptr;       // pixel, sample, flags (depth | specular | seen | counts), -
-    float4* hit = nullptr;       // t, b1, b2, prim bits
+    float4* beta = nullptr;      // throughput, pass (bits)
+    float4* radiance = nullptr;  // path radiance so far, pixel (bits)
+    float4* hit = nullptr;       // t, b1, b2, prim (bits)
     float4* sh_o = nullptr;      // shadow ray: origin, -
     float4* sh_d = nullptr;      // direction, final flag
     float4* sh_c = nullptr;      // contribution rgb, -
     uint32_t* queue[2] = {nullptr, nullptr};  // extension queues (ping-pong)
+    uint32_t* class_queue = nullptr;          // one queue per shading class, capacity each
     uint32_t* shadow_queue = nullptr;
-    uint32_t* counters = nullptr;             // [2 * depth_slots + 8]
+    uint32_t* counters = nullptr;
     // film (pixel-indexed, FP64 sums)
     double* film = nullptr;   // radiance sum rgb
     double* film2 = nullptr;  // radiance squared sum rgb
     double* feat = nullptr;   // albedo rgb, normal rgb, luminance^2 (7 per pixel)
-    int* error = nullptr;     // sticky device error word
 };
 
 }  // namespace mypbr_dev

@@ -27,8 +27,16 @@
 
 namespace mypbr_dev {
 
-constexpr uint32_t kFlagSpecular = 1u << 8;
-constexpr uint32_t kFlagSeen = 1u << 9;
+// Path flags, kept in the w lane of the origin: bit 0 specular, bit 1 seen by a
+// shadow ray, then the diffuse / specular / scatter bounce counts (8 bits each).
+constexpr uint32_t kFlagSpecular = 1u;
+constexpr uint32_t kFlagSeen = 2u;
+
+// Shading classes: each has its own queue and kernel, so a warp shades one
+// kind of material and each kernel carries only that material's code.
+constexpr int kShadeClasses = 6;
+enum : int { kClassMiss = 0, kClassLambert = 1, kClassMetal = 2, kClassDielectric = 3, kClassPrincipled = 4,
+             kClassGeneric = 5 };
 
 struct CameraParams {
     float3 center, p00, du, dv, wv, disk_u, disk_v;
@@ -41,16 +49,21 @@ struct WaveParams {
     CameraParams cam;
     RenderBuffers B;
     int max_depth, max_diffuse, max_specular, max_scatter;
-    int transparent_shadows, collect_features, has_lights, pad;
+    int transparent_shadows, collect_features, has_lights, has_media;
     unsigned long long seed;
     int pass0, npass;
     int first_row, band_rows;  // the rows rendered: [first_row, first_row + band_rows)
     unsigned long long* totals;  // extension rays, shadow rays
 };
 
-// Counter slots: extension queue length entering bounce d, shadow queue length of bounce d.
+// Counters: extension queue length entering bounce d; shadow queue length of
+// bounce d; length of shading class c's queue at bounce d.
 MYPBR_DEV uint32_t* ext_counter(const WaveParams& P, int d) { return P.B.counters + d; }
 MYPBR_DEV uint32_t* sh_counter(const WaveParams& P, int d) { return P.B.counters + P.B.depth_slots + d; }
+MYPBR_DEV uint32_t* class_counter(const WaveParams& P, int d, int c) {
+    return P.B.counters + 2 * P.B.depth_slots + d * kShadeClasses + c;
+}
+MYPBR_DEV uint32_t* class_queue(const WaveParams& P, int c) { return P.B.class_queue + size_t(c) * P.B.capacity; }
 
 // One atomic per warp: the active lanes that push get consecutive slots.
 MYPBR_DEV uint32_t warp_push(uint32_t* counter) {
@@ -62,6 +75,19 @@ MYPBR_DEV uint32_t warp_push(uint32_t* counter) {
         base = atomicAdd(counter, uint32_t(__popc(mask)));
     base = __shfl_sync(mask, base, leader);
     return base + uint32_t(__popc(mask & ((1u << lane) - 1u)));
+}
+
+// The same for lanes pushing to different counters: one atomic per distinct counter.
+MYPBR_DEV uint32_t warp_push_keyed(uint32_t* counter) {
+    unsigned mask = __activemask();
+    unsigned peers = __match_any_sync(mask, reinterpret_cast<unsigned long long>(counter));
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader)
+        base = atomicAdd(counter, uint32_t(__popc(peers)));
+    base = __shfl_sync(peers, base, leader);
+    return base + uint32_t(__popc(peers & ((1u << lane) - 1u)));
 }
 
 MYPBR_DEV void film_add(const WaveParams& P, uint32_t pixel, float3 c) {
@@ -82,8 +108,13 @@ MYPBR_DEV void film_add(const WaveParams& P, uint32_t pixel, float3 c) {
     }
 }
 
+// Keys of the random numbers: everything random in a path depends only on
+// (seed, pixel, pass, bounce, stage), never on where the path sits in a wave.
 MYPBR_DEV uint64_t media_key(const WaveParams& P, uint32_t pixel, uint32_t pass, uint32_t depth, uint32_t kind) {
     return mix64(P.seed ^ mix64((uint64_t(pixel) << 24) ^ (uint64_t(pass) << 8) ^ (uint64_t(depth) << 2) ^ kind)) | 1ull;
+}
+MYPBR_DEV Rng bounce_rng(const WaveParams& P, uint32_t pixel, uint32_t pass, int depth, uint32_t stage) {
+    return make_rng(P.seed ^ (0x9e3779b97f4a7c15ull * (uint64_t(depth) * 8 + stage + 1)), pixel, pass);
 }
 
 // camera.h:291-339: a ray through pixel (i, j) for pass `pass`, stratified over
@@ -129,6 +160,9 @@ MYPBR_DEV void camera_ray(const CameraParams& C, int i, int j, int pass, Rng& g,
     d = ps - o;
 }
 
+MYPBR_DEV float bits_f(uint32_t u) { return __uint_as_float(u); }
+MYPBR_DEV uint32_t f_bits(float f) { return __float_as_uint(f); }
+
 __global__ void k_generate(WaveParams P) {
     size_t npix = size_t(P.cam.width) * P.band_rows;
     size_t n = npix * size_t(P.npass);
@@ -141,23 +175,14 @@ __global__ void k_generate(WaveParams P) {
         Rng g = make_rng(P.seed, pixel, pass);
         float3 o, d;
         camera_ray(P.cam, i, j, int(pass), g, o, d);
-        P.B.ray_o[t] = make_float4(o.x, o.y, o.z, 0.001f);
+        P.B.ray_o[t] = make_float4(o.x, o.y, o.z, bits_f(kFlagSpecular));
         P.B.ray_d[t] = make_float4(d.x, d.y, d.z, 0.0f);
-        P.B.beta[t] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        P.B.radiance[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        P.B.rng[t] = make_uint2(uint32_t(g.state), uint32_t(g.state >> 32));
-        P.B.meta[t] = make_uint4(pixel, pass, kFlagSpecular, 0u);
+        P.B.beta[t] = make_float4(1.0f, 1.0f, 1.0f, bits_f(pass));
+        P.B.radiance[t] = make_float4(0.0f, 0.0f, 0.0f, bits_f(pixel));
         P.B.queue[0][t] = uint32_t(t);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
         *ext_counter(P, 0) = uint32_t(n);
-}
-
-MYPBR_DEV Rng load_rng(const WaveParams& P, uint32_t slot) {
-    uint2 s = P.B.rng[slot];
-    Rng g;
-    g.state = (uint64_t(s.y) << 32) | s.x;
-    return g;
 }
 
 // camera.h:253-277: albedo and normal of the first non-specular surface
@@ -166,13 +191,13 @@ __global__ void k_features(WaveParams P) {
     size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
         float4 ro = P.B.ray_o[t], rd = P.B.ray_d[t];
-        uint4 meta = P.B.meta[t];
+        uint32_t pixel = f_bits(P.B.radiance[t].w), pass = f_bits(P.B.beta[t].w);
         float3 o = f3(ro), d = f3(rd);
-        Rng g = make_rng(P.seed ^ 0x5bd1e995ull, meta.x, meta.y);
+        Rng g = make_rng(P.seed ^ 0x5bd1e995ull, pixel, pass);
         float3 tint = f3(1.0f), albedo = f3(1.0f), normal = f3(0.0f);
         bool done = false;
         for (int b = 0; b < 8 && !done; b++) {
-            HitInfo h = closest_hit(P.S, o, d, 0.001f, 3.0e38f, media_key(P, meta.x, meta.y, 100 + b, 3));
+            HitInfo h = closest_hit(P.S, o, d, 0.001f, 3.0e38f, media_key(P, pixel, pass, 100 + b, 3));
             if (h.prim == kMiss)
                 break;
             Surface s = make_surface(P.S, h, o, d);
@@ -196,7 +221,7 @@ __global__ void k_features(WaveParams P) {
             albedo = tint;
             normal = f3(0.0f);
         }
-        double* f = P.B.feat + 7 * size_t(meta.x);
+        double* f = P.B.feat + 7 * size_t(pixel);
         atomicAdd(f, double(albedo.x));
         atomicAdd(f + 1, double(albedo.y));
         atomicAdd(f + 2, double(albedo.z));
@@ -206,6 +231,19 @@ __global__ void k_features(WaveParams P) {
     }
 }
 
+// The material index of a hit primitive.
+MYPBR_DEV int hit_material(const DeviceScene& S, uint32_t prim) {
+    int kind = int(prim >> kKindShift), idx = int(prim & kIndexMask);
+    switch (kind) {
+        case kSphere: return __ldg(&S.sphere_info[idx].x);
+        case kQuad: return __float_as_int(ldg4(S.quads + 5 * idx).w);
+        case kTriangle: return __float_as_int(ldg4(S.tris + 3 * idx).w);
+        case kMedium: return __float_as_int(ldg4(S.media + 3 * idx + 2).y);
+        default: return S.unbounded[idx].material;
+    }
+}
+
+// Closest hits of the extension queue; each ray then joins its shading class's queue.
 __global__ void __launch_bounds__(256) k_extend(WaveParams P, int depth) {
     uint32_t n = *ext_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
@@ -215,37 +253,63 @@ __global__ void __launch_bounds__(256) k_extend(WaveParams P, int depth) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         uint32_t slot = q[k];
         float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
-        uint4 meta = P.B.meta[slot];
-        HitInfo h = closest_hit(P.S, f3(ro), f3(rd), ro.w, 3.0e38f, media_key(P, meta.x, meta.y, uint32_t(depth), 0));
+        uint64_t key = 0;
+        if (P.has_media) {
+            uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
+            key = media_key(P, pixel, pass, uint32_t(depth), 0);
+        }
+        HitInfo h = closest_hit(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
         P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
+        int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h.prim)]);
+        uint32_t* counter = class_counter(P, depth, c);
+        class_queue(P, c)[warp_push_keyed(counter)] = slot;
     }
 }
 
+// scatter() restricted to one class: the compiler keeps only that material's code.
+template <int C>
+constexpr int class_type() {
+    return C == kClassLambert ? kLambertian
+         : C == kClassMetal ? kMetal
+         : C == kClassDielectric ? kDielectric
+         : C == kClassPrincipled ? kPrincipled : -1;
+}
+template <int C>
+MYPBR_DEV bool class_scatter(const DeviceScene& S, int mi, float3 d, const Surface& s, ScatterRec& sr, Rng& g) {
+    if constexpr (C == kClassGeneric)
+        return scatter(S, mi, d, s, sr, g);
+    else
+        return scatter_inner<class_type<C>()>(S, S.materials[mi], d, s, sr, g);
+}
+template <int C>
+MYPBR_DEV float3 class_eval(const DeviceScene& S, int mi, float3 d, const Surface& s, float3 dir) {
+    if constexpr (C == kClassGeneric)
+        return eval(S, mi, d, s, dir);
+    else
+        return eval_inner<class_type<C>()>(S, S.materials[mi], d, s, dir);
+}
+
+// One bounce of ray_color (camera.h:370-457) for the paths of shading class C.
+template <int C>
 __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
-    uint32_t n = *ext_counter(P, depth);
-    const uint32_t* q = P.B.queue[depth & 1];
+    uint32_t n = *class_counter(P, depth, C);
+    const uint32_t* q = class_queue(P, C);
     uint32_t* q_next = P.B.queue[(depth + 1) & 1];
     const DeviceScene& S = P.S;
     uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         uint32_t slot = q[k];
-        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot], hb = P.B.hit[slot];
+        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
         float4 bt = P.B.beta[slot], rad4 = P.B.radiance[slot];
-        uint4 meta = P.B.meta[slot];
-        Rng g = load_rng(P, slot);
+        uint32_t pixel = f_bits(rad4.w), pass = f_bits(bt.w), flags = f_bits(ro.w);
         float3 o = f3(ro), d = f3(rd), beta = f3(bt), rad = f3(rad4);
         float scatter_pdf = rd.w;
-        bool specular = meta.z & kFlagSpecular, seen = meta.z & kFlagSeen;
-        uint32_t diffuse_count = (meta.z >> 16) & 0xff, specular_count = (meta.z >> 24) & 0xff;
-        uint32_t scatter_count = meta.w;
+        bool specular = flags & kFlagSpecular, seen = flags & kFlagSeen;
+        uint32_t diffuse_count = (flags >> 8) & 0xff, specular_count = (flags >> 16) & 0xff;
+        uint32_t scatter_count = flags >> 24;
         bool terminate = false, pushed_shadow = false;
         float3 new_o = o, new_d = d;
-        HitInfo h;
-        h.t = hb.x;
-        h.b1 = hb.y;
-        h.b2 = hb.z;
-        h.prim = __float_as_uint(hb.w);
-        if (h.prim == kMiss) {
+        if constexpr (C == kClassMiss) {
             // camera.h:373-387: the sky is a light, weighted like emission
             float3 sky = escaped_radiance(S, d, depth == 0);
             if (!seen) {
@@ -256,20 +320,30 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
             }
             terminate = true;
         } else {
+            Rng g = bounce_rng(P, pixel, pass, depth, 0);
+            float4 hb = P.B.hit[slot];
+            HitInfo h;
+            h.t = hb.x;
+            h.b1 = hb.y;
+            h.b2 = hb.z;
+            h.prim = __float_as_uint(hb.w);
             Surface s = make_surface(S, h, o, d);
             int mat = s.material;
-            beta *= interior_transmittance(S, mat, h.t * length(d), s.front);  // camera.h:396
-            if (!seen && may_emit(S, mat)) {                                   // camera.h:399-407
-                float3 em = emitted(S, mat, d, s);
-                if (nonzero(em)) {
-                    if (specular || !P.has_lights)
-                        rad += beta * em;
-                    else
-                        rad += beta * em * power_heuristic(scatter_pdf, lights_pdf(S, o, d));
+            if constexpr (C == kClassDielectric || C == kClassGeneric)  // camera.h:396
+                beta *= interior_transmittance(S, mat, h.t * length(d), s.front);
+            if constexpr (C == kClassGeneric) {  // camera.h:399-407
+                if (!seen && may_emit(S, mat)) {
+                    float3 em = emitted(S, mat, d, s);
+                    if (nonzero(em)) {
+                        if (specular || !P.has_lights)
+                            rad += beta * em;
+                        else
+                            rad += beta * em * power_heuristic(scatter_pdf, lights_pdf(S, o, d));
+                    }
                 }
             }
             ScatterRec sr;
-            if (!scatter(S, mat, d, s, sr, g)) {
+            if (!class_scatter<C>(S, mat, d, s, sr, g)) {
                 terminate = true;
             } else if (sr.skip_pdf) {  // camera.h:413-423
                 if (P.max_specular > 0 && ++specular_count > uint32_t(P.max_specular)) {
@@ -283,22 +357,22 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
                     specular = true;
                 }
             } else {  // camera.h:424-448
-                bool vol = is_volume(S, mat);
+                bool vol = (C == kClassGeneric) && is_volume(S, mat);
                 uint32_t& cnt = vol ? scatter_count : diffuse_count;
                 int cap = vol ? P.max_scatter : P.max_diffuse;
                 bool capped = cap > 0 && ++cnt >= uint32_t(cap);
                 bool last = depth == P.max_depth - 1 || capped;
                 seen = false;
-                if (P.has_lights) {  // camera.h:466-506, the shadow ray traced by k_shadow
+                if (P.has_lights) {  // camera.h:466-506; the shadow ray is traced by k_shadow
                     float3 to_light = lights_sample(S, s.p, g);
                     float lp = lights_pdf(S, s.p, to_light);
                     if (lp > 0.0f) {
-                        float3 f = eval(S, mat, d, s, to_light);
+                        float3 f = class_eval<C>(S, mat, d, s, to_light);
                         if (f.x > 0.0f || f.y > 0.0f || f.z > 0.0f) {
                             float w = last ? 1.0f : power_heuristic(lp, sr.pdf.value(to_light));
                             float3 c = beta * f * (w / lp);
                             float3 sd = normalize(to_light);
-                            P.B.sh_o[slot] = make_float4(s.p.x, s.p.y, s.p.z, 0.001f);
+                            P.B.sh_o[slot] = make_float4(s.p.x, s.p.y, s.p.z, 0.0f);
                             P.B.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
                             P.B.sh_c[slot] = make_float4(c.x, c.y, c.z, 0.0f);
                             P.B.shadow_queue[warp_push(sh_counter(P, depth))] = slot;
@@ -314,7 +388,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
                     if (!(spdf > 0.0f)) {
                         terminate = true;
                     } else {
-                        beta *= eval(S, mat, d, s, dir) / spdf;
+                        beta *= class_eval<C>(S, mat, d, s, dir) / spdf;
                         scatter_pdf = spdf;
                         new_o = s.p;
                         new_d = dir;
@@ -335,21 +409,19 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
         }
         if (terminate) {
             if (pushed_shadow) {
-                P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+                P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, rad4.w);
                 P.B.sh_d[slot].w = 1.0f;  // the shadow kernel finishes this path
             } else {
-                film_add(P, meta.x, rad);
+                film_add(P, pixel, rad);
             }
             continue;
         }
-        P.B.ray_o[slot] = make_float4(new_o.x, new_o.y, new_o.z, 0.001f);
+        uint32_t nflags = (specular ? kFlagSpecular : 0u) | (seen ? kFlagSeen : 0u) | (diffuse_count << 8) |
+                          (specular_count << 16) | (scatter_count << 24);
+        P.B.ray_o[slot] = make_float4(new_o.x, new_o.y, new_o.z, bits_f(nflags));
         P.B.ray_d[slot] = make_float4(new_d.x, new_d.y, new_d.z, scatter_pdf);
-        P.B.beta[slot] = make_float4(beta.x, beta.y, beta.z, 0.0f);
-        P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
-        P.B.rng[slot] = make_uint2(uint32_t(g.state), uint32_t(g.state >> 32));
-        uint32_t flags = (specular ? kFlagSpecular : 0u) | (seen ? kFlagSeen : 0u) | (diffuse_count << 16) |
-                         (specular_count << 24);
-        P.B.meta[slot] = make_uint4(meta.x, meta.y, flags, scatter_count);
+        P.B.beta[slot] = make_float4(beta.x, beta.y, beta.z, bt.w);
+        P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, rad4.w);
         q_next[warp_push(ext_counter(P, depth + 1))] = slot;
     }
 }
@@ -363,25 +435,25 @@ __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         uint32_t slot = P.B.shadow_queue[k];
         float4 so = P.B.sh_o[slot], sd = P.B.sh_d[slot], sc = P.B.sh_c[slot];
-        uint4 meta = P.B.meta[slot];
         float3 o = f3(so), d = f3(sd);
+        uint64_t key = 0;
+        uint32_t pixel = 0, pass = 0;
+        if (P.has_media) {
+            pixel = f_bits(P.B.radiance[slot].w);
+            pass = f_bits(P.B.beta[slot].w);
+        }
         float3 through = f3(1.0f), emission = f3(0.0f);
         for (int hop = 0; hop <= 16; hop++) {
-            HitInfo h = closest_hit(S, o, d, 0.001f, 3.0e38f, media_key(P, meta.x, meta.y, uint32_t(depth), 1 + 4 * hop));
+            if (P.has_media)
+                key = media_key(P, pixel, pass, uint32_t(depth), 1 + 4 * hop);
+            HitInfo h = closest_hit(S, o, d, 0.001f, 3.0e38f, key);
             if (h.prim == kMiss) {
                 emission = escaped_radiance(S, d, false);
                 break;
             }
             int kind = int(h.prim >> kKindShift);
-            int mat;
-            if (kind == kQuad)
-                mat = __float_as_int(ldg4(S.quads + 5 * (h.prim & kIndexMask)).w);
-            else if (kind == kTriangle)
-                mat = __float_as_int(ldg4(S.tris + 3 * (h.prim & kIndexMask)).w);
-            else if (kind == kSphere)
-                mat = S.sphere_info[h.prim & kIndexMask].x;
-            else
-                mat = -1;  // media, ground and fog neither emit nor let shadows through
+            int mat = (kind == kSphere || kind == kQuad || kind == kTriangle) ? hit_material(S, h.prim) : -1;
+            // media, the ground and fog neither emit nor let shadows through
             bool through_glass = P.transparent_shadows && hop < 16 && mat >= 0 && lets_shadows_through(S, mat);
             if (!through_glass && (mat < 0 || !may_emit(S, mat)))
                 break;  // blocked by something dark
@@ -394,12 +466,12 @@ __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
             emission = emitted(S, mat, d, s);
             break;
         }
-        float3 add = f3(sc) * through * emission;
-        float3 rad = f3(P.B.radiance[slot]) + add;
+        float4 r4 = P.B.radiance[slot];
+        float3 rad = f3(r4) + f3(sc) * through * emission;
         if (sd.w != 0.0f)
-            film_add(P, meta.x, rad);
+            film_add(P, f_bits(r4.w), rad);
         else
-            P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+            P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, r4.w);
     }
 }
 
@@ -454,14 +526,16 @@ __global__ void k_channel_variance(WaveParams P, int samples, double* out) {
 // ------------------------------------------------------------ host side
 
 int release_buffers(RenderBuffers& rb) {
-    void* ptrs[] = {rb.ray_o, rb.ray_d, rb.beta, rb.radiance, rb.rng, rb.meta, rb.hit, rb.sh_o, rb.sh_d, rb.sh_c,
-                    rb.queue[0], rb.queue[1], rb.shadow_queue, rb.counters, rb.film, rb.film2, rb.feat, rb.error};
+    void* ptrs[] = {rb.ray_o, rb.ray_d, rb.beta, rb.radiance, rb.hit, rb.sh_o, rb.sh_d, rb.sh_c, rb.queue[0],
+                    rb.queue[1], rb.class_queue, rb.shadow_queue, rb.counters, rb.film, rb.film2, rb.feat};
     for (void* p : ptrs)
         if (p)
             cudaFree(p);
     rb = RenderBuffers();
     return MYPBR_OK;
 }
+
+size_t counter_words(int depth_slots) { return size_t(depth_slots) * (2 + kShadeClasses) + 8; }
 
 namespace {
 
@@ -485,20 +559,18 @@ int ensure_buffers(RenderBuffers& rb, size_t capacity, size_t pixels, int depth_
     A(rb.ray_d, capacity);
     A(rb.beta, capacity);
     A(rb.radiance, capacity);
-    A(rb.rng, capacity);
-    A(rb.meta, capacity);
     A(rb.hit, capacity);
     A(rb.sh_o, capacity);
     A(rb.sh_d, capacity);
     A(rb.sh_c, capacity);
     A(rb.queue[0], capacity);
     A(rb.queue[1], capacity);
+    A(rb.class_queue, capacity * kShadeClasses);
     A(rb.shadow_queue, capacity);
-    A(rb.counters, size_t(2 * depth_slots + 8));
+    A(rb.counters, counter_words(depth_slots));
     A(rb.film, 3 * pixels);
     A(rb.film2, 3 * pixels);
     A(rb.feat, 7 * pixels);
-    A(rb.error, 1);
 #undef A
     if (s != MYPBR_OK) {
         release_buffers(rb);
@@ -565,11 +637,17 @@ Launch launch_config(const mypbr_gpu_scene& G) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend, 256, 0);
     L.grid_extend = G.sm_count * std::max(per_sm, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade, 256, 0);
-    L.grid_shade = G.sm_count * std::max(per_sm, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow, 256, 0);
     L.grid_shadow = G.sm_count * std::max(per_sm, 1);
     L.grid_stream = G.sm_count * 8;
+    int worst = 1;
+    for (auto f : {(const void*)k_shade<kClassMiss>, (const void*)k_shade<kClassLambert>,
+                   (const void*)k_shade<kClassMetal>, (const void*)k_shade<kClassDielectric>,
+                   (const void*)k_shade<kClassPrincipled>, (const void*)k_shade<kClassGeneric>}) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, 256, 0);
+        worst = std::max(worst, per_sm);
+    }
+    L.grid_shade = G.sm_count * worst;
     return L;
 }
 
@@ -644,7 +722,7 @@ struct KernelTimer {
 
 // Renders passes [pass0, pass0 + npass) of every pixel of the band into the film.
 int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T) {
-    MYPBR_CUDA(cudaMemsetAsync(P.B.counters, 0, sizeof(uint32_t) * size_t(2 * P.B.depth_slots + 8), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.counters, 0, sizeof(uint32_t) * counter_words(P.B.depth_slots), st));
     TIMED(0, (k_generate<<<L.grid_stream, 256, 0, st>>>(P)));
     launches++;
     if (P.collect_features) {
@@ -653,9 +731,14 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
     }
     for (int depth = 0; depth < P.max_depth; depth++) {
         TIMED(1, (k_extend<<<L.grid_extend, 256, 0, st>>>(P, depth)));
-        TIMED(2, (k_shade<<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassMiss><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassLambert><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassMetal><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassDielectric><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassPrincipled><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassGeneric><<<L.grid_shade, 256, 0, st>>>(P, depth)));
         TIMED(3, (k_shadow<<<L.grid_shadow, 256, 0, st>>>(P, depth)));
-        launches += 3;
+        launches += 2 + kShadeClasses;
     }
     MYPBR_CUDA(cudaGetLastError());
     return MYPBR_OK;
@@ -695,6 +778,7 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
     P.transparent_shadows = o->transparent_shadows;
     P.collect_features = o->collect_features;
     P.has_lights = G->dev.light_count > 0;
+    P.has_media = G->dev.has_media;
     P.seed = o->seed;
     if (size_t(P.cam.width) * P.cam.height > (size_t(1) << 31))
         return bad_arg("mypbr_gpu_render: image too large");
@@ -705,9 +789,9 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
     R.npix = size_t(P.cam.width) * P.band_rows;
     R.timing = o->timing != 0;
     R.spp = o->samples_per_pixel;
-    // About 8M paths in flight per wave (or what the caller asks)
+    // About 32M paths in flight per wave (or what the caller asks)
     int per_wave = o->samples_per_wave > 0 ? o->samples_per_wave
-                                           : int(std::max<size_t>(1, (size_t(8) << 20) / std::max<size_t>(R.npix, 1)));
+                                           : int(std::max<size_t>(1, (size_t(32) << 20) / std::max<size_t>(R.npix, 1)));
     per_wave = std::min(per_wave, R.spp);
     if (save_every > 0)
         per_wave = std::min(per_wave, save_every);
@@ -916,9 +1000,9 @@ constexpr int kNoAllocMaxDepth = 1024;
 constexpr size_t kNoAllocAlign = 256;
 
 constexpr size_t align_up(size_t x) { return (x + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
-constexpr size_t kSlotBytes = 9 * sizeof(float4) + sizeof(uint2) + 3 * sizeof(uint32_t);
+constexpr size_t kSlotBytes = 8 * sizeof(float4) + (3 + kShadeClasses) * sizeof(uint32_t);
 constexpr size_t kPixelBytes = (3 + 3 + 7) * sizeof(double);
-constexpr size_t kCounterBytes = (2 * (kNoAllocMaxDepth + 1) + 8) * sizeof(uint32_t);
+constexpr size_t kCounterBytes = ((2 + kShadeClasses) * (kNoAllocMaxDepth + 1) + 8) * sizeof(uint32_t);
 constexpr size_t kNoAllocNeed = 16 * kNoAllocAlign + kNoAllocMaxPixels * (kSlotBytes + kPixelBytes) + kCounterBytes +
                                 2 * sizeof(unsigned long long);
 constexpr size_t kNoAllocBytes = size_t(18) << 20;
@@ -960,14 +1044,13 @@ RenderBuffers carve(unsigned char* base, unsigned long long** totals) {
     rb.ray_d = reinterpret_cast<float4*>(take(n * sizeof(float4)));
     rb.beta = reinterpret_cast<float4*>(take(n * sizeof(float4)));
     rb.radiance = reinterpret_cast<float4*>(take(n * sizeof(float4)));
-    rb.rng = reinterpret_cast<uint2*>(take(n * sizeof(uint2)));
-    rb.meta = reinterpret_cast<uint4*>(take(n * sizeof(uint4)));
     rb.hit = reinterpret_cast<float4*>(take(n * sizeof(float4)));
     rb.sh_o = reinterpret_cast<float4*>(take(n * sizeof(float4)));
     rb.sh_d = reinterpret_cast<float4*>(take(n * sizeof(float4)));
     rb.sh_c = reinterpret_cast<float4*>(take(n * sizeof(float4)));
     rb.queue[0] = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     rb.queue[1] = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
+    rb.class_queue = reinterpret_cast<uint32_t*>(take(kShadeClasses * n * sizeof(uint32_t)));
     rb.shadow_queue = reinterpret_cast<uint32_t*>(take(n * sizeof(uint32_t)));
     rb.counters = reinterpret_cast<uint32_t*>(take(kCounterBytes));
     rb.film = reinterpret_cast<double*>(take(3 * n * sizeof(double)));
@@ -1019,6 +1102,7 @@ extern "C" int mypbr_gpu_render_noalloc(mypbr_gpu_scene* G, const mypbr_camera* 
     P.transparent_shadows = o->transparent_shadows;
     P.collect_features = o->collect_features;
     P.has_lights = G->dev.light_count > 0;
+    P.has_media = G->dev.has_media;
     P.seed = o->seed;
     unsigned char* base = nullptr;
     int s = noalloc_scratch(G->device, &base);

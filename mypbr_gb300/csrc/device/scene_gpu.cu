@@ -427,6 +427,28 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
         mats.push_back(d);
     }
     PUT(mats, D.materials);
+    // Shading classes (render.cu): 1 lambertian, 2 metal, 3 dielectric,
+    // 4 principled, 5 everything else (wrappers, lights, thin glass, media)
+    std::vector<uint8_t> cls;
+    for (int64_t k = 0; k < F.material_count; k++) {
+        const auto& m = F.materials[k];
+        bool plain = m.emission_tex < 0 && (m.normal_map < 0 || m.type == MYPBR_MAT_PRINCIPLED);
+        uint8_t c = 5;
+        if (plain && m.type == MYPBR_MAT_LAMBERTIAN)
+            c = 1;
+        else if (plain && m.type == MYPBR_MAT_METAL)
+            c = 2;
+        else if (plain && m.type == MYPBR_MAT_DIELECTRIC)
+            c = 3;
+        else if (plain && m.type == MYPBR_MAT_PRINCIPLED)
+            c = 4;
+        cls.push_back(c);
+    }
+    PUT(cls, D.mat_class);
+    D.has_media = F.medium_count > 0;
+    for (int64_t k = 0; k < F.unbounded_count; k++)
+        if (F.unbounded[k].kind == MYPBR_UNBOUNDED_HEIGHT_FOG)
+            D.has_media = 1;
     std::vector<DevTexture> texs;
     for (int64_t k = 0; k < F.texture_count; k++) {
         const auto& t = F.textures[k];
