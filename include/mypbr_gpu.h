@@ -69,8 +69,44 @@ enum {
     MYPBR_PRIM_SPHERE = 0,   /* include/sphere.h:23-52 */
     MYPBR_PRIM_QUAD = 1,     /* include/quad.h:30-81 */
     MYPBR_PRIM_TRIANGLE = 2, /* include/mesh.h:47-108 */
-    MYPBR_PRIM_MEDIUM = 3    /* include/medium.h:60-88 */
+    MYPBR_PRIM_MEDIUM = 3,   /* include/medium.h:60-88 */
+    MYPBR_PRIM_VOXEL_BLOCK = 4 /* include/voxel.h:193-268 */
 };
+
+/* Voxel kinds (include/voxel.h:21): a surface lies where neighbouring cells
+ * differ in kind, opaque cells showing faces towards empty and transparent
+ * ones, transparent cells towards empty ones only. */
+enum { MYPBR_VOXEL_EMPTY = 0, MYPBR_VOXEL_OPAQUE = 1, MYPBR_VOXEL_TRANSPARENT = 2 };
+
+/* One palette entry of a voxel model: the material of that palette index and
+ * its kind. A model's palette is 256 consecutive entries. */
+typedef struct mypbr_voxel_entry {
+    int32_t material;
+    int32_t kind;
+} mypbr_voxel_entry;
+
+/* A placed voxel model (include/voxel.h:164-268): nx*ny*nz palette indices at
+ * `cells` in voxel_cells (x fastest, then y, then z; cell (x, y, z) covers
+ * [x, x+1] x [y, y+1] x [z, z+1] in model space), placed in the world by
+ * transform `xform` (model -> world). Instances of one model share cells.
+ * edge_material >= 0 draws the outlines of the shapes edge_width wide
+ * (voxel.h:313-331). */
+typedef struct mypbr_voxel_model {
+    int32_t nx, ny, nz;
+    int32_t xform;
+    int64_t cells;
+    int32_t palette;       /* first of 256 entries in voxel_palettes */
+    int32_t edge_material;
+    double edge_width;
+} mypbr_voxel_model;
+
+/* A block of a model, cells [lo, hi), walked by a 3D DDA (voxel.h:356-382);
+ * blocks are the BVH primitives of voxel models. */
+typedef struct mypbr_voxel_block {
+    int32_t model;
+    int32_t lo[3], hi[3];
+    int32_t reserved;
+} mypbr_voxel_block;
 
 /* An affine map p -> M p + t with its inverse, as the reference's transform
  * (include/transform.h:72-173). */
@@ -315,6 +351,12 @@ typedef struct mypbr_flat_scene {
     int32_t use_sky;
     int32_t reserved1;
     double background[3];
+
+    /* Voxel models (MYPBR_PRIM_VOXEL_BLOCK primitives index voxel_blocks). */
+    const mypbr_voxel_model* voxel_models;   int64_t voxel_model_count;
+    const mypbr_voxel_block* voxel_blocks;   int64_t voxel_block_count;
+    const mypbr_voxel_entry* voxel_palettes; int64_t voxel_palette_count;
+    const uint8_t* voxel_cells;              int64_t voxel_cell_bytes;
 } mypbr_flat_scene;
 
 /* --------------------------------------------------------------- camera */
@@ -451,8 +493,9 @@ int mypbr_gpu_render_noalloc(mypbr_gpu_scene* scene, const mypbr_camera* cam, co
  * world.hit (hittable_list.h:25-37 over bvh.h:45-86 and scene::unbounded)
  * without media (media are stochastic). rays: n x 8 floats (ox oy oz dx dy dz
  * tmin tmax), device or host memory as `on_device` says. hits: n x 8 floats
- * (t, nx, ny, nz, u, v, front_face, unused) and prim: n x 2 int32 (kind,
- * index; kind -1 on a miss; the ground plane reports kind 4). */
+ * (t, nx, ny, nz, u, v, front_face, material) and prim: n x 2 int32 (kind,
+ * index; kind -1 on a miss; a voxel face reports its block; the ground plane
+ * reports kind 5). */
 int mypbr_gpu_trace(mypbr_gpu_scene* scene, const float* rays, int64_t n, float* hits, int32_t* prim,
                     int on_device);
 
@@ -464,6 +507,26 @@ int mypbr_gpu_trace(mypbr_gpu_scene* scene, const float* rays, int64_t n, float*
  * Host memory. */
 int mypbr_gpu_bsdf_eval(mypbr_gpu_scene* scene, int32_t material, const float* rec, const float* r_in,
                         const float* wi, int64_t n, float* out);
+
+/* ------------------------------------------------------------- denoiser */
+
+/* The settings of the reference's denoiser (include/denoiser.h:39-43). */
+typedef struct mypbr_denoise_opts {
+    int32_t iterations;       /* a-trous passes, taps 2^i apart (5) */
+    int32_t reserved;
+    double sigma_luminance;   /* in standard deviations of the noise (4) */
+    double sigma_normal;      /* distance between normals (0.1) */
+    double sigma_albedo;      /* distance between albedos (0.1) */
+} mypbr_denoise_opts;
+
+void mypbr_denoise_opts_init(mypbr_denoise_opts* opts);
+
+/* denoiser::run (include/denoiser.h:45-75): filters a frame's radiance with
+ * its albedo, normal and variance guides (W*H*3, W*H*3, W*H*3, W*H doubles,
+ * rows from the top left) into out (W*H*3). opts may be NULL (defaults).
+ * Pointers are device memory if on_device, else host memory. Synchronous. */
+int mypbr_gpu_denoise(const double* radiance, const double* albedo, const double* normal, const double* variance,
+                      int32_t width, int32_t height, const mypbr_denoise_opts* opts, double* out, int on_device);
 
 #ifdef __cplusplus
 }

@@ -39,6 +39,14 @@ MYPBR_HD float len2(float3 a) { return dot(a, a); }
 MYPBR_DEV float length(float3 a) { return sqrtf(dot(a, a)); }
 MYPBR_DEV float3 normalize(float3 a) { return a * rsqrtf(dot(a, a)); }
 MYPBR_HD float comp(float3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+MYPBR_HD void set_comp(float3& a, int i, float v) {
+    if (i == 0)
+        a.x = v;
+    else if (i == 1)
+        a.y = v;
+    else
+        a.z = v;
+}
 MYPBR_HD float maxc(float3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
 MYPBR_HD float avg3(float3 a) { return (a.x + a.y + a.z) * (1.0f / 3.0f); }
 MYPBR_HD float luminance(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }

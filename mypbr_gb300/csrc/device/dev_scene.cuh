@@ -14,15 +14,28 @@
 //               indices in tri_shading (n0 n1 n2 t0) (t1 t2 - -).
 //   media       3 float4: (a | density), (b | shape), (xform, material, -, -).
 //   xforms      6 float4: forward rows (m | t), inverse rows (m^-1 | t^-1).
+//   voxels      a model record each (DevVoxelModel); 2 int4 per block:
+//               (model, lo xyz), (hi xyz, -); (material, kind) per palette
+//               entry, 256 per model; one byte per cell, x fastest.
 #pragma once
 
 #include "dev_math.cuh"
 
 namespace mypbr_dev {
 
-enum : int { kSphere = 0, kQuad = 1, kTriangle = 2, kMedium = 3, kGround = 4, kHeightFog = 5 };
+// Primitive kinds in leaf references and hits: 0-4 as the flat scene's
+// MYPBR_PRIM_*, then the unbounded objects tested beside the tree.
+enum : int { kSphere = 0, kQuad = 1, kTriangle = 2, kMedium = 3, kVoxel = 4, kGround = 5, kHeightFog = 6 };
+
+struct DevVoxelModel {
+    int nx, ny, nz, xform;
+    long long cells;  // offset into voxel_cells
+    int palette, edge_material;
+    float edge_width, pad0, pad1, pad2;
+};
 
 constexpr int kBvhStack = 64;
+constexpr int kVoxelBlockMax = 64;  // cells along each side of a voxel block, at most
 constexpr uint32_t kKindShift = 29;
 constexpr uint32_t kIndexMask = (1u << kKindShift) - 1;
 
@@ -67,10 +80,16 @@ struct DeviceScene {
     const float4* media;
     const float4* xforms;
     const DevUnbounded* unbounded;
+    const DevVoxelModel* voxel_models;
+    const int4* voxel_blocks;      // 2 per block: (model, lo xyz), (hi xyz, -)
+    const int2* voxel_palettes;    // (material, kind) per palette entry
+    const uint8_t* voxel_cells;
     int unbounded_count;
     int has_bvh;
     int bvh_node_count;  // interior nodes; a walk visits each at most once
     int has_media;       // media or height fog present (free-flight sampling needs keys)
+    int has_emitters;    // some hittable surface can emit (diffuse light or emissive texture)
+    int has_clear_glass; // some hittable surface lets shadows through (smooth dielectric)
     const uint8_t* mat_class;  // shading class of each material
     int* error;          // sticky device error word (0 = none), read by the host after each call
     // appearance
@@ -328,6 +347,157 @@ MYPBR_DEV bool hit_medium(const DeviceScene& S, int i, float3 o, float3 d, float
     return true;
 }
 
+// ----------------------------------------------------------------- voxels
+
+MYPBR_DEV int voxel_kind(const DeviceScene& S, int palette, int idx) { return __ldg(&S.voxel_palettes[palette + idx].y); }
+
+// The palette index of a cell of the whole model, 0 outside it (voxel.h:284-288).
+MYPBR_DEV int voxel_at(const DevVoxelModel& m, const uint8_t* cells, const int c[3]) {
+    if (unsigned(c[0]) >= unsigned(m.nx) || unsigned(c[1]) >= unsigned(m.ny) || unsigned(c[2]) >= unsigned(m.nz))
+        return 0;
+    return __ldg(cells + (size_t(c[2]) * m.ny + c[1]) * m.nx + c[0]);
+}
+
+MYPBR_DEV bool voxel_face_visible(int k, int n) {  // voxel.h:100-106
+    if (k == 0)
+        return false;
+    if (n == 0)
+        return true;
+    return k == 1 && n == 2;
+}
+
+// on_edge (voxel.h:313-331): within width of an outline of the shapes.
+MYPBR_DEV bool voxel_on_edge(const DeviceScene& S, const DevVoxelModel& m, const uint8_t* cells, float3 p, int axis,
+                             int sign, const int cell[3]) {
+    int k = voxel_kind(S, m.palette, voxel_at(m, cells, cell));
+    for (int side = 1; side <= 2; side++) {
+        int tangent = (axis + side) % 3;
+        float f = comp(p, tangent) - float(cell[tangent]);
+        for (int dir = -1; dir <= 1; dir += 2) {
+            if ((dir > 0 ? 1.0f - f : f) >= m.edge_width)
+                continue;
+            int beside[3] = {cell[0], cell[1], cell[2]};
+            beside[tangent] += dir;
+            int above[3] = {beside[0], beside[1], beside[2]};
+            above[axis] += sign;
+            if (voxel_face_visible(k, voxel_kind(S, m.palette, voxel_at(m, cells, beside))) ||
+                voxel_kind(S, m.palette, voxel_at(m, cells, above)) != 0)
+                return true;
+        }
+    }
+    return false;
+}
+
+// Block i of a placed voxel model, walked cell by cell with a 3D DDA
+// (Amanatides and Woo 1987) in the model's space, as voxel_grid::hit
+// (voxel.h:193-268). A surface is a crossing between cells of different kind
+// (crossing, voxel.h:294-305). On a hit: t, the material (the cell's palette
+// entry, or the outline's) and face = axis | (outward normal positive) << 2.
+MYPBR_DEV bool hit_voxel_block(const DeviceScene& S, int i, float3 ow, float3 dw, float tmin, float tmax, float& t_out,
+                               int& mat_out, int& face_out) {
+    int4 b0 = __ldg(S.voxel_blocks + 2 * i), b1 = __ldg(S.voxel_blocks + 2 * i + 1);
+    const DevVoxelModel m = S.voxel_models[b0.x];
+    XformRef X;
+    load_xform(S, m.xform, X);
+    float3 o = xf_ipoint(X, ow), d = xf_ivec(X, dw);
+    int lo[3] = {b0.y, b0.z, b0.w}, hi[3] = {b1.x, b1.y, b1.z};
+    const uint8_t* cells = S.voxel_cells + m.cells;
+    float t_enter = -3.0e38f, t_exit = 3.0e38f;
+    int enter_axis = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float da = comp(d, a), oa = comp(o, a);
+        if (da == 0.0f) {
+            if (oa < lo[a] || oa > hi[a])
+                return false;
+            continue;
+        }
+        float t0 = (lo[a] - oa) / da, t1 = (hi[a] - oa) / da;
+        if (t0 > t1) {
+            float tmp = t0;
+            t0 = t1;
+            t1 = tmp;
+        }
+        if (t0 > t_enter) {
+            t_enter = t0;
+            enter_axis = a;
+        }
+        t_exit = fminf(t_exit, t1);
+    }
+    bool from_outside = t_enter >= tmin;
+    float t_start = from_outside ? t_enter : tmin;
+    if (t_start > fminf(t_exit, tmax))
+        return false;
+    float3 start = o + t_start * d;
+    int c[3], step[3];
+    float t_next[3], t_delta[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float da = comp(d, a), oa = comp(o, a);
+        c[a] = min(max(int(floorf(comp(start, a))), lo[a]), hi[a] - 1);
+        if (from_outside && a == enter_axis)
+            c[a] = da > 0.0f ? lo[a] : hi[a] - 1;
+        if (da > 0.0f) {
+            step[a] = 1;
+            t_next[a] = (c[a] + 1 - oa) / da;
+            t_delta[a] = 1.0f / da;
+        } else if (da < 0.0f) {
+            step[a] = -1;
+            t_next[a] = (c[a] - oa) / da;
+            t_delta[a] = -1.0f / da;
+        } else {
+            step[a] = 0;
+            t_next[a] = t_delta[a] = 3.0e38f;
+        }
+    }
+    // A crossing at t along axis (step +-1) from a cell of palette index
+    // `from` into cell to_cell of index `to`: the entered cell's face, or the
+    // face of the cell being left seen from inside.
+    auto crossing = [&](float t, int axis, int stp, int from, int to, const int to_cell[3]) {
+        int k_from = voxel_kind(S, m.palette, from), k_to = voxel_kind(S, m.palette, to);
+        int sign, idx, cell[3] = {to_cell[0], to_cell[1], to_cell[2]};
+        if (k_to != 0 && voxel_face_visible(k_to, k_from)) {
+            sign = -stp;
+            idx = to;
+        } else if (voxel_face_visible(k_from, k_to)) {
+            sign = stp;
+            idx = from;
+            cell[axis] -= stp;
+        } else {
+            return false;
+        }
+        t_out = t;
+        face_out = axis | (sign > 0 ? 4 : 0);
+        mat_out = __ldg(&S.voxel_palettes[m.palette + idx].x);
+        if (m.edge_width > 0.0f && voxel_on_edge(S, m, cells, o + t * d, axis, sign, cell))
+            mat_out = m.edge_material;
+        return true;
+    };
+    int index = voxel_at(m, cells, c);
+    if (from_outside) {
+        int behind[3] = {c[0], c[1], c[2]};
+        behind[enter_axis] -= step[enter_axis];
+        if (crossing(t_enter, enter_axis, step[enter_axis], voxel_at(m, cells, behind), index, c))
+            return true;
+    }
+    // The walk stays inside the block: at most its three extents of steps
+    for (int guard = 0; guard < 3 * kVoxelBlockMax + 4; guard++) {
+        int a = t_next[0] < t_next[1] ? (t_next[0] < t_next[2] ? 0 : 2) : (t_next[1] < t_next[2] ? 1 : 2);
+        float t = t_next[a];
+        if (t > tmax)
+            return false;
+        c[a] += step[a];
+        t_next[a] += t_delta[a];
+        int next = voxel_at(m, cells, c);
+        if (crossing(t, a, step[a], index, next, c))
+            return true;
+        if (c[a] < lo[a] || c[a] >= hi[a])
+            return false;
+        index = next;
+    }
+    return false;
+}
+
 // ------------------------------------------------------------- traversal
 
 struct HitInfo {
@@ -342,7 +512,22 @@ MYPBR_DEV float safe_inv(float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysi
 // unbounded objects beside it (main.cpp:70-74 of the reference). media_key
 // seeds free-flight sampling in media; media_key == 0 skips media (used by the
 // deterministic ray-batch query).
+template <bool ANY>
+MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key);
+
 MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
+    return walk<false>(S, o, d, tmin, tmax, media_key);
+}
+
+// Whether anything at all lies along o + t d, t in (tmin, tmax): the walk stops
+// at the first primitive it hits. For shadow rays in scenes where nothing
+// hittable can emit, this is all the reference's closest-hit query decides.
+MYPBR_DEV bool any_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
+    return walk<true>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
+}
+
+template <bool ANY>
+MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
     HitInfo h;
     h.prim = kMiss;
     h.t = tmax;
@@ -400,12 +585,19 @@ MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tm
                         got = hit_quad(S, idx, o, d, tmin, h.t, t, b1, b2);
                     } else if (kind == kMedium && media_key != 0) {
                         got = hit_medium(S, idx, o, d, tmin, h.t, hash_uniform(media_key, uint32_t(idx)), t);
+                    } else if (kind == kVoxel) {
+                        int mat, face;
+                        got = hit_voxel_block(S, idx, o, d, tmin, h.t, t, mat, face);
+                        b1 = __int_as_float(mat);
+                        b2 = __int_as_float(face);
                     }
                     if (got) {
                         h.t = t;
                         h.b1 = b1;
                         h.b2 = b2;
                         h.prim = ref;
+                        if (ANY)
+                            return h;
                     }
                 }
             }
@@ -440,6 +632,8 @@ MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tm
             if (t > tmin && t < h.t) {
                 h.t = t;
                 h.prim = (uint32_t(kGround) << kKindShift) | uint32_t(k);
+                if (ANY)
+                    return h;
             }
         } else if (media_key != 0) {
             float len = length(d);
@@ -460,6 +654,8 @@ MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tm
             if (t < h.t && isfinite(t)) {
                 h.t = t;
                 h.prim = (uint32_t(kHeightFog) << kKindShift) | uint32_t(k);
+                if (ANY)
+                    return h;
             }
         }
     }
@@ -586,6 +782,31 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
         }
     } else if (kind == kMedium) {
         s.material = __float_as_int(ldg4(S.media + 3 * idx + 2).y);
+    } else if (kind == kVoxel) {
+        // voxel_grid::record (voxel.h:333-350) in the model's space, then the
+        // placement as instance::hit does (instance.h:29-40)
+        s.material = __float_as_int(h.b1);
+        int face = __float_as_int(h.b2), axis = face & 3;
+        float sign = (face & 4) ? 1.0f : -1.0f;
+        const DevVoxelModel& m = S.voxel_models[__ldg(&S.voxel_blocks[2 * idx].x)];
+        XformRef X;
+        load_xform(S, m.xform, X);
+        float3 lp = xf_ipoint(X, o) + h.t * xf_ivec(X, d);
+        float3 outward = f3(0.0f), tb = f3(0.0f), tc = f3(0.0f);
+        set_comp(outward, axis, sign);
+        set_comp(tb, (axis + 1) % 3, 1.0f);
+        set_comp(tc, (axis + 2) % 3, 1.0f);
+        float3 du = sign > 0.0f ? tb : tc, dv = sign > 0.0f ? tc : tb;
+        float pu = dot(lp, du), pv = dot(lp, dv);
+        s.u = pu - floorf(pu);
+        s.v = pv - floorf(pv);
+        Surface ls;
+        set_face(ls, xf_ivec(X, d), outward);
+        s.front = ls.front;
+        s.p = xf_point(X, lp);
+        s.normal = normalize(xf_normal(X, ls.normal));
+        s.dpdu = xf_vec(X, du);
+        s.dpdv = xf_vec(X, dv);
     } else if (kind == kGround) {
         DevUnbounded ub = S.unbounded[idx];
         s.material = ub.material;

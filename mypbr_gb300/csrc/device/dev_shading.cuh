@@ -778,10 +778,31 @@ MYPBR_DEV float env_pdf(const DeviceScene& S, float3 dir) {
     return __ldg(S.env_texel_pdf + j * S.env_w + i) / (2.0f * kPi * kPi * st);
 }
 
+// Radiance and density together, from one evaluation of the angles
+// (environment.h:202-228).
+MYPBR_DEV void env_radiance_pdf(const DeviceScene& S, float3 dir, float3& L, float& pdf) {
+    float u, theta;
+    env_angles(S, dir, u, theta);
+    int w = S.env_w, h = S.env_h;
+    float x = u * w - 0.5f;
+    float y = clampf(theta * kInvPi * h - 0.5f, 0.0f, h - 1.0f);
+    float x0 = floorf(x), y0 = floorf(y), fx = x - x0, fy = y - y0;
+    int i0 = (int(x0) + w) % w, i1 = (i0 + 1) % w;
+    int j0 = int(y0), j1 = min(j0 + 1, h - 1);
+    float3 a = f3(ldg4(S.env_pixels + j0 * w + i0)), b = f3(ldg4(S.env_pixels + j0 * w + i1));
+    float3 c = f3(ldg4(S.env_pixels + j1 * w + i0)), e = f3(ldg4(S.env_pixels + j1 * w + i1));
+    L = S.env_intensity * ((1.0f - fy) * ((1.0f - fx) * a + fx * b) + fy * ((1.0f - fx) * c + fx * e));
+    float st = sinf(theta);
+    int i = min(max(int(u * w), 0), w - 1), j = min(max(int(theta * kInvPi * h), 0), h - 1);
+    pdf = st > 0.0f ? __ldg(S.env_texel_pdf + j * w + i) / (2.0f * kPi * kPi * st) : 0.0f;
+}
+
 // Draws a texel from the alias table (same per-texel probability as the
 // reference's marginal / conditional CDFs, environment.h:230-243), then a
-// uniform point inside it.
-MYPBR_DEV float3 env_sample(const DeviceScene& S, Rng& g) {
+// uniform point inside it. With L and pdf, also returns the radiance there
+// (bilinear, as env_radiance) and the density of this sampling, read from the
+// texel instead of recomputing the angles of the direction.
+MYPBR_DEV float3 env_sample(const DeviceScene& S, Rng& g, float3* L = nullptr, float* pdf = nullptr) {
     int n = S.env_w * S.env_h;
     float x = g.next() * n;
     int k = min(int(x), n - 1);
@@ -796,7 +817,24 @@ MYPBR_DEV float3 env_sample(const DeviceScene& S, Rng& g) {
     float phi = 2.0f * kPi * (xx / S.env_w - 0.5f - S.env_rotation);
     float st = sinf(theta), ct = cosf(theta), sp, cp;
     sincosf(phi, &sp, &cp);
+    if (L) {
+        int w = S.env_w, h = S.env_h;
+        float x = xx - 0.5f, y = clampf(yy - 0.5f, 0.0f, h - 1.0f);
+        float x0 = floorf(x), y0 = floorf(y), ffx = x - x0, ffy = y - y0;
+        int i0 = (int(x0) + w) % w, i1 = (i0 + 1) % w;
+        int j0 = int(y0), j1 = min(j0 + 1, h - 1);
+        float3 a = f3(ldg4(S.env_pixels + j0 * w + i0)), b = f3(ldg4(S.env_pixels + j0 * w + i1));
+        float3 c = f3(ldg4(S.env_pixels + j1 * w + i0)), e = f3(ldg4(S.env_pixels + j1 * w + i1));
+        *L = S.env_intensity * ((1.0f - ffy) * ((1.0f - ffx) * a + ffx * b) + ffy * ((1.0f - ffx) * c + ffx * e));
+        *pdf = st > 0.0f ? __ldg(S.env_texel_pdf + k) / (2.0f * kPi * kPi * st) : 0.0f;
+    }
     return f3(st * sp, ct, -st * cp);
+}
+
+// True when the light list is the environment alone and there is no sun:
+// NEE then needs no pdf sum and no second angle evaluation.
+MYPBR_DEV bool env_only(const DeviceScene& S) {
+    return S.light_count == 1 && S.env_w > 0 && !S.sun_enabled && S.lights[0].kind == 1;
 }
 
 MYPBR_DEV bool sun_in_cone(const DeviceScene& S, float3 dir) {

@@ -231,14 +231,15 @@ __global__ void k_features(WaveParams P) {
     }
 }
 
-// The material index of a hit primitive.
-MYPBR_DEV int hit_material(const DeviceScene& S, uint32_t prim) {
-    int kind = int(prim >> kKindShift), idx = int(prim & kIndexMask);
+// The material index of a hit (a voxel face carries its own in b1).
+MYPBR_DEV int hit_material(const DeviceScene& S, const HitInfo& h) {
+    int kind = int(h.prim >> kKindShift), idx = int(h.prim & kIndexMask);
     switch (kind) {
         case kSphere: return __ldg(&S.sphere_info[idx].x);
         case kQuad: return __float_as_int(ldg4(S.quads + 5 * idx).w);
         case kTriangle: return __float_as_int(ldg4(S.tris + 3 * idx).w);
         case kMedium: return __float_as_int(ldg4(S.media + 3 * idx + 2).y);
+        case kVoxel: return __float_as_int(h.b1);
         default: return S.unbounded[idx].material;
     }
 }
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(256) k_extend(WaveParams P, int depth) {
         }
         HitInfo h = closest_hit(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
         P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
-        int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h.prim)]);
+        int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h)]);
         uint32_t* counter = class_counter(P, depth, c);
         class_queue(P, c)[warp_push_keyed(counter)] = slot;
     }
@@ -311,12 +312,19 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
         float3 new_o = o, new_d = d;
         if constexpr (C == kClassMiss) {
             // camera.h:373-387: the sky is a light, weighted like emission
-            float3 sky = escaped_radiance(S, d, depth == 0);
             if (!seen) {
-                if (specular || !P.has_lights)
-                    rad += beta * sky;
-                else
-                    rad += beta * sky * power_heuristic(scatter_pdf, lights_pdf(S, o, d));
+                if (env_only(S)) {
+                    float3 sky;
+                    float lp;
+                    env_radiance_pdf(S, d, sky, lp);
+                    rad += beta * sky * (specular ? 1.0f : power_heuristic(scatter_pdf, lp));
+                } else {
+                    float3 sky = escaped_radiance(S, d, depth == 0);
+                    if (specular || !P.has_lights)
+                        rad += beta * sky;
+                    else
+                        rad += beta * sky * power_heuristic(scatter_pdf, lights_pdf(S, o, d));
+                }
             }
             terminate = true;
         } else {
@@ -364,17 +372,26 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
                 bool last = depth == P.max_depth - 1 || capped;
                 seen = false;
                 if (P.has_lights) {  // camera.h:466-506; the shadow ray is traced by k_shadow
-                    float3 to_light = lights_sample(S, s.p, g);
-                    float lp = lights_pdf(S, s.p, to_light);
+                    // With the sky as the only light, the sample carries its own
+                    // radiance and density; the shadow ray then only tests visibility
+                    bool sky_only = env_only(S) && !S.has_emitters && !(P.transparent_shadows && S.has_clear_glass);
+                    float3 to_light, sky = f3(1.0f);
+                    float lp;
+                    if (sky_only) {
+                        to_light = env_sample(S, g, &sky, &lp);
+                    } else {
+                        to_light = lights_sample(S, s.p, g);
+                        lp = lights_pdf(S, s.p, to_light);
+                    }
                     if (lp > 0.0f) {
                         float3 f = class_eval<C>(S, mat, d, s, to_light);
                         if (f.x > 0.0f || f.y > 0.0f || f.z > 0.0f) {
                             float w = last ? 1.0f : power_heuristic(lp, sr.pdf.value(to_light));
-                            float3 c = beta * f * (w / lp);
+                            float3 c = beta * f * sky * (w / lp);
                             float3 sd = normalize(to_light);
                             P.B.sh_o[slot] = make_float4(s.p.x, s.p.y, s.p.z, 0.0f);
                             P.B.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-                            P.B.sh_c[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+                            P.B.sh_c[slot] = make_float4(c.x, c.y, c.z, sky_only ? 1.0f : 0.0f);
                             P.B.shadow_queue[warp_push(sh_counter(P, depth))] = slot;
                             pushed_shadow = true;
                         }
@@ -443,6 +460,15 @@ __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
             pass = f_bits(P.B.beta[slot].w);
         }
         float3 through = f3(1.0f), emission = f3(0.0f);
+        if (!S.has_emitters && !(P.transparent_shadows && S.has_clear_glass)) {
+            // Nothing the ray can reach emits, and nothing lets it through:
+            // only whether it escapes matters (camera.h:488-503). A sky-only
+            // sample already holds the sky's radiance (sc.w = 1).
+            if (P.has_media)
+                key = media_key(P, pixel, pass, uint32_t(depth), 1);
+            if (!any_hit(S, o, d, 0.001f, 3.0e38f, key))
+                emission = sc.w != 0.0f ? f3(1.0f) : escaped_radiance(S, d, false);
+        } else
         for (int hop = 0; hop <= 16; hop++) {
             if (P.has_media)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1 + 4 * hop);
@@ -452,7 +478,7 @@ __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
                 break;
             }
             int kind = int(h.prim >> kKindShift);
-            int mat = (kind == kSphere || kind == kQuad || kind == kTriangle) ? hit_material(S, h.prim) : -1;
+            int mat = (kind == kSphere || kind == kQuad || kind == kTriangle || kind == kVoxel) ? hit_material(S, h) : -1;
             // media, the ground and fog neither emit nor let shadows through
             bool through_glass = P.transparent_shadows && hop < 16 && mat >= 0 && lets_shadows_through(S, mat);
             if (!through_glass && (mat < 0 || !may_emit(S, mat)))

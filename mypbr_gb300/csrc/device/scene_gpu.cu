@@ -158,12 +158,39 @@ int validate(const mypbr_flat_scene& F) {
             (u.kind == MYPBR_UNBOUNDED_HEIGHT_FOG && !(u.density > 0 && u.scale_height > 0)))
             return bad("unbounded object " + std::to_string(k) + " is malformed");
     }
+    for (int64_t k = 0; k < F.voxel_palette_count; k++) {
+        const auto& e = F.voxel_palettes[k];
+        if (e.kind < MYPBR_VOXEL_EMPTY || e.kind > MYPBR_VOXEL_TRANSPARENT ||
+            (e.kind != MYPBR_VOXEL_EMPTY && !in(e.material, nm)) || (k % 256 == 0 && e.kind != MYPBR_VOXEL_EMPTY))
+            return bad("voxel palette entry " + std::to_string(k) + " is malformed");
+    }
+    for (int64_t k = 0; k < F.voxel_model_count; k++) {
+        const auto& m = F.voxel_models[k];
+        int64_t cells = int64_t(m.nx) * m.ny * m.nz;
+        if (m.nx <= 0 || m.ny <= 0 || m.nz <= 0 || !in(m.xform, F.xform_count) || m.cells < 0 ||
+            m.cells + cells > F.voxel_cell_bytes || m.palette < 0 || m.palette % 256 != 0 ||
+            int64_t(m.palette) + 256 > F.voxel_palette_count || !(m.edge_width >= 0 && m.edge_width < 0.5) ||
+            (m.edge_width > 0 && !in(m.edge_material, nm)))
+            return bad("voxel model " + std::to_string(k) + " is malformed");
+    }
+    for (int64_t k = 0; k < F.voxel_block_count; k++) {
+        const auto& b = F.voxel_blocks[k];
+        if (!in(b.model, F.voxel_model_count))
+            return bad("voxel block " + std::to_string(k) + " names a missing model");
+        const auto& m = F.voxel_models[b.model];
+        const int n[3] = {m.nx, m.ny, m.nz};
+        for (int a = 0; a < 3; a++)
+            if (b.lo[a] < 0 || b.hi[a] > n[a] || b.hi[a] <= b.lo[a] || b.hi[a] - b.lo[a] > kVoxelBlockMax)
+                return bad("voxel block " + std::to_string(k) + " is out of its model or larger than " +
+                           std::to_string(kVoxelBlockMax) + " cells a side");
+    }
     auto prim_count = [&](int kind) -> int64_t {
         switch (kind) {
             case MYPBR_PRIM_SPHERE: return F.sphere_count;
             case MYPBR_PRIM_QUAD: return F.quad_count;
             case MYPBR_PRIM_TRIANGLE: return F.triangle_count;
             case MYPBR_PRIM_MEDIUM: return F.medium_count;
+            case MYPBR_PRIM_VOXEL_BLOCK: return F.voxel_block_count;
             default: return -1;
         }
     };
@@ -411,6 +438,35 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     PUT(unb, D.unbounded);
     D.unbounded_count = int(unb.size());
 
+    std::vector<DevVoxelModel> vmodels;
+    for (int64_t k = 0; k < F.voxel_model_count; k++) {
+        const auto& m = F.voxel_models[k];
+        DevVoxelModel d{};
+        d.nx = m.nx;
+        d.ny = m.ny;
+        d.nz = m.nz;
+        d.xform = m.xform;
+        d.cells = m.cells;
+        d.palette = m.palette;
+        d.edge_material = m.edge_material;
+        d.edge_width = float(m.edge_width);
+        vmodels.push_back(d);
+    }
+    PUT(vmodels, D.voxel_models);
+    std::vector<int4> vblocks;
+    for (int64_t k = 0; k < F.voxel_block_count; k++) {
+        const auto& b = F.voxel_blocks[k];
+        vblocks.push_back(make_int4(b.model, b.lo[0], b.lo[1], b.lo[2]));
+        vblocks.push_back(make_int4(b.hi[0], b.hi[1], b.hi[2], 0));
+    }
+    PUT(vblocks, D.voxel_blocks);
+    std::vector<int2> vpal;
+    for (int64_t k = 0; k < F.voxel_palette_count; k++)
+        vpal.push_back(make_int2(F.voxel_palettes[k].material, F.voxel_palettes[k].kind));
+    PUT(vpal, D.voxel_palettes);
+    std::vector<uint8_t> vcells(F.voxel_cells, F.voxel_cells + F.voxel_cell_bytes);
+    PUT(vcells, D.voxel_cells);
+
     // ---- appearance
     std::vector<DevMaterial> mats;
     for (int64_t k = 0; k < F.material_count; k++) {
@@ -445,6 +501,13 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
         cls.push_back(c);
     }
     PUT(cls, D.mat_class);
+    for (int64_t k = 0; k < F.material_count; k++) {
+        const auto& m = F.materials[k];
+        if (m.type == MYPBR_MAT_DIFFUSE_LIGHT || m.emission_tex >= 0)
+            D.has_emitters = 1;
+        if (m.type == MYPBR_MAT_DIELECTRIC && m.p[1] == 0)
+            D.has_clear_glass = 1;
+    }
     D.has_media = F.medium_count > 0;
     for (int64_t k = 0; k < F.unbounded_count; k++)
         if (F.unbounded[k].kind == MYPBR_UNBOUNDED_HEIGHT_FOG)

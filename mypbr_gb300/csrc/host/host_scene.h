@@ -24,6 +24,10 @@ struct mypbr_host_scene {
     std::vector<float> texels_hdr;
     std::vector<mypbr_light> lights;
     std::vector<mypbr_light_member> light_members;
+    std::vector<mypbr_voxel_model> voxel_models;
+    std::vector<mypbr_voxel_block> voxel_blocks;
+    std::vector<mypbr_voxel_entry> voxel_palettes;
+    std::vector<uint8_t> voxel_cells;
     std::vector<float> env_pixels;
     int env_width = 0, env_height = 0;
     double env_intensity = 1, env_rotation = 0;

@@ -10,9 +10,10 @@
 // world-space quads and triangles (spheres and media keep their transform,
 // as instance::hit does), and one BVH is built over every primitive.
 //
-// Not handled here (MYPBR_ERR_UNSUPPORTED with a message): glTF meshes, .vox
-// models, "sky atmosphere" / "style voxel", cyclorama, softbox, MTL files and
-// 8-bit image textures (PNG/JPEG); .hdr images are read.
+// MagicaVoxel models (`vox`) become voxel blocks walked by a grid DDA, or
+// with `quads` their visible faces. Not handled here (MYPBR_ERR_UNSUPPORTED
+// with a message): glTF meshes, "sky atmosphere" / "style voxel", cyclorama,
+// softbox, MTL files and 8-bit image textures (PNG/JPEG); .hdr images are read.
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -28,6 +29,9 @@
 #include "bvh_build.h"
 #include "host_math.h"
 #include "host_scene.h"
+#include "vox_reader.h"
+
+#include <array>
 
 using namespace mypbr_host;
 
@@ -507,8 +511,10 @@ class Loader {
         return b;
     }
 
-    // Adds one world-space quad (object-space q, u, v moved by xform); returns its index.
-    int push_quad(const V3& q, const V3& u, const V3& v, int mat, const Xf& xform, bool transformed) {
+    // Adds one world-space quad (object-space q, u, v moved by xform); returns
+    // its index. in_bvh = false keeps it out of the BVH (a light-only face).
+    int push_quad(const V3& q, const V3& u, const V3& v, int mat, const Xf& xform, bool transformed,
+                  bool in_bvh = true) {
         mypbr_quad o{};
         V3 n = unit(cross(u, v));
         V3 wq = q, wu = u, wv = v, wn = n;
@@ -528,7 +534,8 @@ class Loader {
         S.quads.push_back(o);
         int index = int(S.quads.size()) - 1;
         Box box = transformed ? xform.box(quad_box(q, u, v)) : quad_box(q, u, v);
-        add_item(MYPBR_PRIM_QUAD, index, box);
+        if (in_bvh)
+            add_item(MYPBR_PRIM_QUAD, index, box);
         return index;
     }
 
@@ -1127,6 +1134,278 @@ class Loader {
 
     bool unsupported = false;
 
+    // A MagicaVoxel palette as materials and voxel kinds (voxel.h:48-97):
+    // sRGB colours decoded to linear albedo; MATL _metal -> principled,
+    // _glass -> absorbing dielectric of kind transparent, _emit -> light,
+    // anything else -> lambertian. Returns the first of the 256 entries.
+    int add_vox_palette(const VoxFile& vox, double emission_scale, std::vector<bool>& emissive) {
+        auto number = [](const std::map<std::string, std::string>& props, const char* key, double fallback) {
+            auto it = props.find(key);
+            if (it == props.end())
+                return fallback;
+            try {
+                return std::stod(it->second);
+            } catch (...) {
+                return fallback;
+            }
+        };
+        auto srgb = [](double e) { return e <= 0.04045 ? e / 12.92 : std::pow((e + 0.055) / 1.055, 2.4); };
+        int base = int(S.voxel_palettes.size());
+        emissive.assign(256, false);
+        for (int k = 0; k < 256; k++) {
+            const V3& c = vox.palette[k];
+            V3 albedo(srgb(c.x), srgb(c.y), srgb(c.z));
+            const auto& props = vox.materials[k];
+            auto type_it = props.find("_type");
+            std::string type = type_it == props.end() ? "_diffuse" : type_it->second;
+            double roughness = std::clamp(number(props, "_rough", 0.1), 0.0, 1.0);
+            double ior = number(props, "_ri", 1 + number(props, "_ior", 0.5));
+            if (ior <= 1)
+                ior = 1.5;
+            mypbr_voxel_entry e{};
+            e.kind = k == 0 ? MYPBR_VOXEL_EMPTY : MYPBR_VOXEL_OPAQUE;
+            mypbr_material m = blank_material(MYPBR_MAT_LAMBERTIAN);
+            if (type == "_metal") {
+                double metallic =
+                    number(props, "_plastic", 0) > 0 ? 0 : std::clamp(number(props, "_metal", 1), 0.0, 1.0);
+                m.type = MYPBR_MAT_PRINCIPLED;
+                m.tex[0] = add_texture_solid(albedo);
+                m.tex[1] = add_texture_solid(V3(metallic, metallic, metallic));
+                m.tex[2] = add_texture_solid(V3(roughness, roughness, roughness));
+                double r0 = (ior - 1) / (ior + 1);
+                m.p[0] = r0 * r0;
+                m.p[13] = m.p[14] = m.p[15] = 1;
+            } else if (type == "_glass") {
+                double att = std::clamp(number(props, "_att", 0.5), 0.0, 1.0);
+                m.type = MYPBR_MAT_DIELECTRIC;
+                m.p[0] = ior;
+                m.p[1] = roughness <= 0.05 ? 0 : roughness;
+                for (int ch = 0; ch < 3; ch++) {
+                    double tint = std::clamp((1 - att) + att * albedo[ch], 1e-3, 1.0);
+                    m.p[2 + ch] = -std::log(tint) / 1.0;
+                }
+                e.kind = MYPBR_VOXEL_TRANSPARENT;
+            } else if (type == "_emit") {
+                double strength = number(props, "_emit", 1) * std::pow(10.0, number(props, "_flux", 0)) * emission_scale;
+                m.type = MYPBR_MAT_DIFFUSE_LIGHT;
+                for (int ch = 0; ch < 3; ch++)
+                    m.p[ch] = strength * albedo[ch];
+                m.p[3] = 180;
+                m.p[4] = kInf;
+                m.p[5] = 1;
+                emissive[size_t(k)] = strength > 0;
+            } else {
+                m.tex[0] = add_texture_solid(albedo);
+            }
+            e.material = add_material(m);
+            S.voxel_palettes.push_back(e);
+        }
+        return base;
+    }
+
+    static bool face_visible(int k, int n) {  // voxel.h:100-106
+        if (k == MYPBR_VOXEL_EMPTY)
+            return false;
+        if (n == MYPBR_VOXEL_EMPTY)
+            return true;
+        return k == MYPBR_VOXEL_OPAQUE && n == MYPBR_VOXEL_TRANSPARENT;
+    }
+
+    struct VoxFace {
+        V3 q, u, v;
+        int material;
+        bool emissive;
+    };
+
+    // The visible faces of a model in model space, wound so that cross(u, v)
+    // points out of the cell (voxel.h:112-147).
+    std::vector<VoxFace> vox_faces(const VoxModel& m, int palette, const std::vector<bool>& emissive) {
+        static const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+        static const double corner[6][3] = {{1, 0, 0}, {0, 0, 0}, {0, 1, 0}, {0, 0, 0}, {0, 0, 1}, {0, 0, 0}};
+        static const double us[6][3] = {{0, 1, 0}, {0, 0, 1}, {0, 0, 1}, {1, 0, 0}, {1, 0, 0}, {0, 1, 0}};
+        static const double vs[6][3] = {{0, 0, 1}, {0, 1, 0}, {1, 0, 0}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+        std::vector<VoxFace> faces;
+        auto kind = [&](int idx) { return S.voxel_palettes[size_t(palette + idx)].kind; };
+        for (int z = 0; z < m.nz; z++)
+            for (int y = 0; y < m.ny; y++)
+                for (int x = 0; x < m.nx; x++) {
+                    int idx = m.at(x, y, z);
+                    int k = kind(idx);
+                    if (k == MYPBR_VOXEL_EMPTY)
+                        continue;
+                    for (int f = 0; f < 6; f++) {
+                        int n = kind(m.at(x + off[f][0], y + off[f][1], z + off[f][2]));
+                        if (!face_visible(k, n))
+                            continue;
+                        VoxFace face;
+                        face.q = V3(x + corner[f][0], y + corner[f][1], z + corner[f][2]);
+                        face.u = V3(us[f][0], us[f][1], us[f][2]);
+                        face.v = V3(vs[f][0], vs[f][1], vs[f][2]);
+                        face.material = S.voxel_palettes[size_t(palette + idx)].material;
+                        face.emissive = emissive[size_t(idx)];
+                        faces.push_back(face);
+                    }
+                }
+        return faces;
+    }
+
+    // vox <file> [quads] [emission <s>] [edges <w> [<r g b>]] [transforms] (scene.h:341-429)
+    bool parse_vox(std::istringstream& in) {
+        const char* usage = "expected 'vox <file.vox> [quads] [emission <scale>] [edges <width> [<r g b>]] [transforms]'";
+        std::string file, token;
+        if (!(in >> file))
+            return fail(usage);
+        if (file[0] != '/')
+            file = scene_dir + file;
+        bool quads = false;
+        double emission = 1, edge_width = 0;
+        V3 edge_color(0, 0, 0);
+        std::vector<std::string> rest;
+        while (in >> token)
+            rest.push_back(token);
+        size_t k = 0;
+        for (; k < rest.size(); k++) {
+            if (rest[k] == "quads") {
+                quads = true;
+            } else if (rest[k] == "emission" && k + 1 < rest.size()) {
+                std::istringstream number(rest[++k]);
+                if (!(number >> emission) || emission < 0)
+                    return fail(usage);
+            } else if (rest[k] == "edges" && k + 1 < rest.size()) {
+                std::istringstream number(rest[++k]);
+                if (!(number >> edge_width) || edge_width <= 0 || edge_width >= 0.5)
+                    return fail(usage);
+                if (k + 3 < rest.size()) {
+                    std::istringstream rgb(rest[k + 1] + ' ' + rest[k + 2] + ' ' + rest[k + 3]);
+                    V3 c;
+                    if (rgb >> c.x >> c.y >> c.z) {
+                        edge_color = c;
+                        k += 3;
+                    }
+                }
+            } else {
+                break;
+            }
+        }
+        std::string tail_text;
+        for (; k < rest.size(); k++)
+            tail_text += rest[k] + ' ';
+        std::istringstream tail(tail_text);
+        int mat;
+        Xf xform;
+        bool transformed;
+        error.clear();
+        if (!read_tail(tail, mat, xform, transformed))
+            return fail(error);
+        if (mat != default_material)
+            return fail("vox models take their materials from the file's palette");
+        VoxFile vox;
+        std::string err;
+        if (!read_vox(file, vox, err))
+            return fail(err);
+        std::vector<bool> emissive;
+        int palette = add_vox_palette(vox, emission, emissive);
+        int edge_material = (!quads && edge_width > 0) ? lambertian(edge_color) : -1;
+        struct ModelData {
+            int64_t cells;
+            std::vector<VoxFace> faces;
+            std::vector<std::array<int, 6>> blocks;  // lo, hi
+            Box box;                                 // model-space box of the geometry
+        };
+        std::vector<ModelData> models(vox.models.size());
+        for (size_t mi = 0; mi < vox.models.size(); mi++) {
+            const VoxModel& m = vox.models[mi];
+            ModelData& md = models[mi];
+            md.faces = vox_faces(m, palette, emissive);
+            if (quads) {
+                for (const auto& f : md.faces)
+                    md.box.grow(quad_box(f.q, f.u, f.v));
+                continue;
+            }
+            md.cells = int64_t(S.voxel_cells.size());
+            S.voxel_cells.insert(S.voxel_cells.end(), m.cells.begin(), m.cells.end());
+            const int block = 8;  // voxel.h:356
+            for (int z0 = 0; z0 < m.nz; z0 += block)
+                for (int y0 = 0; y0 < m.ny; y0 += block)
+                    for (int x0 = 0; x0 < m.nx; x0 += block) {
+                        int lo[3] = {x0 + block, y0 + block, z0 + block}, hi[3] = {x0, y0, z0};
+                        for (int z = z0; z < std::min(z0 + block, m.nz); z++)
+                            for (int y = y0; y < std::min(y0 + block, m.ny); y++)
+                                for (int x = x0; x < std::min(x0 + block, m.nx); x++)
+                                    if (S.voxel_palettes[size_t(palette + m.at(x, y, z))].kind != MYPBR_VOXEL_EMPTY) {
+                                        int c[3] = {x, y, z};
+                                        for (int a = 0; a < 3; a++) {
+                                            lo[a] = std::min(lo[a], c[a]);
+                                            hi[a] = std::max(hi[a], c[a] + 1);
+                                        }
+                                    }
+                        if (hi[0] > lo[0]) {
+                            md.blocks.push_back({lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]});
+                            md.box.grow(Box::from_points(V3(lo[0], lo[1], lo[2]), V3(hi[0], hi[1], hi[2])));
+                        }
+                    }
+        }
+        // MagicaVoxel is z-up: +z becomes +y (and +y becomes -z)
+        Xf z_up = Xf::rotate(-90, V3(1, 0, 0));
+        for (const auto& placed : vox.instances) {
+            const ModelData& md = models[size_t(placed.model)];
+            Xf to_world = xform.then_after(z_up.then_after(placed.xform));
+            bool has_emitters = false;
+            for (const auto& f : md.faces)
+                has_emitters = has_emitters || f.emissive;
+            if (has_emitters && !to_world.is_similarity())
+                return fail("a vox model with emissive voxels can only be scaled uniformly");
+            if (!md.box.empty())
+                world_box.grow(to_world.box(md.box));
+            std::vector<int> emitter_quads;
+            if (quads) {
+                for (const auto& f : md.faces) {
+                    int qi = push_quad(f.q, f.u, f.v, f.material, to_world, true);
+                    if (f.emissive)
+                        emitter_quads.push_back(qi);
+                }
+            } else {
+                mypbr_voxel_model vm{};
+                const VoxModel& m = vox.models[size_t(placed.model)];
+                vm.nx = m.nx;
+                vm.ny = m.ny;
+                vm.nz = m.nz;
+                vm.xform = add_xform(to_world);
+                vm.cells = md.cells;
+                vm.palette = palette;
+                vm.edge_material = edge_material;
+                vm.edge_width = edge_width;
+                S.voxel_models.push_back(vm);
+                int model_index = int(S.voxel_models.size()) - 1;
+                for (const auto& b : md.blocks) {
+                    mypbr_voxel_block vb{};
+                    vb.model = model_index;
+                    for (int a = 0; a < 3; a++) {
+                        vb.lo[a] = b[size_t(a)];
+                        vb.hi[a] = b[size_t(3 + a)];
+                    }
+                    S.voxel_blocks.push_back(vb);
+                    Box box = Box::from_points(V3(b[0], b[1], b[2]), V3(b[3], b[4], b[5]));
+                    add_item(MYPBR_PRIM_VOXEL_BLOCK, int(S.voxel_blocks.size()) - 1, to_world.box(box));
+                }
+                // emissive faces are sampled as lights; the grid itself is hit
+                for (const auto& f : md.faces)
+                    if (f.emissive)
+                        emitter_quads.push_back(push_quad(f.q, f.u, f.v, f.material, to_world, true, false));
+            }
+            if (!emitter_quads.empty()) {
+                double power = 0;
+                int first = int(S.light_members.size());
+                for (int qi : emitter_quads) {
+                    power += kPi * 1.0 * average_emission_luminance(S.quads[size_t(qi)].material);
+                    add_member(MYPBR_PRIM_QUAD, qi, 1.0 / double(emitter_quads.size()));
+                }
+                add_light(first, int(emitter_quads.size()), power * to_world.area_scale());
+            }
+        }
+        return true;
+    }
+
     bool parse_line(std::istringstream& in, const std::string& keyword) {
         auto& cam = S.camera;
         auto& opts = S.opts;
@@ -1471,7 +1750,9 @@ class Loader {
             std::string extra;
             if (tail >> extra)
                 return fail("unexpected value '" + extra + "'");
-        } else if (keyword == "vox" || keyword == "cyclorama" || keyword == "softbox") {
+        } else if (keyword == "vox") {
+            return parse_vox(in);
+        } else if (keyword == "cyclorama" || keyword == "softbox") {
             unsupported = true;
             return fail("'" + keyword + "' is not supported by this backend");
         } else {
@@ -1691,6 +1972,14 @@ void mypbr_host_scene::finalize() {
     flat.background[0] = background.x;
     flat.background[1] = background.y;
     flat.background[2] = background.z;
+    flat.voxel_models = voxel_models.data();
+    flat.voxel_model_count = int64_t(voxel_models.size());
+    flat.voxel_blocks = voxel_blocks.data();
+    flat.voxel_block_count = int64_t(voxel_blocks.size());
+    flat.voxel_palettes = voxel_palettes.data();
+    flat.voxel_palette_count = int64_t(voxel_palettes.size());
+    flat.voxel_cells = voxel_cells.data();
+    flat.voxel_cell_bytes = int64_t(voxel_cells.size());
     // Camera height as camera::initialize computes it (camera.h:143-144)
     int h = int(camera.image_width / camera.aspect_ratio);
     camera.image_height = h < 1 ? 1 : h;

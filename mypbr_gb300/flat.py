@@ -25,6 +25,12 @@ _COUNTS = {"positions": "position_count", "normals": "normal_count", "uvs": "uv_
            "meshes": "mesh_count", "unbounded": "unbounded_count"}
 
 
+# Arrays after the sky fields, appended to the struct when voxels were added
+_VOXEL_ARRAYS = ["voxel_models", "voxel_blocks", "voxel_palettes", "voxel_cells"]
+_COUNTS.update({"voxel_models": "voxel_model_count", "voxel_blocks": "voxel_block_count",
+                "voxel_palettes": "voxel_palette_count", "voxel_cells": "voxel_cell_bytes"})
+
+
 def _count_name(a):
     return _COUNTS.get(a, a[:-1] + "_count")
 
@@ -33,7 +39,8 @@ class FlatScene(ctypes.Structure):
     _fields_ = ([("abi_version", ctypes.c_uint32), ("reserved0", ctypes.c_uint32)] +
                 [f for a in _ARRAYS for f in ((a, _vp), (_count_name(a), _i64))] +
                 [("environment", Environment), ("sun", Sun), ("use_sky", _i32), ("reserved1", _i32),
-                 ("background", _f64 * 3)])
+                 ("background", _f64 * 3)] +
+                [f for a in _VOXEL_ARRAYS for f in ((a, _vp), (_count_name(a), _i64))])
 
 
 DTYPES = {
@@ -64,6 +71,11 @@ DTYPES = {
     "lights": np.dtype([("kind", "<i4"), ("first_member", "<i4"), ("member_count", "<i4"), ("reserved", "<i4"),
                         ("probability", "<f8")]),
     "light_members": np.dtype([("prim_kind", "<i4"), ("prim_index", "<i4"), ("weight", "<f8")]),
+    "voxel_models": np.dtype([("n", "<i4", 3), ("xform", "<i4"), ("cells", "<i8"), ("palette", "<i4"),
+                              ("edge_material", "<i4"), ("edge_width", "<f8")]),
+    "voxel_blocks": np.dtype([("model", "<i4"), ("lo", "<i4", 3), ("hi", "<i4", 3), ("reserved", "<i4")]),
+    "voxel_palettes": np.dtype([("material", "<i4"), ("kind", "<i4")]),
+    "voxel_cells": np.dtype("u1"),
 }
 
 
@@ -71,7 +83,7 @@ def view(scene):
     """The flat scene of a mypbr_gb300.Scene as a dict of numpy arrays (copies)."""
     fs = FlatScene.from_address(scene.flat)
     out = {}
-    for a in _ARRAYS:
+    for a in _ARRAYS + _VOXEL_ARRAYS:
         n = getattr(fs, _count_name(a))
         ptr = getattr(fs, a)
         dt = DTYPES[a]

@@ -44,12 +44,26 @@ def lib():
         L.oracle_environment.restype = None
         L.oracle_render.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp]
         L.oracle_render.restype = ctypes.c_int
+        L.oracle_denoise.argtypes = [dp, dp, dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, dp]
+        L.oracle_denoise.restype = None
         _lib = L
     return _lib
 
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def denoise(radiance, albedo, normal, variance, iterations=5, sigma_luminance=4.0, sigma_normal=0.1,
+            sigma_albedo=0.1):
+    """denoiser::run (denoiser.h:45-193) in FP64; inputs (H, W, 3) and (H, W)."""
+    h, w = variance.shape
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (radiance, albedo, normal, variance)]
+    out = np.zeros((h, w, 3))
+    lib().oracle_denoise(*[_dp(a) for a in arrs], w, h, iterations, sigma_luminance, sigma_normal, sigma_albedo,
+                         _dp(out))
+    return out
 
 
 def ggx_table():

@@ -473,6 +473,157 @@ bool hit_height_fog(const mypbr_unbounded& hf, const V& o, const V& d, double tm
     return true;
 }
 
+// ---------------------------------------------------------------- voxels
+
+// A block of a placed voxel model: voxel_grid::hit (voxel.h:193-268) in the
+// model's space, a 3D DDA (Amanatides and Woo 1987) whose surfaces are the
+// crossings between cells of different kind (voxel.h:294-305), placed in the
+// world as instance::hit does (instance.h:29-40).
+struct VoxelWalk {
+    const Scene& S;
+    const mypbr_voxel_model& m;
+    const uint8_t* cells;
+    int kind_of(int idx) const { return S.f->voxel_palettes[m.palette + idx].kind; }
+    int at(const int c[3]) const {  // voxel.h:284-288
+        if (unsigned(c[0]) >= unsigned(m.nx) || unsigned(c[1]) >= unsigned(m.ny) || unsigned(c[2]) >= unsigned(m.nz))
+            return 0;
+        return cells[(size_t(c[2]) * m.ny + c[1]) * m.nx + c[0]];
+    }
+    static bool face_visible(int k, int n) {  // voxel.h:100-106
+        if (k == MYPBR_VOXEL_EMPTY)
+            return false;
+        if (n == MYPBR_VOXEL_EMPTY)
+            return true;
+        return k == MYPBR_VOXEL_OPAQUE && n == MYPBR_VOXEL_TRANSPARENT;
+    }
+    bool on_edge(const V& p, int axis, int sign, const int cell[3]) const {  // voxel.h:313-331
+        int k = kind_of(at(cell));
+        for (int side = 1; side <= 2; side++) {
+            int tangent = (axis + side) % 3;
+            double f = p[tangent] - cell[tangent];
+            for (int dir = -1; dir <= 1; dir += 2) {
+                if ((dir > 0 ? 1 - f : f) >= m.edge_width)
+                    continue;
+                int beside[3] = {cell[0], cell[1], cell[2]};
+                beside[tangent] += dir;
+                int above[3] = {beside[0], beside[1], beside[2]};
+                above[axis] += sign;
+                if (face_visible(k, kind_of(at(beside))) || kind_of(at(above)) != MYPBR_VOXEL_EMPTY)
+                    return true;
+            }
+        }
+        return false;
+    }
+    // voxel.h:333-350, in model space
+    bool record(const V& o, const V& d, double t, int axis, int sign, int index, const int cell[3], Hit& rec) const {
+        rec.t = t;
+        rec.p = o + t * d;
+        V outward, tb, tc;
+        outward[axis] = sign;
+        tb[(axis + 1) % 3] = 1;
+        tc[(axis + 2) % 3] = 1;
+        rec.dpdu = sign > 0 ? tb : tc;
+        rec.dpdv = sign > 0 ? tc : tb;
+        rec.u = dot(rec.p, rec.dpdu) - std::floor(dot(rec.p, rec.dpdu));
+        rec.v = dot(rec.p, rec.dpdv) - std::floor(dot(rec.p, rec.dpdv));
+        rec.mat = m.edge_width > 0 && on_edge(rec.p, axis, sign, cell) ? m.edge_material
+                                                                        : S.f->voxel_palettes[m.palette + index].material;
+        rec.set_face(d, outward);
+        return true;
+    }
+    bool crossing(const V& o, const V& d, double t, int axis, int step, int from, int to, const int to_cell[3],
+                  Hit& rec) const {  // voxel.h:294-305
+        int k_from = kind_of(from), k_to = kind_of(to);
+        if (k_to != MYPBR_VOXEL_EMPTY && face_visible(k_to, k_from))
+            return record(o, d, t, axis, -step, to, to_cell, rec);
+        if (face_visible(k_from, k_to)) {
+            int from_cell[3] = {to_cell[0], to_cell[1], to_cell[2]};
+            from_cell[axis] -= step;
+            return record(o, d, t, axis, step, from, from_cell, rec);
+        }
+        return false;
+    }
+    bool hit(const int lo[3], const int hi[3], const V& o, const V& d, double tmin, double tmax, Hit& rec) const {
+        double t_enter = -INF, t_exit = INF;
+        int enter_axis = 0;
+        for (int a = 0; a < 3; a++) {
+            if (d[a] == 0) {
+                if (o[a] < lo[a] || o[a] > hi[a])
+                    return false;
+                continue;
+            }
+            double t0 = (lo[a] - o[a]) / d[a], t1 = (hi[a] - o[a]) / d[a];
+            if (t0 > t1)
+                std::swap(t0, t1);
+            if (t0 > t_enter) {
+                t_enter = t0;
+                enter_axis = a;
+            }
+            t_exit = std::fmin(t_exit, t1);
+        }
+        bool from_outside = t_enter >= tmin;
+        double t_start = from_outside ? t_enter : tmin;
+        if (t_start > std::fmin(t_exit, tmax))
+            return false;
+        V start = o + t_start * d;
+        int c[3], step[3];
+        double t_next[3], t_delta[3];
+        for (int a = 0; a < 3; a++) {
+            c[a] = std::clamp(int(std::floor(start[a])), lo[a], hi[a] - 1);
+            if (from_outside && a == enter_axis)
+                c[a] = d[a] > 0 ? lo[a] : hi[a] - 1;
+            if (d[a] > 0) {
+                step[a] = 1;
+                t_next[a] = (c[a] + 1 - o[a]) / d[a];
+                t_delta[a] = 1 / d[a];
+            } else if (d[a] < 0) {
+                step[a] = -1;
+                t_next[a] = (c[a] - o[a]) / d[a];
+                t_delta[a] = -1 / d[a];
+            } else {
+                step[a] = 0;
+                t_next[a] = t_delta[a] = INF;
+            }
+        }
+        int index = at(c);
+        if (from_outside) {
+            int behind[3] = {c[0], c[1], c[2]};
+            behind[enter_axis] -= step[enter_axis];
+            if (crossing(o, d, t_enter, enter_axis, step[enter_axis], at(behind), index, c, rec))
+                return true;
+        }
+        while (true) {
+            int a = t_next[0] < t_next[1] ? (t_next[0] < t_next[2] ? 0 : 2) : (t_next[1] < t_next[2] ? 1 : 2);
+            double t = t_next[a];
+            if (t > tmax)
+                return false;
+            c[a] += step[a];
+            t_next[a] += t_delta[a];
+            int next = at(c);
+            if (crossing(o, d, t, a, step[a], index, next, c, rec))
+                return true;
+            if (c[a] < lo[a] || c[a] >= hi[a])
+                return false;
+            index = next;
+        }
+    }
+};
+
+bool hit_voxel_block(const Scene& S, int i, const V& o, const V& d, double tmin, double tmax, Hit& rec) {
+    const auto& b = S.f->voxel_blocks[i];
+    const auto& m = S.f->voxel_models[b.model];
+    const Xform& X = S.xf[m.xform];
+    VoxelWalk w{S, m, S.f->voxel_cells + m.cells};
+    V lo = X.ipoint(o), ld = X.ivec(d);
+    if (!w.hit(b.lo, b.hi, lo, ld, tmin, tmax, rec))
+        return false;
+    rec.p = X.point(rec.p);
+    rec.normal = unit(X.normal(rec.normal));
+    rec.dpdu = X.vec(rec.dpdu);
+    rec.dpdv = X.vec(rec.dpdv);
+    return true;
+}
+
 bool hit_prim(const Scene& S, int kind, int index, const V& o, const V& d, double tmin, double tmax, Hit& rec,
               Rng* g) {
     bool h = false;
@@ -481,6 +632,7 @@ bool hit_prim(const Scene& S, int kind, int index, const V& o, const V& d, doubl
         case MYPBR_PRIM_QUAD: h = hit_quad(S, index, o, d, tmin, tmax, rec); break;
         case MYPBR_PRIM_TRIANGLE: h = hit_triangle(S, index, o, d, tmin, tmax, rec); break;
         case MYPBR_PRIM_MEDIUM: h = g ? hit_medium(S, index, o, d, tmin, tmax, rec, *g) : false; break;
+        case MYPBR_PRIM_VOXEL_BLOCK: h = hit_voxel_block(S, index, o, d, tmin, tmax, rec); break;
         default: break;
     }
     if (h) {
@@ -566,7 +718,7 @@ bool world_hit(const Scene& S, const V& o, const V& d, double tmin, double tmax,
         else if (g)
             h = hit_height_fog(ub, o, d, tmin, closest, tmp, *g);
         if (h) {
-            tmp.kind = 4 + ub.kind;
+            tmp.kind = 5 + ub.kind;  // after the MYPBR_PRIM_* kinds
             tmp.index = int(k);
             any = true;
             closest = tmp.t;
@@ -2023,3 +2175,116 @@ void setup(Scene& S, const mypbr_flat_scene* f) {
 }
 
 }  // namespace
+
+// ------------------------------------------------------------- denoiser
+
+namespace {
+
+double lum3(const double* c) { return 0.2126 * c[0] + 0.7152 * c[1] + 0.0722 * c[2]; }
+
+}  // namespace
+
+extern "C" {
+
+// denoiser::run (denoiser.h:45-193), FP64: firefly clamp, then `iterations`
+// edge-avoiding a-trous passes (B3 5x5 taps spread 2^i apart) on lighting =
+// radiance / (albedo + 1e-3), weighted by normal, albedo and the luminance
+// within sigma_luminance standard deviations; out = lighting * (albedo + 1e-3).
+// All arrays W*H(*3), rows from the top left.
+void oracle_denoise(const double* radiance, const double* albedo, const double* normal, const double* variance,
+                    int width, int height, int iterations, double sigma_luminance, double sigma_normal,
+                    double sigma_albedo, double* out) {
+    const double eps = 1e-3;
+    size_t n = size_t(width) * height;
+    std::vector<double> light(3 * n), var(n);
+    for (size_t k = 0; k < n; k++) {
+        double a[3] = {albedo[3 * k] + eps, albedo[3 * k + 1] + eps, albedo[3 * k + 2] + eps};
+        for (int c = 0; c < 3; c++)
+            light[3 * k + c] = radiance[3 * k + c] / a[c];
+        double la = lum3(a);
+        var[k] = variance[k] / (la * la);
+    }
+    // remove_fireflies (denoiser.h:90-111)
+    std::vector<double> src = light;
+    for (int j = 1; j < height - 1; j++)
+        for (int i = 1; i < width - 1; i++) {
+            size_t p = size_t(j) * width + i;
+            double l = lum3(&src[3 * p]);
+            if (l <= 0 || std::sqrt(var[p]) < 0.5 * l)
+                continue;
+            double brightest = 0;
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++)
+                    if (dx || dy)
+                        brightest = std::fmax(brightest, lum3(&src[3 * (p + dy * width + dx)]));
+            if (l > brightest) {
+                double s = brightest / l;
+                for (int c = 0; c < 3; c++)
+                    light[3 * p + c] = s * src[3 * p + c];
+                var[p] *= s * s;
+            }
+        }
+    static const double kern[5] = {1.0 / 16, 1.0 / 4, 3.0 / 8, 1.0 / 4, 1.0 / 16};
+    std::vector<double> nl(3 * n), nv(n), bv(n);
+    double inv_n = 1 / (sigma_normal * sigma_normal), inv_a = 1 / (sigma_albedo * sigma_albedo);
+    for (int it = 0; it < iterations; it++) {
+        // blur3x3 (denoiser.h:158-178)
+        for (int j = 0; j < height; j++)
+            for (int i = 0; i < width; i++) {
+                static const double k3[3] = {0.25, 0.5, 0.25};
+                double sum = 0, w = 0;
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        int x = i + dx, y = j + dy;
+                        if (x < 0 || x >= width || y < 0 || y >= height)
+                            continue;
+                        double wt = k3[dx + 1] * k3[dy + 1];
+                        sum += wt * var[size_t(y) * width + x];
+                        w += wt;
+                    }
+                bv[size_t(j) * width + i] = sum / w;
+            }
+        int step = 1 << it;
+        // filter_pixel (denoiser.h:113-156)
+        for (int j = 0; j < height; j++)
+            for (int i = 0; i < width; i++) {
+                size_t p = size_t(j) * width + i;
+                double lp = lum3(&light[3 * p]);
+                double scale = sigma_luminance * std::sqrt(std::fmax(bv[p], 0.0)) + 1e-10;
+                double s[3] = {0, 0, 0}, ws = 0, vs = 0;
+                for (int dy = -2; dy <= 2; dy++) {
+                    int y = j + dy * step;
+                    if (y < 0 || y >= height)
+                        continue;
+                    for (int dx = -2; dx <= 2; dx++) {
+                        int x = i + dx * step;
+                        if (x < 0 || x >= width)
+                            continue;
+                        size_t q = size_t(y) * width + x;
+                        double dn = 0, da = 0;
+                        for (int c = 0; c < 3; c++) {
+                            double a = normal[3 * p + c] - normal[3 * q + c], b = albedo[3 * p + c] - albedo[3 * q + c];
+                            dn += a * a;
+                            da += b * b;
+                        }
+                        double w = kern[dx + 2] * kern[dy + 2] * std::exp(-dn * inv_n) * std::exp(-da * inv_a) *
+                                   std::exp(-std::fabs(lp - lum3(&light[3 * q])) / scale);
+                        for (int c = 0; c < 3; c++)
+                            s[c] += w * light[3 * q + c];
+                        ws += w;
+                        vs += w * w * var[q];
+                    }
+                }
+                for (int c = 0; c < 3; c++)
+                    nl[3 * p + c] = s[c] / ws;
+                nv[p] = vs / (ws * ws);
+            }
+        std::swap(light, nl);
+        std::swap(var, nv);
+    }
+    for (size_t k = 0; k < n; k++)
+        for (int c = 0; c < 3; c++)
+            out[3 * k + c] = light[3 * k + c] * (albedo[3 * k + c] + eps);
+}
+
+}  // extern "C"

@@ -16,6 +16,7 @@
 //   render <scene> <width> <spp> <batches> <threads> <out>
 //                                      batch means of camera::render (mean and variance of the mean)
 #include <bvh.h>
+#include <denoiser.h>
 #include <scene.h>
 
 #include <chrono>
@@ -322,6 +323,51 @@ int cmd_render(int argc, char** argv) {
     return 0;
 }
 
+// denoise <w> <h> <seed> <out>: a seeded synthetic frame (noisy radiance over
+// an albedo edge, a normal edge, a few fireflies, per-pixel variance) and
+// denoiser::run's output with the default settings (denoiser.h:39-43).
+int cmd_denoise(int argc, char** argv) {
+    if (argc < 6)
+        return 2;
+    int w = std::atoi(argv[2]), h = std::atoi(argv[3]);
+    Rng g(std::strtoull(argv[4], nullptr, 10));
+    frame f;
+    size_t n = size_t(w) * h;
+    f.radiance.resize(n);
+    f.albedo.resize(n);
+    f.normal.resize(n);
+    f.variance.resize(n);
+    for (int j = 0; j < h; j++)
+        for (int i = 0; i < w; i++) {
+            size_t k = size_t(j) * w + i;
+            color a = i < w / 2 ? color(0.8, 0.7, 0.6) : color(0.2, 0.5, 0.3);
+            vec3 nn = j < h / 3 ? vec3(0, 1, 0) : unit_vector(vec3(0.3, 0.2, 1));
+            double light = 0.5 + 0.3 * std::sin(0.2 * i) * std::cos(0.15 * j);
+            double noise = 1 + 0.6 * (g.next() - 0.5);
+            if (g.next() < 0.01)
+                noise = 40;  // a firefly
+            f.radiance[k] = a * (light * noise);
+            f.albedo[k] = a;
+            f.normal[k] = nn;
+            double l = luminance(f.radiance[k]);
+            f.variance[k] = 0.02 * l * l + 1e-4 + (noise > 10 ? l * l : 0.0);
+        }
+    denoiser dn;
+    dn.threads = 1;
+    auto out = dn.run(f, w, h);
+    Out o(argv[5]);
+    o.put(double(w));
+    o.put(double(h));
+    for (size_t k = 0; k < n; k++) {
+        o.put(f.radiance[k]);
+        o.put(f.albedo[k]);
+        o.put(f.normal[k]);
+        o.put(f.variance[k]);
+        o.put(out[k]);
+    }
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -337,6 +383,7 @@ int main(int argc, char** argv) {
     else if (c == "env") rc = cmd_env(argc, argv);
     else if (c == "ggx") rc = cmd_ggx(argc, argv);
     else if (c == "render") rc = cmd_render(argc, argv);
+    else if (c == "denoise") rc = cmd_denoise(argc, argv);
     if (rc == 2)
         std::cerr << "bad arguments for '" << c << "'\n";
     return rc;

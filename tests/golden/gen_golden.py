@@ -9,6 +9,7 @@ time or on a machine without the reference.
 
     python tests/golden/gen_golden.py            # everything
     python tests/golden/gen_golden.py render     # one group
+    python tests/golden/gen_golden.py render voxels.scene   # one render
 """
 import math
 import os
@@ -57,6 +58,108 @@ def make_env_fixture():
     lobe = 200.0 * np.exp(-0.5 * (ang / 0.08) ** 2)
     rgb = sky + lobe[..., None] * np.array([1.0, 0.9, 0.7])
     write_hdr(os.path.join(SCENES, "env_small.hdr"), rgb.astype(np.float64))
+
+
+# ------------------------------------------------------------ .vox files
+#
+# MagicaVoxel's chunk format: "VOX ", version 150, then a MAIN chunk whose
+# children are SIZE/XYZI pairs (one per model), an optional RGBA palette,
+# MATL dictionaries and the nTRN/nGRP/nSHP scene graph. Each chunk is a 4-byte
+# id, the byte sizes of its content and of its children, then both.
+
+def _i32(v):
+    return int(v).to_bytes(4, "little", signed=True)
+
+
+def _vstr(s):
+    b = s.encode()
+    return _i32(len(b)) + b
+
+
+def _vdict(d):
+    return _i32(len(d)) + b"".join(_vstr(k) + _vstr(v) for k, v in d.items())
+
+
+def _chunk(cid, content, children=b""):
+    return cid.encode() + _i32(len(content)) + _i32(len(children)) + content + children
+
+
+def write_vox(path, models, rgba=None, materials=None, graph=None):
+    """models: uint8 arrays indexed [x, y, z] (palette index, 0 empty); rgba:
+    (255, 4) uint8 colours of indices 1..255; materials: {index: {key: value}};
+    graph: list of scene graph chunks, made by the helpers below."""
+    body = b""
+    for m in models:
+        nx, ny, nz = m.shape
+        xs, ys, zs = np.nonzero(m)
+        body += _chunk("SIZE", _i32(nx) + _i32(ny) + _i32(nz))
+        cells = np.stack([xs, ys, zs, m[xs, ys, zs]], axis=1).astype(np.uint8)
+        body += _chunk("XYZI", _i32(len(cells)) + cells.tobytes())
+    for chunk in graph or []:
+        body += chunk
+    if rgba is not None:
+        pal = np.zeros((256, 4), np.uint8)
+        pal[:255] = rgba
+        body += _chunk("RGBA", pal.tobytes())
+    for index, props in (materials or {}).items():
+        body += _chunk("MATL", _i32(index) + _vdict(props))
+    with open(path, "wb") as f:
+        f.write(b"VOX " + _i32(150) + _chunk("MAIN", b"", body))
+
+
+def vox_transform(node, child, translation=None, rotation=None):
+    frame = {}
+    if rotation is not None:
+        frame["_r"] = str(rotation)
+    if translation is not None:
+        frame["_t"] = " ".join(str(int(v)) for v in translation)
+    return _chunk("nTRN", _i32(node) + _vdict({}) + _i32(child) + _i32(-1) + _i32(0) + _i32(1) + _vdict(frame))
+
+
+def vox_group(node, children):
+    return _chunk("nGRP", _i32(node) + _vdict({}) + _i32(len(children)) + b"".join(_i32(c) for c in children))
+
+
+def vox_shape(node, model):
+    return _chunk("nSHP", _i32(node) + _vdict({}) + _i32(1) + _i32(model) + _vdict({}))
+
+
+def make_vox_fixtures():
+    """voxels.vox: a random 13 x 9 x 11 model of empty, opaque, glass and
+    emissive cells with a solid glass corner (the mix of the reference's
+    voxel test), plus a 5 x 4 x 3 model placed twice by a scene graph, once
+    turned by a rotation byte; its own palette, glass, metal and light
+    materials. voxels_default.vox: one model, no palette, no scene graph
+    (MagicaVoxel's default palette, the model standing on z = 0)."""
+    rng = np.random.default_rng(2024)
+    a = np.zeros((13, 9, 11), np.uint8)
+    x = rng.random(a.shape)
+    pick = rng.random(a.shape)
+    a[(x >= 0.55) & (x < 0.8)] = 1 + (pick[(x >= 0.55) & (x < 0.8)] * 2).astype(np.uint8)
+    a[(x >= 0.8) & (x < 0.95)] = 3 + (pick[(x >= 0.8) & (x < 0.95)] * 2).astype(np.uint8)
+    a[x >= 0.95] = 5
+    a[x >= 0.985] = 6
+    a[:4, :4, :4] = 3
+    b = np.zeros((5, 4, 3), np.uint8)
+    b[:, :, 0] = 7
+    b[1:4, 1:3, 1] = 8
+    b[2, 1, 2] = 2
+    rgba = np.zeros((255, 4), np.uint8)
+    for k in range(255):  # index k + 1: red steps keep lambertian albedos apart
+        rgba[k] = (min(255, 30 + 20 * k), (37 * k) % 256, (91 * k) % 256, 255)
+    materials = {3: {"_type": "_glass", "_ior": "0.5", "_rough": "0"},
+                 4: {"_type": "_glass", "_ior": "0.45", "_rough": "0.3", "_att": "0.8"},
+                 5: {"_type": "_emit", "_emit": "2", "_flux": "0"},
+                 6: {"_type": "_metal", "_metal": "1", "_rough": "0.25"}}
+    # rotation byte 17: row 0 = -y, row 1 = +x, row 2 = +z (a quarter turn about z)
+    graph = [vox_transform(0, 1), vox_group(1, [2, 4, 6]), vox_transform(2, 3, (0, 0, 5)), vox_shape(3, 0),
+             vox_transform(4, 5, (12, -2, 1), 17), vox_shape(5, 1), vox_transform(6, 7, (-11, 3, 2)), vox_shape(7, 1)]
+    write_vox(os.path.join(SCENES, "voxels.vox"), [a, b], rgba, materials, graph)
+    c = np.zeros((6, 5, 4), np.uint8)
+    c[:, :, 0] = 1
+    c[1:5, 1:4, 1] = 200
+    c[2:4, 2, 2:4] = 250
+    write_vox(os.path.join(SCENES, "voxels_default.vox"), [c])
 
 
 def run(*args):
@@ -112,18 +215,28 @@ def gen_ggx():
                         E_avg=recs[:, 3], ms_albedo=recs[:, 4], ms_eval=recs[:, 5])
 
 
+def gen_voxels():
+    recs = run("hits", scene("voxels.scene"), 8000, 4242).reshape(-1, 18)
+    np.savez_compressed(os.path.join(HERE, "hits_voxels.npz"), o=recs[:, 0:3], d=recs[:, 3:6], hit=recs[:, 6],
+                        t=recs[:, 7], normal=recs[:, 8:11], u=recs[:, 11], v=recs[:, 12], front=recs[:, 13],
+                        material_id=recs[:, 14], p=recs[:, 15:18])
+
+
 # (scene, width, spp per batch, batches)
 RENDERS = [
     ("cornell_c1.scene", 64, 64, 16),
     ("env_spheres.scene", 64, 64, 16),
     ("fog_box.scene", 48, 64, 16),
     ("materials.scene", 64, 64, 16),
+    ("voxels.scene", 48, 64, 16),
 ]
 
 
-def gen_render():
+def gen_render(only=None):
     threads = os.cpu_count() or 1
     for name, width, spp, batches in RENDERS:
+        if only and name not in only:
+            continue
         raw = run("render", scene(name), width, spp, batches, threads)
         w, h, s, b, seconds = raw[:5]
         data = raw[5:].reshape(int(h), int(w), 3, 2)
@@ -134,14 +247,30 @@ def gen_render():
         print(f"{name}: {int(w)}x{int(h)}, {int(s)} spp x {int(b)} batches, {seconds:.1f} s")
 
 
+def gen_denoise():
+    raw = run("denoise", 64, 48, 21)
+    w, h = int(raw[0]), int(raw[1])
+    recs = raw[2:].reshape(h, w, 13)
+    np.savez_compressed(os.path.join(HERE, "denoise.npz"), radiance=recs[..., 0:3], albedo=recs[..., 3:6],
+                        normal=recs[..., 6:9], variance=recs[..., 9], out=recs[..., 10:13])
+
+
 GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_env, "ggx": gen_ggx,
-          "render": gen_render}
+          "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels}
 
 if __name__ == "__main__":
     ref = os.environ.get("REFERENCE", "/root/reference")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REFERENCE={ref}"], check=True)
     if not os.path.exists(os.path.join(SCENES, "env_small.hdr")):
         make_env_fixture()
-    for g in (sys.argv[1:] or list(GROUPS)):
+    if not os.path.exists(os.path.join(SCENES, "voxels.vox")):
+        make_vox_fixtures()
+    args = sys.argv[1:]
+    if args[:1] == ["render"] and len(args) > 1:  # render <scene> ...: only those renders
+        gen_render(args[1:])
+        args = []
+    elif not args:
+        args = list(GROUPS)
+    for g in args:
         GROUPS[g]()
         print("wrote", g)

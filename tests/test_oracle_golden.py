@@ -159,10 +159,10 @@ def render_z(rad, var, g):
     return z, tot_z
 
 
-@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials"])
+@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels"])
 def test_oracle_render_matches_reference_render(name):
-    """Per-pixel means within 3 sigma of the combined Monte Carlo error (the
-    the benchmark spec's criterion (d)), for the oracle vs the reference's batch means."""
+    """Per-pixel means within 3 sigma of the combined Monte Carlo error, for
+    the oracle vs the reference's batch means."""
     g = load_golden(f"render_{name}")
     sc = mp.load_scene(scene_path(f"{name}.scene"))
     cam = sc.camera
