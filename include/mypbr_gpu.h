@@ -390,7 +390,8 @@ typedef struct mypbr_render_opts {
     int32_t max_scatter;         /* camera.h:29 */
     int32_t transparent_shadows; /* camera.h:34 */
     int32_t collect_features;    /* camera.h:56: also fill albedo, normal, variance */
-    int32_t guided;              /* reserved for the path-guiding proposal; must be 0 */
+    int32_t guided;              /* path guiding: 0 off; 1 on (8 hidden layers); 2, 4 or 8 hidden
+                                    layers. The scene handle keeps the network between renders. */
     uint64_t seed;               /* seeds the counter-based random numbers */
     int32_t samples_per_wave;    /* passes traced together (0 = automatic) */
     int32_t timing;              /* 1: time each kernel kind with CUDA events (stats) */
@@ -527,6 +528,31 @@ void mypbr_denoise_opts_init(mypbr_denoise_opts* opts);
  * Pointers are device memory if on_device, else host memory. Synchronous. */
 int mypbr_gpu_denoise(const double* radiance, const double* albedo, const double* normal, const double* variance,
                       int32_t width, int32_t height, const mypbr_denoise_opts* opts, double* out, int on_device);
+
+/* ----------------------------------------------------- path guiding
+ *
+ * No counterpart in the reference: a learned sampling proposal, used by
+ * mypbr_gpu_render* when opts->guided != 0. An MLP maps a surface vertex
+ * (position in the scene box, normal, outgoing direction; one-blob encoded
+ * into 128 inputs) through `hidden` ReLU layers of 64 units to 64 outputs,
+ * the first 40 of which are 8 von Mises-Fisher lobes (mean xyz, log kappa,
+ * logit). BF16 weights and activations, FP32 accumulation on the tensor
+ * cores. Weights are passed as FP32, matrix after matrix, each [64 out][in]
+ * row-major (in = 128 for the first, 64 after): 64*128 + hidden*64*64 values.
+ * These entry points expose the kernels to the parity tests. Synchronous. */
+
+/* outputs (n x 64) of the network for encoded inputs (n x 128). */
+int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out);
+/* weight gradients (same layout as weights) of sum_i dout_i . out_i. */
+int mypbr_guide_test_backward(int hidden, const float* weights, const float* inputs, const float* dout, int64_t n,
+                              float* grads);
+/* the training loss -c log q(dir) of mixtures given by raw outputs (n x 64)
+ * and its gradient with respect to those outputs (n x 64). */
+int mypbr_guide_test_loss(const float* raw, const float* dirs, const float* c, int64_t n, float* grad, float* loss);
+/* mixture sampling with uniforms u (n x 3): samples (n x 3), the density at
+ * each sample and at the given directions dirs (n x 3). */
+int mypbr_guide_test_mixture(const float* raw, const float* u, const float* dirs, int64_t n, float* samples,
+                             float* pdf_sample, float* pdf_dir);
 
 #ifdef __cplusplus
 }

@@ -114,6 +114,10 @@ def lib():
                                       vp, vp, ctypes.c_int, PASS_CALLBACK, vp, ctypes.POINTER(RenderStatsStruct)]
     L.mypbr_gpu_trace.argtypes = [vp, fp, i64, fp, ip, ctypes.c_int]
     L.mypbr_gpu_bsdf_eval.argtypes = [vp, i32, fp, fp, fp, i64, fp]
+    L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
+    L.mypbr_guide_test_backward.argtypes = [ctypes.c_int, fp, fp, fp, i64, fp]
+    L.mypbr_guide_test_loss.argtypes = [fp, fp, fp, i64, fp, fp]
+    L.mypbr_guide_test_mixture.argtypes = [fp, fp, fp, i64, fp, fp, fp]
     _lib = L
     return L
 
@@ -319,3 +323,56 @@ def ggx_albedo_table():
     out = np.zeros(32 * 32 + 32, dtype=np.float64)
     check(lib().mypbr_ggx_albedo_table(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
     return out[:1024].reshape(32, 32), out[1024:]
+
+
+# ------------------------------------------------------------ path guiding
+
+def guide_params(hidden):
+    """Number of weights of a guiding network with `hidden` hidden layers."""
+    return 64 * 128 + hidden * 64 * 64
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def guide_forward(hidden, weights, inputs):
+    """Network outputs (n, 64) for encoded inputs (n, 128), on the tensor cores."""
+    w, x = _f32(weights), _f32(inputs)
+    out = np.zeros((x.shape[0], 64), dtype=np.float32)
+    check(lib().mypbr_guide_test_forward(int(hidden), _fptr(w), _fptr(x), x.shape[0], _fptr(out)))
+    return out
+
+
+def guide_backward(hidden, weights, inputs, dout):
+    """Weight gradients of sum(dout * outputs), on the tensor cores."""
+    w, x, g = _f32(weights), _f32(inputs), _f32(dout)
+    grads = np.zeros(guide_params(hidden), dtype=np.float32)
+    check(lib().mypbr_guide_test_backward(int(hidden), _fptr(w), _fptr(x), _fptr(g), x.shape[0], _fptr(grads)))
+    return grads
+
+
+def guide_loss(raw, dirs, c):
+    """(gradient (n, 64), loss (n,)) of -c log q(dir) for mixtures given by raw outputs."""
+    raw, dirs, c = _f32(raw), _f32(dirs), _f32(c)
+    n = raw.shape[0]
+    grad = np.zeros((n, 64), dtype=np.float32)
+    loss = np.zeros(n, dtype=np.float32)
+    check(lib().mypbr_guide_test_loss(_fptr(raw), _fptr(dirs), _fptr(c), n, _fptr(grad), _fptr(loss)))
+    return grad, loss
+
+
+def guide_mixture(raw, u, dirs):
+    """(samples (n, 3), pdf at the samples (n,), pdf at dirs (n,)) of the packed mixtures."""
+    raw, u, dirs = _f32(raw), _f32(u), _f32(dirs)
+    n = raw.shape[0]
+    samples = np.zeros((n, 3), dtype=np.float32)
+    ps = np.zeros(n, dtype=np.float32)
+    pd = np.zeros(n, dtype=np.float32)
+    check(lib().mypbr_guide_test_mixture(_fptr(raw), _fptr(u), _fptr(dirs), n, _fptr(samples), _fptr(ps),
+                                         _fptr(pd)))
+    return samples, ps, pd

@@ -6,7 +6,7 @@
 #include <vector>
 
 #include "../../../include/mypbr_gpu.h"
-#include "dev_scene.cuh"
+#include "guide.cuh"
 
 namespace mypbr_dev {
 
@@ -35,6 +35,28 @@ struct RenderBuffers {
     double* feat = nullptr;   // albedo rgb, normal rgb, luminance^2 (7 per pixel)
 };
 
+// The guiding network of a scene and what training it needs on the device.
+struct GuideState {
+    int hidden = 0;                  // 0: no network yet
+    int params = 0;
+    __nv_bfloat16* w = nullptr;      // canonical BF16 copies the kernels read
+    __nv_bfloat16* wt = nullptr;
+    float* master = nullptr;         // FP32 weights, Adam moments, gradients ([out][in] per matrix)
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grad = nullptr;
+    float* stats = nullptr;          // [0] loss sum, [1] weight sum of the current batch
+    __nv_bfloat16* scratch = nullptr;  // per training CTA: transposed activations of one tile
+    int train_ctas = 0;
+    long long steps = 0;             // Adam steps taken
+    float3 box_lo{}, box_inv{};      // scene box for the position encoding
+    // recording buffers (slot-indexed, grown with the render buffers)
+    GuideRecords rec{};
+    size_t rec_slots = 0;
+    __half* packed = nullptr;        // per slot: the vertex's decoded mixture (GuidePacked)
+    size_t packed_slots = 0;
+};
+
 }  // namespace mypbr_dev
 
 struct mypbr_gpu_scene {
@@ -46,6 +68,8 @@ struct mypbr_gpu_scene {
     size_t leaf_ref_count = 0;
     int64_t material_count = 0;
     mypbr_dev::RenderBuffers rb;
+    mypbr_dev::GuideState guide;
+    float3 box_lo{-1.0f, -1.0f, -1.0f}, box_hi{1.0f, 1.0f, 1.0f};  // bounds of the BVH's primitives
 };
 
 namespace mypbr_dev {
@@ -54,6 +78,13 @@ void set_error_message(const std::string& m);
 int cuda_fail(cudaError_t e, const char* what);
 int release_buffers(RenderBuffers& rb);
 int check_device_error(mypbr_gpu_scene* G);
+int release_guide(GuideState& g);
+// Creates the network (seeded initial weights) if the scene has none of this size.
+int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed);
+// Mixture buffers for `mix_slots` path slots, training records for the first `rec_slots`.
+int guide_ensure_records(mypbr_gpu_scene* G, size_t mix_slots, size_t rec_slots, int depth);
+// `steps` Adam steps on batches drawn from the recorded vertices.
+int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaStream_t st);
 
 }  // namespace mypbr_dev
 

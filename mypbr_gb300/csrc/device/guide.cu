@@ -1,0 +1,728 @@
+// Training of the guiding network on the tensor cores, its Adam optimiser,
+// and pointwise entry points that the tests compare with the CPU oracle.
+//
+// One training step: k_guide_prep sums the sample weights of a batch drawn
+// from the recorded vertices; k_guide_train runs forward and backward for
+// tiles of 128 samples (one CTA of 128 threads per tile, a thread per
+// sample) and adds the weight gradients into FP32 sums; k_guide_adam updates
+// the FP32 master weights and rewrites the BF16 copies the kernels read.
+//
+// Backward per matrix l with input H (batch x in) and output gradient dZ
+// (batch x 64), both BF16:
+//   dW^T = H^T dZ   (tcgen05.mma M = 128 (in, zero-padded), N = 64, K = 128 batch)
+//   dX   = dZ W     (M = 128 batch, N = 64 in, K = 64), masked by the ReLU of
+//                   the layer below to give that layer's dZ.
+// The transposed activations H^T of each layer are kept in a per-CTA scratch
+// area in global memory (L2 resident) between the forward and backward pass.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dev_shading.cuh"
+#include "gpu_scene.h"
+
+namespace mypbr_dev {
+
+namespace {
+
+constexpr size_t kTrainSmem = 32768 + 16384 + 32768 + 16384 + 64;
+
+MYPBR_DEV uint32_t hash_u32(uint32_t a, uint32_t b) {
+    uint64_t z = mix64((uint64_t(a) << 32) ^ b ^ 0x5bd1e995ull);
+    return uint32_t(z ^ (z >> 32));
+}
+
+// Loss weight of a recorded vertex: luminance of (f cos / pdf) * L_i, with
+// L_i = (final radiance - radiance at the next vertex) / throughput there.
+MYPBR_DEV float record_weight(const GuideRecords& R, uint32_t r, uint32_t slot) {
+    float4 f = R.fac[r], mk = R.mark[r], bn = R.bnext[r], fin = R.fin[slot];
+    float li_r = bn.x > 0.0f ? (fin.x - mk.x) / bn.x : 0.0f;
+    float li_g = bn.y > 0.0f ? (fin.y - mk.y) / bn.y : 0.0f;
+    float li_b = bn.z > 0.0f ? (fin.z - mk.z) / bn.z : 0.0f;
+    float c = 0.2126f * f.x * li_r + 0.7152f * f.y * li_g + 0.0722f * f.z * li_b;
+    return isfinite(c) ? fminf(fmaxf(c, 0.0f), 1e6f) : 0.0f;
+}
+
+// Training rows drawn from the recorded vertices (uniformly, by a hash of
+// the step and the row).
+struct RecordSource {
+    GuideRecords R;
+    uint32_t step;
+    const float* stats;  // [1]: sum of the batch's weights
+    MYPBR_DEV long long count(long long rows) const { return rows; }
+    MYPBR_DEV bool pick(long long i, uint32_t& r) const {
+        uint32_t n = *R.count;
+        if (i < 0 || n == 0)
+            return false;
+        r = R.list[hash_u32(step, uint32_t(i)) % n];
+        return true;
+    }
+    MYPBR_DEV void fill(long long i, __nv_bfloat16* A, int row) const {
+        uint32_t r;
+        if (!pick(i, r)) {
+            guide_encode_row(nullptr, A, row);
+            return;
+        }
+        float4 a = R.in0[r], b = R.in1[r];
+        float s[7] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z};
+        guide_encode_row(s, A, row);
+    }
+    MYPBR_DEV float dout(long long i, const float* v, float* g) const {
+#pragma unroll
+        for (int k = 0; k < kGuideOut; k++)
+            g[k] = 0.0f;
+        uint32_t r;
+        float total = stats[1];
+        if (!pick(i, r) || !(total > 0.0f))
+            return 0.0f;
+        float c = record_weight(R, r, r / uint32_t(R.depth)) / total;
+        if (c <= 0.0f)
+            return 0.0f;
+        float4 d = R.dir[r];
+        return guide_loss_grad(v, f3(d.x, d.y, d.z), c, g);
+    }
+};
+
+// Rows given by the caller: encoded inputs and output gradients (tests).
+struct GivenSource {
+    const float* inputs;  // n x 128
+    const float* grads;   // n x 64
+    MYPBR_DEV long long count(long long rows) const { return rows; }
+    MYPBR_DEV void fill(long long i, __nv_bfloat16* A, int row) const {
+#pragma unroll 1
+        for (int b = 0; b < kGuideIn / 8; b++) {
+            float v[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++)
+                v[e] = i >= 0 ? inputs[i * kGuideIn + 8 * b + e] : 0.0f;
+            uint4 u;
+            u.x = pack_bf16(v[0], v[1]);
+            u.y = pack_bf16(v[2], v[3]);
+            u.z = pack_bf16(v[4], v[5]);
+            u.w = pack_bf16(v[6], v[7]);
+            *reinterpret_cast<uint4*>(A + canon(row, 8 * b, kGuideIn)) = u;
+        }
+    }
+    MYPBR_DEV float dout(long long i, const float*, float* g) const {
+#pragma unroll
+        for (int k = 0; k < kGuideOut; k++)
+            g[k] = i >= 0 ? grads[i * kGuideOut + k] : 0.0f;
+        return 0.0f;
+    }
+};
+
+struct RowSink {
+    float* out;  // n x 64
+    MYPBR_DEV void put(long long i, const float* v) const {
+        float4* o = reinterpret_cast<float4*>(out + i * kGuideOut);
+#pragma unroll
+        for (int k = 0; k < kGuideOut / 4; k++)
+            o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    }
+};
+
+MYPBR_DEV void copy_u4(void* dst, const void* src, int bytes) {
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x)
+        d[k] = s[k];
+}
+
+// Row `row` of a canonical K = 128 (batch) tile holding a transposed matrix:
+// writes value v of feature f at (f, row).
+MYPBR_DEV void store_col_bf16(__nv_bfloat16* tileT, int row, int features, const float* v) {
+    for (int f = 0; f < features; f++)
+        tileT[canon(f, row, 128)] = __float2bfloat16_rn(v[f]);
+}
+
+template <int HIDDEN, class Src>
+__global__ void __launch_bounds__(128) k_guide_train(GuideNetView net, Src src, long long rows,
+                                                     __nv_bfloat16* scratch, float* loss_sum) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(smem);  // 128 x 128
+    __nv_bfloat16* Wb = A + 128 * 128;                            // 64 x 128
+    __nv_bfloat16* HT = Wb + 64 * 128;                            // 128 x 128
+    __nv_bfloat16* DZT = HT + 128 * 128;                          // 64 x 128
+    uint64_t* bar = reinterpret_cast<uint64_t*>(DZT + 64 * 128);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+    __nv_bfloat16* scr = scratch + size_t(blockIdx.x) * (HIDDEN + 1) * 128 * 128;
+    const int row = threadIdx.x, warp = threadIdx.x >> 5;
+    // rows 64..127 of HT stay zero for the 64-wide layers (they pad M to 128)
+    for (int k = threadIdx.x; k < 64 * 128 / 8; k += blockDim.x)
+        reinterpret_cast<uint4*>(HT + 64 * 128)[k] = make_uint4(0, 0, 0, 0);
+    if (warp == 0)
+        tc::tmem_alloc(tmem_slot, 128);
+    if (threadIdx.x == 0)
+        tc::bar_init(bar, 1);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tmem_slot;
+    uint32_t phase = 0;
+    const uint32_t idesc = tc::idesc_bf16(128, 64);
+    bool failed = false;
+    float loss_acc = 0.0f;
+    long long tiles = (rows + 127) / 128;
+    // Issues the MMAs (thread 0), then every thread waits for them; false on a timeout.
+    auto wait_mma = [&]() {
+        bool ok = tc::bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0)
+                atomicCAS(net.error, 0, 3);
+            tc::bar_wait(bar, phase ^ 1);  // once more, bounded, for the MMAs in flight
+            return false;
+        }
+        tc::fence_after();
+        return true;
+    };
+    for (long long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        long long i = tile * 128 + row;
+        long long src_i = i < rows ? i : -1;
+        src.fill(src_i, A, row);
+        {  // H_0^T: this row's 128 inputs, read back from the tile
+            float v[128];
+#pragma unroll
+            for (int b = 0; b < 16; b++) {
+                uint4 u = *reinterpret_cast<const uint4*>(A + canon(row, 8 * b, 128));
+                const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&u);
+#pragma unroll
+                for (int e = 0; e < 8; e++)
+                    v[8 * b + e] = __bfloat162float(h[e]);
+            }
+            store_col_bf16(scr, row, 128, v);
+        }
+        uint32_t mask[2 * HIDDEN + 2];
+        float dz[64];
+        // ---- forward
+#pragma unroll
+        for (int l = 0; l <= HIDDEN; l++) {
+            const int K = guide_in(l);
+            copy_u4(Wb, net.w + guide_offset(l), 64 * K * 2);
+            tc::fence_smem();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                tc::fence_after();
+                uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(Wb);
+                for (int s = 0; s < K / 16; s++)
+                    tc::mma(tmem, tc::desc(a0 + 256 * s, 128, K * 16), tc::desc(b0 + 256 * s, 128, K * 16), idesc,
+                            s > 0);
+                tc::commit(bar);
+            }
+            if (!wait_mma()) {
+                failed = true;
+                break;
+            }
+            float v[64];
+            tc::tmem_row64(tmem, 0, v);
+            tc::fence_before();
+            if (l < HIDDEN) {
+                uint32_t m0 = 0, m1 = 0;
+#pragma unroll
+                for (int k = 0; k < 64; k++) {
+                    bool on = v[k] > 0.0f;
+                    if (k < 32)
+                        m0 |= on ? (1u << k) : 0u;
+                    else
+                        m1 |= on ? (1u << (k - 32)) : 0u;
+                    v[k] = on ? v[k] : 0.0f;
+                }
+                mask[2 * l] = m0;
+                mask[2 * l + 1] = m1;
+                store_row_bf16(A, row, kGuideWidth, 0, v);
+                // the stored BF16 values, transposed, for this layer's weight gradient
+                float r[64];
+#pragma unroll
+                for (int k = 0; k < 64; k++)
+                    r[k] = __bfloat162float(__float2bfloat16_rn(v[k]));
+                store_col_bf16(scr + size_t(l + 1) * 128 * 128, row, 64, r);
+            } else {
+                loss_acc += src.dout(src_i, v, dz);
+            }
+        }
+        if (failed)
+            break;
+        // ---- backward
+#pragma unroll
+        for (int l = HIDDEN; l >= 0; l--) {
+            const int in = guide_in(l);
+            store_row_bf16(A, row, kGuideWidth, 0, dz);  // dZ [batch][64]
+            store_col_bf16(DZT, row, 64, dz);           // dZ^T [64][batch]
+            copy_u4(Wb, net.wt + guide_offset(l), in * 64 * 2);
+            copy_u4(HT, scr + size_t(l) * 128 * 128, in * 128 * 2);
+            tc::fence_smem();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                tc::fence_after();
+                uint32_t h0 = tc::smem_u32(HT), z0 = tc::smem_u32(DZT);
+                for (int s = 0; s < 8; s++)
+                    tc::mma(tmem + 64, tc::desc(h0 + 256 * s, 128, 2048), tc::desc(z0 + 256 * s, 128, 2048), idesc,
+                            s > 0);
+                if (l > 0) {
+                    uint32_t a0 = tc::smem_u32(A), w0 = tc::smem_u32(Wb);
+                    for (int s = 0; s < 4; s++)
+                        tc::mma(tmem, tc::desc(a0 + 256 * s, 128, 1024), tc::desc(w0 + 256 * s, 128, 1024), idesc,
+                                s > 0);
+                }
+                tc::commit(bar);
+            }
+            if (!wait_mma()) {
+                failed = true;
+                break;
+            }
+            float gw[64];
+            tc::tmem_row64(tmem, 64, gw);  // row = input feature `row`
+            if (row < in) {
+                float* gbase = net.grad + guide_offset(l) + row;
+#pragma unroll 4
+                for (int j = 0; j < 64; j++)
+                    if (gw[j] != 0.0f)
+                        atomicAdd(gbase + j * in, gw[j]);
+            }
+            if (l > 0) {
+                float dx[64];
+                tc::tmem_row64(tmem, 0, dx);
+                uint32_t m0 = mask[2 * (l - 1)], m1 = mask[2 * (l - 1) + 1];
+#pragma unroll
+                for (int k = 0; k < 64; k++) {
+                    bool on = k < 32 ? ((m0 >> k) & 1u) : ((m1 >> (k - 32)) & 1u);
+                    dz[k] = on ? dx[k] : 0.0f;
+                }
+            }
+            tc::fence_before();
+            if (l == 0) {  // layer 0 filled all of HT: clear the padding rows again
+                __syncthreads();
+                for (int k = threadIdx.x; k < 64 * 128 / 8; k += blockDim.x)
+                    reinterpret_cast<uint4*>(HT + 64 * 128)[k] = make_uint4(0, 0, 0, 0);
+            }
+        }
+    }
+    // warp-reduced loss
+    for (int o = 16; o > 0; o >>= 1)
+        loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
+    if ((threadIdx.x & 31) == 0 && loss_sum && loss_acc != 0.0f)
+        atomicAdd(loss_sum, loss_acc);
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after();
+        tc::tmem_free(tmem, 128);
+    }
+}
+
+// Sum of the batch's weights (normalises the loss so the weights sum to 1).
+__global__ void k_guide_prep(RecordSource src, long long rows, float* stats) {
+    float acc = 0.0f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < rows;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint32_t r;
+        if (src.pick(i, r))
+            acc += record_weight(src.R, r, r / uint32_t(src.R.depth));
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc != 0.0f)
+        atomicAdd(stats + 1, acc);
+}
+
+MYPBR_DEV void param_coords(int p, int& l, int& j, int& t, int& in) {
+    if (p < kGuideWidth * kGuideIn) {
+        l = 0;
+        in = kGuideIn;
+    } else {
+        l = 1 + (p - kGuideWidth * kGuideIn) / (kGuideWidth * kGuideWidth);
+        in = kGuideWidth;
+    }
+    int local = p - guide_offset(l);
+    j = local / in;
+    t = local % in;
+}
+
+// Adam (Kingma and Ba 2015) on the FP32 masters, then the BF16 copies.
+// lr == 0 only republishes the copies.
+__global__ void k_guide_adam(float* master, float* m, float* v, float* grad, __nv_bfloat16* w,
+                             __nv_bfloat16* wt, int params, float lr, float b1t, float b2t) {
+    const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < params; p += gridDim.x * blockDim.x) {
+        float x = master[p];
+        if (lr > 0.0f) {
+            float g = grad[p];
+            g = isfinite(g) ? g : 0.0f;
+            float mm = b1 * m[p] + (1.0f - b1) * g;
+            float vv = b2 * v[p] + (1.0f - b2) * g * g;
+            m[p] = mm;
+            v[p] = vv;
+            x -= lr * (mm / (1.0f - b1t)) / (sqrtf(vv / (1.0f - b2t)) + eps);
+            master[p] = x;
+        }
+        grad[p] = 0.0f;
+        int l, j, t, in;
+        param_coords(p, l, j, t, in);
+        __nv_bfloat16 h = __float2bfloat16_rn(x);
+        w[guide_offset(l) + canon(j, t, in)] = h;
+        wt[guide_offset(l) + canon(t, j, kGuideWidth)] = h;
+    }
+}
+
+__global__ void k_loss_test(const float* raw, const float* dirs, const float* c, long long n, float* grad,
+                            float* loss) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float g[kGuideOut];
+        float3 w = f3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
+        loss[i] = guide_loss_grad(raw + i * kGuideOut, w, c[i], g);
+        for (int k = 0; k < kGuideOut; k++)
+            grad[i * kGuideOut + k] = k < kGuideUsed ? g[k] : 0.0f;
+    }
+}
+
+__global__ void k_mixture_test(const float* raw, const float* u, const float* dirs, long long n, float* samples,
+                               float* pdf_sample, float* pdf_dir) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        GuidePacked pk;
+        guide_pack(raw + i * kGuideOut, pk);
+        GuideMix m;
+        guide_unpack(pk, m);
+        float3 s = guide_sample(m, u[3 * i], u[3 * i + 1], u[3 * i + 2]);
+        samples[3 * i] = s.x;
+        samples[3 * i + 1] = s.y;
+        samples[3 * i + 2] = s.z;
+        pdf_sample[i] = guide_pdf(m, s);
+        pdf_dir[i] = guide_pdf(m, normalize(f3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2])));
+    }
+}
+
+template <class Kernel>
+int set_smem(Kernel k, size_t bytes) {
+    MYPBR_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+    return MYPBR_OK;
+}
+
+template <int H, class Src>
+int launch_train(GuideNetView net, Src src, long long rows, int ctas, __nv_bfloat16* scratch, float* loss,
+                 cudaStream_t st) {
+    auto k = k_guide_train<H, Src>;
+    int rc = set_smem(k, kTrainSmem);
+    if (rc != MYPBR_OK)
+        return rc;
+    k<<<ctas, 128, kTrainSmem, st>>>(net, src, rows, scratch, loss);
+    MYPBR_CUDA(cudaGetLastError());
+    return MYPBR_OK;
+}
+
+template <class Src>
+int train_dispatch(int hidden, GuideNetView net, Src src, long long rows, int ctas, __nv_bfloat16* scratch,
+                   float* loss, cudaStream_t st) {
+    switch (hidden) {
+        case 2: return launch_train<2>(net, src, rows, ctas, scratch, loss, st);
+        case 4: return launch_train<4>(net, src, rows, ctas, scratch, loss, st);
+        case 8: return launch_train<8>(net, src, rows, ctas, scratch, loss, st);
+        default:
+            set_error_message("guiding networks have 2, 4 or 8 hidden layers");
+            return MYPBR_ERR_UNSUPPORTED;
+    }
+}
+
+// Seeded He-uniform initial weights (the output layer scaled by 1/2).
+std::vector<float> initial_weights(int hidden, unsigned long long seed) {
+    std::vector<float> w(size_t(guide_params(hidden)));
+    uint64_t state = seed * 0x9e3779b97f4a7c15ull + 0x632be59bd9b4e019ull;
+    auto uniform = [&]() {
+        state = state * 6364136223846793005ull + 1442695040888963407ull;
+        return double(state >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l <= hidden; l++) {
+        int in = guide_in(l);
+        double b = std::sqrt(6.0 / in) * (l == hidden ? 0.5 : 1.0);
+        for (int k = 0; k < kGuideWidth * in; k++)
+            w[size_t(guide_offset(l) + k)] = float((2 * uniform() - 1) * b);
+    }
+    return w;
+}
+
+template <typename T>
+int dalloc(T*& p, size_t n) {
+    MYPBR_CUDA(cudaMalloc(&p, n * sizeof(T)));
+    return MYPBR_OK;
+}
+
+// A network for the test entry points: weights given by the caller.
+struct TempNet {
+    GuideState g;
+    int* err = nullptr;
+    ~TempNet() {
+        release_guide(g);
+        cudaFree(err);
+    }
+};
+
+int temp_net(TempNet& T, int hidden, const float* weights) {
+    if (hidden != 2 && hidden != 4 && hidden != 8) {
+        set_error_message("guiding networks have 2, 4 or 8 hidden layers");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    GuideState& g = T.g;
+    g.hidden = hidden;
+    g.params = guide_params(hidden);
+    size_t P = size_t(g.params);
+    int rc;
+    if ((rc = dalloc(g.w, P)) || (rc = dalloc(g.wt, P)) || (rc = dalloc(g.master, P)) || (rc = dalloc(g.m, P)) ||
+        (rc = dalloc(g.v, P)) || (rc = dalloc(g.grad, P)) || (rc = dalloc(T.err, 1)))
+        return rc;
+    MYPBR_CUDA(cudaMemcpy(g.master, weights, P * 4, cudaMemcpyHostToDevice));
+    MYPBR_CUDA(cudaMemset(g.grad, 0, P * 4));
+    MYPBR_CUDA(cudaMemset(T.err, 0, 4));
+    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
+    MYPBR_CUDA(cudaGetLastError());
+    return MYPBR_OK;
+}
+
+GuideNetView view_of(GuideState& g, int* err) { return GuideNetView{g.hidden, g.w, g.wt, g.grad, err}; }
+
+int read_error(int* err) {
+    int e = 0;
+    MYPBR_CUDA(cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost));
+    if (e != 0) {
+        set_error_message("a tensor-core wait of the guiding network timed out");
+        return MYPBR_ERR_DEVICE_CHECK;
+    }
+    return MYPBR_OK;
+}
+
+}  // namespace
+
+int release_guide(GuideState& g) {
+    void* ptrs[] = {g.w, g.wt, g.master, g.m, g.v, g.grad, g.stats, g.scratch, g.rec.in0, g.rec.in1, g.rec.dir,
+                    g.rec.fac, g.rec.mark, g.rec.bnext, g.rec.fin, g.rec.list, g.rec.count, g.packed};
+    for (void* p : ptrs)
+        if (p)
+            cudaFree(p);
+    g = GuideState{};
+    return MYPBR_OK;
+}
+
+int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed) {
+    GuideState& g = G->guide;
+    if (g.hidden == hidden)
+        return MYPBR_OK;
+    if (hidden != 2 && hidden != 4 && hidden != 8) {
+        set_error_message("guiding networks have 2, 4 or 8 hidden layers");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    GuideRecords keep = g.rec;
+    size_t keep_slots = g.rec_slots;
+    __half* keep_packed = g.packed;
+    size_t keep_packed_slots = g.packed_slots;
+    g.rec = GuideRecords{};
+    g.packed = nullptr;
+    release_guide(g);
+    g.rec = keep;
+    g.rec_slots = keep_slots;
+    g.packed = keep_packed;
+    g.packed_slots = keep_packed_slots;
+    g.hidden = hidden;
+    g.params = guide_params(hidden);
+    size_t P = size_t(g.params);
+    g.train_ctas = G->sm_count;
+    int rc;
+    if ((rc = dalloc(g.w, P)) || (rc = dalloc(g.wt, P)) || (rc = dalloc(g.master, P)) || (rc = dalloc(g.m, P)) ||
+        (rc = dalloc(g.v, P)) || (rc = dalloc(g.grad, P)) || (rc = dalloc(g.stats, 4)) ||
+        (rc = dalloc(g.scratch, size_t(g.train_ctas) * (hidden + 1) * 128 * 128)))
+        return rc;
+    std::vector<float> w0 = initial_weights(hidden, seed);
+    MYPBR_CUDA(cudaMemcpy(g.master, w0.data(), P * 4, cudaMemcpyHostToDevice));
+    MYPBR_CUDA(cudaMemset(g.m, 0, P * 4));
+    MYPBR_CUDA(cudaMemset(g.v, 0, P * 4));
+    MYPBR_CUDA(cudaMemset(g.grad, 0, P * 4));
+    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
+    MYPBR_CUDA(cudaGetLastError());
+    g.steps = 0;
+    // the position encoding spans the scene's bounding box
+    float3 lo = G->box_lo, hi = G->box_hi;
+    g.box_lo = lo;
+    g.box_inv = f3(1.0f / fmaxf(hi.x - lo.x, 1e-6f), 1.0f / fmaxf(hi.y - lo.y, 1e-6f), 1.0f / fmaxf(hi.z - lo.z, 1e-6f));
+    return MYPBR_OK;
+}
+
+int guide_ensure_records(mypbr_gpu_scene* G, size_t mix_slots, size_t slots, int depth) {
+    GuideState& g = G->guide;
+    if (g.packed_slots < mix_slots) {
+        if (g.packed)
+            cudaFree(g.packed);
+        g.packed = nullptr;
+        g.packed_slots = 0;
+        int rc = dalloc(g.packed, mix_slots * sizeof(GuidePacked) / sizeof(__half));
+        if (rc != MYPBR_OK)
+            return rc;
+        g.packed_slots = mix_slots;
+    }
+    if (g.rec_slots >= slots && g.rec.depth == depth)
+        return MYPBR_OK;
+    void* old[] = {g.rec.in0, g.rec.in1, g.rec.dir, g.rec.fac, g.rec.mark, g.rec.bnext, g.rec.fin, g.rec.list,
+                   g.rec.count};
+    for (void* p : old)
+        if (p)
+            cudaFree(p);
+    g.rec = GuideRecords{};
+    g.rec_slots = 0;
+    size_t n = slots * size_t(depth);
+    int rc;
+    if ((rc = dalloc(g.rec.in0, n)) || (rc = dalloc(g.rec.in1, n)) || (rc = dalloc(g.rec.dir, n)) ||
+        (rc = dalloc(g.rec.fac, n)) || (rc = dalloc(g.rec.mark, n)) || (rc = dalloc(g.rec.bnext, n)) ||
+        (rc = dalloc(g.rec.fin, slots)) || (rc = dalloc(g.rec.list, n)) || (rc = dalloc(g.rec.count, 1)))
+        return rc;
+    g.rec.depth = depth;
+    g.rec.capacity = uint32_t(n);
+    g.rec_slots = slots;
+    MYPBR_CUDA(cudaMemset(g.rec.count, 0, 4));
+    return MYPBR_OK;
+}
+
+int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaStream_t st) {
+    GuideState& g = G->guide;
+    if (g.hidden == 0 || g.rec.count == nullptr)
+        return MYPBR_OK;
+    long long rows = (long long)batch_tiles * 128;
+    GuideNetView net = view_of(g, G->dev.error);
+    for (int s = 0; s < steps; s++) {
+        RecordSource src{g.rec, uint32_t(g.steps * 7919 + 17), g.stats};
+        MYPBR_CUDA(cudaMemsetAsync(g.stats, 0, 4 * sizeof(float), st));
+        k_guide_prep<<<G->sm_count * 2, 256, 0, st>>>(src, rows, g.stats);
+        MYPBR_CUDA(cudaGetLastError());
+        int rc = train_dispatch(g.hidden, net, src, rows, g.train_ctas, g.scratch, g.stats, st);
+        if (rc != MYPBR_OK)
+            return rc;
+        g.steps++;
+        float b1t = std::pow(0.9f, float(g.steps)), b2t = std::pow(0.99f, float(g.steps));
+        k_guide_adam<<<(g.params + 255) / 256, 256, 0, st>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, lr,
+                                                            b1t, b2t);
+        MYPBR_CUDA(cudaGetLastError());
+    }
+    return MYPBR_OK;
+}
+
+}  // namespace mypbr_dev
+
+using namespace mypbr_dev;
+
+extern "C" {
+
+int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out) {
+    if (!weights || !inputs || !out || n < 0)
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    TempNet T;
+    int rc = temp_net(T, hidden, weights);
+    if (rc != MYPBR_OK)
+        return rc;
+    float *d_in = nullptr, *d_out = nullptr;
+    if ((rc = dalloc(d_in, size_t(n) * kGuideIn + 1)) || (rc = dalloc(d_out, size_t(n) * kGuideOut + 1)))
+        return rc;
+    cudaMemcpy(d_in, inputs, size_t(n) * kGuideIn * 4, cudaMemcpyHostToDevice);
+    size_t smem = guide_forward_smem(hidden);
+    auto k = k_guide_forward<GivenSource, RowSink>;
+    rc = set_smem(k, smem);
+    if (rc == MYPBR_OK) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        long long tiles = (n + 127) / 128;
+        int grid = int(std::min<long long>(std::max<long long>(tiles, 1), 2LL * sms));
+        k<<<grid, 128, smem>>>(view_of(T.g, T.err), GivenSource{d_in, nullptr}, RowSink{d_out}, n);
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "k_guide_forward");
+        else
+            rc = read_error(T.err);
+    }
+    if (rc == MYPBR_OK)
+        cudaMemcpy(out, d_out, size_t(n) * kGuideOut * 4, cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    cudaFree(d_out);
+    return rc;
+}
+
+int mypbr_guide_test_backward(int hidden, const float* weights, const float* inputs, const float* dout, int64_t n,
+                              float* grads) {
+    if (!weights || !inputs || !dout || !grads || n < 0)
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    TempNet T;
+    int rc = temp_net(T, hidden, weights);
+    if (rc != MYPBR_OK)
+        return rc;
+    float *d_in = nullptr, *d_g = nullptr;
+    __nv_bfloat16* scratch = nullptr;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long tiles = (n + 127) / 128;
+    int ctas = int(std::min<long long>(std::max<long long>(tiles, 1), sms));
+    if ((rc = dalloc(d_in, size_t(n) * kGuideIn + 1)) || (rc = dalloc(d_g, size_t(n) * kGuideOut + 1)) ||
+        (rc = dalloc(scratch, size_t(ctas) * (hidden + 1) * 128 * 128)))
+        return rc;
+    cudaMemcpy(d_in, inputs, size_t(n) * kGuideIn * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_g, dout, size_t(n) * kGuideOut * 4, cudaMemcpyHostToDevice);
+    rc = train_dispatch(hidden, view_of(T.g, T.err), GivenSource{d_in, d_g}, n, ctas, scratch, nullptr, 0);
+    if (rc == MYPBR_OK) {
+        cudaError_t e = cudaDeviceSynchronize();
+        rc = e != cudaSuccess ? cuda_fail(e, "k_guide_train") : read_error(T.err);
+    }
+    if (rc == MYPBR_OK)
+        cudaMemcpy(grads, T.g.grad, size_t(T.g.params) * 4, cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    cudaFree(d_g);
+    cudaFree(scratch);
+    return rc;
+}
+
+int mypbr_guide_test_loss(const float* raw, const float* dirs, const float* c, int64_t n, float* grad, float* loss) {
+    if (!raw || !dirs || !c || !grad || !loss || n < 0)
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    float *d_raw, *d_dirs, *d_c, *d_grad, *d_loss;
+    int rc;
+    if ((rc = dalloc(d_raw, size_t(n) * kGuideOut + 1)) || (rc = dalloc(d_dirs, size_t(n) * 3 + 1)) ||
+        (rc = dalloc(d_c, size_t(n) + 1)) || (rc = dalloc(d_grad, size_t(n) * kGuideOut + 1)) ||
+        (rc = dalloc(d_loss, size_t(n) + 1)))
+        return rc;
+    cudaMemcpy(d_raw, raw, size_t(n) * kGuideOut * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_dirs, dirs, size_t(n) * 12, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_c, c, size_t(n) * 4, cudaMemcpyHostToDevice);
+    k_loss_test<<<64, 128>>>(d_raw, d_dirs, d_c, n, d_grad, d_loss);
+    cudaError_t e = cudaDeviceSynchronize();
+    rc = e != cudaSuccess ? cuda_fail(e, "k_loss_test") : MYPBR_OK;
+    if (rc == MYPBR_OK) {
+        cudaMemcpy(grad, d_grad, size_t(n) * kGuideOut * 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(loss, d_loss, size_t(n) * 4, cudaMemcpyDeviceToHost);
+    }
+    for (void* p : {(void*)d_raw, (void*)d_dirs, (void*)d_c, (void*)d_grad, (void*)d_loss})
+        cudaFree(p);
+    return rc;
+}
+
+int mypbr_guide_test_mixture(const float* raw, const float* u, const float* dirs, int64_t n, float* samples,
+                             float* pdf_sample, float* pdf_dir) {
+    if (!raw || !u || !dirs || !samples || !pdf_sample || !pdf_dir || n < 0)
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    float *d_raw, *d_u, *d_dirs, *d_s, *d_ps, *d_pd;
+    int rc;
+    if ((rc = dalloc(d_raw, size_t(n) * kGuideOut + 1)) || (rc = dalloc(d_u, size_t(n) * 3 + 1)) ||
+        (rc = dalloc(d_dirs, size_t(n) * 3 + 1)) || (rc = dalloc(d_s, size_t(n) * 3 + 1)) ||
+        (rc = dalloc(d_ps, size_t(n) + 1)) || (rc = dalloc(d_pd, size_t(n) + 1)))
+        return rc;
+    cudaMemcpy(d_raw, raw, size_t(n) * kGuideOut * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_u, u, size_t(n) * 12, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_dirs, dirs, size_t(n) * 12, cudaMemcpyHostToDevice);
+    k_mixture_test<<<64, 128>>>(d_raw, d_u, d_dirs, n, d_s, d_ps, d_pd);
+    cudaError_t e = cudaDeviceSynchronize();
+    rc = e != cudaSuccess ? cuda_fail(e, "k_mixture_test") : MYPBR_OK;
+    if (rc == MYPBR_OK) {
+        cudaMemcpy(samples, d_s, size_t(n) * 12, cudaMemcpyDeviceToHost);
+        cudaMemcpy(pdf_sample, d_ps, size_t(n) * 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(pdf_dir, d_pd, size_t(n) * 4, cudaMemcpyDeviceToHost);
+    }
+    for (void* p : {(void*)d_raw, (void*)d_u, (void*)d_dirs, (void*)d_s, (void*)d_ps, (void*)d_pd})
+        cudaFree(p);
+    return rc;
+}
+
+}  // extern "C"

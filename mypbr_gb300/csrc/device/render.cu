@@ -54,6 +54,14 @@ struct WaveParams {
     int pass0, npass;
     int first_row, band_rows;  // the rows rendered: [first_row, first_row + band_rows)
     unsigned long long* totals;  // extension rays, shadow rays
+    // path guiding
+    int guided;                // mixtures were computed for this wave's guidable vertices
+    float guide_alpha;         // probability of sampling the mixture there (one-sample MIS)
+    int record;                // write training records
+    GuideRecords rec;          // slots below rec_slots record their first rec.depth vertices
+    uint32_t rec_slots;
+    GuidePacked* guide_mix;    // per slot
+    float3 guide_lo, guide_inv;
 };
 
 // Counters: extension queue length entering bounce d; shadow queue length of
@@ -290,8 +298,16 @@ MYPBR_DEV float3 class_eval(const DeviceScene& S, int mi, float3 d, const Surfac
         return eval_inner<class_type<C>()>(S, S.materials[mi], d, s, dir);
 }
 
-// One bounce of ray_color (camera.h:370-457) for the paths of shading class C.
+// Classes whose non-specular vertices the guiding network serves.
 template <int C>
+constexpr bool kGuidable() {
+    return C == kClassLambert || C == kClassMetal || C == kClassPrincipled || C == kClassGeneric;
+}
+
+// One bounce of ray_color (camera.h:370-457) for the paths of shading class C.
+// GUIDED: the variant of guided renders, which reads the learned mixtures and
+// writes training records (plain renders keep the leaner code).
+template <int C, bool GUIDED>
 __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
     uint32_t n = *class_counter(P, depth, C);
     const uint32_t* q = class_queue(P, C);
@@ -310,6 +326,13 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
         uint32_t scatter_count = flags >> 24;
         bool terminate = false, pushed_shadow = false;
         float3 new_o = o, new_d = d;
+        int rec_at = -1;  // record written at this vertex (index), listed if the path goes on
+        if (GUIDED && P.record && slot < P.rec_slots && depth >= 1 && depth - 1 < P.rec.depth) {
+            // what the previous vertex's record needs: radiance and throughput on arrival here
+            uint32_t r = slot * uint32_t(P.rec.depth) + uint32_t(depth - 1);
+            P.rec.mark[r] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+            P.rec.bnext[r] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+        }
         if constexpr (C == kClassMiss) {
             // camera.h:373-387: the sky is a light, weighted like emission
             if (!seen) {
@@ -371,6 +394,22 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
                 bool capped = cap > 0 && ++cnt >= uint32_t(cap);
                 bool last = depth == P.max_depth - 1 || capped;
                 seen = false;
+                // The learned mixture as one more proposal: directions come from
+                // it with probability alpha, else from the BSDF, and every MIS
+                // weight and throughput uses the combined density.
+                GuideMix gm;
+                bool use_guide = false;
+                if constexpr (GUIDED && kGuidable<C>()) {
+                    if (P.guided && P.guide_alpha > 0.0f && !vol) {
+                        guide_unpack(P.guide_mix[slot], gm);
+                        use_guide = true;
+                    }
+                }
+                auto mis_pdf = [&](float3 dir) {
+                    float pb = sr.pdf.value(dir);
+                    return use_guide ? P.guide_alpha * guide_pdf(gm, normalize(dir)) + (1.0f - P.guide_alpha) * pb
+                                     : pb;
+                };
                 if (P.has_lights) {  // camera.h:466-506; the shadow ray is traced by k_shadow
                     // With the sky as the only light, the sample carries its own
                     // radiance and density; the shadow ray then only tests visibility
@@ -386,7 +425,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
                     if (lp > 0.0f) {
                         float3 f = class_eval<C>(S, mat, d, s, to_light);
                         if (f.x > 0.0f || f.y > 0.0f || f.z > 0.0f) {
-                            float w = last ? 1.0f : power_heuristic(lp, sr.pdf.value(to_light));
+                            float w = last ? 1.0f : power_heuristic(lp, mis_pdf(to_light));
                             float3 c = beta * f * sky * (w / lp);
                             float3 sd = normalize(to_light);
                             P.B.sh_o[slot] = make_float4(s.p.x, s.p.y, s.p.z, 0.0f);
@@ -400,16 +439,36 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
                 if (capped) {
                     terminate = true;
                 } else {
-                    float3 dir = sr.pdf.generate(g);
-                    float spdf = sr.pdf.value(dir);
+                    float3 dir;
+                    if (use_guide && g.next() < P.guide_alpha) {
+                        float u0 = g.next(), u1 = g.next();
+                        dir = guide_sample(gm, u0, u1, g.next());
+                    } else {
+                        dir = sr.pdf.generate(g);
+                    }
+                    float spdf = mis_pdf(dir);
                     if (!(spdf > 0.0f)) {
                         terminate = true;
                     } else {
-                        beta *= class_eval<C>(S, mat, d, s, dir) / spdf;
+                        float3 factor = class_eval<C>(S, mat, d, s, dir) / spdf;
+                        beta *= factor;
                         scatter_pdf = spdf;
                         new_o = s.p;
                         new_d = dir;
                         specular = false;
+                        if constexpr (GUIDED && kGuidable<C>()) {
+                            if (P.record && !vol && slot < P.rec_slots && depth < P.rec.depth) {
+                                float sc[7];
+                                guide_scalars(s.p, s.normal, normalize(-1.0f * d), P.guide_lo, P.guide_inv, sc);
+                                float3 wd = normalize(dir);
+                                uint32_t r = slot * uint32_t(P.rec.depth) + uint32_t(depth);
+                                P.rec.in0[r] = make_float4(sc[0], sc[1], sc[2], sc[3]);
+                                P.rec.in1[r] = make_float4(sc[4], sc[5], sc[6], 0.0f);
+                                P.rec.dir[r] = make_float4(wd.x, wd.y, wd.z, 0.0f);
+                                P.rec.fac[r] = make_float4(factor.x, factor.y, factor.z, 0.0f);
+                                rec_at = int(r);
+                            }
+                        }
                     }
                 }
             }
@@ -430,9 +489,13 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
                 P.B.sh_d[slot].w = 1.0f;  // the shadow kernel finishes this path
             } else {
                 film_add(P, pixel, rad);
+                if (GUIDED && P.record && slot < P.rec_slots)
+                    P.rec.fin[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
             }
             continue;
         }
+        if (GUIDED && rec_at >= 0)  // the path goes on: the next vertex completes the record
+            P.rec.list[warp_push(P.rec.count)] = uint32_t(rec_at);
         uint32_t nflags = (specular ? kFlagSpecular : 0u) | (seen ? kFlagSeen : 0u) | (diffuse_count << 8) |
                           (specular_count << 16) | (scatter_count << 24);
         P.B.ray_o[slot] = make_float4(new_o.x, new_o.y, new_o.z, bits_f(nflags));
@@ -494,9 +557,11 @@ __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
         }
         float4 r4 = P.B.radiance[slot];
         float3 rad = f3(r4) + f3(sc) * through * emission;
-        if (sd.w != 0.0f)
+        if (sd.w != 0.0f) {
             film_add(P, f_bits(r4.w), rad);
-        else
+            if (P.record && slot < P.rec_slots)
+                P.rec.fin[slot] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        } else
             P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, r4.w);
     }
 }
@@ -560,6 +625,41 @@ int release_buffers(RenderBuffers& rb) {
     rb = RenderBuffers();
     return MYPBR_OK;
 }
+
+// The guiding network's rows: the vertices of shading class `cls` at a bounce.
+struct GuideQueueSource {
+    WaveParams P;
+    int depth, cls;
+    MYPBR_DEV long long count(long long) const { return *class_counter(P, depth, cls); }
+    MYPBR_DEV void fill(long long i, __nv_bfloat16* A, int row) const {
+        if (i < 0) {
+            guide_encode_row(nullptr, A, row);
+            return;
+        }
+        uint32_t slot = class_queue(P, cls)[i];
+        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot], hb = P.B.hit[slot];
+        HitInfo h;
+        h.t = hb.x;
+        h.b1 = hb.y;
+        h.b2 = hb.z;
+        h.prim = __float_as_uint(hb.w);
+        Surface s = make_surface(P.S, h, f3(ro), f3(rd));
+        float sc[7];
+        guide_scalars(s.p, s.normal, normalize(-1.0f * f3(rd)), P.guide_lo, P.guide_inv, sc);
+        guide_encode_row(sc, A, row);
+    }
+};
+
+struct GuidePackSink {
+    WaveParams P;
+    int cls;
+    MYPBR_DEV void put(long long i, const float* v) const {
+        uint32_t slot = class_queue(P, cls)[i];
+        GuidePacked pk;
+        guide_pack(v, pk);
+        P.guide_mix[slot] = pk;
+    }
+};
 
 size_t counter_words(int depth_slots) { return size_t(depth_slots) * (2 + kShadeClasses) + 8; }
 
@@ -656,6 +756,10 @@ int bad_arg(const std::string& m) {
 
 struct Launch {
     int grid_extend, grid_shade, grid_shadow, grid_stream;
+    bool guided_kernels = false;  // the shading variants of guided renders
+    int grid_guide = 0;
+    size_t guide_smem = 0;
+    GuideNetView net{};
 };
 
 Launch launch_config(const mypbr_gpu_scene& G) {
@@ -667,9 +771,9 @@ Launch launch_config(const mypbr_gpu_scene& G) {
     L.grid_shadow = G.sm_count * std::max(per_sm, 1);
     L.grid_stream = G.sm_count * 8;
     int worst = 1;
-    for (auto f : {(const void*)k_shade<kClassMiss>, (const void*)k_shade<kClassLambert>,
-                   (const void*)k_shade<kClassMetal>, (const void*)k_shade<kClassDielectric>,
-                   (const void*)k_shade<kClassPrincipled>, (const void*)k_shade<kClassGeneric>}) {
+    for (auto f : {(const void*)k_shade<kClassMiss, false>, (const void*)k_shade<kClassLambert, false>,
+                   (const void*)k_shade<kClassMetal, false>, (const void*)k_shade<kClassDielectric, false>,
+                   (const void*)k_shade<kClassPrincipled, false>, (const void*)k_shade<kClassGeneric, false>}) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, 256, 0);
         worst = std::max(worst, per_sm);
     }
@@ -757,12 +861,28 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
     }
     for (int depth = 0; depth < P.max_depth; depth++) {
         TIMED(1, (k_extend<<<L.grid_extend, 256, 0, st>>>(P, depth)));
-        TIMED(2, (k_shade<kClassMiss><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-        TIMED(2, (k_shade<kClassLambert><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-        TIMED(2, (k_shade<kClassMetal><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-        TIMED(2, (k_shade<kClassDielectric><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-        TIMED(2, (k_shade<kClassPrincipled><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-        TIMED(2, (k_shade<kClassGeneric><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        if (P.guided) {  // the mixtures of this bounce's guidable vertices
+            for (int cls : {kClassLambert, kClassMetal, kClassPrincipled, kClassGeneric}) {
+                TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128, L.guide_smem, st>>>(
+                             L.net, GuideQueueSource{P, depth, cls}, GuidePackSink{P, cls}, 0)));
+                launches++;
+            }
+        }
+        if (L.guided_kernels) {
+            TIMED(2, (k_shade<kClassMiss, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassLambert, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMetal, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassDielectric, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassPrincipled, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassGeneric, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        } else {
+            TIMED(2, (k_shade<kClassMiss, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassLambert, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMetal, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassDielectric, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassPrincipled, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassGeneric, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+        }
         TIMED(3, (k_shadow<<<L.grid_shadow, 256, 0, st>>>(P, depth)));
         launches += 2 + kShadeClasses;
     }
@@ -778,17 +898,25 @@ struct RenderSetup {
     int spp, per_wave;
     size_t npix;  // pixels of the band
     bool timing;
+    bool guided = false, fixed_waves = false;
+    int per_wave_train = 0;  // passes per training wave of a guided render
 };
+
+// Guided renders: the first waves are small and recorded, each followed by
+// Adam steps on their vertices; later waves keep training online, lightly.
+constexpr int kGuideTrainWaves = 8;
+constexpr int kGuideStepsEarly = 24, kGuideStepsLate = 4;
+constexpr int kGuideMinSteps = 24;    // steps before the mixture is sampled at all
+constexpr int kGuideMaxSteps = 1500;  // no recording or training past this
+constexpr float kGuideAlpha = 0.5f, kGuideLr = 4e-3f;
 
 int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* o, int save_every, RenderSetup& R) {
     if (!G || !cam || !o)
         return bad_arg("mypbr_gpu_render: null argument");
     if (cam->image_width < 1 || o->samples_per_pixel < 1 || o->max_depth < 1 || o->max_depth > 4096)
         return bad_arg("mypbr_gpu_render: image_width, samples_per_pixel and max_depth must be positive");
-    if (o->guided != 0) {
-        set_error_message("mypbr_gpu_render: the guided sampler is not available in this build");
-        return MYPBR_ERR_UNSUPPORTED;
-    }
+    if (o->guided < 0)
+        return bad_arg("mypbr_gpu_render: guided must be 0 (off), 1 (default network) or 2, 4, 8 hidden layers");
     if (o->max_diffuse > 255 || o->max_specular > 255 || o->max_diffuse < 0 || o->max_specular < 0 ||
         o->max_scatter < 0)
         return bad_arg("mypbr_gpu_render: bounce caps must be in [0, 255]");
@@ -829,6 +957,37 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
         return s;
     P.B = G->rb;
     R.L = launch_config(*G);
+    R.guided = o->guided != 0;
+    R.fixed_waves = o->samples_per_wave > 0;
+    if (R.guided) {
+        int hidden = (o->guided == 2 || o->guided == 4 || o->guided == 8) ? o->guided : 8;
+        s = guide_ensure(G, hidden, o->seed ^ 0x9d2c5680ull);
+        if (s != MYPBR_OK)
+            return s;
+        size_t slots = R.npix * size_t(per_wave);
+        // training waves: about 2M paths each, every one recorded
+        R.per_wave_train = std::max(1, std::min(per_wave, int((size_t(2) << 20) / std::max<size_t>(R.npix, 1))));
+        if (R.fixed_waves)
+            R.per_wave_train = per_wave;
+        size_t rec_slots = std::min(slots, std::max(R.npix * size_t(R.per_wave_train), size_t(1)));
+        s = guide_ensure_records(G, slots, rec_slots, kGuideRecordDepth);
+        if (s != MYPBR_OK)
+            return s;
+        GuideState& g = G->guide;
+        P.rec = g.rec;
+        P.rec_slots = uint32_t(g.rec_slots);
+        P.guide_mix = reinterpret_cast<GuidePacked*>(g.packed);
+        P.guide_lo = g.box_lo;
+        P.guide_inv = g.box_inv;
+        R.L.net = GuideNetView{g.hidden, g.w, g.wt, g.grad, G->dev.error};
+        R.L.guide_smem = guide_forward_smem(g.hidden);
+        auto k = k_guide_forward<GuideQueueSource, GuidePackSink>;
+        MYPBR_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(R.L.guide_smem)));
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, R.L.guide_smem);
+        R.L.grid_guide = G->sm_count * std::max(per_sm, 1);
+        R.L.guided_kernels = true;
+    }
     return MYPBR_OK;
 }
 
@@ -857,12 +1016,32 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
     KernelTimer T;
     T.on = R.timing;
     T.st = st;
-    for (int pass0 = 0; pass0 < R.spp; pass0 += R.per_wave) {
+    int wave = 0;
+    for (int pass0 = 0; pass0 < R.spp; pass0 += P.npass, wave++) {
+        bool train_wave = R.guided && wave < kGuideTrainWaves;
         P.pass0 = pass0;
-        P.npass = std::min(R.per_wave, R.spp - pass0);
+        P.npass = std::min(train_wave ? R.per_wave_train : R.per_wave, R.spp - pass0);
+        if (save_every > 0)  // waves end on every multiple of save_every
+            P.npass = std::min(P.npass, save_every - pass0 % save_every);
+        if (R.guided) {
+            const GuideState& g = G->guide;
+            P.guided = g.steps >= kGuideMinSteps;
+            P.guide_alpha = P.guided ? kGuideAlpha : 0.0f;
+            P.record = g.steps < kGuideMaxSteps;
+            if (P.record)
+                MYPBR_CUDA(cudaMemsetAsync(P.rec.count, 0, sizeof(uint32_t), st));
+        }
         int s = run_wave(P, R.L, st, launches, T);
         if (s != MYPBR_OK)
             return s;
+        if (R.guided && P.record) {
+            if ((s = T.begin(4)) != MYPBR_OK)
+                return s;
+            s = guide_train(G, train_wave ? kGuideStepsEarly : kGuideStepsLate, 4 * G->sm_count, kGuideLr, st);
+            if (s != MYPBR_OK || (s = T.end()) != MYPBR_OK)
+                return s;
+            launches += 3 * (train_wave ? kGuideStepsEarly : kGuideStepsLate);
+        }
         int done = pass0 + P.npass;
         if (cb && save_every > 0 && done % save_every == 0 && done < R.spp) {
             k_resolve<<<R.L.grid_stream, 256, 0, st>>>(P, done, d_rad, d_alb, d_nrm, d_var);

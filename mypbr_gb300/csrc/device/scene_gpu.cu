@@ -301,6 +301,9 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     int interior = 0;
     D.has_bvh = F.bvh_prim_count > 0;
     if (D.has_bvh) {
+        const auto& root = F.bvh_nodes[0];
+        G.box_lo = make_float3(float(root.bmin[0]), float(root.bmin[1]), float(root.bmin[2]));
+        G.box_hi = make_float3(float(root.bmax[0]), float(root.bmax[1]), float(root.bmax[2]));
         G.max_depth_bvh = bvh_depth(F);
         if (G.max_depth_bvh >= kBvhStack) {
             set_error_message("mypbr_gpu_scene_create: BVH depth " + std::to_string(G.max_depth_bvh) +
@@ -694,6 +697,7 @@ extern "C" void mypbr_gpu_scene_destroy(mypbr_gpu_scene* scene) {
     if (!scene)
         return;
     mypbr_dev::release_buffers(scene->rb);
+    mypbr_dev::release_guide(scene->guide);
     for (void* p : scene->allocations)
         cudaFree(p);
     delete scene;

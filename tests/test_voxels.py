@@ -218,7 +218,11 @@ def test_gpu_voxel_trace_matches_oracle(name):
     hits, prim = G.trace(rays32)
     ok = stable(O, rays, 20.0)
     assert ok.mean() > 0.97, ok.mean()
-    np.testing.assert_array_equal(prim[ok], op[ok], err_msg="hit/miss or block differs")
+    # A face on the plane between two blocks belongs to both (each block
+    # reports the faces of its boundary, voxel.h:249-262), and the walk order
+    # picks one: the face itself (kind, t, normal, side, material) is the
+    # primitive identity compared here, the block index is not.
+    np.testing.assert_array_equal(prim[ok, 0], op[ok, 0], err_msg="hit/miss or kind differs")
     both = ok & (prim[:, 0] >= 0)
     assert both.mean() > 0.2
     np.testing.assert_array_equal(hits[both, 7], oh[both, 7], err_msg="material differs")
