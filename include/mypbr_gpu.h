@@ -529,6 +529,40 @@ void mypbr_denoise_opts_init(mypbr_denoise_opts* opts);
 int mypbr_gpu_denoise(const double* radiance, const double* albedo, const double* normal, const double* variance,
                       int32_t width, int32_t height, const mypbr_denoise_opts* opts, double* out, int on_device);
 
+/* ------------------------------------------------ display and images */
+
+/* Tonemappers of display_settings (include/tonemap.h:10). */
+enum { MYPBR_TONEMAP_NONE = 0, MYPBR_TONEMAP_REINHARD = 1, MYPBR_TONEMAP_ACES = 2 };
+
+/* display_settings + post_settings (include/tonemap.h:12-18,
+ * include/postprocess.h:13-21). */
+typedef struct mypbr_display_opts {
+    double exposure;        /* stops: radiance x 2^exposure */
+    int32_t tonemap;        /* MYPBR_TONEMAP_* */
+    int32_t reserved;
+    double bloom;           /* strength, 0 = off */
+    double bloom_threshold; /* luminance above which pixels glow */
+    double bloom_radius;    /* reach of the glow, fraction of the image width */
+    double vignette;        /* corner darkening, 0 = off */
+} mypbr_display_opts;
+
+void mypbr_display_opts_init(mypbr_display_opts* opts);
+
+/* postprocess (include/postprocess.h:104-151) of a radiance image (W*H*3
+ * doubles, rows from the top left) on the GPU: into `linear` (W*H*3 doubles,
+ * may be NULL) the bloomed and vignetted radiance; into `rgb8` (W*H*3 bytes,
+ * may be NULL) the display image after exposure, tonemapping and the sRGB
+ * curve (display_settings::apply + to_byte, tonemap.h:28-37, color3.h:33-36).
+ * Pointers are device memory if on_device, else host memory. */
+int mypbr_gpu_display(const double* radiance, int32_t width, int32_t height, const mypbr_display_opts* opts,
+                      double* linear, uint8_t* rgb8, int on_device);
+
+/* write_image (include/image_io.h:84-106): the format follows the extension;
+ * .png and .ppm are display images (post-processed on the GPU), .hdr and .pfm
+ * the raw radiance; an empty path writes PPM to stdout. */
+int mypbr_write_image(const char* path, const double* radiance, int32_t width, int32_t height,
+                      const mypbr_display_opts* opts, int on_device);
+
 /* ----------------------------------------------------- path guiding
  *
  * No counterpart in the reference: a learned sampling proposal, used by

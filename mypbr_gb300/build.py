@@ -24,6 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]
 CU_FLAGS = ARCH + COMMON + ["-lineinfo", "--use_fast_math", "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
 CPP_FLAGS = ARCH + COMMON + ["-Xcompiler", "-Wall"]
+# Sources whose FP64 arithmetic must round like the reference's (no fused multiply-add)
+NO_FMA = {"post.cu"}
 
 
 def nvcc():
@@ -71,6 +73,8 @@ def build(verbose=False, extra_flags=()):
     for src in cu + cpp:
         obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
         flags = CU_FLAGS if src.endswith(".cu") else CPP_FLAGS
+        if os.path.basename(src) in NO_FMA:
+            flags = flags + ["-fmad=false"]
         if headers_changed or not os.path.exists(obj) or os.path.getmtime(obj) < os.path.getmtime(src):
             jobs.append((src, obj, flags, list(extra_flags)))
     if jobs:

@@ -15,9 +15,12 @@
 //   ggx    <out>                      ggx_albedo_table E(mu, alpha) / E_avg and ggx_ms_* on a grid
 //   render <scene> <width> <spp> <batches> <threads> <out>
 //                                      batch means of camera::render (mean and variance of the mean)
+//   denoise <w> <h> <seed> <out>      denoiser::run on a seeded frame
+//   post   <w> <h> <seed> <out>       postprocess + display_settings::apply + to_byte on a seeded image
 #include <bvh.h>
 #include <denoiser.h>
 #include <scene.h>
+#include <tonemap.h>
 
 #include <chrono>
 #include <cstdio>
@@ -368,6 +371,57 @@ int cmd_denoise(int argc, char** argv) {
     return 0;
 }
 
+// A seeded HDR image: a gradient, noise and a few very bright spots. Then for
+// each of four display settings: the post-processed radiance and the bytes
+// of display_settings::apply + to_byte.
+int cmd_post(int argc, char** argv) {
+    if (argc < 6)
+        return 2;
+    int w = std::atoi(argv[2]), h = std::atoi(argv[3]);
+    Rng g(std::strtoull(argv[4], nullptr, 10));
+    size_t n = size_t(w) * h;
+    std::vector<color> px(n);
+    for (int j = 0; j < h; j++)
+        for (int i = 0; i < w; i++) {
+            double base = 0.05 + 0.9 * double(i) / w * (0.3 + 0.7 * double(j) / h);
+            px[size_t(j) * w + i] = color(base * (0.8 + 0.4 * g.next()), base * (0.6 + 0.4 * g.next()),
+                                          base * (0.3 + 0.6 * g.next()));
+            if (g.next() < 0.004)
+                px[size_t(j) * w + i] = color(40 * g.next(), 30 * g.next(), 20 * g.next());
+        }
+    Out o(argv[5]);
+    o.put(double(w));
+    o.put(double(h));
+    for (const auto& c : px)
+        o.put(c);
+    struct Setting {
+        double exposure, bloom, threshold, radius, vignette;
+        tonemapper op;
+    } settings[4] = {{0, 0, 1, 0.04, 0, tonemapper::none},
+                     {0.5, 0.3, 1, 0.08, 0.4, tonemapper::reinhard},
+                     {-0.7, 0.8, 0.5, 0.2, 0, tonemapper::aces},
+                     {1.3, 0.15, 2, 0.01, 1.5, tonemapper::none}};
+    for (const auto& st : settings) {
+        display_settings d;
+        d.exposure = st.exposure;
+        d.op = st.op;
+        d.post.bloom = st.bloom;
+        d.post.bloom_threshold = st.threshold;
+        d.post.bloom_radius = st.radius;
+        d.post.vignette = st.vignette;
+        std::vector<color> post = d.post.active() ? postprocess(px, w, h, d.post) : px;
+        for (const auto& c : post)
+            o.put(c);
+        for (const auto& c : post) {
+            color a = d.apply(c);
+            o.put(double(to_byte(a.x())));
+            o.put(double(to_byte(a.y())));
+            o.put(double(to_byte(a.z())));
+        }
+    }
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -384,6 +438,7 @@ int main(int argc, char** argv) {
     else if (c == "ggx") rc = cmd_ggx(argc, argv);
     else if (c == "render") rc = cmd_render(argc, argv);
     else if (c == "denoise") rc = cmd_denoise(argc, argv);
+    else if (c == "post") rc = cmd_post(argc, argv);
     if (rc == 2)
         std::cerr << "bad arguments for '" << c << "'\n";
     return rc;

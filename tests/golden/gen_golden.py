@@ -255,8 +255,23 @@ def gen_denoise():
                         normal=recs[..., 6:9], variance=recs[..., 9], out=recs[..., 10:13])
 
 
+# display settings of ref_harness post: (exposure, tonemap, bloom, threshold, radius, vignette)
+POST_SETTINGS = [(0.0, 0, 0.0, 1.0, 0.04, 0.0), (0.5, 1, 0.3, 1.0, 0.08, 0.4), (-0.7, 2, 0.8, 0.5, 0.2, 0.0),
+                 (1.3, 0, 0.15, 2.0, 0.01, 1.5)]
+
+
+def gen_post():
+    raw = run("post", 97, 61, 8)
+    w, h = int(raw[0]), int(raw[1])
+    n = w * h
+    img = raw[2:2 + 3 * n].reshape(h, w, 3)
+    rest = raw[2 + 3 * n:].reshape(len(POST_SETTINGS), 2, h, w, 3)
+    np.savez_compressed(os.path.join(HERE, "post.npz"), image=img, linear=rest[:, 0],
+                        rgb8=rest[:, 1].astype(np.uint8), settings=np.array(POST_SETTINGS))
+
+
 GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_env, "ggx": gen_ggx,
-          "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels}
+          "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post}
 
 if __name__ == "__main__":
     ref = os.environ.get("REFERENCE", "/root/reference")
