@@ -1,4 +1,6 @@
-"""Benchmark: Mpaths/s of the wavefront path tracer on the 1000-sphere field.
+"""Benchmark: Mpaths/s of the wavefront path tracer on the 1000-sphere field
+(default), or time to relMSE 0.01 of guided against plain rendering on the
+occluded voxel hall (--workload voxel_hall).
 
 Workload (the headline configuration): a seeded field of 1000 spheres on a
 ground sphere (r = 1000 at y = -1000), centres uniform in [-11, 11] x [0.2, 1.2]
@@ -16,6 +18,16 @@ with host buffers: mypbr_gpu_scene_create (uploads the flat scene) +
 mypbr_gpu_render (renders, copies the FP64 frame back) + destroy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--spp S]
+  python bench.py --workload voxel_hall [--hall-width 480] [--ref-spp 65536]
+
+voxel_hall: the 512^3 voxel world lit through six slits (workloads.py),
+rendered at --hall-width x 9/16 with max depth 16. relMSE = mean over pixels
+and channels of (x - r)^2 / (r^2 + 0.01) against a plain render at --ref-spp
+samples (FP64 film). Each method renders at doubling spp (a fresh, untrained
+network for every guided render, so training time is inside each timing)
+until relMSE <= 0.01; the time there is interpolated log-log between the two
+bracketing renders, or extrapolated as relMSE ~ 1/spp past the last one. The
+CPU figure extrapolates the oracle's relMSE the same way from a bounded run.
 
 --impl reference times the CPU implementation of the same path (the FP64
 restatement of the reference's camera::render in oracle/, on every host core)
@@ -46,68 +58,7 @@ UNIT = "Mpaths/s"
 
 # ------------------------------------------------------------ the workload
 
-def write_hdr(path, rgb):
-    """Writes float RGB (H, W, 3) as a flat Radiance RGBE file."""
-    h, w, _ = rgb.shape
-    v = rgb.max(axis=2)
-    m, e = np.frexp(v)
-    scale = np.where(v > 1e-32, m * 256.0 / np.maximum(v, 1e-38), 0.0)
-    out = np.zeros((h, w, 4), dtype=np.uint8)
-    for c in range(3):
-        out[..., c] = np.clip(np.floor(rgb[..., c] * scale), 0, 255).astype(np.uint8)
-    out[..., 3] = np.where(v > 1e-32, e + 128, 0).astype(np.uint8)
-    with open(path, "wb") as f:
-        f.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
-        f.write(f"-Y {h} +X {w}\n".encode())
-        f.write(out.tobytes())
-
-
-def sky_image(w=1024, h=512):
-    """Sky gradient plus a Gaussian sun lobe (angular radius 0.5 deg, peak 5e4),
-    in the equirectangular layout of environment.h:334-348 (row 0 at +y)."""
-    j, i = np.meshgrid(np.arange(h) + 0.5, np.arange(w) + 0.5, indexing="ij")
-    theta = math.pi * j / h
-    phi = 2 * math.pi * (i / w - 0.5)
-    d = np.stack([np.sin(theta) * np.sin(phi), np.cos(theta), -np.sin(theta) * np.cos(phi)], axis=2)
-    up = np.clip(d[..., 1], 0, 1)
-    horizon = np.array([0.75, 0.85, 1.0])
-    zenith = np.array([0.15, 0.35, 0.85])
-    sky = horizon * (1 - up[..., None]) + zenith * up[..., None]
-    below = d[..., 1] < 0
-    sky[below] = np.array([0.12, 0.11, 0.10])
-    el, az = math.radians(35), math.radians(60)
-    sun = np.array([math.cos(el) * math.sin(az), math.sin(el), -math.cos(el) * math.cos(az)])
-    ang = np.arccos(np.clip((d * sun).sum(axis=2), -1, 1))
-    sigma = math.radians(0.5)
-    lobe = 5e4 * np.exp(-0.5 * (ang / sigma) ** 2)
-    return sky + lobe[..., None] * np.array([1.0, 0.95, 0.85])
-
-
-def sphere_field_scene(directory, seed=2, spp=256, width=WIDTH, height=HEIGHT, depth=16):
-    rng = np.random.default_rng(seed)
-    write_hdr(os.path.join(directory, "sky.hdr"), sky_image())
-    lines = [f"image_width {width}", f"aspect_ratio {width}/{height}", f"samples_per_pixel {spp}",
-             f"max_depth {depth}", "camera lookfrom 0 6 18  lookat 0 0 0  vup 0 1 0  vfov 35",
-             "environment sky.hdr", "material ground lambertian 0.5 0.5 0.5", "sphere 0 -1000 0 1000 ground"]
-    n = 1000
-    centers = np.stack([rng.uniform(-11, 11, n), rng.uniform(0.2, 1.2, n), rng.uniform(-11, 11, n)], axis=1)
-    radii = rng.lognormal(-1.6, 0.3, n)
-    kind = rng.uniform(size=n)
-    for k in range(n):
-        if kind[k] < 0.60:
-            a = rng.uniform(0, 1, 3)
-            lines.append(f"material m{k} lambertian {a[0]:.6f} {a[1]:.6f} {a[2]:.6f}")
-        elif kind[k] < 0.85:
-            a = rng.uniform(0.5, 1, 3)
-            lines.append(f"material m{k} metal {a[0]:.6f} {a[1]:.6f} {a[2]:.6f} {rng.uniform(0.02, 0.6):.6f}")
-        else:
-            lines.append(f"material m{k} dielectric 1.5")
-        c = centers[k]
-        lines.append(f"sphere {c[0]:.6f} {c[1]:.6f} {c[2]:.6f} {radii[k]:.6f} m{k}")
-    path = os.path.join(directory, "sphere_field.scene")
-    with open(path, "w") as f:
-        f.write("\n".join(lines) + "\n")
-    return path
+from mypbr_gb300.workloads import sphere_field_scene, voxel_hall_scene  # noqa: E402
 
 
 WORKLOAD = {"workload": "sphere_field_1000_hdri", "width": WIDTH, "height": HEIGHT, "spp": 256, "max_depth": 16,
@@ -373,6 +324,94 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def rel_mse(x, ref, eps=0.01):
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + eps)))
+
+
+def time_to_target(points, target):
+    """points: [(spp, seconds, relMSE)] at increasing spp. Seconds to reach target."""
+    prev = None
+    for spp, t, e in points:
+        if e <= target:
+            if prev is None or prev[2] <= e:
+                return t, "measured"
+            # log-log interpolation between the bracketing renders
+            f = (math.log(prev[2]) - math.log(target)) / (math.log(prev[2]) - math.log(e))
+            return math.exp(math.log(prev[1]) + f * (math.log(t) - math.log(prev[1]))), "interpolated"
+        prev = (spp, t, e)
+    spp, t, e = points[-1]
+    return t * e / target, "extrapolated (relMSE ~ 1/spp)"
+
+
+def run_voxel_hall(args):
+    import mypbr_gb300 as mp
+    width = args.hall_width
+    height = width * 9 // 16
+    target = 0.01
+    with tempfile.TemporaryDirectory() as d:
+        scene = mp.load_scene(voxel_hall_scene(d, size=512, width=width, height=height, spp=64))
+    cam = scene.camera
+    G = mp.GpuScene(scene)
+
+    def render(gs, spp, guided, seed):
+        cam.samples_per_pixel = spp
+        cam.guided = guided
+        cam.seed = seed
+        cam.samples_per_wave = 0
+        t0 = time.perf_counter()
+        img, _, _ = mp.render_ex(cam, gs)
+        return img, time.perf_counter() - t0
+
+    render(G, 16, 0, 7)  # warm-up
+    ref, t_ref = render(G, args.ref_spp, 0, 12345)
+    curves = {}
+    for name, guided in (("plain", 0), ("guided", args.hidden)):
+        pts = []
+        spp = 16
+        while spp <= args.max_spp:
+            gs = mp.GpuScene(scene) if guided else G  # guided: an untrained network every time
+            img, t = render(gs, spp, guided, 1 + spp)
+            if guided:
+                gs.close()
+            e = rel_mse(img, ref)
+            pts.append((spp, t, e))
+            print(f"{name} spp {spp}: {t:.3f} s relMSE {e:.5f}", file=sys.stderr, flush=True)
+            if e <= target / 2:
+                break
+            spp *= 2
+        tt, how = time_to_target(pts, target)
+        curves[name] = {"time_to_target_s": tt, "how": how,
+                        "points": [{"spp": s_, "seconds": t_, "relMSE": e_} for s_, t_, e_ in pts]}
+    # CPU: the oracle on all host cores, a bounded run, extrapolated as relMSE ~ 1/spp
+    import oracle as orc
+    threads = os.cpu_count() or 1
+    O = orc.OracleScene(scene)
+    spp = 4
+    while True:
+        cam.samples_per_pixel = spp
+        t0 = time.perf_counter()
+        cpu_img, _, _ = O.render(cam, threads=threads)
+        cpu_t = time.perf_counter() - t0
+        cpu_spp = spp
+        if cpu_t > args.cpu_budget / 3 or spp >= 256:
+            break
+        spp *= 2
+    cpu_e = rel_mse(cpu_img, ref)
+    cpu_tt = cpu_t * cpu_e / target
+    line = {"metric": "time to relMSE 0.01 on the occluded voxel hall, guided GPU", "value": curves["guided"]["time_to_target_s"],
+            "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": "voxel_hall_512", "width": width, "height": height, "max_depth": 16,
+                       "reference_spp": args.ref_spp, "reference_seconds": t_ref, "relmse_eps": 0.01,
+                       "guide_hidden_layers": args.hidden, "sky": "uniform 0.35 0.45 0.6",
+                       "sun": "elevation 40 azimuth 160 intensity 1000 angle 0.54"},
+            "plain": curves["plain"], "guided": curves["guided"],
+            "guided_speedup_vs_plain": curves["plain"]["time_to_target_s"] / curves["guided"]["time_to_target_s"],
+            "cpu_baseline": {"time_to_target_s": cpu_tt, "cores": threads, "kind": "port",
+                             "sample": f"{cpu_spp} spp in {cpu_t:.1f} s, relMSE {cpu_e:.4f}, extrapolated ~1/spp"},
+            "guided_speedup_vs_cpu": cpu_tt / curves["guided"]["time_to_target_s"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -384,7 +423,16 @@ def main():
     p.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
     p.add_argument("--reference-budget", type=float, default=8.0, help="seconds per reference step")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", choices=["sphere_field", "voxel_hall"], default="sphere_field")
+    p.add_argument("--hall-width", type=int, default=480)
+    p.add_argument("--ref-spp", type=int, default=65536)
+    p.add_argument("--max-spp", type=int, default=16384)
+    p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
     args = p.parse_args()
+    if args.workload == "voxel_hall":
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        run_voxel_hall(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":

@@ -529,6 +529,65 @@ void mypbr_denoise_opts_init(mypbr_denoise_opts* opts);
 int mypbr_gpu_denoise(const double* radiance, const double* albedo, const double* normal, const double* variance,
                       int32_t width, int32_t height, const mypbr_denoise_opts* opts, double* out, int on_device);
 
+/* ------------------------------------------------------------ sky bake */
+
+/* atmosphere_settings (include/atmosphere.h:39-46): densities relative to
+ * Earth's, the haze's forward scattering, the overall radiance scale. */
+typedef struct mypbr_sky_settings {
+    double rayleigh, mie, mie_g, ozone, intensity;
+} mypbr_sky_settings;
+
+void mypbr_sky_settings_init(mypbr_sky_settings* settings);
+
+/* atmosphere::bake and sun_transmittance (atmosphere.h:53-108): the
+ * single-scattering sky for a sun in sun_direction of irradiance
+ * sun_irradiance, as a width x height equirectangular image (rgb, 3 doubles
+ * per pixel, host memory), and (if not NULL) the sun's transmittance through
+ * the air (3 doubles). on_gpu: bake on the device, else on the host. The
+ * scene loader bakes `sky atmosphere` skies the same way (256 x 128). */
+int mypbr_sky_bake(const mypbr_sky_settings* settings, const double sun_direction[3], const double sun_irradiance[3],
+                   int32_t width, int32_t height, double* rgb, double* sun_transmittance, int on_gpu);
+
+/* ------------------------------------------------------------ batches */
+
+/* One render of a batch: device output buffers as for mypbr_gpu_render_device
+ * (albedo / normal / variance may be NULL unless opts->collect_features). */
+typedef struct mypbr_batch_job {
+    mypbr_gpu_scene* scene;
+    const mypbr_camera* camera;
+    const mypbr_render_opts* opts;
+    double* radiance;
+    double* albedo;
+    double* normal;
+    double* variance;
+    int32_t status;   /* out: this job's status */
+    int32_t reserved;
+} mypbr_batch_job;
+
+/* Renders every job (many scenes or frames of different sizes and spp): jobs
+ * on different scene handles run concurrently on the handles' own streams,
+ * one wave of each in turn, waves replayed from captured CUDA graphs; jobs on
+ * one handle run in order. Returns when all are done: the first failing
+ * job's status, or MYPBR_OK. No counterpart in the reference (its renders
+ * are one at a time, camera.h:79-105). */
+int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n);
+
+/* The autotuner's choice for a scene handle and view: threads per block of
+ * the bounce kernels and paths per wave, with the Mpaths/s of each of the 8
+ * trials (block 128 then 256, each with 4M, 8M, 16M, 32M paths). */
+typedef struct mypbr_tune_result {
+    int32_t block;
+    int32_t reserved;
+    int64_t wave_paths;
+    double mpaths_per_s;
+    double trial_mpaths[8];
+} mypbr_tune_result;
+
+/* Times short renders of the view with each setting and keeps the fastest on
+ * the handle: later renders use it unless opts->samples_per_wave is set. */
+int mypbr_gpu_autotune(mypbr_gpu_scene* scene, const mypbr_camera* camera, const mypbr_render_opts* opts,
+                       mypbr_tune_result* out);
+
 /* ------------------------------------------------ display and images */
 
 /* Tonemappers of display_settings (include/tonemap.h:10). */

@@ -72,6 +72,31 @@ class RenderStatsStruct(ctypes.Structure):
 
 PASS_CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_void_p)
 
+TONEMAPPERS = {"none": 0, "reinhard": 1, "aces": 2}
+
+
+class BatchJobStruct(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("camera", ctypes.POINTER(CameraStruct)),
+                ("opts", ctypes.POINTER(RenderOptsStruct)), ("radiance", ctypes.c_void_p),
+                ("albedo", ctypes.c_void_p), ("normal", ctypes.c_void_p), ("variance", ctypes.c_void_p),
+                ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class SkySettingsStruct(ctypes.Structure):
+    _fields_ = [("rayleigh", ctypes.c_double), ("mie", ctypes.c_double), ("mie_g", ctypes.c_double),
+                ("ozone", ctypes.c_double), ("intensity", ctypes.c_double)]
+
+
+class TuneResultStruct(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("reserved", ctypes.c_int32), ("wave_paths", ctypes.c_int64),
+                ("mpaths_per_s", ctypes.c_double), ("trial_mpaths", ctypes.c_double * 8)]
+
+
+class DisplayOptsStruct(ctypes.Structure):
+    _fields_ = [("exposure", ctypes.c_double), ("tonemap", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("bloom", ctypes.c_double), ("bloom_threshold", ctypes.c_double), ("bloom_radius", ctypes.c_double),
+                ("vignette", ctypes.c_double)]
+
 _lib = None
 
 
@@ -114,6 +139,17 @@ def lib():
                                       vp, vp, ctypes.c_int, PASS_CALLBACK, vp, ctypes.POINTER(RenderStatsStruct)]
     L.mypbr_gpu_trace.argtypes = [vp, fp, i64, fp, ip, ctypes.c_int]
     L.mypbr_gpu_bsdf_eval.argtypes = [vp, i32, fp, fp, fp, i64, fp]
+    L.mypbr_gpu_render_batch.argtypes = [ctypes.POINTER(BatchJobStruct), i32]
+    L.mypbr_sky_settings_init.argtypes = [ctypes.POINTER(SkySettingsStruct)]
+    L.mypbr_sky_settings_init.restype = None
+    L.mypbr_sky_bake.argtypes = [ctypes.POINTER(SkySettingsStruct), dp, dp, i32, i32, dp, dp, ctypes.c_int]
+    L.mypbr_gpu_autotune.argtypes = [vp, ctypes.POINTER(CameraStruct), ctypes.POINTER(RenderOptsStruct),
+                                     ctypes.POINTER(TuneResultStruct)]
+    L.mypbr_display_opts_init.argtypes = [ctypes.POINTER(DisplayOptsStruct)]
+    L.mypbr_display_opts_init.restype = None
+    L.mypbr_gpu_display.argtypes = [dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), dp,
+                                    ctypes.POINTER(ctypes.c_uint8), ctypes.c_int]
+    L.mypbr_write_image.argtypes = [ctypes.c_char_p, dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), ctypes.c_int]
     L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
     L.mypbr_guide_test_backward.argtypes = [ctypes.c_int, fp, fp, fp, i64, fp]
     L.mypbr_guide_test_loss.argtypes = [fp, fp, fp, i64, fp, fp]
@@ -376,3 +412,82 @@ def guide_mixture(raw, u, dirs):
     check(lib().mypbr_guide_test_mixture(_fptr(raw), _fptr(u), _fptr(dirs), n, _fptr(samples), _fptr(ps),
                                          _fptr(pd)))
     return samples, ps, pd
+
+
+# ------------------------------------------------------------ display
+
+def display_opts(exposure=0.0, tonemap="none", bloom=0.0, bloom_threshold=1.0, bloom_radius=0.04, vignette=0.0):
+    """display_settings + post_settings (tonemap.h:12-18, postprocess.h:13-21)."""
+    o = DisplayOptsStruct()
+    lib().mypbr_display_opts_init(ctypes.byref(o))
+    o.exposure = exposure
+    o.tonemap = TONEMAPPERS[tonemap] if isinstance(tonemap, str) else int(tonemap)
+    o.bloom, o.bloom_threshold, o.bloom_radius, o.vignette = bloom, bloom_threshold, bloom_radius, vignette
+    return o
+
+
+def display(radiance, opts=None):
+    """(post-processed radiance (H, W, 3), display bytes (H, W, 3) uint8) on the GPU."""
+    rad = np.ascontiguousarray(radiance, dtype=np.float64)
+    h, w, _ = rad.shape
+    lin = np.zeros_like(rad)
+    rgb = np.zeros((h, w, 3), dtype=np.uint8)
+    o = opts if opts is not None else display_opts()
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(lib().mypbr_gpu_display(rad.ctypes.data_as(dp), w, h, ctypes.byref(o), lin.ctypes.data_as(dp),
+                                  rgb.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), 0))
+    return lin, rgb
+
+
+def write_image(path, radiance, opts=None):
+    """write_image (image_io.h:84-106): .png, .ppm, .hdr or .pfm by extension."""
+    rad = np.ascontiguousarray(radiance, dtype=np.float64)
+    h, w, _ = rad.shape
+    o = opts if opts is not None else display_opts()
+    check(lib().mypbr_write_image(str(path).encode(), rad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), w, h,
+                                  ctypes.byref(o), 0))
+
+
+# ------------------------------------------------------------ batches and tuning
+
+def render_batch(jobs):
+    """jobs: [(gpu_scene, camera, radiance_device_pointer)] with the radiance
+    buffers (H*W*3 float64) in device memory. Renders them all
+    (mypbr_gpu_render_batch); returns the per-job statuses."""
+    n = len(jobs)
+    arr = (BatchJobStruct * n)()
+    keep = []
+    for k, (gs, cam, ptr) in enumerate(jobs):
+        c, o = cam.structs()
+        keep.append((c, o))
+        arr[k].scene = gs.handle
+        arr[k].camera = ctypes.pointer(c)
+        arr[k].opts = ctypes.pointer(o)
+        arr[k].radiance = int(ptr)
+    status = lib().mypbr_gpu_render_batch(arr, n)
+    codes = [arr[k].status for k in range(n)]
+    check(status)
+    return codes
+
+
+def autotune(camera, gpu_scene):
+    """Runs the autotuner for this view; returns its choice and trial rates."""
+    c, o = camera.structs()
+    r = TuneResultStruct()
+    check(lib().mypbr_gpu_autotune(gpu_scene.handle, ctypes.byref(c), ctypes.byref(o), ctypes.byref(r)))
+    return {"block": r.block, "wave_paths": r.wave_paths, "mpaths_per_s": r.mpaths_per_s,
+            "trials": list(r.trial_mpaths)}
+
+
+def sky_bake(sun_direction, sun_irradiance, width=256, height=128, rayleigh=1.0, mie=1.0, mie_g=0.8, ozone=1.0,
+             intensity=3.0, on_gpu=False):
+    """atmosphere::bake + sun_transmittance: (image (H, W, 3), transmittance (3,))."""
+    s = SkySettingsStruct(rayleigh, mie, mie_g, ozone, intensity)
+    d = np.ascontiguousarray(sun_direction, dtype=np.float64)
+    e = np.ascontiguousarray(sun_irradiance, dtype=np.float64)
+    img = np.zeros((height, width, 3))
+    t = np.zeros(3)
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(lib().mypbr_sky_bake(ctypes.byref(s), d.ctypes.data_as(dp), e.ctypes.data_as(dp), width, height,
+                               img.ctypes.data_as(dp), t.ctypes.data_as(dp), int(on_gpu)))
+    return img, t

@@ -31,7 +31,8 @@ struct DevVoxelModel {
     int nx, ny, nz, xform;
     long long cells;  // offset into voxel_cells
     int palette, edge_material;
-    float edge_width, pad0, pad1, pad2;
+    float edge_width, pad0;
+    long long kinds;  // offset into voxel_kinds (the cells' kinds under this model's palette)
 };
 
 constexpr int kBvhStack = 64;
@@ -84,10 +85,12 @@ struct DeviceScene {
     const int4* voxel_blocks;      // 2 per block: (model, lo xyz), (hi xyz, -)
     const int2* voxel_palettes;    // (material, kind) per palette entry
     const uint8_t* voxel_cells;
+    const uint8_t* voxel_kinds;    // per cell: 0 empty, 1 opaque, 2 transparent
     int unbounded_count;
     int has_bvh;
     int bvh_node_count;  // interior nodes; a walk visits each at most once
     int has_media;       // media or height fog present (free-flight sampling needs keys)
+    int has_voxels;      // voxel blocks among the BVH's primitives
     int has_emitters;    // some hittable surface can emit (diffuse light or emissive texture)
     int has_clear_glass; // some hittable surface lets shadows through (smooth dielectric)
     const uint8_t* mat_class;  // shading class of each material
@@ -349,13 +352,13 @@ MYPBR_DEV bool hit_medium(const DeviceScene& S, int i, float3 o, float3 d, float
 
 // ----------------------------------------------------------------- voxels
 
-MYPBR_DEV int voxel_kind(const DeviceScene& S, int palette, int idx) { return __ldg(&S.voxel_palettes[palette + idx].y); }
-
-// The palette index of a cell of the whole model, 0 outside it (voxel.h:284-288).
-MYPBR_DEV int voxel_at(const DevVoxelModel& m, const uint8_t* cells, const int c[3]) {
-    if (unsigned(c[0]) >= unsigned(m.nx) || unsigned(c[1]) >= unsigned(m.ny) || unsigned(c[2]) >= unsigned(m.nz))
+// The kind of a cell of the whole model (kinds hold one byte per cell:
+// 0 empty, 1 opaque, 2 transparent, precomputed from the palette), 0 outside
+// it (voxel.h:284-288).
+MYPBR_DEV int voxel_kind_at(const DevVoxelModel& m, const uint8_t* kinds, int x, int y, int z) {
+    if (unsigned(x) >= unsigned(m.nx) || unsigned(y) >= unsigned(m.ny) || unsigned(z) >= unsigned(m.nz))
         return 0;
-    return __ldg(cells + (size_t(c[2]) * m.ny + c[1]) * m.nx + c[0]);
+    return __ldg(kinds + (size_t(z) * m.ny + y) * m.nx + x);
 }
 
 MYPBR_DEV bool voxel_face_visible(int k, int n) {  // voxel.h:100-106
@@ -367,9 +370,9 @@ MYPBR_DEV bool voxel_face_visible(int k, int n) {  // voxel.h:100-106
 }
 
 // on_edge (voxel.h:313-331): within width of an outline of the shapes.
-MYPBR_DEV bool voxel_on_edge(const DeviceScene& S, const DevVoxelModel& m, const uint8_t* cells, float3 p, int axis,
-                             int sign, const int cell[3]) {
-    int k = voxel_kind(S, m.palette, voxel_at(m, cells, cell));
+MYPBR_DEV bool voxel_on_edge(const DevVoxelModel& m, const uint8_t* kinds, float3 p, int axis, int sign,
+                             const int cell[3]) {
+    int k = voxel_kind_at(m, kinds, cell[0], cell[1], cell[2]);
     for (int side = 1; side <= 2; side++) {
         int tangent = (axis + side) % 3;
         float f = comp(p, tangent) - float(cell[tangent]);
@@ -380,19 +383,40 @@ MYPBR_DEV bool voxel_on_edge(const DeviceScene& S, const DevVoxelModel& m, const
             beside[tangent] += dir;
             int above[3] = {beside[0], beside[1], beside[2]};
             above[axis] += sign;
-            if (voxel_face_visible(k, voxel_kind(S, m.palette, voxel_at(m, cells, beside))) ||
-                voxel_kind(S, m.palette, voxel_at(m, cells, above)) != 0)
+            if (voxel_face_visible(k, voxel_kind_at(m, kinds, beside[0], beside[1], beside[2])) ||
+                voxel_kind_at(m, kinds, above[0], above[1], above[2]) != 0)
                 return true;
         }
     }
     return false;
 }
 
+// The hit on the face of cell (x, y, z) whose outward normal is along axis
+// with the given sign: material (the cell's palette entry, or the outline's).
+MYPBR_DEV int voxel_face_material(const DeviceScene& S, const DevVoxelModel& m, const uint8_t* kinds, float3 p,
+                                  int axis, int sign, int x, int y, int z) {
+    int cell[3] = {x, y, z};
+    if (m.edge_width > 0.0f && voxel_on_edge(m, kinds, p, axis, sign, cell))
+        return m.edge_material;
+    int idx = __ldg(S.voxel_cells + m.cells + (size_t(z) * m.ny + y) * m.nx + x);
+    return __ldg(&S.voxel_palettes[m.palette + idx].x);
+}
+
+// A crossing from a cell of kind kf into one of kind kt along +-axis: which
+// face is a surface, if any (crossing, voxel.h:294-305). 1: the entered
+// cell's face; 2: the face of the cell being left, seen from inside; 0: none.
+MYPBR_DEV int voxel_crossing(int kf, int kt) {
+    if (kt != 0 && voxel_face_visible(kt, kf))
+        return 1;
+    return voxel_face_visible(kf, kt) ? 2 : 0;
+}
+
 // Block i of a placed voxel model, walked cell by cell with a 3D DDA
 // (Amanatides and Woo 1987) in the model's space, as voxel_grid::hit
-// (voxel.h:193-268). A surface is a crossing between cells of different kind
-// (crossing, voxel.h:294-305). On a hit: t, the material (the cell's palette
-// entry, or the outline's) and face = axis | (outward normal positive) << 2.
+// (voxel.h:193-268). A surface is a crossing between cells of different kind.
+// On a hit: t, the material and face = axis | (outward normal positive) << 2.
+// The walk keeps its cell, step and next-plane distances in scalars (no
+// dynamically indexed arrays, which would live in local memory).
 MYPBR_DEV bool hit_voxel_block(const DeviceScene& S, int i, float3 ow, float3 dw, float tmin, float tmax, float& t_out,
                                int& mat_out, int& face_out) {
     int4 b0 = __ldg(S.voxel_blocks + 2 * i), b1 = __ldg(S.voxel_blocks + 2 * i + 1);
@@ -400,100 +424,116 @@ MYPBR_DEV bool hit_voxel_block(const DeviceScene& S, int i, float3 ow, float3 dw
     XformRef X;
     load_xform(S, m.xform, X);
     float3 o = xf_ipoint(X, ow), d = xf_ivec(X, dw);
-    int lo[3] = {b0.y, b0.z, b0.w}, hi[3] = {b1.x, b1.y, b1.z};
-    const uint8_t* cells = S.voxel_cells + m.cells;
+    const uint8_t* kinds = S.voxel_kinds + m.kinds;
+    const float lox = float(b0.y), loy = float(b0.z), loz = float(b0.w);
+    const float hix = float(b1.x), hiy = float(b1.y), hiz = float(b1.z);
+    // where the ray's line enters and leaves the block
     float t_enter = -3.0e38f, t_exit = 3.0e38f;
     int enter_axis = 0;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        float da = comp(d, a), oa = comp(o, a);
-        if (da == 0.0f) {
-            if (oa < lo[a] || oa > hi[a])
-                return false;
-            continue;
-        }
-        float t0 = (lo[a] - oa) / da, t1 = (hi[a] - oa) / da;
-        if (t0 > t1) {
-            float tmp = t0;
-            t0 = t1;
-            t1 = tmp;
-        }
-        if (t0 > t_enter) {
-            t_enter = t0;
-            enter_axis = a;
-        }
-        t_exit = fminf(t_exit, t1);
+#define MYPBR_SLAB(A, DA, OA, LO, HI)                  \
+    if (DA == 0.0f) {                                  \
+        if (OA < LO || OA > HI)                        \
+            return false;                              \
+    } else {                                           \
+        float t0 = (LO - OA) / DA, t1 = (HI - OA) / DA; \
+        if (t0 > t1) {                                 \
+            float tmp = t0;                            \
+            t0 = t1;                                   \
+            t1 = tmp;                                  \
+        }                                              \
+        if (t0 > t_enter) {                            \
+            t_enter = t0;                              \
+            enter_axis = A;                            \
+        }                                              \
+        t_exit = fminf(t_exit, t1);                    \
     }
+    MYPBR_SLAB(0, d.x, o.x, lox, hix)
+    MYPBR_SLAB(1, d.y, o.y, loy, hiy)
+    MYPBR_SLAB(2, d.z, o.z, loz, hiz)
+#undef MYPBR_SLAB
     bool from_outside = t_enter >= tmin;
     float t_start = from_outside ? t_enter : tmin;
     if (t_start > fminf(t_exit, tmax))
         return false;
     float3 start = o + t_start * d;
-    int c[3], step[3];
-    float t_next[3], t_delta[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        float da = comp(d, a), oa = comp(o, a);
-        c[a] = min(max(int(floorf(comp(start, a))), lo[a]), hi[a] - 1);
-        if (from_outside && a == enter_axis)
-            c[a] = da > 0.0f ? lo[a] : hi[a] - 1;
-        if (da > 0.0f) {
-            step[a] = 1;
-            t_next[a] = (c[a] + 1 - oa) / da;
-            t_delta[a] = 1.0f / da;
-        } else if (da < 0.0f) {
-            step[a] = -1;
-            t_next[a] = (c[a] - oa) / da;
-            t_delta[a] = -1.0f / da;
-        } else {
-            step[a] = 0;
-            t_next[a] = t_delta[a] = 3.0e38f;
-        }
+    int cx = min(max(int(floorf(start.x)), b0.y), b1.x - 1);
+    int cy = min(max(int(floorf(start.y)), b0.z), b1.y - 1);
+    int cz = min(max(int(floorf(start.z)), b0.w), b1.z - 1);
+    if (from_outside) {  // the layer just inside the entry face
+        if (enter_axis == 0)
+            cx = d.x > 0.0f ? b0.y : b1.x - 1;
+        else if (enter_axis == 1)
+            cy = d.y > 0.0f ? b0.z : b1.y - 1;
+        else
+            cz = d.z > 0.0f ? b0.w : b1.z - 1;
     }
-    // A crossing at t along axis (step +-1) from a cell of palette index
-    // `from` into cell to_cell of index `to`: the entered cell's face, or the
-    // face of the cell being left seen from inside.
-    auto crossing = [&](float t, int axis, int stp, int from, int to, const int to_cell[3]) {
-        int k_from = voxel_kind(S, m.palette, from), k_to = voxel_kind(S, m.palette, to);
-        int sign, idx, cell[3] = {to_cell[0], to_cell[1], to_cell[2]};
-        if (k_to != 0 && voxel_face_visible(k_to, k_from)) {
-            sign = -stp;
-            idx = to;
-        } else if (voxel_face_visible(k_from, k_to)) {
-            sign = stp;
-            idx = from;
-            cell[axis] -= stp;
-        } else {
-            return false;
-        }
-        t_out = t;
-        face_out = axis | (sign > 0 ? 4 : 0);
-        mat_out = __ldg(&S.voxel_palettes[m.palette + idx].x);
-        if (m.edge_width > 0.0f && voxel_on_edge(S, m, cells, o + t * d, axis, sign, cell))
-            mat_out = m.edge_material;
-        return true;
-    };
-    int index = voxel_at(m, cells, c);
+    const int sx = d.x > 0.0f ? 1 : (d.x < 0.0f ? -1 : 0);
+    const int sy = d.y > 0.0f ? 1 : (d.y < 0.0f ? -1 : 0);
+    const int sz = d.z > 0.0f ? 1 : (d.z < 0.0f ? -1 : 0);
+    float tnx = sx > 0 ? (cx + 1 - o.x) / d.x : (sx < 0 ? (cx - o.x) / d.x : 3.0e38f);
+    float tny = sy > 0 ? (cy + 1 - o.y) / d.y : (sy < 0 ? (cy - o.y) / d.y : 3.0e38f);
+    float tnz = sz > 0 ? (cz + 1 - o.z) / d.z : (sz < 0 ? (cz - o.z) / d.z : 3.0e38f);
+    const float tdx = sx != 0 ? fabsf(1.0f / d.x) : 3.0e38f;
+    const float tdy = sy != 0 ? fabsf(1.0f / d.y) : 3.0e38f;
+    const float tdz = sz != 0 ? fabsf(1.0f / d.z) : 3.0e38f;
+    int k_cur = voxel_kind_at(m, kinds, cx, cy, cz);
     if (from_outside) {
-        int behind[3] = {c[0], c[1], c[2]};
-        behind[enter_axis] -= step[enter_axis];
-        if (crossing(t_enter, enter_axis, step[enter_axis], voxel_at(m, cells, behind), index, c))
+        // crossing into the block from the cell behind the entry face
+        int bx = cx - (enter_axis == 0 ? sx : 0), by = cy - (enter_axis == 1 ? sy : 0),
+            bz = cz - (enter_axis == 2 ? sz : 0);
+        int stp = enter_axis == 0 ? sx : (enter_axis == 1 ? sy : sz);
+        int which = voxel_crossing(voxel_kind_at(m, kinds, bx, by, bz), k_cur);
+        if (which != 0) {
+            int sign = which == 1 ? -stp : stp;
+            t_out = t_enter;
+            face_out = enter_axis | (sign > 0 ? 4 : 0);
+            float3 p = o + t_enter * d;
+            mat_out = which == 1 ? voxel_face_material(S, m, kinds, p, enter_axis, sign, cx, cy, cz)
+                                 : voxel_face_material(S, m, kinds, p, enter_axis, sign, bx, by, bz);
             return true;
+        }
     }
-    // The walk stays inside the block: at most its three extents of steps
+    // the walk stays inside the block: at most its three extents of steps
     for (int guard = 0; guard < 3 * kVoxelBlockMax + 4; guard++) {
-        int a = t_next[0] < t_next[1] ? (t_next[0] < t_next[2] ? 0 : 2) : (t_next[1] < t_next[2] ? 1 : 2);
-        float t = t_next[a];
+        int a = tnx < tny ? (tnx < tnz ? 0 : 2) : (tny < tnz ? 1 : 2);
+        float t;
+        int px = cx, py = cy, pz = cz, stp;
+        bool left;
+        if (a == 0) {
+            t = tnx;
+            cx += sx;
+            tnx += tdx;
+            stp = sx;
+            left = cx < b0.y || cx >= b1.x;
+        } else if (a == 1) {
+            t = tny;
+            cy += sy;
+            tny += tdy;
+            stp = sy;
+            left = cy < b0.z || cy >= b1.y;
+        } else {
+            t = tnz;
+            cz += sz;
+            tnz += tdz;
+            stp = sz;
+            left = cz < b0.w || cz >= b1.z;
+        }
         if (t > tmax)
             return false;
-        c[a] += step[a];
-        t_next[a] += t_delta[a];
-        int next = voxel_at(m, cells, c);
-        if (crossing(t, a, step[a], index, next, c))
+        int k_next = voxel_kind_at(m, kinds, cx, cy, cz);
+        int which = voxel_crossing(k_cur, k_next);
+        if (which != 0) {
+            int sign = which == 1 ? -stp : stp;
+            t_out = t;
+            face_out = a | (sign > 0 ? 4 : 0);
+            float3 p = o + t * d;
+            mat_out = which == 1 ? voxel_face_material(S, m, kinds, p, a, sign, cx, cy, cz)
+                                 : voxel_face_material(S, m, kinds, p, a, sign, px, py, pz);
             return true;
-        if (c[a] < lo[a] || c[a] >= hi[a])
-            return false;
-        index = next;
+        }
+        if (left)
+            return false;  // left the block
+        k_cur = k_next;
     }
     return false;
 }
@@ -512,21 +552,25 @@ MYPBR_DEV float safe_inv(float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysi
 // unbounded objects beside it (main.cpp:70-74 of the reference). media_key
 // seeds free-flight sampling in media; media_key == 0 skips media (used by the
 // deterministic ray-batch query).
-template <bool ANY>
+// VOX: whether voxel blocks are tested (kernels for scenes without voxels
+// leave that code out, and with it its registers).
+template <bool ANY, bool VOX = true>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key);
 
+template <bool VOX = true>
 MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
-    return walk<false>(S, o, d, tmin, tmax, media_key);
+    return walk<false, VOX>(S, o, d, tmin, tmax, media_key);
 }
 
 // Whether anything at all lies along o + t d, t in (tmin, tmax): the walk stops
 // at the first primitive it hits. For shadow rays in scenes where nothing
 // hittable can emit, this is all the reference's closest-hit query decides.
+template <bool VOX = true>
 MYPBR_DEV bool any_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
-    return walk<true>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
+    return walk<true, VOX>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
 }
 
-template <bool ANY>
+template <bool ANY, bool VOX>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
     HitInfo h;
     h.prim = kMiss;
@@ -585,7 +629,7 @@ MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, flo
                         got = hit_quad(S, idx, o, d, tmin, h.t, t, b1, b2);
                     } else if (kind == kMedium && media_key != 0) {
                         got = hit_medium(S, idx, o, d, tmin, h.t, hash_uniform(media_key, uint32_t(idx)), t);
-                    } else if (kind == kVoxel) {
+                    } else if (VOX && kind == kVoxel) {
                         int mat, face;
                         got = hit_voxel_block(S, idx, o, d, tmin, h.t, t, mat, face);
                         b1 = __int_as_float(mat);

@@ -29,6 +29,7 @@ struct RenderBuffers {
     uint32_t* class_queue = nullptr;          // one queue per shading class, capacity each
     uint32_t* shadow_queue = nullptr;
     uint32_t* counters = nullptr;
+    int* wave_state = nullptr;   // (first pass, passes) of the wave a captured graph replays; null: kernel arguments
     // film (pixel-indexed, FP64 sums)
     double* film = nullptr;   // radiance sum rgb
     double* film2 = nullptr;  // radiance squared sum rgb
@@ -70,6 +71,10 @@ struct mypbr_gpu_scene {
     mypbr_dev::RenderBuffers rb;
     mypbr_dev::GuideState guide;
     float3 box_lo{-1.0f, -1.0f, -1.0f}, box_hi{1.0f, 1.0f, 1.0f};  // bounds of the BVH's primitives
+    cudaStream_t stream = nullptr;  // the handle's own stream, for renders with host buffers (graph capture needs one)
+    // autotuned launch settings (0: built-in defaults)
+    size_t tuned_wave_paths = 0;
+    int tuned_block = 0;
 };
 
 namespace mypbr_dev {

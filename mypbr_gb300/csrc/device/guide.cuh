@@ -341,6 +341,10 @@ MYPBR_HD size_t guide_forward_smem(int hidden) {
 template <class Src, class Sink>
 __global__ void __launch_bounds__(128) k_guide_forward(GuideNetView net, Src src, Sink sink, long long rows) {
     extern __shared__ __align__(1024) uint8_t smem[];
+    rows = src.count(rows);
+    long long tiles = (rows + 127) / 128;
+    if (blockIdx.x >= tiles)
+        return;  // no tile for this CTA: nothing loaded, nothing allocated
     int P = guide_params(net.hidden);
     __nv_bfloat16* W = reinterpret_cast<__nv_bfloat16*>(smem);
     __nv_bfloat16* A = W + P;
@@ -364,8 +368,6 @@ __global__ void __launch_bounds__(128) k_guide_forward(GuideNetView net, Src src
     uint32_t tmem = *tmem_slot;
     uint32_t phase = 0;
     const uint32_t idesc = tc::idesc_bf16(128, 64);
-    rows = src.count(rows);
-    long long tiles = (rows + 127) / 128;
     bool failed = false;
     for (long long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         long long i = tile * 128 + row;

@@ -14,7 +14,7 @@ __global__ void k_trace(DeviceScene S, const float* rays, long long n, float* hi
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         const float* r = rays + 8 * k;
         float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
-        HitInfo h = closest_hit(S, o, d, r[6], r[7], 0);
+        HitInfo h = closest_hit<true>(S, o, d, r[6], r[7], 0);
         float* out = hits + 8 * k;
         if (h.prim == kMiss) {
             for (int c = 0; c < 8; c++)

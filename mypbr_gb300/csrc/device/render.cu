@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -171,14 +172,26 @@ MYPBR_DEV void camera_ray(const CameraParams& C, int i, int j, int pass, Rng& g,
 MYPBR_DEV float bits_f(uint32_t u) { return __uint_as_float(u); }
 MYPBR_DEV uint32_t f_bits(float f) { return __float_as_uint(f); }
 
+// (first pass, number of passes) of the current wave: from device memory when
+// a captured graph replays the wave, else from the kernel arguments.
+MYPBR_DEV int2 wave_of(const WaveParams& P) {
+    return P.B.wave_state ? make_int2(P.B.wave_state[0], P.B.wave_state[1]) : make_int2(P.pass0, P.npass);
+}
+
+__global__ void k_set_wave(int* state, int pass0, int npass) {
+    state[0] = pass0;
+    state[1] = npass;
+}
+
 __global__ void k_generate(WaveParams P) {
+    const int2 wv = wave_of(P);
     size_t npix = size_t(P.cam.width) * P.band_rows;
-    size_t n = npix * size_t(P.npass);
+    size_t n = npix * size_t(wv.y);
     size_t stride = size_t(gridDim.x) * blockDim.x;
     size_t first_pixel = size_t(P.first_row) * P.cam.width;
     for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
         uint32_t pixel = uint32_t(first_pixel + t % npix);
-        uint32_t pass = uint32_t(P.pass0 + int(t / npix));
+        uint32_t pass = uint32_t(wv.x + int(t / npix));
         int i = int(pixel % uint32_t(P.cam.width)), j = int(pixel / uint32_t(P.cam.width));
         Rng g = make_rng(P.seed, pixel, pass);
         float3 o, d;
@@ -195,7 +208,7 @@ __global__ void k_generate(WaveParams P) {
 
 // camera.h:253-277: albedo and normal of the first non-specular surface
 __global__ void k_features(WaveParams P) {
-    size_t n = size_t(P.cam.width) * P.band_rows * size_t(P.npass);
+    size_t n = size_t(P.cam.width) * P.band_rows * size_t(wave_of(P).y);
     size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
         float4 ro = P.B.ray_o[t], rd = P.B.ray_d[t];
@@ -205,7 +218,7 @@ __global__ void k_features(WaveParams P) {
         float3 tint = f3(1.0f), albedo = f3(1.0f), normal = f3(0.0f);
         bool done = false;
         for (int b = 0; b < 8 && !done; b++) {
-            HitInfo h = closest_hit(P.S, o, d, 0.001f, 3.0e38f, media_key(P, pixel, pass, 100 + b, 3));
+            HitInfo h = closest_hit<true>(P.S, o, d, 0.001f, 3.0e38f, media_key(P, pixel, pass, 100 + b, 3));
             if (h.prim == kMiss)
                 break;
             Surface s = make_surface(P.S, h, o, d);
@@ -253,6 +266,7 @@ MYPBR_DEV int hit_material(const DeviceScene& S, const HitInfo& h) {
 }
 
 // Closest hits of the extension queue; each ray then joins its shading class's queue.
+template <bool VOX>
 __global__ void __launch_bounds__(256) k_extend(WaveParams P, int depth) {
     uint32_t n = *ext_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
@@ -267,7 +281,7 @@ __global__ void __launch_bounds__(256) k_extend(WaveParams P, int depth) {
             uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
             key = media_key(P, pixel, pass, uint32_t(depth), 0);
         }
-        HitInfo h = closest_hit(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
+        HitInfo h = closest_hit<VOX>(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
         P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
         int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h)]);
         uint32_t* counter = class_counter(P, depth, c);
@@ -506,6 +520,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
     }
 }
 
+template <bool VOX>
 __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
     uint32_t n = *sh_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
@@ -529,13 +544,13 @@ __global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
             // sample already holds the sky's radiance (sc.w = 1).
             if (P.has_media)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1);
-            if (!any_hit(S, o, d, 0.001f, 3.0e38f, key))
+            if (!any_hit<VOX>(S, o, d, 0.001f, 3.0e38f, key))
                 emission = sc.w != 0.0f ? f3(1.0f) : escaped_radiance(S, d, false);
         } else
         for (int hop = 0; hop <= 16; hop++) {
             if (P.has_media)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1 + 4 * hop);
-            HitInfo h = closest_hit(S, o, d, 0.001f, 3.0e38f, key);
+            HitInfo h = closest_hit<VOX>(S, o, d, 0.001f, 3.0e38f, key);
             if (h.prim == kMiss) {
                 emission = escaped_radiance(S, d, false);
                 break;
@@ -618,7 +633,8 @@ __global__ void k_channel_variance(WaveParams P, int samples, double* out) {
 
 int release_buffers(RenderBuffers& rb) {
     void* ptrs[] = {rb.ray_o, rb.ray_d, rb.beta, rb.radiance, rb.hit, rb.sh_o, rb.sh_d, rb.sh_c, rb.queue[0],
-                    rb.queue[1], rb.class_queue, rb.shadow_queue, rb.counters, rb.film, rb.film2, rb.feat};
+                    rb.queue[1], rb.class_queue, rb.shadow_queue, rb.counters, rb.wave_state, rb.film, rb.film2,
+                    rb.feat};
     for (void* p : ptrs)
         if (p)
             cudaFree(p);
@@ -626,17 +642,39 @@ int release_buffers(RenderBuffers& rb) {
     return MYPBR_OK;
 }
 
-// The guiding network's rows: the vertices of shading class `cls` at a bounce.
+// The guiding network's rows at a bounce: the vertices of the guidable
+// shading classes' queues, one after another.
+MYPBR_HD constexpr int guided_class(int c) {
+    return c == 0 ? kClassLambert : c == 1 ? kClassMetal : c == 2 ? kClassPrincipled : kClassGeneric;
+}
+
+MYPBR_DEV uint32_t guided_slot(const WaveParams& P, int depth, long long i) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        long long n = *class_counter(P, depth, guided_class(c));
+        if (i < n)
+            return class_queue(P, guided_class(c))[i];
+        i -= n;
+    }
+    return 0;  // not reached: i < count()
+}
+
 struct GuideQueueSource {
     WaveParams P;
-    int depth, cls;
-    MYPBR_DEV long long count(long long) const { return *class_counter(P, depth, cls); }
+    int depth;
+    MYPBR_DEV long long count(long long) const {
+        long long n = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+            n += *class_counter(P, depth, guided_class(c));
+        return n;
+    }
     MYPBR_DEV void fill(long long i, __nv_bfloat16* A, int row) const {
         if (i < 0) {
             guide_encode_row(nullptr, A, row);
             return;
         }
-        uint32_t slot = class_queue(P, cls)[i];
+        uint32_t slot = guided_slot(P, depth, i);
         float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot], hb = P.B.hit[slot];
         HitInfo h;
         h.t = hb.x;
@@ -652,9 +690,9 @@ struct GuideQueueSource {
 
 struct GuidePackSink {
     WaveParams P;
-    int cls;
+    int depth;
     MYPBR_DEV void put(long long i, const float* v) const {
-        uint32_t slot = class_queue(P, cls)[i];
+        uint32_t slot = guided_slot(P, depth, i);
         GuidePacked pk;
         guide_pack(v, pk);
         P.guide_mix[slot] = pk;
@@ -694,6 +732,7 @@ int ensure_buffers(RenderBuffers& rb, size_t capacity, size_t pixels, int depth_
     A(rb.class_queue, capacity * kShadeClasses);
     A(rb.shadow_queue, capacity);
     A(rb.counters, counter_words(depth_slots));
+    A(rb.wave_state, 2);
     A(rb.film, 3 * pixels);
     A(rb.film2, 3 * pixels);
     A(rb.feat, 7 * pixels);
@@ -756,25 +795,31 @@ int bad_arg(const std::string& m) {
 
 struct Launch {
     int grid_extend, grid_shade, grid_shadow, grid_stream;
+    int block = 256;              // threads per block of extend, shade and shadow
     bool guided_kernels = false;  // the shading variants of guided renders
     int grid_guide = 0;
     size_t guide_smem = 0;
     GuideNetView net{};
 };
 
-Launch launch_config(const mypbr_gpu_scene& G) {
+// Grids of `block` threads: SMs x resident blocks (persistent-style loops).
+Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
     Launch L{};
+    L.block = block == 128 || block == 256 ? block : (G.tuned_block ? G.tuned_block : 256);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend, 256, 0);
+    bool vox = G.dev.has_voxels;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vox ? (const void*)k_extend<true> : (const void*)k_extend<false>,
+                                                  L.block, 0);
     L.grid_extend = G.sm_count * std::max(per_sm, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vox ? (const void*)k_shadow<true> : (const void*)k_shadow<false>,
+                                                  L.block, 0);
     L.grid_shadow = G.sm_count * std::max(per_sm, 1);
     L.grid_stream = G.sm_count * 8;
     int worst = 1;
     for (auto f : {(const void*)k_shade<kClassMiss, false>, (const void*)k_shade<kClassLambert, false>,
                    (const void*)k_shade<kClassMetal, false>, (const void*)k_shade<kClassDielectric, false>,
                    (const void*)k_shade<kClassPrincipled, false>, (const void*)k_shade<kClassGeneric, false>}) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, L.block, 0);
         worst = std::max(worst, per_sm);
     }
     L.grid_shade = G.sm_count * worst;
@@ -860,34 +905,98 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
         launches++;
     }
     for (int depth = 0; depth < P.max_depth; depth++) {
-        TIMED(1, (k_extend<<<L.grid_extend, 256, 0, st>>>(P, depth)));
+        if (P.S.has_voxels)
+            TIMED(1, (k_extend<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+        else
+            TIMED(1, (k_extend<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         if (P.guided) {  // the mixtures of this bounce's guidable vertices
-            for (int cls : {kClassLambert, kClassMetal, kClassPrincipled, kClassGeneric}) {
-                TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128, L.guide_smem, st>>>(
-                             L.net, GuideQueueSource{P, depth, cls}, GuidePackSink{P, cls}, 0)));
-                launches++;
-            }
+            TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128, L.guide_smem, st>>>(
+                         L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
+            launches++;
         }
         if (L.guided_kernels) {
-            TIMED(2, (k_shade<kClassMiss, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassLambert, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassMetal, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassDielectric, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassPrincipled, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassGeneric, true><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMiss, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassLambert, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMetal, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassDielectric, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassPrincipled, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassGeneric, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
         } else {
-            TIMED(2, (k_shade<kClassMiss, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassLambert, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassMetal, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassDielectric, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassPrincipled, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassGeneric, false><<<L.grid_shade, 256, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMiss, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassLambert, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMetal, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassDielectric, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassPrincipled, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassGeneric, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
         }
-        TIMED(3, (k_shadow<<<L.grid_shadow, 256, 0, st>>>(P, depth)));
+        if (P.S.has_voxels)
+            TIMED(3, (k_shadow<true><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
+        else
+            TIMED(3, (k_shadow<false><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
         launches += 2 + kShadeClasses;
     }
     MYPBR_CUDA(cudaGetLastError());
     return MYPBR_OK;
+}
+
+// One wave's kernel sequence captured as a CUDA graph and replayed for every
+// wave with the same settings; the pass range is read from device memory
+// (wave_state), set by a one-thread kernel before each replay.
+struct WaveGraph {
+    cudaGraphExec_t exec = nullptr;
+    int key = -1;
+    uint64_t launches = 0;  // kernels in the graph
+    ~WaveGraph() {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+    }
+};
+
+int launch_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T,
+                WaveGraph* graph) {
+    if (!graph)
+        return run_wave(P, L, st, launches, T);
+    int key = (P.guided ? 1 : 0) | (P.record ? 2 : 0) | (P.guide_alpha > 0.0f ? 4 : 0);
+    if (!graph->exec || graph->key != key) {
+        if (graph->exec) {
+            cudaGraphExecDestroy(graph->exec);
+            graph->exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        MYPBR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        uint64_t n = 0;
+        int s = run_wave(P, L, st, n, T);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (s != MYPBR_OK) {
+            if (g)
+                cudaGraphDestroy(g);
+            return s;
+        }
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&graph->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaGraphInstantiate");
+        graph->key = key;
+        graph->launches = n;
+    }
+    k_set_wave<<<1, 1, 0, st>>>(P.B.wave_state, P.pass0, P.npass);
+    MYPBR_CUDA(cudaGraphLaunch(graph->exec, st));
+    launches += graph->launches + 1;
+    return MYPBR_OK;
+}
+
+// Whether waves on stream st may be captured: not the legacy default stream,
+// and not a stream the caller is capturing already (our launches then go
+// into the caller's graph as they are).
+bool graphs_allowed(cudaStream_t st) {
+    if (st == nullptr || st == cudaStreamLegacy)
+        return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess)
+        return false;
+    return cs == cudaStreamCaptureStatusNone;
 }
 
 }  // namespace
@@ -943,9 +1052,10 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
     R.npix = size_t(P.cam.width) * P.band_rows;
     R.timing = o->timing != 0;
     R.spp = o->samples_per_pixel;
-    // About 32M paths in flight per wave (or what the caller asks)
+    // About 32M paths in flight per wave (or the autotuned size, or what the caller asks)
+    size_t wave_paths = G->tuned_wave_paths ? G->tuned_wave_paths : (size_t(32) << 20);
     int per_wave = o->samples_per_wave > 0 ? o->samples_per_wave
-                                           : int(std::max<size_t>(1, (size_t(32) << 20) / std::max<size_t>(R.npix, 1)));
+                                           : int(std::max<size_t>(1, wave_paths / std::max<size_t>(R.npix, 1)));
     per_wave = std::min(per_wave, R.spp);
     if (save_every > 0)
         per_wave = std::min(per_wave, save_every);
@@ -991,6 +1101,39 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
     return MYPBR_OK;
 }
 
+// Wave number `wave` of a render, starting at pass0: its size, the guiding
+// state, the kernels (replayed from `graph` when given), then for guided
+// renders the training steps on what the wave recorded.
+int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int save_every, cudaStream_t st,
+                uint64_t& launches, KernelTimer& T, WaveGraph* graph) {
+    WaveParams& P = R.P;
+    bool train_wave = R.guided && wave < kGuideTrainWaves;
+    P.pass0 = pass0;
+    P.npass = std::min(train_wave ? R.per_wave_train : R.per_wave, R.spp - pass0);
+    if (save_every > 0)  // waves end on every multiple of save_every
+        P.npass = std::min(P.npass, save_every - pass0 % save_every);
+    if (R.guided) {
+        const GuideState& g = G->guide;
+        P.guided = g.steps >= kGuideMinSteps;
+        P.guide_alpha = P.guided ? kGuideAlpha : 0.0f;
+        P.record = g.steps < kGuideMaxSteps;
+        if (P.record)
+            MYPBR_CUDA(cudaMemsetAsync(P.rec.count, 0, sizeof(uint32_t), st));
+    }
+    int s = launch_wave(P, R.L, st, launches, T, graph);
+    if (s != MYPBR_OK)
+        return s;
+    if (R.guided && P.record) {
+        if ((s = T.begin(4)) != MYPBR_OK)
+            return s;
+        s = guide_train(G, train_wave ? kGuideStepsEarly : kGuideStepsLate, 4 * G->sm_count, kGuideLr, st);
+        if (s != MYPBR_OK || (s = T.end()) != MYPBR_OK)
+            return s;
+        launches += 3 * (train_wave ? kGuideStepsEarly : kGuideStepsLate);
+    }
+    return MYPBR_OK;
+}
+
 struct Totals {
     unsigned long long* d = nullptr;
     ~Totals() {
@@ -1016,32 +1159,15 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
     KernelTimer T;
     T.on = R.timing;
     T.st = st;
+    // per-kernel timing needs events around each launch: no graph then
+    WaveGraph graph;
+    bool use_graph = !T.on && graphs_allowed(st);
+    P.B.wave_state = use_graph ? G->rb.wave_state : nullptr;
     int wave = 0;
     for (int pass0 = 0; pass0 < R.spp; pass0 += P.npass, wave++) {
-        bool train_wave = R.guided && wave < kGuideTrainWaves;
-        P.pass0 = pass0;
-        P.npass = std::min(train_wave ? R.per_wave_train : R.per_wave, R.spp - pass0);
-        if (save_every > 0)  // waves end on every multiple of save_every
-            P.npass = std::min(P.npass, save_every - pass0 % save_every);
-        if (R.guided) {
-            const GuideState& g = G->guide;
-            P.guided = g.steps >= kGuideMinSteps;
-            P.guide_alpha = P.guided ? kGuideAlpha : 0.0f;
-            P.record = g.steps < kGuideMaxSteps;
-            if (P.record)
-                MYPBR_CUDA(cudaMemsetAsync(P.rec.count, 0, sizeof(uint32_t), st));
-        }
-        int s = run_wave(P, R.L, st, launches, T);
+        int s = render_wave(G, R, wave, pass0, save_every, st, launches, T, use_graph ? &graph : nullptr);
         if (s != MYPBR_OK)
             return s;
-        if (R.guided && P.record) {
-            if ((s = T.begin(4)) != MYPBR_OK)
-                return s;
-            s = guide_train(G, train_wave ? kGuideStepsEarly : kGuideStepsLate, 4 * G->sm_count, kGuideLr, st);
-            if (s != MYPBR_OK || (s = T.end()) != MYPBR_OK)
-                return s;
-            launches += 3 * (train_wave ? kGuideStepsEarly : kGuideStepsLate);
-        }
         int done = pass0 + P.npass;
         if (cb && save_every > 0 && done % save_every == 0 && done < R.spp) {
             k_resolve<<<R.L.grid_stream, 256, 0, st>>>(P, done, d_rad, d_alb, d_nrm, d_var);
@@ -1144,7 +1270,7 @@ extern "C" int mypbr_gpu_render_ex(mypbr_gpu_scene* G, const mypbr_camera* cam, 
     }
     if (channel_variance)
         MYPBR_CUDA(cudaMalloc(&chv.p, 3 * full * sizeof(double)));
-    cudaStream_t st = nullptr;
+    cudaStream_t st = G->stream;
     s = render_all(G, R, st, rad.p, alb.p, nrm.p, var.p, chv.p, save_every, on_pass, user, radiance,
                    feats ? albedo : nullptr, feats ? normal : nullptr, feats ? variance : nullptr, stats);
     if (s != MYPBR_OK)
@@ -1173,6 +1299,197 @@ extern "C" int mypbr_gpu_render(mypbr_gpu_scene* G, const mypbr_camera* cam, con
                                 mypbr_pass_callback on_pass, void* user) {
     return mypbr_gpu_render_ex(G, cam, opts, radiance, albedo, normal, variance, nullptr, save_every, on_pass, user,
                                nullptr);
+}
+
+// ------------------------------------------------------------ batches
+//
+// Many renders at once: every job's waves are launched in turn, one wave per
+// job per round, each job on its scene handle's own stream, so renders of
+// different scenes overlap on the GPU while their waves replay as captured
+// graphs. Jobs that share a scene handle run one after another (they share
+// its path buffers and network).
+
+namespace mypbr_dev {
+namespace {
+
+struct BatchJob {
+    RenderSetup R;
+    WaveGraph graph;
+    KernelTimer T;
+    Totals tot;
+    uint64_t launches = 0;
+    int pass0 = 0, wave = 0;
+    bool started = false;
+};
+
+int job_start(mypbr_batch_job& jb, BatchJob& j) {
+    mypbr_gpu_scene* G = jb.scene;
+    if (!jb.radiance)
+        return bad_arg("mypbr_gpu_render_batch: every job needs a radiance buffer");
+    int s = prepare(G, jb.camera, jb.opts, 0, j.R);
+    if (s != MYPBR_OK)
+        return s;
+    WaveParams& P = j.R.P;
+    cudaStream_t st = G->stream;
+    MYPBR_CUDA(cudaMalloc(&j.tot.d, 2 * sizeof(unsigned long long)));
+    MYPBR_CUDA(cudaMemsetAsync(j.tot.d, 0, 2 * sizeof(unsigned long long), st));
+    P.totals = j.tot.d;
+    size_t full = size_t(P.cam.width) * P.cam.height;
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * full * sizeof(double), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * full * sizeof(double), st));
+    if (P.collect_features)
+        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * full * sizeof(double), st));
+    P.B.wave_state = G->rb.wave_state;
+    j.T.st = st;
+    j.started = true;
+    return MYPBR_OK;
+}
+
+}  // namespace
+}  // namespace mypbr_dev
+
+extern "C" int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n) {
+    if (n < 0 || (n > 0 && !jobs))
+        return bad_arg("mypbr_gpu_render_batch: bad job list");
+    std::vector<std::unique_ptr<BatchJob>> J;
+    std::vector<mypbr_gpu_scene*> scenes;            // in first-use order
+    std::vector<std::vector<int>> order;             // job indices per scene
+    for (int i = 0; i < n; i++) {
+        jobs[i].status = MYPBR_ERR_INVALID_ARGUMENT;
+        J.emplace_back(new BatchJob());
+        if (!jobs[i].scene || !jobs[i].camera || !jobs[i].opts)
+            continue;
+        auto it = std::find(scenes.begin(), scenes.end(), jobs[i].scene);
+        if (it == scenes.end()) {
+            scenes.push_back(jobs[i].scene);
+            order.emplace_back();
+            it = scenes.end() - 1;
+        }
+        order[size_t(it - scenes.begin())].push_back(i);
+    }
+    std::vector<size_t> next(scenes.size(), 0);
+    int first_error = MYPBR_OK;
+    bool any = true;
+    while (any) {
+        any = false;
+        for (size_t k = 0; k < scenes.size(); k++) {
+            if (next[k] >= order[k].size())
+                continue;
+            any = true;
+            int i = order[k][next[k]];
+            mypbr_batch_job& jb = jobs[i];
+            BatchJob& j = *J[size_t(i)];
+            mypbr_gpu_scene* G = scenes[k];
+            int s = MYPBR_OK;
+            if (!j.started)
+                s = job_start(jb, j);
+            if (s == MYPBR_OK && j.pass0 < j.R.spp) {
+                s = render_wave(G, j.R, j.wave, j.pass0, 0, G->stream, j.launches, j.T, &j.graph);
+                j.pass0 += j.R.P.npass;
+                j.wave++;
+                if (s == MYPBR_OK)
+                    continue;  // this job's next wave in the next round
+            }
+            if (s == MYPBR_OK) {  // all waves launched: the averages into the caller's buffers
+                WaveParams& P = j.R.P;
+                k_resolve<<<j.R.L.grid_stream, 256, 0, G->stream>>>(P, j.R.spp, jb.radiance, jb.albedo, jb.normal,
+                                                                   jb.variance);
+                cudaError_t e = cudaGetLastError();
+                s = e == cudaSuccess ? MYPBR_OK : cuda_fail(e, "k_resolve");
+                // the next job of this scene reuses the buffers: the stream orders it
+            }
+            jb.status = s;
+            if (s != MYPBR_OK && first_error == MYPBR_OK)
+                first_error = s;
+            next[k]++;
+        }
+    }
+    for (mypbr_gpu_scene* G : scenes) {
+        cudaError_t e = cudaStreamSynchronize(G->stream);
+        int s = e == cudaSuccess ? check_device_error(G) : cuda_fail(e, "mypbr_gpu_render_batch");
+        if (s != MYPBR_OK) {
+            for (int i = 0; i < n; i++)
+                if (jobs[i].scene == G && jobs[i].status == MYPBR_OK)
+                    jobs[i].status = s;
+            if (first_error == MYPBR_OK)
+                first_error = s;
+        }
+    }
+    for (int i = 0; i < n; i++)
+        if (jobs[i].status != MYPBR_OK && first_error == MYPBR_OK)
+            first_error = jobs[i].status;
+    return first_error;
+}
+
+// ------------------------------------------------------------ autotuner
+//
+// Tries the threads per block of the bounce kernels (128, 256) and the paths
+// per wave (4M, 8M, 16M, 32M: the queue capacity) on short renders of the
+// given view, and keeps the fastest on the scene handle for later renders.
+
+extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* opts,
+                                  mypbr_tune_result* out) {
+    if (!G || !cam || !opts)
+        return bad_arg("mypbr_gpu_autotune: null argument");
+    mypbr_render_opts o = *opts;
+    o.samples_per_wave = 0;
+    o.timing = 0;
+    o.guided = 0;
+    int w = cam->image_width;
+    int h = cam->image_height > 0 ? cam->image_height : std::max(1, int(cam->image_width / cam->aspect_ratio));
+    size_t npix = size_t(w) * h;
+    // about 64M paths per trial, at most the caller's spp
+    o.samples_per_pixel = int(std::max<size_t>(1, std::min<size_t>(size_t(opts->samples_per_pixel),
+                                                                       (size_t(64) << 20) / std::max<size_t>(npix, 1))));
+    DevBuf rad;
+    MYPBR_CUDA(cudaMalloc(&rad.p, 3 * npix * sizeof(double)));
+    const int blocks[2] = {128, 256};
+    const size_t waves[4] = {size_t(4) << 20, size_t(8) << 20, size_t(16) << 20, size_t(32) << 20};
+    mypbr_tune_result res{};
+    double best = -1;
+    size_t keep_paths = G->tuned_wave_paths;
+    int keep_block = G->tuned_block;
+    cudaEvent_t e0, e1;
+    MYPBR_CUDA(cudaEventCreate(&e0));
+    MYPBR_CUDA(cudaEventCreate(&e1));
+    int status = MYPBR_OK;
+    int trial = 0;
+    for (int b : blocks) {
+        for (size_t wp : waves) {
+            G->tuned_block = b;
+            G->tuned_wave_paths = wp;
+            float ms = 0;
+            for (int rep = 0; rep < 2 && status == MYPBR_OK; rep++) {  // the first run warms up
+                cudaEventRecord(e0, G->stream);
+                status = mypbr_gpu_render_device(G, cam, &o, rad.p, nullptr, nullptr, nullptr, G->stream, nullptr);
+                cudaEventRecord(e1, G->stream);
+                cudaEventSynchronize(e1);
+                cudaEventElapsedTime(&ms, e0, e1);
+            }
+            if (status != MYPBR_OK)
+                break;
+            double mp = double(npix) * o.samples_per_pixel / (ms * 1e-3) / 1e6;
+            res.trial_mpaths[trial++] = mp;
+            if (mp > best) {
+                best = mp;
+                res.block = b;
+                res.wave_paths = int64_t(wp);
+                res.mpaths_per_s = mp;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (status != MYPBR_OK) {
+        G->tuned_wave_paths = keep_paths;
+        G->tuned_block = keep_block;
+        return status;
+    }
+    G->tuned_block = res.block;
+    G->tuned_wave_paths = size_t(res.wave_paths);
+    if (out)
+        *out = res;
+    return MYPBR_OK;
 }
 
 // ------------------------------------------------- render without allocation

@@ -7,6 +7,7 @@
 // and leaf references, light members. The BVH depth is checked against the
 // traversal stack the kernels hold.
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -280,12 +281,16 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     mypbr_gpu_scene& G = *holder;
     MYPBR_CUDA(cudaGetDevice(&G.device));
     MYPBR_CUDA(cudaDeviceGetAttribute(&G.sm_count, cudaDevAttrMultiProcessorCount, G.device));
+    MYPBR_CUDA(cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking));
     DeviceScene& D = G.dev;
     Uploader up{G};
     auto fail_cleanup = [&](int s) {
         for (void* p : G.allocations)
             cudaFree(p);
         G.allocations.clear();
+        if (G.stream)
+            cudaStreamDestroy(G.stream);
+        G.stream = nullptr;
         return s;
     };
 #define PUT(vec, dst)                          \
@@ -308,7 +313,7 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
         if (G.max_depth_bvh >= kBvhStack) {
             set_error_message("mypbr_gpu_scene_create: BVH depth " + std::to_string(G.max_depth_bvh) +
                               " exceeds the traversal stack (" + std::to_string(kBvhStack) + ")");
-            return MYPBR_ERR_UNSUPPORTED;
+            return fail_cleanup(MYPBR_ERR_UNSUPPORTED);
         }
         std::vector<int> new_index(size_t(F.bvh_node_count), -1);
         for (int64_t k = 0; k < F.bvh_node_count; k++)
@@ -441,7 +446,11 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     PUT(unb, D.unbounded);
     D.unbounded_count = int(unb.size());
 
+    // Per (cells, palette) pair, the cells' kinds: the DDA then reads one byte
+    // per step and looks the palette up only for the material of a hit.
     std::vector<DevVoxelModel> vmodels;
+    std::vector<uint8_t> vkinds;
+    std::map<std::pair<int64_t, int>, long long> kinds_at;
     for (int64_t k = 0; k < F.voxel_model_count; k++) {
         const auto& m = F.voxel_models[k];
         DevVoxelModel d{};
@@ -453,9 +462,22 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
         d.palette = m.palette;
         d.edge_material = m.edge_material;
         d.edge_width = float(m.edge_width);
+        auto key = std::make_pair(int64_t(m.cells), int(m.palette));
+        auto it = kinds_at.find(key);
+        if (it == kinds_at.end()) {
+            size_t n = size_t(m.nx) * m.ny * m.nz;
+            long long off = (long long)vkinds.size();
+            vkinds.resize(vkinds.size() + n);
+            for (size_t c = 0; c < n; c++)
+                vkinds[size_t(off) + c] = uint8_t(F.voxel_palettes[m.palette + F.voxel_cells[m.cells + int64_t(c)]].kind);
+            it = kinds_at.emplace(key, off).first;
+        }
+        d.kinds = it->second;
         vmodels.push_back(d);
     }
     PUT(vmodels, D.voxel_models);
+    PUT(vkinds, D.voxel_kinds);
+    D.has_voxels = F.voxel_block_count > 0;
     std::vector<int4> vblocks;
     for (int64_t k = 0; k < F.voxel_block_count; k++) {
         const auto& b = F.voxel_blocks[k];
@@ -700,5 +722,7 @@ extern "C" void mypbr_gpu_scene_destroy(mypbr_gpu_scene* scene) {
     mypbr_dev::release_guide(scene->guide);
     for (void* p : scene->allocations)
         cudaFree(p);
+    if (scene->stream)
+        cudaStreamDestroy(scene->stream);
     delete scene;
 }

@@ -11,9 +11,10 @@
 // as instance::hit does), and one BVH is built over every primitive.
 //
 // MagicaVoxel models (`vox`) become voxel blocks walked by a grid DDA, or
-// with `quads` their visible faces. Not handled here (MYPBR_ERR_UNSUPPORTED
-// with a message): glTF meshes, "sky atmosphere" / "style voxel", cyclorama,
-// softbox, MTL files and 8-bit image textures (PNG/JPEG); .hdr images are read.
+// with `quads` their visible faces; `sky atmosphere` is baked into a 256 x 128
+// environment (sky_model.h). Not handled here (MYPBR_ERR_UNSUPPORTED with a
+// message): glTF meshes, cyclorama, softbox, MTL files and 8-bit image
+// textures (PNG/JPEG); .hdr images are read.
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -29,6 +30,7 @@
 #include "bvh_build.h"
 #include "host_math.h"
 #include "host_scene.h"
+#include "sky_model.h"
 #include "vox_reader.h"
 
 #include <array>
@@ -248,6 +250,8 @@ class Loader {
     V3 sun_tint{1, 1, 1};
     bool sun_disk = true;
     bool sky_uniform = false, sky_atmosphere = false;
+    mypbr_sky::Settings air;
+    std::vector<double> env_fp64;  // a baked sky's pixels as the reference keeps them (FP64), for its power
     V3 sky_radiance;
     bool ground = false;
     double ground_height = 0;
@@ -1537,9 +1541,18 @@ class Loader {
                 sky_uniform = true;
                 S.use_sky = true;
                 sky_atmosphere = false;
-            } else if (type == "atmosphere") {
-                std::string rest;
-                while (in >> rest) {
+            } else if (type == "atmosphere") {  // scene.h:574-586
+                const char* usage =
+                    "expected 'sky atmosphere [rayleigh <x>] [mie <x>] [mie_g <g>] [ozone <x>] [intensity <s>]'";
+                std::string key;
+                while (in >> key) {
+                    bool ok = (key == "rayleigh" && in >> air.rayleigh && air.rayleigh >= 0) ||
+                              (key == "mie" && in >> air.mie && air.mie >= 0) ||
+                              (key == "mie_g" && in >> air.mie_g && air.mie_g > -1 && air.mie_g < 1) ||
+                              (key == "ozone" && in >> air.ozone && air.ozone >= 0) ||
+                              (key == "intensity" && in >> air.intensity && air.intensity >= 0);
+                    if (!ok)
+                        return fail(usage);
                 }
                 sky_atmosphere = true;
                 sky_uniform = false;
@@ -1581,6 +1594,7 @@ class Loader {
             sun_disk = true;
             sky_uniform = false;
             sky_atmosphere = voxel;
+            air = mypbr_sky::Settings();
             S.use_sky = true;
             ground = voxel;
             ground_material = voxel ? lambertian(V3(0.3, 0.3, 0.3)) : default_material;
@@ -1782,8 +1796,11 @@ class Loader {
             double s = std::sin(kPi * (j + 0.5) / h);
             for (int i = 0; i < w; i++) {
                 // "sky uniform" keeps its FP64 radiance, as the reference's in-memory sky does
-                const float* p = &S.env_pixels[(size_t(j) * w + i) * 3];
-                V3 c = uniform_sky_env ? sky_radiance : V3(p[0], p[1], p[2]);
+                size_t k = (size_t(j) * w + i) * 3;
+                const float* p = &S.env_pixels[k];
+                V3 c = uniform_sky_env     ? sky_radiance
+                       : !env_fp64.empty() ? V3(env_fp64[k], env_fp64[k + 1], env_fp64[k + 2])
+                                           : V3(p[0], p[1], p[2]);
                 double wgt = luminance(c) * s;
                 sum += std::fmax(wgt, 0.0);
             }
@@ -1810,9 +1827,28 @@ class Loader {
         double el = radians(sun_elevation), az = radians(sun_azimuth);
         V3 sun_dir(std::cos(el) * std::sin(az), std::sin(el), -std::cos(el) * std::cos(az));
         V3 sun_irr = sun_intensity * sun_tint;
-        if (sky_atmosphere) {
-            unsupported = true;
-            return fail("'sky atmosphere' is not supported by this backend");
+        if (sky_atmosphere) {  // scene.h:1220-1230: a 256 x 128 bake, the sun reddened by the air
+            if (has_environment)
+                return fail("'sky atmosphere' and 'environment' can't be used together");
+            const int w = 256, h = 128;
+            double sd[3] = {sun_dir.x, sun_dir.y, sun_dir.z};
+            mypbr_sky::C3 irr{sun_irr.x, sun_irr.y, sun_irr.z};
+            std::vector<float> rgb(size_t(w) * h * 3);
+            env_fp64.assign(rgb.size(), 0.0);
+            for (int j = 0; j < h; j++)
+                for (int i = 0; i < w; i++) {
+                    mypbr_sky::C3 c = mypbr_sky::bake_pixel(air, i, j, w, h, sd, irr);
+                    size_t k = (size_t(j) * w + i) * 3;
+                    env_fp64[k] = c.r;
+                    env_fp64[k + 1] = c.g;
+                    env_fp64[k + 2] = c.b;
+                    rgb[k] = float(c.r);
+                    rgb[k + 1] = float(c.g);
+                    rgb[k + 2] = float(c.b);
+                }
+            set_environment(w, h, std::move(rgb), 1.0, 0.0);
+            mypbr_sky::C3 t = mypbr_sky::sun_transmittance(air, sd);
+            sun_irr = V3(sun_irr.x * t.r, sun_irr.y * t.g, sun_irr.z * t.b);
         }
         if (sun_on) {
             S.sun.enabled = 1;

@@ -9,6 +9,10 @@ own inputs (.scene text, Radiance .hdr, MagicaVoxel .vox).
                       a uniform sky; 1920 x 1080, depth 16. Inside the hall
                       nearly all light arrives after a bounce off a few small
                       sunlit patches: occluded lighting.
+  triangle_room_scene a 20 x 8 x 30 room of about 2,000,000 triangles (fBm-
+                      displaced walls, 400 columns) with 32 principled
+                      materials and 16 emissive quads; 1920 x 1080, 64 spp,
+                      depth 12.
 
 No dataset is involved: every input is generated here from a seed.
 """
@@ -285,6 +289,116 @@ def voxel_hall_scene(directory, size=512, seed=5, spp=64, width=1920, height=108
              "sun elevation 40 azimuth 160 intensity 1000 angle 0.54",
              "vox hall.vox"]
     path = os.path.join(directory, "voxel_hall.scene")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return path
+
+
+# ------------------------------------------------------------ the triangle room
+
+def _fbm(points, rng_seed, octaves=4):
+    """A smooth scalar field over 3D points: sums of random plane waves."""
+    rng = np.random.default_rng(rng_seed)
+    out = np.zeros(len(points))
+    amp, freq = 1.0, 0.6
+    for _ in range(octaves):
+        for _ in range(3):
+            k = rng.normal(size=3)
+            k *= freq / np.linalg.norm(k)
+            out += amp * np.sin(points @ k + rng.uniform(0, 2 * np.pi))
+        amp *= 0.5
+        freq *= 2.1
+    return out / 3.0
+
+
+def _grid(corner, u, v, nu, nv):
+    """Vertices (nu+1)(nv+1) x 3 and triangles 2 nu nv x 3 of a subdivided parallelogram."""
+    a, b = np.meshgrid(np.linspace(0, 1, nu + 1), np.linspace(0, 1, nv + 1), indexing="ij")
+    verts = corner + a.reshape(-1, 1) * u + b.reshape(-1, 1) * v
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    p00 = (i * (nv + 1) + j).ravel()
+    p10 = p00 + (nv + 1)
+    tris = np.concatenate([np.stack([p00, p10, p10 + 1], 1), np.stack([p00, p10 + 1, p00 + 1], 1)])
+    return verts, tris
+
+
+def _column(cx, cz, radius, height, segs, rings):
+    """An open cylinder around the y axis at (cx, cz)."""
+    ang = np.linspace(0, 2 * np.pi, segs + 1)[:-1]
+    y = np.linspace(0, height, rings + 1)
+    A, Y = np.meshgrid(ang, y, indexing="ij")
+    verts = np.stack([cx + radius * np.cos(A).ravel(), Y.ravel(), cz + radius * np.sin(A).ravel()], 1)
+    i, j = np.meshgrid(np.arange(segs), np.arange(rings), indexing="ij")
+    p00 = (i * (rings + 1) + j).ravel()
+    p10 = ((i + 1) % segs * (rings + 1) + j).ravel()
+    tris = np.concatenate([np.stack([p00, p00 + 1, p10], 1), np.stack([p10, p00 + 1, p10 + 1], 1)])
+    return verts, tris
+
+
+def triangle_room_scene(directory, triangles=2_000_000, seed=3, spp=64, width=1920, height=1080, depth=12):
+    """A 20 x 8 x 30 room whose walls, floor and ceiling are finely tessellated
+    and displaced by fBm, with 400 columns in 20 rows; 32 principled
+    materials (roughness U[0.05, 1], metallic 0 or 1) picked per column and per
+    wall patch through `usemtl m0..m31`; 16 emissive quads under the ceiling
+    with emission lognormal(2, 1). About `triangles` triangles in one OBJ."""
+    rng = np.random.default_rng(seed)
+    parts = []  # (verts, tris, material index)
+    # columns: 400, each segs x rings x 2 triangles
+    col_tris = triangles // 2
+    per_col = col_tris // 400
+    segs = 32
+    rings = max(1, per_col // (2 * segs))
+    for r in range(20):
+        for c in range(20):
+            cx = -9 + 18 * (c + 0.5) / 20
+            cz = -14 + 28 * (r + 0.5) / 20
+            v, t = _column(cx, cz, 0.18, 8.0, segs, rings)
+            parts.append((v, t, int(rng.integers(32))))
+    # walls, floor, ceiling: the rest, split by area into 4 x 4 patches each
+    faces = [((-10, 0, -15), (20, 0, 0), (0, 0, 30)), ((-10, 8, -15), (0, 0, 30), (20, 0, 0)),
+             ((-10, 0, -15), (0, 0, 30), (0, 8, 0)), ((10, 0, -15), (0, 8, 0), (0, 0, 30)),
+             ((-10, 0, -15), (0, 8, 0), (20, 0, 0)), ((-10, 0, 15), (20, 0, 0), (0, 8, 0))]
+    areas = [np.linalg.norm(np.cross(u, v)) for _, u, v in faces]
+    left = triangles - sum(len(p[1]) for p in parts)
+    for (corner, u, v), area in zip(faces, areas):
+        u, v, corner = np.array(u, float), np.array(v, float), np.array(corner, float)
+        n_face = left * area / sum(areas) / 2
+        lu, lv = np.linalg.norm(u), np.linalg.norm(v)
+        cell = np.sqrt(lu * lv / n_face)
+        nu, nv = max(4, int(lu / cell) // 4 * 4), max(4, int(lv / cell) // 4 * 4)
+        normal = np.cross(u, v) / np.linalg.norm(np.cross(u, v))
+        for pu in range(4):
+            for pv in range(4):
+                vv, tt = _grid(corner + pu / 4 * u + pv / 4 * v, u / 4, v / 4, nu // 4, nv // 4)
+                vv = vv + 0.06 * _fbm(vv, seed + 7)[:, None] * normal
+                parts.append((vv, tt, int(rng.integers(32))))
+    obj = os.path.join(directory, "room.obj")
+    with open(obj, "w") as f:
+        base = 1
+        for verts, _, _ in parts:
+            np.savetxt(f, verts, fmt="v %.5f %.5f %.5f")
+        for verts, tris, m in parts:
+            f.write(f"usemtl m{m}\n")
+            np.savetxt(f, tris + base, fmt="f %d %d %d")
+            base += len(verts)
+    lines = [f"image_width {width}", f"aspect_ratio {width}/{height}", f"samples_per_pixel {spp}",
+             f"max_depth {depth}", "background 0 0 0",
+             "camera lookfrom 0 3.2 -13.5  lookat 0 2.6 0  vup 0 1 0  vfov 60"]
+    for m in range(32):
+        col = rng.uniform(0.1, 0.9, 3)
+        rough = rng.uniform(0.05, 1.0)
+        metal = int(rng.integers(2))
+        lines.append(f"material m{m} principled color {col[0]:.4f} {col[1]:.4f} {col[2]:.4f} "
+                     f"roughness {rough:.4f} metallic {metal}")
+    for k in range(16):
+        e = rng.lognormal(2.0, 1.0)
+        tint = rng.uniform(0.7, 1.0, 3)
+        lines.append(f"material lamp{k} emissive {e * tint[0]:.4f} {e * tint[1]:.4f} {e * tint[2]:.4f}")
+        x = -8 + 16 * ((k % 4) + 0.5) / 4
+        z = -12 + 24 * ((k // 4) + 0.5) / 4
+        lines.append(f"quad {x - 0.6:.3f} 7.95 {z - 0.6:.3f}  1.2 0 0  0 0 1.2  lamp{k}")
+    lines.append("mesh room.obj m0")
+    path = os.path.join(directory, "triangle_room.scene")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
     return path

@@ -17,9 +17,11 @@
 //                                      batch means of camera::render (mean and variance of the mean)
 //   denoise <w> <h> <seed> <out>      denoiser::run on a seeded frame
 //   post   <w> <h> <seed> <out>       postprocess + display_settings::apply + to_byte on a seeded image
+//   sky    <w> <h> <out>              atmosphere::bake and sun_transmittance for four suns and settings
 #include <bvh.h>
 #include <denoiser.h>
 #include <scene.h>
+#include <atmosphere.h>
 #include <tonemap.h>
 
 #include <chrono>
@@ -422,6 +424,35 @@ int cmd_post(int argc, char** argv) {
     return 0;
 }
 
+// Four (settings, sun) cases: the default air at a high, a low and a set sun,
+// and a hazier, ozone-free air; per case the bake then the transmittance.
+int cmd_sky(int argc, char** argv) {
+    if (argc < 5)
+        return 2;
+    int w = std::atoi(argv[2]), h = std::atoi(argv[3]);
+    Out o(argv[4]);
+    struct Case {
+        double el, az, e, rayleigh, mie, g, ozone, intensity;
+    } cases[4] = {{40, 160, 1000, 1, 1, 0.8, 1, 3}, {5, 60, 4, 1, 1, 0.8, 1, 3}, {-2, 250, 10, 1, 1, 0.8, 1, 3},
+                  {25, 300, 3, 1.5, 4, 0.9, 0, 2}};
+    for (const auto& c : cases) {
+        atmosphere_settings s;
+        s.rayleigh = c.rayleigh;
+        s.mie = c.mie;
+        s.mie_g = c.g;
+        s.ozone = c.ozone;
+        s.intensity = c.intensity;
+        atmosphere air(s);
+        double el = degrees_to_radians(c.el), az = degrees_to_radians(c.az);
+        vec3 dir(std::cos(el) * std::sin(az), std::sin(el), -std::cos(el) * std::cos(az));
+        color irr(c.e, 0.9 * c.e, 0.8 * c.e);
+        for (const auto& p : air.bake(w, h, dir, irr))
+            o.put(p);
+        o.put(air.sun_transmittance(dir));
+    }
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -439,6 +470,7 @@ int main(int argc, char** argv) {
     else if (c == "render") rc = cmd_render(argc, argv);
     else if (c == "denoise") rc = cmd_denoise(argc, argv);
     else if (c == "post") rc = cmd_post(argc, argv);
+    else if (c == "sky") rc = cmd_sky(argc, argv);
     if (rc == 2)
         std::cerr << "bad arguments for '" << c << "'\n";
     return rc;

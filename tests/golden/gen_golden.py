@@ -229,6 +229,7 @@ RENDERS = [
     ("fog_box.scene", 48, 64, 16),
     ("materials.scene", 64, 64, 16),
     ("voxels.scene", 48, 64, 16),
+    ("voxels_style.scene", 48, 64, 16),
 ]
 
 
@@ -270,8 +271,25 @@ def gen_post():
                         rgb8=rest[:, 1].astype(np.uint8), settings=np.array(POST_SETTINGS))
 
 
+# (elevation, azimuth, irradiance, rayleigh, mie, mie_g, ozone, intensity) of ref_harness sky
+SKY_CASES = [(40, 160, 1000, 1, 1, 0.8, 1, 3), (5, 60, 4, 1, 1, 0.8, 1, 3), (-2, 250, 10, 1, 1, 0.8, 1, 3),
+             (25, 300, 3, 1.5, 4, 0.9, 0, 2)]
+
+
+def gen_sky():
+    w, h = 64, 32
+    raw = run("sky", w, h).reshape(len(SKY_CASES), -1)
+    np.savez_compressed(os.path.join(HERE, "sky.npz"), bake=raw[:, :-3].reshape(len(SKY_CASES), h, w, 3),
+                        sun_transmittance=raw[:, -3:], cases=np.array(SKY_CASES, dtype=float))
+    recs = run("lights", scene("voxels_style.scene"), 1500, 31)
+    n = int(recs[0])
+    np.savez_compressed(os.path.join(HERE, "lights_style.npz"), probability=recs[1:1 + n],
+                        origin=recs[1 + n:].reshape(-1, 7)[:, 0:3], dir=recs[1 + n:].reshape(-1, 7)[:, 3:6],
+                        pdf=recs[1 + n:].reshape(-1, 7)[:, 6])
+
+
 GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_env, "ggx": gen_ggx,
-          "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post}
+          "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post, "sky": gen_sky}
 
 if __name__ == "__main__":
     ref = os.environ.get("REFERENCE", "/root/reference")

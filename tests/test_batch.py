@@ -1,0 +1,88 @@
+"""Batched renders, graph replay and the autotuner: they change how the work
+is launched, never the result. Random numbers are keyed by (seed, pixel,
+pass, bounce), so every arrangement renders the same samples; only the order
+of the FP64 film additions differs (relative differences ~1e-15)."""
+import numpy as np
+import pytest
+
+import mypbr_gb300 as mp
+from conftest import scene_path
+
+pytestmark = pytest.mark.gpu
+
+
+def camera_of(sc, width, spp, seed=3, depth=None):
+    cam = sc.camera
+    cam.image_width = width
+    cam.samples_per_pixel = spp
+    cam.seed = seed
+    if depth:
+        cam.max_depth = depth
+    return cam
+
+
+def test_graph_replay_matches_direct_launches():
+    sc = mp.load_scene(scene_path("cornell_c1.scene"))
+    G = mp.GpuScene(sc)
+    cam = camera_of(sc, 48, 64)
+    cam.samples_per_wave = 4  # many waves: the graph is replayed 16 times
+    graphed = cam.render(G).radiance
+    cam.timing = 1  # per-kernel events: direct launches
+    direct, _, _ = mp.render_ex(cam, G)
+    np.testing.assert_allclose(graphed, direct, rtol=1e-12, atol=1e-14)
+
+
+def test_batch_matches_single_renders():
+    torch = pytest.importorskip("torch")
+    names = ["cornell_c1", "materials", "voxels", "env_spheres"]
+    setups = []
+    for k, name in enumerate(names):
+        sc = mp.load_scene(scene_path(f"{name}.scene"))
+        G = mp.GpuScene(sc)
+        setups.append((sc, G, camera_of(sc, 32 + 8 * k, 16 * (k + 1), seed=10 + k)))
+    # two more jobs on the first scene handle (run after its first, in order)
+    extra = [camera_of(mp.load_scene(scene_path("cornell_c1.scene")), 40, 8, seed=99),
+             camera_of(mp.load_scene(scene_path("cornell_c1.scene")), 24, 32, seed=98)]
+    jobs, bufs, expect = [], [], []
+    for sc, G, cam in setups:
+        h = cam.height()
+        buf = torch.zeros((h, cam.image_width, 3), dtype=torch.float64, device="cuda")
+        bufs.append(buf)
+        jobs.append((G, cam, buf.data_ptr()))
+        expect.append(cam.render(G).radiance)
+    for cam in extra:
+        G = setups[0][1]
+        buf = torch.zeros((cam.height(), cam.image_width, 3), dtype=torch.float64, device="cuda")
+        bufs.append(buf)
+        jobs.append((G, cam, buf.data_ptr()))
+        expect.append(cam.render(G).radiance)
+    codes = mp.render_batch(jobs)
+    assert codes == [0] * len(jobs)
+    torch.cuda.synchronize()
+    for buf, ref in zip(bufs, expect):
+        np.testing.assert_allclose(buf.cpu().numpy(), ref, rtol=1e-12, atol=1e-14)
+
+
+def test_batch_reports_a_bad_job():
+    torch = pytest.importorskip("torch")
+    sc = mp.load_scene(scene_path("cornell_c1.scene"))
+    G = mp.GpuScene(sc)
+    good = camera_of(sc, 16, 4)
+    bad = camera_of(mp.load_scene(scene_path("cornell_c1.scene")), 16, 4)
+    bad.max_depth = 0
+    b1 = torch.zeros((good.height(), 16, 3), dtype=torch.float64, device="cuda")
+    b2 = torch.zeros((bad.height(), 16, 3), dtype=torch.float64, device="cuda")
+    with pytest.raises(mp.MypbrError):
+        mp.render_batch([(G, good, b1.data_ptr()), (G, bad, b2.data_ptr())])
+
+
+def test_autotune_keeps_the_result():
+    sc = mp.load_scene(scene_path("materials.scene"))
+    G = mp.GpuScene(sc)
+    cam = camera_of(sc, 64, 32)
+    before = cam.render(G).radiance
+    r = mp.autotune(cam, G)
+    assert r["block"] in (128, 256) and r["wave_paths"] in (4 << 20, 8 << 20, 16 << 20, 32 << 20)
+    assert all(t > 0 for t in r["trials"]) and r["mpaths_per_s"] == max(r["trials"])
+    after = cam.render(G).radiance
+    np.testing.assert_allclose(after, before, rtol=1e-12, atol=1e-14)

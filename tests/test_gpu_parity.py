@@ -219,7 +219,7 @@ def render_gpu(name, width, spp, seed=7):
     return rad, chv
 
 
-@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels"])
+@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style"])
 def test_render_matches_reference(name):
     g = load_golden(f"render_{name}")
     rad, var = render_gpu(name, g["mean"].shape[1], 1024)

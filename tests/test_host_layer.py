@@ -63,7 +63,7 @@ def test_scene_errors_name_the_line():
 
 def test_unsupported_features_are_reported():
     expect_error("vox island.vox\n", 7, "cannot open")
-    expect_error("sphere 0 0 0 1\nsky atmosphere\n", 2, "'sky atmosphere' is not supported")
+    expect_error("sphere 0 0 0 1\nsky atmosphere mie_g 1.5\n", 7, "expected 'sky atmosphere")
     expect_error("mesh car.glb\n", 2, "glTF meshes are not read")
 
 
