@@ -19,6 +19,7 @@ mypbr_gpu_render (renders, copies the FP64 frame back) + destroy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--spp S]
   python bench.py --workload voxel_hall [--hall-width 480] [--ref-spp 65536]
+  python bench.py --workload cornell | triangle_room | batch
 
 voxel_hall: the 512^3 voxel world lit through six slits (workloads.py),
 rendered at --hall-width x 9/16 with max depth 16. relMSE = mean over pixels
@@ -58,7 +59,8 @@ UNIT = "Mpaths/s"
 
 # ------------------------------------------------------------ the workload
 
-from mypbr_gb300.workloads import sphere_field_scene, voxel_hall_scene  # noqa: E402
+from mypbr_gb300.workloads import (batch_scenes, cornell_scene, sphere_field_scene,  # noqa: E402
+                                   triangle_room_scene, voxel_hall_scene)
 
 
 WORKLOAD = {"workload": "sphere_field_1000_hdri", "width": WIDTH, "height": HEIGHT, "spp": 256, "max_depth": 16,
@@ -412,6 +414,109 @@ def run_voxel_hall(args):
     print(json.dumps(line), flush=True)
 
 
+def render_rate(mp, scene, spp, steps, warmup, guided=0):
+    """Device-resident Mpaths/s of a scene (CUDA events around the render on
+    the scene handle's stream is what mypbr_gpu_render_ex times)."""
+    cam = scene.camera
+    cam.samples_per_pixel = spp
+    cam.guided = guided
+    G = mp.GpuScene(scene)
+    times = []
+    st = None
+    for k in range(warmup + steps):
+        cam.seed = 100 + k
+        t0 = time.perf_counter()
+        img, _, st = mp.render_ex(cam, G)
+        if k >= warmup:
+            times.append(time.perf_counter() - t0)
+    G.close()
+    t = statistics.median(times)
+    return st["paths"] / t / 1e6, t, st
+
+
+def run_simple(args, workload):
+    """C1 (Cornell box, 256^2, 64 spp, depth 50) or C3 (the 2M-triangle room,
+    1080p, 64 spp, depth 12): Mpaths/s, timed around mypbr_gpu_render_ex
+    (scene resident, FP64 frame copied back), and the CPU oracle beside it."""
+    import mypbr_gb300 as mp
+    with tempfile.TemporaryDirectory() as d:
+        if workload == "cornell":
+            scene = mp.load_scene(cornell_scene(d))
+            spp, cfg = 64, {"workload": "cornell_box_c1", "width": 256, "height": 256, "spp": 64, "max_depth": 50}
+        else:
+            scene = mp.load_scene(triangle_room_scene(d))
+            spp, cfg = 64, {"workload": "triangle_room_2m", "width": 1920, "height": 1080, "spp": 64,
+                            "max_depth": 12, "triangles": 1985856, "materials": "32 principled", "lights": 16}
+    value, t, st = render_rate(mp, scene, spp, args.steps, args.warmup)
+    line = {"metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "dtype": "fp32",
+            "data": "synthetic", "config": cfg,
+            "rays": {"extension_per_path": st["extension_rays"] / st["paths"],
+                     "shadow_per_path": st["shadow_rays"] / st["paths"],
+                     "mrays_per_s": (st["extension_rays"] + st["shadow_rays"]) / t / 1e6}}
+    if workload == "triangle_room" and args.hidden:
+        gv, gt, _ = render_rate(mp, scene, spp, max(1, args.steps // 2), 1, guided=args.hidden)
+        line["guided"] = {"value": gv, "ms_per_step": gt * 1e3, "hidden_layers": args.hidden,
+                          "note": "untrained network at the first render; later renders train further"}
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        h = scene.camera.height()
+        rows = max(1, min(h, int(h * 0.02))) if workload == "triangle_room" else h
+        t_cpu, ex = oracle_render_timed(scene, spp, threads, rows=(h // 2 - rows // 2, rows))
+        line["cpu_baseline"] = {"value": ex["paths"] / t_cpu / 1e6, "unit": "Mpaths/s", "cores": threads,
+                                "kind": "port", "sample": f"{rows} rows at {spp} spp ({ex['paths']} paths, {t_cpu:.1f} s)"}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args):
+    """C4: 64 scenes of uneven size, resolution and spp (half of them with a
+    haze medium) rendered by one mypbr_gpu_render_batch call, then each frame
+    denoised (5 iterations) on the device. Aggregate Mpaths/s over the batch."""
+    import torch
+
+    import mypbr_gb300 as mp
+    d = tempfile.mkdtemp()
+    items = batch_scenes(d, count=args.batch_count)
+    scenes, cams, bufs = [], [], []
+    for path, width, spp in items:
+        sc = mp.load_scene(path)
+        G = mp.GpuScene(sc)
+        cam = sc.camera
+        cam.samples_per_pixel = spp
+        cam.collect_features = 0
+        # about 2M paths in flight per job: 64 handles' path buffers stay near 30 GB
+        cam.samples_per_wave = max(1, (2 << 20) // (cam.height() * cam.image_width))
+        scenes.append((sc, G))
+        cams.append(cam)
+        bufs.append(torch.zeros((cam.height(), cam.image_width, 3), dtype=torch.float64, device="cuda"))
+    jobs = [(G, cam, b.data_ptr()) for (sc, G), cam, b in zip(scenes, cams, bufs)]
+    paths = sum(c.height() * c.image_width * c.samples_per_pixel for c in cams)
+    mp.render_batch(jobs)  # warm-up: buffers, graphs
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        mp.render_batch(jobs)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    # one by one, for the batch's gain
+    t0 = time.perf_counter()
+    for (sc, G), cam, b in zip(scenes, cams, bufs):
+        mp.render_batch([(G, cam, b.data_ptr())])
+    torch.cuda.synchronize()
+    t_serial = time.perf_counter() - t0
+    line = {"metric": "Mpaths/s over a batch of 64 scenes", "value": paths / t / 1e6, "unit": "Mpaths/s",
+            "n_gpus": 1, "steps": args.steps, "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
+            "ms_per_step": t * 1e3,
+            "config": {"workload": "batch_64", "scenes": len(items), "paths": int(paths),
+                       "triangles": "10k..1M log-uniform (a third of the scenes)",
+                       "resolutions": "64^2..1024^2 log-uniform", "spp": "16..1024 log-uniform",
+                       "media": "every other scene: fog 0.02, albedo 0.9, g 0.6"},
+            "one_by_one_ms": t_serial * 1e3, "batch_speedup": t_serial / t}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -423,15 +528,24 @@ def main():
     p.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
     p.add_argument("--reference-budget", type=float, default=8.0, help="seconds per reference step")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["sphere_field", "voxel_hall"], default="sphere_field")
+    p.add_argument("--workload", choices=["sphere_field", "voxel_hall", "cornell", "triangle_room", "batch"],
+                   default="sphere_field")
+    p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--ref-spp", type=int, default=65536)
     p.add_argument("--max-spp", type=int, default=16384)
     p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
     args = p.parse_args()
-    if args.workload == "voxel_hall":
+    if args.workload != "sphere_field":
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if args.workload == "voxel_hall":
         run_voxel_hall(args)
+        return
+    if args.workload in ("cornell", "triangle_room"):
+        run_simple(args, args.workload)
+        return
+    if args.workload == "batch":
+        run_batch(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

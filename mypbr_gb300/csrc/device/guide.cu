@@ -627,8 +627,8 @@ int mypbr_guide_test_forward(int hidden, const float* weights, const float* inpu
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         long long tiles = (n + 127) / 128;
-        int grid = int(std::min<long long>(std::max<long long>(tiles, 1), 2LL * sms));
-        k<<<grid, 128, smem>>>(view_of(T.g, T.err), GivenSource{d_in, nullptr}, RowSink{d_out}, n);
+        int grid = int(std::min<long long>(std::max<long long>((tiles + kGuideGroups - 1) / kGuideGroups, 1), sms));
+        k<<<grid, 128 * kGuideGroups, smem>>>(view_of(T.g, T.err), GivenSource{d_in, nullptr}, RowSink{d_out}, n);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess)
             rc = cuda_fail(e, "k_guide_forward");

@@ -4,8 +4,9 @@
 // BSDF (one-sample MIS with probability alpha) and next-event estimation, so
 // the estimator stays unbiased whatever the network has learned.
 //
-// Network: input one-blob encoding (7 scalars in [0, 1] x 16 Gaussian bins =
-// 112, a constant 1 as bias, zero padding to 128) -> `hidden` layers of 64
+// Network: input one-blob encoding (7 scalars in [0, 1]: position 3 x 32
+// Gaussian bins, normal and outgoing direction angles 4 x 6; a constant 1 as
+// bias, zero padding to 128) -> `hidden` layers of 64
 // ReLU units -> 64 outputs, of which 40 are used: per lobe (mu_x, mu_y, mu_z,
 // log kappa, logit). BF16 weights and activations, FP32 accumulation on the
 // tensor cores (tcgen05.mma, accumulators in TMEM).
@@ -32,7 +33,6 @@ constexpr int kGuideWidth = 64;
 constexpr int kGuideOut = 64;
 constexpr int kGuideLobes = 8;
 constexpr int kGuideUsed = 5 * kGuideLobes;  // raw outputs in use
-constexpr int kGuideBins = 16;
 constexpr int kGuideScalars = 7;
 constexpr int kGuideMaxHidden = 8;
 constexpr int kGuideRecordDepth = 4;  // vertices of a path recorded for training
@@ -60,17 +60,28 @@ MYPBR_DEV void guide_scalars(float3 p, float3 n, float3 wo, float3 box_lo, float
     s[6] = (atan2f(wo.z, wo.x) + kPi) * (0.5f * kInvPi);
 }
 
-// One-blob value of bin b for scalar s: a Gaussian of width 1/16 centred on the bin.
-MYPBR_DEV float one_blob(float s, int b) {
-    float x = (s - (float(b) + 0.5f) * (1.0f / kGuideBins)) * float(kGuideBins);
+// One-blob encoding (Mueller et al., "Neural Importance Sampling", 2019):
+// scalar i gets guide_bins_of(i) bins, each a Gaussian of width one bin centred
+// on it. Position gets the finer grid (32 bins per axis), the four angles 6
+// bins each; then a constant 1 (the first layer's bias) and zero padding:
+// 3 x 32 + 4 x 6 + 1 = 121 of the 128 inputs.
+MYPBR_HD constexpr int guide_bins_of(int i) { return i < 3 ? 32 : 6; }
+MYPBR_HD constexpr int guide_first_bin(int i) { return i < 3 ? 32 * i : 96 + 6 * (i - 3); }
+constexpr int kGuideEncoded = 3 * 32 + 4 * 6;  // 120 one-blob features
+
+MYPBR_DEV float one_blob(float s, int b, int bins) {
+    float x = (s - (float(b) + 0.5f) / float(bins)) * float(bins);
     return __expf(-0.5f * x * x);
 }
 
 // Input feature k (0..127) of the encoded vertex.
 MYPBR_DEV float guide_feature(const float s[7], int k) {
-    if (k < kGuideScalars * kGuideBins)
-        return one_blob(s[k / kGuideBins], k % kGuideBins);
-    return k == kGuideScalars * kGuideBins ? 1.0f : 0.0f;
+    if (k < kGuideEncoded) {
+        int i = k < 96 ? k / 32 : 3 + (k - 96) / 6;
+        int b = k - guide_first_bin(i);
+        return one_blob(s[i], b, guide_bins_of(i));
+    }
+    return k == kGuideEncoded ? 1.0f : 0.0f;
 }
 
 // ------------------------------------------------------------- mixture
@@ -327,56 +338,81 @@ struct GuideNetView {
     int* error;                    // sticky error word: 3 = a tensor-core wait timed out
 };
 
+// Tiles of 128 rows a forward CTA works on at once: one group of 4 warps
+// (128 threads, a thread per row) per tile, all groups sharing one copy of
+// the weights in shared memory and each with its own activation tile,
+// mbarrier and 64 TMEM columns, synchronising with its own named barrier.
+constexpr int kGuideGroups = 4;
+
 // Shared memory of the forward kernel: every weight matrix, then one
-// 128 x 128 activation tile, then the barrier and the TMEM address.
+// 128 x 128 activation tile per group, then the barriers and the TMEM address.
 MYPBR_HD size_t guide_forward_smem(int hidden) {
-    return size_t(guide_params(hidden)) * 2 + size_t(128 * kGuideIn) * 2 + 64;
+    return size_t(guide_params(hidden)) * 2 + size_t(kGuideGroups) * 128 * kGuideIn * 2 + 64;
 }
 
-// Batched MLP forward on the tensor cores: each CTA (128 threads, one per
-// row) walks tiles of 128 rows. Src::count(rows) gives the number of rows
-// (it may read a device counter); Src::fill(i, tile, row) writes the encoded
-// input row (BF16, canonical, K = 128), i = -1 for padding rows;
-// Sink::put(i, v) takes the 64 FP32 outputs of row i.
+namespace tc {
+// Named barrier of `count` threads; returns whether any thread passed `pred`.
+MYPBR_DEV bool group_sync_or(int id, int count, bool pred) {
+    uint32_t out;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(out)
+        : "r"(uint32_t(pred)), "r"(id), "r"(count)
+        : "memory");
+    return out != 0;
+}
+MYPBR_DEV void group_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+}  // namespace tc
+
+// Batched MLP forward on the tensor cores: each CTA (kGuideGroups groups of
+// 128 threads, one thread per row) walks tiles of 128 rows, a tile per group
+// at a time. Src::count(rows) gives the number of rows (it may read a device
+// counter); Src::fill(i, tile, row) writes the encoded input row (BF16,
+// canonical, K = 128), i = -1 for padding rows; Sink::put(i, v) takes the 64
+// FP32 outputs of row i.
 template <class Src, class Sink>
-__global__ void __launch_bounds__(128) k_guide_forward(GuideNetView net, Src src, Sink sink, long long rows) {
+__global__ void __launch_bounds__(128 * kGuideGroups) k_guide_forward(GuideNetView net, Src src, Sink sink,
+                                                                      long long rows) {
     extern __shared__ __align__(1024) uint8_t smem[];
     rows = src.count(rows);
-    long long tiles = (rows + 127) / 128;
-    if (blockIdx.x >= tiles)
+    const long long tiles = (rows + 127) / 128;
+    if ((long long)blockIdx.x * kGuideGroups >= tiles)
         return;  // no tile for this CTA: nothing loaded, nothing allocated
-    int P = guide_params(net.hidden);
+    const int P = guide_params(net.hidden);
+    const int group = threadIdx.x >> 7, row = threadIdx.x & 127, warp = threadIdx.x >> 5;
     __nv_bfloat16* W = reinterpret_cast<__nv_bfloat16*>(smem);
-    __nv_bfloat16* A = W + P;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(A + 128 * kGuideIn);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
-    int row = threadIdx.x, warp = threadIdx.x >> 5;
-    // the weights stay resident for every tile this CTA handles
-    {
+    __nv_bfloat16* A = W + P + size_t(group) * 128 * kGuideIn;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(W + P + size_t(kGuideGroups) * 128 * kGuideIn);
+    uint64_t* bar = bars + group;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kGuideGroups);
+    {  // the weights stay resident for every tile this CTA handles
         const uint4* g = reinterpret_cast<const uint4*>(net.w);
         uint4* s = reinterpret_cast<uint4*>(W);
         for (int k = threadIdx.x; k < P / 8; k += blockDim.x)
             s[k] = g[k];
     }
     if (warp == 0)
-        tc::tmem_alloc(tmem_slot, 64);
-    if (threadIdx.x == 0)
+        tc::tmem_alloc(tmem_slot, 64 * kGuideGroups);
+    if (row == 0)
         tc::bar_init(bar, 1);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    uint32_t tmem = *tmem_slot;
+    const uint32_t tmem = *tmem_slot + uint32_t(64 * group);
+    const int bar_id = 1 + group;  // named barrier 0 is __syncthreads
     uint32_t phase = 0;
     const uint32_t idesc = tc::idesc_bf16(128, 64);
     bool failed = false;
-    for (long long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+    for (long long tile = (long long)blockIdx.x * kGuideGroups + group; tile < tiles && !failed;
+         tile += (long long)gridDim.x * kGuideGroups) {
         long long i = tile * 128 + row;
         src.fill(i < rows ? i : -1, A, row);
         for (int l = 0; l <= net.hidden; l++) {
             int K = guide_in(l);
             tc::fence_smem();
-            __syncthreads();
-            if (threadIdx.x == 0) {
+            tc::group_sync(bar_id, 128);
+            if (row == 0) {
                 tc::fence_after();
                 uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(W + guide_offset(l));
                 for (int s = 0; s < K / 16; s++)
@@ -386,8 +422,8 @@ __global__ void __launch_bounds__(128) k_guide_forward(GuideNetView net, Src src
             }
             bool ok = tc::bar_wait(bar, phase);
             phase ^= 1;
-            if (__syncthreads_or(!ok)) {
-                if (threadIdx.x == 0)
+            if (tc::group_sync_or(bar_id, 128, !ok)) {
+                if (row == 0)
                     atomicCAS(net.error, 0, 3);
                 tc::bar_wait(bar, phase ^ 1);  // once more, bounded, for the MMAs in flight
                 failed = true;
@@ -411,7 +447,7 @@ __global__ void __launch_bounds__(128) k_guide_forward(GuideNetView net, Src src
     __syncthreads();
     if (warp == 0) {
         tc::fence_after();
-        tc::tmem_free(tmem, 64);
+        tc::tmem_free(*tmem_slot, 64 * kGuideGroups);
     }
 }
 

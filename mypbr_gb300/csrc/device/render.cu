@@ -267,7 +267,7 @@ MYPBR_DEV int hit_material(const DeviceScene& S, const HitInfo& h) {
 
 // Closest hits of the extension queue; each ray then joins its shading class's queue.
 template <bool VOX>
-__global__ void __launch_bounds__(256) k_extend(WaveParams P, int depth) {
+__global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
     uint32_t n = *ext_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
         atomicAdd(&P.totals[0], (unsigned long long)n);
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
 }
 
 template <bool VOX>
-__global__ void __launch_bounds__(256) k_shadow(WaveParams P, int depth) {
+__global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
     uint32_t n = *sh_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
         atomicAdd(&P.totals[1], (unsigned long long)n);
@@ -910,7 +910,7 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
         else
             TIMED(1, (k_extend<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         if (P.guided) {  // the mixtures of this bounce's guidable vertices
-            TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128, L.guide_smem, st>>>(
+            TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
                          L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
             launches++;
         }
@@ -1014,8 +1014,9 @@ struct RenderSetup {
 // Guided renders: the first waves are small and recorded, each followed by
 // Adam steps on their vertices; later waves keep training online, lightly.
 constexpr int kGuideTrainWaves = 8;
-constexpr int kGuideStepsEarly = 24, kGuideStepsLate = 4;
-constexpr int kGuideMinSteps = 24;    // steps before the mixture is sampled at all
+constexpr int kGuideStepsEarly = 16, kGuideStepsLate = 4;
+constexpr int kGuideMinSteps = 16;    // steps before the mixture is sampled at all
+constexpr int kGuideBatchTilesPerSm = 2;  // 128-sample tiles per SM in one step (39K samples on 152 SMs)
 constexpr int kGuideMaxSteps = 1500;  // no recording or training past this
 constexpr float kGuideAlpha = 0.5f, kGuideLr = 4e-3f;
 
@@ -1094,7 +1095,7 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
         auto k = k_guide_forward<GuideQueueSource, GuidePackSink>;
         MYPBR_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(R.L.guide_smem)));
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, R.L.guide_smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128 * kGuideGroups, R.L.guide_smem);
         R.L.grid_guide = G->sm_count * std::max(per_sm, 1);
         R.L.guided_kernels = true;
     }
@@ -1126,7 +1127,8 @@ int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int sav
     if (R.guided && P.record) {
         if ((s = T.begin(4)) != MYPBR_OK)
             return s;
-        s = guide_train(G, train_wave ? kGuideStepsEarly : kGuideStepsLate, 4 * G->sm_count, kGuideLr, st);
+        s = guide_train(G, train_wave ? kGuideStepsEarly : kGuideStepsLate, kGuideBatchTilesPerSm * G->sm_count,
+                        kGuideLr, st);
         if (s != MYPBR_OK || (s = T.end()) != MYPBR_OK)
             return s;
         launches += 3 * (train_wave ? kGuideStepsEarly : kGuideStepsLate);

@@ -402,3 +402,54 @@ def triangle_room_scene(directory, triangles=2_000_000, seed=3, spp=64, width=19
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
     return path
+
+
+# ------------------------------------------------------------ Cornell box
+
+def cornell_scene(directory, width=256, spp=64, depth=50):
+    """The plain Cornell box: room 0..555, red / green side walls, a 130 x 105
+    light of emission 15 at y = 554, two white boxes turned about y."""
+    lines = [f"image_width {width}", "aspect_ratio 1", f"samples_per_pixel {spp}", f"max_depth {depth}",
+             "background 0 0 0", "camera lookfrom 278 278 -800  lookat 278 278 0  vup 0 1 0  vfov 40",
+             "material red lambertian 0.65 0.05 0.05", "material white lambertian 0.73 0.73 0.73",
+             "material green lambertian 0.12 0.45 0.15", "material lamp emissive 15 15 15",
+             "quad 555 0 0  0 555 0  0 0 555  green", "quad 0 0 0  0 555 0  0 0 555  red",
+             "quad 343 554 332  -130 0 0  0 0 -105  lamp", "quad 0 0 0  555 0 0  0 0 555  white",
+             "quad 555 555 555  -555 0 0  0 0 -555  white", "quad 0 0 555  555 0 0  0 555 0  white",
+             "box 0 0 0  165 330 165  white  rotate_y 15  translate 265 0 295",
+             "box 0 0 0  165 165 165  white  rotate_y -18  translate 130 0 65"]
+    path = os.path.join(directory, "cornell.scene")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return path
+
+
+# ------------------------------------------------------------ a batch of scenes
+
+def batch_scenes(directory, count=64, seed=4):
+    """`count` scenes from the generators above with uneven sizes: triangle
+    rooms of log-uniform 10k..1M triangles, Cornell boxes and sphere fields;
+    resolutions log-uniform 64^2..1024^2 (square), spp log-uniform 16..1024;
+    every other scene filled with a haze medium (density 0.02, albedo 0.9,
+    g 0.6). Returns [(path, width, spp)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        sub = os.path.join(directory, f"s{k:02d}")
+        os.makedirs(sub, exist_ok=True)
+        width = int(round(np.exp(rng.uniform(np.log(64), np.log(1024)))))
+        spp = int(round(np.exp(rng.uniform(np.log(16), np.log(1024)))))
+        kind = k % 3
+        if kind == 0:
+            tris = int(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
+            path = triangle_room_scene(sub, triangles=tris, seed=seed + k, spp=spp, width=width, height=width,
+                                       depth=12)
+        elif kind == 1:
+            path = cornell_scene(sub, width=width, spp=spp)
+        else:
+            path = sphere_field_scene(sub, seed=seed + k, spp=spp, width=width, height=width)
+        if k % 2 == 1:
+            with open(path, "a") as f:
+                f.write("material haze volume 0.9 0.9 0.9 g 0.6\nfog 0.02 haze\n")
+        out.append((path, width, spp))
+    return out

@@ -11,7 +11,7 @@ tensor cores read them; sums are exact (FP64) here and FP32 on the device.
 """
 import numpy as np
 
-IN, WIDTH, OUT, LOBES, BINS = 128, 64, 64, 8, 16
+IN, WIDTH, OUT, LOBES = 128, 64, 64, 8
 LOG_KAPPA_MIN, LOG_KAPPA_MAX = -4.0, 9.0
 
 
@@ -65,15 +65,22 @@ def backward(weights, hidden, x, dout, rounding=True):
     return np.concatenate([g.ravel() for g in grads])
 
 
+BINS_OF = [32, 32, 32, 6, 6, 6, 6]  # position axes, then normal and outgoing angles
+
+
 def one_blob(s):
-    """Encoded inputs (n, 128) of scalars s (n, 7) in [0, 1]."""
+    """Encoded inputs (n, 128) of scalars s (n, 7) in [0, 1]: each scalar's
+    Gaussian bins one after another, then a constant 1, then zeros."""
     s = np.asarray(s, dtype=np.float64)
-    centres = (np.arange(BINS) + 0.5) / BINS
-    x = (s[:, :, None] - centres[None, None, :]) * BINS
-    enc = np.exp(-0.5 * x * x).reshape(len(s), 7 * BINS)
+    parts = []
+    for i, bins in enumerate(BINS_OF):
+        centres = (np.arange(bins) + 0.5) / bins
+        x = (s[:, i:i + 1] - centres[None, :]) * bins
+        parts.append(np.exp(-0.5 * x * x))
+    enc = np.concatenate(parts, axis=1)
     out = np.zeros((len(s), IN))
-    out[:, :7 * BINS] = enc
-    out[:, 7 * BINS] = 1.0
+    out[:, :enc.shape[1]] = enc
+    out[:, enc.shape[1]] = 1.0
     return out
 
 
