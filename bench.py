@@ -20,6 +20,8 @@ mypbr_gpu_render (renders, copies the FP64 frame back) + destroy.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--spp S]
   python bench.py --workload voxel_hall [--hall-width 480] [--ref-spp 65536]
   python bench.py --workload cornell | triangle_room | batch
+  python bench.py --workload hall_render [--hall-size 128] [--hall-width 256] [--spp 96] [--hidden 8]
+                  [--per-wave 8]      (one render; the profiling case of the guiding kernels)
 
 voxel_hall: the 512^3 voxel world lit through six slits (workloads.py),
 rendered at --hall-width x 9/16 with max depth 16. relMSE = mean over pixels
@@ -364,17 +366,18 @@ def run_voxel_hall(args):
         img, _, _ = mp.render_ex(cam, gs)
         return img, time.perf_counter() - t0
 
-    render(G, 16, 0, 7)  # warm-up
+    render(G, 16, 0, 7)  # warm-up: path buffers
     ref, t_ref = render(G, args.ref_spp, 0, 12345)
+    Gg = mp.GpuScene(scene)
+    render(Gg, 64, args.hidden, 7)  # warm-up: guiding buffers and network
     curves = {}
     for name, guided in (("plain", 0), ("guided", args.hidden)):
         pts = []
         spp = 16
         while spp <= args.max_spp:
-            gs = mp.GpuScene(scene) if guided else G  # guided: an untrained network every time
-            img, t = render(gs, spp, guided, 1 + spp)
-            if guided:
-                gs.close()
+            if guided:  # an untrained network every time: training is inside each timing
+                mp.guide_reset(Gg)
+            img, t = render(Gg if guided else G, spp, guided, 1 + spp)
             e = rel_mse(img, ref)
             pts.append((spp, t, e))
             print(f"{name} spp {spp}: {t:.3f} s relMSE {e:.5f}", file=sys.stderr, flush=True)
@@ -517,6 +520,31 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_hall_render(args):
+    """One render of the voxel hall (the case the profiles of the guiding
+    kernels are taken on): --hall-size cells a side, --hall-width pixels
+    wide (9:16), --spp samples, --hidden layers (0: plain), --per-wave passes
+    per wave (0: automatic)."""
+    import mypbr_gb300 as mp
+    with tempfile.TemporaryDirectory() as d:
+        w = args.hall_width
+        scene = mp.load_scene(voxel_hall_scene(d, size=args.hall_size, width=w, height=w * 9 // 16, spp=args.spp))
+    G = mp.GpuScene(scene)
+    cam = scene.camera
+    cam.samples_per_pixel = args.spp
+    cam.guided = args.hidden
+    cam.samples_per_wave = args.per_wave
+    cam.seed = 1
+    t0 = time.perf_counter()
+    img, _, st = mp.render_ex(cam, G)
+    t = time.perf_counter() - t0
+    print(json.dumps({"metric": "Mpaths/s", "value": st["paths"] / t / 1e6, "unit": "Mpaths/s", "seconds": t,
+                      "config": {"workload": f"voxel_hall_{args.hall_size}", "width": w, "height": w * 9 // 16,
+                                 "spp": args.spp, "guided_hidden_layers": args.hidden,
+                                 "samples_per_wave": args.per_wave},
+                      "mean_radiance": float(img.mean()), "stats": st}), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -528,8 +556,10 @@ def main():
     p.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
     p.add_argument("--reference-budget", type=float, default=8.0, help="seconds per reference step")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["sphere_field", "voxel_hall", "cornell", "triangle_room", "batch"],
-                   default="sphere_field")
+    p.add_argument("--workload", choices=["sphere_field", "voxel_hall", "cornell", "triangle_room", "batch",
+                                          "hall_render"], default="sphere_field")
+    p.add_argument("--hall-size", type=int, default=512)
+    p.add_argument("--per-wave", type=int, default=0)
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--ref-spp", type=int, default=65536)
@@ -546,6 +576,9 @@ def main():
         return
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "hall_render":
+        run_hall_render(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

@@ -634,6 +634,10 @@ int mypbr_write_image(const char* path, const double* radiance, int32_t width, i
  * row-major (in = 128 for the first, 64 after): 64*128 + hidden*64*64 values.
  * These entry points expose the kernels to the parity tests. Synchronous. */
 
+/* Puts the scene handle's guiding network back to its initial (untrained)
+ * weights, keeping its buffers: the next guided render starts from scratch. */
+int mypbr_guide_reset(mypbr_gpu_scene* scene);
+
 /* outputs (n x 64) of the network for encoded inputs (n x 128). */
 int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out);
 /* weight gradients (same layout as weights) of sum_i dout_i . out_i. */

@@ -150,6 +150,7 @@ def lib():
     L.mypbr_gpu_display.argtypes = [dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), dp,
                                     ctypes.POINTER(ctypes.c_uint8), ctypes.c_int]
     L.mypbr_write_image.argtypes = [ctypes.c_char_p, dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), ctypes.c_int]
+    L.mypbr_guide_reset.argtypes = [vp]
     L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
     L.mypbr_guide_test_backward.argtypes = [ctypes.c_int, fp, fp, fp, i64, fp]
     L.mypbr_guide_test_loss.argtypes = [fp, fp, fp, i64, fp, fp]
@@ -491,3 +492,8 @@ def sky_bake(sun_direction, sun_irradiance, width=256, height=128, rayleigh=1.0,
     check(lib().mypbr_sky_bake(ctypes.byref(s), d.ctypes.data_as(dp), e.ctypes.data_as(dp), width, height,
                                img.ctypes.data_as(dp), t.ctypes.data_as(dp), int(on_gpu)))
     return img, t
+
+
+def guide_reset(gpu_scene):
+    """The handle's guiding network back to its untrained weights (buffers kept)."""
+    check(lib().mypbr_guide_reset(gpu_scene.handle))

@@ -608,6 +608,27 @@ using namespace mypbr_dev;
 
 extern "C" {
 
+int mypbr_guide_reset(mypbr_gpu_scene* scene) {
+    if (!scene) {
+        set_error_message("mypbr_guide_reset: null scene");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    GuideState& g = scene->guide;
+    if (g.hidden == 0)
+        return MYPBR_OK;
+    std::vector<float> w0 = initial_weights(g.hidden, 0x9d2c5680ull);
+    size_t P = size_t(g.params);
+    MYPBR_CUDA(cudaMemcpy(g.master, w0.data(), P * 4, cudaMemcpyHostToDevice));
+    MYPBR_CUDA(cudaMemset(g.m, 0, P * 4));
+    MYPBR_CUDA(cudaMemset(g.v, 0, P * 4));
+    MYPBR_CUDA(cudaMemset(g.grad, 0, P * 4));
+    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
+    MYPBR_CUDA(cudaGetLastError());
+    MYPBR_CUDA(cudaDeviceSynchronize());
+    g.steps = 0;
+    return MYPBR_OK;
+}
+
 int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out) {
     if (!weights || !inputs || !out || n < 0)
         return MYPBR_ERR_INVALID_ARGUMENT;
