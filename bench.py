@@ -213,6 +213,7 @@ def run_ours(args):
     cam.samples_per_pixel = args.spp
     cam.seed = 1000 + rank  # independent samples per rank
     gpu = mp.GpuScene(scene)
+    mp.set_launch(gpu, block=args.block, traversal=args.traversal)
     L = mp.lib()
     c, o = cam.structs()
     w, h = c.image_width, c.image_height
@@ -278,6 +279,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         g2 = mp.GpuScene(scene)
+        mp.set_launch(g2, block=args.block, traversal=args.traversal)
         mp.check(L.mypbr_gpu_render(g2.handle, ctypes.byref(c), ctypes.byref(o), ctypes.c_void_p(host.ctypes.data),
                                     None, None, None, 0, mp.PASS_CALLBACK(), None))
         g2.close()
@@ -305,7 +307,8 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-                "config": dict(WORKLOAD, spp=args.spp, parallelism=f"samples x{world}"),
+                "config": dict(WORKLOAD, spp=args.spp, parallelism=f"samples x{world}", traversal=args.traversal,
+                               block=args.block or 256),
                 "gpu_launches": int(launches),
                 "rays": {"extension_per_path": totals["ext"] / (paths_per_step * args.steps),
                          "shadow_per_path": totals["sh"] / (paths_per_step * args.steps),
@@ -560,6 +563,9 @@ def main():
                                           "hall_render"], default="sphere_field")
     p.add_argument("--hall-size", type=int, default=512)
     p.add_argument("--per-wave", type=int, default=0)
+    p.add_argument("--traversal", type=int, default=0, choices=[0, 1],
+                   help="1: extend lanes take new rays as theirs finish")
+    p.add_argument("--block", type=int, default=0, choices=[0, 128, 256])
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--ref-spp", type=int, default=65536)

@@ -573,15 +573,21 @@ typedef struct mypbr_batch_job {
 int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n);
 
 /* The autotuner's choice for a scene handle and view: threads per block of
- * the bounce kernels and paths per wave, with the Mpaths/s of each of the 8
- * trials (block 128 then 256, each with 4M, 8M, 16M, 32M paths). */
+ * the bounce kernels, paths per wave and the traversal scheme (0: each lane
+ * walks its ray to the end; 1: lanes take new rays as theirs finish), with
+ * the Mpaths/s of each of the 16 trials (traversal 0 then 1; within each,
+ * block 128 then 256; within each, 4M, 8M, 16M, 32M paths). */
 typedef struct mypbr_tune_result {
     int32_t block;
-    int32_t reserved;
+    int32_t traversal;
     int64_t wave_paths;
     double mpaths_per_s;
-    double trial_mpaths[8];
+    double trial_mpaths[16];
 } mypbr_tune_result;
+
+/* Sets the launch settings the autotuner would set (0 keeps a setting's
+ * default: block 256, 32M paths per wave, traversal 0). */
+int mypbr_gpu_set_launch(mypbr_gpu_scene* scene, int32_t block, int64_t wave_paths, int32_t traversal);
 
 /* Times short renders of the view with each setting and keeps the fastest on
  * the handle: later renders use it unless opts->samples_per_wave is set. */

@@ -88,8 +88,8 @@ class SkySettingsStruct(ctypes.Structure):
 
 
 class TuneResultStruct(ctypes.Structure):
-    _fields_ = [("block", ctypes.c_int32), ("reserved", ctypes.c_int32), ("wave_paths", ctypes.c_int64),
-                ("mpaths_per_s", ctypes.c_double), ("trial_mpaths", ctypes.c_double * 8)]
+    _fields_ = [("block", ctypes.c_int32), ("traversal", ctypes.c_int32), ("wave_paths", ctypes.c_int64),
+                ("mpaths_per_s", ctypes.c_double), ("trial_mpaths", ctypes.c_double * 16)]
 
 
 class DisplayOptsStruct(ctypes.Structure):
@@ -140,6 +140,7 @@ def lib():
     L.mypbr_gpu_trace.argtypes = [vp, fp, i64, fp, ip, ctypes.c_int]
     L.mypbr_gpu_bsdf_eval.argtypes = [vp, i32, fp, fp, fp, i64, fp]
     L.mypbr_gpu_render_batch.argtypes = [ctypes.POINTER(BatchJobStruct), i32]
+    L.mypbr_gpu_set_launch.argtypes = [vp, i32, i64, i32]
     L.mypbr_sky_settings_init.argtypes = [ctypes.POINTER(SkySettingsStruct)]
     L.mypbr_sky_settings_init.restype = None
     L.mypbr_sky_bake.argtypes = [ctypes.POINTER(SkySettingsStruct), dp, dp, i32, i32, dp, dp, ctypes.c_int]
@@ -476,8 +477,13 @@ def autotune(camera, gpu_scene):
     c, o = camera.structs()
     r = TuneResultStruct()
     check(lib().mypbr_gpu_autotune(gpu_scene.handle, ctypes.byref(c), ctypes.byref(o), ctypes.byref(r)))
-    return {"block": r.block, "wave_paths": r.wave_paths, "mpaths_per_s": r.mpaths_per_s,
-            "trials": list(r.trial_mpaths)}
+    return {"block": r.block, "traversal": r.traversal, "wave_paths": r.wave_paths,
+            "mpaths_per_s": r.mpaths_per_s, "trials": list(r.trial_mpaths)}
+
+
+def set_launch(gpu_scene, block=0, wave_paths=0, traversal=0):
+    """Launch settings of later renders of this handle (0 = default)."""
+    check(lib().mypbr_gpu_set_launch(gpu_scene.handle, block, wave_paths, traversal))
 
 
 def sky_bake(sun_direction, sun_irradiance, width=256, height=128, rayleigh=1.0, mie=1.0, mie_g=0.8, ozone=1.0,

@@ -570,102 +570,144 @@ MYPBR_DEV bool any_hit(const DeviceScene& S, float3 o, float3 d, float tmin, flo
     return walk<true, VOX>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
 }
 
-template <bool ANY, bool VOX>
-MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
+// A ray's BVH walk, advanced one interior node at a time (walk_node), so that
+// a persistent kernel can give a lane a new ray as soon as its last one is
+// done instead of waiting for the slowest lane of its warp.
+struct WalkState {
+    float3 o, d, inv, oi;
+    TriRay tr;
+    float tmin;
+    uint64_t media_key;
     HitInfo h;
-    h.prim = kMiss;
-    h.t = tmax;
-    h.b1 = h.b2 = 0.0f;
-    if (S.has_bvh) {
-        float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
-        float3 oi = -1.0f * (o * inv);
-        TriRay tr = make_tri_ray(d);
-        int stack[kBvhStack];
-        int sp = 0;
-        int node = 0;
-        // A tree walk enters each interior node at most once; the cap only
-        // guards against a malformed tree, which it reports instead of spinning.
-        int visits = 0;
-        while (true) {
-            if (++visits > S.bvh_node_count + 1) {
-                atomicCAS(S.error, 0, 1);
-                break;
-            }
-            const float4* n = S.bvh + 4 * node;
-            float4 a0 = ldg4(n), a1 = ldg4(n + 1), c0 = ldg4(n + 2), c1 = ldg4(n + 3);
-            // slab tests of both children against (tmin, best)
-            float lx0 = fmaf(a0.x, inv.x, oi.x), hx0 = fmaf(a1.x, inv.x, oi.x);
-            float ly0 = fmaf(a0.y, inv.y, oi.y), hy0 = fmaf(a1.y, inv.y, oi.y);
-            float lz0 = fmaf(a0.z, inv.z, oi.z), hz0 = fmaf(a1.z, inv.z, oi.z);
-            float n0 = fmaxf(fmaxf(fminf(lx0, hx0), fminf(ly0, hy0)), fmaxf(fminf(lz0, hz0), tmin));
-            float f0 = fminf(fminf(fmaxf(lx0, hx0), fmaxf(ly0, hy0)), fminf(fmaxf(lz0, hz0), h.t));
-            float lx1 = fmaf(c0.x, inv.x, oi.x), hx1 = fmaf(c1.x, inv.x, oi.x);
-            float ly1 = fmaf(c0.y, inv.y, oi.y), hy1 = fmaf(c1.y, inv.y, oi.y);
-            float lz1 = fmaf(c0.z, inv.z, oi.z), hz1 = fmaf(c1.z, inv.z, oi.z);
-            float n1 = fmaxf(fmaxf(fminf(lx1, hx1), fminf(ly1, hy1)), fmaxf(fminf(lz1, hz1), tmin));
-            float f1 = fminf(fminf(fmaxf(lx1, hx1), fmaxf(ly1, hy1)), fminf(fmaxf(lz1, hz1), h.t));
-            // A small relative widening keeps FP32 slab tests conservative
-            bool h0 = n0 <= f0 * 1.00000024f + 1e-30f;
-            bool h1 = n1 <= f1 * 1.00000024f + 1e-30f;
-            int i0 = __float_as_int(a0.w), k0 = __float_as_int(a1.w);
-            int i1 = __float_as_int(c0.w), k1 = __float_as_int(c1.w);
+    int node, sp, visits;
+};
+// The walk's stack lives beside its state (a kBvhStack-entry local array),
+// so that the state's scalars can stay in registers.
+
+MYPBR_DEV void walk_init(const DeviceScene& S, WalkState& W, float3 o, float3 d, float tmin, float tmax,
+                         uint64_t media_key) {
+    W.o = o;
+    W.d = d;
+    W.tmin = tmin;
+    W.media_key = media_key;
+    W.h.prim = kMiss;
+    W.h.t = tmax;
+    W.h.b1 = W.h.b2 = 0.0f;
+    W.inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    W.oi = -1.0f * (o * W.inv);
+    W.tr = make_tri_ray(d);
+    W.node = 0;
+    W.sp = S.has_bvh ? 0 : -1;  // -1: nothing (left) to walk
+    W.visits = 0;
+}
+
+// One interior node: slab tests of both children, the primitives of child
+// leaves, then the next node. Returns false once the walk is over (or, with
+// ANY, a hit was found).
+template <bool ANY, bool VOX>
+MYPBR_DEV bool walk_node(const DeviceScene& S, WalkState& W, int* stack) {
+    if (W.sp < 0)
+        return false;
+    // A tree walk enters each interior node at most once; the cap only guards
+    // against a malformed tree, which it reports instead of spinning.
+    if (++W.visits > S.bvh_node_count + 1) {
+        atomicCAS(S.error, 0, 1);
+        W.sp = -1;
+        return false;
+    }
+    const float3 o = W.o, d = W.d, inv = W.inv, oi = W.oi;
+    const float tmin = W.tmin;
+    HitInfo& h = W.h;
+    const float4* n = S.bvh + 4 * W.node;
+    float4 a0 = ldg4(n), a1 = ldg4(n + 1), c0 = ldg4(n + 2), c1 = ldg4(n + 3);
+    // slab tests of both children against (tmin, best)
+    float lx0 = fmaf(a0.x, inv.x, oi.x), hx0 = fmaf(a1.x, inv.x, oi.x);
+    float ly0 = fmaf(a0.y, inv.y, oi.y), hy0 = fmaf(a1.y, inv.y, oi.y);
+    float lz0 = fmaf(a0.z, inv.z, oi.z), hz0 = fmaf(a1.z, inv.z, oi.z);
+    float n0 = fmaxf(fmaxf(fminf(lx0, hx0), fminf(ly0, hy0)), fmaxf(fminf(lz0, hz0), tmin));
+    float f0 = fminf(fminf(fmaxf(lx0, hx0), fmaxf(ly0, hy0)), fminf(fmaxf(lz0, hz0), h.t));
+    float lx1 = fmaf(c0.x, inv.x, oi.x), hx1 = fmaf(c1.x, inv.x, oi.x);
+    float ly1 = fmaf(c0.y, inv.y, oi.y), hy1 = fmaf(c1.y, inv.y, oi.y);
+    float lz1 = fmaf(c0.z, inv.z, oi.z), hz1 = fmaf(c1.z, inv.z, oi.z);
+    float n1 = fmaxf(fmaxf(fminf(lx1, hx1), fminf(ly1, hy1)), fmaxf(fminf(lz1, hz1), tmin));
+    float f1 = fminf(fminf(fmaxf(lx1, hx1), fmaxf(ly1, hy1)), fminf(fmaxf(lz1, hz1), h.t));
+    // A small relative widening keeps FP32 slab tests conservative
+    bool h0 = n0 <= f0 * 1.00000024f + 1e-30f;
+    bool h1 = n1 <= f1 * 1.00000024f + 1e-30f;
+    int i0 = __float_as_int(a0.w), k0 = __float_as_int(a1.w);
+    int i1 = __float_as_int(c0.w), k1 = __float_as_int(c1.w);
 #pragma unroll
-            for (int side = 0; side < 2; side++) {
-                bool hit = side == 0 ? h0 : h1;
-                int cnt = side == 0 ? k0 : k1;
-                int first = side == 0 ? i0 : i1;
-                if (!(hit && cnt > 0))
-                    continue;
-                for (int k = 0; k < cnt; k++) {
-                    uint32_t ref = __ldg(S.leaf_refs + first + k);
-                    int kind = int(ref >> kKindShift), idx = int(ref & kIndexMask);
-                    float t, b1 = 0.0f, b2 = 0.0f;
-                    bool got = false;
-                    if (kind == kTriangle) {
-                        got = hit_triangle(S, idx, o, tr, tmin, h.t, t, b1, b2);
-                    } else if (kind == kSphere) {
-                        got = hit_sphere(S, idx, o, d, tmin, h.t, t);
-                    } else if (kind == kQuad) {
-                        got = hit_quad(S, idx, o, d, tmin, h.t, t, b1, b2);
-                    } else if (kind == kMedium && media_key != 0) {
-                        got = hit_medium(S, idx, o, d, tmin, h.t, hash_uniform(media_key, uint32_t(idx)), t);
-                    } else if (VOX && kind == kVoxel) {
-                        int mat, face;
-                        got = hit_voxel_block(S, idx, o, d, tmin, h.t, t, mat, face);
-                        b1 = __int_as_float(mat);
-                        b2 = __int_as_float(face);
-                    }
-                    if (got) {
-                        h.t = t;
-                        h.b1 = b1;
-                        h.b2 = b2;
-                        h.prim = ref;
-                        if (ANY)
-                            return h;
-                    }
-                }
+    for (int side = 0; side < 2; side++) {
+        bool hit = side == 0 ? h0 : h1;
+        int cnt = side == 0 ? k0 : k1;
+        int first = side == 0 ? i0 : i1;
+        if (!(hit && cnt > 0))
+            continue;
+        for (int k = 0; k < cnt; k++) {
+            uint32_t ref = __ldg(S.leaf_refs + first + k);
+            int kind = int(ref >> kKindShift), idx = int(ref & kIndexMask);
+            float t, b1 = 0.0f, b2 = 0.0f;
+            bool got = false;
+            if (kind == kTriangle) {
+                got = hit_triangle(S, idx, o, W.tr, tmin, h.t, t, b1, b2);
+            } else if (kind == kSphere) {
+                got = hit_sphere(S, idx, o, d, tmin, h.t, t);
+            } else if (kind == kQuad) {
+                got = hit_quad(S, idx, o, d, tmin, h.t, t, b1, b2);
+            } else if (kind == kMedium && W.media_key != 0) {
+                got = hit_medium(S, idx, o, d, tmin, h.t, hash_uniform(W.media_key, uint32_t(idx)), t);
+            } else if (VOX && kind == kVoxel) {
+                int mat, face;
+                got = hit_voxel_block(S, idx, o, d, tmin, h.t, t, mat, face);
+                b1 = __int_as_float(mat);
+                b2 = __int_as_float(face);
             }
-            h0 = h0 && k0 == 0;
-            h1 = h1 && k1 == 0;
-            if (h0 && h1) {
-                bool first0 = n0 <= n1;
-                if (sp == kBvhStack) {  // deeper than the host-checked depth: report, stop
-                    atomicCAS(S.error, 0, 2);
-                    break;
+            if (got) {
+                h.t = t;
+                h.b1 = b1;
+                h.b2 = b2;
+                h.prim = ref;
+                if (ANY) {
+                    W.sp = -1;
+                    return false;
                 }
-                stack[sp++] = first0 ? i1 : i0;
-                node = first0 ? i0 : i1;
-            } else if (h0) {
-                node = i0;
-            } else if (h1) {
-                node = i1;
-            } else {
-                if (sp == 0)
-                    break;
-                node = stack[--sp];
             }
         }
     }
+    h0 = h0 && k0 == 0;
+    h1 = h1 && k1 == 0;
+    if (h0 && h1) {
+        bool first0 = n0 <= n1;
+        if (W.sp == kBvhStack) {  // deeper than the host-checked depth: report, stop
+            atomicCAS(S.error, 0, 2);
+            W.sp = -1;
+            return false;
+        }
+        stack[W.sp++] = first0 ? i1 : i0;
+        W.node = first0 ? i0 : i1;
+    } else if (h0) {
+        W.node = i0;
+    } else if (h1) {
+        W.node = i1;
+    } else {
+        if (W.sp == 0) {
+            W.sp = -1;
+            return false;
+        }
+        W.node = stack[--W.sp];
+    }
+    return true;
+}
+
+// The unbounded objects beside the BVH, after the walk.
+template <bool ANY>
+MYPBR_DEV void walk_unbounded(const DeviceScene& S, WalkState& W) {
+    const float3 o = W.o, d = W.d;
+    const float tmin = W.tmin;
+    const uint64_t media_key = W.media_key;
+    HitInfo& h = W.h;
+    if (ANY && h.prim != kMiss)
+        return;
     // The ground (plane.h:17-34) and height fog (medium.h:352-381) beside the BVH
     for (int k = 0; k < S.unbounded_count; k++) {
         DevUnbounded ub = S.unbounded[k];
@@ -677,7 +719,7 @@ MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, flo
                 h.t = t;
                 h.prim = (uint32_t(kGround) << kKindShift) | uint32_t(k);
                 if (ANY)
-                    return h;
+                    return;
             }
         } else if (media_key != 0) {
             float len = length(d);
@@ -699,11 +741,21 @@ MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, flo
                 h.t = t;
                 h.prim = (uint32_t(kHeightFog) << kKindShift) | uint32_t(k);
                 if (ANY)
-                    return h;
+                    return;
             }
         }
     }
-    return h;
+}
+
+template <bool ANY, bool VOX>
+MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
+    WalkState W;
+    int stack[kBvhStack];
+    walk_init(S, W, o, d, tmin, tmax, media_key);
+    while (walk_node<ANY, VOX>(S, W, stack)) {
+    }
+    walk_unbounded<ANY>(S, W);
+    return W.h;
 }
 
 // ------------------------------------------------------- surface records

@@ -75,6 +75,7 @@ struct mypbr_gpu_scene {
     // autotuned launch settings (0: built-in defaults)
     size_t tuned_wave_paths = 0;
     int tuned_block = 0;
+    int tuned_traversal = 0;  // 0: one ray per lane to the end (k_extend); 1: lanes take new rays (k_extend_pt)
 };
 
 namespace mypbr_dev {

@@ -73,6 +73,10 @@ MYPBR_DEV uint32_t* class_counter(const WaveParams& P, int d, int c) {
     return P.B.counters + 2 * P.B.depth_slots + d * kShadeClasses + c;
 }
 MYPBR_DEV uint32_t* class_queue(const WaveParams& P, int c) { return P.B.class_queue + size_t(c) * P.B.capacity; }
+// Rays of bounce d's extension queue handed out so far (the persistent extend kernel).
+MYPBR_DEV uint32_t* fetch_counter(const WaveParams& P, int d) {
+    return P.B.counters + (2 + kShadeClasses) * P.B.depth_slots + d;
+}
 
 // One atomic per warp: the active lanes that push get consecutive slots.
 MYPBR_DEV uint32_t warp_push(uint32_t* counter) {
@@ -286,6 +290,67 @@ __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
         int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h)]);
         uint32_t* counter = class_counter(P, depth, c);
         class_queue(P, c)[warp_push_keyed(counter)] = slot;
+    }
+}
+
+// k_extend with lanes that take a new ray as soon as theirs is done: a warp
+// advances all its rays one BVH node per step, and when at least a quarter of
+// its lanes are idle (or all), it takes that many rays from the queue with
+// one atomic. Lanes then do not wait for the slowest ray of their warp (the
+// replacement of terminated rays of Aila and Laine, "Understanding the
+// Efficiency of Ray Traversal on GPUs", HPG 2009). Same hits as k_extend.
+template <bool VOX>
+__global__ void __launch_bounds__(256, 3) k_extend_pt(WaveParams P, int depth) {
+    const uint32_t n = *ext_counter(P, depth);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
+        atomicAdd(&P.totals[0], (unsigned long long)n);
+    const uint32_t* q = P.B.queue[depth & 1];
+    uint32_t* fetch = fetch_counter(P, depth);
+    const int lane = threadIdx.x & 31;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    WalkState W;
+    int stack[kBvhStack];
+    uint32_t slot = 0;
+    bool active = false, exhausted = false;
+    // every lane's walk is bounded (node visits); this bounds the warp's steps
+    // by the rays one warp could ever be given, were it given all of them
+    const long long max_steps = (long long)(n + 32) * (long long)(P.S.bvh_node_count + 2) + 64;
+    for (long long step = 0; step < max_steps; step++) {
+        unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
+        unsigned busy = __ballot_sync(0xffffffffu, active);
+        if (idle != 0 && (__popc(idle) >= 8 || busy == 0)) {
+            int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(fetch, uint32_t(__popc(idle)));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active && !exhausted) {
+                uint32_t k = base + uint32_t(__popc(idle & lanes_below));
+                if (k < n) {
+                    slot = q[k];
+                    float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
+                    uint64_t key = 0;
+                    if (P.has_media) {
+                        uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
+                        key = media_key(P, pixel, pass, uint32_t(depth), 0);
+                    }
+                    walk_init(P.S, W, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, exhausted))
+            break;
+        if (active && !walk_node<false, VOX>(P.S, W, stack)) {
+            walk_unbounded<false>(P.S, W);
+            const HitInfo& h = W.h;
+            P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
+            int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h)]);
+            class_queue(P, c)[warp_push_keyed(class_counter(P, depth, c))] = slot;
+            active = false;
+        }
     }
 }
 
@@ -699,7 +764,7 @@ struct GuidePackSink {
     }
 };
 
-size_t counter_words(int depth_slots) { return size_t(depth_slots) * (2 + kShadeClasses) + 8; }
+size_t counter_words(int depth_slots) { return size_t(depth_slots) * (3 + kShadeClasses) + 8; }
 
 namespace {
 
@@ -796,6 +861,7 @@ int bad_arg(const std::string& m) {
 struct Launch {
     int grid_extend, grid_shade, grid_shadow, grid_stream;
     int block = 256;              // threads per block of extend, shade and shadow
+    bool persistent = false;      // extend with lanes that take new rays (k_extend_pt)
     bool guided_kernels = false;  // the shading variants of guided renders
     int grid_guide = 0;
     size_t guide_smem = 0;
@@ -806,6 +872,7 @@ struct Launch {
 Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
     Launch L{};
     L.block = block == 128 || block == 256 ? block : (G.tuned_block ? G.tuned_block : 256);
+    L.persistent = G.tuned_traversal == 1;
     int per_sm = 0;
     bool vox = G.dev.has_voxels;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vox ? (const void*)k_extend<true> : (const void*)k_extend<false>,
@@ -905,7 +972,11 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
         launches++;
     }
     for (int depth = 0; depth < P.max_depth; depth++) {
-        if (P.S.has_voxels)
+        if (L.persistent && P.S.has_voxels)
+            TIMED(1, (k_extend_pt<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+        else if (L.persistent)
+            TIMED(1, (k_extend_pt<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+        else if (P.S.has_voxels)
             TIMED(1, (k_extend<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else
             TIMED(1, (k_extend<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
@@ -1450,14 +1521,16 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
     mypbr_tune_result res{};
     double best = -1;
     size_t keep_paths = G->tuned_wave_paths;
-    int keep_block = G->tuned_block;
+    int keep_block = G->tuned_block, keep_trav = G->tuned_traversal;
     cudaEvent_t e0, e1;
     MYPBR_CUDA(cudaEventCreate(&e0));
     MYPBR_CUDA(cudaEventCreate(&e1));
     int status = MYPBR_OK;
     int trial = 0;
+    for (int trav = 0; trav < 2; trav++)
     for (int b : blocks) {
         for (size_t wp : waves) {
+            G->tuned_traversal = trav;
             G->tuned_block = b;
             G->tuned_wave_paths = wp;
             float ms = 0;
@@ -1475,6 +1548,7 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
             if (mp > best) {
                 best = mp;
                 res.block = b;
+                res.traversal = trav;
                 res.wave_paths = int64_t(wp);
                 res.mpaths_per_s = mp;
             }
@@ -1485,12 +1559,23 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
     if (status != MYPBR_OK) {
         G->tuned_wave_paths = keep_paths;
         G->tuned_block = keep_block;
+        G->tuned_traversal = keep_trav;
         return status;
     }
     G->tuned_block = res.block;
+    G->tuned_traversal = res.traversal;
     G->tuned_wave_paths = size_t(res.wave_paths);
     if (out)
         *out = res;
+    return MYPBR_OK;
+}
+
+extern "C" int mypbr_gpu_set_launch(mypbr_gpu_scene* G, int32_t block, int64_t wave_paths, int32_t traversal) {
+    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 1)
+        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0 or 1");
+    G->tuned_block = block;
+    G->tuned_wave_paths = size_t(wave_paths);
+    G->tuned_traversal = traversal;
     return MYPBR_OK;
 }
 
@@ -1526,7 +1611,7 @@ constexpr size_t kNoAllocAlign = 256;
 constexpr size_t align_up(size_t x) { return (x + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
 constexpr size_t kSlotBytes = 8 * sizeof(float4) + (3 + kShadeClasses) * sizeof(uint32_t);
 constexpr size_t kPixelBytes = (3 + 3 + 7) * sizeof(double);
-constexpr size_t kCounterBytes = ((2 + kShadeClasses) * (kNoAllocMaxDepth + 1) + 8) * sizeof(uint32_t);
+constexpr size_t kCounterBytes = ((3 + kShadeClasses) * (kNoAllocMaxDepth + 1) + 8) * sizeof(uint32_t);
 constexpr size_t kNoAllocNeed = 16 * kNoAllocAlign + kNoAllocMaxPixels * (kSlotBytes + kPixelBytes) + kCounterBytes +
                                 2 * sizeof(unsigned long long);
 constexpr size_t kNoAllocBytes = size_t(18) << 20;

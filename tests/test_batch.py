@@ -83,6 +83,23 @@ def test_autotune_keeps_the_result():
     before = cam.render(G).radiance
     r = mp.autotune(cam, G)
     assert r["block"] in (128, 256) and r["wave_paths"] in (4 << 20, 8 << 20, 16 << 20, 32 << 20)
+    assert r["traversal"] in (0, 1)
     assert all(t > 0 for t in r["trials"]) and r["mpaths_per_s"] == max(r["trials"])
     after = cam.render(G).radiance
     np.testing.assert_allclose(after, before, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["materials", "voxels", "fog_box"])
+def test_persistent_traversal_matches(name):
+    """Lanes that take new rays as theirs finish find the same hits."""
+    sc = mp.load_scene(scene_path(f"{name}.scene"))
+    G = mp.GpuScene(sc)
+    cam = camera_of(sc, 48, 16)
+    mp.set_launch(G, traversal=0)
+    a = cam.render(G).radiance
+    mp.set_launch(G, traversal=1)
+    b = cam.render(G).radiance
+    mp.set_launch(G, block=128, wave_paths=1 << 16, traversal=1)
+    c = cam.render(G).radiance
+    np.testing.assert_allclose(b, a, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(c, a, rtol=1e-12, atol=1e-14)
