@@ -533,6 +533,7 @@ def run_hall_render(args):
         w = args.hall_width
         scene = mp.load_scene(voxel_hall_scene(d, size=args.hall_size, width=w, height=w * 9 // 16, spp=args.spp))
     G = mp.GpuScene(scene)
+    mp.set_launch(G, block=args.block, traversal=args.traversal)
     cam = scene.camera
     cam.samples_per_pixel = args.spp
     cam.guided = args.hidden

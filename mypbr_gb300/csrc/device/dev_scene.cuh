@@ -747,15 +747,142 @@ MYPBR_DEV void walk_unbounded(const DeviceScene& S, WalkState& W) {
     }
 }
 
+// The whole walk in one loop (the form the per-ray kernels use; walk_node
+// above is the same step, resumable, for k_extend_pt).
 template <bool ANY, bool VOX>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
-    WalkState W;
-    int stack[kBvhStack];
-    walk_init(S, W, o, d, tmin, tmax, media_key);
-    while (walk_node<ANY, VOX>(S, W, stack)) {
+    HitInfo h;
+    h.prim = kMiss;
+    h.t = tmax;
+    h.b1 = h.b2 = 0.0f;
+    if (S.has_bvh) {
+        float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+        float3 oi = -1.0f * (o * inv);
+        TriRay tr = make_tri_ray(d);
+        int stack[kBvhStack];
+        int sp = 0;
+        int node = 0;
+        // A tree walk enters each interior node at most once; the cap only
+        // guards against a malformed tree, which it reports instead of spinning.
+        int visits = 0;
+        while (true) {
+            if (++visits > S.bvh_node_count + 1) {
+                atomicCAS(S.error, 0, 1);
+                break;
+            }
+            const float4* n = S.bvh + 4 * node;
+            float4 a0 = ldg4(n), a1 = ldg4(n + 1), c0 = ldg4(n + 2), c1 = ldg4(n + 3);
+            // slab tests of both children against (tmin, best)
+            float lx0 = fmaf(a0.x, inv.x, oi.x), hx0 = fmaf(a1.x, inv.x, oi.x);
+            float ly0 = fmaf(a0.y, inv.y, oi.y), hy0 = fmaf(a1.y, inv.y, oi.y);
+            float lz0 = fmaf(a0.z, inv.z, oi.z), hz0 = fmaf(a1.z, inv.z, oi.z);
+            float n0 = fmaxf(fmaxf(fminf(lx0, hx0), fminf(ly0, hy0)), fmaxf(fminf(lz0, hz0), tmin));
+            float f0 = fminf(fminf(fmaxf(lx0, hx0), fmaxf(ly0, hy0)), fminf(fmaxf(lz0, hz0), h.t));
+            float lx1 = fmaf(c0.x, inv.x, oi.x), hx1 = fmaf(c1.x, inv.x, oi.x);
+            float ly1 = fmaf(c0.y, inv.y, oi.y), hy1 = fmaf(c1.y, inv.y, oi.y);
+            float lz1 = fmaf(c0.z, inv.z, oi.z), hz1 = fmaf(c1.z, inv.z, oi.z);
+            float n1 = fmaxf(fmaxf(fminf(lx1, hx1), fminf(ly1, hy1)), fmaxf(fminf(lz1, hz1), tmin));
+            float f1 = fminf(fminf(fmaxf(lx1, hx1), fmaxf(ly1, hy1)), fminf(fmaxf(lz1, hz1), h.t));
+            // A small relative widening keeps FP32 slab tests conservative
+            bool h0 = n0 <= f0 * 1.00000024f + 1e-30f;
+            bool h1 = n1 <= f1 * 1.00000024f + 1e-30f;
+            int i0 = __float_as_int(a0.w), k0 = __float_as_int(a1.w);
+            int i1 = __float_as_int(c0.w), k1 = __float_as_int(c1.w);
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                bool hit = side == 0 ? h0 : h1;
+                int cnt = side == 0 ? k0 : k1;
+                int first = side == 0 ? i0 : i1;
+                if (!(hit && cnt > 0))
+                    continue;
+                for (int k = 0; k < cnt; k++) {
+                    uint32_t ref = __ldg(S.leaf_refs + first + k);
+                    int kind = int(ref >> kKindShift), idx = int(ref & kIndexMask);
+                    float t, b1 = 0.0f, b2 = 0.0f;
+                    bool got = false;
+                    if (kind == kTriangle) {
+                        got = hit_triangle(S, idx, o, tr, tmin, h.t, t, b1, b2);
+                    } else if (kind == kSphere) {
+                        got = hit_sphere(S, idx, o, d, tmin, h.t, t);
+                    } else if (kind == kQuad) {
+                        got = hit_quad(S, idx, o, d, tmin, h.t, t, b1, b2);
+                    } else if (kind == kMedium && media_key != 0) {
+                        got = hit_medium(S, idx, o, d, tmin, h.t, hash_uniform(media_key, uint32_t(idx)), t);
+                    } else if (VOX && kind == kVoxel) {
+                        int mat, face;
+                        got = hit_voxel_block(S, idx, o, d, tmin, h.t, t, mat, face);
+                        b1 = __int_as_float(mat);
+                        b2 = __int_as_float(face);
+                    }
+                    if (got) {
+                        h.t = t;
+                        h.b1 = b1;
+                        h.b2 = b2;
+                        h.prim = ref;
+                        if (ANY)
+                            return h;
+                    }
+                }
+            }
+            h0 = h0 && k0 == 0;
+            h1 = h1 && k1 == 0;
+            if (h0 && h1) {
+                bool first0 = n0 <= n1;
+                if (sp == kBvhStack) {  // deeper than the host-checked depth: report, stop
+                    atomicCAS(S.error, 0, 2);
+                    break;
+                }
+                stack[sp++] = first0 ? i1 : i0;
+                node = first0 ? i0 : i1;
+            } else if (h0) {
+                node = i0;
+            } else if (h1) {
+                node = i1;
+            } else {
+                if (sp == 0)
+                    break;
+                node = stack[--sp];
+            }
+        }
     }
-    walk_unbounded<ANY>(S, W);
-    return W.h;
+    // The ground (plane.h:17-34) and height fog (medium.h:352-381) beside the BVH
+    for (int k = 0; k < S.unbounded_count; k++) {
+        DevUnbounded ub = S.unbounded[k];
+        if (ub.kind == 0) {
+            if (fabsf(d.y) < 1e-12f)
+                continue;
+            float t = (ub.height - o.y) / d.y;
+            if (t > tmin && t < h.t) {
+                h.t = t;
+                h.prim = (uint32_t(kGround) << kKindShift) | uint32_t(k);
+                if (ANY)
+                    return h;
+            }
+        } else if (media_key != 0) {
+            float len = length(d);
+            float kk = d.y / ub.scale_height;
+            float start = ub.density * len * expf(-(o.y + tmin * d.y - ub.height) / ub.scale_height);
+            if (!(start > 0.0f))
+                continue;
+            float tau = -logf(1.0f - hash_uniform(media_key, 0x40000000u + uint32_t(k)));
+            float t;
+            if (fabsf(kk) < 1e-12f) {
+                t = tmin + tau / start;
+            } else {
+                float x = 1.0f - tau * kk / start;
+                if (x <= 0.0f)
+                    continue;
+                t = tmin - logf(x) / kk;
+            }
+            if (t < h.t && isfinite(t)) {
+                h.t = t;
+                h.prim = (uint32_t(kHeightFog) << kKindShift) | uint32_t(k);
+                if (ANY)
+                    return h;
+            }
+        }
+    }
+    return h;
 }
 
 // ------------------------------------------------------- surface records
