@@ -529,6 +529,31 @@ void mypbr_denoise_opts_init(mypbr_denoise_opts* opts);
 int mypbr_gpu_denoise(const double* radiance, const double* albedo, const double* normal, const double* variance,
                       int32_t width, int32_t height, const mypbr_denoise_opts* opts, double* out, int on_device);
 
+/* ------------------------------------------------------ device BVH build */
+
+enum { MYPBR_BVH_LBVH = 1 };
+
+/* What a device BVH build did: primitives, interior nodes, depth (interior
+ * nodes on the deepest path), build time on the device, and the SAH cost
+ * (node visits 0.125, primitive tests 1, relative to the root's area) of the
+ * new tree and of the one it replaced. */
+typedef struct mypbr_bvh_report {
+    int64_t primitives;
+    int64_t nodes;
+    int32_t depth;
+    int32_t reserved;
+    double build_ms;
+    double sah_cost;
+    double sah_cost_before;
+} mypbr_bvh_report;
+
+/* Rebuilds the scene handle's BVH on the device (MYPBR_BVH_LBVH: a linear BVH
+ * over Morton-sorted primitive centroids, Karras 2012) and uses it for later
+ * renders and queries. No counterpart in the reference, whose host SAH build
+ * (bvh.h:110-205, built here by mypbr_gpu_scene_create) stays the default
+ * and the quality reference. */
+int mypbr_gpu_scene_rebuild_bvh(mypbr_gpu_scene* scene, int32_t method, mypbr_bvh_report* report);
+
 /* ------------------------------------------------------------ sky bake */
 
 /* atmosphere_settings (include/atmosphere.h:39-46): densities relative to

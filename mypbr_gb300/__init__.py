@@ -82,6 +82,12 @@ class BatchJobStruct(ctypes.Structure):
                 ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class BvhReportStruct(ctypes.Structure):
+    _fields_ = [("primitives", ctypes.c_int64), ("nodes", ctypes.c_int64), ("depth", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("build_ms", ctypes.c_double), ("sah_cost", ctypes.c_double),
+                ("sah_cost_before", ctypes.c_double)]
+
+
 class SkySettingsStruct(ctypes.Structure):
     _fields_ = [("rayleigh", ctypes.c_double), ("mie", ctypes.c_double), ("mie_g", ctypes.c_double),
                 ("ozone", ctypes.c_double), ("intensity", ctypes.c_double)]
@@ -141,6 +147,7 @@ def lib():
     L.mypbr_gpu_bsdf_eval.argtypes = [vp, i32, fp, fp, fp, i64, fp]
     L.mypbr_gpu_render_batch.argtypes = [ctypes.POINTER(BatchJobStruct), i32]
     L.mypbr_gpu_set_launch.argtypes = [vp, i32, i64, i32]
+    L.mypbr_gpu_scene_rebuild_bvh.argtypes = [vp, i32, ctypes.POINTER(BvhReportStruct)]
     L.mypbr_sky_settings_init.argtypes = [ctypes.POINTER(SkySettingsStruct)]
     L.mypbr_sky_settings_init.restype = None
     L.mypbr_sky_bake.argtypes = [ctypes.POINTER(SkySettingsStruct), dp, dp, i32, i32, dp, dp, ctypes.c_int]
@@ -503,3 +510,10 @@ def sky_bake(sun_direction, sun_irradiance, width=256, height=128, rayleigh=1.0,
 def guide_reset(gpu_scene):
     """The handle's guiding network back to its untrained weights (buffers kept)."""
     check(lib().mypbr_guide_reset(gpu_scene.handle))
+
+
+def rebuild_bvh(gpu_scene):
+    """Replaces the handle's BVH by a linear BVH built on the device; returns the report."""
+    r = BvhReportStruct()
+    check(lib().mypbr_gpu_scene_rebuild_bvh(gpu_scene.handle, 1, ctypes.byref(r)))
+    return {k: getattr(r, k) for k, _ in BvhReportStruct._fields_ if k != "reserved"}

@@ -344,9 +344,8 @@ def triangle_room_scene(directory, triangles=2_000_000, seed=3, spp=64, width=19
     rng = np.random.default_rng(seed)
     parts = []  # (verts, tris, material index)
     # columns: 400, each segs x rings x 2 triangles
-    col_tris = triangles // 2
-    per_col = col_tris // 400
-    segs = 32
+    per_col = max(12, triangles // 2 // 400)
+    segs = min(32, max(6, per_col // 2))
     rings = max(1, per_col // (2 * segs))
     for r in range(20):
         for c in range(20):
@@ -359,7 +358,7 @@ def triangle_room_scene(directory, triangles=2_000_000, seed=3, spp=64, width=19
              ((-10, 0, -15), (0, 0, 30), (0, 8, 0)), ((10, 0, -15), (0, 8, 0), (0, 0, 30)),
              ((-10, 0, -15), (0, 8, 0), (20, 0, 0)), ((-10, 0, 15), (20, 0, 0), (0, 8, 0))]
     areas = [np.linalg.norm(np.cross(u, v)) for _, u, v in faces]
-    left = triangles - sum(len(p[1]) for p in parts)
+    left = max(triangles - sum(len(p[1]) for p in parts), 6 * 16 * 32)
     for (corner, u, v), area in zip(faces, areas):
         u, v, corner = np.array(u, float), np.array(v, float), np.array(corner, float)
         n_face = left * area / sum(areas) / 2
