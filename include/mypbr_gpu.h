@@ -139,7 +139,8 @@ typedef struct mypbr_quad {
 
 /* Triangle flags. */
 enum {
-    MYPBR_TRI_FLIP_NORMAL = 1 /* geometric normal is -normalize(e1 x e2) (mirroring transform) */
+    MYPBR_TRI_FLIP_NORMAL = 1, /* geometric normal is -normalize(e1 x e2) (mirroring transform) */
+    MYPBR_TRI_ALPHA_MASK = 2   /* the mesh's alpha_mask cuts holes in this triangle (include/mesh.h:23-26) */
 };
 
 /* One triangle of a mesh by vertex indices (include/mesh.h:28-44); normal and
@@ -159,7 +160,10 @@ typedef struct mypbr_mesh {
     int64_t first_triangle;
     int64_t triangle_count;
     int32_t material;
-    int32_t reserved;
+    /* Image texture whose coverage masks the mesh's triangles that carry
+     * MYPBR_TRI_ALPHA_MASK (include/mesh.h:81-86): a ray hits where the
+     * coverage is a with probability a. Read only for those triangles. */
+    int32_t alpha_mask;
 } mypbr_mesh;
 
 /* A homogeneous medium of the given density (collisions per unit length) in
@@ -215,7 +219,8 @@ enum {
 enum {
     MYPBR_TEXF_HDR = 1,    /* texels are RGB float in texels_hdr, else RGBA8 in texels_ldr */
     MYPBR_TEXF_LINEAR = 2, /* 8-bit values are data (k / 255), not sRGB */
-    MYPBR_TEXF_REPEAT = 4  /* wrap (u, v) instead of clamping */
+    MYPBR_TEXF_REPEAT = 4, /* wrap (u, v) instead of clamping */
+    MYPBR_TEXF_GREY_MASK = 8 /* no alpha channel: as a mask, the grey level (red byte) is the coverage */
 };
 typedef struct mypbr_texture {
     int32_t type;
@@ -646,6 +651,16 @@ void mypbr_display_opts_init(mypbr_display_opts* opts);
  * Pointers are device memory if on_device, else host memory. */
 int mypbr_gpu_display(const double* radiance, int32_t width, int32_t height, const mypbr_display_opts* opts,
                       double* linear, uint8_t* rgb8, int on_device);
+
+/* Decodes an 8-bit image file (PNG of any color type and depth, interlaced
+ * or not, with tRNS; TGA types 1, 2, 3 and their run-length forms) to RGBA
+ * bytes, rows from the top, as image_texture loads one (stbi_load with 4
+ * channels, include/texture.h:67-98). *channels is the file's own count as
+ * stb_image reports it (1 grey, 2 grey + alpha, 3 RGB, 4 RGBA). With rgba
+ * NULL only the size is returned; else rgba holds capacity >= w * h * 4 bytes.
+ * JPEG, BMP and GIF files give MYPBR_ERR_UNSUPPORTED. */
+int mypbr_image_read(const char* path, int32_t* width, int32_t* height, int32_t* channels, uint8_t* rgba,
+                     int64_t capacity);
 
 /* write_image (include/image_io.h:84-106): the format follows the extension;
  * .png and .ppm are display images (post-processed on the GPU), .hdr and .pfm

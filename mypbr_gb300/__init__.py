@@ -130,6 +130,8 @@ def lib():
     L.mypbr_scene_free.argtypes = [vp]
     L.mypbr_scene_free.restype = None
     L.mypbr_ggx_albedo_table.argtypes = [dp]
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    L.mypbr_image_read.argtypes = [ctypes.c_char_p, i32p, i32p, i32p, vp, ctypes.c_int64]
     L.mypbr_camera_init.argtypes = [ctypes.POINTER(CameraStruct)]
     L.mypbr_camera_init.restype = None
     L.mypbr_render_opts_init.argtypes = [ctypes.POINTER(RenderOptsStruct)]
@@ -368,6 +370,16 @@ def ggx_albedo_table():
     out = np.zeros(32 * 32 + 32, dtype=np.float64)
     check(lib().mypbr_ggx_albedo_table(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
     return out[:1024].reshape(32, 32), out[1024:]
+
+
+def read_image(path):
+    """An 8-bit image file as image_texture decodes it: (RGBA bytes [H, W, 4], channels)."""
+    w, h, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    b = os.fsencode(path)
+    check(lib().mypbr_image_read(b, ctypes.byref(w), ctypes.byref(h), ctypes.byref(c), None, 0))
+    out = np.zeros((h.value, w.value, 4), dtype=np.uint8)
+    check(lib().mypbr_image_read(b, ctypes.byref(w), ctypes.byref(h), ctypes.byref(c), out.ctypes.data, out.nbytes))
+    return out, c.value
 
 
 # ------------------------------------------------------------ path guiding

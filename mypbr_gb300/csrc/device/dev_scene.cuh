@@ -90,6 +90,7 @@ struct DeviceScene {
     int has_bvh;
     int bvh_node_count;  // interior nodes; a walk visits each at most once
     int has_media;       // media or height fog present (free-flight sampling needs keys)
+    int has_alpha;       // some triangle carries an alpha mask (its coverage test needs keys)
     int has_voxels;      // voxel blocks among the BVH's primitives
     int has_emitters;    // some hittable surface can emit (diffuse light or emissive texture)
     int has_clear_glass; // some hittable surface lets shadows through (smooth dielectric)
@@ -252,8 +253,51 @@ MYPBR_DEV TriRay make_tri_ray(float3 d) {
 
 // Barycentrics b1, b2 are the weights of v1 and v2, the reference's (u, v)
 // without texture coordinates (mesh.h:72-79).
+// The coverage test of an alpha-masked triangle (mesh.h:23-26, 81-86): a ray
+// meets the surface where the mask's coverage is a with probability a. The
+// uniform number is a hash of the ray's key and the triangle, so the answer
+// does not depend on the order the walk meets primitives in; with key 0 (a
+// query without random numbers) the surface is there wherever a > 0.
+// Coverage is the alpha byte / 255, or the grey level without an alpha
+// channel (texture.h:129-135), at the nearest texel of the interpolated uv.
+MYPBR_DEV bool alpha_covers(const DeviceScene& S, int i, float b1, float b2, uint64_t key) {
+    int4 sb = S.tri_shading[2 * i + 1];
+    if (sb.z < 0)
+        return true;
+    int4 sa = S.tri_shading[2 * i];
+    float u = b1, v = b2;
+    if (sa.w >= 0) {
+        float2 t0 = S.uvs[sa.w], t1 = S.uvs[sb.x], t2 = S.uvs[sb.y];
+        float b0 = 1.0f - b1 - b2;
+        u = b0 * t0.x + b1 * t1.x + b2 * t2.x;
+        v = b0 * t0.y + b1 * t1.y + b2 * t2.y;
+    }
+    const DevTexture& tx = S.textures[sb.z];
+    if (tx.flags & 4) {
+        u -= floorf(u);
+        v -= floorf(v);
+    } else {
+        u = fminf(fmaxf(u, 0.0f), 1.0f);
+        v = fminf(fmaxf(v, 0.0f), 1.0f);
+    }
+    v = 1.0f - v;
+    int x = min(max(int(u * tx.width), 0), tx.width - 1);
+    int y = min(max(int(v * tx.height), 0), tx.height - 1);
+    long long k = tx.offset + (long long)y * tx.width + x;
+    int a = S.texels_ldr[4 * k + ((tx.flags & 8) ? 0 : 3)];
+    if (a >= 255)
+        return true;
+    if (key == 0)
+        return a > 0;
+    return hash_uniform(key, 0x80000000u | uint32_t(i)) * 255.0f < float(a);
+}
+
+// MASKED = false treats an alpha-masked triangle as solid (the light-sampling
+// density of a mesh light, which ignores holes as its power estimate does,
+// mesh.h:138).
+template <bool MASKED = true>
 MYPBR_DEV bool hit_triangle(const DeviceScene& S, int i, float3 o, const TriRay& R, float tmin, float tmax, float& t,
-                            float& b1, float& b2) {
+                            float& b1, float& b2, uint64_t key = 0) {
     const float4* tp = S.tris + 3 * i;
     float3 A = f3(ldg4(tp)) - o, B = f3(ldg4(tp + 1)) - o, C = f3(ldg4(tp + 2)) - o;
     float Az = comp(A, R.kz), Bz = comp(B, R.kz), Cz = comp(C, R.kz);
@@ -276,6 +320,9 @@ MYPBR_DEV bool hit_triangle(const DeviceScene& S, int i, float3 o, const TriRay&
     float inv = 1.0f / det;
     float tt = T * inv;
     if (!(tt > tmin && tt < tmax))
+        return false;
+    // checked before the caller's closest hit changes (mesh.h:81-86)
+    if (MASKED && S.has_alpha && !alpha_covers(S, i, V * inv, W * inv, key))
         return false;
     t = tt;
     b1 = V * inv;
@@ -649,7 +696,7 @@ MYPBR_DEV bool walk_node(const DeviceScene& S, WalkState& W, int* stack) {
             float t, b1 = 0.0f, b2 = 0.0f;
             bool got = false;
             if (kind == kTriangle) {
-                got = hit_triangle(S, idx, o, W.tr, tmin, h.t, t, b1, b2);
+                got = hit_triangle(S, idx, o, W.tr, tmin, h.t, t, b1, b2, W.media_key);
             } else if (kind == kSphere) {
                 got = hit_sphere(S, idx, o, d, tmin, h.t, t);
             } else if (kind == kQuad) {
@@ -801,7 +848,7 @@ MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, flo
                     float t, b1 = 0.0f, b2 = 0.0f;
                     bool got = false;
                     if (kind == kTriangle) {
-                        got = hit_triangle(S, idx, o, tr, tmin, h.t, t, b1, b2);
+                        got = hit_triangle(S, idx, o, tr, tmin, h.t, t, b1, b2, media_key);
                     } else if (kind == kSphere) {
                         got = hit_sphere(S, idx, o, d, tmin, h.t, t);
                     } else if (kind == kQuad) {

@@ -882,7 +882,7 @@ MYPBR_DEV float member_pdf(const DeviceScene& S, const DevMember& mb, float3 o, 
     // triangle
     TriRay tr = make_tri_ray(d);
     float t, b1, b2;
-    if (!hit_triangle(S, mb.index, o, tr, 0.001f, 3.0e38f, t, b1, b2))
+    if (!hit_triangle<false>(S, mb.index, o, tr, 0.001f, 3.0e38f, t, b1, b2))
         return 0.0f;
     const float4* tp = S.tris + 3 * mb.index;
     float3 v0 = f3(ldg4(tp));

@@ -50,7 +50,8 @@ struct WaveParams {
     CameraParams cam;
     RenderBuffers B;
     int max_depth, max_diffuse, max_specular, max_scatter;
-    int transparent_shadows, collect_features, has_lights, has_media;
+    int transparent_shadows, collect_features, has_lights;
+    int keyed;  // rays carry random keys: media, height fog or alpha masks
     unsigned long long seed;
     int pass0, npass;
     int first_row, band_rows;  // the rows rendered: [first_row, first_row + band_rows)
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
         uint32_t slot = q[k];
         float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
         uint64_t key = 0;
-        if (P.has_media) {
+        if (P.keyed) {
             uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
             key = media_key(P, pixel, pass, uint32_t(depth), 0);
         }
@@ -330,7 +331,7 @@ __global__ void __launch_bounds__(256, 3) k_extend_pt(WaveParams P, int depth) {
                     slot = q[k];
                     float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
                     uint64_t key = 0;
-                    if (P.has_media) {
+                    if (P.keyed) {
                         uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
                         key = media_key(P, pixel, pass, uint32_t(depth), 0);
                     }
@@ -598,7 +599,7 @@ __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
         float3 o = f3(so), d = f3(sd);
         uint64_t key = 0;
         uint32_t pixel = 0, pass = 0;
-        if (P.has_media) {
+        if (P.keyed) {
             pixel = f_bits(P.B.radiance[slot].w);
             pass = f_bits(P.B.beta[slot].w);
         }
@@ -607,13 +608,13 @@ __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
             // Nothing the ray can reach emits, and nothing lets it through:
             // only whether it escapes matters (camera.h:488-503). A sky-only
             // sample already holds the sky's radiance (sc.w = 1).
-            if (P.has_media)
+            if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1);
             if (!any_hit<VOX>(S, o, d, 0.001f, 3.0e38f, key))
                 emission = sc.w != 0.0f ? f3(1.0f) : escaped_radiance(S, d, false);
         } else
         for (int hop = 0; hop <= 16; hop++) {
-            if (P.has_media)
+            if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1 + 4 * hop);
             HitInfo h = closest_hit<VOX>(S, o, d, 0.001f, 3.0e38f, key);
             if (h.prim == kMiss) {
@@ -1113,7 +1114,7 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
     P.transparent_shadows = o->transparent_shadows;
     P.collect_features = o->collect_features;
     P.has_lights = G->dev.light_count > 0;
-    P.has_media = G->dev.has_media;
+    P.keyed = G->dev.has_media || G->dev.has_alpha;
     P.seed = o->seed;
     if (size_t(P.cam.width) * P.cam.height > (size_t(1) << 31))
         return bad_arg("mypbr_gpu_render: image too large");
@@ -1711,7 +1712,7 @@ extern "C" int mypbr_gpu_render_noalloc(mypbr_gpu_scene* G, const mypbr_camera* 
     P.transparent_shadows = o->transparent_shadows;
     P.collect_features = o->collect_features;
     P.has_lights = G->dev.light_count > 0;
-    P.has_media = G->dev.has_media;
+    P.keyed = G->dev.has_media || G->dev.has_alpha;
     P.seed = o->seed;
     unsigned char* base = nullptr;
     int s = noalloc_scratch(G->device, &base);

@@ -146,6 +146,13 @@ int validate(const mypbr_flat_scene& F) {
         if ((t.n[0] < 0) != (t.n[1] < 0) || (t.n[0] < 0) != (t.n[2] < 0) || (t.t[0] < 0) != (t.t[1] < 0) ||
             (t.t[0] < 0) != (t.t[2] < 0))
             return bad("triangle " + std::to_string(k) + " mixes present and missing normals or uvs");
+        if (t.flags & MYPBR_TRI_ALPHA_MASK) {
+            if (!in(t.mesh, F.mesh_count))
+                return bad("masked triangle " + std::to_string(k) + " names no mesh");
+            int mask = F.meshes[t.mesh].alpha_mask;
+            if (!in(mask, F.texture_count) || F.textures[mask].type != MYPBR_TEX_IMAGE)
+                return bad("mesh " + std::to_string(t.mesh) + "'s alpha mask is not an image texture");
+        }
     }
     for (int64_t k = 0; k < F.medium_count; k++) {
         const auto& m = F.media[k];
@@ -399,7 +406,16 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
             tris.push_back(make_float4(float(p[0]), float(p[1]), float(p[2]), ibits(w)));
         }
         tri_shading.push_back(make_int4(t.n[0], t.n[1], t.n[2], t.t[0]));
-        tri_shading.push_back(make_int4(t.t[1], t.t[2], -1, -1));
+        // an HDR image is opaque everywhere (texture.h:107-110): no test
+        int mask = -1;
+        if (t.flags & MYPBR_TRI_ALPHA_MASK) {
+            int m = F.meshes[t.mesh].alpha_mask;
+            if (!(F.textures[m].flags & MYPBR_TEXF_HDR)) {
+                mask = m;
+                D.has_alpha = 1;
+            }
+        }
+        tri_shading.push_back(make_int4(t.t[1], t.t[2], mask, -1));
     }
     PUT(tris, D.tris);
     PUT(tri_shading, D.tri_shading);

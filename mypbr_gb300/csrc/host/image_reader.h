@@ -1,0 +1,31 @@
+// Decoding of 8-bit image files for textures: PNG and TGA, to RGBA bytes.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace mypbr_host {
+
+// An 8-bit image as RGBA bytes, rows from the top, with the number of
+// channels the file holds as stb_image counts them (1 grey, 2 grey + alpha,
+// 3 RGB, 4 RGBA; a PNG tRNS chunk adds an alpha channel).
+struct LdrImage {
+    int width = 0, height = 0, channels = 0;
+    std::vector<uint8_t> rgba;
+};
+
+bool decode_png(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
+bool decode_tga(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
+
+// The kind of image file the bytes start with.
+enum class ImageKind { Png, Hdr, Jpeg, Bmp, Gif, Other };
+ImageKind sniff_image(const uint8_t* bytes, size_t size);
+
+bool read_file_bytes(const std::string& path, std::vector<uint8_t>& bytes);
+
+// An 8-bit image file (PNG, or TGA as the fallback for files no signature
+// names, as stb_image tries it last).
+bool read_ldr_image(const std::string& path, LdrImage& out, std::string& error);
+
+}  // namespace mypbr_host

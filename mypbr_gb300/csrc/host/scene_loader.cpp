@@ -24,12 +24,14 @@
 #include <memory>
 #include <sstream>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../../include/mypbr_gpu.h"
 #include "bvh_build.h"
 #include "host_math.h"
 #include "host_scene.h"
+#include "image_reader.h"
 #include "sky_model.h"
 #include "vox_reader.h"
 
@@ -301,6 +303,86 @@ class Loader {
         auto m = blank_material(MYPBR_MAT_LAMBERTIAN);
         m.tex[0] = add_texture_solid(albedo);
         return add_material(m);
+    }
+
+    // ------------------------------------------------------ images
+
+    // What image_texture knows of an 8-bit image beyond its pixels
+    // (texture.h:107-117, 161-181).
+    struct ImageInfo {
+        bool alpha_channel = false, opaque = true, grey = false;
+    };
+    std::map<std::tuple<std::string, bool, bool>, int> image_cache;  // (path, repeat, linear) -> texture
+    std::map<int, ImageInfo> image_info;                              // texture -> 8-bit image facts
+
+    // An image texture from a file, loaded once per (path, repeat, linear):
+    // Radiance HDR as linear floats, PNG or TGA as RGBA bytes (texture.h:67-98).
+    // Returns the texture index, or -1 with err empty if the file is missing or
+    // unreadable, or naming a format this backend does not decode.
+    int load_image(const std::string& file, bool repeat, bool linear, std::string& err) {
+        err.clear();
+        auto key = std::make_tuple(file, repeat, linear);
+        auto hit = image_cache.find(key);
+        if (hit != image_cache.end())
+            return hit->second;
+        std::vector<uint8_t> head;
+        {
+            std::ifstream f(file, std::ios::binary);
+            if (!f)
+                return -1;
+            head.resize(16);
+            f.read(reinterpret_cast<char*>(head.data()), 16);
+            head.resize(size_t(f.gcount()));
+        }
+        mypbr_texture t{};
+        t.type = MYPBR_TEX_IMAGE;
+        t.a = t.b = -1;
+        int flags = (linear ? MYPBR_TEXF_LINEAR : 0) | (repeat ? MYPBR_TEXF_REPEAT : 0);
+        mypbr_host::ImageKind kind = mypbr_host::sniff_image(head.data(), head.size());
+        ImageInfo info;
+        if (kind == mypbr_host::ImageKind::Hdr) {
+            int w, h;
+            std::vector<float> rgb;
+            std::string e;
+            if (!read_hdr(file, w, h, rgb, e))
+                return -1;
+            t.width = w;
+            t.height = h;
+            t.flags = flags | MYPBR_TEXF_HDR;
+            t.offset = int64_t(S.texels_hdr.size() / 3);
+            S.texels_hdr.insert(S.texels_hdr.end(), rgb.begin(), rgb.end());
+        } else {
+            mypbr_host::LdrImage img;
+            std::string e;
+            if (!mypbr_host::read_ldr_image(file, img, e)) {
+                if (kind == mypbr_host::ImageKind::Jpeg || kind == mypbr_host::ImageKind::Bmp ||
+                    kind == mypbr_host::ImageKind::Gif)
+                    err = e;
+                return -1;
+            }
+            // take_ldr (texture.h:161-181): the mask reads the alpha channel,
+            // or the grey level of an image without one
+            info.alpha_channel = img.channels == 2 || img.channels == 4;
+            size_t mask_offset = info.alpha_channel ? 3 : 0;
+            for (size_t k = mask_offset; k < img.rgba.size(); k += 4)
+                if (img.rgba[k] < 255) {
+                    info.opaque = false;
+                    break;
+                }
+            info.grey = img.channels <= 2;
+            for (size_t k = 0; info.grey && k < img.rgba.size(); k += 4)
+                info.grey = img.rgba[k] == img.rgba[k + 1] && img.rgba[k] == img.rgba[k + 2];
+            t.width = img.width;
+            t.height = img.height;
+            t.flags = flags | (info.alpha_channel ? 0 : MYPBR_TEXF_GREY_MASK);
+            t.offset = int64_t(S.texels_ldr.size() / 4);
+            S.texels_ldr.insert(S.texels_ldr.end(), img.rgba.begin(), img.rgba.end());
+        }
+        S.textures.push_back(t);
+        int index = int(S.textures.size()) - 1;
+        image_cache[key] = index;
+        image_info[index] = info;
+        return index;
     }
 
     bool is_emissive(int mat) const { return S.materials[mat].type == MYPBR_MAT_DIFFUSE_LIGHT; }
@@ -634,9 +716,150 @@ class Loader {
         return true;
     }
 
-    // A Wavefront OBJ file (include/obj_loader.h:191-340, without MTL files):
-    // faces triangulated as fans, degenerate triangles dropped, one part per
-    // usemtl material (scene material of that name, else the line's material).
+    // A material of an MTL file with the mask that cuts holes in the
+    // surfaces using it (-1 when they are opaque), obj_loader.h:25-31.
+    struct MtlMaterial {
+        int material = -1, alpha_mask = -1;
+    };
+
+    // Reads an MTL file into result (include/obj_loader.h:33-177): Kd / map_Kd
+    // give a lambertian, a non-black Ks a principled material with roughness
+    // sqrt(sqrt(2 / (Ns + 2))) and ior Ni (1.5 unless above 1), Ke an emissive
+    // one; norm / map_Bump / bump / map_Disp / disp a tangent-space normal map
+    // (grey images under the bump and disp names are height maps, skipped);
+    // map_d, else an alpha channel in map_Kd, the alpha mask. Textures repeat
+    // and are relative to the MTL file; options before a file name are skipped
+    // by taking the last word. An image that cannot be loaded gives a warning
+    // and the plain color. False only if the file cannot be opened.
+    bool load_mtl(const std::string& path, std::map<std::string, MtlMaterial>& result, std::string& err) {
+        std::ifstream file(path);
+        if (!file) {
+            err = "cannot open '" + path + "'";
+            return false;
+        }
+        auto slash = path.find_last_of('/');
+        std::string dir = slash == std::string::npos ? "" : path.substr(0, slash + 1);
+        auto image = [&](const std::string& name, bool linear) {
+            std::string full = name[0] == '/' ? name : dir + name;
+            std::string e;
+            int t = load_image(full, true, linear, e);
+            if (t < 0)
+                std::fprintf(stderr, "Warning: %s: cannot load texture '%s'\n", path.c_str(), full.c_str());
+            return t;
+        };
+        struct Entry {
+            V3 kd{0.8, 0.8, 0.8}, ks{0, 0, 0}, ke{0, 0, 0};
+            double ns = 0, ni = 1.5;
+            int map_kd = -1, map_d = -1, normal_map = -1;
+        };
+        std::vector<std::pair<std::string, Entry>> entries;
+        std::string line;
+        while (std::getline(file, line)) {
+            std::istringstream in(line);
+            std::string keyword;
+            if (!(in >> keyword) || keyword[0] == '#')
+                continue;
+            if (keyword == "newmtl") {
+                std::string name;
+                in >> name;
+                entries.push_back({name, Entry()});
+                continue;
+            }
+            if (entries.empty())
+                continue;
+            Entry& e = entries.back().second;
+            auto read_color = [&](V3& c) {
+                double r, g, b;
+                if (in >> r) {
+                    c = V3(r, r, r);  // one value is grey
+                    if (in >> g >> b)
+                        c = V3(r, g, b);
+                }
+            };
+            auto last_word = [&]() {
+                std::string word, last;
+                while (in >> word)
+                    last = word;
+                return last;
+            };
+            if (keyword == "Kd") {
+                read_color(e.kd);
+            } else if (keyword == "Ks") {
+                read_color(e.ks);
+            } else if (keyword == "Ke") {
+                read_color(e.ke);
+            } else if (keyword == "Ns") {
+                in >> e.ns;
+            } else if (keyword == "Ni") {
+                in >> e.ni;
+            } else if (keyword == "map_Kd") {
+                std::string f = last_word();
+                if (!f.empty())
+                    e.map_kd = image(f, false);
+            } else if (keyword == "map_d") {
+                std::string f = last_word();
+                if (!f.empty())
+                    e.map_d = image(f, false);
+            } else if (keyword == "norm" || keyword == "map_Bump" || keyword == "map_bump" || keyword == "bump" ||
+                       keyword == "map_Disp" || keyword == "disp") {
+                std::string f = last_word();
+                if (f.empty() || !use_normal_maps)
+                    continue;
+                int t = image(f, true);
+                if (t >= 0 && keyword != "norm" && image_info[t].grey) {
+                    std::fprintf(stderr, "Warning: %s: '%s' is a height map; only normal maps are supported\n",
+                                 path.c_str(), f.c_str());
+                    continue;
+                }
+                if (t >= 0)
+                    e.normal_map = t;
+            }
+        }
+        for (auto& [name, e] : entries) {
+            MtlMaterial out;
+            int base = e.map_kd >= 0 ? e.map_kd : -1;
+            bool emits = e.ke.length_squared() > 0;
+            mypbr_material m;
+            if (emits) {
+                m = blank_material(MYPBR_MAT_DIFFUSE_LIGHT);
+                m.p[0] = e.ke.x;
+                m.p[1] = e.ke.y;
+                m.p[2] = e.ke.z;
+                m.p[3] = 180;
+                m.p[4] = kInf;
+                m.p[5] = 1;
+            } else if (e.ks.length_squared() > 0) {
+                double roughness = std::sqrt(std::sqrt(2 / (std::fmax(e.ns, 0.0) + 2)));
+                double ior = e.ni > 1 ? e.ni : 1.5;
+                m = blank_material(MYPBR_MAT_PRINCIPLED);
+                double r0 = (ior - 1) / (ior + 1);
+                m.p[0] = r0 * r0;
+                m.tex[0] = base >= 0 ? base : add_texture_solid(e.kd);
+                m.tex[1] = add_texture_solid(V3(0, 0, 0));
+                m.tex[2] = add_texture_solid(V3(roughness, roughness, roughness));
+                m.p[13] = m.p[14] = m.p[15] = 1;
+            } else {
+                m = blank_material(MYPBR_MAT_LAMBERTIAN);
+                m.tex[0] = base >= 0 ? base : add_texture_solid(e.kd);
+            }
+            // normal_mapped wraps the surface materials, not lights (obj_loader.h:166-167)
+            if (e.normal_map >= 0 && !emits)
+                m.normal_map = e.normal_map;
+            out.material = add_material(m);
+            if (e.map_d >= 0 && !image_info[e.map_d].opaque)
+                out.alpha_mask = e.map_d;
+            else if (e.map_d < 0 && e.map_kd >= 0 && image_info[e.map_kd].alpha_channel && !image_info[e.map_kd].opaque)
+                out.alpha_mask = e.map_kd;
+            result[name] = out;
+        }
+        return true;
+    }
+
+    // A Wavefront OBJ file (include/obj_loader.h:191-340): faces triangulated
+    // as fans, degenerate triangles dropped, one part per usemtl surface: the
+    // scene material of that name, else the MTL material of that name (from
+    // the mtllib files read so far, with its alpha mask), else the line's
+    // material.
     bool add_obj(const std::string& file, bool smooth, int line_mat, const Xf& xform, bool transformed) {
         std::ifstream in(file);
         if (!in) {
@@ -647,9 +870,13 @@ class Loader {
         struct Face {
             int v[3], n[3], t[3];
         };
-        std::vector<int> part_order;
-        std::map<int, std::vector<Face>> faces;
-        int current = line_mat;
+        using Surface = std::pair<int, int>;  // (material, alpha mask texture or -1)
+        std::vector<Surface> part_order;
+        std::map<Surface, std::vector<Face>> faces;
+        Surface current{line_mat, -1};
+        std::map<std::string, MtlMaterial> file_materials;
+        auto slash = file.find_last_of('/');
+        std::string obj_dir = slash == std::string::npos ? "" : file.substr(0, slash + 1);
         auto resolve = [](long index, size_t count) -> int {
             if (index > 0 && size_t(index) <= count)
                 return int(index - 1);
@@ -735,12 +962,26 @@ class Loader {
                 name.erase(0, name.find_first_not_of(" \t"));
                 name.erase(name.find_last_not_of(" \t\r") + 1);
                 auto it = materials.find(name);
-                current = it != materials.end() ? it->second : line_mat;
+                auto mtl = file_materials.find(name);
+                if (it != materials.end())
+                    current = {it->second, -1};
+                else if (mtl != file_materials.end())
+                    current = {mtl->second.material, mtl->second.alpha_mask};
+                else
+                    current = {line_mat, -1};
+            } else if (line.compare(size_t(s - line.c_str()), 6, "mtllib") == 0) {
+                // usually one file name; several are allowed
+                std::string names(s + 6);
+                std::istringstream list(names);
+                std::string name, mtl_error;
+                while (list >> name)
+                    if (!load_mtl(name[0] == '/' ? name : obj_dir + name, file_materials, mtl_error))
+                        std::fprintf(stderr, "Warning: %s: %s\n", file.c_str(), mtl_error.c_str());
             }
         }
         if (smooth && nrm.empty()) {
             nrm.assign(pos.size(), V3());
-            for (int pm : part_order)
+            for (const Surface& pm : part_order)
                 for (auto& f : faces[pm]) {
                     const V3& p0 = pos[f.v[0]];
                     V3 n = cross(pos[f.v[1]] - p0, pos[f.v[2]] - p0);
@@ -754,8 +995,8 @@ class Loader {
             error = "'" + file + "' has no faces";
             return false;
         }
-        for (int pm : part_order)
-            if (!check_light_xform(pm, xform, transformed))
+        for (const Surface& pm : part_order)
+            if (!check_light_xform(pm.first, xform, transformed))
                 return false;
 
         // Vertex data in world space; normals by the inverse transpose, kept
@@ -779,12 +1020,14 @@ class Loader {
         }
         bool flip = transformed && xform.det() < 0;
         double area_scale = transformed ? xform.area_scale() : 1.0;
-        for (int pm : part_order) {
-            const auto& fs = faces[pm];
+        for (const Surface& surface : part_order) {
+            const auto& fs = faces[surface];
+            const int pm = surface.first, mask = surface.second;
             mypbr_mesh mesh{};
             mesh.first_triangle = int64_t(S.triangles.size());
             mesh.triangle_count = int64_t(fs.size());
             mesh.material = pm;
+            mesh.alpha_mask = mask;
             S.meshes.push_back(mesh);
             int mesh_index = int(S.meshes.size()) - 1;
             Box part_box;
@@ -804,7 +1047,7 @@ class Loader {
                 if (t.t[0] < 0 || t.t[1] < 0 || t.t[2] < 0)
                     t.t[0] = t.t[1] = t.t[2] = -1;
                 t.material = pm;
-                t.flags = flip ? MYPBR_TRI_FLIP_NORMAL : 0;
+                t.flags = (flip ? MYPBR_TRI_FLIP_NORMAL : 0) | (mask >= 0 ? MYPBR_TRI_ALPHA_MASK : 0);
                 t.mesh = mesh_index;
                 S.triangles.push_back(t);
                 int ti = int(S.triangles.size()) - 1;
@@ -1107,29 +1350,16 @@ class Loader {
             }
             if (file[0] != '/')
                 file = scene_dir + file;
-            auto ends_with = [&](const char* suf) {
-                size_t n = std::strlen(suf);
-                return file.size() >= n && file.compare(file.size() - n, n, suf) == 0;
-            };
-            if (!ends_with(".hdr")) {
-                unsupported = true;
-                return fail("image texture '" + file + "': only .hdr images are read by this backend");
-            }
-            int w, h;
-            std::vector<float> rgb;
             std::string err;
-            if (!read_hdr(file, w, h, rgb, err))
+            int index = load_image(file, false, linear, err);
+            if (index < 0) {
+                if (!err.empty()) {
+                    unsupported = true;
+                    return fail("image texture '" + file + "': " + err);
+                }
                 return fail("cannot load image '" + file + "'");
-            mypbr_texture t{};
-            t.type = MYPBR_TEX_IMAGE;
-            t.a = t.b = -1;
-            t.width = w;
-            t.height = h;
-            t.flags = MYPBR_TEXF_HDR | (linear ? MYPBR_TEXF_LINEAR : 0);
-            t.offset = int64_t(S.texels_hdr.size() / 3);
-            S.texels_hdr.insert(S.texels_hdr.end(), rgb.begin(), rgb.end());
-            S.textures.push_back(t);
-            textures[name] = int(S.textures.size()) - 1;
+            }
+            textures[name] = index;
         } else {
             return fail("unknown texture type '" + type + "'");
         }
@@ -2128,6 +2358,39 @@ int mypbr_ggx_albedo_table(double* out) {
         return MYPBR_ERR_INVALID_ARGUMENT;
     }
     ggx_albedo_table(out);
+    return MYPBR_OK;
+}
+
+int mypbr_image_read(const char* path, int32_t* width, int32_t* height, int32_t* channels, uint8_t* rgba,
+                     int64_t capacity) {
+    if (!path || !width || !height || !channels) {
+        set_error("mypbr_image_read: null argument");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    clear_error();
+    mypbr_host::LdrImage img;
+    std::string err;
+    if (!mypbr_host::read_ldr_image(path, img, err)) {
+        std::vector<uint8_t> probe;
+        bool readable = mypbr_host::read_file_bytes(path, probe);
+        set_error("cannot load image '" + std::string(path) + "': " + err);
+        if (!readable)
+            return MYPBR_ERR_IO;
+        auto kind = mypbr_host::sniff_image(probe.data(), probe.size());
+        bool other_format = kind == mypbr_host::ImageKind::Jpeg || kind == mypbr_host::ImageKind::Bmp ||
+                            kind == mypbr_host::ImageKind::Gif || kind == mypbr_host::ImageKind::Hdr;
+        return other_format ? MYPBR_ERR_UNSUPPORTED : MYPBR_ERR_BAD_SCENE;
+    }
+    *width = img.width;
+    *height = img.height;
+    *channels = img.channels;
+    if (rgba) {
+        if (capacity < int64_t(img.rgba.size())) {
+            set_error("mypbr_image_read: the buffer holds fewer than width * height * 4 bytes");
+            return MYPBR_ERR_INVALID_ARGUMENT;
+        }
+        std::memcpy(rgba, img.rgba.data(), img.rgba.size());
+    }
     return MYPBR_OK;
 }
 

@@ -53,7 +53,7 @@ DTYPES = {
     "triangles": np.dtype([("v", "<i4", 3), ("n", "<i4", 3), ("t", "<i4", 3), ("material", "<i4"),
                            ("flags", "<i4"), ("mesh", "<i4")]),
     "meshes": np.dtype([("first_triangle", "<i8"), ("triangle_count", "<i8"), ("material", "<i4"),
-                        ("reserved", "<i4")]),
+                        ("alpha_mask", "<i4")]),
     "media": np.dtype([("shape", "<i4"), ("xform", "<i4"), ("material", "<i4"), ("reserved", "<i4"),
                        ("density", "<f8"), ("a", "<f8", 3), ("b", "<f8", 3)]),
     "xforms": np.dtype([("m", "<f8", (3, 3)), ("t", "<f8", 3), ("inv_m", "<f8", (3, 3)), ("inv_t", "<f8", 3)]),

@@ -285,8 +285,35 @@ bool hit_quad(const Scene& S, int i, const V& o, const V& d, double tmin, double
 
 V pos(const Scene& S, int k) { return V(S.f->positions + 3 * int64_t(k)); }
 
-// mesh.h:47-108 (Moller-Trumbore; alpha masks are not part of the flat scene)
-bool hit_triangle(const Scene& S, int i, const V& o, const V& d, double tmin, double tmax, Hit& rec) {
+// image_texture::alpha_value (texture.h:129-135) of the mask of a triangle
+// flagged MYPBR_TRI_ALPHA_MASK: the alpha byte, or the grey level of an image
+// without an alpha channel, at the nearest pixel (texture.h:184-197), / 255.
+// An HDR image is opaque.
+double alpha_coverage(const Scene& S, const mypbr_triangle& tr, double u, double v) {
+    const mypbr_texture& tx = S.f->textures[S.f->meshes[tr.mesh].alpha_mask];
+    if (tx.flags & MYPBR_TEXF_HDR)
+        return 1;
+    if (tx.flags & MYPBR_TEXF_REPEAT) {
+        u -= std::floor(u);
+        v -= std::floor(v);
+    } else {
+        u = std::fmin(std::fmax(u, 0.0), 1.0);
+        v = std::fmin(std::fmax(v, 0.0), 1.0);
+    }
+    v = 1.0 - v;
+    int x = std::clamp(int(u * tx.width), 0, tx.width - 1);
+    int y = std::clamp(int(v * tx.height), 0, tx.height - 1);
+    int64_t k = tx.offset + int64_t(y) * tx.width + x;
+    return S.f->texels_ldr[4 * k + ((tx.flags & MYPBR_TEXF_GREY_MASK) ? 0 : 3)] / 255.0;
+}
+
+// mesh.h:47-108 (Moller-Trumbore). An alpha-masked triangle is met with
+// probability equal to its coverage (mesh.h:81-86), decided with g; without
+// g (queries that draw no random numbers) it is there wherever the coverage
+// is above 0, and with masked false it is solid (light sampling densities,
+// whose holes are ignored like the power estimate's, mesh.h:138).
+bool hit_triangle(const Scene& S, int i, const V& o, const V& d, double tmin, double tmax, Hit& rec,
+                  Rng* rng = nullptr, bool masked = true) {
     const auto& tr = S.f->triangles[i];
     V p0 = pos(S, tr.v[0]);
     V e1 = pos(S, tr.v[1]) - p0, e2 = pos(S, tr.v[2]) - p0;
@@ -317,6 +344,12 @@ bool hit_triangle(const Scene& S, int i, const V& o, const V& d, double tmin, do
         V uv = b0 * uv0 + b1 * uv1 + b2 * uv2;
         u = uv.x;
         v = uv.y;
+    }
+    // checked before rec changes: a miss keeps the closest hit so far
+    if (masked && (tr.flags & MYPBR_TRI_ALPHA_MASK)) {
+        double coverage = alpha_coverage(S, tr, u, v);
+        if (coverage < 1 && (rng ? rng->next() >= coverage : coverage <= 0))
+            return false;
     }
     rec.t = t;
     rec.u = u;
@@ -630,7 +663,7 @@ bool hit_prim(const Scene& S, int kind, int index, const V& o, const V& d, doubl
     switch (kind) {
         case MYPBR_PRIM_SPHERE: h = hit_sphere(S, index, o, d, tmin, tmax, rec); break;
         case MYPBR_PRIM_QUAD: h = hit_quad(S, index, o, d, tmin, tmax, rec); break;
-        case MYPBR_PRIM_TRIANGLE: h = hit_triangle(S, index, o, d, tmin, tmax, rec); break;
+        case MYPBR_PRIM_TRIANGLE: h = hit_triangle(S, index, o, d, tmin, tmax, rec, g); break;
         case MYPBR_PRIM_MEDIUM: h = g ? hit_medium(S, index, o, d, tmin, tmax, rec, *g) : false; break;
         case MYPBR_PRIM_VOXEL_BLOCK: h = hit_voxel_block(S, index, o, d, tmin, tmax, rec); break;
         default: break;
@@ -1557,7 +1590,7 @@ double member_pdf(const Scene& S, const mypbr_light_member& mb, const V& o, cons
             return d2 / (cosine * area);
         }
         case MYPBR_PRIM_TRIANGLE: {
-            if (!hit_triangle(S, mb.prim_index, o, d, 0.001, INF, rec))
+            if (!hit_triangle(S, mb.prim_index, o, d, 0.001, INF, rec, nullptr, false))
                 return 0;
             const auto& tr = S.f->triangles[mb.prim_index];
             V p0 = pos(S, tr.v[0]);

@@ -18,6 +18,7 @@
 //   denoise <w> <h> <seed> <out>      denoiser::run on a seeded frame
 //   post   <w> <h> <seed> <out>       postprocess + display_settings::apply + to_byte on a seeded image
 //   sky    <w> <h> <out>              atmosphere::bake and sun_transmittance for four suns and settings
+//   image  <file> <out>               image_texture's decoding of an 8-bit file (stb_image)
 #include <bvh.h>
 #include <denoiser.h>
 #include <scene.h>
@@ -453,6 +454,33 @@ int cmd_sky(int argc, char** argv) {
     return 0;
 }
 
+// image <file> <out>: how image_texture reads an 8-bit file (texture.h:67-98,
+// 161-181): stb_image's width, height and channel count, the texture's
+// has_alpha_channel / fully_opaque / greyscale, then the RGBA bytes (as
+// doubles) — or a single -1 if stb_image cannot decode the file.
+int cmd_image(int argc, char** argv) {
+    if (argc < 4)
+        return 2;
+    Out out(argv[3]);
+    int w, h, channels;
+    unsigned char* data = stbi_load(argv[2], &w, &h, &channels, 4);
+    if (!data) {
+        out.put(-1.0);
+        return 0;
+    }
+    image_texture tex(argv[2], false, false);
+    out.put(double(w));
+    out.put(double(h));
+    out.put(double(channels));
+    out.put(tex.has_alpha_channel() ? 1.0 : 0.0);
+    out.put(tex.fully_opaque() ? 1.0 : 0.0);
+    out.put(tex.greyscale() ? 1.0 : 0.0);
+    for (size_t k = 0; k < size_t(w) * h * 4; k++)
+        out.put(double(data[k]));
+    stbi_image_free(data);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -471,6 +499,7 @@ int main(int argc, char** argv) {
     else if (c == "denoise") rc = cmd_denoise(argc, argv);
     else if (c == "post") rc = cmd_post(argc, argv);
     else if (c == "sky") rc = cmd_sky(argc, argv);
+    else if (c == "image") rc = cmd_image(argc, argv);
     if (rc == 2)
         std::cerr << "bad arguments for '" << c << "'\n";
     return rc;

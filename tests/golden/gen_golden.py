@@ -230,6 +230,7 @@ RENDERS = [
     ("materials.scene", 64, 64, 16),
     ("voxels.scene", 48, 64, 16),
     ("voxels_style.scene", 48, 64, 16),
+    ("alpha_masks.scene", 48, 64, 16),
 ]
 
 
@@ -288,8 +289,62 @@ def gen_sky():
                         pdf=recs[1 + n:].reshape(-1, 7)[:, 6])
 
 
+def make_mask_fixtures():
+    """The textures of masks.mtl (alpha_masks.scene)."""
+    sys.path.insert(0, HERE)
+    from image_fixtures import write_png, write_tga
+    n = 16
+    y, x = np.mgrid[0:n, 0:n]
+    r = np.hypot(x - 7.5, y - 7.5)
+    leaf = np.zeros((n, n, 4), dtype=np.int64)
+    leaf[..., 0] = 40 + 8 * x
+    leaf[..., 1] = 150 + 4 * y
+    leaf[..., 2] = 60
+    leaf[..., 3] = np.where(r < 5, 255, np.where(r < 7, 128, 0))  # solid disk, half-covered ring, holes
+    write_png(os.path.join(SCENES, "leaf.png"), leaf, 6, 8)
+    veil = (x * 255 // (n - 1))[..., None]  # coverage 0 at the left edge to 1 at the right
+    write_png(os.path.join(SCENES, "veil.png"), veil, 0, 8)
+    paint = np.zeros((8, 8, 4), dtype=np.uint8)
+    yy, xx = np.mgrid[0:8, 0:8]
+    paint[..., 0] = np.where((xx + yy) % 2 == 0, 220, 30)
+    paint[..., 1] = 90
+    paint[..., 2] = np.where((xx + yy) % 2 == 0, 40, 200)
+    paint[..., 3] = 255
+    write_tga(os.path.join(SCENES, "paint.tga"), paint, 2, 24)
+    tilt = np.zeros((8, 8, 3), dtype=np.int64)
+    tilt[..., 0] = np.where(xx < 4, 170, 90)
+    tilt[..., 1] = 128
+    tilt[..., 2] = 235
+    write_png(os.path.join(SCENES, "ripples.png"), tilt, 2, 8)
+    write_png(os.path.join(SCENES, "height.png"), ((xx * 30) % 256)[..., None], 0, 8)
+    opaque = np.zeros((4, 4, 4), dtype=np.int64)
+    opaque[..., 0] = 200
+    opaque[..., 1] = 180
+    opaque[..., 2] = 40
+    opaque[..., 3] = 255
+    write_png(os.path.join(SCENES, "opaque_alpha.png"), opaque, 6, 8)
+
+
+def gen_images():
+    """stb_image's decoding (through image_texture) of every image fixture."""
+    sys.path.insert(0, HERE)
+    from image_fixtures import make_image_fixtures
+    folder = os.path.join(HERE, "images")
+    names = make_image_fixtures(folder)
+    out = {}
+    for name in names:
+        raw = run("image", os.path.join(folder, name))
+        if raw[0] < 0:
+            raise RuntimeError(f"stb_image cannot decode {name}")
+        w, h = int(raw[0]), int(raw[1])
+        out[name + ":meta"] = raw[:6].astype(np.int32)
+        out[name + ":rgba"] = raw[6:].astype(np.uint8).reshape(h, w, 4)
+    np.savez_compressed(os.path.join(HERE, "images.npz"), **out)
+
+
 GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_env, "ggx": gen_ggx,
-          "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post, "sky": gen_sky}
+          "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post, "sky": gen_sky,
+          "images": gen_images}
 
 if __name__ == "__main__":
     ref = os.environ.get("REFERENCE", "/root/reference")
@@ -298,6 +353,8 @@ if __name__ == "__main__":
         make_env_fixture()
     if not os.path.exists(os.path.join(SCENES, "voxels.vox")):
         make_vox_fixtures()
+    if not os.path.exists(os.path.join(SCENES, "leaf.png")):
+        make_mask_fixtures()
     args = sys.argv[1:]
     if args[:1] == ["render"] and len(args) > 1:  # render <scene> ...: only those renders
         gen_render(args[1:])

@@ -1,0 +1,221 @@
+"""Small PNG and TGA writers for the image-decoding fixtures.
+
+Every PNG color type and bit depth (grey 1/2/4/8/16, RGB 8/16, palette
+1/2/4/8, grey + alpha 8/16, RGBA 8/16), tRNS keys and palette alphas, Adam7
+interlacing, all five scanline filters and stored / fixed / dynamic deflate
+blocks; TGA true color (15/16, 24, 32 bit), grey and color-mapped images,
+plain and run-length coded, bottom-up and top-down. The pixel values are
+seeded, so the files are reproducible.
+"""
+import os
+import struct
+import zlib
+
+import numpy as np
+
+ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
+CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
+
+
+def _chunk(kind, data):
+    return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+
+def _pack_row(samples, depth):
+    if depth == 8:
+        return bytes(int(s) for s in samples)
+    if depth == 16:
+        return b"".join(struct.pack(">H", int(s)) for s in samples)
+    out, acc, used = bytearray(), 0, 0
+    for s in samples:
+        acc = (acc << depth) | int(s)
+        used += depth
+        if used == 8:
+            out.append(acc)
+            acc, used = 0, 0
+    if used:
+        out.append(acc << (8 - used))
+    return bytes(out)
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    if pa <= pb and pa <= pc:
+        return a
+    return b if pb <= pc else c
+
+
+def _filter(kind, row, prev, bpp):
+    out = bytearray([kind])
+    for i, x in enumerate(row):
+        a = row[i - bpp] if i >= bpp else 0
+        b = prev[i]
+        c = prev[i - bpp] if i >= bpp else 0
+        pred = [0, a, b, (a + b) // 2, _paeth(a, b, c)][kind]
+        out.append((x - pred) & 255)
+    return bytes(out)
+
+
+def write_png(path, samples, ctype, depth, palette=None, trns=None, interlace=False, level=6):
+    """samples: (H, W, channels) integers at the file's depth (palette indices for ctype 3)."""
+    h, w = samples.shape[:2]
+    ch = CHANNELS[ctype]
+    bpp = max(1, ch * depth // 8)
+    raw = bytearray()
+    passes = ADAM7 if interlace else [(0, 0, 1, 1)]
+    for p, (x0, y0, dx, dy) in enumerate(passes):
+        sub = samples[y0::dy, x0::dx]
+        if sub.shape[0] == 0 or sub.shape[1] == 0:
+            continue
+        prev = bytes(len(_pack_row(sub[0].reshape(-1), depth)))
+        for y in range(sub.shape[0]):
+            row = _pack_row(sub[y].reshape(-1), depth)
+            raw += _filter((y + p) % 5, row, prev, bpp)
+            prev = row
+    data = b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, int(interlace)))
+    if palette is not None:
+        data += _chunk(b"PLTE", bytes(np.asarray(palette, dtype=np.uint8).reshape(-1)))
+    if trns is not None:
+        data += _chunk(b"tRNS", bytes(trns))
+    comp = zlib.compress(bytes(raw), level)
+    # two IDAT chunks: the stream may be split anywhere
+    half = len(comp) // 2
+    data += _chunk(b"IDAT", comp[:half]) + _chunk(b"IDAT", comp[half:]) + _chunk(b"IEND", b"")
+    with open(path, "wb") as f:
+        f.write(data)
+
+
+def _tga_pixels(rgba, bits):
+    """Pixel bytes of a TGA true-color / grey image, from RGBA rows (bottom row first handled by caller)."""
+    px = []
+    for r, g, b, a in rgba.reshape(-1, 4):
+        if bits == 32:
+            px.append(bytes([b, g, r, a]))
+        elif bits == 24:
+            px.append(bytes([b, g, r]))
+        elif bits in (15, 16):
+            v = ((int(r) >> 3) << 10) | ((int(g) >> 3) << 5) | (int(b) >> 3)
+            px.append(struct.pack("<H", v))
+        else:
+            px.append(bytes([r]))
+    return px
+
+
+def _rle(px):
+    out, i = bytearray(), 0
+    while i < len(px):
+        run = 1
+        while i + run < len(px) and run < 128 and px[i + run] == px[i]:
+            run += 1
+        if run >= 2:
+            out.append(0x80 | (run - 1))
+            out += px[i]
+            i += run
+            continue
+        j = i + 1
+        while j < len(px) and j - i < 128 and not (j + 1 < len(px) and px[j + 1] == px[j]):
+            j += 1
+        out.append(j - i - 1)
+        for k in range(i, j):
+            out += px[k]
+        i = j
+    return bytes(out)
+
+
+def write_tga(path, rgba, kind, bits, top_first=False, rle=False, palette=None, image_id=b""):
+    """rgba: (H, W, 4) bytes; kind 1 (color-mapped: rgba holds indices in channel 0), 2 (true color), 3 (grey)."""
+    h, w = rgba.shape[:2]
+    rows = rgba if top_first else rgba[::-1]
+    if kind == 1:
+        px = [bytes([int(i)]) for i in rows[..., 0].reshape(-1)]
+        pal = b"".join(bytes([b, g, r]) for r, g, b in np.asarray(palette, dtype=np.uint8))
+        cmap = (1, 0, len(palette), 24)
+        depth = 8
+    else:
+        px = _tga_pixels(rows, bits)
+        pal = b""
+        cmap = (0, 0, 0, 0)
+        depth = bits
+    alpha_bits = 8 if bits == 32 else (1 if bits == 16 else 0)
+    desc = alpha_bits | (0x20 if top_first else 0)
+    head = struct.pack("<BBBHHBHHHHBB", len(image_id), cmap[0], kind + (8 if rle else 0), cmap[1], cmap[2],
+                       cmap[3], 0, 0, w, h, depth, desc)
+    body = _rle(px) if rle else b"".join(px)
+    with open(path, "wb") as f:
+        f.write(head + image_id + pal + body + b"\0" * 8 + b"TRUEVISION-XFILE.\0")
+
+
+def make_image_fixtures(folder):
+    """Writes the fixture set into folder; returns the file names."""
+    os.makedirs(folder, exist_ok=True)
+    rng = np.random.default_rng(2024)
+    names = []
+    w, h = 13, 7  # odd sizes: partial bytes at low depths, empty Adam7 passes
+
+    def grad(maxv, ch):
+        y, x = np.mgrid[0:h, 0:w]
+        base = np.stack([(x * 7 + y * 3 + c * 5) % (maxv + 1) for c in range(ch)], axis=-1)
+        noise = rng.integers(0, maxv + 1, size=(h, w, ch))
+        pick = rng.random((h, w, 1)) < 0.3
+        return np.where(pick, noise, base)
+
+    def png(name, *args, **kw):
+        write_png(os.path.join(folder, name), *args, **kw)
+        names.append(name)
+
+    for depth in (1, 2, 4, 8, 16):
+        png(f"grey{depth}.png", grad((1 << depth) - 1, 1), 0, depth)
+    png("grey8_key.png", grad(255, 1), 0, 8, trns=struct.pack(">H", 21))
+    png("grey4_key_interlaced.png", grad(15, 1), 0, 4, trns=struct.pack(">H", 3), interlace=True)
+    png("rgb8.png", grad(255, 3), 2, 8)
+    png("rgb16.png", grad(65535, 3), 2, 16)
+    rgb = grad(255, 3)
+    rgb[2, 3] = rgb[5, 9] = (10, 20, 30)
+    png("rgb8_key.png", rgb, 2, 8, trns=struct.pack(">HHH", 10, 20, 30))
+    for depth in (1, 2, 4, 8):
+        n = 1 << depth
+        pal = rng.integers(0, 256, size=(n, 3))
+        png(f"palette{depth}.png", grad(n - 1, 1), 3, depth, palette=pal)
+    pal = rng.integers(0, 256, size=(16, 3))
+    png("palette4_trns.png", grad(15, 1), 3, 4, palette=pal, trns=bytes([0, 128, 255, 7, 64]))
+    png("palette2_interlaced.png", grad(3, 1), 3, 2, palette=pal[:4], interlace=True)
+    png("ga8.png", grad(255, 2), 4, 8)
+    png("ga16.png", grad(65535, 2), 4, 16)
+    png("rgba8.png", grad(255, 4), 6, 8)
+    png("rgba16.png", grad(65535, 4), 6, 16)
+    png("rgba8_interlaced.png", grad(255, 4), 6, 8, interlace=True)
+    opaque = grad(255, 4)
+    opaque[..., 3] = 255
+    png("rgba8_opaque.png", opaque, 6, 8)
+    grey_rgb = np.repeat(grad(255, 1), 3, axis=-1)
+    png("rgb8_grey_values.png", grey_rgb, 2, 8)
+    png("ga8_opaque.png", np.concatenate([grad(255, 1), np.full((h, w, 1), 255)], axis=-1), 4, 8)
+    png("rgb8_stored.png", grad(255, 3), 2, 8, level=0)
+    # a larger image: dynamic Huffman blocks and long back-references
+    y, x = np.mgrid[0:96, 0:80]
+    big = np.stack([(x * 3) % 256, (y * 2) % 256, ((x + y) * 5) % 256, np.where((x // 8 + y // 8) % 2 == 0, 255, 40)],
+                   axis=-1)
+    write_png(os.path.join(folder, "rgba8_large.png"), big, 6, 8, level=9)
+    names.append("rgba8_large.png")
+
+    def tga(name, *args, **kw):
+        write_tga(os.path.join(folder, name), *args, **kw)
+        names.append(name)
+
+    rgba = grad(255, 4).astype(np.uint8)
+    tga("true24.tga", rgba, 2, 24)
+    tga("true32_top.tga", rgba, 2, 32, top_first=True)
+    runs = rgba.copy()
+    runs[1:4, :, :] = (200, 100, 50, 128)
+    tga("true32_rle.tga", runs, 2, 32, rle=True)
+    tga("true24_rle_top.tga", runs, 2, 24, rle=True, top_first=True, image_id=b"fixture")
+    tga("true16.tga", rgba, 2, 16)
+    tga("grey8.tga", rgba, 3, 8)
+    tga("grey8_rle.tga", runs, 3, 8, rle=True)
+    idx = grad(11, 1).astype(np.uint8)
+    idx4 = np.concatenate([idx, idx, idx, idx], axis=-1)
+    pal = rng.integers(0, 256, size=(12, 3))
+    tga("mapped8.tga", idx4, 1, 8, palette=pal)
+    tga("mapped8_rle.tga", idx4, 1, 8, rle=True, palette=pal, top_first=True)
+    return names

@@ -90,6 +90,34 @@ def test_trace_matches_oracle_and_reference(scene_name, golden, scale):
     np.testing.assert_array_equal(hits[both, 6], ohits[both, 6])
 
 
+def test_trace_alpha_masks_match_oracle():
+    """Queries carry no random numbers: a masked triangle is there wherever
+    its coverage is above 0, on the device as in the oracle. Rays aim at the
+    leaf (holes, a half-covered ring) and the veil (a coverage ramp)."""
+    sc, G = gpu_scene("alpha_masks")
+    rng = np.random.default_rng(11)
+    n = 6000
+    target = np.where(rng.random((n, 1)) < 0.5,
+                      np.column_stack([rng.uniform(-1.8, -0.3, n), rng.uniform(0.2, 1.7, n), np.zeros(n)]),
+                      np.column_stack([rng.uniform(0.2, 1.7, n), rng.uniform(0.2, 1.7, n), np.full(n, 0.3)]))
+    origin = np.column_stack([rng.uniform(-1, 1, n), rng.uniform(0.5, 1.5, n), np.full(n, 5.0)])
+    rays = np.zeros((n, 8))
+    rays[:, 0:3] = origin
+    rays[:, 3:6] = target - origin
+    rays[:, 6] = 0.001
+    rays[:, 7] = 3e38
+    rays = rays.astype(np.float32).astype(np.float64)
+    O = orc.OracleScene(sc)
+    ohits, oprim = O.trace(rays)
+    hits, prim = G.trace(rays.astype(np.float32))
+    ok = stable_mask(O, rays, 3.0)
+    assert ok.mean() > 0.97, ok.mean()
+    np.testing.assert_array_equal(prim[ok], oprim[ok])
+    # both the holes and the masked surfaces were met
+    tri = oprim[ok, 0] == 2
+    assert 0.2 < tri.mean() < 0.9, tri.mean()
+
+
 def test_bsdf_matches_reference():
     sc, G = gpu_scene("bsdf_probe")
     b = load_golden("bsdf_probe")
@@ -219,7 +247,8 @@ def render_gpu(name, width, spp, seed=7):
     return rad, chv
 
 
-@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style"])
+@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style",
+                                  "alpha_masks"])
 def test_render_matches_reference(name):
     g = load_golden(f"render_{name}")
     rad, var = render_gpu(name, g["mean"].shape[1], 1024)

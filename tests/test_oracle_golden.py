@@ -159,7 +159,8 @@ def render_z(rad, var, g):
     return z, tot_z
 
 
-@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style"])
+@pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style",
+                                  "alpha_masks"])
 def test_oracle_render_matches_reference_render(name):
     """Per-pixel means within 3 sigma of the combined Monte Carlo error, for
     the oracle vs the reference's batch means."""
