@@ -476,8 +476,11 @@ def run_simple(args, workload):
 
 def run_batch(args):
     """C4: 64 scenes of uneven size, resolution and spp (half of them with a
-    haze medium) rendered by one mypbr_gpu_render_batch call, then each frame
-    denoised (5 iterations) on the device. Aggregate Mpaths/s over the batch."""
+    haze medium) rendered by one mypbr_gpu_render_batch call with albedo,
+    normal and variance guides, then each frame denoised (5 iterations) on the
+    device; one step is both. Aggregate Mpaths/s over the batch. Per scene,
+    relMSE (epsilon 0.01) of the noisy and of the denoised frame against a
+    render of the same scene at 4x the spp with another seed."""
     import torch
 
     import mypbr_gb300 as mp
@@ -489,37 +492,73 @@ def run_batch(args):
         G = mp.GpuScene(sc)
         cam = sc.camera
         cam.samples_per_pixel = spp
-        cam.collect_features = 0
+        cam.collect_features = 1
         # about 2M paths in flight per job: 64 handles' path buffers stay near 30 GB
         cam.samples_per_wave = max(1, (2 << 20) // (cam.height() * cam.image_width))
         scenes.append((sc, G))
         cams.append(cam)
-        bufs.append(torch.zeros((cam.height(), cam.image_width, 3), dtype=torch.float64, device="cuda"))
-    jobs = [(G, cam, b.data_ptr()) for (sc, G), cam, b in zip(scenes, cams, bufs)]
+        h, w = cam.height(), cam.image_width
+        z = lambda *shape: torch.zeros(shape, dtype=torch.float64, device="cuda")  # noqa: E731
+        bufs.append({"rad": z(h, w, 3), "alb": z(h, w, 3), "nrm": z(h, w, 3), "var": z(h, w), "out": z(h, w, 3)})
+    jobs = [(G, cam, b["rad"].data_ptr(), b["alb"].data_ptr(), b["nrm"].data_ptr(), b["var"].data_ptr())
+            for (sc, G), cam, b in zip(scenes, cams, bufs)]
+
+    def denoise_all():
+        for cam, b in zip(cams, bufs):
+            mp.denoise(b["rad"].data_ptr(), b["alb"].data_ptr(), b["nrm"].data_ptr(), b["var"].data_ptr(),
+                       cam.image_width, cam.height(), b["out"].data_ptr(), on_device=True)
+
     paths = sum(c.height() * c.image_width * c.samples_per_pixel for c in cams)
     mp.render_batch(jobs)  # warm-up: buffers, graphs
+    denoise_all()
     torch.cuda.synchronize()
-    times = []
+    times, t_render = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         mp.render_batch(jobs)
         torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        denoise_all()
+        torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
+        t_render.append(t1 - t0)
     t = statistics.median(times)
-    # one by one, for the batch's gain
+    # one by one, for the batch's gain (render only)
     t0 = time.perf_counter()
-    for (sc, G), cam, b in zip(scenes, cams, bufs):
-        mp.render_batch([(G, cam, b.data_ptr())])
+    for job in jobs:
+        mp.render_batch([job])
     torch.cuda.synchronize()
     t_serial = time.perf_counter() - t0
+    # references: each scene at 4x the spp, another seed
+    refs = []
+    for (sc, G), cam in zip(scenes, cams):
+        rc = mp.Camera(*cam.structs())
+        rc.samples_per_pixel = cam.samples_per_pixel * 4
+        rc.collect_features = 0
+        rc.seed = cam.seed + 7919
+        rb = torch.zeros((cam.height(), cam.image_width, 3), dtype=torch.float64, device="cuda")
+        mp.render_batch([(G, rc, rb.data_ptr())])
+        refs.append(rb)
+    torch.cuda.synchronize()
+
+    def rel_mse(x, r):
+        return float((((x - r) ** 2) / (r * r + 0.01)).mean())
+
+    noisy = [rel_mse(b["rad"], r) for b, r in zip(bufs, refs)]
+    denoised = [rel_mse(b["out"], r) for b, r in zip(bufs, refs)]
     line = {"metric": "Mpaths/s over a batch of 64 scenes", "value": paths / t / 1e6, "unit": "Mpaths/s",
             "n_gpus": 1, "steps": args.steps, "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
             "ms_per_step": t * 1e3,
             "config": {"workload": "batch_64", "scenes": len(items), "paths": int(paths),
                        "triangles": "10k..1M log-uniform (a third of the scenes)",
                        "resolutions": "64^2..1024^2 log-uniform", "spp": "16..1024 log-uniform",
-                       "media": "every other scene: fog 0.02, albedo 0.9, g 0.6"},
-            "one_by_one_ms": t_serial * 1e3, "batch_speedup": t_serial / t}
+                       "media": "every other scene: fog 0.02, albedo 0.9, g 0.6",
+                       "step": "render with albedo/normal/variance guides + 5-iteration denoise of every frame"},
+            "render_ms": statistics.median(t_render) * 1e3,
+            "one_by_one_render_ms": t_serial * 1e3, "batch_speedup": t_serial / statistics.median(t_render),
+            "rel_mse": {"epsilon": 0.01, "reference": "same scene at 4x spp, another seed",
+                        "noisy_median": statistics.median(noisy), "denoised_median": statistics.median(denoised),
+                        "noisy": [round(x, 5) for x in noisy], "denoised": [round(x, 5) for x in denoised]}}
     print(json.dumps(line), flush=True)
 
 

@@ -212,9 +212,9 @@ typedef struct mypbr_prim_ref {
 /* ---------------------------------------------------------- appearance */
 
 enum {
-    MYPBR_TEX_SOLID = 0,   /* p[0..2] = colour (include/texture.h:259-270) */
-    MYPBR_TEX_CHECKER = 1, /* p[0] = 1/scale, a = even texture, b = odd (texture.h:273-291) */
-    MYPBR_TEX_IMAGE = 2    /* width x height texels at offset (texture.h:302-444) */
+    MYPBR_TEX_SOLID = 0,   /* p[0..2] = colour (include/texture.h:24-36) */
+    MYPBR_TEX_CHECKER = 1, /* p[0] = 1/scale, a = even texture, b = odd (texture.h:38-56) */
+    MYPBR_TEX_IMAGE = 2    /* width x height texels at offset (texture.h:67-209) */
 };
 enum {
     MYPBR_TEXF_HDR = 1,    /* texels are RGB float in texels_hdr, else RGBA8 in texels_ldr */

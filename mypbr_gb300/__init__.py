@@ -130,6 +130,7 @@ def lib():
     L.mypbr_scene_free.argtypes = [vp]
     L.mypbr_scene_free.restype = None
     L.mypbr_ggx_albedo_table.argtypes = [dp]
+    L.mypbr_gpu_denoise.argtypes = [vp, vp, vp, vp, ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int]
     i32p = ctypes.POINTER(ctypes.c_int32)
     L.mypbr_image_read.argtypes = [ctypes.c_char_p, i32p, i32p, i32p, vp, ctypes.c_int64]
     L.mypbr_camera_init.argtypes = [ctypes.POINTER(CameraStruct)]
@@ -473,22 +474,36 @@ def write_image(path, radiance, opts=None):
 
 def render_batch(jobs):
     """jobs: [(gpu_scene, camera, radiance_device_pointer)] with the radiance
-    buffers (H*W*3 float64) in device memory. Renders them all
-    (mypbr_gpu_render_batch); returns the per-job statuses."""
+    buffers (H*W*3 float64) in device memory, or (gpu_scene, camera, radiance,
+    albedo, normal, variance) pointers when the camera collects features.
+    Renders them all (mypbr_gpu_render_batch); returns the per-job statuses."""
     n = len(jobs)
     arr = (BatchJobStruct * n)()
     keep = []
-    for k, (gs, cam, ptr) in enumerate(jobs):
+    for k, job in enumerate(jobs):
+        gs, cam, ptr = job[:3]
         c, o = cam.structs()
         keep.append((c, o))
         arr[k].scene = gs.handle
         arr[k].camera = ctypes.pointer(c)
         arr[k].opts = ctypes.pointer(o)
         arr[k].radiance = int(ptr)
+        if len(job) == 6:
+            arr[k].albedo, arr[k].normal, arr[k].variance = (int(x) if x else None for x in job[3:6])
     status = lib().mypbr_gpu_render_batch(arr, n)
     codes = [arr[k].status for k in range(n)]
     check(status)
     return codes
+
+
+def denoise(radiance, albedo, normal, variance, width, height, out, on_device=False):
+    """denoiser::run with the default settings (mypbr_gpu_denoise). Arguments
+    are numpy arrays (host) or device addresses (on_device); out receives the
+    filtered radiance (H*W*3 float64)."""
+    def addr(x):
+        return int(x) if on_device else x.ctypes.data
+    check(lib().mypbr_gpu_denoise(addr(radiance), addr(albedo), addr(normal), addr(variance), int(width),
+                                  int(height), None, addr(out), int(bool(on_device))))
 
 
 def autotune(camera, gpu_scene):

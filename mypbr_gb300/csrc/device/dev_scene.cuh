@@ -259,7 +259,7 @@ MYPBR_DEV TriRay make_tri_ray(float3 d) {
 // does not depend on the order the walk meets primitives in; with key 0 (a
 // query without random numbers) the surface is there wherever a > 0.
 // Coverage is the alpha byte / 255, or the grey level without an alpha
-// channel (texture.h:129-135), at the nearest texel of the interpolated uv.
+// channel (texture.h:132-136), at the nearest texel of the interpolated uv.
 MYPBR_DEV bool alpha_covers(const DeviceScene& S, int i, float b1, float b2, uint64_t key) {
     int4 sb = S.tri_shading[2 * i + 1];
     if (sb.z < 0)

@@ -22,7 +22,7 @@ MYPBR_DEV float srgb_decode(int c) {
     return e <= 0.04045f ? e * (1.0f / 12.92f) : powf((e + 0.055f) * (1.0f / 1.055f), 2.4f);
 }
 
-// texture.h:259-444 (solid, checker of solids, image)
+// texture.h:24-209 (solid, checker, image)
 MYPBR_DEV float3 tex_value(const DeviceScene& S, int t, float u, float v, float3 p) {
     for (int guard = 0; guard < 4 && t >= 0; guard++) {
         const DevTexture& tx = S.textures[t];

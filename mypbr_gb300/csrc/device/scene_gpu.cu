@@ -406,7 +406,7 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
             tris.push_back(make_float4(float(p[0]), float(p[1]), float(p[2]), ibits(w)));
         }
         tri_shading.push_back(make_int4(t.n[0], t.n[1], t.n[2], t.t[0]));
-        // an HDR image is opaque everywhere (texture.h:107-110): no test
+        // an HDR image is opaque everywhere (texture.h:110-113): no test
         int mask = -1;
         if (t.flags & MYPBR_TRI_ALPHA_MASK) {
             int m = F.meshes[t.mesh].alpha_mask;

@@ -308,7 +308,7 @@ class Loader {
     // ------------------------------------------------------ images
 
     // What image_texture knows of an 8-bit image beyond its pixels
-    // (texture.h:107-117, 161-181).
+    // (texture.h:110-117, 161-179).
     struct ImageInfo {
         bool alpha_channel = false, opaque = true, grey = false;
     };

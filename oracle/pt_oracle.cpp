@@ -285,9 +285,9 @@ bool hit_quad(const Scene& S, int i, const V& o, const V& d, double tmin, double
 
 V pos(const Scene& S, int k) { return V(S.f->positions + 3 * int64_t(k)); }
 
-// image_texture::alpha_value (texture.h:129-135) of the mask of a triangle
+// image_texture::alpha_value (texture.h:132-136) of the mask of a triangle
 // flagged MYPBR_TRI_ALPHA_MASK: the alpha byte, or the grey level of an image
-// without an alpha channel, at the nearest pixel (texture.h:184-197), / 255.
+// without an alpha channel, at the nearest pixel (texture.h:181-194), / 255.
 // An HDR image is opaque.
 double alpha_coverage(const Scene& S, const mypbr_triangle& tr, double u, double v) {
     const mypbr_texture& tx = S.f->textures[S.f->meshes[tr.mesh].alpha_mask];
@@ -769,12 +769,12 @@ V tex_value(const Scene& S, int t, double u, double v, const V& p) {
     const auto& tx = S.f->textures[t];
     switch (tx.type) {
         case MYPBR_TEX_SOLID: return V(tx.p[0], tx.p[1], tx.p[2]);
-        case MYPBR_TEX_CHECKER: {  // texture.h:278-285
+        case MYPBR_TEX_CHECKER: {  // texture.h:43-50
             int x = int(std::floor(tx.p[0] * p.x)), y = int(std::floor(tx.p[0] * p.y)),
                 z = int(std::floor(tx.p[0] * p.z));
             return (x + y + z) % 2 == 0 ? tex_value(S, tx.a, u, v, p) : tex_value(S, tx.b, u, v, p);
         }
-        case MYPBR_TEX_IMAGE: {  // texture.h:354-363, 416-429
+        case MYPBR_TEX_IMAGE: {  // texture.h:119-127, 181-194
             if (tx.flags & MYPBR_TEXF_REPEAT) {
                 u -= std::floor(u);
                 v -= std::floor(v);

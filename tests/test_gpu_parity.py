@@ -112,6 +112,10 @@ def test_trace_alpha_masks_match_oracle():
     hits, prim = G.trace(rays.astype(np.float32))
     ok = stable_mask(O, rays, 3.0)
     assert ok.mean() > 0.97, ok.mean()
+    # triangles 8 and 9 of masks.obj are one triangle with both windings (an
+    # exact tie: either answer is right)
+    for p in (prim, oprim):
+        p[(p[:, 0] == 2) & (p[:, 1] == 9), 1] = 8
     np.testing.assert_array_equal(prim[ok], oprim[ok])
     # both the holes and the masked surfaces were met
     tri = oprim[ok, 0] == 2
