@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define MYPBR_ABI_VERSION 1
+#define MYPBR_ABI_VERSION 2
 
 /* ------------------------------------------------------------------ status */
 
@@ -214,7 +214,13 @@ typedef struct mypbr_prim_ref {
 enum {
     MYPBR_TEX_SOLID = 0,   /* p[0..2] = colour (include/texture.h:24-36) */
     MYPBR_TEX_CHECKER = 1, /* p[0] = 1/scale, a = even texture, b = odd (texture.h:38-56) */
-    MYPBR_TEX_IMAGE = 2    /* width x height texels at offset (texture.h:67-209) */
+    MYPBR_TEX_IMAGE = 2,   /* width x height texels at offset (texture.h:67-209) */
+    /* Wrappers of texture a (a < this texture's index, chains at most 6 deep): */
+    MYPBR_TEX_SCALED = 3,       /* p[0..2] x a (scaled_texture, texture.h:212-225) */
+    MYPBR_TEX_CHANNEL = 4,      /* grey p[0] x channel b (0 red, 1 green, 2 blue) of a (texture.h:228-245) */
+    MYPBR_TEX_UV_TRANSFORM = 5, /* a at moved (u, v): offset p[0..1], rotation p[2] radians, scale p[3..4]
+                                   (KHR_texture_transform, uv_transform_texture, texture.h:248-267) */
+    MYPBR_TEX_NORMAL_SCALE = 6  /* encoded normal of a with its tilt times p[0] (texture.h:270-282) */
 };
 enum {
     MYPBR_TEXF_HDR = 1,    /* texels are RGB float in texels_hdr, else RGBA8 in texels_ldr */
@@ -228,7 +234,7 @@ typedef struct mypbr_texture {
     int32_t width, height;
     int32_t flags;
     int64_t offset; /* first texel (ldr: byte offset / 4 per texel; hdr: float offset / 3) */
-    double p[4];
+    double p[6];
 } mypbr_texture;
 
 enum {

@@ -54,7 +54,7 @@ struct DevMaterial {
 struct DevTexture {
     int type, a, b, width, height, flags;
     long long offset;
-    float p[4];
+    float p[8];  // the ABI's six parameters (uv transforms: cos and sin of the rotation in p[2], p[5])
 };
 
 struct DevLight {

@@ -22,38 +22,77 @@ MYPBR_DEV float srgb_decode(int c) {
     return e <= 0.04045f ? e * (1.0f / 12.92f) : powf((e + 0.055f) * (1.0f / 1.055f), 2.4f);
 }
 
-// texture.h:24-209 (solid, checker, image)
+// texture.h:24-282: solid, checker and image textures, and the wrappers
+// around them (scaled, channel, uv transform, normal scale). A chain holds at
+// most two wrappers that change the value (checked at upload); they apply
+// innermost first once the plain texture's value is known.
 MYPBR_DEV float3 tex_value(const DeviceScene& S, int t, float u, float v, float3 p) {
-    for (int guard = 0; guard < 4 && t >= 0; guard++) {
+    int outer0 = -1, outer1 = -1;
+    float3 c = f3(0.0f);
+    for (int guard = 0; guard < 8 && t >= 0; guard++) {
         const DevTexture& tx = S.textures[t];
-        if (tx.type == 0)
-            return f3(tx.p[0], tx.p[1], tx.p[2]);
+        if (tx.type == 0) {
+            c = f3(tx.p[0], tx.p[1], tx.p[2]);
+            break;
+        }
         if (tx.type == 1) {
             int x = int(floorf(tx.p[0] * p.x)), y = int(floorf(tx.p[0] * p.y)), z = int(floorf(tx.p[0] * p.z));
             t = ((x + y + z) % 2 == 0) ? tx.a : tx.b;
             continue;
         }
-        if (tx.flags & 4) {
-            u -= floorf(u);
-            v -= floorf(v);
+        if (tx.type == 2) {
+            if (tx.flags & 4) {
+                u -= floorf(u);
+                v -= floorf(v);
+            } else {
+                u = clampf(u, 0.0f, 1.0f);
+                v = clampf(v, 0.0f, 1.0f);
+            }
+            v = 1.0f - v;
+            int i = min(max(int(u * tx.width), 0), tx.width - 1);
+            int j = min(max(int(v * tx.height), 0), tx.height - 1);
+            long long k = tx.offset + (long long)j * tx.width + i;
+            if (tx.flags & 1) {
+                const float* px = S.texels_hdr + 3 * k;
+                c = f3(px[0], px[1], px[2]);
+            } else {
+                const uint8_t* px = S.texels_ldr + 4 * k;
+                if (tx.flags & 2)
+                    c = f3(px[0], px[1], px[2]) * (1.0f / 255.0f);
+                else
+                    c = f3(srgb_decode(px[0]), srgb_decode(px[1]), srgb_decode(px[2]));
+            }
+            break;
+        }
+        if (tx.type == 5) {
+            // uv_transform_texture::value (texture.h:255-259), in glTF's
+            // coordinates where v runs down the image; p[2], p[5] = cos, sin
+            float su = tx.p[3] * u, sv = tx.p[4] * (1.0f - v);
+            float tu = tx.p[2] * su + tx.p[5] * sv + tx.p[0];
+            float tv = -tx.p[5] * su + tx.p[2] * sv + tx.p[1];
+            u = tu;
+            v = 1.0f - tv;
+        } else if (outer0 < 0) {
+            outer0 = t;
         } else {
-            u = clampf(u, 0.0f, 1.0f);
-            v = clampf(v, 0.0f, 1.0f);
+            outer1 = t;
         }
-        v = 1.0f - v;
-        int i = min(max(int(u * tx.width), 0), tx.width - 1);
-        int j = min(max(int(v * tx.height), 0), tx.height - 1);
-        long long k = tx.offset + (long long)j * tx.width + i;
-        if (tx.flags & 1) {
-            const float* px = S.texels_hdr + 3 * k;
-            return f3(px[0], px[1], px[2]);
-        }
-        const uint8_t* px = S.texels_ldr + 4 * k;
-        if (tx.flags & 2)
-            return f3(px[0], px[1], px[2]) * (1.0f / 255.0f);
-        return f3(srgb_decode(px[0]), srgb_decode(px[1]), srgb_decode(px[2]));
+        t = tx.a;
     }
-    return f3(0.0f);
+    for (int k = 0; k < 2; k++) {
+        int o = k == 0 ? outer1 : outer0;
+        if (o < 0)
+            continue;
+        const DevTexture& tx = S.textures[o];
+        if (tx.type == 3) {
+            c = c * f3(tx.p[0], tx.p[1], tx.p[2]);
+        } else if (tx.type == 4) {
+            c = f3(tx.p[0] * comp(c, tx.b));
+        } else {
+            c = f3(0.5f + tx.p[0] * (c.x - 0.5f), 0.5f + tx.p[0] * (c.y - 0.5f), c.z);
+        }
+    }
+    return c;
 }
 
 // ------------------------------------------------------- microfacet model

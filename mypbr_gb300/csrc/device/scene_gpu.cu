@@ -109,10 +109,25 @@ int validate(const mypbr_flat_scene& F) {
     }
     for (int64_t k = 0; k < nt; k++) {
         const auto& t = F.textures[k];
+        auto plain = [&](int c) {
+            return in(c, nt) && (F.textures[c].type == MYPBR_TEX_SOLID || F.textures[c].type == MYPBR_TEX_IMAGE);
+        };
         if (t.type == MYPBR_TEX_CHECKER) {
-            if (!in(t.a, nt) || !in(t.b, nt) || F.textures[t.a].type == MYPBR_TEX_CHECKER ||
-                F.textures[t.b].type == MYPBR_TEX_CHECKER)
+            if (!plain(t.a) || !plain(t.b))
                 return bad("checker texture " + std::to_string(k) + " must pick between two plain textures");
+        } else if (t.type >= MYPBR_TEX_SCALED && t.type <= MYPBR_TEX_NORMAL_SCALE) {
+            // wrappers name an earlier texture, so chains end; at most 6
+            // deep, with at most two that change the value
+            int depth = 0, value_ops = 0;
+            for (int64_t c = k; c >= 0 && F.textures[c].type >= MYPBR_TEX_SCALED; c = F.textures[c].a) {
+                if (!(F.textures[c].a >= 0 && F.textures[c].a < c) || ++depth > 6)
+                    return bad("texture " + std::to_string(k) + " wraps a missing or later texture, or too deep");
+                value_ops += F.textures[c].type != MYPBR_TEX_UV_TRANSFORM;
+            }
+            if (value_ops > 2)
+                return bad("texture " + std::to_string(k) + " stacks more than two scaling wrappers");
+            if (t.type == MYPBR_TEX_CHANNEL && (t.b < 0 || t.b > 2))
+                return bad("channel texture " + std::to_string(k) + " names no color channel");
         } else if (t.type == MYPBR_TEX_IMAGE) {
             int64_t texels = int64_t(t.width) * t.height;
             if (t.width <= 0 || t.height <= 0 || t.offset < 0)
@@ -564,8 +579,12 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
         d.height = t.height;
         d.flags = t.flags;
         d.offset = t.offset;
-        for (int p = 0; p < 4; p++)
+        for (int p = 0; p < 6; p++)
             d.p[p] = float(t.p[p]);
+        if (t.type == MYPBR_TEX_UV_TRANSFORM) {
+            d.p[2] = float(std::cos(t.p[2]));
+            d.p[5] = float(std::sin(t.p[2]));
+        }
         texs.push_back(d);
     }
     PUT(texs, D.textures);

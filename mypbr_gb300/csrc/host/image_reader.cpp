@@ -271,9 +271,13 @@ bool read_ldr_image(const std::string& path, LdrImage& out, std::string& error) 
         error = "cannot open '" + path + "'";
         return false;
     }
-    switch (sniff_image(bytes.data(), bytes.size())) {
-        case ImageKind::Png: return decode_png(bytes.data(), bytes.size(), out, error);
-        case ImageKind::Other: return decode_tga(bytes.data(), bytes.size(), out, error);
+    return decode_ldr_image(bytes.data(), bytes.size(), out, error);
+}
+
+bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error) {
+    switch (sniff_image(bytes, size)) {
+        case ImageKind::Png: return decode_png(bytes, size, out, error);
+        case ImageKind::Other: return decode_tga(bytes, size, out, error);
         case ImageKind::Jpeg: error = "JPEG images are not decoded by this backend"; return false;
         case ImageKind::Bmp: error = "BMP images are not decoded by this backend"; return false;
         case ImageKind::Gif: error = "GIF images are not decoded by this backend"; return false;

@@ -27,5 +27,6 @@ bool read_file_bytes(const std::string& path, std::vector<uint8_t>& bytes);
 // An 8-bit image file (PNG, or TGA as the fallback for files no signature
 // names, as stb_image tries it last).
 bool read_ldr_image(const std::string& path, LdrImage& out, std::string& error);
+bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
 
 }  // namespace mypbr_host

@@ -22,6 +22,7 @@
 #include <fstream>
 #include <map>
 #include <memory>
+#include <set>
 #include <sstream>
 #include <string>
 #include <tuple>
@@ -31,10 +32,12 @@
 #include "bvh_build.h"
 #include "host_math.h"
 #include "host_scene.h"
+#include "gltf_reader.h"
 #include "image_reader.h"
 #include "sky_model.h"
 #include "vox_reader.h"
 
+#include <algorithm>
 #include <array>
 
 using namespace mypbr_host;
@@ -55,12 +58,8 @@ void clear_error() { g_last_error.clear(); }
 // Reads a Radiance RGBE (.hdr) image as linear RGB floats, row 0 at the top.
 // Each pixel is mantissa * 2^(exponent - 136) per channel (exponent 0 is
 // black); scanlines may be flat or use the newer per-channel run-length code.
-bool read_hdr(const std::string& path, int& width, int& height, std::vector<float>& rgb, std::string& error) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) {
-        error = "cannot open '" + path + "'";
-        return false;
-    }
+bool decode_hdr(std::istream& f, const std::string& path, int& width, int& height, std::vector<float>& rgb,
+                std::string& error) {
     std::string line;
     if (!std::getline(f, line) || (line.rfind("#?RADIANCE", 0) != 0 && line.rfind("#?RGBE", 0) != 0)) {
         error = "'" + path + "' is not a Radiance .hdr file";
@@ -164,6 +163,15 @@ bool read_hdr(const std::string& path, int& width, int& height, std::vector<floa
         }
     }
     return true;
+}
+
+bool read_hdr(const std::string& path, int& width, int& height, std::vector<float>& rgb, std::string& error) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) {
+        error = "cannot open '" + path + "'";
+        return false;
+    }
+    return decode_hdr(f, path, width, height, rgb, error);
 }
 
 // --------------------------------------------------------- Fresnel helpers
@@ -305,6 +313,18 @@ class Loader {
         return add_material(m);
     }
 
+    // principled(base, metallic, roughness, ior) without a coat (material.h:346-387)
+    static mypbr_material principled_desc(int base, int metallic, int roughness, double ior) {
+        auto m = blank_material(MYPBR_MAT_PRINCIPLED);
+        double r0 = (ior - 1) / (ior + 1);
+        m.p[0] = r0 * r0;
+        m.tex[0] = base;
+        m.tex[1] = metallic;
+        m.tex[2] = roughness;
+        m.p[13] = m.p[14] = m.p[15] = 1;
+        return m;
+    }
+
     // ------------------------------------------------------ images
 
     // What image_texture knows of an 8-bit image beyond its pixels
@@ -325,26 +345,31 @@ class Loader {
         auto hit = image_cache.find(key);
         if (hit != image_cache.end())
             return hit->second;
-        std::vector<uint8_t> head;
-        {
-            std::ifstream f(file, std::ios::binary);
-            if (!f)
-                return -1;
-            head.resize(16);
-            f.read(reinterpret_cast<char*>(head.data()), 16);
-            head.resize(size_t(f.gcount()));
-        }
+        std::vector<uint8_t> bytes;
+        if (!mypbr_host::read_file_bytes(file, bytes))
+            return -1;
+        int index = add_image(bytes, repeat, linear, err);
+        if (index >= 0)
+            image_cache[key] = index;
+        return index;
+    }
+
+    // An image texture from an image file's bytes (a file, or one held in a
+    // glTF buffer); -1 as load_image says.
+    int add_image(const std::vector<uint8_t>& bytes, bool repeat, bool linear, std::string& err) {
+        err.clear();
         mypbr_texture t{};
         t.type = MYPBR_TEX_IMAGE;
         t.a = t.b = -1;
         int flags = (linear ? MYPBR_TEXF_LINEAR : 0) | (repeat ? MYPBR_TEXF_REPEAT : 0);
-        mypbr_host::ImageKind kind = mypbr_host::sniff_image(head.data(), head.size());
+        mypbr_host::ImageKind kind = mypbr_host::sniff_image(bytes.data(), bytes.size());
         ImageInfo info;
         if (kind == mypbr_host::ImageKind::Hdr) {
             int w, h;
             std::vector<float> rgb;
             std::string e;
-            if (!read_hdr(file, w, h, rgb, e))
+            std::istringstream in(std::string(bytes.begin(), bytes.end()));
+            if (!decode_hdr(in, "image", w, h, rgb, e))
                 return -1;
             t.width = w;
             t.height = h;
@@ -354,7 +379,7 @@ class Loader {
         } else {
             mypbr_host::LdrImage img;
             std::string e;
-            if (!mypbr_host::read_ldr_image(file, img, e)) {
+            if (!mypbr_host::decode_ldr_image(bytes.data(), bytes.size(), img, e)) {
                 if (kind == mypbr_host::ImageKind::Jpeg || kind == mypbr_host::ImageKind::Bmp ||
                     kind == mypbr_host::ImageKind::Gif)
                     err = e;
@@ -380,9 +405,41 @@ class Loader {
         }
         S.textures.push_back(t);
         int index = int(S.textures.size()) - 1;
-        image_cache[key] = index;
         image_info[index] = info;
         return index;
+    }
+
+    // A 1 x 1 white image whose alpha is the coverage: a constant mask
+    // (texture.h:100-106, glTF's baseColorFactor alpha without a texture).
+    int coverage_image(double coverage) {
+        uint8_t a = uint8_t(std::lround(255 * std::clamp(coverage, 0.0, 1.0)));
+        mypbr_texture t{};
+        t.type = MYPBR_TEX_IMAGE;
+        t.a = t.b = -1;
+        t.width = t.height = 1;
+        t.offset = int64_t(S.texels_ldr.size() / 4);
+        for (uint8_t b : {uint8_t(255), uint8_t(255), uint8_t(255), a})
+            S.texels_ldr.push_back(b);
+        S.textures.push_back(t);
+        int index = int(S.textures.size()) - 1;
+        ImageInfo info;
+        info.alpha_channel = true;
+        info.opaque = a == 255;
+        image_info[index] = info;
+        return index;
+    }
+
+    // A wrapper texture around inner (MYPBR_TEX_SCALED ... NORMAL_SCALE).
+    int wrap_texture(int type, int inner, std::initializer_list<double> p, int b = -1) {
+        mypbr_texture t{};
+        t.type = type;
+        t.a = inner;
+        t.b = b;
+        int k = 0;
+        for (double x : p)
+            t.p[k++] = x;
+        S.textures.push_back(t);
+        return int(S.textures.size()) - 1;
     }
 
     bool is_emissive(int mat) const { return S.materials[mat].type == MYPBR_MAT_DIFFUSE_LIGHT; }
@@ -860,6 +917,11 @@ class Loader {
     // scene material of that name, else the MTL material of that name (from
     // the mtllib files read so far, with its alpha mask), else the line's
     // material.
+    struct Face {
+        int v[3], n[3], t[3];
+    };
+    using Surface = std::pair<int, int>;  // (material, alpha mask texture or -1)
+
     bool add_obj(const std::string& file, bool smooth, int line_mat, const Xf& xform, bool transformed) {
         std::ifstream in(file);
         if (!in) {
@@ -867,10 +929,6 @@ class Loader {
             return false;
         }
         std::vector<V3> pos, nrm, uv;
-        struct Face {
-            int v[3], n[3], t[3];
-        };
-        using Surface = std::pair<int, int>;  // (material, alpha mask texture or -1)
         std::vector<Surface> part_order;
         std::map<Surface, std::vector<Face>> faces;
         Surface current{line_mat, -1};
@@ -995,6 +1053,218 @@ class Loader {
             error = "'" + file + "' has no faces";
             return false;
         }
+        return add_mesh_parts(pos, nrm, uv, part_order, faces, xform, transformed);
+    }
+
+    // A glTF 2.0 model (gltf_loader.h:59-363): its metallic-roughness
+    // materials mapped onto principled / thin glass / emissive ones, base
+    // color alpha as a coverage mask, one part per surface. override_mat >= 0
+    // replaces every material (a clay render); replace swaps materials by
+    // name. Warnings and the list of features left out go to stderr.
+    bool add_gltf(const std::string& file, int override_mat, const std::map<std::string, int>& replace,
+                  const Xf& xform, bool transformed) {
+        mypbr_host::GltfModel g;
+        if (!mypbr_host::read_gltf(file, g, error))
+            return false;
+        for (const auto& r : replace) {
+            bool found = false;
+            for (const auto& m : g.materials)
+                found = found || m.name == r.first;
+            if (!found) {
+                error = "'" + file + "' has no material named '" + r.first + "'";
+                return false;
+            }
+        }
+        std::set<std::string>& ignored = g.ignored;
+        // images once per (image, linear): colors as sRGB, data linear
+        std::map<std::pair<int, bool>, int> images;
+        auto image_of = [&](int texture, bool linear) -> int {
+            if (texture < 0 || texture >= int(g.textures.size()))
+                return -1;
+            int im = g.textures[size_t(texture)].image;
+            if (im < 0 || im >= int(g.images.size()))
+                return -1;
+            auto key = std::make_pair(im, linear);
+            auto it = images.find(key);
+            if (it != images.end())
+                return it->second;
+            const auto& src = g.images[size_t(im)];
+            bool repeat = g.textures[size_t(texture)].repeat;
+            std::string e;
+            int t = -1;
+            if (!src.bytes.empty())
+                t = add_image(src.bytes, repeat, linear, e);
+            else if (!src.path.empty())
+                t = load_image(src.path, repeat, linear, e);
+            if (t < 0)
+                std::fprintf(stderr, "Warning: %s: cannot load image '%s'\n", file.c_str(), src.label.c_str());
+            images[key] = t;
+            return t;
+        };
+        // a texture view: the image, moved by KHR_texture_transform
+        auto view = [&](const mypbr_host::GltfTextureRef& r, bool linear) -> int {
+            if (r.texcoord != 0) {
+                ignored.insert("second texture coordinates");
+                return -1;
+            }
+            int t = image_of(r.texture, linear);
+            if (t >= 0 && r.has_transform)
+                t = wrap_texture(MYPBR_TEX_UV_TRANSFORM, t,
+                                 {r.offset[0], r.offset[1], r.rotation, r.scale[0], r.scale[1]});
+            return t;
+        };
+        auto normal_view = [&](const mypbr_host::GltfTextureRef& r) -> int {
+            if (!use_normal_maps)
+                return -1;
+            int t = view(r, true);
+            if (t >= 0 && r.strength != 1)
+                t = wrap_texture(MYPBR_TEX_NORMAL_SCALE, t, {r.strength});
+            return t;
+        };
+        std::map<int, Surface> converted;
+        auto convert = [&](int index) -> Surface {
+            auto it = converted.find(index);
+            if (it != converted.end())
+                return it->second;
+            Surface result{-1, -1};
+            if (index < 0) {
+                // the specification's default material: white, metallic 1, roughness 1
+                result.first = override_mat >= 0
+                                   ? override_mat
+                                   : add_material(principled_desc(add_texture_solid(V3(1, 1, 1)),
+                                                                  add_texture_solid(V3(1, 1, 1)),
+                                                                  add_texture_solid(V3(1, 1, 1)), 1.5));
+                return converted[index] = result;
+            }
+            const auto& m = g.materials[size_t(index)];
+            if (auto r = replace.find(m.name); !m.name.empty() && r != replace.end()) {
+                result.first = r->second;
+                return converted[index] = result;
+            }
+            V3 base_factor(m.base_color[0], m.base_color[1], m.base_color[2]);
+            int base_image = view(m.base_texture, false);
+            if (m.alpha_mode != 0 && !m.base_texture.has_transform) {
+                int image = image_of(m.base_texture.texture, false);
+                double alpha = m.base_color[3];
+                if (image >= 0 && image_info[image].alpha_channel && !image_info[image].opaque) {
+                    result.second = image;
+                    if (alpha < 1)
+                        ignored.insert("alpha factor times an alpha texture (the texture is used alone)");
+                } else if (image < 0 && alpha < 1) {
+                    // a constant coverage: MASK cuts it at alphaCutoff, BLEND keeps it
+                    if (m.alpha_mode == 1)
+                        alpha = alpha >= m.alpha_cutoff ? 1 : 0;
+                    if (alpha < 1)
+                        result.second = coverage_image(alpha);
+                }
+            }
+            if (override_mat >= 0) {
+                result.first = override_mat;
+                return converted[index] = result;
+            }
+            for (const auto& u : m.unsupported)
+                ignored.insert(u);
+            int base = base_image >= 0
+                           ? wrap_texture(MYPBR_TEX_SCALED, base_image, {base_factor.x, base_factor.y, base_factor.z})
+                           : add_texture_solid(base_factor);
+            mypbr_material mat;
+            if (m.has_transmission && m.transmission > 0) {
+                if (m.transmission < 1 || m.roughness > 0)
+                    ignored.insert("partial or rough transmission");
+                mat = blank_material(MYPBR_MAT_THIN_DIELECTRIC);
+                mat.p[0] = m.ior;
+                mat.p[2] = base_factor.x;
+                mat.p[3] = base_factor.y;
+                mat.p[4] = base_factor.z;
+            } else {
+                int metallic, roughness;
+                int mr = view(m.metal_rough_texture, true);
+                if (mr >= 0) {
+                    metallic = wrap_texture(MYPBR_TEX_CHANNEL, mr, {m.metallic}, 2);
+                    roughness = wrap_texture(MYPBR_TEX_CHANNEL, mr, {m.roughness}, 1);
+                } else {
+                    metallic = add_texture_solid(V3(m.metallic, m.metallic, m.metallic));
+                    roughness = add_texture_solid(V3(m.roughness, m.roughness, m.roughness));
+                }
+                mat = principled_desc(base, metallic, roughness, m.ior);
+                mat.tex[3] = normal_view(m.normal_texture);
+                if (m.has_clearcoat && m.clearcoat > 0) {
+                    // weight in red, roughness in green, each times its factor; without
+                    // a clearcoatNormalTexture the coat is not bent
+                    int t = view(m.clearcoat_texture, true);
+                    int weight = t >= 0 ? wrap_texture(MYPBR_TEX_CHANNEL, t, {m.clearcoat}, 0)
+                                        : add_texture_solid(V3(m.clearcoat, m.clearcoat, m.clearcoat));
+                    t = view(m.clearcoat_roughness_texture, true);
+                    double cr = m.clearcoat_roughness;
+                    int coat_rough = t >= 0 ? wrap_texture(MYPBR_TEX_CHANNEL, t, {cr}, 1)
+                                            : add_texture_solid(V3(cr, cr, cr));
+                    mat.flags |= MYPBR_MATF_COAT;
+                    mat.tex[4] = weight;
+                    mat.tex[5] = coat_rough;
+                    mat.tex[6] = normal_view(m.clearcoat_normal_texture);
+                }
+            }
+            V3 emission = V3(m.emissive[0], m.emissive[1], m.emissive[2]) * m.emissive_strength;
+            if (emission.length_squared() > 0) {
+                if (m.emissive_texture.texture >= 0) {
+                    // emissive_surface: glows, but is not sampled as a light
+                    int image = view(m.emissive_texture, false);
+                    if (image >= 0)
+                        mat.emission_tex = wrap_texture(MYPBR_TEX_SCALED, image, {emission.x, emission.y, emission.z});
+                } else {
+                    mat = blank_material(MYPBR_MAT_DIFFUSE_LIGHT);  // a light of the scene
+                    mat.p[0] = emission.x;
+                    mat.p[1] = emission.y;
+                    mat.p[2] = emission.z;
+                    mat.p[3] = 180;
+                    mat.p[4] = kInf;
+                    mat.p[5] = 1;
+                }
+            }
+            result.first = add_material(mat);
+            return converted[index] = result;
+        };
+
+        std::vector<V3> pos, nrm, uv;
+        for (size_t k = 0; k + 2 < g.positions.size(); k += 3)
+            pos.emplace_back(g.positions[k], g.positions[k + 1], g.positions[k + 2]);
+        for (size_t k = 0; k + 2 < g.normals.size(); k += 3)
+            nrm.emplace_back(g.normals[k], g.normals[k + 1], g.normals[k + 2]);
+        for (size_t k = 0; k + 1 < g.uvs.size(); k += 2)
+            uv.emplace_back(g.uvs[k], g.uvs[k + 1], 0);
+        std::vector<Surface> part_order;
+        std::map<Surface, std::vector<Face>> faces;
+        for (const auto& f : g.faces) {
+            Surface sf = convert(f.material);
+            Face face;
+            for (int c = 0; c < 3; c++) {
+                face.v[c] = f.v[c];
+                face.n[c] = f.n[c];
+                face.t[c] = f.t[c];
+            }
+            if (!faces.count(sf))
+                part_order.push_back(sf);
+            faces[sf].push_back(face);
+        }
+        if (!ignored.empty()) {
+            std::string list;
+            for (const auto& what : ignored)
+                list += (list.empty() ? " " : ", ") + what;
+            std::fprintf(stderr, "Note: %s: not supported, left out:%s\n", file.c_str(), list.c_str());
+        }
+        if (part_order.empty()) {
+            error = "'" + file + "' has no triangles";
+            return false;
+        }
+        return add_mesh_parts(pos, nrm, uv, part_order, faces, xform, transformed);
+    }
+
+    // The parts of a mesh file: its vertex data (in the file's space) and its
+    // faces grouped by surface, in the order the surfaces were first used.
+    // Each part is a mesh (mesh.h:175-216); an emissive part is a light.
+    bool add_mesh_parts(const std::vector<V3>& pos, const std::vector<V3>& nrm, const std::vector<V3>& uv,
+                        const std::vector<Surface>& part_order, std::map<Surface, std::vector<Face>>& faces,
+                        const Xf& xform, bool transformed) {
         for (const Surface& pm : part_order)
             if (!check_light_xform(pm.first, xform, transformed))
                 return false;
@@ -1979,17 +2249,36 @@ class Loader {
                 size_t n = std::strlen(suf);
                 return file.size() >= n && file.compare(file.size() - n, n, suf) == 0;
             };
-            if (ends_with(".gltf") || ends_with(".glb")) {
-                unsupported = true;
-                return fail("glTF meshes are not read by this backend");
+            // then any number of "replace <file material> <scene material>" (glTF)
+            std::map<std::string, int> replace;
+            std::streampos mark = tail.tellg();
+            std::string token;
+            while (tail >> token && token == "replace") {
+                std::string from, to;
+                if (!(tail >> from >> to))
+                    return fail("expected 'replace <material in the file> <scene material>'");
+                auto it = materials.find(to);
+                if (it == materials.end())
+                    return fail("unknown material '" + to + "'");
+                replace[from] = it->second;
+                mark = tail.tellg();
             }
+            tail.clear();
+            tail.seekg(mark);
             int mat;
             Xf xform;
             bool transformed;
             error.clear();
             if (!read_tail(tail, mat, xform, transformed))
                 return fail(error);
-            if (!add_obj(file, smooth, mat, xform, transformed))
+            if (!replace.empty() && mat != default_material)
+                return fail("'replace' and a material for the whole mesh can't be used together");
+            bool gltf = ends_with(".gltf") || ends_with(".glb");
+            if (!gltf && !replace.empty())
+                return fail("'replace' is for glTF files (OBJ files take scene materials by usemtl name)");
+            // glTF files bring their own materials: one named on the line replaces them all
+            if (gltf ? !add_gltf(file, mat == default_material ? -1 : mat, replace, xform, transformed)
+                     : !add_obj(file, smooth, mat, xform, transformed))
                 return fail(error);
             std::string extra;
             if (tail >> extra)

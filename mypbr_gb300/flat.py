@@ -65,7 +65,7 @@ DTYPES = {
     "materials": np.dtype([("type", "<i4"), ("flags", "<i4"), ("tex", "<i4", 8), ("normal_map", "<i4"),
                            ("emission_tex", "<i4"), ("p", "<f8", 16)]),
     "textures": np.dtype([("type", "<i4"), ("a", "<i4"), ("b", "<i4"), ("width", "<i4"), ("height", "<i4"),
-                          ("flags", "<i4"), ("offset", "<i8"), ("p", "<f8", 4)]),
+                          ("flags", "<i4"), ("offset", "<i8"), ("p", "<f8", 6)]),
     "texels_ldr": np.dtype("u1"),
     "texels_hdr": np.dtype("<f4"),
     "lights": np.dtype([("kind", "<i4"), ("first_member", "<i4"), ("member_count", "<i4"), ("reserved", "<i4"),

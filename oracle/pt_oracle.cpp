@@ -799,6 +799,23 @@ V tex_value(const Scene& S, int t, double u, double v, const V& p) {
             };
             return V(dec(px[0]), dec(px[1]), dec(px[2]));
         }
+        case MYPBR_TEX_SCALED:  // texture.h:216-218
+            return V(tx.p[0], tx.p[1], tx.p[2]) * tex_value(S, tx.a, u, v, p);
+        case MYPBR_TEX_CHANNEL: {  // texture.h:233-236
+            double x = tx.p[0] * tex_value(S, tx.a, u, v, p)[tx.b];
+            return V(x, x, x);
+        }
+        case MYPBR_TEX_UV_TRANSFORM: {  // texture.h:255-259
+            double c = std::cos(tx.p[2]), s = std::sin(tx.p[2]);
+            double su = tx.p[3] * u, sv = tx.p[4] * (1 - v);
+            double tu = c * su + s * sv + tx.p[0];
+            double tv = -s * su + c * sv + tx.p[1];
+            return tex_value(S, tx.a, tu, 1 - tv, p);
+        }
+        case MYPBR_TEX_NORMAL_SCALE: {  // texture.h:274-277
+            V c = tex_value(S, tx.a, u, v, p);
+            return V(0.5 + tx.p[0] * (c.x - 0.5), 0.5 + tx.p[0] * (c.y - 0.5), c.z);
+        }
     }
     return V(0, 0, 0);
 }

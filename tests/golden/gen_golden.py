@@ -231,6 +231,7 @@ RENDERS = [
     ("voxels.scene", 48, 64, 16),
     ("voxels_style.scene", 48, 64, 16),
     ("alpha_masks.scene", 48, 64, 16),
+    ("gallery.scene", 48, 64, 16),
 ]
 
 
@@ -325,6 +326,14 @@ def make_mask_fixtures():
     write_png(os.path.join(SCENES, "opaque_alpha.png"), opaque, 6, 8)
 
 
+def gen_gltf():
+    """world.hit on the glTF gallery (every hit deterministic: the partial-coverage veil replaced)."""
+    recs = run("hits", scene("gallery_hits.scene"), 6000, 31337).reshape(-1, 18)
+    np.savez_compressed(os.path.join(HERE, "hits_gallery.npz"), o=recs[:, 0:3], d=recs[:, 3:6], hit=recs[:, 6],
+                        t=recs[:, 7], normal=recs[:, 8:11], u=recs[:, 11], v=recs[:, 12], front=recs[:, 13],
+                        p=recs[:, 15:18])
+
+
 def gen_images():
     """stb_image's decoding (through image_texture) of every image fixture."""
     sys.path.insert(0, HERE)
@@ -344,7 +353,7 @@ def gen_images():
 
 GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_env, "ggx": gen_ggx,
           "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post, "sky": gen_sky,
-          "images": gen_images}
+          "images": gen_images, "gltf": gen_gltf}
 
 if __name__ == "__main__":
     ref = os.environ.get("REFERENCE", "/root/reference")
@@ -355,6 +364,10 @@ if __name__ == "__main__":
         make_vox_fixtures()
     if not os.path.exists(os.path.join(SCENES, "leaf.png")):
         make_mask_fixtures()
+    if not os.path.exists(os.path.join(SCENES, "gallery.glb")):
+        sys.path.insert(0, HERE)
+        from gltf_fixtures import make_gltf_fixtures
+        make_gltf_fixtures(SCENES)
     args = sys.argv[1:]
     if args[:1] == ["render"] and len(args) > 1:  # render <scene> ...: only those renders
         gen_render(args[1:])

@@ -48,7 +48,8 @@ def stable_mask(O, rays, scale, trials=4, seed=0):
     return ok
 
 
-@pytest.mark.parametrize("scene_name,golden,scale", [("hits_mix", "hits_mix", 10.0), ("cornell_c1", "hits_cornell", 555.0)])
+@pytest.mark.parametrize("scene_name,golden,scale", [("hits_mix", "hits_mix", 10.0), ("cornell_c1", "hits_cornell", 555.0),
+                                                     ("gallery_hits", "hits_gallery", 4.0)])
 def test_trace_matches_oracle_and_reference(scene_name, golden, scale):
     sc, G = gpu_scene(scene_name)
     g = load_golden(golden)
@@ -252,7 +253,7 @@ def render_gpu(name, width, spp, seed=7):
 
 
 @pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style",
-                                  "alpha_masks"])
+                                  "alpha_masks", "gallery"])
 def test_render_matches_reference(name):
     g = load_golden(f"render_{name}")
     rad, var = render_gpu(name, g["mean"].shape[1], 1024)

@@ -38,7 +38,8 @@ def material_ids(scene):
     return np.array(ids)
 
 
-@pytest.mark.parametrize("scene_name,golden", [("hits_mix", "hits_mix"), ("cornell_c1", "hits_cornell")])
+@pytest.mark.parametrize("scene_name,golden", [("hits_mix", "hits_mix"), ("cornell_c1", "hits_cornell"),
+                                               ("gallery_hits", "hits_gallery")])
 def test_closest_hits_match_reference(scene_name, golden):
     sc = mp.load_scene(scene_path(f"{scene_name}.scene"))
     g = load_golden(golden)
@@ -160,7 +161,7 @@ def render_z(rad, var, g):
 
 
 @pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style",
-                                  "alpha_masks"])
+                                  "alpha_masks", "gallery"])
 def test_oracle_render_matches_reference_render(name):
     """Per-pixel means within 3 sigma of the combined Monte Carlo error, for
     the oracle vs the reference's batch means."""
