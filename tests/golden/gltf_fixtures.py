@@ -150,13 +150,13 @@ def _images(folder):
         out[name] = open(path, "rb").read()
 
     paint = np.stack([40 + 12 * x, 60 + 8 * y, np.full_like(x, 200), np.full_like(x, 255)], axis=-1)
-    png("paint.png", paint, 6)
-    png("metal_rough.png", np.stack([np.zeros_like(x), 30 + 12 * y, np.where(x < 8, 255, 0)], axis=-1), 2)
-    png("bumps.png", np.stack([np.where((x // 4) % 2 == 0, 170, 86), np.full_like(x, 128), np.full_like(x, 230)],
+    png("gallery_paint.png", paint, 6)
+    png("gallery_metal_rough.png", np.stack([np.zeros_like(x), 30 + 12 * y, np.where(x < 8, 255, 0)], axis=-1), 2)
+    png("gallery_bumps.png", np.stack([np.where((x // 4) % 2 == 0, 170, 86), np.full_like(x, 128), np.full_like(x, 230)],
                               axis=-1), 2)
     r = np.hypot(x - 7.5, y - 7.5)
-    png("leaf.png", np.stack([40 + 8 * x, 150 + 4 * y, np.full_like(x, 60), np.where(r < 6, 255, 0)], axis=-1), 6)
-    png("glow.png", np.stack([np.full_like(x, 255), 128 + 8 * y, np.where((x + y) % 2 == 0, 40, 220)], axis=-1), 2)
+    png("gallery_leaf.png", np.stack([40 + 8 * x, 150 + 4 * y, np.full_like(x, 60), np.where(r < 6, 255, 0)], axis=-1), 6)
+    png("gallery_glow.png", np.stack([np.full_like(x, 255), 128 + 8 * y, np.where((x + y) % 2 == 0, 40, 220)], axis=-1), 2)
     return out
 
 
@@ -214,12 +214,12 @@ def make_gltf_fixtures(folder):
     """Writes gallery.glb, gallery.gltf and the image files into folder."""
     os.makedirs(folder, exist_ok=True)
     imgs = _images(folder)
-    names = ["paint.png", "metal_rough.png", "bumps.png", "leaf.png", "glow.png"]
+    names = ["gallery_paint.png", "gallery_metal_rough.png", "gallery_bumps.png", "gallery_leaf.png", "gallery_glow.png"]
     # .glb: the leaf image inside the binary chunk, the rest beside it
     b = _Builder()
     meshes = _mesh_primitives(b)
-    leaf_view = b.view(imgs["leaf.png"])
-    refs = [{"uri": n} if n != "leaf.png" else {"bufferView": leaf_view, "mimeType": "image/png", "name": "leaf"}
+    leaf_view = b.view(imgs["gallery_leaf.png"])
+    refs = [{"uri": n} if n != "gallery_leaf.png" else {"bufferView": leaf_view, "mimeType": "image/png", "name": "leaf"}
             for n in names]
     doc = _document(b, meshes, refs)
     while len(b.bin) % 4:

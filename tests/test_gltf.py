@@ -184,9 +184,9 @@ def test_missing_image_is_a_warning(tmp_path, capfd):
     for name in os.listdir(SCENES):
         if name.startswith("gallery.") or name.endswith(".png"):
             shutil.copy(os.path.join(SCENES, name), tmp_path / name)
-    os.remove(tmp_path / "glow.png")
+    os.remove(tmp_path / "gallery_glow.png")
     f = flat.view(mp.parse_scene("mesh gallery.gltf\n", str(tmp_path)))
-    assert "cannot load image 'glow.png'" in capfd.readouterr().err
+    assert "cannot load image 'gallery_glow.png'" in capfd.readouterr().err
     assert not any(m["emission_tex"] >= 0 for m in f["materials"])
 
 

@@ -64,7 +64,8 @@ def test_scene_errors_name_the_line():
 def test_unsupported_features_are_reported():
     expect_error("vox island.vox\n", 7, "cannot open")
     expect_error("sphere 0 0 0 1\nsky atmosphere mie_g 1.5\n", 7, "expected 'sky atmosphere")
-    expect_error("mesh car.glb\n", 2, "glTF meshes are not read")
+    expect_error("mesh car.glb\n", 7, "cannot read glTF file")  # gltf_loader.h:65-67
+    expect_error("cyclorama 10\n", 2, "not supported by this backend")
 
 
 def test_missing_file_is_io_error():
