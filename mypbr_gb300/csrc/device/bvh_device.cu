@@ -361,9 +361,21 @@ extern "C" int mypbr_gpu_scene_rebuild_bvh(mypbr_gpu_scene* G, int32_t method, m
     // the new tree replaces the old one (whose arrays stay until the handle goes)
     G->allocations.push_back(nodes.p);
     G->allocations.push_back(sorted_refs.p);
+    // and its 4-wide form, when the 4-wide walk's stack can hold it
+    std::vector<float4> wide;
+    int depth4 = 0;
+    collapse_to_4(after, wide, depth4);
+    float4* wide_p = nullptr;
+    if (3 * (depth4 + 1) <= kBvh4Stack) {
+        MYPBR_CUDA(cudaMalloc(&wide_p, wide.size() * sizeof(float4)));
+        MYPBR_CUDA(cudaMemcpy(wide_p, wide.data(), wide.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        G->allocations.push_back(wide_p);
+    }
     D.bvh = nodes.p;
     D.leaf_refs = sorted_refs.p;
     D.bvh_node_count = n - 1;
+    D.bvh4 = wide_p;
+    D.bvh4_node_count = wide_p ? int(wide.size() / 8) : 0;
     nodes.p = nullptr;
     sorted_refs.p = nullptr;
     G->max_depth_bvh = depth;

@@ -39,6 +39,7 @@ MYPBR_HD float len2(float3 a) { return dot(a, a); }
 MYPBR_DEV float length(float3 a) { return sqrtf(dot(a, a)); }
 MYPBR_DEV float3 normalize(float3 a) { return a * rsqrtf(dot(a, a)); }
 MYPBR_HD float comp(float3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+MYPBR_HD float comp4(float4 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : (i == 2 ? a.z : a.w)); }
 MYPBR_HD void set_comp(float3& a, int i, float v) {
     if (i == 0)
         a.x = v;

@@ -71,6 +71,8 @@ struct DeviceScene {
     // geometry
     const float4* bvh;
     const uint32_t* leaf_refs;
+    const float4* bvh4;  // the same tree collapsed to 4 children per node (nullptr: not built)
+    int bvh4_node_count;
     const float4* spheres;
     const int2* sphere_info;
     const float4* quads;
@@ -601,20 +603,21 @@ MYPBR_DEV float safe_inv(float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysi
 // deterministic ray-batch query).
 // VOX: whether voxel blocks are tested (kernels for scenes without voxels
 // leave that code out, and with it its registers).
-template <bool ANY, bool VOX = true>
+// WIDE: walk the 4-wide tree (S.bvh4) instead of the binary one.
+template <bool ANY, bool VOX = true, bool WIDE = false>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key);
 
-template <bool VOX = true>
+template <bool VOX = true, bool WIDE = false>
 MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
-    return walk<false, VOX>(S, o, d, tmin, tmax, media_key);
+    return walk<false, VOX, WIDE>(S, o, d, tmin, tmax, media_key);
 }
 
 // Whether anything at all lies along o + t d, t in (tmin, tmax): the walk stops
 // at the first primitive it hits. For shadow rays in scenes where nothing
 // hittable can emit, this is all the reference's closest-hit query decides.
-template <bool VOX = true>
+template <bool VOX = true, bool WIDE = false>
 MYPBR_DEV bool any_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
-    return walk<true, VOX>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
+    return walk<true, VOX, WIDE>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
 }
 
 // A ray's BVH walk, advanced one interior node at a time (walk_node), so that
@@ -794,15 +797,149 @@ MYPBR_DEV void walk_unbounded(const DeviceScene& S, WalkState& W) {
     }
 }
 
+// The primitives of one leaf (count refs from first) against the ray; true
+// when ANY and one was hit.
+template <bool ANY, bool VOX>
+MYPBR_DEV bool test_leaf(const DeviceScene& S, int first, int count, float3 o, float3 d, const TriRay& tr, float tmin,
+                         uint64_t media_key, HitInfo& h) {
+    for (int k = 0; k < count; k++) {
+        uint32_t ref = __ldg(S.leaf_refs + first + k);
+        int kind = int(ref >> kKindShift), idx = int(ref & kIndexMask);
+        float t, b1 = 0.0f, b2 = 0.0f;
+        bool got = false;
+        if (kind == kTriangle) {
+            got = hit_triangle(S, idx, o, tr, tmin, h.t, t, b1, b2, media_key);
+        } else if (kind == kSphere) {
+            got = hit_sphere(S, idx, o, d, tmin, h.t, t);
+        } else if (kind == kQuad) {
+            got = hit_quad(S, idx, o, d, tmin, h.t, t, b1, b2);
+        } else if (kind == kMedium && media_key != 0) {
+            got = hit_medium(S, idx, o, d, tmin, h.t, hash_uniform(media_key, uint32_t(idx)), t);
+        } else if (VOX && kind == kVoxel) {
+            int mat, face;
+            got = hit_voxel_block(S, idx, o, d, tmin, h.t, t, mat, face);
+            b1 = __int_as_float(mat);
+            b2 = __int_as_float(face);
+        }
+        if (got) {
+            h.t = t;
+            h.b1 = b1;
+            h.b2 = b2;
+            h.prim = ref;
+            if (ANY)
+                return true;
+        }
+    }
+    return false;
+}
+
+MYPBR_DEV int pick4(int4 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w)); }
+
+// The walk over the 4-wide tree. A node (8 float4, 128 B) holds its four
+// children's boxes as rows (x lo, x hi, y lo, y hi, z lo, z hi; one lane per
+// child), their indices and their kinds (count > 0: a leaf of that many
+// references from the index; 0: an interior node; -1: an empty slot). Leaves
+// among the children a ray meets are tested at once; the interior ones still
+// nearer than the closest hit are visited nearest first (a five-comparison
+// sorting network), the others pushed. The host bounds the stack (three
+// entries per level) before it enables this walk.
+constexpr int kBvh4Stack = 64;
+template <bool ANY, bool VOX>
+MYPBR_DEV bool walk_tree4(const DeviceScene& S, float3 o, float3 d, float tmin, uint64_t media_key, HitInfo& h) {
+    float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    float3 oi = -1.0f * (o * inv);
+    TriRay tr = make_tri_ray(d);
+    int stack[kBvh4Stack];
+    int sp = 0;
+    int node = 0;
+    int visits = 0;
+    while (true) {
+        if (++visits > S.bvh4_node_count + 1) {  // a tree walk enters each node at most once
+            atomicCAS(S.error, 0, 1);
+            return false;
+        }
+        const float4* n = S.bvh4 + 8 * node;
+        float4 xl = ldg4(n), xh = ldg4(n + 1), yl = ldg4(n + 2), yh = ldg4(n + 3), zl = ldg4(n + 4),
+               zh = ldg4(n + 5);
+        int4 child = __ldg(reinterpret_cast<const int4*>(n + 6));
+        int4 count = __ldg(reinterpret_cast<const int4*>(n + 7));
+        float near[4];
+        unsigned leaves = 0, inner = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            float ax = comp4(xl, c), bx = comp4(xh, c), ay = comp4(yl, c), by = comp4(yh, c), az = comp4(zl, c),
+                  bz = comp4(zh, c);
+            float lx = fmaf(ax, inv.x, oi.x), hx = fmaf(bx, inv.x, oi.x);
+            float ly = fmaf(ay, inv.y, oi.y), hy = fmaf(by, inv.y, oi.y);
+            float lz = fmaf(az, inv.z, oi.z), hz = fmaf(bz, inv.z, oi.z);
+            float tn = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fmaxf(fminf(lz, hz), tmin));
+            float tf = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fminf(fmaxf(lz, hz), h.t));
+            int cnt = pick4(count, c);
+            // a small relative widening keeps FP32 slab tests conservative
+            bool met = tn <= tf * 1.00000024f + 1e-30f && cnt >= 0;
+            near[c] = tn;
+            leaves |= (met && cnt > 0) ? 1u << c : 0u;
+            inner |= (met && cnt == 0) ? 1u << c : 0u;
+        }
+        for (unsigned m = leaves; m; m &= m - 1) {
+            int c = __ffs(m) - 1;
+            if (test_leaf<ANY, VOX>(S, pick4(child, c), pick4(count, c), o, d, tr, tmin, media_key, h))
+                return true;
+        }
+        // the interior children still nearer than the closest hit, nearest first
+        float k0 = (inner & 1u) && near[0] <= h.t ? near[0] : INFINITY;
+        float k1 = (inner & 2u) && near[1] <= h.t ? near[1] : INFINITY;
+        float k2 = (inner & 4u) && near[2] <= h.t ? near[2] : INFINITY;
+        float k3 = (inner & 8u) && near[3] <= h.t ? near[3] : INFINITY;
+        int c0 = child.x, c1 = child.y, c2 = child.z, c3 = child.w;
+        auto cswap = [](float& ka, int& ca, float& kb, int& cb) {
+            if (kb < ka) {
+                float tk = ka;
+                ka = kb;
+                kb = tk;
+                int tc = ca;
+                ca = cb;
+                cb = tc;
+            }
+        };
+        cswap(k0, c0, k1, c1);
+        cswap(k2, c2, k3, c3);
+        cswap(k0, c0, k2, c2);
+        cswap(k1, c1, k3, c3);
+        cswap(k1, c1, k2, c2);
+        int pushes = (k1 < INFINITY) + (k2 < INFINITY) + (k3 < INFINITY);
+        if (sp + pushes > kBvh4Stack) {  // deeper than the host-checked bound: report, stop
+            atomicCAS(S.error, 0, 2);
+            return false;
+        }
+        if (k3 < INFINITY)
+            stack[sp++] = c3;
+        if (k2 < INFINITY)
+            stack[sp++] = c2;
+        if (k1 < INFINITY)
+            stack[sp++] = c1;
+        if (k0 < INFINITY) {
+            node = c0;
+        } else {
+            if (sp == 0)
+                return false;
+            node = stack[--sp];
+        }
+    }
+}
+
 // The whole walk in one loop (the form the per-ray kernels use; walk_node
 // above is the same step, resumable, for k_extend_pt).
-template <bool ANY, bool VOX>
+template <bool ANY, bool VOX, bool WIDE>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
     HitInfo h;
     h.prim = kMiss;
     h.t = tmax;
     h.b1 = h.b2 = 0.0f;
-    if (S.has_bvh) {
+    if constexpr (WIDE) {
+        if (S.has_bvh && walk_tree4<ANY, VOX>(S, o, d, tmin, media_key, h))
+            return h;
+    } else if (S.has_bvh) {
         float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
         float3 oi = -1.0f * (o * inv);
         TriRay tr = make_tri_ray(d);

@@ -75,7 +75,8 @@ struct mypbr_gpu_scene {
     // autotuned launch settings (0: built-in defaults)
     size_t tuned_wave_paths = 0;
     int tuned_block = 0;
-    int tuned_traversal = 0;  // 0: one ray per lane to the end (k_extend); 1: lanes take new rays (k_extend_pt)
+    int tuned_traversal = 0;  // 0: one ray per lane to the end (k_extend); 1: lanes take new rays (k_extend_pt);
+                              // 2: as 0 over the 4-wide tree
 };
 
 namespace mypbr_dev {
@@ -91,6 +92,8 @@ int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed);
 int guide_ensure_records(mypbr_gpu_scene* G, size_t mix_slots, size_t rec_slots, int depth);
 // `steps` Adam steps on batches drawn from the recorded vertices.
 int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaStream_t st);
+// The binary tree's device nodes collapsed to four children per node (walk_tree4's layout); depth: deepest level.
+void collapse_to_4(const std::vector<float4>& bin, std::vector<float4>& out, int& depth);
 
 }  // namespace mypbr_dev
 

@@ -271,7 +271,7 @@ MYPBR_DEV int hit_material(const DeviceScene& S, const HitInfo& h) {
 }
 
 // Closest hits of the extension queue; each ray then joins its shading class's queue.
-template <bool VOX>
+template <bool VOX, bool WIDE>
 __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
     uint32_t n = *ext_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
             uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
             key = media_key(P, pixel, pass, uint32_t(depth), 0);
         }
-        HitInfo h = closest_hit<VOX>(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
+        HitInfo h = closest_hit<VOX, WIDE>(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
         P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
         int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h)]);
         uint32_t* counter = class_counter(P, depth, c);
@@ -586,7 +586,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
     }
 }
 
-template <bool VOX>
+template <bool VOX, bool WIDE>
 __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
     uint32_t n = *sh_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
@@ -610,13 +610,13 @@ __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
             // sample already holds the sky's radiance (sc.w = 1).
             if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1);
-            if (!any_hit<VOX>(S, o, d, 0.001f, 3.0e38f, key))
+            if (!any_hit<VOX, WIDE>(S, o, d, 0.001f, 3.0e38f, key))
                 emission = sc.w != 0.0f ? f3(1.0f) : escaped_radiance(S, d, false);
         } else
         for (int hop = 0; hop <= 16; hop++) {
             if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1 + 4 * hop);
-            HitInfo h = closest_hit<VOX>(S, o, d, 0.001f, 3.0e38f, key);
+            HitInfo h = closest_hit<VOX, WIDE>(S, o, d, 0.001f, 3.0e38f, key);
             if (h.prim == kMiss) {
                 emission = escaped_radiance(S, d, false);
                 break;
@@ -863,6 +863,7 @@ struct Launch {
     int grid_extend, grid_shade, grid_shadow, grid_stream;
     int block = 256;              // threads per block of extend, shade and shadow
     bool persistent = false;      // extend with lanes that take new rays (k_extend_pt)
+    bool wide = false;            // walk the 4-wide tree
     bool guided_kernels = false;  // the shading variants of guided renders
     int grid_guide = 0;
     size_t guide_smem = 0;
@@ -874,13 +875,16 @@ Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
     Launch L{};
     L.block = block == 128 || block == 256 ? block : (G.tuned_block ? G.tuned_block : 256);
     L.persistent = G.tuned_traversal == 1;
+    L.wide = G.tuned_traversal == 2 && G.dev.bvh4 != nullptr;
     int per_sm = 0;
     bool vox = G.dev.has_voxels;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vox ? (const void*)k_extend<true> : (const void*)k_extend<false>,
-                                                  L.block, 0);
+    const void* extend = L.wide ? (vox ? (const void*)k_extend<true, true> : (const void*)k_extend<false, true>)
+                                : (vox ? (const void*)k_extend<true, false> : (const void*)k_extend<false, false>);
+    const void* shadow = L.wide ? (vox ? (const void*)k_shadow<true, true> : (const void*)k_shadow<false, true>)
+                                : (vox ? (const void*)k_shadow<true, false> : (const void*)k_shadow<false, false>);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend, L.block, 0);
     L.grid_extend = G.sm_count * std::max(per_sm, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vox ? (const void*)k_shadow<true> : (const void*)k_shadow<false>,
-                                                  L.block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shadow, L.block, 0);
     L.grid_shadow = G.sm_count * std::max(per_sm, 1);
     L.grid_stream = G.sm_count * 8;
     int worst = 1;
@@ -977,10 +981,14 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
             TIMED(1, (k_extend_pt<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else if (L.persistent)
             TIMED(1, (k_extend_pt<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+        else if (L.wide && P.S.has_voxels)
+            TIMED(1, (k_extend<true, true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+        else if (L.wide)
+            TIMED(1, (k_extend<false, true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else if (P.S.has_voxels)
-            TIMED(1, (k_extend<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+            TIMED(1, (k_extend<true, false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else
-            TIMED(1, (k_extend<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+            TIMED(1, (k_extend<false, false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         if (P.guided) {  // the mixtures of this bounce's guidable vertices
             TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
                          L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
@@ -1001,10 +1009,14 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
             TIMED(2, (k_shade<kClassPrincipled, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
             TIMED(2, (k_shade<kClassGeneric, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
         }
-        if (P.S.has_voxels)
-            TIMED(3, (k_shadow<true><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
+        if (L.wide && P.S.has_voxels)
+            TIMED(3, (k_shadow<true, true><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
+        else if (L.wide)
+            TIMED(3, (k_shadow<false, true><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
+        else if (P.S.has_voxels)
+            TIMED(3, (k_shadow<true, false><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
         else
-            TIMED(3, (k_shadow<false><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
+            TIMED(3, (k_shadow<false, false><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
         launches += 2 + kShadeClasses;
     }
     MYPBR_CUDA(cudaGetLastError());
@@ -1528,8 +1540,12 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
     MYPBR_CUDA(cudaEventCreate(&e1));
     int status = MYPBR_OK;
     int trial = 0;
-    for (int trav = 0; trav < 2; trav++)
+    for (int trav = 0; trav < 3; trav++)
     for (int b : blocks) {
+        if (trav == 2 && G->dev.bvh4 == nullptr) {  // no 4-wide tree: those trials are skipped
+            trial += 4;
+            continue;
+        }
         for (size_t wp : waves) {
             G->tuned_traversal = trav;
             G->tuned_block = b;
@@ -1572,8 +1588,8 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
 }
 
 extern "C" int mypbr_gpu_set_launch(mypbr_gpu_scene* G, int32_t block, int64_t wave_paths, int32_t traversal) {
-    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 1)
-        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0 or 1");
+    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 2)
+        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0, 1 or 2");
     G->tuned_block = block;
     G->tuned_wave_paths = size_t(wave_paths);
     G->tuned_traversal = traversal;

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <map>
 #include <cmath>
+#include <functional>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -55,6 +56,11 @@ float ibits(int i) {
     float f;
     std::memcpy(&f, &i, sizeof f);
     return f;
+}
+int float_bits(float f) {
+    int i;
+    std::memcpy(&i, &f, sizeof i);
+    return i;
 }
 
 int bad(const std::string& m) {
@@ -377,6 +383,20 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     PUT(nodes, D.bvh);
     PUT(refs, D.leaf_refs);
     D.bvh_node_count = interior;
+    {
+        std::vector<float4> nodes4;
+        int depth4 = 0;
+        if (D.has_bvh)
+            collapse_to_4(nodes, nodes4, depth4);
+        // the 4-wide walk's stack takes at most three entries per level
+        if (!nodes4.empty() && 3 * (depth4 + 1) <= kBvh4Stack) {
+            PUT(nodes4, D.bvh4);
+            D.bvh4_node_count = int(nodes4.size() / 8);
+        } else {
+            D.bvh4 = nullptr;
+            D.bvh4_node_count = 0;
+        }
+    }
     {
         std::vector<int> zero(1, 0);
         const int* err = nullptr;
@@ -722,6 +742,88 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
 #undef PUT
     *out = holder.release();
     return MYPBR_OK;
+}
+
+}  // namespace mypbr_dev
+
+namespace mypbr_dev {
+
+// The binary tree (64-byte nodes holding both children's boxes) collapsed to
+// four children per node: starting from a node's two children, the interior
+// child of largest surface area is replaced by its own two children until
+// there are four or none is interior. Node layout as walk_tree4 reads it.
+// depth: the deepest level of the result (0 at the root).
+void collapse_to_4(const std::vector<float4>& bin, std::vector<float4>& out, int& depth) {
+    struct Child {
+        float4 lo, hi;  // w: index, count (float bits) as in the binary node
+        int index() const { return float_bits(lo.w); }
+        int count() const { return float_bits(hi.w); }
+    };
+    auto children = [&](int i, Child* c) {
+        c[0] = {bin[size_t(i) * 4], bin[size_t(i) * 4 + 1]};
+        c[1] = {bin[size_t(i) * 4 + 2], bin[size_t(i) * 4 + 3]};
+    };
+    auto area = [](const Child& c) {
+        double x = double(c.hi.x) - c.lo.x, y = double(c.hi.y) - c.lo.y, z = double(c.hi.z) - c.lo.z;
+        if (!(x >= 0 && y >= 0 && z >= 0) || !std::isfinite(x + y + z))
+            return -1.0;
+        return x * y + y * z + z * x;
+    };
+    depth = 0;
+    std::function<int(int, int)> build = [&](int i, int level) -> int {
+        depth = std::max(depth, level);
+        Child list[4];
+        children(i, list);
+        int n = 2;
+        while (n < 4) {
+            int best = -1;
+            double best_area = -2;
+            for (int k = 0; k < n; k++)
+                if (list[k].count() == 0 && area(list[k]) > best_area) {
+                    best = k;
+                    best_area = area(list[k]);
+                }
+            if (best < 0)
+                break;
+            Child sub[2];
+            children(list[best].index(), sub);
+            list[best] = sub[0];
+            list[n++] = sub[1];
+        }
+        int me = int(out.size() / 8);
+        out.resize(out.size() + 8);
+        int child[4], count[4];
+        for (int k = 0; k < 4; k++) {
+            if (k >= n) {
+                child[k] = 0;
+                count[k] = -1;
+            } else if (list[k].count() > 0) {
+                child[k] = list[k].index();
+                count[k] = list[k].count();
+            } else {
+                child[k] = build(list[k].index(), level + 1);
+                count[k] = 0;
+            }
+        }
+        float4* row = &out[size_t(me) * 8];
+        const float inf = INFINITY;
+        float v[6][4];
+        for (int k = 0; k < 4; k++) {
+            bool used = k < n;
+            v[0][k] = used ? list[k].lo.x : inf;
+            v[1][k] = used ? list[k].hi.x : inf;
+            v[2][k] = used ? list[k].lo.y : inf;
+            v[3][k] = used ? list[k].hi.y : inf;
+            v[4][k] = used ? list[k].lo.z : inf;
+            v[5][k] = used ? list[k].hi.z : inf;
+        }
+        for (int r = 0; r < 6; r++)
+            row[r] = make_float4(v[r][0], v[r][1], v[r][2], v[r][3]);
+        row[6] = make_float4(ibits(child[0]), ibits(child[1]), ibits(child[2]), ibits(child[3]));
+        row[7] = make_float4(ibits(count[0]), ibits(count[1]), ibits(count[2]), ibits(count[3]));
+        return me;
+    };
+    build(0, 0);
 }
 
 }  // namespace mypbr_dev
