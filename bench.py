@@ -420,13 +420,14 @@ def run_voxel_hall(args):
     print(json.dumps(line), flush=True)
 
 
-def render_rate(mp, scene, spp, steps, warmup, guided=0):
+def render_rate(mp, scene, spp, steps, warmup, guided=0, block=0, traversal=0):
     """Device-resident Mpaths/s of a scene (CUDA events around the render on
     the scene handle's stream is what mypbr_gpu_render_ex times)."""
     cam = scene.camera
     cam.samples_per_pixel = spp
     cam.guided = guided
     G = mp.GpuScene(scene)
+    mp.set_launch(G, block=block, traversal=traversal)
     times = []
     st = None
     for k in range(warmup + steps):
@@ -438,6 +439,43 @@ def render_rate(mp, scene, spp, steps, warmup, guided=0):
     G.close()
     t = statistics.median(times)
     return st["paths"] / t / 1e6, t, st
+
+
+def equal_time_relmse(mp, scene, spp, args):
+    """C3's equal-time comparison: a plain render at spp, a guided one (the
+    network trained inside its own time, from scratch) given the same time,
+    both against a plain render at --c3-ref-spp; relMSE = mean over pixels
+    and channels of (x - r)^2 / (r^2 + 0.01)."""
+    cam = scene.camera
+
+    def render(spp_, guided, seed):
+        G = mp.GpuScene(scene)
+        mp.set_launch(G, block=args.block, traversal=args.traversal)
+        cam.samples_per_pixel = spp_
+        cam.guided = guided
+        cam.seed = seed
+        t0 = time.perf_counter()
+        img, _, st = mp.render_ex(cam, G)
+        secs = time.perf_counter() - t0
+        G.close()
+        return img, secs, st
+
+    ref, t_ref, _ = render(args.c3_ref_spp, 0, 991)
+
+    def rel(img):
+        return float(np.mean((img - ref) ** 2 / (ref * ref + 0.01)))
+
+    plain, t_plain, _ = render(spp, 0, 7)
+    # the guided rate at this spp, then the spp that fills the plain render's time
+    _, t_probe, _ = render(spp, args.hidden, 8)
+    spp_g = max(1, int(spp * t_plain / t_probe))
+    guided, t_guided, _ = render(spp_g, args.hidden, 9)
+    cam.guided = 0
+    return {"seconds_plain": t_plain, "seconds_guided": t_guided, "reference_spp": args.c3_ref_spp,
+            "reference_seconds": t_ref, "relmse_eps": 0.01,
+            "plain": {"spp": spp, "relmse": rel(plain)}, "guided": {"spp": spp_g, "relmse": rel(guided)},
+            "hidden_layers": args.hidden,
+            "relmse_ratio_plain_over_guided": rel(plain) / max(rel(guided), 1e-30)}
 
 
 def run_simple(args, workload):
@@ -453,7 +491,7 @@ def run_simple(args, workload):
             scene = mp.load_scene(triangle_room_scene(d))
             spp, cfg = 64, {"workload": "triangle_room_2m", "width": 1920, "height": 1080, "spp": 64,
                             "max_depth": 12, "triangles": 1985856, "materials": "32 principled", "lights": 16}
-    value, t, st = render_rate(mp, scene, spp, args.steps, args.warmup)
+    value, t, st = render_rate(mp, scene, spp, args.steps, args.warmup, block=args.block, traversal=args.traversal)
     line = {"metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "dtype": "fp32",
             "data": "synthetic", "config": cfg,
@@ -461,9 +499,11 @@ def run_simple(args, workload):
                      "shadow_per_path": st["shadow_rays"] / st["paths"],
                      "mrays_per_s": (st["extension_rays"] + st["shadow_rays"]) / t / 1e6}}
     if workload == "triangle_room" and args.hidden:
-        gv, gt, _ = render_rate(mp, scene, spp, max(1, args.steps // 2), 1, guided=args.hidden)
+        gv, gt, _ = render_rate(mp, scene, spp, max(1, args.steps // 2), 1, guided=args.hidden,
+                                block=args.block, traversal=args.traversal)
         line["guided"] = {"value": gv, "ms_per_step": gt * 1e3, "hidden_layers": args.hidden,
                           "note": "untrained network at the first render; later renders train further"}
+        line["equal_time"] = equal_time_relmse(mp, scene, spp, args)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         h = scene.camera.height()
@@ -609,6 +649,7 @@ def main():
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--ref-spp", type=int, default=65536)
+    p.add_argument("--c3-ref-spp", type=int, default=1024, help="spp of the triangle room's reference render")
     p.add_argument("--max-spp", type=int, default=16384)
     p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
     args = p.parse_args()

@@ -672,6 +672,16 @@ int mypbr_gpu_display(const double* radiance, int32_t width, int32_t height, con
 int mypbr_image_read(const char* path, int32_t* width, int32_t* height, int32_t* channels, uint8_t* rgba,
                      int64_t capacity);
 
+/* The environment's sampling tables for an equirectangular image (W*H*3
+ * floats, rows from the top): texel_pdf (W*H floats) = p * W * H with p
+ * proportional to luminance x sin(theta) (environment.h:147-176; a black
+ * image: rows by sin(theta)), and alias (W*H pairs of floats: probability,
+ * alias index as int bits) an alias table holding the same distribution.
+ * on_gpu: built on the device (the way mypbr_gpu_scene_create builds them),
+ * else on the host with Vose's method. Host pointers. */
+int mypbr_env_distribution(const float* rgb, int32_t width, int32_t height, float* texel_pdf, float* alias,
+                           int on_gpu);
+
 /* write_image (include/image_io.h:84-106): the format follows the extension;
  * .png and .ppm are display images (post-processed on the GPU), .hdr and .pfm
  * the raw radiance; an empty path writes PPM to stdout. */

@@ -131,6 +131,7 @@ def lib():
     L.mypbr_scene_free.restype = None
     L.mypbr_ggx_albedo_table.argtypes = [dp]
     L.mypbr_gpu_denoise.argtypes = [vp, vp, vp, vp, ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int]
+    L.mypbr_env_distribution.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int]
     i32p = ctypes.POINTER(ctypes.c_int32)
     L.mypbr_image_read.argtypes = [ctypes.c_char_p, i32p, i32p, i32p, vp, ctypes.c_int64]
     L.mypbr_camera_init.argtypes = [ctypes.POINTER(CameraStruct)]
@@ -504,6 +505,17 @@ def denoise(radiance, albedo, normal, variance, width, height, out, on_device=Fa
         return int(x) if on_device else x.ctypes.data
     check(lib().mypbr_gpu_denoise(addr(radiance), addr(albedo), addr(normal), addr(variance), int(width),
                                   int(height), None, addr(out), int(bool(on_device))))
+
+
+def env_distribution(rgb, on_gpu=False):
+    """The environment's sampling tables for an (H, W, 3) float32 image:
+    (texel pdf p*W*H [H, W], alias probabilities [H*W], alias indices [H*W])."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    h, w = rgb.shape[:2]
+    pdf = np.zeros((h, w), dtype=np.float32)
+    alias = np.zeros((h * w, 2), dtype=np.float32)
+    check(lib().mypbr_env_distribution(rgb.ctypes.data, w, h, pdf.ctypes.data, alias.ctypes.data, int(bool(on_gpu))))
+    return pdf, alias[:, 0].copy(), alias[:, 1].copy().view(np.int32)
 
 
 def autotune(camera, gpu_scene):

@@ -94,6 +94,10 @@ int guide_ensure_records(mypbr_gpu_scene* G, size_t mix_slots, size_t rec_slots,
 int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaStream_t st);
 // The binary tree's device nodes collapsed to four children per node (walk_tree4's layout); depth: deepest level.
 void collapse_to_4(const std::vector<float4>& bin, std::vector<float4>& out, int& depth);
+// The environment's pdf table (p n per texel) and alias table (probability, alias index bits) from its
+// pixels (w x h x 3 floats): on the device (device pointers, env_dist.cu) or on the host (Vose's method).
+int build_env_distribution(const float* rgb, int w, int h, float* texel_pdf, float2* alias, cudaStream_t st);
+void env_distribution_host(const float* rgb, int w, int h, float* texel_pdf, float2* alias);
 
 }  // namespace mypbr_dev
 

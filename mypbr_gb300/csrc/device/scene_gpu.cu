@@ -663,62 +663,36 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
         int w = D.env_w, h = D.env_h;
         size_t n = size_t(w) * h;
         std::vector<float4> px(n);
-        std::vector<double> wgt(n);
-        std::vector<double> row(h, 0.0);
-        const double kPiD = 3.1415926535897932385;
-        double total = 0;
-        for (int j = 0; j < h; j++) {
-            double st = std::sin(kPiD * (j + 0.5) / h);
-            for (int i = 0; i < w; i++) {
-                const float* p = F.environment.pixels + (size_t(j) * w + i) * 3;
-                px[size_t(j) * w + i] = make_float4(p[0], p[1], p[2], 0.0f);
-                double l = 0.2126 * p[0] + 0.7152 * p[1] + 0.0722 * p[2];
-                wgt[size_t(j) * w + i] = std::fmax(l * st, 0.0);
-                row[j] += wgt[size_t(j) * w + i];
-            }
-            total += row[j];
-        }
-        std::vector<double> prob(n);
-        if (total > 0) {
-            for (size_t k = 0; k < n; k++)
-                prob[k] = wgt[k] / total;
-        } else {
-            // A black sky: rows by sin(theta), uniform within a row (environment.h:302-309)
-            double s = 0;
-            for (int j = 0; j < h; j++)
-                s += std::sin(kPiD * (j + 0.5) / h);
-            for (int j = 0; j < h; j++)
-                for (int i = 0; i < w; i++)
-                    prob[size_t(j) * w + i] = std::sin(kPiD * (j + 0.5) / h) / s / w;
-        }
-        std::vector<float> texel_pdf(n);
-        for (size_t k = 0; k < n; k++)
-            texel_pdf[k] = float(prob[k] * double(w) * double(h));
-        // Vose's alias method
-        std::vector<float2> alias(n);
-        std::vector<double> scaled(n);
-        std::vector<uint32_t> small, large;
         for (size_t k = 0; k < n; k++) {
-            scaled[k] = prob[k] * double(n);
-            (scaled[k] < 1.0 ? small : large).push_back(uint32_t(k));
+            const float* p = F.environment.pixels + 3 * k;
+            px[k] = make_float4(p[0], p[1], p[2], 0.0f);
         }
-        while (!small.empty() && !large.empty()) {
-            uint32_t s = small.back(), l = large.back();
-            small.pop_back();
-            alias[s] = make_float2(float(scaled[s]), ibits(int(l)));
-            scaled[l] = (scaled[l] + scaled[s]) - 1.0;
-            if (scaled[l] < 1.0) {
-                large.pop_back();
-                small.push_back(l);
-            }
-        }
-        for (uint32_t l : large)
-            alias[l] = make_float2(1.0f, ibits(int(l)));
-        for (uint32_t s : small)
-            alias[s] = make_float2(1.0f, ibits(int(s)));
         PUT(px, D.env_pixels);
-        PUT(texel_pdf, D.env_texel_pdf);
-        PUT(alias, D.env_alias);
+        // the sampling distribution, built on the device from the pixels
+        float* rgb = nullptr;
+        float* texel_pdf = nullptr;
+        float2* alias = nullptr;
+        if (cudaMalloc(&rgb, n * 3 * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&texel_pdf, n * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&alias, n * sizeof(float2)) != cudaSuccess) {
+            cudaFree(rgb);
+            cudaFree(texel_pdf);
+            cudaFree(alias);
+            set_error_message("mypbr_gpu_scene_create: out of device memory for the environment");
+            return fail_cleanup(MYPBR_ERR_OUT_OF_MEMORY);
+        }
+        G.allocations.push_back(texel_pdf);
+        G.allocations.push_back(alias);
+        int st = MYPBR_OK;
+        if (cudaMemcpy(rgb, F.environment.pixels, n * 3 * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+            st = cuda_fail(cudaGetLastError(), "environment upload");
+        if (st == MYPBR_OK)
+            st = build_env_distribution(rgb, w, h, texel_pdf, alias, G.stream);
+        cudaFree(rgb);
+        if (st != MYPBR_OK)
+            return fail_cleanup(st);
+        D.env_texel_pdf = texel_pdf;
+        D.env_alias = alias;
     }
 
     // ---- sun (sun.h:23-43) and the plain sky
@@ -747,6 +721,55 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
 }  // namespace mypbr_dev
 
 namespace mypbr_dev {
+
+// The environment's sampling tables on the host: per-texel weights
+// luminance x sin(theta) (environment.h:147-176; rows by sin(theta) for a
+// black sky, environment.h:302-309), the pdf table p n and Vose's alias table.
+void env_distribution_host(const float* rgb, int w, int h, float* texel_pdf, float2* alias) {
+    size_t n = size_t(w) * h;
+    std::vector<double> wgt(n);
+    const double kPiD = 3.1415926535897932385;
+    double total = 0;
+    for (int j = 0; j < h; j++) {
+        double st = std::sin(kPiD * (j + 0.5) / h);
+        for (int i = 0; i < w; i++) {
+            const float* p = rgb + (size_t(j) * w + i) * 3;
+            double l = 0.2126 * p[0] + 0.7152 * p[1] + 0.0722 * p[2];
+            wgt[size_t(j) * w + i] = std::fmax(l * st, 0.0);
+            total += wgt[size_t(j) * w + i];
+        }
+    }
+    if (!(total > 0)) {
+        total = 0;
+        for (int j = 0; j < h; j++)
+            for (int i = 0; i < w; i++) {
+                wgt[size_t(j) * w + i] = std::sin(kPiD * (j + 0.5) / h);
+                total += wgt[size_t(j) * w + i];
+            }
+    }
+    std::vector<double> scaled(n);
+    std::vector<uint32_t> small, large;
+    for (size_t k = 0; k < n; k++) {
+        double prob = wgt[k] / total;
+        texel_pdf[k] = float(prob * double(n));
+        scaled[k] = prob * double(n);
+        (scaled[k] < 1.0 ? small : large).push_back(uint32_t(k));
+    }
+    while (!small.empty() && !large.empty()) {
+        uint32_t s = small.back(), l = large.back();
+        small.pop_back();
+        alias[s] = make_float2(float(scaled[s]), ibits(int(l)));
+        scaled[l] = (scaled[l] + scaled[s]) - 1.0;
+        if (scaled[l] < 1.0) {
+            large.pop_back();
+            small.push_back(l);
+        }
+    }
+    for (uint32_t l : large)
+        alias[l] = make_float2(1.0f, ibits(int(l)));
+    for (uint32_t s : small)
+        alias[s] = make_float2(1.0f, ibits(int(s)));
+}
 
 // The binary tree (64-byte nodes holding both children's boxes) collapsed to
 // four children per node: starting from a node's two children, the interior
