@@ -278,7 +278,7 @@ bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::str
     switch (sniff_image(bytes, size)) {
         case ImageKind::Png: return decode_png(bytes, size, out, error);
         case ImageKind::Other: return decode_tga(bytes, size, out, error);
-        case ImageKind::Jpeg: error = "JPEG images are not decoded by this backend"; return false;
+        case ImageKind::Jpeg: return decode_jpeg(bytes, size, out, error);
         case ImageKind::Bmp: error = "BMP images are not decoded by this backend"; return false;
         case ImageKind::Gif: error = "GIF images are not decoded by this backend"; return false;
         case ImageKind::Hdr: error = "a Radiance HDR image is not an 8-bit image"; return false;

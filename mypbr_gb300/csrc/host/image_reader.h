@@ -1,4 +1,4 @@
-// Decoding of 8-bit image files for textures: PNG and TGA, to RGBA bytes.
+// Decoding of 8-bit image files for textures: PNG, TGA and baseline JPEG, to RGBA bytes.
 #pragma once
 
 #include <cstdint>
@@ -17,6 +17,7 @@ struct LdrImage {
 
 bool decode_png(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
 bool decode_tga(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
+bool decode_jpeg(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
 
 // The kind of image file the bytes start with.
 enum class ImageKind { Png, Hdr, Jpeg, Bmp, Gif, Other };
@@ -24,8 +25,8 @@ ImageKind sniff_image(const uint8_t* bytes, size_t size);
 
 bool read_file_bytes(const std::string& path, std::vector<uint8_t>& bytes);
 
-// An 8-bit image file (PNG, or TGA as the fallback for files no signature
-// names, as stb_image tries it last).
+// An 8-bit image file (PNG, baseline JPEG, or TGA as the fallback for files
+// no signature names, as stb_image tries it last).
 bool read_ldr_image(const std::string& path, LdrImage& out, std::string& error);
 bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
 

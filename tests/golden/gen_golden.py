@@ -338,8 +338,9 @@ def gen_images():
     """stb_image's decoding (through image_texture) of every image fixture."""
     sys.path.insert(0, HERE)
     from image_fixtures import make_image_fixtures
+    from jpeg_fixtures import make_jpeg_fixtures
     folder = os.path.join(HERE, "images")
-    names = make_image_fixtures(folder)
+    names = make_image_fixtures(folder) + make_jpeg_fixtures(folder)
     out = {}
     for name in names:
         raw = run("image", os.path.join(folder, name))
