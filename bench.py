@@ -643,8 +643,8 @@ def main():
                                           "hall_render"], default="sphere_field")
     p.add_argument("--hall-size", type=int, default=512)
     p.add_argument("--per-wave", type=int, default=0)
-    p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2],
-                   help="1: extend lanes take new rays as theirs finish; 2: the 4-wide tree")
+    p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3],
+                   help="1: extend lanes take new rays as theirs finish; 2: the 4-wide tree; 3: postponed leaves")
     p.add_argument("--block", type=int, default=0, choices=[0, 128, 256])
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)

@@ -375,6 +375,7 @@ extern "C" int mypbr_gpu_scene_rebuild_bvh(mypbr_gpu_scene* G, int32_t method, m
     D.leaf_refs = sorted_refs.p;
     D.bvh_node_count = n - 1;
     D.bvh4 = wide_p;
+    D.postponed_ok = n < (1 << 26);  // one reference per leaf
     D.bvh4_node_count = wide_p ? int(wide.size() / 8) : 0;
     nodes.p = nullptr;
     sorted_refs.p = nullptr;

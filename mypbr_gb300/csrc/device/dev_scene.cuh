@@ -73,6 +73,7 @@ struct DeviceScene {
     const uint32_t* leaf_refs;
     const float4* bvh4;  // the same tree collapsed to 4 children per node (nullptr: not built)
     int bvh4_node_count;
+    int postponed_ok;    // leaves small enough to pack into walk_postponed's stack entries
     const float4* spheres;
     const int2* sphere_info;
     const float4* quads;
@@ -603,21 +604,24 @@ MYPBR_DEV float safe_inv(float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysi
 // deterministic ray-batch query).
 // VOX: whether voxel blocks are tested (kernels for scenes without voxels
 // leave that code out, and with it its registers).
-// WIDE: walk the 4-wide tree (S.bvh4) instead of the binary one.
-template <bool ANY, bool VOX = true, bool WIDE = false>
+// WALK: which walk. 0: the binary tree, leaves tested as soon as they are
+// met; 1: the 4-wide tree (S.bvh4); 2: the binary tree with leaves postponed
+// until every lane of the warp holds one (walk_postponed).
+enum : int { kWalkBinary = 0, kWalkWide = 1, kWalkPostponed = 2 };
+template <bool ANY, bool VOX = true, int WALK = kWalkBinary>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key);
 
-template <bool VOX = true, bool WIDE = false>
+template <bool VOX = true, int WALK = kWalkBinary>
 MYPBR_DEV HitInfo closest_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
-    return walk<false, VOX, WIDE>(S, o, d, tmin, tmax, media_key);
+    return walk<false, VOX, WALK>(S, o, d, tmin, tmax, media_key);
 }
 
 // Whether anything at all lies along o + t d, t in (tmin, tmax): the walk stops
 // at the first primitive it hits. For shadow rays in scenes where nothing
 // hittable can emit, this is all the reference's closest-hit query decides.
-template <bool VOX = true, bool WIDE = false>
+template <bool VOX = true, int WALK = kWalkBinary>
 MYPBR_DEV bool any_hit(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
-    return walk<true, VOX, WIDE>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
+    return walk<true, VOX, WALK>(S, o, d, tmin, tmax, media_key).prim != 0xffffffffu;
 }
 
 // A ray's BVH walk, advanced one interior node at a time (walk_node), so that
@@ -928,16 +932,101 @@ MYPBR_DEV bool walk_tree4(const DeviceScene& S, float3 o, float3 d, float tmin, 
     }
 }
 
+// The binary walk with leaves postponed (Aila and Laine, "Understanding the
+// Efficiency of Ray Traversal on GPUs", HPG 2009): a lane that meets a leaf
+// keeps it aside and walks on through inner nodes until every active lane of
+// its warp holds a leaf (or is done); then the warp tests its leaves
+// together. The stack holds inner nodes (>= 0) and leaves (~(first << 4 |
+// count), below 0); the host enables this walk only when every leaf has
+// fewer than 16 references and the references number fewer than 2^26.
+// Returns true when ANY and a hit was found.
+constexpr int kWalkDone = int(0x80000000u);
+template <bool ANY, bool VOX>
+MYPBR_DEV bool walk_postponed(const DeviceScene& S, float3 o, float3 d, float tmin, uint64_t media_key, HitInfo& h) {
+    float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    float3 oi = -1.0f * (o * inv);
+    TriRay tr = make_tri_ray(d);
+    int stack[kBvhStack];
+    int sp = 0;
+    int node = 0;      // the entry being walked: an inner node, a leaf, or kWalkDone
+    int leaf = 0;      // the postponed leaf (< 0), or 0 for none
+    int visits = 0;
+    while (node != kWalkDone || leaf < 0) {
+        // inner nodes until this lane holds a leaf and the whole warp does
+        while (node >= 0) {
+            if (++visits > S.bvh_node_count + 1) {  // a tree walk enters each inner node at most once
+                atomicCAS(S.error, 0, 1);
+                return false;
+            }
+            const float4* n = S.bvh + 4 * node;
+            float4 a0 = ldg4(n), a1 = ldg4(n + 1), c0 = ldg4(n + 2), c1 = ldg4(n + 3);
+            float lx0 = fmaf(a0.x, inv.x, oi.x), hx0 = fmaf(a1.x, inv.x, oi.x);
+            float ly0 = fmaf(a0.y, inv.y, oi.y), hy0 = fmaf(a1.y, inv.y, oi.y);
+            float lz0 = fmaf(a0.z, inv.z, oi.z), hz0 = fmaf(a1.z, inv.z, oi.z);
+            float n0 = fmaxf(fmaxf(fminf(lx0, hx0), fminf(ly0, hy0)), fmaxf(fminf(lz0, hz0), tmin));
+            float f0 = fminf(fminf(fmaxf(lx0, hx0), fmaxf(ly0, hy0)), fminf(fmaxf(lz0, hz0), h.t));
+            float lx1 = fmaf(c0.x, inv.x, oi.x), hx1 = fmaf(c1.x, inv.x, oi.x);
+            float ly1 = fmaf(c0.y, inv.y, oi.y), hy1 = fmaf(c1.y, inv.y, oi.y);
+            float lz1 = fmaf(c0.z, inv.z, oi.z), hz1 = fmaf(c1.z, inv.z, oi.z);
+            float n1 = fmaxf(fmaxf(fminf(lx1, hx1), fminf(ly1, hy1)), fmaxf(fminf(lz1, hz1), tmin));
+            float f1 = fminf(fminf(fmaxf(lx1, hx1), fmaxf(ly1, hy1)), fminf(fmaxf(lz1, hz1), h.t));
+            bool h0 = n0 <= f0 * 1.00000024f + 1e-30f;
+            bool h1 = n1 <= f1 * 1.00000024f + 1e-30f;
+            int k0 = __float_as_int(a1.w), k1 = __float_as_int(c1.w);
+            // a child as a walk entry: the inner node, or the leaf packed below 0
+            int e0 = k0 > 0 ? ~((__float_as_int(a0.w) << 4) | k0) : __float_as_int(a0.w);
+            int e1 = k1 > 0 ? ~((__float_as_int(c0.w) << 4) | k1) : __float_as_int(c0.w);
+            if (h0 && h1) {
+                bool first0 = n0 <= n1;
+                if (sp == kBvhStack) {
+                    atomicCAS(S.error, 0, 2);
+                    return false;
+                }
+                stack[sp++] = first0 ? e1 : e0;
+                node = first0 ? e0 : e1;
+            } else if (h0) {
+                node = e0;
+            } else if (h1) {
+                node = e1;
+            } else {
+                node = sp > 0 ? stack[--sp] : kWalkDone;
+            }
+            // a leaf met while none is held is put aside, and the walk goes on
+            if (node < 0 && node != kWalkDone && leaf == 0) {
+                leaf = node;
+                node = sp > 0 ? stack[--sp] : kWalkDone;
+            }
+            if (__all_sync(__activemask(), leaf < 0 || node == kWalkDone))
+                break;
+        }
+        // the leaves: the postponed one, then any the walk stands on
+        while (leaf < 0) {
+            int packed = ~leaf;
+            if (test_leaf<ANY, VOX>(S, packed >> 4, packed & 15, o, d, tr, tmin, media_key, h))
+                return true;
+            leaf = 0;
+            if (node < 0 && node != kWalkDone) {
+                leaf = node;
+                node = sp > 0 ? stack[--sp] : kWalkDone;
+            }
+        }
+    }
+    return false;
+}
+
 // The whole walk in one loop (the form the per-ray kernels use; walk_node
 // above is the same step, resumable, for k_extend_pt).
-template <bool ANY, bool VOX, bool WIDE>
+template <bool ANY, bool VOX, int WALK>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key) {
     HitInfo h;
     h.prim = kMiss;
     h.t = tmax;
     h.b1 = h.b2 = 0.0f;
-    if constexpr (WIDE) {
+    if constexpr (WALK == kWalkWide) {
         if (S.has_bvh && walk_tree4<ANY, VOX>(S, o, d, tmin, media_key, h))
+            return h;
+    } else if constexpr (WALK == kWalkPostponed) {
+        if (S.has_bvh && walk_postponed<ANY, VOX>(S, o, d, tmin, media_key, h))
             return h;
     } else if (S.has_bvh) {
         float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));

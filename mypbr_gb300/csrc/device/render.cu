@@ -271,7 +271,7 @@ MYPBR_DEV int hit_material(const DeviceScene& S, const HitInfo& h) {
 }
 
 // Closest hits of the extension queue; each ray then joins its shading class's queue.
-template <bool VOX, bool WIDE>
+template <bool VOX, int WALK>
 __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
     uint32_t n = *ext_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
             uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
             key = media_key(P, pixel, pass, uint32_t(depth), 0);
         }
-        HitInfo h = closest_hit<VOX, WIDE>(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
+        HitInfo h = closest_hit<VOX, WALK>(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
         P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
         int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h)]);
         uint32_t* counter = class_counter(P, depth, c);
@@ -387,8 +387,16 @@ constexpr bool kGuidable() {
 // One bounce of ray_color (camera.h:370-457) for the paths of shading class C.
 // GUIDED: the variant of guided renders, which reads the learned mixtures and
 // writes training records (plain renders keep the leaner code).
+// Blocks of 256 a multiprocessor should hold: the shading kernels wait on
+// path-state loads far more than they compute (ncu: long-scoreboard stalls,
+// a quarter of the warps resident at 107 registers), so the lean classes
+// trade a few spilled registers for more resident warps.
+constexpr int shade_min_blocks(int c, bool guided) {
+    return guided ? 2 : (c == kClassMiss ? 4 : (c == kClassPrincipled ? 2 : (c == kClassGeneric ? 1 : 3)));
+}
+
 template <int C, bool GUIDED>
-__global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
+__global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(WaveParams P, int depth) {
     uint32_t n = *class_counter(P, depth, C);
     const uint32_t* q = class_queue(P, C);
     uint32_t* q_next = P.B.queue[(depth + 1) & 1];
@@ -586,7 +594,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
     }
 }
 
-template <bool VOX, bool WIDE>
+template <bool VOX, int WALK>
 __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
     uint32_t n = *sh_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
@@ -610,13 +618,13 @@ __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
             // sample already holds the sky's radiance (sc.w = 1).
             if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1);
-            if (!any_hit<VOX, WIDE>(S, o, d, 0.001f, 3.0e38f, key))
+            if (!any_hit<VOX, WALK>(S, o, d, 0.001f, 3.0e38f, key))
                 emission = sc.w != 0.0f ? f3(1.0f) : escaped_radiance(S, d, false);
         } else
         for (int hop = 0; hop <= 16; hop++) {
             if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1 + 4 * hop);
-            HitInfo h = closest_hit<VOX, WIDE>(S, o, d, 0.001f, 3.0e38f, key);
+            HitInfo h = closest_hit<VOX, WALK>(S, o, d, 0.001f, 3.0e38f, key);
             if (h.prim == kMiss) {
                 emission = escaped_radiance(S, d, false);
                 break;
@@ -863,25 +871,49 @@ struct Launch {
     int grid_extend, grid_shade, grid_shadow, grid_stream;
     int block = 256;              // threads per block of extend, shade and shadow
     bool persistent = false;      // extend with lanes that take new rays (k_extend_pt)
-    bool wide = false;            // walk the 4-wide tree
+    int walk = kWalkBinary;       // which walk extend and shadow use
     bool guided_kernels = false;  // the shading variants of guided renders
     int grid_guide = 0;
     size_t guide_smem = 0;
     GuideNetView net{};
 };
 
+// A bounce kernel (WaveParams, depth) launched through its address, so that
+// graph capture records it like a <<<>>> launch.
+void launch_bounce_kernel(const void* fn, int grid, int block, cudaStream_t st, WaveParams& P, int depth) {
+    void* args[2] = {&P, &depth};
+    cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, st);
+}
+
+// The extend and shadow kernels of a walk, with or without the voxel code.
+const void* extend_kernel(bool vox, int walk) {
+    if (walk == kWalkWide)
+        return vox ? (const void*)k_extend<true, kWalkWide> : (const void*)k_extend<false, kWalkWide>;
+    if (walk == kWalkPostponed)
+        return vox ? (const void*)k_extend<true, kWalkPostponed> : (const void*)k_extend<false, kWalkPostponed>;
+    return vox ? (const void*)k_extend<true, kWalkBinary> : (const void*)k_extend<false, kWalkBinary>;
+}
+const void* shadow_kernel(bool vox, int walk) {
+    if (walk == kWalkWide)
+        return vox ? (const void*)k_shadow<true, kWalkWide> : (const void*)k_shadow<false, kWalkWide>;
+    if (walk == kWalkPostponed)
+        return vox ? (const void*)k_shadow<true, kWalkPostponed> : (const void*)k_shadow<false, kWalkPostponed>;
+    return vox ? (const void*)k_shadow<true, kWalkBinary> : (const void*)k_shadow<false, kWalkBinary>;
+}
+
 // Grids of `block` threads: SMs x resident blocks (persistent-style loops).
 Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
     Launch L{};
     L.block = block == 128 || block == 256 ? block : (G.tuned_block ? G.tuned_block : 256);
     L.persistent = G.tuned_traversal == 1;
-    L.wide = G.tuned_traversal == 2 && G.dev.bvh4 != nullptr;
+    if (G.tuned_traversal == 2 && G.dev.bvh4 != nullptr)
+        L.walk = kWalkWide;
+    else if (G.tuned_traversal == 3 && G.dev.postponed_ok)
+        L.walk = kWalkPostponed;
     int per_sm = 0;
     bool vox = G.dev.has_voxels;
-    const void* extend = L.wide ? (vox ? (const void*)k_extend<true, true> : (const void*)k_extend<false, true>)
-                                : (vox ? (const void*)k_extend<true, false> : (const void*)k_extend<false, false>);
-    const void* shadow = L.wide ? (vox ? (const void*)k_shadow<true, true> : (const void*)k_shadow<false, true>)
-                                : (vox ? (const void*)k_shadow<true, false> : (const void*)k_shadow<false, false>);
+    const void* extend = extend_kernel(vox, L.walk);
+    const void* shadow = shadow_kernel(vox, L.walk);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend, L.block, 0);
     L.grid_extend = G.sm_count * std::max(per_sm, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shadow, L.block, 0);
@@ -981,14 +1013,8 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
             TIMED(1, (k_extend_pt<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else if (L.persistent)
             TIMED(1, (k_extend_pt<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
-        else if (L.wide && P.S.has_voxels)
-            TIMED(1, (k_extend<true, true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
-        else if (L.wide)
-            TIMED(1, (k_extend<false, true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
-        else if (P.S.has_voxels)
-            TIMED(1, (k_extend<true, false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else
-            TIMED(1, (k_extend<false, false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+            TIMED(1, (launch_bounce_kernel(extend_kernel(P.S.has_voxels, L.walk), L.grid_extend, L.block, st, P, depth)));
         if (P.guided) {  // the mixtures of this bounce's guidable vertices
             TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
                          L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
@@ -1009,14 +1035,7 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
             TIMED(2, (k_shade<kClassPrincipled, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
             TIMED(2, (k_shade<kClassGeneric, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
         }
-        if (L.wide && P.S.has_voxels)
-            TIMED(3, (k_shadow<true, true><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
-        else if (L.wide)
-            TIMED(3, (k_shadow<false, true><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
-        else if (P.S.has_voxels)
-            TIMED(3, (k_shadow<true, false><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
-        else
-            TIMED(3, (k_shadow<false, false><<<L.grid_shadow, L.block, 0, st>>>(P, depth)));
+        TIMED(3, (launch_bounce_kernel(shadow_kernel(P.S.has_voxels, L.walk), L.grid_shadow, L.block, st, P, depth)));
         launches += 2 + kShadeClasses;
     }
     MYPBR_CUDA(cudaGetLastError());
@@ -1540,10 +1559,10 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
     MYPBR_CUDA(cudaEventCreate(&e1));
     int status = MYPBR_OK;
     int trial = 0;
-    for (int trav = 0; trav < 3; trav++)
+    for (int trav = 0; trav < 4; trav++)
     for (int b : blocks) {
-        if (trav == 2 && G->dev.bvh4 == nullptr) {  // no 4-wide tree: those trials are skipped
-            trial += 4;
+        if ((trav == 2 && G->dev.bvh4 == nullptr) || (trav == 3 && !G->dev.postponed_ok)) {
+            trial += 4;  // a walk this scene's tree does not allow: trials skipped
             continue;
         }
         for (size_t wp : waves) {
@@ -1588,8 +1607,8 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
 }
 
 extern "C" int mypbr_gpu_set_launch(mypbr_gpu_scene* G, int32_t block, int64_t wave_paths, int32_t traversal) {
-    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 2)
-        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0, 1 or 2");
+    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 3)
+        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0 to 3");
     G->tuned_block = block;
     G->tuned_wave_paths = size_t(wave_paths);
     G->tuned_traversal = traversal;

@@ -383,6 +383,11 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     PUT(nodes, D.bvh);
     PUT(refs, D.leaf_refs);
     D.bvh_node_count = interior;
+    // walk_postponed packs a leaf as first << 4 | count in a stack entry
+    D.postponed_ok = D.has_bvh && F.bvh_prim_count < (int64_t(1) << 26);
+    for (size_t k = 0; D.postponed_ok && k < nodes.size(); k += 2)
+        if (float_bits(nodes[k + 1].w) >= 16)
+            D.postponed_ok = 0;
     {
         std::vector<float4> nodes4;
         int depth4 = 0;
