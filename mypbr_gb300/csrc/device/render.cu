@@ -387,12 +387,12 @@ constexpr bool kGuidable() {
 // One bounce of ray_color (camera.h:370-457) for the paths of shading class C.
 // GUIDED: the variant of guided renders, which reads the learned mixtures and
 // writes training records (plain renders keep the leaner code).
-// Blocks of 256 a multiprocessor should hold: the shading kernels wait on
-// path-state loads far more than they compute (ncu: long-scoreboard stalls,
-// a quarter of the warps resident at 107 registers), so the lean classes
-// trade a few spilled registers for more resident warps.
+// Blocks of 256 a multiprocessor should hold. The plain shading kernels are
+// left to the compiler (forcing 3 blocks of the lean classes, with a few
+// spilled registers, measured no faster); the guided ones would otherwise
+// take up to 211 registers, one block per multiprocessor.
 constexpr int shade_min_blocks(int c, bool guided) {
-    return guided ? 2 : (c == kClassMiss ? 4 : (c == kClassPrincipled ? 2 : (c == kClassGeneric ? 1 : 3)));
+    return guided ? 2 : (c == kClassMiss ? 1 : 1);
 }
 
 template <int C, bool GUIDED>
