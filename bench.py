@@ -55,6 +55,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WIDTH, HEIGHT = 1920, 1080
+# DRAM bytes k_extend moves per ray, from one ncu capture of the same kernel on
+# a 4-spp wave of this workload (299.0 MB read + 136.7 MB written, 8,294,400
+# rays): the ray record, hit record and queue entries, the tree staying in L2
+EXTEND_DRAM_BYTES_PER_RAY = (299.0e6 + 136.7e6) / 8294400
 METRIC = "Mpaths/s at 1080p"
 UNIT = "Mpaths/s"
 
@@ -315,7 +319,11 @@ def run_ours(args):
                          "mrays_per_s": world * (totals["ext"] + totals["sh"]) / (total_ms * 1e-3) / 1e6},
                 "kernel_time_share": shares,
                 "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
-                             "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": None,
+                             "unit": "GB/s", "frac": achieved / peak if peak else None,
+                             "traffic": EXTEND_DRAM_BYTES_PER_RAY * ext_per_launch,
+                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_extend on a "
+                                               "4-spp wave (435.7 MB for 8,294,400 camera rays), scaled to the "
+                                               "rays of an average launch",
                              "peak_source": peak_src, "bytes_per_ray": bytes_per_ray,
                              "avg_launch_ms": ms_ext, "rays_per_launch": ext_per_launch},
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
