@@ -50,7 +50,9 @@ struct GuideState {
     __nv_bfloat16* scratch = nullptr;  // per training CTA: transposed activations of one tile
     int train_ctas = 0;
     long long steps = 0;             // Adam steps taken
-    float3 box_lo{}, box_inv{};      // scene box for the position encoding
+    float3 box_lo{}, box_inv{};      // box of the position encoding: the scene's, then where paths go
+    bool box_fitted = false;         // narrowed to the recorded vertices (once per fresh network)
+    int box_version = 0;             // bumped when the box changes (waves captured before must be re-captured)
     // recording buffers (slot-indexed, grown with the render buffers)
     GuideRecords rec{};
     size_t rec_slots = 0;
@@ -92,6 +94,10 @@ int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed);
 int guide_ensure_records(mypbr_gpu_scene* G, size_t mix_slots, size_t rec_slots, int depth);
 // `steps` Adam steps on batches drawn from the recorded vertices.
 int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaStream_t st);
+// Narrows a fresh network's position box to where the recorded vertices lie
+// (1st to 99th percentile per axis, plus a margin) and re-expresses the
+// records in it. Synchronises the stream once.
+int guide_fit_box(mypbr_gpu_scene* G, cudaStream_t st);
 // The binary tree's device nodes collapsed to four children per node (walk_tree4's layout); depth: deepest level.
 void collapse_to_4(const std::vector<float4>& bin, std::vector<float4>& out, int& depth);
 // The environment's pdf table (p n per texel) and alias table (probability, alias index bits) from its

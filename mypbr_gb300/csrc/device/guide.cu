@@ -502,6 +502,110 @@ int release_guide(GuideState& g) {
     return MYPBR_OK;
 }
 
+// The position encoding's box: the scene's bounding box, until a fresh
+// network's first recorded wave narrows it (guide_fit_box).
+void set_scene_box(mypbr_gpu_scene* G) {
+    GuideState& g = G->guide;
+    float3 lo = G->box_lo, hi = G->box_hi;
+    g.box_lo = lo;
+    g.box_inv = f3(1.0f / fmaxf(hi.x - lo.x, 1e-6f), 1.0f / fmaxf(hi.y - lo.y, 1e-6f), 1.0f / fmaxf(hi.z - lo.z, 1e-6f));
+    g.box_fitted = false;
+    g.box_version++;
+}
+
+constexpr int kBoxBins = 1024;
+
+// histograms of the recorded vertices' positions (in the current box), per axis
+__global__ void k_guide_box_histogram(GuideRecords rec, uint32_t* hist) {
+    uint32_t n = min(*rec.count, rec.capacity);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        float4 s = rec.in0[rec.list[k]];
+        atomicAdd(&hist[0 * kBoxBins + min(int(s.x * kBoxBins), kBoxBins - 1)], 1u);
+        atomicAdd(&hist[1 * kBoxBins + min(int(s.y * kBoxBins), kBoxBins - 1)], 1u);
+        atomicAdd(&hist[2 * kBoxBins + min(int(s.z * kBoxBins), kBoxBins - 1)], 1u);
+    }
+}
+
+// the records' positions re-expressed in the sub-box [a, b] of the current one
+__global__ void k_guide_box_rescale(GuideRecords rec, float3 a, float3 inv_width) {
+    uint32_t n = min(*rec.count, rec.capacity);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        uint32_t r = rec.list[k];
+        float4 s = rec.in0[r];
+        s.x = clampf((s.x - a.x) * inv_width.x, 0.0f, 1.0f);
+        s.y = clampf((s.y - a.y) * inv_width.y, 0.0f, 1.0f);
+        s.z = clampf((s.z - a.z) * inv_width.z, 0.0f, 1.0f);
+        rec.in0[r] = s;
+    }
+}
+
+int guide_fit_box(mypbr_gpu_scene* G, cudaStream_t st) {
+    GuideState& g = G->guide;
+    if (g.box_fitted)
+        return MYPBR_OK;
+    g.box_fitted = true;
+    uint32_t* hist = nullptr;
+    MYPBR_CUDA(cudaMalloc(&hist, 3 * kBoxBins * sizeof(uint32_t)));
+    std::vector<uint32_t> h(3 * kBoxBins);
+    int rc = MYPBR_OK;
+    if (cudaMemsetAsync(hist, 0, 3 * kBoxBins * sizeof(uint32_t), st) != cudaSuccess)
+        rc = cuda_fail(cudaGetLastError(), "guide_fit_box");
+    if (rc == MYPBR_OK) {
+        k_guide_box_histogram<<<4 * G->sm_count, 256, 0, st>>>(g.rec, hist);
+        if (cudaMemcpyAsync(h.data(), hist, h.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            rc = cuda_fail(cudaGetLastError(), "guide_fit_box");
+    }
+    cudaFree(hist);
+    if (rc != MYPBR_OK)
+        return rc;
+    // per axis: the 1st and 99th percentiles, widened by a tenth of their span
+    float a[3], b[3];
+    bool narrower = false;
+    for (int axis = 0; axis < 3; axis++) {
+        const uint32_t* H = &h[size_t(axis) * kBoxBins];
+        uint64_t total = 0;
+        for (int k = 0; k < kBoxBins; k++)
+            total += H[k];
+        if (total < 1024)
+            return MYPBR_OK;  // too few vertices to judge: the scene box stays
+        uint64_t run = 0;
+        int lo = 0, hi = kBoxBins - 1;
+        for (int k = 0; k < kBoxBins; k++) {
+            run += H[k];
+            if (run * 100 >= total) {
+                lo = k;
+                break;
+            }
+        }
+        run = 0;
+        for (int k = kBoxBins - 1; k >= 0; k--) {
+            run += H[k];
+            if (run * 100 >= total) {
+                hi = k;
+                break;
+            }
+        }
+        float x0 = float(lo) / kBoxBins, x1 = float(hi + 1) / kBoxBins;
+        float margin = 0.1f * (x1 - x0) + 1.0f / kBoxBins;
+        a[axis] = fmaxf(0.0f, x0 - margin);
+        b[axis] = fminf(1.0f, x1 + margin);
+        narrower = narrower || (b[axis] - a[axis]) < 0.8f;
+    }
+    if (!narrower)
+        return MYPBR_OK;
+    float3 A = make_float3(a[0], a[1], a[2]);
+    float3 inv = make_float3(1.0f / (b[0] - a[0]), 1.0f / (b[1] - a[1]), 1.0f / (b[2] - a[2]));
+    k_guide_box_rescale<<<4 * G->sm_count, 256, 0, st>>>(g.rec, A, inv);
+    MYPBR_CUDA(cudaGetLastError());
+    // the new box in world units: lo + a / inv_old, width (b - a) / inv_old
+    float3 lo0 = g.box_lo, inv0 = g.box_inv;
+    g.box_lo = make_float3(lo0.x + a[0] / inv0.x, lo0.y + a[1] / inv0.y, lo0.z + a[2] / inv0.z);
+    g.box_inv = make_float3(inv0.x / (b[0] - a[0]), inv0.y / (b[1] - a[1]), inv0.z / (b[2] - a[2]));
+    g.box_version++;
+    return MYPBR_OK;
+}
+
 int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed) {
     GuideState& g = G->guide;
     if (g.hidden == hidden)
@@ -538,10 +642,7 @@ int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed) {
     k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
     MYPBR_CUDA(cudaGetLastError());
     g.steps = 0;
-    // the position encoding spans the scene's bounding box
-    float3 lo = G->box_lo, hi = G->box_hi;
-    g.box_lo = lo;
-    g.box_inv = f3(1.0f / fmaxf(hi.x - lo.x, 1e-6f), 1.0f / fmaxf(hi.y - lo.y, 1e-6f), 1.0f / fmaxf(hi.z - lo.z, 1e-6f));
+    set_scene_box(G);
     return MYPBR_OK;
 }
 
@@ -626,6 +727,7 @@ int mypbr_guide_reset(mypbr_gpu_scene* scene) {
     MYPBR_CUDA(cudaGetLastError());
     MYPBR_CUDA(cudaDeviceSynchronize());
     g.steps = 0;
+    set_scene_box(scene);
     return MYPBR_OK;
 }
 

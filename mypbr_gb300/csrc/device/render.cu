@@ -1227,6 +1227,19 @@ int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int sav
     int s = launch_wave(P, R.L, st, launches, T, graph);
     if (s != MYPBR_OK)
         return s;
+    if (R.guided && P.record && !G->guide.box_fitted && G->guide.steps == 0) {
+        // a fresh network: its position encoding is narrowed to where this
+        // wave's vertices lie before it learns anything
+        int version = G->guide.box_version;
+        if ((s = guide_fit_box(G, st)) != MYPBR_OK)
+            return s;
+        if (G->guide.box_version != version) {
+            P.guide_lo = G->guide.box_lo;
+            P.guide_inv = G->guide.box_inv;
+            if (graph)
+                graph->key = -1;  // the captured kernels hold the old box
+        }
+    }
     if (R.guided && P.record) {
         if ((s = T.begin(4)) != MYPBR_OK)
             return s;
