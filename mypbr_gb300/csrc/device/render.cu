@@ -36,6 +36,10 @@ constexpr uint32_t kFlagSeen = 2u;
 // Shading classes: each has its own queue and kernel, so a warp shades one
 // kind of material and each kernel carries only that material's code.
 constexpr int kShadeClasses = 6;
+// Bounces at which guided renders sample the learned mixture (the network
+// is trained on the first kGuideRecordDepth vertices of a path).
+constexpr int kGuideDepths = 16;
+
 enum : int { kClassMiss = 0, kClassLambert = 1, kClassMetal = 2, kClassDielectric = 3, kClassPrincipled = 4,
              kClassGeneric = 5 };
 
@@ -488,7 +492,7 @@ __global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(Wave
                 GuideMix gm;
                 bool use_guide = false;
                 if constexpr (GUIDED && kGuidable<C>()) {
-                    if (P.guided && P.guide_alpha > 0.0f && !vol) {
+                    if (P.guided && P.guide_alpha > 0.0f && !vol && depth < kGuideDepths) {
                         guide_unpack(P.guide_mix[slot], gm);
                         use_guide = true;
                     }
@@ -1015,7 +1019,7 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
             TIMED(1, (k_extend_pt<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else
             TIMED(1, (launch_bounce_kernel(extend_kernel(P.S.has_voxels, L.walk), L.grid_extend, L.block, st, P, depth)));
-        if (P.guided) {  // the mixtures of this bounce's guidable vertices
+        if (P.guided && depth < kGuideDepths) {  // the mixtures of this bounce's guidable vertices
             TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
                          L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
             launches++;
