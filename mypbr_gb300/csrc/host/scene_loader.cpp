@@ -888,13 +888,9 @@ class Loader {
             } else if (e.ks.length_squared() > 0) {
                 double roughness = std::sqrt(std::sqrt(2 / (std::fmax(e.ns, 0.0) + 2)));
                 double ior = e.ni > 1 ? e.ni : 1.5;
-                m = blank_material(MYPBR_MAT_PRINCIPLED);
-                double r0 = (ior - 1) / (ior + 1);
-                m.p[0] = r0 * r0;
-                m.tex[0] = base >= 0 ? base : add_texture_solid(e.kd);
-                m.tex[1] = add_texture_solid(V3(0, 0, 0));
-                m.tex[2] = add_texture_solid(V3(roughness, roughness, roughness));
-                m.p[13] = m.p[14] = m.p[15] = 1;
+                int color = base >= 0 ? base : add_texture_solid(e.kd);
+                int metallic = add_texture_solid(V3(0, 0, 0));
+                m = principled_desc(color, metallic, add_texture_solid(V3(roughness, roughness, roughness)), ior);
             } else {
                 m = blank_material(MYPBR_MAT_LAMBERTIAN);
                 m.tex[0] = base >= 0 ? base : add_texture_solid(e.kd);
