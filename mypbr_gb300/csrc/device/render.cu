@@ -36,9 +36,12 @@ constexpr uint32_t kFlagSeen = 2u;
 // Shading classes: each has its own queue and kernel, so a warp shades one
 // kind of material and each kernel carries only that material's code.
 constexpr int kShadeClasses = 6;
-// Bounces at which guided renders sample the learned mixture (the network
-// is trained on the first kGuideRecordDepth vertices of a path).
-constexpr int kGuideDepths = 16;
+// Bounces at which guided renders sample the learned mixture: the first two
+// scattering events of a path, which decide most of what the camera sees
+// (the network is trained on the first kGuideRecordDepth vertices). On the
+// occluded voxel hall, guiding every bounce cost 14 % more time for no
+// measurable drop in error.
+constexpr int kGuideDepths = 2;
 
 enum : int { kClassMiss = 0, kClassLambert = 1, kClassMetal = 2, kClassDielectric = 3, kClassPrincipled = 4,
              kClassGeneric = 5 };
