@@ -28,9 +28,19 @@ rendered at --hall-width x 9/16 with max depth 16. relMSE = mean over pixels
 and channels of (x - r)^2 / (r^2 + 0.01) against a plain render at --ref-spp
 samples (FP64 film). Each method renders at doubling spp (a fresh, untrained
 network for every guided render, so training time is inside each timing)
-until relMSE <= 0.01; the time there is interpolated log-log between the two
-bracketing renders, or extrapolated as relMSE ~ 1/spp past the last one. The
-CPU figure extrapolates the oracle's relMSE the same way from a bounded run.
+until relMSE <= 0.01 or --max-spp; the time there is interpolated log-log
+between the two bracketing renders, or extrapolated as relMSE = c/spp with c
+fitted to the three highest-spp renders. The oracle is the plain estimator
+itself, so the CPU figure is the plain curve's spp to target at the oracle's
+measured seconds per spp (a bounded run on every host core).
+
+cornell / triangle_room: Mpaths/s of C1 / C3 (render_ex, scene resident),
+the oracle beside it; with --hidden H the triangle room also renders guided
+and compares plain and guided relMSE at equal time against --c3-ref-spp.
+batch: C4, 64 scenes in one mypbr_gpu_render_batch call with feature guides,
+every frame denoised, per-scene relMSE against 4x-spp renders.
+--traversal 0..3 picks the walk (binary; lanes taking new rays; 4-wide tree;
+binary with postponed leaves), --block the threads per block.
 
 --impl reference times the CPU implementation of the same path (the FP64
 restatement of the reference's camera::render in oracle/, on every host core)
