@@ -204,8 +204,14 @@ bool make_accessor(Doc& d, long long index, Accessor& a) {
     }
     a.count = size_t(count);
     const Json* bv = j->find("bufferView");
-    if (!bv || bv->kind != Json::Number)
+    if (!bv || bv->kind != Json::Number) {
+        // all zeros: sized by the count alone, which must stay sane
+        if (a.count > (size_t(1) << 24)) {
+            d.error = "accessor " + std::to_string(index) + " has no data for its " + std::to_string(count) + " elements";
+            return false;
+        }
         return true;
+    }
     size_t length, stride;
     const uint8_t* bytes = view_bytes(d, (long long)bv->number, length, stride);
     long long off = j->integer("byteOffset", 0);
