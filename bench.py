@@ -335,7 +335,12 @@ def run_ours(args):
                                                "4-spp wave (435.7 MB for 8,294,400 camera rays), scaled to the "
                                                "rays of an average launch",
                              "peak_source": peak_src, "bytes_per_ray": bytes_per_ray,
-                             "avg_launch_ms": ms_ext, "rays_per_launch": ext_per_launch},
+                             "avg_launch_ms": ms_ext, "rays_per_launch": ext_per_launch,
+                             # the walk's real bound is instruction issue under divergence: the
+                             # same ncu capture's issue-slot utilisation and lanes per instruction
+                             "issue": {"issue_active_frac": [0.587, 0.610], "threads_per_instruction": [26.6, 12.9],
+                                       "source": "ncu smsp__issue_active and smsp__thread_inst_executed_per_"
+                                                 "inst_executed of k_extend, bounces 0 and 1 of a 4-spp wave"}},
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(w * h * 3 * 8)},
                 "clocks": clk}
