@@ -75,3 +75,21 @@ def test_device_bvh_on_a_triangle_room():
     b = cam.render(G2).radiance
     close = np.isclose(a, b, rtol=1e-5, atol=1e-6)
     assert close.mean() > 0.999, close.mean()
+
+
+@pytest.mark.parametrize("traversal", [2, 3])
+def test_device_bvh_with_the_other_walks(traversal):
+    """After an LBVH rebuild the 4-wide tree is rebuilt from it and the
+    postponed-leaf walk stays allowed: both render what the binary walk does."""
+    sc = mp.load_scene(scene_path("materials.scene"))
+    G = mp.GpuScene(sc)
+    mp.rebuild_bvh(G)
+    cam = sc.camera
+    cam.image_width = 48
+    cam.samples_per_pixel = 16
+    cam.seed = 3
+    mp.set_launch(G, traversal=0)
+    a = cam.render(G).radiance
+    mp.set_launch(G, traversal=traversal)
+    b = cam.render(G).radiance
+    np.testing.assert_allclose(b, a, rtol=1e-5, atol=1e-7)
