@@ -1034,7 +1034,6 @@ MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, flo
         TriRay tr = make_tri_ray(d);
         int stack[kBvhStack];
         int sp = 0;
-        int top = -1;  // the stack's top entry (-1: empty), held out of memory
         int node = 0;
         // A tree walk enters each interior node at most once; the cap only
         // guards against a malformed tree, which it reports instead of spinning.
@@ -1106,22 +1105,16 @@ MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, flo
                     atomicCAS(S.error, 0, 2);
                     break;
                 }
-                // the stack's top entry lives in a register: a pop hands it
-                // over at once and refills it from memory while the popped
-                // node is fetched
-                if (top >= 0)
-                    stack[sp++] = top;
-                top = first0 ? i1 : i0;
+                stack[sp++] = first0 ? i1 : i0;
                 node = first0 ? i0 : i1;
             } else if (h0) {
                 node = i0;
             } else if (h1) {
                 node = i1;
             } else {
-                if (top < 0)
+                if (sp == 0)
                     break;
-                node = top;
-                top = sp > 0 ? stack[--sp] : -1;
+                node = stack[--sp];
             }
         }
     }
