@@ -460,14 +460,19 @@ def run_voxel_hall(args):
     print(json.dumps(line), flush=True)
 
 
-def render_rate(mp, scene, spp, steps, warmup, guided=0, block=0, traversal=0):
+def render_rate(mp, scene, spp, steps, warmup, guided=0, block=0, traversal=0, tune=None):
     """Device-resident Mpaths/s of a scene (CUDA events around the render on
-    the scene handle's stream is what mypbr_gpu_render_ex times)."""
+    the scene handle's stream is what mypbr_gpu_render_ex times). With tune
+    (a dict), the autotuner picks the launch settings first and tune gets its
+    choice."""
     cam = scene.camera
     cam.samples_per_pixel = spp
     cam.guided = guided
     G = mp.GpuScene(scene)
     mp.set_launch(G, block=block, traversal=traversal)
+    if tune is not None:
+        r = mp.autotune(cam, G)
+        tune.update({k: r[k] for k in ("block", "traversal", "wave_paths")})
     times = []
     st = None
     for k in range(warmup + steps):
@@ -531,7 +536,11 @@ def run_simple(args, workload):
             scene = mp.load_scene(triangle_room_scene(d))
             spp, cfg = 64, {"workload": "triangle_room_2m", "width": 1920, "height": 1080, "spp": 64,
                             "max_depth": 12, "triangles": 1985856, "materials": "32 principled", "lights": 16}
-    value, t, st = render_rate(mp, scene, spp, args.steps, args.warmup, block=args.block, traversal=args.traversal)
+    tune = {} if args.autotune else None
+    value, t, st = render_rate(mp, scene, spp, args.steps, args.warmup, block=args.block, traversal=args.traversal,
+                               tune=tune)
+    if tune:
+        cfg = dict(cfg, launch=dict(tune, chosen_by="mypbr_gpu_autotune"))
     line = {"metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "dtype": "fp32",
             "data": "synthetic", "config": cfg,
@@ -686,6 +695,7 @@ def main():
     p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3],
                    help="1: extend lanes take new rays as theirs finish; 2: the 4-wide tree; 3: postponed leaves")
     p.add_argument("--block", type=int, default=0, choices=[0, 128, 256])
+    p.add_argument("--autotune", action="store_true", help="cornell / triangle_room: autotuned launch settings")
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--ref-spp", type=int, default=65536)

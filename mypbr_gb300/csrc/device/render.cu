@@ -411,8 +411,11 @@ __global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(Wave
     uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         uint32_t slot = q[k];
-        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
-        float4 bt = P.B.beta[slot], rad4 = P.B.radiance[slot];
+        // the path's state, read once (streaming loads: no reuse to cache for),
+        // the hit record with it so that all five loads are in flight together
+        float4 ro = __ldcs(&P.B.ray_o[slot]), rd = __ldcs(&P.B.ray_d[slot]);
+        float4 bt = __ldcs(&P.B.beta[slot]), rad4 = __ldcs(&P.B.radiance[slot]);
+        float4 hb = C == kClassMiss ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : __ldcs(&P.B.hit[slot]);
         uint32_t pixel = f_bits(rad4.w), pass = f_bits(bt.w), flags = f_bits(ro.w);
         float3 o = f3(ro), d = f3(rd), beta = f3(bt), rad = f3(rad4);
         float scatter_pdf = rd.w;
@@ -447,7 +450,6 @@ __global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(Wave
             terminate = true;
         } else {
             Rng g = bounce_rng(P, pixel, pass, depth, 0);
-            float4 hb = P.B.hit[slot];
             HitInfo h;
             h.t = hb.x;
             h.b1 = hb.y;
