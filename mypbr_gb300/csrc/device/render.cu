@@ -394,16 +394,8 @@ constexpr bool kGuidable() {
 // One bounce of ray_color (camera.h:370-457) for the paths of shading class C.
 // GUIDED: the variant of guided renders, which reads the learned mixtures and
 // writes training records (plain renders keep the leaner code).
-// Blocks of 256 a multiprocessor should hold. The plain shading kernels are
-// left to the compiler (forcing 3 blocks of the lean classes, with a few
-// spilled registers, measured no faster); the guided ones would otherwise
-// take up to 211 registers, one block per multiprocessor.
-constexpr int shade_min_blocks(int c, bool guided) {
-    return guided ? 2 : (c == kClassMiss ? 1 : 1);
-}
-
 template <int C, bool GUIDED>
-__global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(WaveParams P, int depth) {
+__device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
     uint32_t n = *class_counter(P, depth, C);
     const uint32_t* q = class_queue(P, C);
     uint32_t* q_next = P.B.queue[(depth + 1) & 1];
@@ -411,11 +403,8 @@ __global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(Wave
     uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         uint32_t slot = q[k];
-        // the path's state, read once (streaming loads: no reuse to cache for),
-        // the hit record with it so that all five loads are in flight together
-        float4 ro = __ldcs(&P.B.ray_o[slot]), rd = __ldcs(&P.B.ray_d[slot]);
-        float4 bt = __ldcs(&P.B.beta[slot]), rad4 = __ldcs(&P.B.radiance[slot]);
-        float4 hb = C == kClassMiss ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : __ldcs(&P.B.hit[slot]);
+        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot];
+        float4 bt = P.B.beta[slot], rad4 = P.B.radiance[slot];
         uint32_t pixel = f_bits(rad4.w), pass = f_bits(bt.w), flags = f_bits(ro.w);
         float3 o = f3(ro), d = f3(rd), beta = f3(bt), rad = f3(rad4);
         float scatter_pdf = rd.w;
@@ -450,6 +439,7 @@ __global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(Wave
             terminate = true;
         } else {
             Rng g = bounce_rng(P, pixel, pass, depth, 0);
+            float4 hb = P.B.hit[slot];
             HitInfo h;
             h.t = hb.x;
             h.b1 = hb.y;
@@ -601,6 +591,20 @@ __global__ void __launch_bounds__(256, shade_min_blocks(C, GUIDED)) k_shade(Wave
         P.B.radiance[slot] = make_float4(rad.x, rad.y, rad.z, rad4.w);
         q_next[warp_push(ext_counter(P, depth + 1))] = slot;
     }
+}
+
+// The shading kernels. The plain ones leave registers to the compiler
+// (requiring one or three resident blocks instead, with more registers or a
+// few spills, measured 2.5 % slower on the sphere field); the guided ones
+// would take up to 211 registers, one block of 256 per multiprocessor, and
+// are held to two (a guided render 19 % faster).
+template <int C>
+__global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
+    shade_body<C, false>(P, depth);
+}
+template <int C>
+__global__ void __launch_bounds__(256, 2) k_shade_guided(WaveParams P, int depth) {
+    shade_body<C, true>(P, depth);
 }
 
 template <bool VOX, int WALK>
@@ -929,9 +933,9 @@ Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
     L.grid_shadow = G.sm_count * std::max(per_sm, 1);
     L.grid_stream = G.sm_count * 8;
     int worst = 1;
-    for (auto f : {(const void*)k_shade<kClassMiss, false>, (const void*)k_shade<kClassLambert, false>,
-                   (const void*)k_shade<kClassMetal, false>, (const void*)k_shade<kClassDielectric, false>,
-                   (const void*)k_shade<kClassPrincipled, false>, (const void*)k_shade<kClassGeneric, false>}) {
+    for (auto f : {(const void*)k_shade<kClassMiss>, (const void*)k_shade<kClassLambert>,
+                   (const void*)k_shade<kClassMetal>, (const void*)k_shade<kClassDielectric>,
+                   (const void*)k_shade<kClassPrincipled>, (const void*)k_shade<kClassGeneric>}) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, L.block, 0);
         worst = std::max(worst, per_sm);
     }
@@ -1030,19 +1034,19 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
             launches++;
         }
         if (L.guided_kernels) {
-            TIMED(2, (k_shade<kClassMiss, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassLambert, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassMetal, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassDielectric, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassPrincipled, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassGeneric, true><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade_guided<kClassMiss><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade_guided<kClassLambert><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade_guided<kClassMetal><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade_guided<kClassDielectric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade_guided<kClassPrincipled><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade_guided<kClassGeneric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
         } else {
-            TIMED(2, (k_shade<kClassMiss, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassLambert, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassMetal, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassDielectric, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassPrincipled, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassGeneric, false><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMiss><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassLambert><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassMetal><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassDielectric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassPrincipled><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+            TIMED(2, (k_shade<kClassGeneric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
         }
         TIMED(3, (launch_bounce_kernel(shadow_kernel(P.S.has_voxels, L.walk), L.grid_shadow, L.block, st, P, depth)));
         launches += 2 + kShadeClasses;
