@@ -690,6 +690,12 @@ int mypbr_env_distribution(const float* rgb, int32_t width, int32_t height, floa
 int mypbr_write_image(const char* path, const double* radiance, int32_t width, int32_t height,
                       const mypbr_display_opts* opts, int on_device);
 
+/* The failure path of the device's bounded waits, without a fault: one CTA
+ * waits on an mbarrier phase that nothing completes, gives up after about a
+ * second, and this returns MYPBR_ERR_DEVICE_TIMEOUT; the context stays
+ * usable. For tests. */
+int mypbr_gpu_test_wait_timeout(void);
+
 /* ----------------------------------------------------- path guiding
  *
  * No counterpart in the reference: a learned sampling proposal, used by

@@ -132,6 +132,7 @@ def lib():
     L.mypbr_ggx_albedo_table.argtypes = [dp]
     L.mypbr_gpu_denoise.argtypes = [vp, vp, vp, vp, ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int]
     L.mypbr_env_distribution.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int]
+    L.mypbr_gpu_test_wait_timeout.argtypes = []
     i32p = ctypes.POINTER(ctypes.c_int32)
     L.mypbr_image_read.argtypes = [ctypes.c_char_p, i32p, i32p, i32p, vp, ctypes.c_int64]
     L.mypbr_camera_init.argtypes = [ctypes.POINTER(CameraStruct)]

@@ -485,9 +485,21 @@ int read_error(int* err) {
     MYPBR_CUDA(cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost));
     if (e != 0) {
         set_error_message("a tensor-core wait of the guiding network timed out");
-        return MYPBR_ERR_DEVICE_CHECK;
+        return MYPBR_ERR_DEVICE_TIMEOUT;
     }
     return MYPBR_OK;
+}
+
+// One CTA waits, through the same bounded wait the tensor-core kernels use,
+// on an mbarrier phase nothing completes: after the wait's limit (about a
+// second of clocks) it records the timeout in the error word and returns.
+__global__ void k_wait_probe(int* err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0)
+        tc::bar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0 && !tc::bar_wait(&bar, 0))
+        atomicCAS(err, 0, 3);
 }
 
 }  // namespace
@@ -849,3 +861,27 @@ int mypbr_guide_test_mixture(const float* raw, const float* u, const float* dirs
 }
 
 }  // extern "C"
+
+// The failure path of the bounded device waits, exercised without a fault:
+// a wait that nothing ends gives up, the host reads MYPBR_ERR_DEVICE_TIMEOUT,
+// and the context stays usable.
+extern "C" int mypbr_gpu_test_wait_timeout(void) {
+    using namespace mypbr_dev;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        set_error_message("mypbr_gpu_test_wait_timeout: no CUDA device");
+        return MYPBR_ERR_NO_DEVICE;
+    }
+    int* err = nullptr;
+    MYPBR_CUDA(cudaMalloc(&err, sizeof(int)));
+    int rc = MYPBR_OK;
+    if (cudaMemset(err, 0, sizeof(int)) != cudaSuccess)
+        rc = cuda_fail(cudaGetLastError(), "mypbr_gpu_test_wait_timeout");
+    if (rc == MYPBR_OK) {
+        k_wait_probe<<<1, 32>>>(err);
+        cudaError_t e = cudaDeviceSynchronize();
+        rc = e != cudaSuccess ? cuda_fail(e, "k_wait_probe") : read_error(err);
+    }
+    cudaFree(err);
+    return rc;
+}

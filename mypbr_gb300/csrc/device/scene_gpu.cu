@@ -874,6 +874,10 @@ int check_device_error(mypbr_gpu_scene* G) {
         return MYPBR_OK;
     int zero = 0;
     MYPBR_CUDA(cudaMemcpy(G->dev.error, &zero, sizeof zero, cudaMemcpyHostToDevice));
+    if (e == 3) {
+        set_error_message("device wait: a tensor-core wait of the guiding network ran past its limit");
+        return MYPBR_ERR_DEVICE_TIMEOUT;
+    }
     set_error_message(e == 1 ? "device check: a BVH walk visited more nodes than the tree has"
                              : "device check: a BVH walk overflowed its stack");
     return MYPBR_ERR_DEVICE_CHECK;
