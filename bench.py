@@ -460,7 +460,7 @@ def run_voxel_hall(args):
     print(json.dumps(line), flush=True)
 
 
-def render_rate(mp, scene, spp, steps, warmup, guided=0, block=0, traversal=0, tune=None):
+def render_rate(mp, scene, spp, steps, warmup, guided=0, block=0, traversal=0, tune=None, wave_paths=0):
     """Device-resident Mpaths/s of a scene (CUDA events around the render on
     the scene handle's stream is what mypbr_gpu_render_ex times). With tune
     (a dict), the autotuner picks the launch settings first and tune gets its
@@ -469,7 +469,7 @@ def render_rate(mp, scene, spp, steps, warmup, guided=0, block=0, traversal=0, t
     cam.samples_per_pixel = spp
     cam.guided = guided
     G = mp.GpuScene(scene)
-    mp.set_launch(G, block=block, traversal=traversal)
+    mp.set_launch(G, block=block, wave_paths=wave_paths, traversal=traversal)
     if tune is not None:
         r = mp.autotune(cam, G)
         tune.update({k: r[k] for k in ("block", "traversal", "wave_paths")})
@@ -538,7 +538,7 @@ def run_simple(args, workload):
                             "max_depth": 12, "triangles": 1985856, "materials": "32 principled", "lights": 16}
     tune = {} if args.autotune else None
     value, t, st = render_rate(mp, scene, spp, args.steps, args.warmup, block=args.block, traversal=args.traversal,
-                               tune=tune)
+                               tune=tune, wave_paths=args.wave_paths)
     if tune:
         cfg = dict(cfg, launch=dict(tune, chosen_by="mypbr_gpu_autotune"))
     line = {"metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
@@ -696,6 +696,7 @@ def main():
                    help="1: extend lanes take new rays as theirs finish; 2: the 4-wide tree; 3: postponed leaves")
     p.add_argument("--block", type=int, default=0, choices=[0, 128, 256])
     p.add_argument("--autotune", action="store_true", help="cornell / triangle_room: autotuned launch settings")
+    p.add_argument("--wave-paths", type=int, default=0, help="cornell / triangle_room: paths per wave (0: default)")
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--ref-spp", type=int, default=65536)
