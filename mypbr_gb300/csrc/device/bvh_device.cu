@@ -293,6 +293,7 @@ struct DevArr {
 using namespace mypbr_dev;
 
 extern "C" int mypbr_gpu_scene_rebuild_bvh(mypbr_gpu_scene* G, int32_t method, mypbr_bvh_report* report) {
+    mypbr_dev::NvtxRange range("mypbr LBVH build");
     if (!G || method != MYPBR_BVH_LBVH) {
         set_error_message("mypbr_gpu_scene_rebuild_bvh: a scene and MYPBR_BVH_LBVH are required");
         return MYPBR_ERR_INVALID_ARGUMENT;

@@ -189,6 +189,7 @@ extern "C" void mypbr_denoise_opts_init(mypbr_denoise_opts* o) {
 extern "C" int mypbr_gpu_denoise(const double* radiance, const double* albedo, const double* normal,
                                  const double* variance, int32_t width, int32_t height, const mypbr_denoise_opts* opts,
                                  double* out, int on_device) {
+    mypbr_dev::NvtxRange range("mypbr denoise");
     if (!radiance || !albedo || !normal || !variance || !out || width < 1 || height < 1)
         return bad("mypbr_gpu_denoise: bad argument");
     mypbr_denoise_opts o;

@@ -140,6 +140,7 @@ __global__ void k_env_alias(const double* q, const uint32_t* order, const double
 // rgb: device, w * h * 3 floats. Writes device texel_pdf (n floats) and
 // alias (n float2: probability, alias index bits).
 int build_env_distribution(const float* rgb, int w, int h, float* texel_pdf, float2* alias, cudaStream_t st) {
+    NvtxRange range("mypbr environment tables");
     size_t n = size_t(w) * h;
     if (n == 0)
         return MYPBR_OK;

@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../../include/mypbr_gpu.h"
 #include "guide.cuh"
 
@@ -82,6 +84,15 @@ struct mypbr_gpu_scene {
 };
 
 namespace mypbr_dev {
+
+// An NVTX range around a stage (render, wave, training, uploads, builds), for
+// profilers that show them; nothing is recorded unless a tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 void set_error_message(const std::string& m);
 int cuda_fail(cudaError_t e, const char* what);

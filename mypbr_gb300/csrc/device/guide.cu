@@ -693,6 +693,7 @@ int guide_ensure_records(mypbr_gpu_scene* G, size_t mix_slots, size_t slots, int
 }
 
 int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaStream_t st) {
+    NvtxRange range("mypbr guide training");
     GuideState& g = G->guide;
     if (g.hidden == 0 || g.rec.count == nullptr)
         return MYPBR_OK;

@@ -1223,6 +1223,7 @@ int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts
 // renders the training steps on what the wave recorded.
 int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int save_every, cudaStream_t st,
                 uint64_t& launches, KernelTimer& T, WaveGraph* graph) {
+    NvtxRange range("mypbr wave");
     WaveParams& P = R.P;
     bool train_wave = R.guided && wave < kGuideTrainWaves;
     P.pass0 = pass0;
@@ -1276,6 +1277,7 @@ struct Totals {
 int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_rad, double* d_alb, double* d_nrm,
                double* d_var, double* d_chvar, int save_every, mypbr_pass_callback cb, void* user,
                double* h_rad, double* h_alb, double* h_nrm, double* h_var, mypbr_render_stats* stats) {
+    NvtxRange range("mypbr render");
     WaveParams& P = R.P;
     Totals tot;
     MYPBR_CUDA(cudaMalloc(&tot.d, 2 * sizeof(unsigned long long)));

@@ -857,6 +857,7 @@ void collapse_to_4(const std::vector<float4>& bin, std::vector<float4>& out, int
 }  // namespace mypbr_dev
 
 extern "C" int mypbr_gpu_scene_create(const mypbr_flat_scene* scene, mypbr_gpu_scene** out) {
+    mypbr_dev::NvtxRange range("mypbr scene upload");
     try {
         return mypbr_dev::create_scene(scene, out);
     } catch (const std::bad_alloc&) {
