@@ -39,8 +39,9 @@ the oracle beside it; with --hidden H the triangle room also renders guided
 and compares plain and guided relMSE at equal time against --c3-ref-spp.
 batch: C4, 64 scenes in one mypbr_gpu_render_batch call with feature guides,
 every frame denoised, per-scene relMSE against 4x-spp renders.
---traversal 0..3 picks the walk (binary; lanes taking new rays; 4-wide tree;
-binary with postponed leaves), --block the threads per block.
+--traversal 0..4 picks the walk (the scene's default: postponed leaves where
+triangles fill most leaves, else binary; lanes taking new rays; 4-wide tree;
+postponed leaves; plain binary), --block the threads per block.
 
 --impl reference times the CPU implementation of the same path (the FP64
 restatement of the reference's camera::render in oracle/, on every host core)
@@ -692,8 +693,9 @@ def main():
                                           "hall_render"], default="sphere_field")
     p.add_argument("--hall-size", type=int, default=512)
     p.add_argument("--per-wave", type=int, default=0)
-    p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3],
-                   help="1: extend lanes take new rays as theirs finish; 2: the 4-wide tree; 3: postponed leaves")
+    p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                   help="0: the scene's default; 1: extend lanes take new rays as theirs finish; 2: the 4-wide "
+                        "tree; 3: postponed leaves; 4: the plain binary walk")
     p.add_argument("--block", type=int, default=0, choices=[0, 128, 256])
     p.add_argument("--autotune", action="store_true", help="cornell / triangle_room: autotuned launch settings")
     p.add_argument("--wave-paths", type=int, default=0, help="cornell / triangle_room: paths per wave (0: default)")

@@ -609,13 +609,14 @@ typedef struct mypbr_batch_job {
 int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n);
 
 /* The autotuner's choice for a scene handle and view: threads per block of
- * the bounce kernels, paths per wave and the traversal scheme (0: each lane
- * walks its ray to the end over the binary tree; 1: lanes take new rays as
- * theirs finish; 2: as 0 over the tree collapsed to 4 children per node;
- * 3: as 0 with leaves postponed until the warp's lanes all hold one), with
- * the Mpaths/s of each of the 32 trials (traversal 0 to 3; within each,
- * block 128 then 256; within each, 4M, 8M, 16M, 32M paths; 0 for trials
- * skipped because the scene's tree does not allow that walk). */
+ * the bounce kernels, paths per wave and the traversal scheme (1: lanes take
+ * new rays as theirs finish; 2: each lane walks its ray to the end over the
+ * tree collapsed to 4 children per node; 3: the binary tree with leaves
+ * postponed until the warp's lanes all hold one; 4: the plain binary walk;
+ * 0, the default, is 3 for trees whose leaves are mostly triangles and 4
+ * otherwise), with the Mpaths/s of each of the 32 trials (traversal 1 to 4;
+ * within each, block 128 then 256; within each, 4M, 8M, 16M, 32M paths; 0
+ * for trials skipped because the scene's tree does not allow that walk). */
 typedef struct mypbr_tune_result {
     int32_t block;
     int32_t traversal;
@@ -627,7 +628,7 @@ typedef struct mypbr_tune_result {
 /* Sets the launch settings the autotuner would set (0 keeps a setting's
  * default: block 256, 32M paths per wave, traversal 0). A traversal the
  * scene's tree does not allow (2 without a 4-wide tree, 3 with leaves of 16
- * or more references) walks the binary tree as 0 does. */
+ * or more references) walks the plain binary tree. */
 int mypbr_gpu_set_launch(mypbr_gpu_scene* scene, int32_t block, int64_t wave_paths, int32_t traversal);
 
 /* Times short renders of the view with each setting and keeps the fastest on

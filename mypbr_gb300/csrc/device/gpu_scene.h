@@ -79,8 +79,9 @@ struct mypbr_gpu_scene {
     // autotuned launch settings (0: built-in defaults)
     size_t tuned_wave_paths = 0;
     int tuned_block = 0;
-    int tuned_traversal = 0;  // 0: one ray per lane to the end (k_extend); 1: lanes take new rays (k_extend_pt);
-                              // 2: as 0 over the 4-wide tree
+    int tuned_traversal = 0;  // 0: the scene's default (3 or 4); 1: lanes take new rays (k_extend_pt);
+                              // 2: the 4-wide tree; 3: postponed leaves; 4: the plain binary walk
+    bool prefer_postponed = false;  // triangles fill most leaves: traversal 0 means 3
 };
 
 namespace mypbr_dev {

@@ -918,10 +918,15 @@ const void* shadow_kernel(bool vox, int walk) {
 Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
     Launch L{};
     L.block = block == 128 || block == 256 ? block : (G.tuned_block ? G.tuned_block : 256);
-    L.persistent = G.tuned_traversal == 1;
-    if (G.tuned_traversal == 2 && G.dev.bvh4 != nullptr)
+    // traversal 0 is the scene's default: leaves postponed where triangles
+    // fill most of the leaves (their tests diverge), the plain binary walk else
+    int trav = G.tuned_traversal;
+    if (trav == 0)
+        trav = G.prefer_postponed && G.dev.postponed_ok ? 3 : 4;
+    L.persistent = trav == 1;
+    if (trav == 2 && G.dev.bvh4 != nullptr)
         L.walk = kWalkWide;
-    else if (G.tuned_traversal == 3 && G.dev.postponed_ok)
+    else if (trav == 3 && G.dev.postponed_ok)
         L.walk = kWalkPostponed;
     int per_sm = 0;
     bool vox = G.dev.has_voxels;
@@ -1587,7 +1592,7 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
     MYPBR_CUDA(cudaEventCreate(&e1));
     int status = MYPBR_OK;
     int trial = 0;
-    for (int trav = 0; trav < 4; trav++)
+    for (int trav = 1; trav <= 4; trav++)
     for (int b : blocks) {
         if ((trav == 2 && G->dev.bvh4 == nullptr) || (trav == 3 && !G->dev.postponed_ok)) {
             trial += 4;  // a walk this scene's tree does not allow: trials skipped
@@ -1635,8 +1640,8 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
 }
 
 extern "C" int mypbr_gpu_set_launch(mypbr_gpu_scene* G, int32_t block, int64_t wave_paths, int32_t traversal) {
-    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 3)
-        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0 to 3");
+    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 4)
+        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0 to 4");
     G->tuned_block = block;
     G->tuned_wave_paths = size_t(wave_paths);
     G->tuned_traversal = traversal;

@@ -385,6 +385,12 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     D.bvh_node_count = interior;
     // walk_postponed packs a leaf as first << 4 | count in a stack entry
     D.postponed_ok = D.has_bvh && F.bvh_prim_count < (int64_t(1) << 26);
+    {
+        int64_t tris = 0;
+        for (int64_t k = 0; k < F.bvh_prim_count; k++)
+            tris += F.bvh_prims[k].kind == MYPBR_PRIM_TRIANGLE;
+        G.prefer_postponed = 2 * tris >= F.bvh_prim_count && F.bvh_prim_count > 0;
+    }
     for (size_t k = 0; D.postponed_ok && k < nodes.size(); k += 2)
         if (float_bits(nodes[k + 1].w) >= 16)
             D.postponed_ok = 0;

@@ -88,7 +88,7 @@ def test_device_bvh_with_the_other_walks(traversal):
     cam.image_width = 48
     cam.samples_per_pixel = 16
     cam.seed = 3
-    mp.set_launch(G, traversal=0)
+    mp.set_launch(G, traversal=4)
     a = cam.render(G).radiance
     mp.set_launch(G, traversal=traversal)
     b = cam.render(G).radiance
