@@ -1,4 +1,4 @@
-// Decoding of 8-bit image files for textures: PNG, TGA and baseline JPEG, to RGBA bytes.
+// Decoding of 8-bit image files for textures: PNG, TGA and JPEG, to RGBA bytes.
 #pragma once
 
 #include <cstdint>
@@ -25,7 +25,7 @@ ImageKind sniff_image(const uint8_t* bytes, size_t size);
 
 bool read_file_bytes(const std::string& path, std::vector<uint8_t>& bytes);
 
-// An 8-bit image file (PNG, baseline JPEG, or TGA as the fallback for files
+// An 8-bit image file (PNG, JPEG, or TGA as the fallback for files
 // no signature names, as stb_image tries it last).
 bool read_ldr_image(const std::string& path, LdrImage& out, std::string& error);
 bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);

@@ -1,8 +1,12 @@
-// Baseline JPEG decoding (ITU-T T.81, JFIF) for 8-bit image textures, as
-// stb_image reads them for the reference (texture.h:67-98): sequential
-// Huffman-coded frames (SOF0 / SOF1) of 1 or 3 components with any sampling
-// factors, restart intervals, 8- or 16-bit quantisation tables. Progressive,
-// lossless, arithmetic-coded and 12-bit files are reported as unsupported.
+// JPEG decoding (ITU-T T.81, JFIF) for 8-bit image textures, as stb_image
+// reads them for the reference (texture.h:67-98): sequential and progressive
+// Huffman-coded frames (SOF0 / SOF1 / SOF2) of 1 or 3 components with any
+// sampling factors, restart intervals, 8- or 16-bit quantisation tables.
+// Progressive scans (T.81 G.1.2) fill quantised coefficients band by band:
+// DC first and refinement bits, AC first passes with end-of-band runs, AC
+// refinement (correction bits for coefficients already nonzero, new ones of
+// magnitude 1 << Al); the frame is transformed once all scans are in.
+// Lossless, arithmetic-coded and 12-bit files are reported as unsupported.
 //
 // Per 8 x 8 block: Huffman-decoded DC difference and run-length AC
 // coefficients (zigzag order), dequantised, an inverse DCT evaluated as two
@@ -40,6 +44,7 @@ struct Component {
     int td = 0, ta = 0;  // Huffman tables of the current scan
     int bw = 0, bh = 0;  // blocks across and down, padded to whole MCUs
     std::vector<uint8_t> plane;  // bw * 8 x bh * 8 samples
+    std::vector<int16_t> coef;   // progressive frames: quantised coefficients, 64 per block in zigzag order
     int dc = 0;
 };
 
@@ -201,7 +206,7 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
     HuffTable dc[4], ac[4];
     std::vector<Component> comps;
     int width = 0, height = 0, hmax = 1, vmax = 1, restart = 0;
-    bool frame = false, adobe_rgb = false, adobe = false;
+    bool frame = false, adobe_rgb = false, adobe = false, progressive = false;
     size_t pos = 2;
     static const Idct idct;
     auto corrupt = [&](const char* what) {
@@ -277,7 +282,8 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
                 adobe = true;
                 adobe_rgb = s[11] == 0;
             }
-        } else if (m == 0xc0 || m == 0xc1) {  // SOF0 / SOF1
+        } else if (m == 0xc0 || m == 0xc1 || m == 0xc2) {  // SOF0 / SOF1 / SOF2 (progressive)
+            progressive = m == 0xc2;
             if (sl < 6 || s[0] != 8) {
                 error = "JPEG images of 12-bit precision are not decoded by this backend";
                 return false;
@@ -306,11 +312,12 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
                 c.bw = mcux * c.h;
                 c.bh = mcuy * c.v;
                 c.plane.assign(size_t(c.bw) * 8 * size_t(c.bh) * 8, 0);
+                if (progressive)
+                    c.coef.assign(size_t(c.bw) * size_t(c.bh) * 64, 0);
             }
             frame = true;
-        } else if ((m >= 0xc2 && m <= 0xc3) || (m >= 0xc5 && m <= 0xcf && m != 0xc8 && m != 0xcc)) {
-            error = m == 0xc2 ? "progressive JPEG images are not decoded by this backend"
-                              : "lossless, hierarchical or arithmetic-coded JPEG images are not decoded by this backend";
+        } else if (m == 0xc3 || (m >= 0xc5 && m <= 0xcf && m != 0xc8 && m != 0xcc)) {
+            error = "lossless, hierarchical or arithmetic-coded JPEG images are not decoded by this backend";
             return false;
         } else if (m == 0xda) {  // SOS: the (single, interleaved or not) scan
             if (!frame)
@@ -328,12 +335,111 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
                     return corrupt("scan component");
                 found->td = s[2 + 2 * i] >> 4;
                 found->ta = s[2 + 2 * i] & 15;
-                if (found->td > 3 || found->ta > 3 || !dc[found->td].present || !ac[found->ta].present)
-                    return corrupt("missing Huffman table");
+                if (found->td > 3 || found->ta > 3)
+                    return corrupt("Huffman table index");
                 sc.push_back(found);
             }
+            // spectral selection and successive approximation (progressive scans)
+            int ss = s[1 + 2 * ns], se = s[2 + 2 * ns], ah = s[3 + 2 * ns] >> 4, al = s[3 + 2 * ns] & 15;
+            for (auto* c : sc) {
+                bool need_dc = progressive ? (ss == 0 && ah == 0) : true;
+                bool need_ac = progressive ? ss > 0 : true;
+                if ((need_dc && !dc[c->td].present) || (need_ac && !ac[c->ta].present))
+                    return corrupt("missing Huffman table");
+            }
+            if (progressive && (se > 63 || ss > se || (ss == 0 && se != 0) || (ss > 0 && ns != 1) || al > 13))
+                return corrupt("progressive scan parameters");
             pos += 2 + len;
             Bits bits{b + pos, n - pos};
+            int eobrun = 0;
+            // one block of a progressive scan, into the component's coefficients
+            auto prog_block = [&](Component& c, int bx, int by) {
+                if (bx >= c.bw || by >= c.bh)
+                    return true;
+                int16_t* z = &c.coef[(size_t(by) * c.bw + size_t(bx)) * 64];
+                if (ss == 0) {  // DC
+                    if (ah == 0) {
+                        int t = decode_symbol(bits, dc[c.td]);
+                        if (t < 0 || t > 11)
+                            return false;
+                        c.dc += extend(bits.bits(t), t);
+                        z[0] = int16_t(c.dc * (1 << al));
+                    } else if (bits.bit()) {
+                        z[0] = int16_t(z[0] | (1 << al));
+                    }
+                    return true;
+                }
+                if (ah == 0) {  // AC, first pass of this band
+                    if (eobrun > 0) {
+                        eobrun--;
+                        return true;
+                    }
+                    for (int k = ss; k <= se; k++) {
+                        int rs = decode_symbol(bits, ac[c.ta]);
+                        if (rs < 0)
+                            return false;
+                        int r = rs >> 4, sz = rs & 15;
+                        if (sz == 0) {
+                            if (r < 15) {  // a run of end-of-bands
+                                eobrun = (1 << r) - 1 + (r ? bits.bits(r) : 0);
+                                break;
+                            }
+                            k += 15;  // sixteen zeros
+                            continue;
+                        }
+                        k += r;
+                        if (k > se)
+                            return false;
+                        z[k] = int16_t(extend(bits.bits(sz), sz) * (1 << al));
+                    }
+                    return true;
+                }
+                // AC refinement: a correction bit for every coefficient already
+                // nonzero, new coefficients of magnitude 1 << al
+                int p1 = 1 << al, m1 = -(1 << al);
+                int k = ss;
+                if (eobrun == 0) {
+                    for (; k <= se;) {
+                        int rs = decode_symbol(bits, ac[c.ta]);
+                        if (rs < 0)
+                            return false;
+                        int r = rs >> 4, sz = rs & 15, value = 0;
+                        if (sz) {
+                            if (sz != 1)
+                                return false;
+                            value = bits.bit() ? p1 : m1;
+                        } else if (r != 15) {
+                            eobrun = (1 << r) + (r ? bits.bits(r) : 0);
+                            break;
+                        }
+                        while (k <= se) {
+                            int16_t& v = z[k];
+                            if (v != 0) {
+                                if (bits.bit() && (v & p1) == 0)
+                                    v = int16_t(v >= 0 ? v + p1 : v + m1);
+                            } else {
+                                if (r == 0) {
+                                    if (value)
+                                        v = int16_t(value);
+                                    k++;
+                                    break;
+                                }
+                                r--;
+                            }
+                            k++;
+                        }
+                    }
+                }
+                if (eobrun > 0) {
+                    for (; k <= se; k++) {
+                        int16_t& v = z[k];
+                        if (v != 0 && bits.bit() && (v & p1) == 0)
+                            v = int16_t(v >= 0 ? v + p1 : v + m1);
+                    }
+                    eobrun--;
+                }
+                return true;
+            };
             int coef[64];
             auto block = [&](Component& c, int bx, int by) {
                 std::fill(coef, coef + 64, 0);
@@ -390,15 +496,19 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
                         bits.reset();
                         for (auto* c : sc)
                             c->dc = 0;
+                        eobrun = 0;
                         todo = restart;
                     }
+                    auto one = [&](Component& c, int bx, int by) {
+                        return progressive ? prog_block(c, bx, by) : block(c, bx, by);
+                    };
                     if (interleaved) {
                         for (auto* c : sc)
                             for (int v = 0; v < c->v; v++)
                                 for (int h = 0; h < c->h; h++)
-                                    if (!block(*c, ux * c->h + h, uy * c->v + v))
+                                    if (!one(*c, ux * c->h + h, uy * c->v + v))
                                         return corrupt("entropy-coded data");
-                    } else if (!block(*sc[0], ux, uy)) {
+                    } else if (!one(*sc[0], ux, uy)) {
                         return corrupt("entropy-coded data");
                     }
                     if (restart)
@@ -411,6 +521,20 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
     }
     if (!frame)
         return corrupt("no frame");
+    if (progressive) {
+        int coef[64];
+        for (auto& c : comps) {
+            const uint16_t* q = quant[c.tq];
+            int stride = c.bw * 8;
+            for (int by = 0; by < c.bh; by++)
+                for (int bx = 0; bx < c.bw; bx++) {
+                    const int16_t* z = &c.coef[(size_t(by) * c.bw + size_t(bx)) * 64];
+                    for (int k = 0; k < 64; k++)
+                        coef[kZigzag[k]] = z[k] * q[kZigzag[k]];
+                    idct.run(coef, &c.plane[size_t(by) * 8 * stride + size_t(bx) * 8], stride);
+                }
+        }
+    }
     out.width = width;
     out.height = height;
     out.channels = int(comps.size()) == 1 ? 1 : 3;

@@ -1,6 +1,8 @@
-"""A small baseline JPEG writer for the decoding fixtures.
+"""A small JPEG writer for the decoding fixtures: baseline and progressive.
 
-Sequential DCT, Huffman tables built per image from its own symbol counts
+Sequential or progressive DCT (spectral selection and successive
+approximation: DC and AC first passes with end-of-band runs, refinement
+passes with correction bits), Huffman tables built per image from its own symbol counts
 (valid JPEG: the tables travel in the DHT segments), quantisation tables of
 its own (8- or 16-bit), JFIF YCbCr with any of 4:4:4, 4:2:2, 4:2:0 and 4:4:0
 subsampling or a single grey component, optional restart intervals, one
@@ -97,7 +99,130 @@ def _segment(marker, payload):
     return struct.pack(">BBH", 0xFF, marker, len(payload) + 2) + payload
 
 
-def write_jpeg(path, rgb, sampling=(1, 1), grey=False, quality=2, restart=0, separate_scans=False, wide_quant=False):
+def _progressive_script(ncomp):
+    """Scans (components, Ss, Se, Ah, Al) of a progressive file: DC first with
+    one bit held back, luma low band, chroma, luma high band, then the
+    refinement passes (the shape of libjpeg's simple progression)."""
+    if ncomp == 1:
+        return [([0], 0, 0, 0, 1), ([0], 1, 5, 0, 2), ([0], 6, 63, 0, 2), ([0], 1, 63, 2, 1), ([0], 0, 0, 1, 0),
+                ([0], 1, 63, 1, 0)]
+    return [([0, 1, 2], 0, 0, 0, 1), ([0], 1, 5, 0, 2), ([2], 1, 63, 0, 1), ([1], 1, 63, 0, 1), ([0], 6, 63, 0, 2),
+            ([0], 1, 63, 2, 1), ([0, 1, 2], 0, 0, 1, 0), ([2], 1, 63, 1, 0), ([1], 1, 63, 1, 0), ([0], 1, 63, 1, 0)]
+
+
+def _mag_bits(v, size):
+    """JPEG's value bits: v itself if positive, its ones' complement if negative."""
+    return v if v >= 0 else (v + (1 << size) - 1)
+
+
+def _progressive_stream(blocks, comp_list, units, factors, ss, se, ah, al, tables, restart, interleaved):
+    """Items of one progressive scan: ("dc"|"ac", table, symbol, (bits, n)),
+    ("raw", bits, n) and ("rst", index)."""
+    items = []
+    pred = {c: 0 for c in comp_list}
+    state = {"eobrun": 0, "be": []}
+
+    def flush_eob(table):
+        run = state["eobrun"]
+        if run:
+            nb = run.bit_length() - 1
+            items.append(("ac", table, nb << 4, (run - (1 << nb), nb)))
+            state["eobrun"] = 0
+        for b in state["be"]:
+            items.append(("raw", b, 1))
+        state["be"] = []
+
+    table = tables[comp_list[0]]
+    count = 0
+    for uy, ux in units:
+        if restart and count and count % restart == 0:
+            if ss > 0:
+                flush_eob(table)
+            items.append(("rst", count // restart - 1))
+            pred = {c: 0 for c in comp_list}
+        for c in comp_list:
+            fh, fv = factors[c]
+            cells = [(uy * fv + j, ux * fh + i) for j in range(fv) for i in range(fh)] if interleaved else [(uy, ux)]
+            for by, bx in cells:
+                zz = [int(x) for x in blocks[c][by, bx]]
+                if ss == 0:
+                    if ah == 0:
+                        v = zz[0] >> al  # arithmetic shift, as the refinement bits expect
+                        d = v - pred[c]
+                        pred[c] = v
+                        size = _category(d)
+                        items.append(("dc", tables[c], size, (_mag_bits(d, size), size)))
+                    else:
+                        items.append(("raw", (zz[0] >> al) & 1, 1))
+                    continue
+                if ah == 0:
+                    vals = []
+                    for k in range(ss, se + 1):
+                        t = zz[k]
+                        m = abs(t) >> al
+                        vals.append(-m if t < 0 else m)
+                    last = max([i for i, v in enumerate(vals) if v != 0], default=-1)
+                    if last < 0:
+                        state["eobrun"] += 1
+                        if state["eobrun"] == 0x7FFF:
+                            flush_eob(table)
+                        continue
+                    flush_eob(table)
+                    run = 0
+                    for i in range(last + 1):
+                        v = vals[i]
+                        if v == 0:
+                            run += 1
+                            continue
+                        while run > 15:
+                            items.append(("ac", table, 0xF0, (0, 0)))
+                            run -= 16
+                        size = _category(v)
+                        items.append(("ac", table, (run << 4) | size, (_mag_bits(v, size), size)))
+                        run = 0
+                    if last < se - ss:
+                        state["eobrun"] += 1
+                        if state["eobrun"] == 0x7FFF:
+                            flush_eob(table)
+                    continue
+                # AC refinement
+                absv = [abs(zz[k]) >> al for k in range(ss, se + 1)]
+                eob = max([i for i, a in enumerate(absv) if a == 1], default=-1)
+                run, br = 0, []
+                for i, a in enumerate(absv):
+                    if a == 0:
+                        run += 1
+                        continue
+                    while run > 15 and i <= eob:
+                        flush_eob(table)
+                        items.append(("ac", table, 0xF0, (0, 0)))
+                        run -= 16
+                        for b in br:
+                            items.append(("raw", b, 1))
+                        br = []
+                    if a > 1:
+                        br.append(a & 1)
+                        continue
+                    flush_eob(table)
+                    items.append(("ac", table, (run << 4) | 1, (0, 0)))
+                    items.append(("raw", 0 if zz[ss + i] < 0 else 1, 1))
+                    for b in br:
+                        items.append(("raw", b, 1))
+                    br = []
+                    run = 0
+                if run > 0 or br:
+                    state["eobrun"] += 1
+                    state["be"] += br
+                    if state["eobrun"] == 0x7FFF or len(state["be"]) > 900:
+                        flush_eob(table)
+        count += 1
+    if ss > 0:
+        flush_eob(table)
+    return items
+
+
+def write_jpeg(path, rgb, sampling=(1, 1), grey=False, quality=2, restart=0, separate_scans=False, wide_quant=False,
+               progressive=False):
     """rgb: (H, W, 3) uint8 (or (H, W) for grey). sampling: luma (h, v) factors, chroma 1 x 1."""
     h, w = rgb.shape[:2]
     if grey:
@@ -189,7 +314,23 @@ def write_jpeg(path, rgb, sampling=(1, 1), grey=False, quality=2, restart=0, sep
         else:
             units = [(y, x) for y in range(mcuy) for x in range(mcux)]
         scans = [(comps, units)]
-    streams = [symbols_of(cl, units) for cl, units in scans]
+    spectral = [(0, 63, 0, 0)] * len(scans)
+    if progressive:
+        ncomp_ = 1 if grey else 3
+        scans, spectral, streams = [], [], []
+        for cl, ss, se, ah, al in _progressive_script(ncomp_):
+            if len(cl) > 1:  # interleaved DC scan: MCUs
+                units = [(y, x) for y in range(mcuy) for x in range(mcux)]
+            else:  # one component: its own blocks covering the image
+                c = cl[0]
+                fh, fv = factors[c]
+                comp_w, comp_h = -(-w * fh // hmax), -(-h * fv // vmax)
+                units = [(y, x) for y in range(-(-comp_h // 8)) for x in range(-(-comp_w // 8))]
+            scans.append((cl, units))
+            spectral.append((ss, se, ah, al))
+            streams.append(_progressive_stream(blocks, cl, units, factors, ss, se, ah, al, tables, restart, len(cl) > 1))
+    else:
+        streams = [symbols_of(cl, units) for cl, units in scans]
     # Huffman tables from the counts of all scans
     freq = {}
     for st in streams:
@@ -217,12 +358,13 @@ def write_jpeg(path, rgb, sampling=(1, 1), grey=False, quality=2, restart=0, sep
     for c in range(ncomp):
         fh, fv = factors[c]
         sof += bytes([c + 1, (fh << 4) | fv, 0 if c == 0 else 1])
-    out += _segment(0xC0, sof)
+    out += _segment(0xC2 if progressive else 0xC0, sof)
     out += _segment(0xC4, bytes(dht))
     if restart:
         out += _segment(0xDD, struct.pack(">H", restart))
-    for (cl, _), st in zip(scans, streams):
-        sos = bytes([len(cl)]) + b"".join(bytes([c + 1, (tables[c] << 4) | tables[c]]) for c in cl) + b"\x00\x3F\x00"
+    for (cl, _), st, (ss, se, ah, al) in zip(scans, streams, spectral):
+        sos = bytes([len(cl)]) + b"".join(bytes([c + 1, (tables[c] << 4) | tables[c]]) for c in cl)
+        sos += bytes([ss, se, (ah << 4) | al])
         out += _segment(0xDA, sos)
         bw_ = _BitWriter()
         for item in st:
@@ -230,6 +372,9 @@ def write_jpeg(path, rgb, sampling=(1, 1), grey=False, quality=2, restart=0, sep
                 bw_.flush()
                 out += bw_.out + bytes([0xFF, 0xD0 + item[1] % 8])
                 bw_ = _BitWriter()
+                continue
+            if item[0] == "raw":
+                bw_.put(item[1], item[2])
                 continue
             kind, t, sym, (extra, nbits) = item
             code, length = codes[(kind, t)][sym]
@@ -265,6 +410,10 @@ def make_jpeg_fixtures(folder):
         ("ycc422_scans.jpg", dict(sampling=(2, 1), separate_scans=True), (18, 30)),
         ("ycc444_q16.jpg", dict(sampling=(1, 1), wide_quant=True, quality=1), (16, 16)),
         ("ycc420_large.jpg", dict(sampling=(2, 2), quality=1), (96, 128)),
+        ("prog420.jpg", dict(sampling=(2, 2), progressive=True, quality=1), (45, 61)),
+        ("prog444.jpg", dict(sampling=(1, 1), progressive=True), (24, 40)),
+        ("prog_grey.jpg", dict(grey=True, progressive=True, quality=1), (33, 27)),
+        ("prog422_restart.jpg", dict(sampling=(2, 1), progressive=True, restart=3), (32, 48)),
     ]
     for name, kw, (h, w) in cases:
         write_jpeg(os.path.join(folder, name), image(h, w), **kw)

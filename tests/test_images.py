@@ -35,10 +35,10 @@ def test_decode_matches_stb(name):
 
 @pytest.mark.parametrize("name", [n for n in FIXTURES if n.endswith(".jpg")])
 def test_jpeg_decode_close_to_stb(name):
-    """Baseline JPEG: the inverse DCT and colour conversion are the standard's
-    (FP32 here, fixed point in stb_image), so bytes may differ by a few counts:
-    at most 3, on average under 0.2; chroma upsampling, edges included, and
-    the channel count as stb_image's."""
+    """Baseline and progressive JPEG: the inverse DCT and colour conversion are
+    the standard's (FP32 here, fixed point in stb_image), so bytes may differ
+    by a few counts: at most 3, on average under 0.2; chroma upsampling, edges
+    included, and the channel count as stb_image's."""
     rgba, channels = mp.read_image(os.path.join(IMAGES, name))
     ref = _g[name + ":rgba"]
     assert channels == _g[name + ":meta"][2]
@@ -91,12 +91,12 @@ def test_missing_image_is_an_error(tmp_path):
         _texture_scene(tmp_path, str(tmp_path / "nope.png"))
 
 
-def test_progressive_jpeg_is_reported_unsupported(tmp_path):
+def test_arithmetic_coded_jpeg_is_reported_unsupported(tmp_path):
     p = tmp_path / "photo.jpg"
-    # SOI, then a progressive frame header (SOF2)
-    p.write_bytes(b"\xff\xd8\xff\xc2\x00\x11\x08\x00\x10\x00\x10\x03\x01\x22\x00\x02\x11\x01\x03\x11\x01"
+    # SOI, then an arithmetic-coded frame header (SOF9)
+    p.write_bytes(b"\xff\xd8\xff\xc9\x00\x11\x08\x00\x10\x00\x10\x03\x01\x22\x00\x02\x11\x01\x03\x11\x01"
                   + b"\xff\xd9")
-    with pytest.raises(mp.MypbrError, match="progressive JPEG") as e:
+    with pytest.raises(mp.MypbrError, match="arithmetic-coded") as e:
         _texture_scene(tmp_path, str(p))
     assert e.value.status == 2
     with pytest.raises(mp.MypbrError) as e2:
