@@ -81,7 +81,7 @@ struct mypbr_gpu_scene {
     int tuned_block = 0;
     int tuned_traversal = 0;  // 0: the scene's default (3 or 4); 1: lanes take new rays (k_extend_pt);
                               // 2: the 4-wide tree; 3: postponed leaves; 4: the plain binary walk
-    bool prefer_postponed = false;  // triangles fill most leaves: traversal 0 means 3
+    bool prefer_postponed = false;  // spheres fill fewer than half the leaves: traversal 0 means 3
 };
 
 namespace mypbr_dev {

@@ -917,12 +917,12 @@ const void* shadow_kernel(bool vox, int walk) {
 // Grids of `block` threads: SMs x resident blocks (persistent-style loops).
 Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
     Launch L{};
-    // 128-thread blocks suit the triangle scenes' postponed-leaf walk (6 %
-    // faster on the 2 M-triangle room), 256 the rest
+    // 128-thread blocks suit the postponed-leaf walk (6 % faster on the
+    // 2 M-triangle room, 6 % on the guided voxel hall), 256 the rest
     int default_block = G.prefer_postponed && G.tuned_traversal == 0 ? 128 : 256;
     L.block = block == 128 || block == 256 ? block : (G.tuned_block ? G.tuned_block : default_block);
-    // traversal 0 is the scene's default: leaves postponed where triangles
-    // fill most of the leaves (their tests diverge), the plain binary walk else
+    // traversal 0 is the scene's default: leaves postponed unless spheres fill
+    // most of the leaves (other leaves' tests diverge), the plain binary walk else
     int trav = G.tuned_traversal;
     if (trav == 0)
         trav = G.prefer_postponed && G.dev.postponed_ok ? 3 : 4;

@@ -386,10 +386,14 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
     // walk_postponed packs a leaf as first << 4 | count in a stack entry
     D.postponed_ok = D.has_bvh && F.bvh_prim_count < (int64_t(1) << 26);
     {
-        int64_t tris = 0;
+        // leaves of triangles, quads, media or voxel blocks make the lanes of
+        // a warp diverge in their tests (voxel blocks most: a DDA walk each);
+        // spheres are one cheap test. Postponed leaves are the default unless
+        // spheres fill most leaves.
+        int64_t spheres = 0;
         for (int64_t k = 0; k < F.bvh_prim_count; k++)
-            tris += F.bvh_prims[k].kind == MYPBR_PRIM_TRIANGLE;
-        G.prefer_postponed = 2 * tris >= F.bvh_prim_count && F.bvh_prim_count > 0;
+            spheres += F.bvh_prims[k].kind == MYPBR_PRIM_SPHERE;
+        G.prefer_postponed = 2 * spheres < F.bvh_prim_count;
     }
     for (size_t k = 0; D.postponed_ok && k < nodes.size(); k += 2)
         if (float_bits(nodes[k + 1].w) >= 16)
