@@ -666,12 +666,13 @@ int mypbr_gpu_display(const double* radiance, int32_t width, int32_t height, con
 
 /* Decodes an 8-bit image file (PNG of any color type and depth, interlaced
  * or not, with tRNS; TGA types 1, 2, 3 and their run-length forms; baseline
- * and progressive JPEG) to RGBA bytes, rows from the top, as image_texture loads one
+ * and progressive JPEG; BMP of 1, 4, 8, 16, 24 and 32 bits; binary PGM / PPM
+ * of 8 and 16 bits) to RGBA bytes, rows from the top, as image_texture loads one
  * (stbi_load with 4 channels, include/texture.h:67-98). *channels is the
  * file's own count as stb_image reports it (1 grey, 2 grey + alpha, 3 RGB,
  * 4 RGBA). With rgba NULL only the size is returned; else rgba holds
- * capacity >= w * h * 4 bytes. Arithmetic-coded or lossless JPEG, BMP and
- * GIF files give MYPBR_ERR_UNSUPPORTED. */
+ * capacity >= w * h * 4 bytes. Arithmetic-coded or lossless JPEG, run-length
+ * BMP and GIF files give MYPBR_ERR_UNSUPPORTED. */
 int mypbr_image_read(const char* path, int32_t* width, int32_t* height, int32_t* channels, uint8_t* rgba,
                      int64_t capacity);
 

@@ -262,6 +262,8 @@ ImageKind sniff_image(const uint8_t* b, size_t n) {
         return ImageKind::Bmp;
     if (starts("GIF8"))
         return ImageKind::Gif;
+    if (starts("P5") || starts("P6"))
+        return ImageKind::Pnm;
     return ImageKind::Other;
 }
 
@@ -279,7 +281,8 @@ bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::str
         case ImageKind::Png: return decode_png(bytes, size, out, error);
         case ImageKind::Other: return decode_tga(bytes, size, out, error);
         case ImageKind::Jpeg: return decode_jpeg(bytes, size, out, error);
-        case ImageKind::Bmp: error = "BMP images are not decoded by this backend"; return false;
+        case ImageKind::Bmp: return decode_bmp(bytes, size, out, error);
+        case ImageKind::Pnm: return decode_pnm(bytes, size, out, error);
         case ImageKind::Gif: error = "GIF images are not decoded by this backend"; return false;
         case ImageKind::Hdr: error = "a Radiance HDR image is not an 8-bit image"; return false;
     }

@@ -1,4 +1,5 @@
-// Decoding of 8-bit image files for textures: PNG, TGA and JPEG, to RGBA bytes.
+// Decoding of 8-bit image files for textures: PNG, TGA, JPEG, BMP and binary
+// PGM / PPM, to RGBA bytes.
 #pragma once
 
 #include <cstdint>
@@ -18,14 +19,16 @@ struct LdrImage {
 bool decode_png(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
 bool decode_tga(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
 bool decode_jpeg(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
+bool decode_bmp(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
+bool decode_pnm(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);
 
 // The kind of image file the bytes start with.
-enum class ImageKind { Png, Hdr, Jpeg, Bmp, Gif, Other };
+enum class ImageKind { Png, Hdr, Jpeg, Bmp, Gif, Pnm, Other };
 ImageKind sniff_image(const uint8_t* bytes, size_t size);
 
 bool read_file_bytes(const std::string& path, std::vector<uint8_t>& bytes);
 
-// An 8-bit image file (PNG, JPEG, or TGA as the fallback for files
+// An 8-bit image file (PNG, JPEG, BMP, PGM / PPM, or TGA as the fallback for files
 // no signature names, as stb_image tries it last).
 bool read_ldr_image(const std::string& path, LdrImage& out, std::string& error);
 bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::string& error);

@@ -381,7 +381,7 @@ class Loader {
             std::string e;
             if (!mypbr_host::decode_ldr_image(bytes.data(), bytes.size(), img, e)) {
                 if (kind == mypbr_host::ImageKind::Jpeg || kind == mypbr_host::ImageKind::Bmp ||
-                    kind == mypbr_host::ImageKind::Gif)
+                    kind == mypbr_host::ImageKind::Gif || kind == mypbr_host::ImageKind::Pnm)
                     err = e;
                 return -1;
             }

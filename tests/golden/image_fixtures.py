@@ -4,8 +4,11 @@ Every PNG color type and bit depth (grey 1/2/4/8/16, RGB 8/16, palette
 1/2/4/8, grey + alpha 8/16, RGBA 8/16), tRNS keys and palette alphas, Adam7
 interlacing, all five scanline filters and stored / fixed / dynamic deflate
 blocks; TGA true color (15/16, 24, 32 bit), grey and color-mapped images,
-plain and run-length coded, bottom-up and top-down. The pixel values are
-seeded, so the files are reproducible.
+plain and run-length coded, bottom-up and top-down; BMP through every header
+size (OS/2, 40, 56, v4, v5) at 1/4/8 bits through a palette, 16 bits 5-5-5 and
+5-6-5, 24 bits, 32 bits with and without alpha (an all-zero alpha channel
+included), bottom-up and top-down; binary PGM / PPM at 8 and 16 bits with
+header comments. The pixel values are seeded, so the files are reproducible.
 """
 import os
 import struct
@@ -146,6 +149,83 @@ def write_tga(path, rgba, kind, bits, top_first=False, rle=False, palette=None, 
         f.write(head + image_id + pal + body + b"\0" * 8 + b"TRUEVISION-XFILE.\0")
 
 
+def _bmp_masks_pixel(px, masks):
+    """Packs integer channel values (already at each field's width) into one word."""
+    v = 0
+    for c, m in zip(px, masks):
+        if m:
+            shift = (m & -m).bit_length() - 1
+            v |= (int(c) << shift) & m
+    return v
+
+
+def write_bmp(path, pixels, bpp, hsz=40, palette=None, masks=None, compress=None, top_down=False, gap=0):
+    """A BMP file: `pixels` (h, w) palette indices for bpp <= 8, else (h, w, c)
+    channel values at the widths of `masks` (r, g, b, a) for 16 / 32 bits, or
+    BGR-ready RGB bytes for 24 bits. `gap` bytes of padding sit between the
+    header (+ palette) and the pixels."""
+    h, w = pixels.shape[:2]
+    if compress is None:
+        compress = 3 if masks is not None and hsz in (40, 56, 108, 124) and bpp in (16, 32) else 0
+    rows = []
+    for y in (range(h) if top_down else range(h - 1, -1, -1)):
+        row = bytearray()
+        if bpp <= 8:
+            acc, used = 0, 0
+            for x in range(w):
+                acc = (acc << bpp) | int(pixels[y, x])
+                used += bpp
+                if used == 8:
+                    row.append(acc)
+                    acc, used = 0, 0
+            if used:
+                row.append(acc << (8 - used))
+        elif bpp == 24:
+            for x in range(w):
+                r, g, b = (int(c) for c in pixels[y, x, :3])
+                row += bytes([b, g, r])
+        else:
+            for x in range(w):
+                v = _bmp_masks_pixel(pixels[y, x], masks)
+                row += struct.pack("<H" if bpp == 16 else "<I", v)
+        row += bytes((-len(row)) % 4)
+        rows.append(bytes(row))
+    pal = b""
+    if palette is not None:
+        pal = b"".join(bytes([int(c[2]), int(c[1]), int(c[0])]) + (b"" if hsz == 12 else b"\0") for c in palette)
+    if hsz == 12:
+        info = struct.pack("<IHHHH", 12, w, h, 1, bpp)
+    else:
+        info = struct.pack("<IiiHHIIiiII", hsz, w, -h if top_down else h, 1, bpp, compress, 0, 2835, 2835,
+                           len(palette) if palette is not None else 0, 0)
+        if hsz == 56:
+            m = list(masks or (0, 0, 0, 0))
+            info += struct.pack("<IIII", *m)
+        elif hsz in (108, 124):
+            m = list(masks or (0, 0, 0, 0))
+            info += struct.pack("<IIII", *m) + b"BGRs" + bytes(48)
+            if hsz == 124:
+                info += bytes(16)
+    extra = b""
+    if hsz in (40, 56) and compress == 3:  # stb reads these three after a 56-byte header too
+        extra = struct.pack("<III", *masks[:3])
+    offset = 14 + len(info) + len(extra) + len(pal) + gap
+    body = b"".join(rows)
+    head = b"BM" + struct.pack("<IHHI", offset + len(body), 0, 0, offset)
+    with open(path, "wb") as f:
+        f.write(head + info + extra + pal + bytes(gap) + body + bytes(gap))
+
+
+def write_pnm(path, samples, maxv, comment=False):
+    """Binary PGM (h, w) or PPM (h, w, 3), big-endian samples above 255."""
+    h, w = samples.shape[:2]
+    kind = b"P6" if samples.ndim == 3 else b"P5"
+    head = kind + (b"\n# a comment line\n" if comment else b"\n") + f"{w} {h}\n{maxv}\n".encode()
+    data = samples.astype(">u2" if maxv > 255 else "u1").tobytes()
+    with open(path, "wb") as f:
+        f.write(head + data)
+
+
 def make_image_fixtures(folder):
     """Writes the fixture set into folder; returns the file names."""
     os.makedirs(folder, exist_ok=True)
@@ -218,4 +298,47 @@ def make_image_fixtures(folder):
     pal = rng.integers(0, 256, size=(12, 3))
     tga("mapped8.tga", idx4, 1, 8, palette=pal)
     tga("mapped8_rle.tga", idx4, 1, 8, rle=True, palette=pal, top_first=True)
+
+    def bmp(name, *args, **kw):
+        write_bmp(os.path.join(folder, name), *args, **kw)
+        names.append(name)
+
+    for bits in (1, 4, 8):
+        n = 1 << bits
+        pal = rng.integers(0, 256, size=(n, 3))
+        bmp(f"pal{bits}.bmp", grad(n - 1, 1)[..., 0], bits, palette=pal)
+    pal = rng.integers(0, 256, size=(16, 3))
+    bmp("pal4_top.bmp", grad(15, 1)[..., 0], 4, palette=pal, top_down=True)
+    bmp("pal8_short.bmp", grad(9, 1)[..., 0], 8, palette=pal[:10])
+    bmp("pal8_os2.bmp", grad(9, 1)[..., 0], 8, hsz=12, palette=np.concatenate([pal[:10], pal[:4]]))
+    bmp("pal4_v5.bmp", grad(15, 1)[..., 0], 4, hsz=124, palette=pal)
+    bmp("rgb24.bmp", grad(255, 3), 24)
+    bmp("rgb24_top.bmp", grad(255, 3), 24, top_down=True)
+    bmp("rgb24_os2.bmp", grad(255, 3), 24, hsz=12)
+    bmp("rgb24_v4.bmp", grad(255, 3), 24, hsz=108)
+    bmp("rgb555.bmp", grad(31, 3), 16, masks=(31 << 10, 31 << 5, 31, 0), compress=0)
+    bmp("rgb565.bmp", np.concatenate([grad(31, 1), grad(63, 1), grad(31, 1)], axis=-1), 16,
+        masks=(31 << 11, 63 << 5, 31, 0))
+    bmp("argb1555_v5.bmp", np.concatenate([grad(31, 3), grad(1, 1)], axis=-1), 16, hsz=124,
+        masks=(31 << 10, 31 << 5, 31, 1 << 15))
+    bmp("argb4444_56.bmp", grad(15, 4), 16, hsz=56, masks=(15 << 8, 15 << 4, 15, 15 << 12))
+    bmp("bgra32.bmp", grad(255, 4), 32, masks=(0xff0000, 0xff00, 0xff, 0xff000000), compress=0)
+    zero_alpha = grad(255, 4)
+    zero_alpha[..., 3] = 0
+    bmp("bgra32_alpha0.bmp", zero_alpha, 32, masks=(0xff0000, 0xff00, 0xff, 0xff000000), compress=0)
+    bmp("rgba32_v5.bmp", grad(255, 4), 32, hsz=124, masks=(0xff, 0xff00, 0xff0000, 0xff000000))
+    bmp("rgb32_fields.bmp", grad(255, 3), 32, masks=(0xff000000, 0xff0000, 0xff00, 0))
+    bmp("rgb32_v4_default.bmp", grad(255, 4), 32, hsz=108, masks=(0xff0000, 0xff00, 0xff, 0xff000000),
+        compress=0, top_down=True)
+    bmp("rgb24_gap.bmp", grad(255, 3), 24, gap=4)
+
+    def pnm(name, *args, **kw):
+        write_pnm(os.path.join(folder, name), *args, **kw)
+        names.append(name)
+
+    pnm("grey8.pgm", grad(255, 1)[..., 0], 255)
+    pnm("grey8_comment.pgm", grad(200, 1)[..., 0], 200, comment=True)
+    pnm("rgb8.ppm", grad(255, 3), 255, comment=True)
+    pnm("rgb16.ppm", grad(65535, 3), 65535)
+    pnm("grey16.pgm", grad(4095, 1)[..., 0], 4095)
     return names

@@ -117,6 +117,64 @@ def test_truncated_png_is_rejected(tmp_path):
         _texture_scene(tmp_path, str(p))
 
 
+def test_run_length_bmp_is_reported_unsupported(tmp_path):
+    """stb_image reads neither RLE nor embedded JPEG / PNG BMP files."""
+    data = bytearray(open(os.path.join(IMAGES, "pal8.bmp"), "rb").read())
+    for compress, words in ((1, "run-length"), (4, "embedded JPEG")):
+        struct.pack_into("<I", data, 30, compress)
+        p = tmp_path / f"c{compress}.bmp"
+        p.write_bytes(bytes(data))
+        with pytest.raises(mp.MypbrError, match=words) as e:
+            mp.read_image(str(p))
+        assert e.value.status == 2
+        with pytest.raises(mp.MypbrError, match=words):
+            _texture_scene(tmp_path, str(p))
+
+
+@pytest.mark.parametrize("name", ["rgb24.bmp", "pal4.bmp", "bgra32.bmp", "rgb8.ppm", "grey16.pgm"])
+def test_truncated_bmp_and_pnm_are_rejected(name, tmp_path):
+    """Cut inside the pixels: an error (stb_image reads zeros past the end
+    of a BMP and rejects a short PGM / PPM)."""
+    data = open(os.path.join(IMAGES, name), "rb").read()
+    p = tmp_path / ("cut" + os.path.splitext(name)[1])
+    p.write_bytes(data[:len(data) - 7])
+    with pytest.raises(mp.MypbrError, match="truncated"):
+        mp.read_image(str(p))
+
+
+def test_bmp_headers_that_are_not_images(tmp_path):
+    data = bytearray(open(os.path.join(IMAGES, "rgb24.bmp"), "rb").read())
+    bad = bytearray(data)
+    struct.pack_into("<I", bad, 14, 64)  # no such info header size
+    (tmp_path / "h.bmp").write_bytes(bytes(bad))
+    with pytest.raises(mp.MypbrError, match="header of 64 bytes"):
+        mp.read_image(str(tmp_path / "h.bmp"))
+    bad = bytearray(data)
+    struct.pack_into("<i", bad, 18, 0)  # zero width
+    (tmp_path / "w.bmp").write_bytes(bytes(bad))
+    with pytest.raises(mp.MypbrError):
+        mp.read_image(str(tmp_path / "w.bmp"))
+    (tmp_path / "z.pgm").write_bytes(b"P5\n0 4\n255\n")
+    with pytest.raises(mp.MypbrError, match="zero or overflowing width"):
+        mp.read_image(str(tmp_path / "z.pgm"))
+    (tmp_path / "o.ppm").write_bytes(b"P6\n4 99999999999\n255\n")
+    with pytest.raises(mp.MypbrError, match="overflowing height"):
+        mp.read_image(str(tmp_path / "o.ppm"))
+
+
+@pytest.mark.parametrize("name", ["argb1555_v5.bmp", "pal8_os2.bmp", "grey8.pgm"])
+def test_bmp_and_pnm_textures_in_scenes(name, tmp_path):
+    sc = _texture_scene(tmp_path, os.path.join(IMAGES, name))
+    f = flat.view(sc)
+    t = f["textures"][-1]
+    meta = _g[name + ":meta"]
+    assert t["type"] == 2 and t["width"] == meta[0] and t["height"] == meta[1]
+    assert bool(t["flags"] & 8) == (not meta[3])
+    n = int(meta[0] * meta[1] * 4)
+    np.testing.assert_array_equal(f["texels_ldr"][t["offset"] * 4: t["offset"] * 4 + n],
+                                  _g[name + ":rgba"].reshape(-1))
+
+
 # ------------------------------------------------------------------ MTL
 
 
