@@ -26,7 +26,9 @@ mypbr_gpu_render (renders, copies the FP64 frame back) + destroy.
 voxel_hall: the 512^3 voxel world lit through six slits (workloads.py),
 rendered at --hall-width x 9/16 with max depth 16. relMSE = mean over pixels
 and channels of (x - r)^2 / (r^2 + 0.01) against a plain render at --ref-spp
-samples (FP64 film). Each method renders at doubling spp (a fresh, untrained
+samples (FP64 film), minus the reference's own noise: the reference is the
+mean of two independent half-spp renders, whose difference estimates that
+noise (relMSE_raw in each point is the uncorrected value). Each method renders at doubling spp (a fresh, untrained
 network for every guided render, so training time is inside each timing)
 until relMSE <= 0.01 or --max-spp; the time there is interpolated log-log
 between the two bracketing renders, or extrapolated as relMSE = c/spp with c
@@ -359,6 +361,15 @@ def rel_mse(x, ref, eps=0.01):
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + eps)))
 
 
+def reference_noise(half_a, half_b, eps=0.01):
+    """The relMSE that the reference's own noise adds to every comparison
+    against it. The reference is the mean of two independent renders of half
+    its spp each; per pixel (a - b)^2 / 4 estimates the variance of that mean
+    without bias, so E[relMSE(x, ref)] = relMSE(x, truth) + this value."""
+    ref = 0.5 * (half_a + half_b)
+    return float(np.mean((half_a - half_b) ** 2 / 4.0 / (ref ** 2 + eps)))
+
+
 def time_to_target(points, target):
     """points: [(spp, seconds, relMSE)] at increasing spp. Seconds to reach target."""
     prev = None
@@ -404,7 +415,19 @@ def run_voxel_hall(args):
         return img, time.perf_counter() - t0
 
     render(G, 16, 0, 7)  # warm-up: path buffers
-    ref, t_ref = render(G, args.ref_spp, 0, 12345)
+    # the reference as two independent halves: their difference measures the
+    # reference's own noise, which is taken out of every relMSE below (a 65,536-
+    # spp plain reference still carries relMSE ~0.04 on this scene, four times
+    # the target, so an uncorrected curve levels off above the target)
+    ref_a, t_a = render(G, args.ref_spp // 2, 0, 12345)
+    ref_b, t_b = render(G, args.ref_spp // 2, 0, 54321)
+    ref, t_ref = 0.5 * (ref_a + ref_b), t_a + t_b
+    floor = reference_noise(ref_a, ref_b)
+    del ref_a, ref_b
+
+    def error(img):
+        raw = rel_mse(img, ref)
+        return max(raw - floor, 1e-12), raw
     Gg = mp.GpuScene(scene)
     render(Gg, 64, args.hidden, 7)  # warm-up: guiding buffers and network
     curves = {}
@@ -415,15 +438,16 @@ def run_voxel_hall(args):
             if guided:  # an untrained network every time: training is inside each timing
                 mp.guide_reset(Gg)
             img, t = render(Gg if guided else G, spp, guided, 1 + spp)
-            e = rel_mse(img, ref)
-            pts.append((spp, t, e))
-            print(f"{name} spp {spp}: {t:.3f} s relMSE {e:.5f}", file=sys.stderr, flush=True)
+            e, raw = error(img)
+            pts.append((spp, t, e, raw))
+            print(f"{name} spp {spp}: {t:.3f} s relMSE {e:.5f} (raw {raw:.5f})", file=sys.stderr, flush=True)
             if e <= target / 2:
                 break
             spp *= 2
-        tt, how = time_to_target(pts, target)
+        tt, how = time_to_target([p_[:3] for p_ in pts], target)
         curves[name] = {"time_to_target_s": tt, "how": how,
-                        "points": [{"spp": s_, "seconds": t_, "relMSE": e_} for s_, t_, e_ in pts]}
+                        "points": [{"spp": s_, "seconds": t_, "relMSE": e_, "relMSE_raw": r_}
+                                   for s_, t_, e_, r_ in pts]}
     # CPU: the oracle on all host cores, a bounded run, extrapolated as relMSE ~ 1/spp
     import oracle as orc
     threads = os.cpu_count() or 1
@@ -438,7 +462,7 @@ def run_voxel_hall(args):
         if cpu_t > args.cpu_budget / 3 or spp >= 256:
             break
         spp *= 2
-    cpu_e = rel_mse(cpu_img, ref)
+    cpu_e, _ = error(cpu_img)
     # the oracle is the plain estimator itself (same sampling, renders within
     # 3 sigma of each other), so it needs the spp the plain GPU curve needs;
     # its time is that many samples at its measured seconds per sample
@@ -449,6 +473,9 @@ def run_voxel_hall(args):
             "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "fp32", "data": "synthetic",
             "config": {"workload": "voxel_hall_512", "width": width, "height": height, "max_depth": 16,
                        "reference_spp": args.ref_spp, "reference_seconds": t_ref, "relmse_eps": 0.01,
+                       "reference_noise_relmse": floor,
+                       "relmse": "against the reference, minus the reference's own noise (two independent "
+                                 "halves; relMSE_raw is uncorrected)",
                        "guide_hidden_layers": args.hidden, "sky": "uniform 0.35 0.45 0.6",
                        "sun": "elevation 40 azimuth 160 intensity 1000 angle 0.54"},
             "plain": curves["plain"], "guided": curves["guided"],

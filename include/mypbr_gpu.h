@@ -666,13 +666,13 @@ int mypbr_gpu_display(const double* radiance, int32_t width, int32_t height, con
 
 /* Decodes an 8-bit image file (PNG of any color type and depth, interlaced
  * or not, with tRNS; TGA types 1, 2, 3 and their run-length forms; baseline
- * and progressive JPEG; BMP of 1, 4, 8, 16, 24 and 32 bits; binary PGM / PPM
- * of 8 and 16 bits) to RGBA bytes, rows from the top, as image_texture loads one
+ * and progressive JPEG; BMP of 1, 4, 8, 16, 24 and 32 bits; GIF, first frame;
+ * binary PGM / PPM of 8 and 16 bits) to RGBA bytes, rows from the top, as image_texture loads one
  * (stbi_load with 4 channels, include/texture.h:67-98). *channels is the
  * file's own count as stb_image reports it (1 grey, 2 grey + alpha, 3 RGB,
  * 4 RGBA). With rgba NULL only the size is returned; else rgba holds
- * capacity >= w * h * 4 bytes. Arithmetic-coded or lossless JPEG, run-length
- * BMP and GIF files give MYPBR_ERR_UNSUPPORTED. */
+ * capacity >= w * h * 4 bytes. Arithmetic-coded or lossless JPEG and
+ * run-length BMP files give MYPBR_ERR_UNSUPPORTED. */
 int mypbr_image_read(const char* path, int32_t* width, int32_t* height, int32_t* channels, uint8_t* rgba,
                      int64_t capacity);
 
@@ -713,6 +713,15 @@ int mypbr_gpu_test_wait_timeout(void);
 /* Puts the scene handle's guiding network back to its initial (untrained)
  * weights, keeping its buffers: the next guided render starts from scratch. */
 int mypbr_guide_reset(mypbr_gpu_scene* scene);
+
+/* How guided renders of this scene handle sample: at the first `depths`
+ * bounces of a path (1..4096; default 2), a direction comes from the learned
+ * mixture with probability `alpha` (0 < alpha < 1; default 0.5), else from
+ * the BSDF, and the density used is the mixture of both (one-sample MIS), so
+ * the estimate stays unbiased whatever the network outputs: the BSDF
+ * proposal keeps every direction the BSDF can scatter into reachable. The
+ * setting applies from the next render. */
+int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths);
 
 /* outputs (n x 64) of the network for encoded inputs (n x 128). */
 int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out);

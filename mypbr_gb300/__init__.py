@@ -164,6 +164,7 @@ def lib():
                                     ctypes.POINTER(ctypes.c_uint8), ctypes.c_int]
     L.mypbr_write_image.argtypes = [ctypes.c_char_p, dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), ctypes.c_int]
     L.mypbr_guide_reset.argtypes = [vp]
+    L.mypbr_guide_configure.argtypes = [vp, ctypes.c_float, i32]
     L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
     L.mypbr_guide_test_backward.argtypes = [ctypes.c_int, fp, fp, fp, i64, fp]
     L.mypbr_guide_test_loss.argtypes = [fp, fp, fp, i64, fp, fp]
@@ -550,6 +551,13 @@ def sky_bake(sun_direction, sun_irradiance, width=256, height=128, rayleigh=1.0,
 def guide_reset(gpu_scene):
     """The handle's guiding network back to its untrained weights (buffers kept)."""
     check(lib().mypbr_guide_reset(gpu_scene.handle))
+
+
+def guide_configure(gpu_scene, alpha=0.5, depths=2):
+    """Guided sampling of the handle: the mixture drawn with probability alpha
+    (0 < alpha < 1, else the BSDF) at the first `depths` bounces of a path."""
+    check(lib().mypbr_guide_configure(gpu_scene.handle if gpu_scene is not None else None, float(alpha),
+                                      int(depths)))
 
 
 def rebuild_bvh(gpu_scene):

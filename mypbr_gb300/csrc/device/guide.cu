@@ -744,6 +744,20 @@ int mypbr_guide_reset(mypbr_gpu_scene* scene) {
     return MYPBR_OK;
 }
 
+int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths) {
+    if (!scene) {
+        set_error_message("mypbr_guide_configure: null scene");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    if (!(alpha > 0.0f && alpha < 1.0f) || depths < 1 || depths > 4096) {
+        set_error_message("mypbr_guide_configure: alpha must lie in (0, 1) and depths in [1, 4096]");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    scene->guide.alpha = alpha;
+    scene->guide.depths = depths;
+    return MYPBR_OK;
+}
+
 int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out) {
     if (!weights || !inputs || !out || n < 0)
         return MYPBR_ERR_INVALID_ARGUMENT;

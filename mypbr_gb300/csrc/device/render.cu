@@ -36,12 +36,6 @@ constexpr uint32_t kFlagSeen = 2u;
 // Shading classes: each has its own queue and kernel, so a warp shades one
 // kind of material and each kernel carries only that material's code.
 constexpr int kShadeClasses = 6;
-// Bounces at which guided renders sample the learned mixture: the first two
-// scattering events of a path, which decide most of what the camera sees
-// (the network is trained on the first kGuideRecordDepth vertices). On the
-// occluded voxel hall, guiding every bounce cost 14 % more time for no
-// measurable drop in error.
-constexpr int kGuideDepths = 2;
 
 enum : int { kClassMiss = 0, kClassLambert = 1, kClassMetal = 2, kClassDielectric = 3, kClassPrincipled = 4,
              kClassGeneric = 5 };
@@ -66,6 +60,7 @@ struct WaveParams {
     // path guiding
     int guided;                // mixtures were computed for this wave's guidable vertices
     float guide_alpha;         // probability of sampling the mixture there (one-sample MIS)
+    int guide_depths;          // bounces below this sample the mixture
     int record;                // write training records
     GuideRecords rec;          // slots below rec_slots record their first rec.depth vertices
     uint32_t rec_slots;
@@ -487,7 +482,7 @@ __device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
                 GuideMix gm;
                 bool use_guide = false;
                 if constexpr (GUIDED && kGuidable<C>()) {
-                    if (P.guided && P.guide_alpha > 0.0f && !vol && depth < kGuideDepths) {
+                    if (P.guided && P.guide_alpha > 0.0f && !vol && depth < P.guide_depths) {
                         guide_unpack(P.guide_mix[slot], gm);
                         use_guide = true;
                     }
@@ -1036,7 +1031,7 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
             TIMED(1, (k_extend_pt<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
         else
             TIMED(1, (launch_bounce_kernel(extend_kernel(P.S.has_voxels, L.walk), L.grid_extend, L.block, st, P, depth)));
-        if (P.guided && depth < kGuideDepths) {  // the mixtures of this bounce's guidable vertices
+        if (P.guided && depth < P.guide_depths) {  // the mixtures of this bounce's guidable vertices
             TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
                          L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
             launches++;
@@ -1080,7 +1075,10 @@ int launch_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launc
                 WaveGraph* graph) {
     if (!graph)
         return run_wave(P, L, st, launches, T);
-    int key = (P.guided ? 1 : 0) | (P.record ? 2 : 0) | (P.guide_alpha > 0.0f ? 4 : 0);
+    // the wave's launches depend on these; the kernels' parameters (captured
+    // by value) on the mixing probability too
+    int key = (P.guided ? 1 : 0) | (P.record ? 2 : 0) | (P.guide_alpha > 0.0f ? 4 : 0) |
+              (P.guided ? (std::min(P.guide_depths, 255) << 3) | (int(P.guide_alpha * 1000.0f + 0.5f) << 11) : 0);
     if (!graph->exec || graph->key != key) {
         if (graph->exec) {
             cudaGraphExecDestroy(graph->exec);
@@ -1142,7 +1140,7 @@ constexpr int kGuideStepsEarly = 16, kGuideStepsLate = 4;
 constexpr int kGuideMinSteps = 16;    // steps before the mixture is sampled at all
 constexpr int kGuideBatchTilesPerSm = 2;  // 128-sample tiles per SM in one step (39K samples on 152 SMs)
 constexpr int kGuideMaxSteps = 1500;  // no recording or training past this
-constexpr float kGuideAlpha = 0.5f, kGuideLr = 4e-3f;
+constexpr float kGuideLr = 4e-3f;
 
 int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* o, int save_every, RenderSetup& R) {
     if (!G || !cam || !o)
@@ -1241,7 +1239,8 @@ int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int sav
     if (R.guided) {
         const GuideState& g = G->guide;
         P.guided = g.steps >= kGuideMinSteps;
-        P.guide_alpha = P.guided ? kGuideAlpha : 0.0f;
+        P.guide_alpha = P.guided ? g.alpha : 0.0f;
+        P.guide_depths = std::min(g.depths, P.max_depth);
         P.record = g.steps < kGuideMaxSteps;
         if (P.record)
             MYPBR_CUDA(cudaMemsetAsync(P.rec.count, 0, sizeof(uint32_t), st));

@@ -84,6 +84,7 @@ bool decode_bmp(const uint8_t* b, size_t n, LdrImage& out, std::string& error) {
         return false;
     if (hsz != 12 && hsz != 40 && hsz != 56 && hsz != 108 && hsz != 124) {
         error = "BMP header of " + std::to_string(hsz) + " bytes is not supported";
+        out.unsupported = true;
         return false;
     }
     size_t header_end = 14 + size_t(hsz);
@@ -128,10 +129,12 @@ bool decode_bmp(const uint8_t* b, size_t n, LdrImage& out, std::string& error) {
         uint32_t compress = le32(h + 12);
         if (compress == 1 || compress == 2) {
             error = "run-length encoded BMP images are not supported";
+            out.unsupported = true;
             return false;
         }
         if (compress >= 4) {
             error = "BMP images with embedded JPEG or PNG data are not supported";
+            out.unsupported = true;
             return false;
         }
         if (compress == 3 && bpp != 16 && bpp != 32)
@@ -202,6 +205,7 @@ bool decode_bmp(const uint8_t* b, size_t n, LdrImage& out, std::string& error) {
         }
         if (bpp != 1 && bpp != 4 && bpp != 8) {
             error = "BMP images of " + std::to_string(bpp) + " bits per pixel are not supported";
+            out.unsupported = true;
             return false;
         }
         const size_t entry = hsz == 12 ? 3 : 4;
@@ -247,6 +251,7 @@ bool decode_bmp(const uint8_t* b, size_t n, LdrImage& out, std::string& error) {
             ac = bit_count(ma);
             if (rc > 8 || gc > 8 || bc > 8 || ac > 8) {
                 error = "BMP channel masks wider than 8 bits are not supported";
+                out.unsupported = true;
                 return false;
             }
         }

@@ -264,6 +264,10 @@ ImageKind sniff_image(const uint8_t* b, size_t n) {
         return ImageKind::Gif;
     if (starts("P5") || starts("P6"))
         return ImageKind::Pnm;
+    if (starts("8BPS"))
+        return ImageKind::Psd;
+    if (n >= 92 && std::memcmp(b, "\x53\x80\xf6\x34", 4) == 0 && std::memcmp(b + 88, "PICT", 4) == 0)
+        return ImageKind::Pic;
     return ImageKind::Other;
 }
 
@@ -283,7 +287,15 @@ bool decode_ldr_image(const uint8_t* bytes, size_t size, LdrImage& out, std::str
         case ImageKind::Jpeg: return decode_jpeg(bytes, size, out, error);
         case ImageKind::Bmp: return decode_bmp(bytes, size, out, error);
         case ImageKind::Pnm: return decode_pnm(bytes, size, out, error);
-        case ImageKind::Gif: error = "GIF images are not decoded by this backend"; return false;
+        case ImageKind::Gif: return decode_gif(bytes, size, out, error);
+        case ImageKind::Psd:
+            error = "Photoshop (PSD) images are not decoded by this backend";
+            out.unsupported = true;
+            return false;
+        case ImageKind::Pic:
+            error = "Softimage PIC images are not decoded by this backend";
+            out.unsupported = true;
+            return false;
         case ImageKind::Hdr: error = "a Radiance HDR image is not an 8-bit image"; return false;
     }
     return false;

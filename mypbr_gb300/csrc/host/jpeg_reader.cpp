@@ -286,6 +286,7 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
             progressive = m == 0xc2;
             if (sl < 6 || s[0] != 8) {
                 error = "JPEG images of 12-bit precision are not decoded by this backend";
+                out.unsupported = true;
                 return false;
             }
             height = be16(s + 1);
@@ -318,6 +319,7 @@ bool decode_jpeg(const uint8_t* b, size_t n, LdrImage& out, std::string& error) 
             frame = true;
         } else if (m == 0xc3 || (m >= 0xc5 && m <= 0xcf && m != 0xc8 && m != 0xcc)) {
             error = "lossless, hierarchical or arithmetic-coded JPEG images are not decoded by this backend";
+            out.unsupported = true;
             return false;
         } else if (m == 0xda) {  // SOS: the (single, interleaved or not) scan
             if (!frame)

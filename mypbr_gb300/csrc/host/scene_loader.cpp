@@ -336,11 +336,15 @@ class Loader {
     std::map<int, ImageInfo> image_info;                              // texture -> 8-bit image facts
 
     // An image texture from a file, loaded once per (path, repeat, linear):
-    // Radiance HDR as linear floats, PNG or TGA as RGBA bytes (texture.h:67-98).
-    // Returns the texture index, or -1 with err empty if the file is missing or
-    // unreadable, or naming a format this backend does not decode.
+    // Radiance HDR as linear floats, the 8-bit formats as RGBA bytes
+    // (texture.h:67-98). Returns the texture index, or -1 with err empty if the
+    // file is missing, else err saying why it did not decode, and
+    // image_unsupported set when that is a variant this backend does not read
+    // (rather than a damaged file).
+    bool image_unsupported = false;
     int load_image(const std::string& file, bool repeat, bool linear, std::string& err) {
         err.clear();
+        image_unsupported = false;
         auto key = std::make_tuple(file, repeat, linear);
         auto hit = image_cache.find(key);
         if (hit != image_cache.end())
@@ -380,9 +384,8 @@ class Loader {
             mypbr_host::LdrImage img;
             std::string e;
             if (!mypbr_host::decode_ldr_image(bytes.data(), bytes.size(), img, e)) {
-                if (kind == mypbr_host::ImageKind::Jpeg || kind == mypbr_host::ImageKind::Bmp ||
-                    kind == mypbr_host::ImageKind::Gif || kind == mypbr_host::ImageKind::Pnm)
-                    err = e;
+                err = e;
+                image_unsupported = img.unsupported;
                 return -1;
             }
             // take_ldr (texture.h:161-181): the mask reads the alpha channel,
@@ -1619,11 +1622,11 @@ class Loader {
             std::string err;
             int index = load_image(file, false, linear, err);
             if (index < 0) {
-                if (!err.empty()) {
+                if (image_unsupported) {
                     unsupported = true;
                     return fail("image texture '" + file + "': " + err);
                 }
-                return fail("cannot load image '" + file + "'");
+                return fail("cannot load image '" + file + "'" + (err.empty() ? "" : ": " + err));
             }
             textures[name] = index;
         } else {
@@ -2662,9 +2665,7 @@ int mypbr_image_read(const char* path, int32_t* width, int32_t* height, int32_t*
         if (!readable)
             return MYPBR_ERR_IO;
         auto kind = mypbr_host::sniff_image(probe.data(), probe.size());
-        bool other_format = kind == mypbr_host::ImageKind::Jpeg || kind == mypbr_host::ImageKind::Bmp ||
-                            kind == mypbr_host::ImageKind::Gif || kind == mypbr_host::ImageKind::Hdr;
-        return other_format ? MYPBR_ERR_UNSUPPORTED : MYPBR_ERR_BAD_SCENE;
+        return img.unsupported || kind == mypbr_host::ImageKind::Hdr ? MYPBR_ERR_UNSUPPORTED : MYPBR_ERR_BAD_SCENE;
     }
     *width = img.width;
     *height = img.height;

@@ -8,7 +8,10 @@ plain and run-length coded, bottom-up and top-down; BMP through every header
 size (OS/2, 40, 56, v4, v5) at 1/4/8 bits through a palette, 16 bits 5-5-5 and
 5-6-5, 24 bits, 32 bits with and without alpha (an all-zero alpha channel
 included), bottom-up and top-down; binary PGM / PPM at 8 and 16 bits with
-header comments. The pixel values are seeded, so the files are reproducible.
+header comments; GIF with global and local tables, interlacing, transparency,
+a background around a smaller image, indices past the table, full code tables
+and a file cut inside its image data. The pixel values are seeded, so the
+files are reproducible.
 """
 import os
 import struct
@@ -226,6 +229,91 @@ def write_pnm(path, samples, maxv, comment=False):
         f.write(head + data)
 
 
+def _gif_lzw(indices, min_size):
+    """GIF LZW code stream of the index list, as data sub-blocks: a clear code
+    first, code width growing with the table, a clear code whenever the
+    table is full, the end code last."""
+    clear, end = 1 << min_size, (1 << min_size) + 1
+    out, acc, used = bytearray(), 0, 0
+    size = min_size + 1
+
+    def put(code):
+        nonlocal acc, used
+        acc |= code << used
+        used += size
+        while used >= 8:
+            out.append(acc & 255)
+            acc >>= 8
+            used -= 8
+
+    def reset():
+        return {(i,): i for i in range(clear)}, end + 1
+
+    table, nxt = reset()
+    put(clear)
+    w = (int(indices[0]),)
+    for k in indices[1:]:
+        wk = w + (int(k),)
+        if wk in table:
+            w = wk
+            continue
+        put(table[w])
+        if nxt < 4096:
+            table[wk] = nxt
+            nxt += 1
+            if nxt > (1 << size) and size < 12:
+                size += 1
+        else:
+            put(clear)
+            table, nxt = reset()
+            size = min_size + 1
+        w = (int(k),)
+    put(table[w])
+    put(end)
+    if used:
+        out.append(acc & 255)
+    blocks = bytearray()
+    for i in range(0, len(out), 255):
+        chunk = out[i:i + 255]
+        blocks += bytes([len(chunk)]) + chunk
+    return bytes([min_size]) + bytes(blocks) + b"\0"
+
+
+def write_gif(path, indices, palette, canvas=None, offset=(0, 0), local=False, interlace=False, transparent=None,
+              background=0, version=b"89a", comment=False, cut=None, min_size=None):
+    """A one-image GIF: `indices` (h, w) into `palette` (entries a power of two,
+    2..256), drawn at `offset` on a canvas (w, h) (the image's size by
+    default), with the table global or local, optionally interlaced, with a
+    transparent index (graphic control extension) and a background index;
+    `cut` keeps only that many leading bytes."""
+    h, w = indices.shape
+    cw, ch = canvas or (w, h)
+    bits = max(1, (len(palette) - 1).bit_length())
+    table = b"".join(bytes([int(c[0]), int(c[1]), int(c[2])]) for c in palette)
+    table += bytes(3 * ((1 << bits) - len(palette)))
+    gflags = 0 if local else 0x80 | (bits - 1)
+    data = b"GIF" + version + struct.pack("<HHBBB", cw, ch, gflags, background, 0)
+    if not local:
+        data += table
+    if comment:
+        data += b"\x21\xfe" + bytes([9]) + b"a fixture" + b"\0"
+    if transparent is not None:
+        data += b"\x21\xf9\x04" + struct.pack("<BHB", 1, 0, transparent) + b"\0"
+    lflags = (0x80 | (bits - 1) if local else 0) | (0x40 if interlace else 0)
+    data += b"\x2c" + struct.pack("<HHHHB", offset[0], offset[1], w, h, lflags)
+    if local:
+        data += table
+    rows = list(range(h))
+    if interlace:
+        rows = [y for start, step in ((0, 8), (4, 8), (2, 4), (1, 2)) for y in range(start, h, step)]
+    order = np.concatenate([indices[y] for y in rows])
+    data += _gif_lzw(order, max(2, bits) if min_size is None else min_size) + b"\x3b"
+    if cut is not None:
+        data = data[:cut]
+    with open(path, "wb") as f:
+        f.write(data)
+
+
 def make_image_fixtures(folder):
     """Writes the fixture set into folder; returns the file names."""
     os.makedirs(folder, exist_ok=True)
@@ -341,4 +429,21 @@ def make_image_fixtures(folder):
     pnm("rgb8.ppm", grad(255, 3), 255, comment=True)
     pnm("rgb16.ppm", grad(65535, 3), 65535)
     pnm("grey16.pgm", grad(4095, 1)[..., 0], 4095)
+
+    def gif(name, *args, **kw):
+        write_gif(os.path.join(folder, name), *args, **kw)
+        names.append(name)
+
+    pal16 = rng.integers(0, 256, size=(16, 3))
+    gif("global16.gif", grad(15, 1)[..., 0], pal16)
+    gif("local8_interlaced.gif", np.concatenate([grad(7, 1), grad(7, 1)[:4]])[..., 0], pal16[:8], local=True,
+        interlace=True, transparent=3)
+    gif("global4_transparent_87a.gif", grad(3, 1)[..., 0], pal16[:4], transparent=1, version=b"87a", comment=True)
+    gif("subrect_background.gif", grad(15, 1)[..., 0], pal16, canvas=(20, 12), offset=(4, 3), background=5)
+    gif("short_table.gif", grad(7, 1)[..., 0], pal16[:4], min_size=3)  # indices past the table
+    y, x = np.mgrid[0:96, 0:128]
+    noisy = np.where(rng.random((96, 128)) < 0.5, rng.integers(0, 256, size=(96, 128)), (x // 4 + y // 3) % 256)
+    pal256 = rng.integers(0, 256, size=(256, 3))
+    gif("large256.gif", noisy, pal256)
+    gif("large256_interlaced_cut.gif", noisy, pal256, interlace=True, cut=6000)
     return names

@@ -197,6 +197,31 @@ def test_guided_render_matches_reference():
     assert np.all(np.abs(tot_z) < 4), tot_z
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("alpha,depths", [(0.3, 1), (0.8, 50)])
+def test_guided_settings_stay_unbiased(alpha, depths):
+    """Other mixing probabilities and guided depths (every bounce of the
+    Cornell box's 50): still within 3 sigma of the reference's image."""
+    g = np.load(f"{GOLDEN}/render_cornell_c1.npz")
+    sc = mp.load_scene(scene_path("cornell_c1.scene"))
+    sc.camera.image_width = g["mean"].shape[1]
+    G = mp.GpuScene(sc)
+    mp.guide_configure(G, alpha=alpha, depths=depths)
+    rad, var, _ = _render(sc, G, 1024, 2, 16)
+    z = (rad - g["mean"]) / np.sqrt(var + g["var_of_mean"] + 1e-30)
+    assert np.mean(np.abs(z) > 3) < 0.02, np.mean(np.abs(z) > 3)
+    assert np.mean(np.abs(z) > 5) < 0.002
+    with pytest.raises(mp.MypbrError, match="alpha must lie"):
+        mp.guide_configure(G, alpha=1.0, depths=2)
+    with pytest.raises(mp.MypbrError, match="depths"):
+        mp.guide_configure(G, alpha=0.5, depths=0)
+
+
+def test_guide_configure_checks_its_handle():
+    with pytest.raises(mp.MypbrError, match="null scene"):
+        mp.guide_configure(None)
+
+
 def rel_mse(x, ref, eps=0.01):
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + eps)))
 

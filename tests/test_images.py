@@ -162,7 +162,53 @@ def test_bmp_headers_that_are_not_images(tmp_path):
         mp.read_image(str(tmp_path / "o.ppm"))
 
 
-@pytest.mark.parametrize("name", ["argb1555_v5.bmp", "pal8_os2.bmp", "grey8.pgm"])
+def test_damaged_and_unsupported_files_are_told_apart(tmp_path):
+    """A variant the decoders do not read is MYPBR_ERR_UNSUPPORTED (status 2)
+    and says what it is; a damaged file of a format they read is a bad scene
+    input (MYPBR_ERR_BAD_SCENE, status 7) with the reason."""
+    (tmp_path / "a.psd").write_bytes(b"8BPS" + bytes(40))
+    with pytest.raises(mp.MypbrError, match="Photoshop") as e:
+        mp.read_image(str(tmp_path / "a.psd"))
+    assert e.value.status == 2
+    pic = bytearray(120)
+    pic[0:4] = b"\x53\x80\xf6\x34"
+    pic[88:92] = b"PICT"
+    (tmp_path / "a.pic").write_bytes(bytes(pic))
+    with pytest.raises(mp.MypbrError, match="Softimage") as e:
+        mp.read_image(str(tmp_path / "a.pic"))
+    assert e.value.status == 2
+    data = open(os.path.join(IMAGES, "rgb24.bmp"), "rb").read()
+    (tmp_path / "cut.bmp").write_bytes(data[:80])
+    with pytest.raises(mp.MypbrError, match="truncated") as e:
+        mp.read_image(str(tmp_path / "cut.bmp"))
+    assert e.value.status == 7
+    with pytest.raises(mp.MypbrError, match="cannot load image .*truncated") as e:
+        _texture_scene(tmp_path, str(tmp_path / "cut.bmp"))
+    assert e.value.status == 7
+
+
+def test_gif_streams_that_are_not_images(tmp_path):
+    data = open(os.path.join(IMAGES, "global16.gif"), "rb").read()
+    head = data[:13 + 48]  # header and the 16-entry global table
+    (tmp_path / "none.gif").write_bytes(head + b"\x3b")
+    with pytest.raises(mp.MypbrError, match="no image"):
+        mp.read_image(str(tmp_path / "none.gif"))
+    (tmp_path / "tag.gif").write_bytes(head + b"\x99")
+    with pytest.raises(mp.MypbrError, match="unknown kind"):
+        mp.read_image(str(tmp_path / "tag.gif"))
+    # an image descriptor reaching past the canvas
+    (tmp_path / "rect.gif").write_bytes(head + b"\x2c" + struct.pack("<HHHHB", 5, 0, 13, 7, 0) + b"\x02\x00\x3b")
+    with pytest.raises(mp.MypbrError, match="outside the canvas"):
+        mp.read_image(str(tmp_path / "rect.gif"))
+    # image data whose first code is not the clear code (code size 4: clear = 16)
+    (tmp_path / "noclear.gif").write_bytes(head + b"\x2c" + struct.pack("<HHHHB", 0, 0, 13, 7, 0) +
+                                           b"\x04\x01\x03\x00\x3b")
+    with pytest.raises(mp.MypbrError, match="clear code"):
+        mp.read_image(str(tmp_path / "noclear.gif"))
+
+
+@pytest.mark.parametrize("name", ["argb1555_v5.bmp", "pal8_os2.bmp", "grey8.pgm", "local8_interlaced.gif",
+                                  "subrect_background.gif"])
 def test_bmp_and_pnm_textures_in_scenes(name, tmp_path):
     sc = _texture_scene(tmp_path, os.path.join(IMAGES, name))
     f = flat.view(sc)
