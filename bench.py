@@ -28,13 +28,18 @@ rendered at --hall-width x 9/16 with max depth 16. relMSE = mean over pixels
 and channels of (x - r)^2 / (r^2 + 0.01) against a plain render at --ref-spp
 samples (FP64 film), minus the reference's own noise: the reference is the
 mean of two independent half-spp renders, whose difference estimates that
-noise (relMSE_raw in each point is the uncorrected value). Each method renders at doubling spp (a fresh, untrained
+noise (relMSE_raw in each point is the uncorrected value). The time to
+target comes from --repeats independent renders of each method at
+--repeat-spp (a fresh network for every guided one): their mean relMSE gives
+c in relMSE = c/spp, and the time is c/0.01 samples at their mean seconds
+per sample. Each method renders at doubling spp (a fresh, untrained
 network for every guided render, so training time is inside each timing)
-until relMSE <= 0.01 or --max-spp; the time there is interpolated log-log
-between the two bracketing renders, or extrapolated as relMSE = c/spp with c
-fitted to the three highest-spp renders. The oracle is the plain estimator
-itself, so the CPU figure is the plain curve's spp to target at the oracle's
-measured seconds per spp (a bounded run on every host core).
+until relMSE <= 0.01 or --max-spp, reported as the curve (with the time to
+target that curve alone gives: interpolated log-log between the bracketing
+renders, or extrapolated from the three highest-spp ones; single renders
+are dominated by a few fireflies). The oracle is the plain estimator
+itself, so the CPU figure is the plain method's spp to target at the
+oracle's measured seconds per spp (a bounded run on every host core).
 
 cornell / triangle_room: Mpaths/s of C1 / C3 (render_ex, scene resident),
 the oracle beside it; with --hidden H the triangle room also renders guided
@@ -445,7 +450,26 @@ def run_voxel_hall(args):
                 break
             spp *= 2
         tt, how = time_to_target([p_[:3] for p_ in pts], target)
-        curves[name] = {"time_to_target_s": tt, "how": how,
+        # the estimate that decides: independent renders at one spp, whose mean
+        # relMSE gives the error constant c = relMSE x spp (one render's relMSE
+        # swings by 3x or more with the fireflies it happens to catch)
+        reps = []
+        for r_ in range(args.repeats):
+            if guided:
+                mp.guide_reset(Gg)
+            img, t = render(Gg if guided else G, args.repeat_spp, guided, 1000 + r_)
+            reps.append((t, error(img)[0]))
+            print(f"{name} repeat {r_} at {args.repeat_spp} spp: {t:.3f} s relMSE {reps[-1][1]:.5f}",
+                  file=sys.stderr, flush=True)
+        rep_t = float(np.mean([t_ for t_, _ in reps]))
+        rep_e = float(np.mean([e_ for _, e_ in reps]))
+        c = rep_e * args.repeat_spp
+        curves[name] = {"time_to_target_s": rep_t / args.repeat_spp * c / target,
+                        "how": f"mean relMSE of {args.repeats} independent renders at {args.repeat_spp} spp, "
+                               "relMSE ~ c/spp",
+                        "error_constant": c, "spp_to_target": c / target,
+                        "repeats": [{"seconds": t_, "relMSE": e_} for t_, e_ in reps],
+                        "curve_time_to_target_s": tt, "curve_how": how,
                         "points": [{"spp": s_, "seconds": t_, "relMSE": e_, "relMSE_raw": r_}
                                    for s_, t_, e_, r_ in pts]}
     # CPU: the oracle on all host cores, a bounded run, extrapolated as relMSE ~ 1/spp
@@ -466,8 +490,7 @@ def run_voxel_hall(args):
     # the oracle is the plain estimator itself (same sampling, renders within
     # 3 sigma of each other), so it needs the spp the plain GPU curve needs;
     # its time is that many samples at its measured seconds per sample
-    plain_pts = [(p_["spp"], p_["seconds"], p_["relMSE"]) for p_ in curves["plain"]["points"]]
-    cpu_tt = cpu_t / cpu_spp * spp_to_target(plain_pts, target)
+    cpu_tt = cpu_t / cpu_spp * curves["plain"]["spp_to_target"]
     cpu_tt_own = cpu_t * cpu_e / target
     line = {"metric": "time to relMSE 0.01 on the occluded voxel hall, guided GPU", "value": curves["guided"]["time_to_target_s"],
             "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "fp32", "data": "synthetic",
@@ -731,6 +754,9 @@ def main():
     p.add_argument("--ref-spp", type=int, default=65536)
     p.add_argument("--c3-ref-spp", type=int, default=1024, help="spp of the triangle room's reference render")
     p.add_argument("--max-spp", type=int, default=32768)
+    p.add_argument("--repeat-spp", type=int, default=8192,
+                   help="voxel_hall: spp of the repeated renders that estimate each method's error constant")
+    p.add_argument("--repeats", type=int, default=4, help="voxel_hall: renders per method at --repeat-spp")
     p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
     args = p.parse_args()
     if args.workload != "sphere_field":

@@ -715,7 +715,7 @@ int mypbr_gpu_test_wait_timeout(void);
 int mypbr_guide_reset(mypbr_gpu_scene* scene);
 
 /* How guided renders of this scene handle sample: at the first `depths`
- * bounces of a path (1..4096; default 2), a direction comes from the learned
+ * bounces of a path (1..4096; default 4), a direction comes from the learned
  * mixture with probability `alpha` (0 < alpha < 1; default 0.5), else from
  * the BSDF, and the density used is the mixture of both (one-sample MIS), so
  * the estimate stays unbiased whatever the network outputs: the BSDF

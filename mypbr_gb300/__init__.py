@@ -553,7 +553,7 @@ def guide_reset(gpu_scene):
     check(lib().mypbr_guide_reset(gpu_scene.handle))
 
 
-def guide_configure(gpu_scene, alpha=0.5, depths=2):
+def guide_configure(gpu_scene, alpha=0.5, depths=4):
     """Guided sampling of the handle: the mixture drawn with probability alpha
     (0 < alpha < 1, else the BSDF) at the first `depths` bounces of a path."""
     check(lib().mypbr_guide_configure(gpu_scene.handle if gpu_scene is not None else None, float(alpha),

@@ -56,11 +56,10 @@ struct GuideState {
     bool box_fitted = false;         // narrowed to the recorded vertices (once per fresh network)
     int box_version = 0;             // bumped when the box changes (waves captured before must be re-captured)
     // sampling: the mixture is drawn with probability alpha (else the BSDF) at
-    // the first `depths` bounces of a path (mypbr_guide_configure). Two: the
-    // first two scattering events decide most of what the camera sees, and the
-    // network is trained on the first kGuideRecordDepth vertices
+    // the first `depths` bounces of a path (mypbr_guide_configure); by default
+    // at the kGuideRecordDepth vertices the network is trained on
     float alpha = 0.5f;
-    int depths = 2;
+    int depths = 4;
     // recording buffers (slot-indexed, grown with the render buffers)
     GuideRecords rec{};
     size_t rec_slots = 0;
