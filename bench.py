@@ -756,7 +756,7 @@ def main():
     p.add_argument("--max-spp", type=int, default=32768)
     p.add_argument("--repeat-spp", type=int, default=8192,
                    help="voxel_hall: spp of the repeated renders that estimate each method's error constant")
-    p.add_argument("--repeats", type=int, default=4, help="voxel_hall: renders per method at --repeat-spp")
+    p.add_argument("--repeats", type=int, default=10, help="voxel_hall: renders per method at --repeat-spp")
     p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
     args = p.parse_args()
     if args.workload != "sphere_field":
