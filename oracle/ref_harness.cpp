@@ -15,6 +15,8 @@
 //   ggx    <out>                      ggx_albedo_table E(mu, alpha) / E_avg and ggx_ms_* on a grid
 //   render <scene> <width> <spp> <batches> <threads> <out>
 //                                      batch means of camera::render (mean and variance of the mean)
+//   features <scene> <width> <spp> <batches> <threads> <out>
+//                                      the same with collect_features: radiance, albedo, normal, variance
 //   denoise <w> <h> <seed> <out>      denoiser::run on a seeded frame
 //   post   <w> <h> <seed> <out>       postprocess + display_settings::apply + to_byte on a seeded image
 //   sky    <w> <h> <out>              atmosphere::bake and sun_transmittance for four suns and settings
@@ -329,6 +331,65 @@ int cmd_render(int argc, char** argv) {
     return 0;
 }
 
+// features <scene> <width> <spp> <batches> <threads> <out>: camera::render
+// with collect_features (camera.h:207-221, first_surface :253-277); per pixel
+// the batch mean and variance of the mean of radiance, albedo and normal
+// (3 x 2 each), then the mean over batches of frame.variance.
+int cmd_features(int argc, char** argv) {
+    if (argc < 8)
+        return 2;
+    scene sc;
+    if (!load(argv[2], sc))
+        return 1;
+    int width = std::atoi(argv[3]), spp = std::atoi(argv[4]), batches = std::atoi(argv[5]);
+    auto& cam = sc.cam;
+    if (width > 0)
+        cam.image_width = width;
+    cam.samples_per_pixel = spp;
+    cam.threads = std::atoi(argv[6]);
+    cam.collect_features = true;
+    World w(sc);
+    std::vector<double> sum, sum2, var;
+    int W = 0, H = 0;
+    std::clog.setstate(std::ios::failbit);
+    for (int b = 0; b < batches; b++) {
+        frame f = cam.render(*w.world, sc.lights);
+        W = cam.image_width;
+        H = cam.height();
+        size_t n = f.radiance.size();
+        if (sum.empty()) {
+            sum.assign(n * 9, 0.0);
+            sum2.assign(n * 9, 0.0);
+            var.assign(n, 0.0);
+        }
+        for (size_t k = 0; k < n; k++) {
+            const color* src[3] = {&f.radiance[k], &f.albedo[k], &f.normal[k]};
+            for (int q = 0; q < 3; q++)
+                for (int c = 0; c < 3; c++) {
+                    double x = (*src[q])[c];
+                    sum[9 * k + 3 * q + c] += x;
+                    sum2[9 * k + 3 * q + c] += x * x;
+                }
+            var[k] += f.variance[k] / batches;
+        }
+    }
+    std::clog.clear();
+    Out out(argv[7]);
+    out.put(double(W));
+    out.put(double(H));
+    out.put(double(spp));
+    out.put(double(batches));
+    for (size_t k = 0; k < var.size(); k++) {
+        for (int q = 0; q < 9; q++) {
+            double m = sum[9 * k + q] / batches;
+            out.put(m);
+            out.put(batches > 1 ? std::fmax(sum2[9 * k + q] / batches - m * m, 0.0) / (batches - 1) : 0.0);
+        }
+        out.put(var[k]);
+    }
+    return 0;
+}
+
 // denoise <w> <h> <seed> <out>: a seeded synthetic frame (noisy radiance over
 // an albedo edge, a normal edge, a few fireflies, per-pixel variance) and
 // denoiser::run's output with the default settings (denoiser.h:39-43).
@@ -496,6 +557,7 @@ int main(int argc, char** argv) {
     else if (c == "env") rc = cmd_env(argc, argv);
     else if (c == "ggx") rc = cmd_ggx(argc, argv);
     else if (c == "render") rc = cmd_render(argc, argv);
+    else if (c == "features") rc = cmd_features(argc, argv);
     else if (c == "denoise") rc = cmd_denoise(argc, argv);
     else if (c == "post") rc = cmd_post(argc, argv);
     else if (c == "sky") rc = cmd_sky(argc, argv);

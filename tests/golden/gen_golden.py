@@ -232,6 +232,9 @@ RENDERS = [
     ("voxels_style.scene", 48, 64, 16),
     ("alpha_masks.scene", 48, 64, 16),
     ("gallery.scene", 48, 64, 16),
+    ("defocus_bokeh.scene", 64, 64, 32),
+    ("ortho.scene", 64, 64, 32),
+    ("checker.scene", 64, 64, 32),
 ]
 
 
@@ -248,6 +251,50 @@ def gen_render(only=None):
                             var_of_mean=data[..., 1].astype(np.float32), spp=int(s * b), batches=int(b),
                             seconds=float(seconds))
         print(f"{name}: {int(w)}x{int(h)}, {int(s)} spp x {int(b)} batches, {seconds:.1f} s")
+
+
+# The benchmark configurations at test size (config_scenes.py): (name, spp per
+# batch, batches). Their scenes are generated into a scratch folder, rendered
+# there, and only the images and the inputs' digest are kept.
+CONFIG_RENDERS = [("c2", 64, 64), ("c3", 64, 32), ("c5", 256, 64)]
+
+
+def gen_configs(only=None):
+    sys.path.insert(0, HERE)
+    import config_scenes
+    threads = os.cpu_count() or 1
+    for name, spp, batches in CONFIG_RENDERS:
+        if only and name not in only:
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
+            path, digest = config_scenes.CONFIGS[name](tmp)
+            raw = run("render", path, 0, spp, batches, threads)
+        w, h, s, b, seconds = raw[:5]
+        data = raw[5:].reshape(int(h), int(w), 3, 2)
+        np.savez_compressed(os.path.join(HERE, f"render_{name}.npz"), mean=data[..., 0].astype(np.float32),
+                            var_of_mean=data[..., 1].astype(np.float32), spp=int(s * b), batches=int(b),
+                            seconds=float(seconds), digest=digest)
+        print(f"{name}: {int(w)}x{int(h)}, {int(s)} spp x {int(b)} batches, {seconds:.1f} s")
+
+
+# (scene, width, spp per batch, batches) of the feature-buffer goldens
+FEATURES = [("materials.scene", 48, 64, 32), ("cornell_c1.scene", 32, 64, 32)]
+
+
+def gen_features():
+    """camera::render with collect_features: radiance, first_surface albedo and
+    normal (camera.h:253-277) and the luminance variance buffer."""
+    threads = os.cpu_count() or 1
+    for name, width, spp, batches in FEATURES:
+        raw = run("features", scene(name), width, spp, batches, threads)
+        w, h = int(raw[0]), int(raw[1])
+        recs = raw[4:].reshape(h, w, 19)
+        mv = recs[..., :18].reshape(h, w, 3, 3, 2)  # quantity, channel, (mean, var of mean)
+        np.savez_compressed(os.path.join(HERE, f"features_{name.replace('.scene', '')}.npz"),
+                            radiance=mv[:, :, 0, :, 0], radiance_var=mv[:, :, 0, :, 1], albedo=mv[:, :, 1, :, 0],
+                            albedo_var=mv[:, :, 1, :, 1], normal=mv[:, :, 2, :, 0], normal_var=mv[:, :, 2, :, 1],
+                            variance=recs[..., 18], spp=int(raw[2]), batches=int(raw[3]))
+        print(f"features {name}: {w}x{h}")
 
 
 def gen_denoise():
@@ -354,7 +401,7 @@ def gen_images():
 
 GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_env, "ggx": gen_ggx,
           "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post, "sky": gen_sky,
-          "images": gen_images, "gltf": gen_gltf}
+          "images": gen_images, "gltf": gen_gltf, "configs": gen_configs, "features": gen_features}
 
 if __name__ == "__main__":
     ref = os.environ.get("REFERENCE", "/root/reference")
@@ -372,6 +419,9 @@ if __name__ == "__main__":
     args = sys.argv[1:]
     if args[:1] == ["render"] and len(args) > 1:  # render <scene> ...: only those renders
         gen_render(args[1:])
+        args = []
+    elif args[:1] == ["configs"] and len(args) > 1:  # configs c2 ...: only those
+        gen_configs(args[1:])
         args = []
     elif not args:
         args = list(GROUPS)

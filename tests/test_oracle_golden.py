@@ -153,7 +153,9 @@ def test_ggx_table_matches_reference():
 
 
 def render_z(rad, var, g):
-    z = (rad - g["mean"]) / np.sqrt(var + g["var_of_mean"] + 1e-30)
+    # pixels without Monte Carlo noise (a uniform sky seen directly) get a
+    # floor of 1e-4 of their value
+    z = (rad - g["mean"]) / np.sqrt(var + g["var_of_mean"] + (1e-4 * np.abs(g["mean"])) ** 2 + 1e-30)
     n = rad.shape[0] * rad.shape[1]
     tot_sigma = np.sqrt(var.sum(axis=(0, 1)) + g["var_of_mean"].sum(axis=(0, 1))) / n
     tot_z = (rad.mean(axis=(0, 1)) - g["mean"].mean(axis=(0, 1))) / tot_sigma
@@ -161,7 +163,7 @@ def render_z(rad, var, g):
 
 
 @pytest.mark.parametrize("name", ["cornell_c1", "env_spheres", "fog_box", "materials", "voxels", "voxels_style",
-                                  "alpha_masks", "gallery"])
+                                  "alpha_masks", "gallery", "defocus_bokeh", "ortho", "checker"])
 def test_oracle_render_matches_reference_render(name):
     """Per-pixel means within 3 sigma of the combined Monte Carlo error, for
     the oracle vs the reference's batch means."""
@@ -173,5 +175,57 @@ def test_oracle_render_matches_reference_render(name):
     rad, var, _ = orc.OracleScene(sc).render(cam, threads=0)
     z, tot_z = render_z(rad, var, g)
     assert np.mean(np.abs(z) > 3) < 0.02
-    assert np.mean(np.abs(z) > 5) < 0.001
+    assert np.mean(np.abs(z) > 5) < 0.002
     assert np.all(np.abs(tot_z) < 4), tot_z
+
+
+@pytest.mark.parametrize("name,spp", [("c2", 1024), ("c3", 1024), ("c5", 8192)])
+def test_oracle_matches_reference_on_configs(name, spp, tmp_path):
+    """The benchmark configurations at test size (tests/golden/config_scenes.py):
+    the generated inputs are the ones the reference rendered (digest), and the
+    oracle's image is within 3 sigma of the reference's. The sample counts are
+    high enough for the per-pixel variance estimates to see the rare bright
+    paths (in the hall, a diffuse bounce that finds a sunlit patch): with a
+    few hundred samples most pixels have not met one yet and their spread is
+    underestimated."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import config_scenes
+    g = load_golden(f"render_{name}")
+    path, digest = config_scenes.CONFIGS[name](str(tmp_path))
+    assert digest == str(g["digest"])
+    sc = mp.load_scene(path)
+    cam = sc.camera
+    assert (cam.image_width, cam.height()) == (g["mean"].shape[1], g["mean"].shape[0])
+    cam.samples_per_pixel = spp
+    rad, var, _ = orc.OracleScene(sc).render(cam, threads=0)
+    z, tot_z = render_z(rad, var, g)
+    assert np.mean(np.abs(z) > 3) < 0.02, np.mean(np.abs(z) > 3)
+    assert np.mean(np.abs(z) > 5) < 0.002
+    assert np.all(np.abs(tot_z) < 4), tot_z
+
+
+@pytest.mark.parametrize("name", ["materials", "cornell_c1"])
+def test_oracle_features_match_reference(name):
+    """first_surface's albedo and normal (camera.h:253-277) and the luminance
+    variance buffer (camera.h:237-244), oracle against reference."""
+    g = load_golden(f"features_{name}")
+    sc = mp.load_scene(scene_path(f"{name}.scene"))
+    h, w = g["albedo"].shape[:2]
+    cam = sc.camera
+    cam.image_width = w
+    spp = int(g["spp"]) * int(g["batches"]) // 4
+    cam.samples_per_pixel = spp
+    rad, var, ex = orc.OracleScene(sc).render(cam, threads=0, features=True)
+    for q in ("albedo", "normal"):
+        # a quarter of the reference's samples: four times its variance; a
+        # floor of one sample's weight where the reference saw no spread
+        z = (ex[q] - g[q]) / np.sqrt(5 * g[f"{q}_var"] + (1.0 / spp) ** 2 + (1e-4 * np.abs(g[q])) ** 2)
+        assert np.mean(np.abs(z) > 3) < 0.02, (q, np.mean(np.abs(z) > 3))
+        assert np.mean(np.abs(z) > 5) < 0.002, q
+    # the variance of the mean over spp samples against the reference's over
+    # spp / batches (times the ratio of sample counts); per pixel the median,
+    # since image sums of variance estimates swing with single fireflies
+    ratio = ex["lum_var"] * (spp / int(g["spp"])) / np.maximum(g["variance"], 1e-30)
+    lit = g["variance"] > 0
+    assert abs(np.median(ratio[lit]) - 1) < 0.1, np.median(ratio[lit])
