@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <map>
 #include <memory>
 #include <set>
@@ -34,6 +35,7 @@
 #include "host_scene.h"
 #include "gltf_reader.h"
 #include "image_reader.h"
+#include "scene_words.h"
 #include "sky_model.h"
 #include "vox_reader.h"
 
@@ -455,125 +457,129 @@ class Loader {
         return luminance(V3(m.p[0], m.p[1], m.p[2]) * m.p[5]);
     }
 
-    // ------------------------------------------------------ number reading
+    // ------------------------------------------------------ values of a line
 
-    bool read_color_or_texture(std::istringstream& in, const std::string& first, int& tex) {
-        if (first == "texture") {
-            std::string name;
-            if (!(in >> name))
-                return false;
-            auto it = textures.find(name);
-            if (it == textures.end()) {
-                error = "unknown texture '" + name + "'";
-                return false;
-            }
-            tex = it->second;
-            return true;
-        }
-        std::istringstream rgb(first);
-        double r, g, b;
-        if (!(rgb >> r) || !(in >> g >> b))
-            return false;
-        tex = add_texture_solid(V3(r, g, b));
-        return true;
-    }
-
-    bool read_texture_name(std::istringstream& in, int& tex) {
+    // "<name>" of a texture defined on an earlier line.
+    bool named_texture(Words& w, int& tex) {
         std::string name;
-        if (!(in >> name)) {
+        if (!w.word(name)) {
             error = "expected a texture name";
             return false;
         }
-        auto it = textures.find(name);
-        if (it == textures.end()) {
+        auto found = textures.find(name);
+        if (found == textures.end()) {
             error = "unknown texture '" + name + "'";
             return false;
         }
-        tex = it->second;
+        tex = found->second;
         return true;
     }
 
-    bool read_value_or_texture(std::istringstream& in, int& tex) {
-        std::string first;
-        if (!(in >> first))
+    // A color: "<r> <g> <b>" (a new solid texture) or "texture <name>". A
+    // missing name leaves `error` empty, so the line's usage is reported.
+    bool color_source(Words& w, int& tex) {
+        if (w.peek() == "texture") {
+            w.skip();
+            if (!w.more())
+                return false;
+            return named_texture(w, tex);
+        }
+        V3 c;
+        if (!w.triple(c))
             return false;
-        if (first == "texture")
-            return read_texture_name(in, tex);
-        std::istringstream number(first);
+        tex = add_texture_solid(c);
+        return true;
+    }
+
+    // A principled weight: a number in [0, 1] (a new grey solid texture) or
+    // "texture <name>" (its red channel is read at every hit).
+    bool unit_source(Words& w, int& tex) {
+        if (w.peek() == "texture") {
+            w.skip();
+            return named_texture(w, tex);
+        }
         double x;
-        if (!(number >> x) || x < 0 || x > 1)
+        if (!w.number(x, between(0, 1, false, false)))
             return false;
         tex = add_texture_solid(V3(x, x, x));
         return true;
     }
 
-    // Optional material name, then transforms in order (scene.h:330-403).
-    bool read_tail(std::istringstream& in, int& mat, Xf& xform, bool& transformed) {
-        mat = default_material;
-        xform = Xf();
-        transformed = false;
-        auto is_transform = [](const std::string& t) {
-            return t == "translate" || t == "scale" || t == "rotate" || t == "rotate_x" || t == "rotate_y" ||
-                   t == "rotate_z";
+    // The transforms an object line may end with, applied in the order
+    // written. `count` numbers follow the name; scale takes one (uniform) or,
+    // when a second number follows, three.
+    struct TransformForm {
+        const char* name;
+        int count;
+        Xf (*step)(const double* v);
+        bool (*valid)(const double* v);
+    };
+    static const TransformForm* transform_form(const std::string& name) {
+        static const TransformForm forms[] = {
+            {"translate", 3, [](const double* v) { return Xf::translate(V3(v[0], v[1], v[2])); }, nullptr},
+            {"scale", 1, [](const double* v) { return Xf::scale(V3(v[0], v[1], v[2])); },
+             [](const double* v) { return v[0] != 0 && v[1] != 0 && v[2] != 0; }},
+            {"rotate", 4, [](const double* v) { return Xf::rotate(v[0], V3(v[1], v[2], v[3])); },
+             [](const double* v) { return V3(v[1], v[2], v[3]).length_squared() > 0; }},
+            {"rotate_x", 1, [](const double* v) { return Xf::rotate(v[0], V3(1, 0, 0)); }, nullptr},
+            {"rotate_y", 1, [](const double* v) { return Xf::rotate(v[0], V3(0, 1, 0)); }, nullptr},
+            {"rotate_z", 1, [](const double* v) { return Xf::rotate(v[0], V3(0, 0, 1)); }, nullptr},
         };
-        std::string token;
-        if (!(in >> token))
-            return true;
-        if (!is_transform(token)) {
-            auto it = materials.find(token);
-            if (it == materials.end()) {
-                error = "unknown material '" + token + "'";
+        for (const auto& f : forms)
+            if (name == f.name)
+                return &f;
+        return nullptr;
+    }
+
+    // Where an object goes: the material named after its geometry (else the
+    // default grey), and the transforms after that (scene.h's grammar,
+    // scene.h:44-243: "Any object can be followed by transforms").
+    struct Placement {
+        int material = -1;
+        Xf xform;            // object space to world space
+        bool moved = false;  // any transform was given
+    };
+
+    bool read_placement(Words& w, Placement& out) {
+        out = Placement();
+        out.material = default_material;
+        if (w.more() && !transform_form(w.peek())) {
+            std::string name;
+            w.word(name);
+            auto found = materials.find(name);
+            if (found == materials.end()) {
+                error = "unknown material '" + name + "'";
                 return false;
             }
-            mat = it->second;
-            if (!(in >> token))
-                return true;
+            out.material = found->second;
         }
-        do {
-            Xf step;
-            bool ok = true;
-            if (token == "translate") {
-                V3 d;
-                ok = bool(in >> d.x >> d.y >> d.z);
-                step = Xf::translate(d);
-            } else if (token == "rotate_x" || token == "rotate_y" || token == "rotate_z") {
-                double deg;
-                ok = bool(in >> deg);
-                V3 axis(token == "rotate_x", token == "rotate_y", token == "rotate_z");
-                step = Xf::rotate(deg, axis);
-            } else if (token == "rotate") {
-                double deg;
-                V3 axis;
-                ok = bool(in >> deg >> axis.x >> axis.y >> axis.z) && axis.length_squared() > 0;
-                if (ok)
-                    step = Xf::rotate(deg, axis);
-            } else if (token == "scale") {
-                V3 f;
-                ok = bool(in >> f.x);
-                if (ok) {
-                    std::streampos mark = in.tellg();
-                    if (in >> f.y) {
-                        ok = bool(in >> f.z);
-                    } else {
-                        in.clear();
-                        in.seekg(mark);
-                        f = V3(f.x, f.x, f.x);
-                    }
-                }
-                ok = ok && f.x != 0 && f.y != 0 && f.z != 0;
-                step = Xf::scale(f);
-            } else {
-                error = "unexpected value '" + token +
+        std::string name;
+        while (w.word(name)) {
+            const TransformForm* form = transform_form(name);
+            if (!form) {
+                error = "unexpected value '" + name +
                         "' (expected a transform: translate, scale, rotate, rotate_x, rotate_y or rotate_z)";
                 return false;
             }
+            double v[4] = {0, 0, 0, 0};
+            bool ok = true;
+            for (int k = 0; k < form->count && ok; k++)
+                ok = w.number(v[k]);
+            if (ok && form->count == 1 && std::string(form->name) == "scale") {
+                if (w.next_is_number())
+                    ok = w.number(v[1]) && w.number(v[2]);
+                else
+                    v[1] = v[2] = v[0];
+            }
+            if (ok && form->valid)
+                ok = form->valid(v);
             if (!ok) {
-                error = "bad values for '" + token + "'";
+                error = "bad values for '" + name + "'";
                 return false;
             }
-            xform = step.then_after(xform);
-            transformed = true;
-        } while (in >> token);
+            out.xform = form->step(v).then_after(out.xform);
+            out.moved = true;
+        }
         return true;
     }
 
@@ -782,23 +788,39 @@ class Loader {
         int material = -1, alpha_mask = -1;
     };
 
-    // Reads an MTL file into result (include/obj_loader.h:33-177): Kd / map_Kd
-    // give a lambertian, a non-black Ks a principled material with roughness
-    // sqrt(sqrt(2 / (Ns + 2))) and ior Ni (1.5 unless above 1), Ke an emissive
-    // one; norm / map_Bump / bump / map_Disp / disp a tangent-space normal map
-    // (grey images under the bump and disp names are height maps, skipped);
-    // map_d, else an alpha channel in map_Kd, the alpha mask. Textures repeat
-    // and are relative to the MTL file; options before a file name are skipped
-    // by taking the last word. An image that cannot be loaded gives a warning
-    // and the plain color. False only if the file cannot be opened.
+    // The directory part of a path, with its slash ("" for a bare name).
+    static std::string directory_of(const std::string& path) {
+        auto slash = path.find_last_of('/');
+        return slash == std::string::npos ? "" : path.substr(0, slash + 1);
+    }
+
+    // One MTL material as its statements leave it (obj_loader.h:33-177 says
+    // what each means and the defaults: Kd 0.8 grey, no Ks or Ke, Ns 0, Ni 1.5).
+    struct MtlEntry {
+        V3 kd{0.8, 0.8, 0.8}, ks{0, 0, 0}, ke{0, 0, 0};
+        double ns = 0, ni = 1.5;
+        int map_kd = -1, map_d = -1, normal_map = -1;
+    };
+
+    // Reads an MTL file into result. Each statement has an entry in a table
+    // that says how it changes the material being defined: Kd / Ks / Ke a
+    // color (one value is grey), Ns / Ni a number, map_Kd / map_d an image
+    // (the last word of the line: options before the file name are skipped),
+    // norm and the bump / displacement names a tangent-space normal map (a
+    // grey image under the bump and disp names is a height map, skipped).
+    // Textures repeat and are relative to the MTL file; one that cannot be
+    // loaded gives a warning and the plain color. Then each material becomes
+    // a lambertian, a principled material (a non-black Ks: roughness
+    // sqrt(sqrt(2 / (Ns + 2))), ior Ni unless it is not above 1) or an
+    // emissive one (a non-black Ke), with map_d, else an alpha channel of
+    // map_Kd, as its coverage mask. False only if the file cannot be opened.
     bool load_mtl(const std::string& path, std::map<std::string, MtlMaterial>& result, std::string& err) {
         std::ifstream file(path);
         if (!file) {
             err = "cannot open '" + path + "'";
             return false;
         }
-        auto slash = path.find_last_of('/');
-        std::string dir = slash == std::string::npos ? "" : path.substr(0, slash + 1);
+        const std::string dir = directory_of(path);
         auto image = [&](const std::string& name, bool linear) {
             std::string full = name[0] == '/' ? name : dir + name;
             std::string e;
@@ -807,108 +829,123 @@ class Loader {
                 std::fprintf(stderr, "Warning: %s: cannot load texture '%s'\n", path.c_str(), full.c_str());
             return t;
         };
-        struct Entry {
-            V3 kd{0.8, 0.8, 0.8}, ks{0, 0, 0}, ke{0, 0, 0};
-            double ns = 0, ni = 1.5;
-            int map_kd = -1, map_d = -1, normal_map = -1;
+        auto last_word = [](Words& w) {
+            std::string word, last;
+            while (w.word(word))
+                last = word;
+            return last;
         };
-        std::vector<std::pair<std::string, Entry>> entries;
-        std::string line;
-        while (std::getline(file, line)) {
-            std::istringstream in(line);
-            std::string keyword;
-            if (!(in >> keyword) || keyword[0] == '#')
-                continue;
-            if (keyword == "newmtl") {
-                std::string name;
-                in >> name;
-                entries.push_back({name, Entry()});
-                continue;
-            }
-            if (entries.empty())
-                continue;
-            Entry& e = entries.back().second;
-            auto read_color = [&](V3& c) {
-                double r, g, b;
-                if (in >> r) {
-                    c = V3(r, r, r);  // one value is grey
-                    if (in >> g >> b)
-                        c = V3(r, g, b);
-                }
+        using Statement = std::function<void(MtlEntry&, Words&)>;
+        auto color = [](V3 MtlEntry::*field) -> Statement {
+            return [field](MtlEntry& e, Words& w) {
+                double grey;
+                if (!w.number(grey))
+                    return;
+                V3 rgb(grey, grey, grey);
+                double g, b;
+                if (w.number(g) && w.number(b))
+                    rgb = V3(grey, g, b);
+                e.*field = rgb;
             };
-            auto last_word = [&]() {
-                std::string word, last;
-                while (in >> word)
-                    last = word;
-                return last;
+        };
+        auto scalar = [](double MtlEntry::*field) -> Statement {
+            return [field](MtlEntry& e, Words& w) {
+                if (!w.more())
+                    return;
+                double x = 0;
+                e.*field = w.number(x) ? x : 0.0;
             };
-            if (keyword == "Kd") {
-                read_color(e.kd);
-            } else if (keyword == "Ks") {
-                read_color(e.ks);
-            } else if (keyword == "Ke") {
-                read_color(e.ke);
-            } else if (keyword == "Ns") {
-                in >> e.ns;
-            } else if (keyword == "Ni") {
-                in >> e.ni;
-            } else if (keyword == "map_Kd") {
-                std::string f = last_word();
+        };
+        auto picture = [&](int MtlEntry::*field) -> Statement {
+            return [&, field](MtlEntry& e, Words& w) {
+                std::string f = last_word(w);
                 if (!f.empty())
-                    e.map_kd = image(f, false);
-            } else if (keyword == "map_d") {
-                std::string f = last_word();
-                if (!f.empty())
-                    e.map_d = image(f, false);
-            } else if (keyword == "norm" || keyword == "map_Bump" || keyword == "map_bump" || keyword == "bump" ||
-                       keyword == "map_Disp" || keyword == "disp") {
-                std::string f = last_word();
+                    e.*field = image(f, false);
+            };
+        };
+        auto normals = [&](bool named_norm) -> Statement {
+            return [&, named_norm](MtlEntry& e, Words& w) {
+                std::string f = last_word(w);
                 if (f.empty() || !use_normal_maps)
-                    continue;
+                    return;
                 int t = image(f, true);
-                if (t >= 0 && keyword != "norm" && image_info[t].grey) {
+                if (t >= 0 && !named_norm && image_info[t].grey) {
                     std::fprintf(stderr, "Warning: %s: '%s' is a height map; only normal maps are supported\n",
                                  path.c_str(), f.c_str());
-                    continue;
+                    return;
                 }
                 if (t >= 0)
                     e.normal_map = t;
+            };
+        };
+        const std::map<std::string, Statement> statements = {
+            {"Kd", color(&MtlEntry::kd)},         {"Ks", color(&MtlEntry::ks)},
+            {"Ke", color(&MtlEntry::ke)},         {"Ns", scalar(&MtlEntry::ns)},
+            {"Ni", scalar(&MtlEntry::ni)},        {"map_Kd", picture(&MtlEntry::map_kd)},
+            {"map_d", picture(&MtlEntry::map_d)}, {"norm", normals(true)},
+            {"map_Bump", normals(false)},         {"map_bump", normals(false)},
+            {"bump", normals(false)},             {"map_Disp", normals(false)},
+            {"disp", normals(false)},
+        };
+        std::vector<std::pair<std::string, MtlEntry>> defined;
+        std::string line;
+        while (std::getline(file, line)) {
+            Words w(line);
+            std::string keyword;
+            if (!w.word(keyword) || keyword[0] == '#')
+                continue;
+            if (keyword == "newmtl") {
+                std::string name;
+                w.word(name);
+                defined.emplace_back(name, MtlEntry());
+                continue;
             }
+            auto st = statements.find(keyword);
+            if (st != statements.end() && !defined.empty())
+                st->second(defined.back().second, w);
         }
-        for (auto& [name, e] : entries) {
-            MtlMaterial out;
-            int base = e.map_kd >= 0 ? e.map_kd : -1;
-            bool emits = e.ke.length_squared() > 0;
-            mypbr_material m;
-            if (emits) {
-                m = blank_material(MYPBR_MAT_DIFFUSE_LIGHT);
-                m.p[0] = e.ke.x;
-                m.p[1] = e.ke.y;
-                m.p[2] = e.ke.z;
-                m.p[3] = 180;
-                m.p[4] = kInf;
-                m.p[5] = 1;
-            } else if (e.ks.length_squared() > 0) {
-                double roughness = std::sqrt(std::sqrt(2 / (std::fmax(e.ns, 0.0) + 2)));
-                double ior = e.ni > 1 ? e.ni : 1.5;
-                int color = base >= 0 ? base : add_texture_solid(e.kd);
-                int metallic = add_texture_solid(V3(0, 0, 0));
-                m = principled_desc(color, metallic, add_texture_solid(V3(roughness, roughness, roughness)), ior);
-            } else {
-                m = blank_material(MYPBR_MAT_LAMBERTIAN);
-                m.tex[0] = base >= 0 ? base : add_texture_solid(e.kd);
-            }
-            // normal_mapped wraps the surface materials, not lights (obj_loader.h:166-167)
-            if (e.normal_map >= 0 && !emits)
-                m.normal_map = e.normal_map;
-            out.material = add_material(m);
-            if (e.map_d >= 0 && !image_info[e.map_d].opaque)
-                out.alpha_mask = e.map_d;
-            else if (e.map_d < 0 && e.map_kd >= 0 && image_info[e.map_kd].alpha_channel && !image_info[e.map_kd].opaque)
-                out.alpha_mask = e.map_kd;
-            result[name] = out;
-        }
+        for (const auto& [name, e] : defined)
+            result[name] = mtl_material(e);
         return true;
+    }
+
+    // The material and coverage mask an MTL entry stands for.
+    MtlMaterial mtl_material(const MtlEntry& e) {
+        MtlMaterial out;
+        auto albedo = [&]() { return e.map_kd >= 0 ? e.map_kd : add_texture_solid(e.kd); };
+        const bool emits = e.ke.length_squared() > 0;
+        mypbr_material m;
+        if (emits) {
+            m = blank_material(MYPBR_MAT_DIFFUSE_LIGHT);
+            m.p[0] = e.ke.x;
+            m.p[1] = e.ke.y;
+            m.p[2] = e.ke.z;
+            m.p[3] = 180;
+            m.p[4] = kInf;
+            m.p[5] = 1;
+        } else if (e.ks.length_squared() > 0) {
+            // a Phong exponent n spreads like a microfacet alpha of
+            // sqrt(2 / (n + 2)), and roughness is sqrt(alpha)
+            double alpha = std::sqrt(2 / (std::max(e.ns, 0.0) + 2));
+            double roughness = std::sqrt(alpha);
+            int color = albedo();
+            int metallic = add_texture_solid(V3(0, 0, 0));
+            int rough = add_texture_solid(V3(roughness, roughness, roughness));
+            m = principled_desc(color, metallic, rough, e.ni > 1 ? e.ni : 1.5);
+        } else {
+            m = blank_material(MYPBR_MAT_LAMBERTIAN);
+            m.tex[0] = albedo();
+        }
+        // a normal map bends surfaces, not lights (obj_loader.h:166-167)
+        if (e.normal_map >= 0 && !emits)
+            m.normal_map = e.normal_map;
+        out.material = add_material(m);
+        auto masks = [&](int t) { return t >= 0 && !image_info[t].opaque; };
+        if (e.map_d >= 0)
+            out.alpha_mask = masks(e.map_d) ? e.map_d : -1;
+        else if (e.map_kd >= 0 && image_info[e.map_kd].alpha_channel && masks(e.map_kd))
+            out.alpha_mask = e.map_kd;
+        return out;
     }
 
     // A Wavefront OBJ file (include/obj_loader.h:191-340): faces triangulated
@@ -921,130 +958,143 @@ class Loader {
     };
     using Surface = std::pair<int, int>;  // (material, alpha mask texture or -1)
 
+    // An OBJ index (1-based, or negative: counted back from the end of the
+    // list so far) as a 0-based one; -1 when it is 0 (absent) or outside.
+    static int obj_index(long index, size_t count) {
+        long n = long(count);
+        long k = index > 0 ? index - 1 : n + index;
+        return index != 0 && k >= 0 && k < n ? int(k) : -1;
+    }
+
+    // Up to `n` leading numbers of the words left (fewer present: zeros).
+    static V3 leading_numbers(Words& w, int n) {
+        double x[3] = {0, 0, 0};
+        for (int k = 0; k < n && w.number(x[k]); k++) {
+        }
+        return V3(x[0], x[1], x[2]);
+    }
+
+    // One corner of a face: "v", "v/t", "v//n" or "v/t/n" (each an OBJ
+    // index; an empty or unreadable t or n is absent). False when v is not
+    // an integer.
+    static bool face_corner(const std::string& word, long& v, long& t, long& n) {
+        long parts[3] = {0, 0, 0};
+        size_t field = 0, begin = 0;
+        for (size_t i = 0; i <= word.size() && field < 3; i++) {
+            if (i < word.size() && word[i] != '/')
+                continue;
+            int value;
+            if (word_is_integer(word.substr(begin, i - begin), value))
+                parts[field] = value;
+            else if (field == 0)
+                return false;
+            field++;
+            begin = i + 1;
+        }
+        v = parts[0];
+        t = parts[1];
+        n = parts[2];
+        return true;
+    }
+
+    // Reads an OBJ file line by line: v / vn / vt lists, f polygons (each
+    // cut into a fan of triangles around its first corner as the corners
+    // arrive; degenerate ones dropped), usemtl (the rest of the line names a
+    // surface: the scene material of that name, else the MTL material of
+    // that name with its mask, else the mesh line's material) and mtllib
+    // (MTL files relative to the OBJ; one that is missing gives a warning).
+    // Other statements are ignored. With `smooth`, a file without normals
+    // gets at each vertex the sum of the (area-weighted) normals of the
+    // faces around it.
     bool add_obj(const std::string& file, bool smooth, int line_mat, const Xf& xform, bool transformed) {
         std::ifstream in(file);
         if (!in) {
             error = "cannot open '" + file + "'";
             return false;
         }
+        const std::string obj_dir = directory_of(file);
         std::vector<V3> pos, nrm, uv;
         std::vector<Surface> part_order;
         std::map<Surface, std::vector<Face>> faces;
         Surface current{line_mat, -1};
         std::map<std::string, MtlMaterial> file_materials;
-        auto slash = file.find_last_of('/');
-        std::string obj_dir = slash == std::string::npos ? "" : file.substr(0, slash + 1);
-        auto resolve = [](long index, size_t count) -> int {
-            if (index > 0 && size_t(index) <= count)
-                return int(index - 1);
-            if (index < 0 && size_t(-index) <= count)
-                return int(long(count) + index);
-            return -1;
+        auto where = [&](int ln) { return file + ":" + std::to_string(ln) + ": "; };
+        auto emit = [&](const int (&c)[3][3]) {
+            const V3& p0 = pos[size_t(c[0][0])];
+            if (cross(pos[size_t(c[1][0])] - p0, pos[size_t(c[2][0])] - p0).near_zero())
+                return;
+            Face f;
+            for (int k = 0; k < 3; k++) {
+                f.v[k] = c[k][0];
+                f.t[k] = c[k][1];
+                f.n[k] = c[k][2];
+            }
+            auto& list = faces[current];
+            if (list.empty())
+                part_order.push_back(current);
+            list.push_back(f);
         };
         std::string line;
-        int ln = 0;
-        while (std::getline(in, line)) {
-            ln++;
-            const char* s = line.c_str();
-            while (*s == ' ' || *s == '\t')
-                s++;
-            auto read_vec = [&](const char* p, int n) {
-                double x[3] = {0, 0, 0};
-                char* end;
-                for (int k = 0; k < n; k++) {
-                    x[k] = std::strtod(p, &end);
-                    p = end;
-                }
-                return V3(x[0], x[1], x[2]);
-            };
-            if (s[0] == 'v' && (s[1] == ' ' || s[1] == '\t')) {
-                pos.push_back(read_vec(s + 2, 3));
-            } else if (s[0] == 'v' && s[1] == 'n') {
-                nrm.push_back(read_vec(s + 2, 3));
-            } else if (s[0] == 'v' && s[1] == 't') {
-                uv.push_back(read_vec(s + 2, 2));
-            } else if (s[0] == 'f' && (s[1] == ' ' || s[1] == '\t')) {
-                std::vector<int> vs, ns, ts;
-                const char* p = s + 2;
-                while (true) {
-                    while (*p == ' ' || *p == '\t' || *p == '\r')
-                        p++;
-                    if (*p == '\0')
-                        break;
-                    char* end;
-                    long v = std::strtol(p, &end, 10), t = 0, n = 0;
-                    if (end == p) {
-                        error = file + ":" + std::to_string(ln) + ": bad face";
+        for (int ln = 1; std::getline(in, line); ln++) {
+            Words w(line);
+            std::string key;
+            if (!w.word(key))
+                continue;
+            if (key == "v") {
+                pos.push_back(leading_numbers(w, 3));
+            } else if (key == "vn") {
+                nrm.push_back(leading_numbers(w, 3));
+            } else if (key == "vt") {
+                uv.push_back(leading_numbers(w, 2));
+            } else if (key == "f") {
+                int fan[3][3];  // first corner, previous corner, this corner: (v, t, n)
+                int corners = 0;
+                std::string word;
+                while (w.word(word)) {
+                    long v, t, n;
+                    if (!face_corner(word, v, t, n)) {
+                        error = where(ln) + "bad face";
                         return false;
                     }
-                    p = end;
-                    if (*p == '/') {
-                        p++;
-                        if (*p != '/') {
-                            t = std::strtol(p, &end, 10);
-                            p = end;
-                        }
-                        if (*p == '/') {
-                            p++;
-                            n = std::strtol(p, &end, 10);
-                            p = end;
-                        }
-                    }
-                    int vi = resolve(v, pos.size());
+                    int vi = obj_index(v, pos.size());
                     if (vi < 0) {
-                        error = file + ":" + std::to_string(ln) + ": vertex index out of range";
+                        error = where(ln) + "vertex index out of range";
                         return false;
                     }
-                    vs.push_back(vi);
-                    ts.push_back(resolve(t, uv.size()));
-                    ns.push_back(resolve(n, nrm.size()));
+                    int slot = std::min(corners, 2);
+                    if (corners >= 3)
+                        std::copy(std::begin(fan[2]), std::end(fan[2]), std::begin(fan[1]));
+                    fan[slot][0] = vi;
+                    fan[slot][1] = obj_index(t, uv.size());
+                    fan[slot][2] = obj_index(n, nrm.size());
+                    if (++corners >= 3)
+                        emit(fan);
                 }
-                for (size_t k = 1; k + 1 < vs.size(); k++) {
-                    Face f;
-                    size_t id[3] = {0, k, k + 1};
-                    for (int c = 0; c < 3; c++) {
-                        f.v[c] = vs[id[c]];
-                        f.n[c] = ns[id[c]];
-                        f.t[c] = ts[id[c]];
-                    }
-                    const V3& p0 = pos[f.v[0]];
-                    if (cross(pos[f.v[1]] - p0, pos[f.v[2]] - p0).near_zero())
-                        continue;
-                    if (!faces.count(current))
-                        part_order.push_back(current);
-                    faces[current].push_back(f);
-                }
-            } else if (line.compare(size_t(s - line.c_str()), 6, "usemtl") == 0) {
-                std::string name(s + 6);
+            } else if (key == "usemtl") {
+                std::string name = line.substr(line.find("usemtl") + 6);
                 name.erase(0, name.find_first_not_of(" \t"));
                 name.erase(name.find_last_not_of(" \t\r") + 1);
-                auto it = materials.find(name);
-                auto mtl = file_materials.find(name);
-                if (it != materials.end())
-                    current = {it->second, -1};
-                else if (mtl != file_materials.end())
-                    current = {mtl->second.material, mtl->second.alpha_mask};
+                if (auto scene_mat = materials.find(name); scene_mat != materials.end())
+                    current = {scene_mat->second, -1};
+                else if (auto own = file_materials.find(name); own != file_materials.end())
+                    current = {own->second.material, own->second.alpha_mask};
                 else
                     current = {line_mat, -1};
-            } else if (line.compare(size_t(s - line.c_str()), 6, "mtllib") == 0) {
-                // usually one file name; several are allowed
-                std::string names(s + 6);
-                std::istringstream list(names);
-                std::string name, mtl_error;
-                while (list >> name)
-                    if (!load_mtl(name[0] == '/' ? name : obj_dir + name, file_materials, mtl_error))
-                        std::fprintf(stderr, "Warning: %s: %s\n", file.c_str(), mtl_error.c_str());
+            } else if (key == "mtllib") {
+                std::string name, why;
+                while (w.word(name))
+                    if (!load_mtl(name[0] == '/' ? name : obj_dir + name, file_materials, why))
+                        std::fprintf(stderr, "Warning: %s: %s\n", file.c_str(), why.c_str());
             }
         }
         if (smooth && nrm.empty()) {
             nrm.assign(pos.size(), V3());
-            for (const Surface& pm : part_order)
-                for (auto& f : faces[pm]) {
-                    const V3& p0 = pos[f.v[0]];
-                    V3 n = cross(pos[f.v[1]] - p0, pos[f.v[2]] - p0);
-                    for (int c = 0; c < 3; c++) {
-                        nrm[f.v[c]] = nrm[f.v[c]] + n;
-                        f.n[c] = f.v[c];
+            for (const Surface& surface : part_order)
+                for (Face& f : faces[surface]) {
+                    V3 area_normal = cross(pos[size_t(f.v[1])] - pos[size_t(f.v[0])], pos[size_t(f.v[2])] - pos[size_t(f.v[0])]);
+                    for (int k = 0; k < 3; k++) {
+                        nrm[size_t(f.v[k])] = nrm[size_t(f.v[k])] + area_normal;
+                        f.n[k] = f.v[k];
                     }
                 }
         }
@@ -1351,288 +1401,318 @@ class Loader {
 
     // ------------------------------------------------------ lines
 
-    bool parse_material(std::istringstream& in) {
-        std::string name, type;
-        if (!(in >> name >> type))
-            return fail("expected 'material <name> <type> <parameters...>'");
-        int normal_map = -1;
-        auto read_normal_map = [&]() {
-            std::string key;
-            if (!(in >> key))
-                return true;
-            if (key != "normal_map") {
-                error = "unexpected value '" + key + "' (expected 'normal_map <texture>')";
-                return false;
-            }
-            return read_texture_name(in, normal_map);
+    // An optional "normal_map <texture>" closing a lambertian or metal line.
+    bool optional_normal_map(Words& w, int& normal_map) {
+        if (!w.more())
+            return true;
+        if (w.peek() != "normal_map") {
+            error = "unexpected value '" + w.peek() + "' (expected 'normal_map <texture>')";
+            return false;
+        }
+        w.skip();
+        return named_texture(w, normal_map);
+    }
+
+    // "key value..." settings in any order: `read` has a reader per key. A
+    // key that is not in it, or whose values are missing or out of range, is
+    // reported with the message `unknown(key)` or `bad(key)` (a reader may
+    // put its own message in `error` instead).
+    using SettingReader = std::function<bool(Words&)>;
+    bool settings(Words& w, const std::map<std::string, SettingReader>& read,
+                  const std::function<std::string(const std::string&)>& unknown,
+                  const std::function<std::string(const std::string&)>& bad) {
+        std::string key;
+        while (w.word(key)) {
+            auto reader = read.find(key);
+            if (reader == read.end())
+                return fail(unknown(key));
+            error.clear();
+            if (!reader->second(w))
+                return fail(error.empty() ? bad(key) : error);
+        }
+        return true;
+    }
+
+    // The material types of a "material <name> <type> ..." line
+    // (scene.h:44-243 documents each; the checks on their values follow it).
+    using MaterialReader = bool (Loader::*)(Words&, mypbr_material&, int&);
+    static const std::map<std::string, MaterialReader>& material_readers() {
+        static const std::map<std::string, MaterialReader> table = {
+            {"lambertian", &Loader::lambertian_line}, {"metal", &Loader::metal_line},
+            {"dielectric", &Loader::dielectric_line}, {"thin_glass", &Loader::thin_glass_line},
+            {"principled", &Loader::principled_line}, {"volume", &Loader::volume_line},
+            {"emissive", &Loader::emissive_line},
         };
-        mypbr_material m = blank_material(0);
-        if (type == "lambertian") {
-            m.type = MYPBR_MAT_LAMBERTIAN;
-            std::string first;
-            error.clear();
-            if (!(in >> first) || !read_color_or_texture(in, first, m.tex[0]))
-                return fail(error.empty()
-                                ? "expected 'material <name> lambertian <r> <g> <b>' or '... lambertian texture <name>'"
-                                : error);
-            if (!read_normal_map())
-                return fail(error);
-        } else if (type == "metal") {
-            const char* usage = "expected 'material <name> metal <r> <g> <b> <roughness>' or "
-                                "'... metal <Al|Ti|Cu|Au|Ag|Cr> <roughness>'";
-            m.type = MYPBR_MAT_METAL;
-            std::string first;
-            double r = 0, g = 0, b = 0, roughness = 0;
-            V3 eta, k;
-            if (!(in >> first))
-                return fail(usage);
-            bool measured = find_conductor(first, eta, k);
-            if (measured) {
-                if (!(in >> roughness) || roughness < 0)
-                    return fail(usage);
-            } else {
-                std::istringstream number(first);
-                if (!(number >> r) || !(in >> g >> b >> roughness) || roughness < 0)
-                    return fail(usage);
-            }
-            error.clear();
-            if (!read_normal_map())
-                return fail(error);
-            m.p[3] = std::clamp(roughness, 0.0, 1.0);
-            if (measured) {
-                V3 f0, f_avg;
-                measured_fresnel(eta, k, f0, f_avg);
-                m.flags |= MYPBR_MATF_MEASURED;
-                for (int c = 0; c < 3; c++) {
-                    m.p[c] = f0[c];
-                    m.p[4 + c] = eta[c];
-                    m.p[7 + c] = k[c];
-                    m.p[10 + c] = f_avg[c];
-                }
-            } else {
-                V3 f0(r, g, b);
-                for (int c = 0; c < 3; c++) {
-                    m.p[c] = f0[c];
-                    m.p[10 + c] = f0[c] + (1 - f0[c]) / 21;
-                }
-            }
-        } else if (type == "dielectric") {
-            const char* usage = "expected 'material <name> dielectric <index of refraction> [roughness <r>] "
-                                "[color <r> <g> <b> [distance <d>]]'";
-            double ior, roughness = 0, distance = 1;
-            V3 tint(1, 1, 1);
-            std::string key;
-            if (!(in >> ior) || ior <= 0)
-                return fail(usage);
-            while (in >> key) {
-                bool ok = true;
-                if (key == "roughness") {
-                    ok = bool(in >> roughness) && roughness >= 0;
-                } else if (key == "color") {
-                    double r, g, b;
-                    ok = bool(in >> r >> g >> b) && r > 0 && g > 0 && b > 0 && r <= 1 && g <= 1 && b <= 1;
-                    tint = V3(r, g, b);
-                } else if (key == "distance") {
-                    ok = bool(in >> distance) && distance > 0;
-                } else {
-                    ok = false;
-                }
-                if (!ok)
-                    return fail(usage);
-            }
-            m.type = MYPBR_MAT_DIELECTRIC;
-            m.p[0] = ior;
-            m.p[1] = std::clamp(roughness, 0.0, 1.0);
-            for (int c = 0; c < 3; c++)
-                m.p[2 + c] = -std::log(tint[c]) / distance;
-        } else if (type == "thin_glass") {
-            const char* usage = "expected 'material <name> thin_glass <index of refraction> [color <r> <g> <b>]'";
-            double ior;
-            V3 tint(1, 1, 1);
-            std::string key;
-            if (!(in >> ior) || ior <= 0)
-                return fail(usage);
-            if (in >> key) {
-                double r, g, b;
-                if (key != "color" || !(in >> r >> g >> b) || r < 0 || g < 0 || b < 0 || r > 1 || g > 1 || b > 1)
-                    return fail(usage);
-                tint = V3(r, g, b);
-            }
-            m.type = MYPBR_MAT_THIN_DIELECTRIC;
-            m.p[0] = ior;
-            for (int c = 0; c < 3; c++)
-                m.p[2 + c] = tint[c];
-        } else if (type == "principled") {
-            m.type = MYPBR_MAT_PRINCIPLED;
-            int base = add_texture_solid(V3(0.8, 0.8, 0.8));
-            int metallic = add_texture_solid(V3(0, 0, 0));
-            int rough = add_texture_solid(V3(0.5, 0.5, 0.5));
-            int coat = -1, coat_rough = -1, coat_normals = -1, base_normals = -1;
-            V3 coat_tint(1, 1, 1), eta, k;
-            bool coat_tinted = false, measured = false;
-            double ior = 1.5;
-            std::string key;
-            error.clear();
-            while (in >> key) {
-                bool ok = true;
-                if (key == "texture") {
-                    ok = read_color_or_texture(in, key, base);
-                } else if (key == "color") {
-                    std::string first;
-                    ok = bool(in >> first) && read_color_or_texture(in, first, base);
-                } else if (key == "metallic") {
-                    ok = read_value_or_texture(in, metallic);
-                } else if (key == "roughness") {
-                    ok = read_value_or_texture(in, rough);
-                } else if (key == "ior") {
-                    ok = bool(in >> ior) && ior > 0;
-                } else if (key == "normal_map") {
-                    ok = read_texture_name(in, base_normals);
-                } else if (key == "clearcoat") {
-                    ok = read_value_or_texture(in, coat);
-                } else if (key == "clearcoat_roughness") {
-                    ok = read_value_or_texture(in, coat_rough);
-                } else if (key == "clearcoat_normal_map") {
-                    ok = read_texture_name(in, coat_normals);
-                } else if (key == "conductor") {
-                    std::string metal_name;
-                    ok = bool(in >> metal_name) && (measured = find_conductor(metal_name, eta, k));
-                    if (!ok)
-                        error = "unknown conductor '" + metal_name + "' (known: Al Ti Cu Au Ag Cr)";
-                } else if (key == "clearcoat_color") {
-                    double r, g, b;
-                    ok = bool(in >> r >> g >> b) && r > 0 && g > 0 && b > 0 && r <= 1 && g <= 1 && b <= 1;
-                    coat_tint = V3(r, g, b);
-                    coat_tinted = true;
-                } else {
-                    return fail("unknown principled setting '" + key + "'");
-                }
-                if (!ok)
-                    return fail(error.empty() ? "bad value for principled setting '" + key + "'" : error);
-            }
-            if ((coat_rough >= 0 || coat_normals >= 0 || coat_tinted) && coat < 0)
-                return fail("clearcoat_roughness, clearcoat_normal_map and clearcoat_color need 'clearcoat <weight>'");
-            double r0 = (ior - 1) / (ior + 1);
-            m.p[0] = r0 * r0;
-            m.tex[0] = base;
-            m.tex[1] = metallic;
-            m.tex[2] = rough;
-            m.tex[3] = use_normal_maps ? base_normals : -1;
-            if (measured) {
-                V3 f0, f_avg;
-                measured_fresnel(eta, k, f0, f_avg);
-                m.flags |= MYPBR_MATF_MEASURED;
-                for (int c = 0; c < 3; c++) {
-                    m.p[4 + c] = eta[c];
-                    m.p[7 + c] = k[c];
-                    m.p[10 + c] = f_avg[c];
-                }
-            }
-            m.p[13] = m.p[14] = m.p[15] = 1;
-            if (coat >= 0) {
-                m.flags |= MYPBR_MATF_COAT;
-                m.tex[4] = coat;
-                m.tex[5] = coat_rough >= 0 ? coat_rough : add_texture_solid(V3(0, 0, 0));
-                m.tex[6] = use_normal_maps ? coat_normals : -1;
-                for (int c = 0; c < 3; c++)
-                    m.p[13 + c] = coat_tint[c];
-                if (!(coat_tint.x == 1 && coat_tint.y == 1 && coat_tint.z == 1))
-                    m.flags |= MYPBR_MATF_COAT_TINT;
-            }
-        } else if (type == "volume") {
-            double r, g, b, aniso = 0;
-            std::string key;
-            if (!(in >> r >> g >> b))
-                return fail("expected 'material <name> volume <r> <g> <b> [g <anisotropy>]'");
-            if (in >> key) {
-                if (key != "g" || !(in >> aniso) || aniso <= -1 || aniso >= 1)
-                    return fail(
-                        "expected 'material <name> volume <r> <g> <b> [g <anisotropy between -1 and 1>]'");
-            }
-            m.type = MYPBR_MAT_PHASE;
-            m.p[0] = r;
-            m.p[1] = g;
-            m.p[2] = b;
-            m.p[3] = aniso;
-        } else if (type == "emissive") {
-            const char* usage = "expected 'material <name> emissive <r> <g> <b> [spread <degrees, 0 to 180>]'";
-            double r, g, b, spread = 180;
-            std::string key;
-            if (!(in >> r >> g >> b))
-                return fail(usage);
-            if (in >> key && (key != "spread" || !(in >> spread) || spread <= 0 || spread > 180))
-                return fail(usage);
-            m.type = MYPBR_MAT_DIFFUSE_LIGHT;
-            m.p[0] = r;
-            m.p[1] = g;
-            m.p[2] = b;
-            m.p[3] = spread;
-            double half = radians(spread) / 2;
-            m.p[4] = spread >= 180 ? kInf : std::tan(half);
-            // Cosine-weighted share of the gridded emission (material.h:600-608)
-            if (half >= kPi / 2 - 1e-9) {
-                m.p[5] = 1;
-            } else {
-                double s = std::sin(half), c = std::cos(half);
-                m.p[5] = s * s - (half - s * c) * c / s;
+        return table;
+    }
+
+    bool lambertian_line(Words& w, mypbr_material& m, int& normal_map) {
+        m.type = MYPBR_MAT_LAMBERTIAN;
+        error.clear();
+        if (!color_source(w, m.tex[0]))
+            return fail(error.empty() ? "expected 'material <name> lambertian <r> <g> <b>' or '... lambertian texture <name>'"
+                                      : error);
+        return optional_normal_map(w, normal_map) || fail(error);
+    }
+
+    bool metal_line(Words& w, mypbr_material& m, int& normal_map) {
+        const char* usage = "expected 'material <name> metal <r> <g> <b> <roughness>' or "
+                            "'... metal <Al|Ti|Cu|Au|Ag|Cr> <roughness>'";
+        m.type = MYPBR_MAT_METAL;
+        V3 eta, k, albedo;
+        double roughness = 0;
+        const bool measured = find_conductor(w.peek(), eta, k);
+        if (measured)
+            w.skip();
+        else if (!w.triple(albedo))
+            return fail(usage);
+        if (!w.number(roughness, non_negative()))
+            return fail(usage);
+        if (!optional_normal_map(w, normal_map))
+            return fail(error);
+        m.p[3] = std::clamp(roughness, 0.0, 1.0);
+        if (measured) {
+            V3 f0, f_avg;
+            measured_fresnel(eta, k, f0, f_avg);
+            m.flags |= MYPBR_MATF_MEASURED;
+            for (int c = 0; c < 3; c++) {
+                m.p[c] = f0[c];
+                m.p[4 + c] = eta[c];
+                m.p[7 + c] = k[c];
+                m.p[10 + c] = f_avg[c];
             }
         } else {
-            return fail("unknown material type '" + type + "'");
+            for (int c = 0; c < 3; c++) {
+                m.p[c] = albedo[c];
+                m.p[10 + c] = albedo[c] + (1 - albedo[c]) / 21;  // Schlick's hemispherical average
+            }
         }
+        return true;
+    }
+
+    bool dielectric_line(Words& w, mypbr_material& m, int&) {
+        const std::string usage = "expected 'material <name> dielectric <index of refraction> [roughness <r>] "
+                                  "[color <r> <g> <b> [distance <d>]]'";
+        double ior, roughness = 0, distance = 1;
+        V3 tint(1, 1, 1);
+        if (!w.number(ior, positive()))
+            return fail(usage);
+        auto says = [&](const std::string&) { return usage; };
+        if (!settings(w,
+                      {{"roughness", [&](Words& v) { return v.number(roughness, non_negative()); }},
+                       {"color", [&](Words& v) { return v.triple(tint, between(0, 1, true, false)); }},
+                       {"distance", [&](Words& v) { return v.number(distance, positive()); }}},
+                      says, says))
+            return false;
+        m.type = MYPBR_MAT_DIELECTRIC;
+        m.p[0] = ior;
+        m.p[1] = std::clamp(roughness, 0.0, 1.0);
+        for (int c = 0; c < 3; c++)
+            m.p[2 + c] = -std::log(tint[c]) / distance;  // Beer-Lambert absorption per unit length
+        return true;
+    }
+
+    bool thin_glass_line(Words& w, mypbr_material& m, int&) {
+        const char* usage = "expected 'material <name> thin_glass <index of refraction> [color <r> <g> <b>]'";
+        double ior;
+        V3 tint(1, 1, 1);
+        if (!w.number(ior, positive()))
+            return fail(usage);
+        if (w.more()) {  // one optional setting
+            std::string key;
+            w.word(key);
+            if (key != "color" || !w.triple(tint, between(0, 1, false, false)))
+                return fail(usage);
+        }
+        m.type = MYPBR_MAT_THIN_DIELECTRIC;
+        m.p[0] = ior;
+        for (int c = 0; c < 3; c++)
+            m.p[2 + c] = tint[c];
+        return true;
+    }
+
+    bool principled_line(Words& w, mypbr_material& m, int&) {
+        m.type = MYPBR_MAT_PRINCIPLED;
+        int base = add_texture_solid(V3(0.8, 0.8, 0.8));
+        int metallic = add_texture_solid(V3(0, 0, 0));
+        int rough = add_texture_solid(V3(0.5, 0.5, 0.5));
+        int coat = -1, coat_rough = -1, coat_normals = -1, base_normals = -1;
+        V3 coat_tint(1, 1, 1), eta, k;
+        bool coat_tinted = false, measured = false;
+        double ior = 1.5;
+        const std::map<std::string, SettingReader> read = {
+            {"texture", [&](Words& v) { return v.more() && named_texture(v, base); }},
+            {"color", [&](Words& v) { return color_source(v, base); }},
+            {"metallic", [&](Words& v) { return unit_source(v, metallic); }},
+            {"roughness", [&](Words& v) { return unit_source(v, rough); }},
+            {"ior", [&](Words& v) { return v.number(ior, positive()); }},
+            {"normal_map", [&](Words& v) { return named_texture(v, base_normals); }},
+            {"clearcoat", [&](Words& v) { return unit_source(v, coat); }},
+            {"clearcoat_roughness", [&](Words& v) { return unit_source(v, coat_rough); }},
+            {"clearcoat_normal_map", [&](Words& v) { return named_texture(v, coat_normals); }},
+            {"conductor",
+             [&](Words& v) {
+                 std::string metal;
+                 v.word(metal);
+                 measured = find_conductor(metal, eta, k);
+                 if (!measured)
+                     error = "unknown conductor '" + metal + "' (known: Al Ti Cu Au Ag Cr)";
+                 return measured;
+             }},
+            {"clearcoat_color",
+             [&](Words& v) { return coat_tinted = v.triple(coat_tint, between(0, 1, true, false)); }},
+        };
+        if (!settings(w, read, [](const std::string& key) { return "unknown principled setting '" + key + "'"; },
+                      [](const std::string& key) { return "bad value for principled setting '" + key + "'"; }))
+            return false;
+        if (coat < 0 && (coat_rough >= 0 || coat_normals >= 0 || coat_tinted))
+            return fail("clearcoat_roughness, clearcoat_normal_map and clearcoat_color need 'clearcoat <weight>'");
+        double r0 = (ior - 1) / (ior + 1);
+        m.p[0] = r0 * r0;
+        m.tex[0] = base;
+        m.tex[1] = metallic;
+        m.tex[2] = rough;
+        m.tex[3] = use_normal_maps ? base_normals : -1;
+        if (measured) {
+            V3 f0, f_avg;
+            measured_fresnel(eta, k, f0, f_avg);
+            m.flags |= MYPBR_MATF_MEASURED;
+            for (int c = 0; c < 3; c++) {
+                m.p[4 + c] = eta[c];
+                m.p[7 + c] = k[c];
+                m.p[10 + c] = f_avg[c];
+            }
+        }
+        m.p[13] = m.p[14] = m.p[15] = 1;
+        if (coat >= 0) {
+            m.flags |= MYPBR_MATF_COAT;
+            m.tex[4] = coat;
+            m.tex[5] = coat_rough >= 0 ? coat_rough : add_texture_solid(V3(0, 0, 0));
+            m.tex[6] = use_normal_maps ? coat_normals : -1;
+            for (int c = 0; c < 3; c++)
+                m.p[13 + c] = coat_tint[c];
+            if (coat_tint.x != 1 || coat_tint.y != 1 || coat_tint.z != 1)
+                m.flags |= MYPBR_MATF_COAT_TINT;
+        }
+        return true;
+    }
+
+    bool volume_line(Words& w, mypbr_material& m, int&) {
+        V3 albedo;
+        double g = 0;
+        if (!w.triple(albedo))
+            return fail("expected 'material <name> volume <r> <g> <b> [g <anisotropy>]'");
+        if (w.more()) {  // one optional setting
+            std::string key;
+            w.word(key);
+            if (key != "g" || !w.number(g, between(-1, 1, true, true)))
+                return fail("expected 'material <name> volume <r> <g> <b> [g <anisotropy between -1 and 1>]'");
+        }
+        m.type = MYPBR_MAT_PHASE;
+        m.p[0] = albedo.x;
+        m.p[1] = albedo.y;
+        m.p[2] = albedo.z;
+        m.p[3] = g;
+        return true;
+    }
+
+    bool emissive_line(Words& w, mypbr_material& m, int&) {
+        const char* usage = "expected 'material <name> emissive <r> <g> <b> [spread <degrees, 0 to 180>]'";
+        V3 radiance;
+        double spread = 180;
+        if (!w.triple(radiance))
+            return fail(usage);
+        if (w.more()) {  // one optional setting
+            std::string key;
+            w.word(key);
+            if (key != "spread" || !w.number(spread, between(0, 180, true, false)))
+                return fail(usage);
+        }
+        m.type = MYPBR_MAT_DIFFUSE_LIGHT;
+        m.p[0] = radiance.x;
+        m.p[1] = radiance.y;
+        m.p[2] = radiance.z;
+        m.p[3] = spread;
+        double half = radians(spread) / 2;
+        m.p[4] = spread >= 180 ? kInf : std::tan(half);
+        // the cosine-weighted share a honeycomb of that spread lets through
+        // (material.h:600-608): 1 for a bare diffuser
+        if (half >= kPi / 2 - 1e-9) {
+            m.p[5] = 1;
+        } else {
+            double sn = std::sin(half), cs = std::cos(half);
+            m.p[5] = sn * sn - (half - sn * cs) * cs / sn;
+        }
+        return true;
+    }
+
+    bool material_line(Words& w) {
+        std::string name, type;
+        if (!w.word(name) || !w.word(type))
+            return fail("expected 'material <name> <type> <parameters...>'");
+        auto reader = material_readers().find(type);
+        if (reader == material_readers().end())
+            return fail("unknown material type '" + type + "'");
+        mypbr_material m = blank_material(0);
+        int normal_map = -1;
+        if (!(this->*(reader->second))(w, m, normal_map))
+            return false;
         if (normal_map >= 0 && use_normal_maps)
             m.normal_map = normal_map;
         materials[name] = add_material(m);
         return true;
     }
 
-    bool parse_texture(std::istringstream& in) {
+    bool texture_line(Words& w) {
         std::string name, type;
-        if (!(in >> name >> type))
+        if (!w.word(name) || !w.word(type))
             return fail("expected 'texture <name> <type> <parameters...>'");
         if (type == "solid") {
-            double r, g, b;
-            if (!(in >> r >> g >> b))
+            V3 c;
+            if (!w.triple(c))
                 return fail("expected 'texture <name> solid <r> <g> <b>'");
-            textures[name] = add_texture_solid(V3(r, g, b));
-        } else if (type == "checker") {
-            double scale, r0, g0, b0, r1, g1, b1;
-            if (!(in >> scale >> r0 >> g0 >> b0 >> r1 >> g1 >> b1) || scale <= 0)
+            textures[name] = add_texture_solid(c);
+            return true;
+        }
+        if (type == "checker") {
+            double scale;
+            V3 even, odd;
+            if (!w.number(scale, positive()) || !w.triple(even) || !w.triple(odd))
                 return fail("expected 'texture <name> checker <scale> <r g b> <r g b>'");
-            int even = add_texture_solid(V3(r0, g0, b0));
-            int odd = add_texture_solid(V3(r1, g1, b1));
             mypbr_texture t{};
             t.type = MYPBR_TEX_CHECKER;
-            t.a = even;
-            t.b = odd;
+            t.a = add_texture_solid(even);
+            t.b = add_texture_solid(odd);
             t.p[0] = 1.0 / scale;
             S.textures.push_back(t);
             textures[name] = int(S.textures.size()) - 1;
-        } else if (type == "image") {
-            std::string file, option;
-            if (!(in >> file))
-                return fail("expected 'texture <name> image <path> [linear]'");
-            bool linear = false;
-            if (in >> option) {
-                if (option != "linear")
-                    return fail("expected 'texture <name> image <path> [linear]'");
-                linear = true;
-            }
+            return true;
+        }
+        if (type == "image") {
+            const char* usage = "expected 'texture <name> image <path> [linear]'";
+            std::string file;
+            if (!w.word(file))
+                return fail(usage);
+            bool linear = w.peek() == "linear";
+            if (linear)
+                w.skip();
+            else if (w.more())
+                return fail(usage);
             if (file[0] != '/')
                 file = scene_dir + file;
-            std::string err;
-            int index = load_image(file, false, linear, err);
+            std::string why;
+            int index = load_image(file, false, linear, why);
             if (index < 0) {
                 if (image_unsupported) {
                     unsupported = true;
-                    return fail("image texture '" + file + "': " + err);
+                    return fail("image texture '" + file + "': " + why);
                 }
-                return fail("cannot load image '" + file + "'" + (err.empty() ? "" : ": " + err));
+                return fail("cannot load image '" + file + "'" + (why.empty() ? "" : ": " + why));
             }
             textures[name] = index;
-        } else {
-            return fail("unknown texture type '" + type + "'");
+            return true;
         }
-        return true;
+        return fail("unknown texture type '" + type + "'");
     }
 
     bool unsupported = false;
@@ -1753,55 +1833,47 @@ class Loader {
     }
 
     // vox <file> [quads] [emission <s>] [edges <w> [<r g b>]] [transforms] (scene.h:341-429)
-    bool parse_vox(std::istringstream& in) {
+    bool vox_line(Words& w) {
         const char* usage = "expected 'vox <file.vox> [quads] [emission <scale>] [edges <width> [<r g b>]] [transforms]'";
-        std::string file, token;
-        if (!(in >> file))
+        std::string file;
+        if (!w.word(file))
             return fail(usage);
         if (file[0] != '/')
             file = scene_dir + file;
         bool quads = false;
         double emission = 1, edge_width = 0;
         V3 edge_color(0, 0, 0);
-        std::vector<std::string> rest;
-        while (in >> token)
-            rest.push_back(token);
-        size_t k = 0;
-        for (; k < rest.size(); k++) {
-            if (rest[k] == "quads") {
+        // options, until a word that is none (a keyword with no value after it
+        // ends them too, and is then read as a material name)
+        for (bool options = true; options && w.more();) {
+            const std::string& key = w.peek();
+            if (key == "quads") {
                 quads = true;
-            } else if (rest[k] == "emission" && k + 1 < rest.size()) {
-                std::istringstream number(rest[++k]);
-                if (!(number >> emission) || emission < 0)
+                w.skip();
+            } else if ((key == "emission" || key == "edges") && w.left() >= 2) {
+                bool edges = key == "edges";
+                w.skip();
+                double x;
+                bool ok = word_is_number(w.peek(), x) &&
+                          (edges ? x > 0 && x < 0.5 : x >= 0);
+                if (!ok)
                     return fail(usage);
-            } else if (rest[k] == "edges" && k + 1 < rest.size()) {
-                std::istringstream number(rest[++k]);
-                if (!(number >> edge_width) || edge_width <= 0 || edge_width >= 0.5)
-                    return fail(usage);
-                if (k + 3 < rest.size()) {
-                    std::istringstream rgb(rest[k + 1] + ' ' + rest[k + 2] + ' ' + rest[k + 3]);
-                    V3 c;
-                    if (rgb >> c.x >> c.y >> c.z) {
-                        edge_color = c;
-                        k += 3;
-                    }
-                }
+                w.skip();
+                (edges ? edge_width : emission) = x;
+                if (edges && w.left() >= 3)
+                    w.triple(edge_color);  // an optional color; left for the tail if it is not one
             } else {
-                break;
+                options = false;
             }
         }
-        std::string tail_text;
-        for (; k < rest.size(); k++)
-            tail_text += rest[k] + ' ';
-        std::istringstream tail(tail_text);
-        int mat;
-        Xf xform;
-        bool transformed;
+        Placement at;
         error.clear();
-        if (!read_tail(tail, mat, xform, transformed))
+        if (!read_placement(w, at))
             return fail(error);
-        if (mat != default_material)
+        if (at.material != default_material)
             return fail("vox models take their materials from the file's palette");
+        const Xf& xform = at.xform;
+        const bool transformed = at.moved;
         VoxFile vox;
         std::string err;
         if (!read_vox(file, vox, err))
@@ -1909,391 +1981,489 @@ class Loader {
         return true;
     }
 
-    bool parse_line(std::istringstream& in, const std::string& keyword) {
-        auto& cam = S.camera;
-        auto& opts = S.opts;
-        if (keyword == "image_width") {
-            if (!(in >> cam.image_width) || cam.image_width < 1)
-                return fail("expected 'image_width <positive integer>'");
-        } else if (keyword == "aspect_ratio") {
-            double num, den = 1.0;
-            if (!(in >> num))
-                return fail("expected 'aspect_ratio <w>/<h>' or 'aspect_ratio <number>'");
-            if (in.peek() == '/') {
-                in.get();
-                if (!(in >> den))
-                    return fail("expected 'aspect_ratio <w>/<h>'");
-            }
-            if (num <= 0 || den <= 0)
-                return fail("aspect_ratio must be positive");
-            cam.aspect_ratio = num / den;
-        } else if (keyword == "samples_per_pixel") {
-            if (!(in >> opts.samples_per_pixel) || opts.samples_per_pixel < 1)
-                return fail("expected 'samples_per_pixel <positive integer>'");
-        } else if (keyword == "max_depth") {
-            if (!(in >> opts.max_depth) || opts.max_depth < 1)
-                return fail("expected 'max_depth <positive integer>'");
-        } else if (keyword == "camera") {
-            std::string key;
-            while (in >> key) {
-                bool ok = true;
-                if (key == "lookfrom")
-                    ok = bool(in >> cam.lookfrom[0] >> cam.lookfrom[1] >> cam.lookfrom[2]);
-                else if (key == "lookat")
-                    ok = bool(in >> cam.lookat[0] >> cam.lookat[1] >> cam.lookat[2]);
-                else if (key == "vup")
-                    ok = bool(in >> cam.vup[0] >> cam.vup[1] >> cam.vup[2]);
-                else if (key == "vfov")
-                    ok = bool(in >> cam.vfov) && cam.vfov > 0 && cam.vfov < 180;
-                else if (key == "aperture")
-                    ok = bool(in >> cam.defocus_angle) && cam.defocus_angle >= 0;
-                else if (key == "focus")
-                    ok = bool(in >> cam.focus_dist) && cam.focus_dist > 0;
-                else if (key == "ortho")
-                    ok = bool(in >> cam.ortho_height) && cam.ortho_height >= 0;
-                else if (key == "blades")
-                    ok = bool(in >> cam.blades) && (cam.blades == 0 || cam.blades >= 3);
-                else if (key == "blade_rotation")
-                    ok = bool(in >> cam.blade_rotation);
-                else
-                    return fail("unknown camera setting '" + key + "'");
-                if (!ok)
-                    return fail("bad value for camera setting '" + key + "'");
-            }
-        } else if (keyword == "vfov") {
-            if (!(in >> cam.vfov) || cam.vfov <= 0 || cam.vfov >= 180)
-                return fail("expected 'vfov <degrees between 0 and 180>'");
-        } else if (keyword == "aperture") {
-            if (!(in >> cam.defocus_angle) || cam.defocus_angle < 0)
-                return fail("expected 'aperture <defocus angle in degrees>'");
-        } else if (keyword == "focus") {
-            if (!(in >> cam.focus_dist) || cam.focus_dist <= 0)
-                return fail("expected 'focus <positive distance>'");
-        } else if (keyword == "background") {
-            double r, g, b;
-            if (!(in >> r >> g >> b))
-                return fail("expected 'background <r> <g> <b>'");
-            S.use_sky = false;
-            S.background = V3(r, g, b);
-        } else if (keyword == "light_selection") {
-            std::string mode;
-            if (!(in >> mode) || (mode != "power" && mode != "uniform"))
-                return fail("expected 'light_selection power|uniform'");
-            power_selection = mode == "power";
-        } else if (keyword == "environment") {
-            std::string file, key;
-            double intensity = 1, rotation = 0;
-            const char* usage = "expected 'environment <file.hdr> [intensity <s>] [rotate <degrees>]'";
-            if (!(in >> file))
-                return fail(usage);
-            while (in >> key) {
-                bool ok = (key == "intensity" && in >> intensity && intensity >= 0) ||
-                          (key == "rotate" && in >> rotation);
-                if (!ok)
-                    return fail(usage);
-            }
-            if (file[0] != '/')
-                file = scene_dir + file;
-            int w, h;
-            std::vector<float> rgb;
-            std::string err;
-            if (!read_hdr(file, w, h, rgb, err))
-                return fail("cannot load environment map '" + file + "'");
-            if (has_environment)
-                return fail("only one environment is allowed");
-            set_environment(w, h, std::move(rgb), intensity, rotation / 360);
-        } else if (keyword == "sun") {
-            const char* usage = "expected 'sun elevation <deg> azimuth <deg> [intensity <E>] [color <r g b>] "
-                                "[angle <deg>] [disk on|off]' or 'sun off'";
-            std::string key;
-            sun_on = true;
-            while (in >> key) {
-                bool ok = true;
-                if (key == "off")
-                    sun_on = false;
-                else if (key == "elevation")
-                    ok = bool(in >> sun_elevation) && sun_elevation >= -90 && sun_elevation <= 90;
-                else if (key == "azimuth")
-                    ok = bool(in >> sun_azimuth);
-                else if (key == "intensity")
-                    ok = bool(in >> sun_intensity) && sun_intensity >= 0;
-                else if (key == "color")
-                    ok = bool(in >> sun_tint.x >> sun_tint.y >> sun_tint.z);
-                else if (key == "angle")
-                    ok = bool(in >> sun_angle) && sun_angle > 0 && sun_angle < 90;
-                else if (key == "disk") {
-                    std::string value;
-                    ok = bool(in >> value) && (value == "on" || value == "off");
-                    sun_disk = value == "on";
-                } else
-                    ok = false;
-                if (!ok)
-                    return fail(usage);
-            }
-        } else if (keyword == "sky") {
-            std::string type;
-            if (!(in >> type))
-                return fail("expected 'sky uniform <r g b>', 'sky atmosphere [...]' or 'sky gradient'");
-            if (type == "uniform") {
-                if (!(in >> sky_radiance.x >> sky_radiance.y >> sky_radiance.z))
-                    return fail("expected 'sky uniform <r g b>'");
-                sky_uniform = true;
-                S.use_sky = true;
-                sky_atmosphere = false;
-            } else if (type == "atmosphere") {  // scene.h:574-586
-                const char* usage =
-                    "expected 'sky atmosphere [rayleigh <x>] [mie <x>] [mie_g <g>] [ozone <x>] [intensity <s>]'";
-                std::string key;
-                while (in >> key) {
-                    bool ok = (key == "rayleigh" && in >> air.rayleigh && air.rayleigh >= 0) ||
-                              (key == "mie" && in >> air.mie && air.mie >= 0) ||
-                              (key == "mie_g" && in >> air.mie_g && air.mie_g > -1 && air.mie_g < 1) ||
-                              (key == "ozone" && in >> air.ozone && air.ozone >= 0) ||
-                              (key == "intensity" && in >> air.intensity && air.intensity >= 0);
-                    if (!ok)
-                        return fail(usage);
-                }
-                sky_atmosphere = true;
-                sky_uniform = false;
-                S.use_sky = true;
-            } else if (type == "gradient") {
-                sky_uniform = false;
-                sky_atmosphere = false;
-                S.use_sky = true;
-            } else {
-                return fail("unknown sky type '" + type + "' (expected uniform, atmosphere or gradient)");
-            }
-        } else if (keyword == "ground") {
-            std::string key;
-            ground = true;
-            while (in >> key) {
-                if (key == "off") {
-                    ground = false;
-                } else if (key == "height") {
-                    if (!(in >> ground_height))
-                        return fail("expected 'ground [height <y>] [material]'");
-                } else {
-                    auto it = materials.find(key);
-                    if (it == materials.end())
-                        return fail("unknown material '" + key + "'");
-                    ground_material = it->second;
-                }
-            }
-        } else if (keyword == "style") {
-            std::string name;
-            if (!(in >> name) || (name != "voxel" && name != "classic"))
-                return fail("expected 'style voxel' or 'style classic'");
-            bool voxel = name == "voxel";
-            sun_on = voxel;
-            sun_elevation = voxel ? 50 : 45;
-            sun_azimuth = voxel ? 50 : 45;
-            sun_intensity = voxel ? 4 : 3;
-            sun_angle = voxel ? 3 : 4;
-            sun_tint = V3(1, 1, 1);
-            sun_disk = true;
-            sky_uniform = false;
-            sky_atmosphere = voxel;
-            air = mypbr_sky::Settings();
-            S.use_sky = true;
-            ground = voxel;
-            ground_material = voxel ? lambertian(V3(0.3, 0.3, 0.3)) : default_material;
-            opts.max_diffuse = voxel ? 2 : 0;
-            opts.max_specular = voxel ? 5 : 0;
-            opts.max_scatter = voxel ? 5 : 0;
-            opts.transparent_shadows = voxel;
-        } else if (keyword == "bounces") {
-            const char* usage = "expected 'bounces [diffuse <n>] [specular <n>] [scatter <n>]'";
-            std::string key;
-            while (in >> key) {
-                bool ok = (key == "diffuse" && in >> opts.max_diffuse && opts.max_diffuse >= 0) ||
-                          (key == "specular" && in >> opts.max_specular && opts.max_specular >= 0) ||
-                          (key == "scatter" && in >> opts.max_scatter && opts.max_scatter >= 0);
-                if (!ok)
-                    return fail(usage);
-            }
-        } else if (keyword == "transparent_shadows") {
-            std::string value;
-            if (!(in >> value) || (value != "on" && value != "off"))
-                return fail("expected 'transparent_shadows on|off'");
-            opts.transparent_shadows = value == "on";
-        } else if (keyword == "height_fog") {
-            double density, scale, base = 0;
-            std::string name, key;
-            const char* usage = "expected 'height_fog <density> <scale height> <volume material> [base <y>]'";
-            if (!(in >> density >> scale >> name) || density <= 0 || scale <= 0)
-                return fail(usage);
-            if (in >> key && (key != "base" || !(in >> base)))
-                return fail(usage);
-            auto it = materials.find(name);
-            if (it == materials.end() || S.materials[it->second].type != MYPBR_MAT_PHASE)
-                return fail("expected a volume material, got '" + name + "'");
-            mypbr_unbounded u{};
-            u.kind = MYPBR_UNBOUNDED_HEIGHT_FOG;
-            u.material = it->second;
-            u.height = base;
-            u.density = density;
-            u.scale_height = scale;
-            S.unbounded.push_back(u);
-        } else if (keyword == "bloom") {
-            // Display settings: they change written images, not the radiance frame
-            double strength;
-            if (!(in >> strength) || strength < 0)
-                return fail("expected 'bloom <strength> [threshold <radiance>] [radius <fraction of width>]'");
-            std::string key;
-            double x;
-            while (in >> key) {
-                if (!((key == "threshold" && in >> x && x >= 0) || (key == "radius" && in >> x && x > 0)))
-                    return fail("expected 'bloom <strength> [threshold <radiance>] [radius <fraction of width>]'");
-            }
-        } else if (keyword == "vignette") {
-            double v;
-            if (!(in >> v) || v < 0)
-                return fail("expected 'vignette <strength>'");
-        } else if (keyword == "exposure") {
-            double v;
-            if (!(in >> v))
-                return fail("expected 'exposure <stops>'");
-        } else if (keyword == "tonemap") {
-            std::string name;
-            if (!(in >> name) || (name != "none" && name != "reinhard" && name != "aces"))
-                return fail("expected 'tonemap none|reinhard|aces'");
-        } else if (keyword == "normal_maps") {
-            std::string state;
-            if (!(in >> state) || (state != "on" && state != "off"))
-                return fail("expected 'normal_maps on|off'");
-            use_normal_maps = state == "on";
-        } else if (keyword == "texture") {
-            return parse_texture(in);
-        } else if (keyword == "material") {
-            return parse_material(in);
-        } else if (keyword == "sphere" || keyword == "quad" || keyword == "box") {
-            int mat;
-            Xf xform;
-            bool transformed;
-            error.clear();
-            if (keyword == "sphere") {
-                double x, y, z, r;
-                if (!(in >> x >> y >> z >> r) || r == 0)
-                    return fail("expected 'sphere <x> <y> <z> <non-zero radius> [material] [transforms]'");
-                if (!read_tail(in, mat, xform, transformed))
-                    return fail(error);
-                if (!add_sphere(V3(x, y, z), r, mat, xform, transformed))
-                    return fail(error);
-            } else if (keyword == "quad") {
-                V3 q, u, v;
-                if (!(in >> q.x >> q.y >> q.z >> u.x >> u.y >> u.z >> v.x >> v.y >> v.z))
-                    return fail("expected 'quad <Qx Qy Qz> <ux uy uz> <vx vy vz> [material] [transforms]'");
-                if (cross(u, v).near_zero())
-                    return fail("quad edges must not be parallel");
-                if (!read_tail(in, mat, xform, transformed))
-                    return fail(error);
-                if (!add_quad(q, u, v, mat, xform, transformed))
-                    return fail(error);
-            } else {
-                V3 a, b;
-                if (!(in >> a.x >> a.y >> a.z >> b.x >> b.y >> b.z))
-                    return fail("expected 'box <x0 y0 z0> <x1 y1 z1> [material] [transforms]'");
-                if (!read_tail(in, mat, xform, transformed))
-                    return fail(error);
-                if (!add_box(a, b, mat, xform, transformed))
-                    return fail(error);
-            }
-        } else if (keyword == "medium") {
-            double density;
-            std::string shape;
-            if (!(in >> density >> shape) || density <= 0)
-                return fail("expected 'medium <positive density> sphere|box <...> <material> [transforms]'");
-            V3 a, b;
-            bool sphere = shape == "sphere";
-            if (sphere) {
-                double r;
-                if (!(in >> a.x >> a.y >> a.z >> r) || r <= 0)
-                    return fail("expected 'medium <density> sphere <x> <y> <z> <positive radius> <material>'");
-                b = V3(r, 0, 0);
-            } else if (shape == "box") {
-                if (!(in >> a.x >> a.y >> a.z >> b.x >> b.y >> b.z))
-                    return fail("expected 'medium <density> box <x0 y0 z0> <x1 y1 z1> <material>'");
-            } else {
-                return fail("a medium's boundary must be 'sphere' or 'box'");
-            }
-            int mat;
-            Xf xform;
-            bool transformed;
-            error.clear();
-            if (!read_tail(in, mat, xform, transformed))
-                return fail(error);
-            if (S.materials[mat].type != MYPBR_MAT_PHASE)
-                return fail("a medium needs a volume material");
-            add_medium(density, sphere, a, b, mat, xform, transformed);
-        } else if (keyword == "fog") {
-            std::string name;
-            if (!(in >> fog_density >> name) || fog_density <= 0)
-                return fail("expected 'fog <positive density> <volume material>'");
-            auto it = materials.find(name);
-            if (it == materials.end() || S.materials[it->second].type != MYPBR_MAT_PHASE)
-                return fail("expected a volume material, got '" + name + "'");
-            fog_material = it->second;
-        } else if (keyword == "mesh") {
-            std::string file;
-            if (!(in >> file))
-                return fail("expected 'mesh <file.obj> [material] [transforms]'");
-            if (file[0] != '/')
-                file = scene_dir + file;
-            std::string rest, first;
-            std::getline(in, rest);
-            std::istringstream peek(rest);
-            bool smooth = (peek >> first) && first == "smooth";
-            std::istringstream tail(smooth ? rest.substr(rest.find("smooth") + 6) : rest);
-            auto ends_with = [&](const char* suf) {
-                size_t n = std::strlen(suf);
-                return file.size() >= n && file.compare(file.size() - n, n, suf) == 0;
-            };
-            // then any number of "replace <file material> <scene material>" (glTF)
-            std::map<std::string, int> replace;
-            std::streampos mark = tail.tellg();
-            std::string token;
-            while (tail >> token && token == "replace") {
-                std::string from, to;
-                if (!(tail >> from >> to))
-                    return fail("expected 'replace <material in the file> <scene material>'");
-                auto it = materials.find(to);
-                if (it == materials.end())
-                    return fail("unknown material '" + to + "'");
-                replace[from] = it->second;
-                mark = tail.tellg();
-            }
-            tail.clear();
-            tail.seekg(mark);
-            int mat;
-            Xf xform;
-            bool transformed;
-            error.clear();
-            if (!read_tail(tail, mat, xform, transformed))
-                return fail(error);
-            if (!replace.empty() && mat != default_material)
-                return fail("'replace' and a material for the whole mesh can't be used together");
-            bool gltf = ends_with(".gltf") || ends_with(".glb");
-            if (!gltf && !replace.empty())
-                return fail("'replace' is for glTF files (OBJ files take scene materials by usemtl name)");
-            // glTF files bring their own materials: one named on the line replaces them all
-            if (gltf ? !add_gltf(file, mat == default_material ? -1 : mat, replace, xform, transformed)
-                     : !add_obj(file, smooth, mat, xform, transformed))
-                return fail(error);
-            std::string extra;
-            if (tail >> extra)
-                return fail("unexpected value '" + extra + "'");
-        } else if (keyword == "vox") {
-            return parse_vox(in);
-        } else if (keyword == "cyclorama" || keyword == "softbox") {
-            unsupported = true;
-            return fail("'" + keyword + "' is not supported by this backend");
-        } else {
+    // ------------------------------------------------------ keywords
+    //
+    // Every keyword of the .scene language (scene.h:44-243) has a handler in
+    // one table; a handler reads its words and says false (with the message
+    // in `error`) when they are wrong. Whatever a handler leaves unread is an
+    // error too ("unexpected value").
+
+    using LineHandler = bool (Loader::*)(Words&);
+    static const std::map<std::string, LineHandler>& keywords() {
+        static const std::map<std::string, LineHandler> table = {
+            {"image_width", &Loader::image_width_line},
+            {"aspect_ratio", &Loader::aspect_ratio_line},
+            {"samples_per_pixel", &Loader::samples_line},
+            {"max_depth", &Loader::max_depth_line},
+            {"camera", &Loader::camera_line},
+            {"vfov", &Loader::vfov_line},
+            {"aperture", &Loader::aperture_line},
+            {"focus", &Loader::focus_line},
+            {"background", &Loader::background_line},
+            {"light_selection", &Loader::light_selection_line},
+            {"environment", &Loader::environment_line},
+            {"sun", &Loader::sun_line},
+            {"sky", &Loader::sky_line},
+            {"ground", &Loader::ground_line},
+            {"style", &Loader::style_line},
+            {"bounces", &Loader::bounces_line},
+            {"transparent_shadows", &Loader::transparent_shadows_line},
+            {"height_fog", &Loader::height_fog_line},
+            {"bloom", &Loader::bloom_line},
+            {"vignette", &Loader::vignette_line},
+            {"exposure", &Loader::exposure_line},
+            {"tonemap", &Loader::tonemap_line},
+            {"normal_maps", &Loader::normal_maps_line},
+            {"texture", &Loader::texture_line},
+            {"material", &Loader::material_line},
+            {"sphere", &Loader::sphere_line},
+            {"quad", &Loader::quad_line},
+            {"box", &Loader::box_line},
+            {"medium", &Loader::medium_line},
+            {"fog", &Loader::fog_line},
+            {"mesh", &Loader::mesh_line},
+            {"vox", &Loader::vox_line},
+            {"cyclorama", &Loader::studio_line},
+            {"softbox", &Loader::studio_line},
+        };
+        return table;
+    }
+
+    bool parse_line(Words& w, const std::string& keyword) {
+        auto handler = keywords().find(keyword);
+        if (handler == keywords().end())
             return fail("unknown keyword '" + keyword + "'");
-        }
-        std::string extra;
-        if (in >> extra)
-            return fail("unexpected value '" + extra + "'");
+        current_keyword = keyword;
+        if (!(this->*(handler->second))(w))
+            return false;
+        if (w.more())
+            return fail("unexpected value '" + w.peek() + "'");
         return true;
+    }
+    std::string current_keyword;
+
+    // One word that must be one of `choices`.
+    static bool one_of(Words& w, std::initializer_list<const char*> choices, std::string& out) {
+        if (!w.more())
+            return false;
+        for (const char* c : choices)
+            if (w.peek() == c) {
+                w.word(out);
+                return true;
+            }
+        return false;
+    }
+    static bool on_off(Words& w, bool& state) {
+        std::string v;
+        if (!one_of(w, {"on", "off"}, v))
+            return false;
+        state = v == "on";
+        return true;
+    }
+    static bool positive_integer(Words& w, int& x) {
+        int v;
+        if (!w.integer(v) || v < 1)
+            return false;
+        x = v;
+        return true;
+    }
+
+    bool image_width_line(Words& w) {
+        return positive_integer(w, S.camera.image_width) || fail("expected 'image_width <positive integer>'");
+    }
+    bool samples_line(Words& w) {
+        return positive_integer(w, S.opts.samples_per_pixel) || fail("expected 'samples_per_pixel <positive integer>'");
+    }
+    bool max_depth_line(Words& w) {
+        return positive_integer(w, S.opts.max_depth) || fail("expected 'max_depth <positive integer>'");
+    }
+
+    // "16/9" or a plain number
+    bool aspect_ratio_line(Words& w) {
+        std::string word;
+        if (!w.word(word))
+            return fail("expected 'aspect_ratio <w>/<h>' or 'aspect_ratio <number>'");
+        size_t slash = word.find('/');
+        double num, den = 1;
+        if (!word_is_number(word.substr(0, slash), num))
+            return fail("expected 'aspect_ratio <w>/<h>' or 'aspect_ratio <number>'");
+        if (slash != std::string::npos && !word_is_number(word.substr(slash + 1), den))
+            return fail("expected 'aspect_ratio <w>/<h>'");
+        if (num <= 0 || den <= 0)
+            return fail("aspect_ratio must be positive");
+        S.camera.aspect_ratio = num / den;
+        return true;
+    }
+
+    bool camera_line(Words& w) {
+        auto& cam = S.camera;
+        return settings(
+            w,
+            {{"lookfrom", [&](Words& v) { return v.triple(cam.lookfrom); }},
+             {"lookat", [&](Words& v) { return v.triple(cam.lookat); }},
+             {"vup", [&](Words& v) { return v.triple(cam.vup); }},
+             {"vfov", [&](Words& v) { return v.number(cam.vfov, between(0, 180, true, true)); }},
+             {"aperture", [&](Words& v) { return v.number(cam.defocus_angle, non_negative()); }},
+             {"focus", [&](Words& v) { return v.number(cam.focus_dist, positive()); }},
+             {"ortho", [&](Words& v) { return v.number(cam.ortho_height, non_negative()); }},
+             {"blades",
+              [&](Words& v) {
+                  int n;
+                  if (!v.integer(n) || (n != 0 && n < 3))
+                      return false;
+                  cam.blades = n;
+                  return true;
+              }},
+             {"blade_rotation", [&](Words& v) { return v.number(cam.blade_rotation); }}},
+            [](const std::string& key) { return "unknown camera setting '" + key + "'"; },
+            [](const std::string& key) { return "bad value for camera setting '" + key + "'"; });
+    }
+
+    bool vfov_line(Words& w) {
+        return w.number(S.camera.vfov, between(0, 180, true, true)) ||
+               fail("expected 'vfov <degrees between 0 and 180>'");
+    }
+    bool aperture_line(Words& w) {
+        return w.number(S.camera.defocus_angle, non_negative()) ||
+               fail("expected 'aperture <defocus angle in degrees>'");
+    }
+    bool focus_line(Words& w) {
+        return w.number(S.camera.focus_dist, positive()) || fail("expected 'focus <positive distance>'");
+    }
+    bool background_line(Words& w) {
+        V3 c;
+        if (!w.triple(c))
+            return fail("expected 'background <r> <g> <b>'");
+        S.use_sky = false;
+        S.background = c;
+        return true;
+    }
+    bool light_selection_line(Words& w) {
+        std::string mode;
+        if (!one_of(w, {"power", "uniform"}, mode))
+            return fail("expected 'light_selection power|uniform'");
+        power_selection = mode == "power";
+        return true;
+    }
+
+    bool environment_line(Words& w) {
+        const std::string usage = "expected 'environment <file.hdr> [intensity <s>] [rotate <degrees>]'";
+        std::string file;
+        double intensity = 1, rotation = 0;
+        if (!w.word(file))
+            return fail(usage);
+        auto says = [&](const std::string&) { return usage; };
+        if (!settings(w,
+                      {{"intensity", [&](Words& v) { return v.number(intensity, non_negative()); }},
+                       {"rotate", [&](Words& v) { return v.number(rotation); }}},
+                      says, says))
+            return false;
+        if (file[0] != '/')
+            file = scene_dir + file;
+        int width, height;
+        std::vector<float> rgb;
+        std::string why;
+        if (!read_hdr(file, width, height, rgb, why))
+            return fail("cannot load environment map '" + file + "'");
+        if (has_environment)
+            return fail("only one environment is allowed");
+        set_environment(width, height, std::move(rgb), intensity, rotation / 360);
+        return true;
+    }
+
+    bool sun_line(Words& w) {
+        const std::string usage = "expected 'sun elevation <deg> azimuth <deg> [intensity <E>] [color <r g b>] "
+                                  "[angle <deg>] [disk on|off]' or 'sun off'";
+        auto says = [&](const std::string&) { return usage; };
+        sun_on = true;
+        return settings(w,
+                        {{"off", [&](Words&) { return !(sun_on = false); }},
+                         {"elevation", [&](Words& v) { return v.number(sun_elevation, between(-90, 90, false, false)); }},
+                         {"azimuth", [&](Words& v) { return v.number(sun_azimuth); }},
+                         {"intensity", [&](Words& v) { return v.number(sun_intensity, non_negative()); }},
+                         {"color", [&](Words& v) { return v.triple(sun_tint); }},
+                         {"angle", [&](Words& v) { return v.number(sun_angle, between(0, 90, true, true)); }},
+                         {"disk", [&](Words& v) { return on_off(v, sun_disk); }}},
+                        says, says);
+    }
+
+    bool sky_line(Words& w) {
+        std::string type;
+        if (!w.word(type))
+            return fail("expected 'sky uniform <r g b>', 'sky atmosphere [...]' or 'sky gradient'");
+        if (type == "uniform") {
+            if (!w.triple(sky_radiance))
+                return fail("expected 'sky uniform <r g b>'");
+            sky_uniform = true;
+            sky_atmosphere = false;
+        } else if (type == "atmosphere") {  // scene.h:574-586
+            const std::string usage =
+                "expected 'sky atmosphere [rayleigh <x>] [mie <x>] [mie_g <g>] [ozone <x>] [intensity <s>]'";
+            auto says = [&](const std::string&) { return usage; };
+            if (!settings(w,
+                          {{"rayleigh", [&](Words& v) { return v.number(air.rayleigh, non_negative()); }},
+                           {"mie", [&](Words& v) { return v.number(air.mie, non_negative()); }},
+                           {"mie_g", [&](Words& v) { return v.number(air.mie_g, between(-1, 1, true, true)); }},
+                           {"ozone", [&](Words& v) { return v.number(air.ozone, non_negative()); }},
+                           {"intensity", [&](Words& v) { return v.number(air.intensity, non_negative()); }}},
+                          says, says))
+                return false;
+            sky_atmosphere = true;
+            sky_uniform = false;
+        } else if (type == "gradient") {
+            sky_uniform = false;
+            sky_atmosphere = false;
+        } else {
+            return fail("unknown sky type '" + type + "' (expected uniform, atmosphere or gradient)");
+        }
+        S.use_sky = true;
+        return true;
+    }
+
+    // "ground [off] [height <y>] [material]", in any order
+    bool ground_line(Words& w) {
+        ground = true;
+        std::string key;
+        while (w.word(key)) {
+            if (key == "off") {
+                ground = false;
+            } else if (key == "height") {
+                if (!w.number(ground_height))
+                    return fail("expected 'ground [height <y>] [material]'");
+            } else {
+                auto found = materials.find(key);
+                if (found == materials.end())
+                    return fail("unknown material '" + key + "'");
+                ground_material = found->second;
+            }
+        }
+        return true;
+    }
+
+    // A preset of the lines it stands for (scene.h:612-640)
+    bool style_line(Words& w) {
+        std::string name;
+        if (!one_of(w, {"voxel", "classic"}, name))
+            return fail("expected 'style voxel' or 'style classic'");
+        const bool voxel = name == "voxel";
+        sun_on = voxel;
+        sun_elevation = voxel ? 50 : 45;
+        sun_azimuth = voxel ? 50 : 45;
+        sun_intensity = voxel ? 4 : 3;
+        sun_angle = voxel ? 3 : 4;
+        sun_tint = V3(1, 1, 1);
+        sun_disk = true;
+        sky_uniform = false;
+        sky_atmosphere = voxel;
+        air = mypbr_sky::Settings();
+        S.use_sky = true;
+        ground = voxel;
+        ground_material = voxel ? lambertian(V3(0.3, 0.3, 0.3)) : default_material;
+        S.opts.max_diffuse = voxel ? 2 : 0;
+        S.opts.max_specular = voxel ? 5 : 0;
+        S.opts.max_scatter = voxel ? 5 : 0;
+        S.opts.transparent_shadows = voxel;
+        return true;
+    }
+
+    bool bounces_line(Words& w) {
+        const std::string usage = "expected 'bounces [diffuse <n>] [specular <n>] [scatter <n>]'";
+        auto says = [&](const std::string&) { return usage; };
+        auto cap = [](int& field) {
+            return [&field](Words& v) {
+                int n;
+                if (!v.integer(n) || n < 0)
+                    return false;
+                field = n;
+                return true;
+            };
+        };
+        return settings(w,
+                        {{"diffuse", cap(S.opts.max_diffuse)},
+                         {"specular", cap(S.opts.max_specular)},
+                         {"scatter", cap(S.opts.max_scatter)}},
+                        says, says);
+    }
+
+    bool transparent_shadows_line(Words& w) {
+        bool on;
+        if (!on_off(w, on))
+            return fail("expected 'transparent_shadows on|off'");
+        S.opts.transparent_shadows = on;
+        return true;
+    }
+    bool normal_maps_line(Words& w) {
+        return on_off(w, use_normal_maps) || fail("expected 'normal_maps on|off'");
+    }
+
+    // A volume material by name, for fog lines
+    bool volume_material(const std::string& name, int& mat) {
+        auto found = materials.find(name);
+        if (found == materials.end() || S.materials[found->second].type != MYPBR_MAT_PHASE)
+            return fail("expected a volume material, got '" + name + "'");
+        mat = found->second;
+        return true;
+    }
+
+    bool height_fog_line(Words& w) {
+        const char* usage = "expected 'height_fog <density> <scale height> <volume material> [base <y>]'";
+        double density, scale, base = 0;
+        std::string name;
+        if (!w.number(density, positive()) || !w.number(scale, positive()) || !w.word(name))
+            return fail(usage);
+        if (w.more()) {  // one optional setting
+            std::string key;
+            w.word(key);
+            if (key != "base" || !w.number(base))
+                return fail(usage);
+        }
+        mypbr_unbounded u{};
+        if (!volume_material(name, u.material))
+            return false;
+        u.kind = MYPBR_UNBOUNDED_HEIGHT_FOG;
+        u.height = base;
+        u.density = density;
+        u.scale_height = scale;
+        S.unbounded.push_back(u);
+        return true;
+    }
+
+    bool fog_line(Words& w) {
+        std::string name;
+        if (!w.number(fog_density, positive()) || !w.word(name))
+            return fail("expected 'fog <positive density> <volume material>'");
+        return volume_material(name, fog_material);
+    }
+
+    // Display settings: they change written images, not the radiance
+    // frame, so they are checked and not kept.
+    bool bloom_line(Words& w) {
+        const std::string usage = "expected 'bloom <strength> [threshold <radiance>] [radius <fraction of width>]'";
+        double x;
+        if (!w.number(x, non_negative()))
+            return fail(usage);
+        auto says = [&](const std::string&) { return usage; };
+        return settings(w,
+                        {{"threshold", [&](Words& v) { return v.number(x, non_negative()); }},
+                         {"radius", [&](Words& v) { return v.number(x, positive()); }}},
+                        says, says);
+    }
+    bool vignette_line(Words& w) {
+        double v;
+        return w.number(v, non_negative()) || fail("expected 'vignette <strength>'");
+    }
+    bool exposure_line(Words& w) {
+        double v;
+        return w.number(v) || fail("expected 'exposure <stops>'");
+    }
+    bool tonemap_line(Words& w) {
+        std::string op;
+        return one_of(w, {"none", "reinhard", "aces"}, op) || fail("expected 'tonemap none|reinhard|aces'");
+    }
+
+    bool studio_line(Words&) {
+        unsupported = true;
+        return fail("'" + current_keyword + "' is not supported by this backend");
+    }
+
+    // ------------------------------------------------------ objects
+
+    bool sphere_line(Words& w) {
+        V3 c;
+        double r;
+        if (!w.triple(c) || !w.number(r) || r == 0)
+            return fail("expected 'sphere <x> <y> <z> <non-zero radius> [material] [transforms]'");
+        Placement at;
+        error.clear();
+        return (read_placement(w, at) && add_sphere(c, r, at.material, at.xform, at.moved)) || fail(error);
+    }
+
+    bool quad_line(Words& w) {
+        V3 q, u, v;
+        if (!w.triple(q) || !w.triple(u) || !w.triple(v))
+            return fail("expected 'quad <Qx Qy Qz> <ux uy uz> <vx vy vz> [material] [transforms]'");
+        if (cross(u, v).near_zero())
+            return fail("quad edges must not be parallel");
+        Placement at;
+        error.clear();
+        return (read_placement(w, at) && add_quad(q, u, v, at.material, at.xform, at.moved)) || fail(error);
+    }
+
+    bool box_line(Words& w) {
+        V3 a, b;
+        if (!w.triple(a) || !w.triple(b))
+            return fail("expected 'box <x0 y0 z0> <x1 y1 z1> [material] [transforms]'");
+        Placement at;
+        error.clear();
+        return (read_placement(w, at) && add_box(a, b, at.material, at.xform, at.moved)) || fail(error);
+    }
+
+    bool medium_line(Words& w) {
+        double density;
+        std::string shape;
+        if (!w.number(density, positive()) || !w.word(shape))
+            return fail("expected 'medium <positive density> sphere|box <...> <material> [transforms]'");
+        V3 a, b;
+        const bool sphere = shape == "sphere";
+        if (sphere) {
+            double r;
+            if (!w.triple(a) || !w.number(r, positive()))
+                return fail("expected 'medium <density> sphere <x> <y> <z> <positive radius> <material>'");
+            b = V3(r, 0, 0);
+        } else if (shape == "box") {
+            if (!w.triple(a) || !w.triple(b))
+                return fail("expected 'medium <density> box <x0 y0 z0> <x1 y1 z1> <material>'");
+        } else {
+            return fail("a medium's boundary must be 'sphere' or 'box'");
+        }
+        Placement at;
+        error.clear();
+        if (!read_placement(w, at))
+            return fail(error);
+        if (S.materials[at.material].type != MYPBR_MAT_PHASE)
+            return fail("a medium needs a volume material");
+        add_medium(density, sphere, a, b, at.material, at.xform, at.moved);
+        return true;
+    }
+
+    // "mesh <file> [smooth] [replace <file material> <scene material>]...
+    // [material] [transforms]": OBJ, or glTF (.gltf / .glb) with its own
+    // materials, which one named on the line replaces all of.
+    bool mesh_line(Words& w) {
+        std::string file;
+        if (!w.word(file))
+            return fail("expected 'mesh <file.obj> [material] [transforms]'");
+        if (file[0] != '/')
+            file = scene_dir + file;
+        const bool smooth = w.peek() == "smooth";
+        if (smooth)
+            w.skip();
+        std::map<std::string, int> replace;
+        while (w.peek() == "replace") {
+            w.skip();
+            std::string from, to;
+            if (!w.word(from) || !w.word(to))
+                return fail("expected 'replace <material in the file> <scene material>'");
+            auto found = materials.find(to);
+            if (found == materials.end())
+                return fail("unknown material '" + to + "'");
+            replace[from] = found->second;
+        }
+        Placement at;
+        error.clear();
+        if (!read_placement(w, at))
+            return fail(error);
+        if (!replace.empty() && at.material != default_material)
+            return fail("'replace' and a material for the whole mesh can't be used together");
+        auto has_suffix = [&](const std::string& suffix) {
+            return file.size() >= suffix.size() && file.compare(file.size() - suffix.size(), suffix.size(), suffix) == 0;
+        };
+        const bool gltf = has_suffix(".gltf") || has_suffix(".glb");
+        if (!gltf && !replace.empty())
+            return fail("'replace' is for glTF files (OBJ files take scene materials by usemtl name)");
+        bool ok = gltf ? add_gltf(file, at.material == default_material ? -1 : at.material, replace, at.xform, at.moved)
+                       : add_obj(file, smooth, at.material, at.xform, at.moved);
+        return ok || fail(error);
     }
 
     void set_environment(int w, int h, std::vector<float> rgb, double intensity, double rotation_turns) {
@@ -2455,11 +2625,11 @@ class Loader {
             auto comment = line.find('#');
             if (comment != std::string::npos)
                 line.erase(comment);
-            std::istringstream in(line);
+            Words w(line);
             std::string keyword;
-            if (!(in >> keyword))
+            if (!w.word(keyword))
                 continue;
-            if (!parse_line(in, keyword)) {
+            if (!parse_line(w, keyword)) {
                 set_error(error);
                 return unsupported ? MYPBR_ERR_UNSUPPORTED : MYPBR_ERR_BAD_SCENE;
             }
