@@ -21,6 +21,7 @@
 //   post   <w> <h> <seed> <out>       postprocess + display_settings::apply + to_byte on a seeded image
 //   sky    <w> <h> <out>              atmosphere::bake and sun_transmittance for four suns and settings
 //   image  <file> <out>               image_texture's decoding of an 8-bit file (stb_image)
+//   load   <scene> <out>              load_scene's result: "ok", or the message it prints (text)
 #include <bvh.h>
 #include <denoiser.h>
 #include <scene.h>
@@ -33,6 +34,7 @@
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -542,6 +544,23 @@ int cmd_image(int argc, char** argv) {
     return 0;
 }
 
+// load <scene> <out>: load_scene on a file; writes "ok" or what it printed
+// on std::cerr ("path:line: message"), as text.
+int cmd_load(int argc, char** argv) {
+    if (argc < 4)
+        return 2;
+    std::ostringstream captured;
+    std::streambuf* old = std::cerr.rdbuf(captured.rdbuf());
+    std::clog.setstate(std::ios::failbit);
+    scene sc;
+    bool ok = load_scene(argv[2], sc);
+    std::clog.clear();
+    std::cerr.rdbuf(old);
+    std::ofstream out(argv[3], std::ios::binary);
+    out << (ok ? std::string("ok") : captured.str());
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -562,6 +581,7 @@ int main(int argc, char** argv) {
     else if (c == "post") rc = cmd_post(argc, argv);
     else if (c == "sky") rc = cmd_sky(argc, argv);
     else if (c == "image") rc = cmd_image(argc, argv);
+    else if (c == "load") rc = cmd_load(argc, argv);
     if (rc == 2)
         std::cerr << "bad arguments for '" << c << "'\n";
     return rc;

@@ -399,9 +399,29 @@ def gen_images():
     np.savez_compressed(os.path.join(HERE, "images.npz"), **out)
 
 
+def gen_messages():
+    """load_scene's outcome on every case of scene_messages.py: "ok" or the
+    message it prints, with the case file's folder written as <dir>/."""
+    sys.path.insert(0, HERE)
+    from scene_messages import CASES, PRELUDE
+    out = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, text in enumerate(CASES):
+            path = os.path.join(tmp, f"case{k}.scene")
+            with open(path, "w") as f:
+                f.write(PRELUDE + text + "\n")
+            result = os.path.join(tmp, "result.txt")
+            subprocess.run([HARNESS, "load", path, result], check=True)
+            msg = open(result).read().strip().replace(tmp + "/", "<dir>/")
+            out.append(msg)
+    np.savez_compressed(os.path.join(HERE, "scene_messages.npz"), cases=np.array(CASES), messages=np.array(out))
+    print(f"{len(out)} scene messages")
+
+
 GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_env, "ggx": gen_ggx,
           "render": gen_render, "denoise": gen_denoise, "voxels": gen_voxels, "post": gen_post, "sky": gen_sky,
-          "images": gen_images, "gltf": gen_gltf, "configs": gen_configs, "features": gen_features}
+          "images": gen_images, "gltf": gen_gltf, "configs": gen_configs, "features": gen_features,
+          "messages": gen_messages}
 
 if __name__ == "__main__":
     ref = os.environ.get("REFERENCE", "/root/reference")

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import mypbr_gb300 as mp
-from conftest import ROOT, scene_path
+from conftest import GOLDEN, ROOT, scene_path
 from mypbr_gb300 import flat
 
 
@@ -164,3 +164,26 @@ def test_scene_create_rejects_bad_indices():
     status = mp.lib().mypbr_gpu_scene_create(ctypes.byref(bad), ctypes.byref(out))
     assert status == 5, status  # MYPBR_ERR_INVALID_ARGUMENT, before looking for a device
     assert b"sphere 0 is malformed" in mp.lib().mypbr_last_error()
+
+
+def test_scene_messages_match_the_reference(tmp_path):
+    """Every case of tests/golden/scene_messages.py through the host loader:
+    it accepts exactly the cases the reference's load_scene accepts, and for
+    the others says what the reference says, byte for byte ("path:line:
+    message", with the case's folder written as <dir>/)."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from scene_messages import PRELUDE
+    g = np.load(os.path.join(GOLDEN, "scene_messages.npz"))
+    wrong = []
+    for k, (text, want) in enumerate(zip(g["cases"], g["messages"])):
+        path = tmp_path / f"case{k}.scene"
+        path.write_text(PRELUDE + str(text) + "\n")
+        try:
+            mp.load_scene(str(path))
+            got = "ok"
+        except mp.MypbrError as e:
+            got = mp.lib().mypbr_last_error().decode().strip().replace(str(tmp_path) + "/", "<dir>/")
+        if got != str(want):
+            wrong.append((str(text), got, str(want)))
+    assert not wrong, "\n".join(f"{t!r}:\n  got  {a}\n  want {b}" for t, a, b in wrong)
