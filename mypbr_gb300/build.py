@@ -101,8 +101,16 @@ def build_oracle():
     reference checkout exists, its golden-vector harness (oracle/_ref)."""
     oracle = os.path.join(ROOT, "oracle")
     subprocess.run(["make", "-s", "-C", oracle], check=True)
-    if os.path.isdir(os.environ.get("REFERENCE", "/root/reference")):
-        subprocess.run(["make", "-s", "-C", oracle, "ref"], check=True)
+    subprocess.run(["make", "-s", "-C", oracle, "ref-if-present"], check=True)
+
+
+def reference_dir():
+    """The reference checkout's folder as oracle/Makefile knows it (the
+    REFERENCE variable there), or None where it is absent."""
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", os.path.join(ROOT, "oracle"), "reference-dir"],
+                       capture_output=True, text=True)
+    path = r.stdout.strip()
+    return path if r.returncode == 0 and path else None
 
 
 if __name__ == "__main__":

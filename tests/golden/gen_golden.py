@@ -1,7 +1,7 @@
 """Writes the golden vectors that pin the oracle to the reference.
 
-Run in a checkout that has the reference (adriendjn/mypbr) at REFERENCE
-(default /root/reference). It builds oracle/_ref/ref_harness from the
+Run in a checkout that has the reference (adriendjn/mypbr) where
+oracle/Makefile's REFERENCE says (or set REFERENCE). It builds oracle/_ref/ref_harness from the
 reference's own headers (oracle/Makefile, target `ref`), runs it on the test
 scenes of tests/golden/scenes/, and stores the results as .npz files next to
 this script. The tests read only those .npz files, so nothing here runs at test
@@ -424,8 +424,8 @@ GROUPS = {"hits": gen_hits, "bsdf": gen_bsdf, "lights": gen_lights, "env": gen_e
           "messages": gen_messages}
 
 if __name__ == "__main__":
-    ref = os.environ.get("REFERENCE", "/root/reference")
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REFERENCE={ref}"], check=True)
+    overrides = [f"REFERENCE={os.environ['REFERENCE']}"] if "REFERENCE" in os.environ else []
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", *overrides], check=True)
     if not os.path.exists(os.path.join(SCENES, "env_small.hdr")):
         make_env_fixture()
     if not os.path.exists(os.path.join(SCENES, "voxels.vox")):
