@@ -1662,15 +1662,18 @@ extern "C" int mypbr_gpu_set_launch(mypbr_gpu_scene* G, int32_t block, int64_t w
 // The scene must already be on the device (mypbr_gpu_scene_create) and the
 // caller passes device output buffers.
 //
-// Limits: at most kNoAllocMaxPixels (65,536) pixels in the rendered rows,
-// max_depth at most kNoAllocMaxDepth. The array (kNoAllocBytes, 18 MiB) exists
-// on every GPU that loads this library, for as long as the library is loaded.
-// Every call reuses it and it keeps the previous call's contents, so the film
-// and counters are cleared at the start of each call; two calls whose work
-// overlaps on the GPU (different streams, or different host threads) race on
-// it and must not be issued. The first call on a device looks the array's
-// device address up (cudaGetSymbolAddress) with that device current; make that
-// first call before capturing any stream.
+// Limits: at most kNoAllocMaxPixels (65,536) pixels in the rendered rows
+// (width x row_count; a band of a larger image is fine), max_depth at most
+// kNoAllocMaxDepth. The array (kNoAllocBytes, 18 MiB) exists on every GPU that
+// loads this library, for as long as the library is loaded. Every call reuses
+// it and it keeps the previous call's contents, so the film and counters are
+// cleared at the start of each call; two calls whose work overlaps on the GPU
+// (different streams, or different host threads) race on it and must not be
+// issued. The first call on a device looks the array's device address up
+// (cudaGetSymbolAddress) with that device current and keeps it; make that
+// first call before any stream capture begins, and do not reset the device
+// (cudaDeviceReset) while the library is loaded, since the kept address would
+// then be stale.
 
 namespace mypbr_dev {
 namespace {
@@ -1756,25 +1759,26 @@ extern "C" int mypbr_gpu_render_noalloc(mypbr_gpu_scene* G, const mypbr_camera* 
     if (o->max_depth > kNoAllocMaxDepth)
         return bad_arg("mypbr_gpu_render_noalloc: max_depth is limited to " + std::to_string(kNoAllocMaxDepth));
     if (o->guided != 0) {
-        set_error_message("mypbr_gpu_render_noalloc: the guided sampler is not available in this build");
+        set_error_message("mypbr_gpu_render_noalloc: guided rendering is not supported by the render without "
+                          "allocation (it has no scratch for the network's training records)");
         return MYPBR_ERR_UNSUPPORTED;
     }
-    if (o->max_diffuse > 255 || o->max_specular > 255 || o->max_diffuse < 0 || o->max_specular < 0 ||
-        o->max_scatter < 0)
+    if (o->max_diffuse > 255 || o->max_specular > 255 || o->max_scatter > 255 || o->max_diffuse < 0 ||
+        o->max_specular < 0 || o->max_scatter < 0)
         return bad_arg("mypbr_gpu_render_noalloc: bounce caps must be in [0, 255]");
     MYPBR_CUDA(cudaSetDevice(G->device));
     WaveParams P{};
     P.S = G->dev;
     P.cam = make_camera(*cam, o->samples_per_pixel);
-    size_t full = size_t(P.cam.width) * P.cam.height;
-    if (full > kNoAllocMaxPixels)
-        return bad_arg("mypbr_gpu_render_noalloc: " + std::to_string(P.cam.width) + " x " +
-                       std::to_string(P.cam.height) + " exceeds the " + std::to_string(kNoAllocMaxPixels) +
-                       "-pixel limit of the render without allocation");
     P.first_row = o->first_row;
     P.band_rows = o->row_count > 0 ? o->row_count : P.cam.height - o->first_row;
     if (o->first_row < 0 || o->row_count < 0 || P.band_rows <= 0 || P.first_row + P.band_rows > P.cam.height)
         return bad_arg("mypbr_gpu_render_noalloc: first_row / row_count outside the image");
+    size_t npix = size_t(P.cam.width) * P.band_rows;
+    if (npix > kNoAllocMaxPixels)
+        return bad_arg("mypbr_gpu_render_noalloc: " + std::to_string(P.cam.width) + " x " +
+                       std::to_string(P.band_rows) + " rendered pixels exceed the " +
+                       std::to_string(kNoAllocMaxPixels) + "-pixel limit of the render without allocation");
     P.max_depth = o->max_depth;
     P.max_diffuse = o->max_diffuse;
     P.max_specular = o->max_specular;
@@ -1789,17 +1793,24 @@ extern "C" int mypbr_gpu_render_noalloc(mypbr_gpu_scene* G, const mypbr_camera* 
     if (s != MYPBR_OK)
         return s;
     P.B = carve(base, &P.totals);
-    size_t npix = size_t(P.cam.width) * P.band_rows;
     int spp = o->samples_per_pixel;
     int per_wave = int(std::max<size_t>(1, kNoAllocMaxPixels / npix));
     per_wave = std::min(per_wave, spp);
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
-    // The array keeps the last call's contents: clear what accumulates
-    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * full * sizeof(double), st));
-    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * full * sizeof(double), st));
+    // The array keeps the last call's contents: clear what accumulates (the
+    // band's film only, which starts at the array's film buffers)
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * npix * sizeof(double), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * npix * sizeof(double), st));
     if (P.collect_features)
-        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * full * sizeof(double), st));
+        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * npix * sizeof(double), st));
     MYPBR_CUDA(cudaMemsetAsync(P.totals, 0, 2 * sizeof(unsigned long long), st));
+    // The kernels index the film by the pixel's place in the whole image; the
+    // array holds only the band's pixels, so the film pointers are moved back
+    // by the band's first pixel (only indices from that pixel on are used)
+    size_t first_pixel = size_t(P.first_row) * P.cam.width;
+    P.B.film -= 3 * first_pixel;
+    P.B.film2 -= 3 * first_pixel;
+    P.B.feat -= 7 * first_pixel;
     Launch L = launch_config(*G);
     uint64_t launches = 0;
     KernelTimer T;  // off: no events are created
