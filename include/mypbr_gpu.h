@@ -491,12 +491,17 @@ int mypbr_gpu_render_ex(mypbr_gpu_scene* scene, const mypbr_camera* cam, const m
  * 18 MiB device array in the library, present on every GPU that loads it until
  * the library is unloaded; the scene comes from mypbr_gpu_scene_create and the
  * outputs are caller-provided device buffers as for mypbr_gpu_render_device.
- * Limits: at most 65,536 pixels in the rendered rows (256 x 256, say) and
- * max_depth <= 1024; larger requests fail with MYPBR_ERR_INVALID_ARGUMENT.
- * Calls share the array: it is cleared at the start of each call, and calls
- * that overlap on the GPU race, so issue one at a time. The first call on a
- * device looks up the array's address with that device current; make it
- * before capturing any stream. Synchronous: returns when the frame is done. */
+ * Limits: at most 65,536 pixels in the rendered rows (width x row_count:
+ * 256 x 256, say, or a 34-row band of a 1920-wide frame), bounce caps at most
+ * 255 and max_depth <= 1024; larger requests fail with
+ * MYPBR_ERR_INVALID_ARGUMENT. Guided rendering is not supported here
+ * (MYPBR_ERR_UNSUPPORTED). The outputs are indexed over the whole image, as
+ * for mypbr_gpu_render_device: only the band's rows are written. Calls share
+ * the array: it is cleared at the start of each call, and calls that overlap
+ * on the GPU race, so issue one at a time. The first call on a device looks up
+ * the array's address with that device current and keeps it: make that first
+ * call before any stream capture begins, and do not reset the device while
+ * the library is loaded. Synchronous: returns when the frame is done. */
 int mypbr_gpu_render_noalloc(mypbr_gpu_scene* scene, const mypbr_camera* cam, const mypbr_render_opts* opts,
                              double* d_radiance, double* d_albedo, double* d_normal, double* d_variance,
                              void* cuda_stream);
