@@ -73,10 +73,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WIDTH, HEIGHT = 1920, 1080
-# DRAM bytes k_extend moves per ray, from one ncu capture of the same kernel on
-# a 4-spp wave of this workload (299.0 MB read + 136.7 MB written, 8,294,400
-# rays): the ray record, hit record and queue entries, the tree staying in L2
-EXTEND_DRAM_BYTES_PER_RAY = (299.0e6 + 136.7e6) / 8294400
+# k_extend as ncu measured it (profiles/k_extend_sphere_field_1080p.md: the
+# capture command, the figures and the commit they were taken at; re-taken
+# whenever k_extend changes): DRAM bytes per ray of bounce 0 of a 4-spp frame
+# (ray records in, hit records and queue entries out, the tree staying in L2)
+# and the issue figures of bounces 0 and 1.
+EXTEND_PROFILE = {
+    "profile": "profiles/k_extend_sphere_field_1080p.md",
+    "dram_bytes": 298.96e6 + 135.86e6, "rays": 8294400,
+    "issue_active_frac": [0.589, 0.611], "threads_per_instruction": [26.55, 12.88],
+}
+EXTEND_DRAM_BYTES_PER_RAY = EXTEND_PROFILE["dram_bytes"] / EXTEND_PROFILE["rays"]
 METRIC = "Mpaths/s at 1080p"
 UNIT = "Mpaths/s"
 
@@ -168,28 +175,36 @@ def flat_bytes(scene):
     return total
 
 
-def oracle_render_timed(scene, spp, threads, rows=None):
+def oracle_render_timed(scene, spp, threads, rows=None, row_stride=1):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     cam = scene.camera
     cam.samples_per_pixel = spp
     O = orc.OracleScene(scene)
     t = time.perf_counter()
-    _, _, ex = O.render(cam, threads=threads, rows=rows)
+    _, _, ex = O.render(cam, threads=threads, rows=rows, row_stride=row_stride)
     return time.perf_counter() - t, ex
 
 
-def cpu_sample(scene, threads, budget_s):
-    """Times the oracle on a bounded sample of the workload: a band of rows of
-    the 1080p frame at the full 256 spp, sized from a short probe to take about
-    budget_s seconds. Returns (Mpaths/s, description)."""
-    probe_rows = 4
-    t1, ex1 = oracle_render_timed(scene, 256, threads, rows=(HEIGHT // 2 - probe_rows // 2, probe_rows))
+def cpu_stride(scene, threads, budget_s):
+    """The row stride of the CPU sample: every k-th row of the 1080p frame at
+    the full 256 spp, k chosen from a short probe (every 108th row) so that
+    the sample takes about budget_s seconds. Rows spread over the whole frame
+    see every part of the image in proportion, unlike a band."""
+    t1, ex1 = oracle_render_timed(scene, 256, threads, rows=(HEIGHT // 216, 0), row_stride=HEIGHT // 10)
     rate = ex1["paths"] / t1
-    rows = int(max(probe_rows, min(HEIGHT, budget_s * rate / (WIDTH * 256))))
-    first = max(0, HEIGHT // 2 - rows // 2)
-    t, ex = oracle_render_timed(scene, 256, threads, rows=(first, rows))
-    return ex["paths"] / t / 1e6, f"rows {first}..{first + rows - 1} of 1920x1080 at 256 spp ({ex['paths']} paths, {t:.1f} s)"
+    rows = max(4, min(HEIGHT, int(budget_s * rate / (WIDTH * 256))))
+    return max(1, HEIGHT // rows)
+
+
+def cpu_sample(scene, threads, stride):
+    """Times the oracle on every `stride`-th row of the frame at 256 spp.
+    Returns (Mpaths/s, paths, seconds, description)."""
+    t, ex = oracle_render_timed(scene, 256, threads, rows=(stride // 2, 0), row_stride=stride)
+    n_rows = ex["paths"] // (WIDTH * 256)
+    desc = (f"every {stride}th row of 1920x1080 ({n_rows} rows from row {stride // 2}) at 256 spp: "
+            f"{ex['paths']} paths in {t:.2f} s")
+    return ex["paths"] / t / 1e6, ex["paths"], t, desc
 
 
 # ------------------------------------------------------------ arms
@@ -202,16 +217,23 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     with tempfile.TemporaryDirectory() as d:
         scene = mp.load_scene(sphere_field_scene(d, spp=256))
-        rates = []
+        stride = cpu_stride(scene, threads, args.reference_budget)
+        rates, seconds, paths = [], [], 0
         desc = ""
         for k in range(args.warmup + args.steps):
-            mpaths, desc = cpu_sample(scene, threads, args.reference_budget)
+            mpaths, n, t, desc = cpu_sample(scene, threads, stride)
             if k >= args.warmup:
                 rates.append(mpaths)
+                seconds.append(t)
+                paths = n
     value = statistics.mean(rates)
-    ms_per_step = WIDTH * HEIGHT * 256 / (value * 1e6) * 1e3
+    frame_ms = WIDTH * HEIGHT * 256 / (value * 1e6) * 1e3
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": statistics.mean(seconds) * 1e3,
+            "ms_per_step_is": f"the timed sample (every {stride}th row of the frame, {paths} paths); a full "
+                              f"1080p frame at this rate would take {frame_ms:.0f} ms",
+            "ms_per_frame_extrapolated": frame_ms,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "config": WORKLOAD, "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "per step: " + desc},
@@ -260,30 +282,31 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     times, launches = [], 0
-    totals = {"ext": 0, "sh": 0, "ms_extend": 0.0, "ms_shade": 0.0, "ms_shadow": 0.0, "ms_generate": 0.0,
-              "n_extend": 0, "n_shade": 0, "n_shadow": 0}
+    totals = {"ext": 0, "sh": 0}
     for _ in range(args.steps):
         flush.fill_(1)
         st = mp.RenderStatsStruct()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        step(st, True)
+        step(st, False)  # the production path: each wave a replayed CUDA graph
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
         launches += st.kernel_launches
         totals["ext"] += st.extension_rays
         totals["sh"] += st.shadow_rays
-        for k in ("ms_extend", "ms_shade", "ms_shadow", "ms_generate"):
-            totals[k] += getattr(st, k)
-        totals["n_extend"] += st.launches_extend
-        totals["n_shade"] += st.launches_shade
-        totals["n_shadow"] += st.launches_shadow
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     clk = clocks.stop()
+    # one more frame, after the timed region, with every kernel launched on its
+    # own between CUDA events: the kernels' shares and k_extend's launch time
+    flush.fill_(1)
+    kst = mp.RenderStatsStruct()
+    step(kst, True)
+    torch.cuda.synchronize()
+    kernel_ms = {k: getattr(kst, k) for k in ("ms_extend", "ms_shade", "ms_shadow", "ms_generate", "ms_other")}
     total_ms = sum(times)
     if world > 1:
         t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
@@ -310,13 +333,44 @@ def run_ours(args):
             e2e_times.append(dt)
     e2e = world * paths_per_step / statistics.mean(e2e_times) / 1e6
 
+    # relMSE of the last timed frame (256 spp) against a 65,536-spp render of
+    # every 8th row, made after the timed region as two independent halves
+    # whose difference measures the reference's own noise (taken out)
+    quality = None
+    if rank == 0 and args.headline_ref_spp > 0:
+        frame = rad.cpu().numpy()
+        rows = list(range(4, h, 8))
+        halves = []
+        o.timing = 0
+        saved = (o.samples_per_pixel, o.seed, o.first_row, o.row_count)
+        t0 = time.perf_counter()
+        for seed in (777001, 777002):
+            half = torch.zeros((h, w, 3), dtype=torch.float64, device=dev)
+            o.samples_per_pixel = args.headline_ref_spp // 2
+            o.seed = seed
+            for j in rows:
+                o.first_row, o.row_count = j, 1
+                mp.check(L.mypbr_gpu_render_device(gpu.handle, ctypes.byref(c), ctypes.byref(o),
+                                                   ctypes.c_void_p(half.data_ptr()), None, None, None,
+                                                   ctypes.c_void_p(stream.cuda_stream), None))
+            torch.cuda.synchronize()
+            halves.append(half.cpu().numpy()[rows])
+        o.samples_per_pixel, o.seed, o.first_row, o.row_count = saved
+        ref = 0.5 * (halves[0] + halves[1])
+        raw = rel_mse(frame[rows], ref)
+        noise = reference_noise(halves[0], halves[1])
+        quality = {"relmse": raw - noise, "relmse_raw": raw, "reference_noise": noise, "epsilon": 0.01,
+                   "reference": f"{args.headline_ref_spp} spp (two independent halves), FP64 film, rows 4, 12, ... "
+                                f"({len(rows)} of {h}), {time.perf_counter() - t0:.1f} s after the timed region",
+                   "of": f"the last timed frame ({args.spp} spp)"}
+
     if rank == 0:
         # roofline of the dominant kernel, extend: algorithmic bytes per ray =
         # ray record read (origin + tmin, direction + pdf: 32 B) + queue index
         # (4 B) + hit record written (16 B)
-        ms_ext = totals["ms_extend"] / max(totals["n_extend"], 1)
+        ms_ext = kst.ms_extend / max(kst.launches_extend, 1)
         bytes_per_ray = 52
-        ext_per_launch = totals["ext"] / max(totals["n_extend"], 1)
+        ext_per_launch = kst.extension_rays / max(kst.launches_extend, 1)
         achieved = bytes_per_ray * ext_per_launch / (ms_ext * 1e-3) / 1e9 if ms_ext > 0 else 0.0
         peak = None
         try:
@@ -325,7 +379,8 @@ def run_ours(args):
             peak_src = "measured"
         except Exception:
             peak, peak_src = 6800.0, "fallback"
-        shares = {k: totals[k] / total_ms for k in ("ms_extend", "ms_shade", "ms_shadow", "ms_generate")}
+        frame_ms = sum(kernel_ms.values())
+        shares = {k: v / frame_ms for k, v in kernel_ms.items()}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -336,25 +391,31 @@ def run_ours(args):
                          "shadow_per_path": totals["sh"] / (paths_per_step * args.steps),
                          "mrays_per_s": world * (totals["ext"] + totals["sh"]) / (total_ms * 1e-3) / 1e6},
                 "kernel_time_share": shares,
+                "kernel_time_share_of": "one extra frame after the timed region, each kernel between CUDA events",
                 "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
                              "unit": "GB/s", "frac": achieved / peak if peak else None,
                              "traffic": EXTEND_DRAM_BYTES_PER_RAY * ext_per_launch,
-                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_extend on a "
-                                               "4-spp wave (435.7 MB for 8,294,400 camera rays), scaled to the "
-                                               "rays of an average launch",
+                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_extend on bounce "
+                                               f"0 of a 4-spp frame ({EXTEND_PROFILE['dram_bytes'] / 1e6:.1f} MB for "
+                                               f"{EXTEND_PROFILE['rays']} camera rays, {EXTEND_PROFILE['profile']}), "
+                                               "scaled to the rays of an average launch",
                              "peak_source": peak_src, "bytes_per_ray": bytes_per_ray,
                              "avg_launch_ms": ms_ext, "rays_per_launch": ext_per_launch,
                              # the walk's real bound is instruction issue under divergence: the
                              # same ncu capture's issue-slot utilisation and lanes per instruction
-                             "issue": {"issue_active_frac": [0.587, 0.610], "threads_per_instruction": [26.6, 12.9],
+                             "issue": {"issue_active_frac": EXTEND_PROFILE["issue_active_frac"],
+                                       "threads_per_instruction": EXTEND_PROFILE["threads_per_instruction"],
                                        "source": "ncu smsp__issue_active and smsp__thread_inst_executed_per_"
-                                                 "inst_executed of k_extend, bounces 0 and 1 of a 4-spp wave"}},
+                                                 "inst_executed of k_extend, bounces 0 and 1 of a 4-spp frame ("
+                                                 + EXTEND_PROFILE["profile"] + ")"}},
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(w * h * 3 * 8)},
                 "clocks": clk}
+        if quality:
+            line["quality"] = quality
         if world == 1 and not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            mpaths, desc = cpu_sample(scene, threads, args.cpu_budget)
+            mpaths, _, _, desc = cpu_sample(scene, threads, cpu_stride(scene, threads, args.cpu_budget))
             line["cpu_baseline"] = {"value": mpaths, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -439,7 +500,7 @@ def run_voxel_hall(args):
     for name, guided in (("plain", 0), ("guided", args.hidden)):
         pts = []
         spp = 16
-        while spp <= args.max_spp:
+        while spp <= args.max_spp and not args.no_curve:
             if guided:  # an untrained network every time: training is inside each timing
                 mp.guide_reset(Gg)
             img, t = render(Gg if guided else G, spp, guided, 1 + spp)
@@ -449,7 +510,7 @@ def run_voxel_hall(args):
             if e <= target / 2:
                 break
             spp *= 2
-        tt, how = time_to_target([p_[:3] for p_ in pts], target)
+        tt, how = time_to_target([p_[:3] for p_ in pts], target) if pts else (None, "no curve rendered")
         # the estimate that decides: independent renders at one spp, whose mean
         # relMSE gives the error constant c = relMSE x spp (one render's relMSE
         # swings by 3x or more with the fireflies it happens to catch)
@@ -737,8 +798,10 @@ def main():
     p.add_argument("--spp", type=int, default=256)
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for cpu_baseline")
-    p.add_argument("--reference-budget", type=float, default=8.0, help="seconds per reference step")
+    p.add_argument("--reference-budget", type=float, default=5.0, help="seconds per reference step")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--headline-ref-spp", type=int, default=65536,
+                   help="spp of the reference the headline frame's relMSE is taken against (0: skip)")
     p.add_argument("--workload", choices=["sphere_field", "voxel_hall", "cornell", "triangle_room", "batch",
                                           "hall_render"], default="sphere_field")
     p.add_argument("--hall-size", type=int, default=512)
@@ -751,6 +814,8 @@ def main():
     p.add_argument("--wave-paths", type=int, default=0, help="cornell / triangle_room: paths per wave (0: default)")
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--hall-width", type=int, default=480)
+    p.add_argument("--no-curve", action="store_true",
+                   help="voxel_hall: skip the doubling-spp curve (the repeated renders decide the time to target)")
     p.add_argument("--ref-spp", type=int, default=65536)
     p.add_argument("--c3-ref-spp", type=int, default=1024, help="spp of the triangle room's reference render")
     p.add_argument("--max-spp", type=int, default=32768)

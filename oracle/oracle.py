@@ -44,6 +44,9 @@ def lib():
         L.oracle_environment.restype = None
         L.oracle_render.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp]
         L.oracle_render.restype = ctypes.c_int
+        L.oracle_render_strided.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            vp, vp, vp, vp, vp, vp]
+        L.oracle_render_strided.restype = ctypes.c_int
         L.oracle_denoise.argtypes = [dp, dp, dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double, dp]
         L.oracle_denoise.restype = None
@@ -130,9 +133,11 @@ class OracleScene:
         lib().oracle_environment(self._h, _dp(direction), n, _dp(rad), _dp(pdf))
         return rad, pdf
 
-    def render(self, camera, threads=0, rows=None, features=False):
+    def render(self, camera, threads=0, rows=None, features=False, row_stride=1):
         """Renders with the oracle. Returns (radiance (H, W, 3), variance of the
-        mean per channel (H, W, 3), extras dict)."""
+        mean per channel (H, W, 3), extras dict). rows = (first, count) renders
+        only those rows; with row_stride k, rows first, first + k, ... (count of
+        them, 0: to the bottom) - the others are left at 0."""
         c, o = camera.structs()
         o.collect_features = int(features)
         w, h = c.image_width, c.image_height
@@ -147,7 +152,8 @@ class OracleScene:
         def p(a):
             return ctypes.c_void_p(a.ctypes.data) if a is not None else ctypes.c_void_p()
 
-        lib().oracle_render(self._h, ctypes.addressof(c), ctypes.addressof(o), int(threads), int(first), int(count),
-                            p(rad), p(var), p(alb), p(nrm), p(lv), p(counts))
+        lib().oracle_render_strided(self._h, ctypes.addressof(c), ctypes.addressof(o), int(threads), int(first),
+                                    int(count) if rows is not None else 0, int(row_stride),
+                                    p(rad), p(var), p(alb), p(nrm), p(lv), p(counts))
         return rad, var, {"albedo": alb, "normal": nrm, "lum_var": lv, "paths": int(counts[0]),
                           "extension_rays": int(counts[1]), "shadow_rays": int(counts[2])}

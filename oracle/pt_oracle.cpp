@@ -2089,26 +2089,32 @@ void oracle_environment(const oracle_scene* s, const double* dir, int64_t n, dou
 // variance of camera.h:236-245 (W*H). counts (may be NULL): paths, extension
 // rays, shadow rays. threads <= 0 uses every hardware thread. first_row /
 // row_count restrict the render to a band of rows (the rest stays 0).
-int oracle_render(const oracle_scene* s, const mypbr_camera* cam, const mypbr_render_opts* opts, int threads,
-                  int first_row, int row_count, double* radiance, double* channel_var, double* albedo,
-                  double* normal, double* lum_var, uint64_t* counts) {
+// Renders rows first_row, first_row + row_stride, ... (row_count of them;
+// row_count <= 0: to the bottom of the image) of the camera's image.
+int oracle_render_strided(const oracle_scene* s, const mypbr_camera* cam, const mypbr_render_opts* opts, int threads,
+                          int first_row, int row_count, int row_stride, double* radiance, double* channel_var,
+                          double* albedo, double* normal, double* lum_var, uint64_t* counts) {
     const Scene& S = *reinterpret_cast<const Scene*>(s);
     Camera C;
     C.init(*cam, opts->samples_per_pixel);
     Integrator I{S, *opts, S.f->light_count > 0};
     int W = C.w, H = C.h, spp = opts->samples_per_pixel;
-    if (row_count <= 0 || first_row + row_count > H)
-        row_count = H - first_row;
+    row_stride = std::max(row_stride, 1);
+    first_row = std::clamp(first_row, 0, H - 1);
+    int most = (H - 1 - first_row) / row_stride + 1;
+    if (row_count <= 0 || row_count > most)
+        row_count = most;
     int nt = threads > 0 ? threads : int(std::thread::hardware_concurrency());
     nt = std::max(nt, 1);
-    std::atomic<int> next_row{first_row};
+    std::atomic<int> next_row{0};
     std::atomic<uint64_t> tot_ext{0}, tot_sh{0};
     auto worker = [&]() {
         uint64_t ext = 0, sh = 0;
         while (true) {
-            int j = next_row.fetch_add(1);
-            if (j >= first_row + row_count)
+            int k = next_row.fetch_add(1);
+            if (k >= row_count)
                 break;
+            int j = first_row + k * row_stride;
             for (int i = 0; i < W; i++) {
                 size_t p = size_t(j) * W + i;
                 V sum, sum2, asum, nsum;
@@ -2170,6 +2176,13 @@ int oracle_render(const oracle_scene* s, const mypbr_camera* cam, const mypbr_re
         counts[2] = tot_sh.load();
     }
     return 0;
+}
+
+int oracle_render(const oracle_scene* s, const mypbr_camera* cam, const mypbr_render_opts* opts, int threads,
+                  int first_row, int row_count, double* radiance, double* channel_var, double* albedo,
+                  double* normal, double* lum_var, uint64_t* counts) {
+    return oracle_render_strided(s, cam, opts, threads, first_row, row_count, 1, radiance, channel_var, albedo,
+                                 normal, lum_var, counts);
 }
 
 }  // extern "C"
