@@ -728,6 +728,9 @@ int mypbr_guide_reset(mypbr_gpu_scene* scene);
  * setting applies from the next render. */
 int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths);
 
+/* the network's encoded inputs (n x 128, BF16 values as floats) of n
+ * vertices given by their 7 scalars in [0, 1] (n x 7). */
+int mypbr_guide_test_encode(const float* scalars, int64_t n, float* out);
 /* outputs (n x 64) of the network for encoded inputs (n x 128). */
 int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out);
 /* weight gradients (same layout as weights) of sum_i dout_i . out_i. */

@@ -165,6 +165,7 @@ def lib():
     L.mypbr_write_image.argtypes = [ctypes.c_char_p, dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), ctypes.c_int]
     L.mypbr_guide_reset.argtypes = [vp]
     L.mypbr_guide_configure.argtypes = [vp, ctypes.c_float, i32]
+    L.mypbr_guide_test_encode.argtypes = [fp, i64, fp]
     L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
     L.mypbr_guide_test_backward.argtypes = [ctypes.c_int, fp, fp, fp, i64, fp]
     L.mypbr_guide_test_loss.argtypes = [fp, fp, fp, i64, fp, fp]
@@ -399,6 +400,15 @@ def _f32(a):
 
 def _fptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def guide_encode(scalars):
+    """The network's encoded inputs (n, 128) of vertices given by their 7
+    scalars (n, 7), as the forward kernels write them (BF16)."""
+    s = _f32(scalars)
+    out = np.zeros((s.shape[0], 128), dtype=np.float32)
+    check(lib().mypbr_guide_test_encode(_fptr(s), s.shape[0], _fptr(out)))
+    return out
 
 
 def guide_forward(hidden, weights, inputs):

@@ -825,6 +825,49 @@ int mypbr_guide_test_backward(int hidden, const float* weights, const float* inp
     return rc;
 }
 
+}  // extern "C"
+
+namespace mypbr_dev {
+// Encodes n rows of 7 scalars into a shared 128-row canonical tile per CTA
+// (guide_encode_row, as the forward kernels do) and copies the BF16 features
+// out as floats.
+__global__ void k_encode_test(const float* scalars, long long n, float* out) {
+    __shared__ __align__(16) __nv_bfloat16 tile[128 * kGuideIn];
+    for (long long base = (long long)blockIdx.x * 128; base < n; base += (long long)gridDim.x * 128) {
+        long long i = base + threadIdx.x;
+        float s[kGuideScalars];
+        for (int k = 0; k < kGuideScalars; k++)
+            s[k] = i < n ? scalars[i * kGuideScalars + k] : 0.0f;
+        guide_encode_row(i < n ? s : nullptr, tile, threadIdx.x);
+        __syncwarp();
+        if (i < n)
+            for (int k = 0; k < kGuideIn; k++)
+                out[i * kGuideIn + k] = __bfloat162float(tile[canon(threadIdx.x, k, kGuideIn)]);
+        __syncthreads();
+    }
+}
+}  // namespace mypbr_dev
+
+extern "C" {
+
+int mypbr_guide_test_encode(const float* scalars, int64_t n, float* out) {
+    if (!scalars || !out || n < 0)
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    float *d_s, *d_out;
+    int rc;
+    if ((rc = dalloc(d_s, size_t(n) * kGuideScalars + 1)) || (rc = dalloc(d_out, size_t(n) * kGuideIn + 1)))
+        return rc;
+    cudaMemcpy(d_s, scalars, size_t(n) * kGuideScalars * 4, cudaMemcpyHostToDevice);
+    k_encode_test<<<64, 128>>>(d_s, n, d_out);
+    cudaError_t e = cudaDeviceSynchronize();
+    rc = e != cudaSuccess ? cuda_fail(e, "k_encode_test") : MYPBR_OK;
+    if (rc == MYPBR_OK)
+        cudaMemcpy(out, d_out, size_t(n) * kGuideIn * 4, cudaMemcpyDeviceToHost);
+    cudaFree(d_s);
+    cudaFree(d_out);
+    return rc;
+}
+
 int mypbr_guide_test_loss(const float* raw, const float* dirs, const float* c, int64_t n, float* grad, float* loss) {
     if (!raw || !dirs || !c || !grad || !loss || n < 0)
         return MYPBR_ERR_INVALID_ARGUMENT;

@@ -293,14 +293,22 @@ MYPBR_DEV void tmem_ld16(uint32_t taddr, float* v) {
 }
 MYPBR_DEV void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// 64 consecutive 32-bit columns of this thread's lane in one load.
+MYPBR_DEV void tmem_ld64(uint32_t taddr, float* v) {
+    uint32_t r[64];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr));
+#pragma unroll
+    for (int k = 0; k < 64; k++)
+        v[k] = __uint_as_float(r[k]);
+}
+
 // 64 columns starting at `col` of this thread's lane.
 MYPBR_DEV void tmem_row64(uint32_t tmem, int col, float* v) {
     uint32_t lane = uint32_t((threadIdx.x >> 5) & 3) * 32u;
-    uint32_t a = tmem + (lane << 16) + uint32_t(col);
-    tmem_ld16(a, v);
-    tmem_ld16(a + 16, v + 16);
-    tmem_ld16(a + 32, v + 32);
-    tmem_ld16(a + 48, v + 48);
+    tmem_ld64(tmem + (lane << 16) + uint32_t(col), v);
     tmem_wait_ld();
 }
 
@@ -309,6 +317,28 @@ MYPBR_DEV void tmem_row64(uint32_t tmem, int col, float* v) {
 MYPBR_DEV uint32_t pack_bf16(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// max(a, 0), max(b, 0) rounded to BF16 and packed (a in the low half), one
+// instruction.
+MYPBR_DEV uint32_t pack_bf16_relu(float a, float b) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
+
+// Writes ReLU of 64 values of row r as BF16 into a canonical K-major tile
+// with K = 64 columns.
+MYPBR_DEV void store_row_bf16_relu(__nv_bfloat16* tile, int r, const float* v) {
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+        uint4 u;
+        u.x = pack_bf16_relu(v[8 * b], v[8 * b + 1]);
+        u.y = pack_bf16_relu(v[8 * b + 2], v[8 * b + 3]);
+        u.z = pack_bf16_relu(v[8 * b + 4], v[8 * b + 5]);
+        u.w = pack_bf16_relu(v[8 * b + 6], v[8 * b + 7]);
+        *reinterpret_cast<uint4*>(tile + canon(r, 8 * b, 64)) = u;
+    }
 }
 
 // Writes 64 values of row r as BF16 into a canonical K-major tile with K
@@ -434,10 +464,7 @@ __global__ void __launch_bounds__(128 * kGuideGroups) k_guide_forward(GuideNetVi
             tc::tmem_row64(tmem, 0, v);
             tc::fence_before();
             if (l < net.hidden) {
-#pragma unroll
-                for (int k = 0; k < 64; k++)
-                    v[k] = fmaxf(v[k], 0.0f);
-                store_row_bf16(A, row, kGuideWidth, 0, v);
+                store_row_bf16_relu(A, row, v);
             } else if (i < rows) {
                 sink.put(i, v);
             }
@@ -451,21 +478,75 @@ __global__ void __launch_bounds__(128 * kGuideGroups) k_guide_forward(GuideNetVi
     }
 }
 
-// Encodes scalars s into row `row` of a canonical K = 128 tile (zeros if s is null).
-MYPBR_DEV void guide_encode_row(const float* s, __nv_bfloat16* tile, int row) {
-#pragma unroll 1
-    for (int b = 0; b < kGuideIn / 8; b++) {
-        float v[8];
+// The one-blob bins of one scalar, out[b] = exp(-0.5 (u - b)^2) with
+// u = s * BINS - 0.5 (guide_feature's values), in blocks of up to 8 bins:
+// one exponential at the block's middle bin m, then outwards by the ratio of
+// neighbouring Gaussians (g[b+1] = g[b] exp(u - b - 0.5) going up, g[b-1] =
+// g[b] exp(b - u - 0.5) going down), each ratio shrinking by 1/e per bin.
+// Three exponentials per block instead of one per bin. Every bin is within 4
+// of m, so a middle value that underflows FP32 (|u - m| > 13) leaves only
+// values below 1e-18 (then 0).
+template <int BINS>
+MYPBR_DEV void one_blob_bins(float s, float* out) {
+    constexpr float kInvE = 0.36787944117144233f;
+    const float u = s * float(BINS) - 0.5f;
 #pragma unroll
-        for (int e = 0; e < 8; e++)
-            v[e] = s ? guide_feature(s, 8 * b + e) : 0.0f;
-        uint4 u;
-        u.x = pack_bf16(v[0], v[1]);
-        u.y = pack_bf16(v[2], v[3]);
-        u.z = pack_bf16(v[4], v[5]);
-        u.w = pack_bf16(v[6], v[7]);
-        *reinterpret_cast<uint4*>(tile + canon(row, 8 * b, kGuideIn)) = u;
+    for (int a = 0; a < BINS; a += 8) {
+        constexpr int kBlock = BINS < 8 ? BINS : 8;
+        const int m = a + kBlock / 2;
+        const float x = u - float(m);
+        const float gm = __expf(-0.5f * x * x);
+        float g = gm, up = __expf(x - 0.5f);
+#pragma unroll
+        for (int b = m; b < a + kBlock; b++) {
+            out[b] = g;
+            g *= up;
+            up *= kInvE;
+        }
+        g = gm;
+        float down = __expf(-x - 0.5f);
+#pragma unroll
+        for (int b = m - 1; b >= a; b--) {
+            g *= down;
+            down *= kInvE;
+            out[b] = g;
+        }
     }
+}
+
+// Packs 8 floats as BF16 into the 16 bytes at `dst`.
+MYPBR_DEV void store8_bf16(__nv_bfloat16* dst, const float* v) {
+    uint4 u;
+    u.x = pack_bf16(v[0], v[1]);
+    u.y = pack_bf16(v[2], v[3]);
+    u.z = pack_bf16(v[4], v[5]);
+    u.w = pack_bf16(v[6], v[7]);
+    *reinterpret_cast<uint4*>(dst) = u;
+}
+
+// Encodes scalars s into row `row` of a canonical K = 128 tile (zeros if s
+// is null): the one-blob features of guide_feature, k = 0..127.
+MYPBR_DEV void guide_encode_row(const float* s, __nv_bfloat16* tile, int row) {
+    float v[kGuideIn];
+    if (s) {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            one_blob_bins<32>(s[i], v + 32 * i);
+#pragma unroll
+        for (int i = 3; i < 7; i++)
+            one_blob_bins<6>(s[i], v + 96 + 6 * (i - 3));
+        v[kGuideEncoded] = 1.0f;
+#pragma unroll
+        for (int k = kGuideEncoded + 1; k < kGuideIn; k++)
+            v[k] = 0.0f;
+    } else {
+#pragma unroll
+        for (int k = 0; k < kGuideIn; k++)
+            v[k] = 0.0f;
+    }
+#pragma unroll
+    for (int b = 0; b < kGuideIn / 8; b++)
+        store8_bf16(tile + canon(row, 8 * b, kGuideIn), v + 8 * b);
 }
 
 // The decoded mixture of a vertex as the shading kernels read it: per lobe

@@ -101,6 +101,27 @@ def test_bf16_rounding_is_nearest_even():
 # ------------------------------------------------------------------- GPU
 
 @pytest.mark.gpu
+def test_encoding_matches_oracle():
+    """The one-blob encoding the forward kernels write (neighbour-ratio
+    recurrence, three exponentials per block of 8 bins) against the oracle's
+    exact Gaussians rounded to BF16: within one BF16 step everywhere, equal
+    for nearly every value that matters (>= 1e-6); values below 1e-18 may be
+    0 (far tails, where FP32 underflows)."""
+    rng = np.random.default_rng(21)
+    s = rng.random((3000, 7))
+    s[:20] = 0.0  # the edges of the unit interval
+    s[20:40] = 1.0
+    got = mp.guide_encode(s.astype(np.float32)).astype(np.float64)
+    want = go.one_blob(s.astype(np.float32).astype(np.float64))
+    want_bf16 = go.bf16(want)
+    ulp = np.abs(want_bf16) * 2.0 ** -7
+    diff = np.abs(got - want_bf16)
+    assert np.all(diff <= ulp + 1e-18), diff.max()
+    visible = want_bf16 >= 1e-6
+    assert np.mean(diff[visible] == 0) > 0.99, np.mean(diff[visible] == 0)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("hidden", [2, 4, 8])
 def test_tensor_core_forward_matches_oracle(hidden):
     w = random_net(hidden, 10 + hidden)
