@@ -56,7 +56,7 @@ struct WaveParams {
     unsigned long long seed;
     int pass0, npass;
     int first_row, band_rows;  // the rows rendered: [first_row, first_row + band_rows)
-    unsigned long long* totals;  // extension rays, shadow rays
+    unsigned long long* totals;  // extension rays, shadow rays, bounces run by a replayed wave graph
     // path guiding
     int guided;                // mixtures were computed for this wave's guidable vertices
     float guide_alpha;         // probability of sampling the mixture there (one-sample MIS)
@@ -185,9 +185,25 @@ MYPBR_DEV int2 wave_of(const WaveParams& P) {
     return P.B.wave_state ? make_int2(P.B.wave_state[0], P.B.wave_state[1]) : make_int2(P.pass0, P.npass);
 }
 
+// The bounce a kernel works on: its argument, or, given -1 (the kernels of a
+// replayed wave graph, which loops over bounces on the device), the bounce
+// counter in device memory.
+MYPBR_DEV int bounce_of(const WaveParams& P, int depth) { return depth >= 0 ? depth : P.B.wave_state[2]; }
+
 __global__ void k_set_wave(int* state, int pass0, int npass) {
     state[0] = pass0;
     state[1] = npass;
+    state[2] = 0;  // bounce
+}
+
+// Ends one bounce of a replayed wave graph's loop: the next bounce runs while
+// it is below max_depth and its extension queue holds paths (once a bounce
+// has none, no later one has any). Counts the bounces run.
+__global__ void k_next_bounce(WaveParams P, cudaGraphConditionalHandle loop) {
+    int next = P.B.wave_state[2] + 1;
+    P.B.wave_state[2] = next;
+    atomicAdd(&P.totals[2], 1ull);
+    cudaGraphSetConditional(loop, next < P.max_depth && *ext_counter(P, next) > 0 ? 1u : 0u);
 }
 
 __global__ void k_generate(WaveParams P) {
@@ -275,6 +291,7 @@ MYPBR_DEV int hit_material(const DeviceScene& S, const HitInfo& h) {
 // Closest hits of the extension queue; each ray then joins its shading class's queue.
 template <bool VOX, int WALK>
 __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
+    depth = bounce_of(P, depth);
     uint32_t n = *ext_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
         atomicAdd(&P.totals[0], (unsigned long long)n);
@@ -304,6 +321,7 @@ __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
 // Efficiency of Ray Traversal on GPUs", HPG 2009). Same hits as k_extend.
 template <bool VOX>
 __global__ void __launch_bounds__(256, 3) k_extend_pt(WaveParams P, int depth) {
+    depth = bounce_of(P, depth);
     const uint32_t n = *ext_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
         atomicAdd(&P.totals[0], (unsigned long long)n);
@@ -595,15 +613,16 @@ __device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
 // are held to two (a guided render 19 % faster).
 template <int C>
 __global__ void __launch_bounds__(256) k_shade(WaveParams P, int depth) {
-    shade_body<C, false>(P, depth);
+    shade_body<C, false>(P, bounce_of(P, depth));
 }
 template <int C>
 __global__ void __launch_bounds__(256, 2) k_shade_guided(WaveParams P, int depth) {
-    shade_body<C, true>(P, depth);
+    shade_body<C, true>(P, bounce_of(P, depth));
 }
 
 template <bool VOX, int WALK>
 __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
+    depth = bounce_of(P, depth);
     uint32_t n = *sh_counter(P, depth);
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0)
         atomicAdd(&P.totals[1], (unsigned long long)n);
@@ -741,14 +760,19 @@ MYPBR_DEV uint32_t guided_slot(const WaveParams& P, int depth, long long i) {
     return 0;  // not reached: i < count()
 }
 
+// The guidable vertices of a bounce (depth -1: the bounce in device memory),
+// none past the guided depths.
 struct GuideQueueSource {
     WaveParams P;
     int depth;
     MYPBR_DEV long long count(long long) const {
+        const int d = bounce_of(P, depth);
+        if (d >= P.guide_depths)
+            return 0;
         long long n = 0;
 #pragma unroll
         for (int c = 0; c < 4; c++)
-            n += *class_counter(P, depth, guided_class(c));
+            n += *class_counter(P, d, guided_class(c));
         return n;
     }
     MYPBR_DEV void fill(long long i, __nv_bfloat16* A, int row) const {
@@ -756,7 +780,7 @@ struct GuideQueueSource {
             guide_encode_row(nullptr, A, row);
             return;
         }
-        uint32_t slot = guided_slot(P, depth, i);
+        uint32_t slot = guided_slot(P, bounce_of(P, depth), i);
         float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot], hb = P.B.hit[slot];
         HitInfo h;
         h.t = hb.x;
@@ -774,7 +798,7 @@ struct GuidePackSink {
     WaveParams P;
     int depth;
     MYPBR_DEV void put(long long i, const float* v) const {
-        uint32_t slot = guided_slot(P, depth, i);
+        uint32_t slot = guided_slot(P, bounce_of(P, depth), i);
         GuidePacked pk;
         guide_pack(v, pk);
         P.guide_mix[slot] = pk;
@@ -814,7 +838,7 @@ int ensure_buffers(RenderBuffers& rb, size_t capacity, size_t pixels, int depth_
     A(rb.class_queue, capacity * kShadeClasses);
     A(rb.shadow_queue, capacity);
     A(rb.counters, counter_words(depth_slots));
-    A(rb.wave_state, 2);
+    A(rb.wave_state, 4);
     A(rb.film, 3 * pixels);
     A(rb.film2, 3 * pixels);
     A(rb.feat, 7 * pixels);
@@ -1015,8 +1039,8 @@ struct KernelTimer {
             return s_;                           \
     } while (0)
 
-// Renders passes [pass0, pass0 + npass) of every pixel of the band into the film.
-int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T) {
+// A wave's start: cleared queue counters, camera rays, feature guides.
+int run_prefix(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T) {
     MYPBR_CUDA(cudaMemsetAsync(P.B.counters, 0, sizeof(uint32_t) * counter_words(P.B.depth_slots), st));
     TIMED(0, (k_generate<<<L.grid_stream, 256, 0, st>>>(P)));
     launches++;
@@ -1024,52 +1048,110 @@ int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches
         TIMED(4, (k_features<<<L.grid_shade, 256, 0, st>>>(P)));
         launches++;
     }
-    for (int depth = 0; depth < P.max_depth; depth++) {
-        if (L.persistent && P.S.has_voxels)
-            TIMED(1, (k_extend_pt<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
-        else if (L.persistent)
-            TIMED(1, (k_extend_pt<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
-        else
-            TIMED(1, (launch_bounce_kernel(extend_kernel(P.S.has_voxels, L.walk), L.grid_extend, L.block, st, P, depth)));
-        if (P.guided && depth < P.guide_depths) {  // the mixtures of this bounce's guidable vertices
-            TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
-                         L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
-            launches++;
-        }
-        if (L.guided_kernels) {
-            TIMED(2, (k_shade_guided<kClassMiss><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade_guided<kClassLambert><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade_guided<kClassMetal><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade_guided<kClassDielectric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade_guided<kClassPrincipled><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade_guided<kClassGeneric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-        } else {
-            TIMED(2, (k_shade<kClassMiss><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassLambert><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassMetal><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassDielectric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassPrincipled><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-            TIMED(2, (k_shade<kClassGeneric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
-        }
-        TIMED(3, (launch_bounce_kernel(shadow_kernel(P.S.has_voxels, L.walk), L.grid_shadow, L.block, st, P, depth)));
-        launches += 2 + kShadeClasses;
+    return MYPBR_OK;
+}
+
+// One bounce: extend, the guiding network's mixtures (guided renders), the
+// shading classes, shadow rays. depth -1: the bounce counter in device memory.
+int run_bounce(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T, int depth) {
+    if (L.persistent && P.S.has_voxels)
+        TIMED(1, (k_extend_pt<true><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+    else if (L.persistent)
+        TIMED(1, (k_extend_pt<false><<<L.grid_extend, L.block, 0, st>>>(P, depth)));
+    else
+        TIMED(1, (launch_bounce_kernel(extend_kernel(P.S.has_voxels, L.walk), L.grid_extend, L.block, st, P, depth)));
+    if (P.guided && (depth < 0 || depth < P.guide_depths)) {  // the mixtures of this bounce's guidable vertices
+        TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
+                     L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
+        launches++;
     }
+    if (L.guided_kernels) {
+        TIMED(2, (k_shade_guided<kClassMiss><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade_guided<kClassLambert><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade_guided<kClassMetal><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade_guided<kClassDielectric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade_guided<kClassPrincipled><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade_guided<kClassGeneric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+    } else {
+        TIMED(2, (k_shade<kClassMiss><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassLambert><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassMetal><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassDielectric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassPrincipled><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+        TIMED(2, (k_shade<kClassGeneric><<<L.grid_shade, L.block, 0, st>>>(P, depth)));
+    }
+    TIMED(3, (launch_bounce_kernel(shadow_kernel(P.S.has_voxels, L.walk), L.grid_shadow, L.block, st, P, depth)));
+    launches += 2 + kShadeClasses;
+    return MYPBR_OK;
+}
+
+// Renders passes [pass0, pass0 + npass) of every pixel of the band into the
+// film, every bounce up to max_depth launched from the host.
+int run_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T) {
+    int s = run_prefix(P, L, st, launches, T);
+    for (int depth = 0; depth < P.max_depth && s == MYPBR_OK; depth++)
+        s = run_bounce(P, L, st, launches, T, depth);
+    if (s != MYPBR_OK)
+        return s;
     MYPBR_CUDA(cudaGetLastError());
     return MYPBR_OK;
 }
 
-// One wave's kernel sequence captured as a CUDA graph and replayed for every
-// wave with the same settings; the pass range is read from device memory
-// (wave_state), set by a one-thread kernel before each replay.
+// A wave's bounces as a CUDA graph replayed for every wave with the same
+// settings: one conditional WHILE node whose body is one bounce's kernels
+// (they read the bounce from device memory) followed by k_next_bounce, which
+// lets the loop go on while the next bounce has paths and is below
+// max_depth. Bounces with no paths are not launched at all, and the loop ends
+// after max_depth bodies at most. The wave's start (counters, camera rays,
+// features) is launched before the graph, with the pass range in device
+// memory (wave_state) set by a one-thread kernel.
 struct WaveGraph {
     cudaGraphExec_t exec = nullptr;
     int key = -1;
-    uint64_t launches = 0;  // kernels in the graph
+    uint64_t per_bounce = 0;  // kernels in one body, k_next_bounce included
     ~WaveGraph() {
         if (exec)
             cudaGraphExecDestroy(exec);
     }
 };
+
+int build_wave_graph(WaveParams& P, const Launch& L, cudaStream_t st, WaveGraph* graph) {
+    cudaGraph_t g = nullptr;
+    MYPBR_CUDA(cudaGraphCreate(&g, 0));
+    struct Owned {
+        cudaGraph_t g;
+        ~Owned() { cudaGraphDestroy(g); }
+    } owned{g};
+    cudaGraphConditionalHandle loop;
+    MYPBR_CUDA(cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    MYPBR_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    MYPBR_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    uint64_t n = 0;
+    KernelTimer off;  // no events inside a graph
+    off.st = st;
+    int s = run_bounce(P, L, st, n, off, -1);
+    if (s == MYPBR_OK)
+        k_next_bounce<<<1, 1, 0, st>>>(P, loop);
+    cudaGraph_t captured = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &captured);
+    if (s != MYPBR_OK)
+        return s;
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaStreamEndCapture (wave graph body)");
+    MYPBR_CUDA(cudaGetLastError());
+    e = cudaGraphInstantiate(&graph->exec, g, 0);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGraphInstantiate");
+    graph->per_bounce = n + 1;
+    return MYPBR_OK;
+}
 
 int launch_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T,
                 WaveGraph* graph) {
@@ -1084,28 +1166,17 @@ int launch_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launc
             cudaGraphExecDestroy(graph->exec);
             graph->exec = nullptr;
         }
-        cudaGraph_t g = nullptr;
-        MYPBR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        uint64_t n = 0;
-        int s = run_wave(P, L, st, n, T);
-        cudaError_t e = cudaStreamEndCapture(st, &g);
-        if (s != MYPBR_OK) {
-            if (g)
-                cudaGraphDestroy(g);
+        int s = build_wave_graph(P, L, st, graph);
+        if (s != MYPBR_OK)
             return s;
-        }
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&graph->exec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaGraphInstantiate");
         graph->key = key;
-        graph->launches = n;
     }
     k_set_wave<<<1, 1, 0, st>>>(P.B.wave_state, P.pass0, P.npass);
+    launches++;
+    int s = run_prefix(P, L, st, launches, T);
+    if (s != MYPBR_OK)
+        return s;
     MYPBR_CUDA(cudaGraphLaunch(graph->exec, st));
-    launches += graph->launches + 1;
     return MYPBR_OK;
 }
 
@@ -1287,8 +1358,8 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
     NvtxRange range("mypbr render");
     WaveParams& P = R.P;
     Totals tot;
-    MYPBR_CUDA(cudaMalloc(&tot.d, 2 * sizeof(unsigned long long)));
-    MYPBR_CUDA(cudaMemsetAsync(tot.d, 0, 2 * sizeof(unsigned long long), st));
+    MYPBR_CUDA(cudaMalloc(&tot.d, 3 * sizeof(unsigned long long)));
+    MYPBR_CUDA(cudaMemsetAsync(tot.d, 0, 3 * sizeof(unsigned long long), st));
     P.totals = tot.d;
     size_t full = size_t(P.cam.width) * P.cam.height;
     MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * full * sizeof(double), st));
@@ -1342,13 +1413,14 @@ int render_all(mypbr_gpu_scene* G, RenderSetup& R, cudaStream_t st, double* d_ra
     MYPBR_CUDA(cudaGetLastError());
     if (stats) {
         *stats = mypbr_render_stats{};
-        unsigned long long t[2];
+        unsigned long long t[3];
         MYPBR_CUDA(cudaMemcpyAsync(t, tot.d, sizeof t, cudaMemcpyDeviceToHost, st));
         MYPBR_CUDA(cudaStreamSynchronize(st));
         stats->paths = uint64_t(R.npix) * uint64_t(R.spp);
         stats->extension_rays = t[0];
         stats->shadow_rays = t[1];
-        stats->kernel_launches = launches;
+        // host launches, plus the kernels of every bounce the wave graphs ran
+        stats->kernel_launches = launches + t[2] * graph.per_bounce;
         int s = T.collect(stats);
         if (s != MYPBR_OK)
             return s;
@@ -1471,8 +1543,8 @@ int job_start(mypbr_batch_job& jb, BatchJob& j) {
         return s;
     WaveParams& P = j.R.P;
     cudaStream_t st = G->stream;
-    MYPBR_CUDA(cudaMalloc(&j.tot.d, 2 * sizeof(unsigned long long)));
-    MYPBR_CUDA(cudaMemsetAsync(j.tot.d, 0, 2 * sizeof(unsigned long long), st));
+    MYPBR_CUDA(cudaMalloc(&j.tot.d, 3 * sizeof(unsigned long long)));
+    MYPBR_CUDA(cudaMemsetAsync(j.tot.d, 0, 3 * sizeof(unsigned long long), st));
     P.totals = j.tot.d;
     size_t full = size_t(P.cam.width) * P.cam.height;
     MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * full * sizeof(double), st));
