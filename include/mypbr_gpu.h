@@ -506,6 +506,15 @@ int mypbr_gpu_render_noalloc(mypbr_gpu_scene* scene, const mypbr_camera* cam, co
                              double* d_radiance, double* d_albedo, double* d_normal, double* d_variance,
                              void* cuda_stream);
 
+/* Self-intersection probe (no counterpart in the reference, whose rays skip
+ * t < 0.001): for n rays (n x 8 as for mypbr_gpu_trace) the closest hit, then
+ * a reflected ray and a ray going on through the surface, both started as
+ * the renderer starts them (hit point moved off the surface by its FP32
+ * error bound). out (n x 4): kind of the first hit (-1 none), 1 where the
+ * reflected / the continued ray met the surface it left, kind of the
+ * reflected ray's hit (-1 none). */
+int mypbr_gpu_test_spawn(mypbr_gpu_scene* scene, const float* rays, int64_t n, int32_t* out);
+
 /* Ray batch query: closest hit of n rays against the scene, the reference's
  * world.hit (hittable_list.h:25-37 over bvh.h:45-86 and scene::unbounded)
  * without media (media are stochastic). rays: n x 8 floats (ox oy oz dx dy dz

@@ -166,6 +166,7 @@ def lib():
     L.mypbr_guide_reset.argtypes = [vp]
     L.mypbr_guide_configure.argtypes = [vp, ctypes.c_float, i32]
     L.mypbr_guide_test_encode.argtypes = [fp, i64, fp]
+    L.mypbr_gpu_test_spawn.argtypes = [vp, fp, i64, ip]
     L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
     L.mypbr_guide_test_backward.argtypes = [ctypes.c_int, fp, fp, fp, i64, fp]
     L.mypbr_guide_test_loss.argtypes = [fp, fp, fp, i64, fp, fp]
@@ -264,6 +265,16 @@ class GpuScene:
         check(lib().mypbr_gpu_trace(self._h, rays.ctypes.data_as(fp), n, hits.ctypes.data_as(fp),
                                     prim.ctypes.data_as(ip), 0))
         return hits, prim
+
+    def spawn_probe(self, rays):
+        """Self-intersection probe (mypbr_gpu_test_spawn): for rays (n, 8)
+        float32, (n, 4) int32 [kind of the hit, reflected ray met its surface,
+        continued ray met its surface, kind of the reflected ray's hit]."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        out = np.zeros((rays.shape[0], 4), dtype=np.int32)
+        fp, ip = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)
+        check(lib().mypbr_gpu_test_spawn(self._h, rays.ctypes.data_as(fp), rays.shape[0], out.ctypes.data_as(ip)))
+        return out
 
     def bsdf_eval(self, material, rec, r_in, wi):
         """eval rgb and scatter pdf of material at records rec (n, 16)."""

@@ -1165,7 +1165,68 @@ struct Surface {
     float u, v;
     int material;
     bool front;
+    float3 ng;    // geometric normal (unit; either side), 0 where there is no surface (a medium)
+    float3 perr;  // per component, a bound on |p - the exact point| from the FP32 arithmetic that made p
 };
+
+// ------------------------------------------------- error-bounded ray origins
+//
+// A hit point computed in FP32 lies off the exact surface by a rounding
+// error whose bound follows from how it was computed (Pharr, Jakob and
+// Humphreys, "Physically Based Rendering", 3rd ed., section 3.9: gamma_n =
+// n u / (1 - n u) bounds n roundings, u = 2^-24). A new ray starts at the hit
+// point moved along the geometric normal, to the side it leaves on, by that
+// bound projected on the normal, then one float step further: the exact
+// surface is then behind the origin. The bounds below are taken at twice the
+// IEEE figure: fast-math reciprocals and square roots round less tightly.
+MYPBR_DEV float err_gamma(int n) {
+    const float u = 5.9604645e-8f;
+    return 2.0f * float(n) * u / (1.0f - float(n) * u);
+}
+MYPBR_DEV float3 abs3(float3 a) { return f3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+
+// The error of X p (+ translation) for a point p with error e: the rounding
+// of the products and sums, and e carried through |M|.
+MYPBR_DEV float3 xf_point_error(const XformRef& X, float3 p, float3 e) {
+    float3 out;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float4 r = X.r[i];
+        float mag = fabsf(r.x * p.x) + fabsf(r.y * p.y) + fabsf(r.z * p.z) + fabsf(r.w);
+        float carried = fabsf(r.x) * e.x + fabsf(r.y) * e.y + fabsf(r.z) * e.z;
+        set_comp(out, i, err_gamma(3) * mag + (1.0f + err_gamma(3)) * carried);
+    }
+    return out;
+}
+
+// The next float after x in the direction of `dir` (> 0: up, < 0: down).
+MYPBR_DEV float float_step(float x, float dir) {
+    if (dir == 0.0f)
+        return x;
+    if (x == 0.0f)
+        return dir > 0.0f ? 1.4e-45f : -1.4e-45f;
+    bool away = (dir > 0.0f) == (x > 0.0f);  // away from zero: the bit pattern grows
+    return __int_as_float(__float_as_int(x) + (away ? 1 : -1));
+}
+
+// The smallest t a walk from o along d accepts: 8 FP32 steps of the
+// origin's largest coordinate, in units of d. Below that the intersection
+// arithmetic cannot tell on which side of the origin a surface lies; the
+// spawn offset has already put the surface just left behind the origin.
+MYPBR_DEV float spawn_tmin(float3 o, float3 d) {
+    float m = fmaxf(fabsf(o.x), fmaxf(fabsf(o.y), fabsf(o.z)));
+    return m * 9.5367431640625e-7f * rsqrtf(dot(d, d));
+}
+
+// Where a ray leaving surface s in direction w starts.
+MYPBR_DEV float3 spawn_origin(const Surface& s, float3 w) {
+    float dist = fabsf(s.ng.x) * s.perr.x + fabsf(s.ng.y) * s.perr.y + fabsf(s.ng.z) * s.perr.z;
+    float3 off = dist * s.ng;
+    if (dot(w, s.ng) < 0.0f)
+        off = -1.0f * off;
+    float3 o = s.p + off;
+    return f3(float_step(o.x, off.x), float_step(o.y, off.y), float_step(o.z, off.z));
+}
 
 MYPBR_DEV void set_face(Surface& s, float3 d, float3 outward) {
     s.front = dot(d, outward) < 0.0f;
@@ -1197,6 +1258,8 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
     s.front = true;
     s.normal = f3(1, 0, 0);
     s.material = 0;
+    s.ng = f3(0.0f);
+    s.perr = f3(0.0f);
     if (kind == kSphere) {
         float4 sp = ldg4(S.spheres + idx);
         int2 info = S.sphere_info[idx];
@@ -1209,6 +1272,8 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
             s.p = c + fabsf(r) * (r < 0.0f ? -outward : outward);  // back onto the surface
             set_face(s, d, outward);
             sphere_uv_tangents(r < 0.0f ? -outward : outward, fabsf(r), s);
+            s.ng = outward;
+            s.perr = err_gamma(6) * (abs3(c) + fabsf(r) * abs3(outward));
         } else {
             XformRef X;
             load_xform(S, info.y, X);
@@ -1218,7 +1283,9 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
             Surface ls;
             set_face(ls, ld, outward);
             float3 un = r < 0.0f ? -outward : outward;
-            sphere_uv_tangents(un * rsqrtf(dot(un, un)), fabsf(r), ls);
+            un = un * rsqrtf(dot(un, un));
+            sphere_uv_tangents(un, fabsf(r), ls);
+            lp = c + fabsf(r) * un;  // back onto the surface, in the sphere's space
             s.u = ls.u;
             s.v = ls.v;
             s.front = ls.front;
@@ -1226,6 +1293,8 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
             s.normal = normalize(xf_normal(X, ls.normal));
             s.dpdu = xf_vec(X, ls.dpdu);
             s.dpdv = xf_vec(X, ls.dpdv);
+            s.ng = normalize(xf_normal(X, un));
+            s.perr = xf_point_error(X, lp, err_gamma(6) * (abs3(c) + fabsf(r) * abs3(un)));
         }
     } else if (kind == kQuad) {
         const float4* q = S.quads + 5 * idx;
@@ -1237,6 +1306,8 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
         s.dpdv = f3(ldg4(q + 2));
         s.p = f3(Q) + h.b1 * s.dpdu + h.b2 * s.dpdv;
         set_face(s, d, f3(ldg4(q + 3)));
+        s.ng = normalize(f3(ldg4(q + 3)));
+        s.perr = err_gamma(5) * (abs3(f3(Q)) + fabsf(h.b1) * abs3(s.dpdu) + fabsf(h.b2) * abs3(s.dpdv));
     } else if (kind == kTriangle) {
         const float4* tp = S.tris + 3 * idx;
         float4 P0 = ldg4(tp), P1 = ldg4(tp + 1), P2 = ldg4(tp + 2);
@@ -1269,6 +1340,10 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
         if (flags & 1)
             g = -g;
         set_face(s, d, g);
+        s.ng = g;
+        // the edges are differences of the stored corners: their rounding too
+        s.perr = err_gamma(7) * (abs3(v0) + fabsf(b1) * (abs3(f3(P1)) + abs3(v0)) +
+                                 fabsf(b2) * (abs3(f3(P2)) + abs3(v0)));
         if (sa.x >= 0) {
             float3 sh = b0 * S.normals[sa.x] + b1 * S.normals[sa.y] + b2 * S.normals[sa.z];
             if (dot(sh, sh) > 0.0f) {
@@ -1287,7 +1362,13 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
         const DevVoxelModel& m = S.voxel_models[__ldg(&S.voxel_blocks[2 * idx].x)];
         XformRef X;
         load_xform(S, m.xform, X);
-        float3 lp = xf_ipoint(X, o) + h.t * xf_ivec(X, d);
+        float3 lo = xf_ipoint(X, o), ld = xf_ivec(X, d);
+        float3 lp = lo + h.t * ld;
+        // the face lies on a whole-number plane of the model's cells: the
+        // point is put on it exactly; along the face, the ray's rounding
+        float3 lerr = err_gamma(4) * (abs3(lo) + abs3(h.t * ld));
+        set_comp(lp, axis, rintf(comp(lp, axis)));
+        set_comp(lerr, axis, 0.0f);
         float3 outward = f3(0.0f), tb = f3(0.0f), tc = f3(0.0f);
         set_comp(outward, axis, sign);
         set_comp(tb, (axis + 1) % 3, 1.0f);
@@ -1303,6 +1384,8 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
         s.normal = normalize(xf_normal(X, ls.normal));
         s.dpdu = xf_vec(X, du);
         s.dpdv = xf_vec(X, dv);
+        s.ng = normalize(xf_normal(X, outward));
+        s.perr = xf_point_error(X, lp, lerr);
     } else if (kind == kGround) {
         DevUnbounded ub = S.unbounded[idx];
         s.material = ub.material;
@@ -1312,6 +1395,7 @@ MYPBR_DEV Surface make_surface(const DeviceScene& S, const HitInfo& h, float3 o,
         s.dpdu = f3(1, 0, 0);
         s.dpdv = f3(0, 0, -1);
         set_face(s, d, f3(0, 1, 0));
+        s.ng = f3(0, 1, 0);  // the point is on the plane exactly (y set to its height)
     } else if (kind == kHeightFog) {
         s.material = S.unbounded[idx].material;
     }

@@ -241,7 +241,7 @@ __global__ void k_features(WaveParams P) {
         float3 tint = f3(1.0f), albedo = f3(1.0f), normal = f3(0.0f);
         bool done = false;
         for (int b = 0; b < 8 && !done; b++) {
-            HitInfo h = closest_hit<true>(P.S, o, d, 0.001f, 3.0e38f, media_key(P, pixel, pass, 100 + b, 3));
+            HitInfo h = closest_hit<true>(P.S, o, d, spawn_tmin(o, d), 3.0e38f, media_key(P, pixel, pass, 100 + b, 3));
             if (h.prim == kMiss)
                 break;
             Surface s = make_surface(P.S, h, o, d);
@@ -257,8 +257,8 @@ __global__ void k_features(WaveParams P) {
                 done = true;
             } else {
                 tint *= sr.attenuation;
-                o = s.p;
                 d = sr.skip_dir;
+                o = spawn_origin(s, d);
             }
         }
         if (!done) {
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(256, 3) k_extend(WaveParams P, int depth) {
             uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
             key = media_key(P, pixel, pass, uint32_t(depth), 0);
         }
-        HitInfo h = closest_hit<VOX, WALK>(P.S, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
+        HitInfo h = closest_hit<VOX, WALK>(P.S, f3(ro), f3(rd), spawn_tmin(f3(ro), f3(rd)), 3.0e38f, key);
         P.B.hit[slot] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.prim));
         int c = h.prim == kMiss ? kClassMiss : int(P.S.mat_class[hit_material(P.S, h)]);
         uint32_t* counter = class_counter(P, depth, c);
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(256, 3) k_extend_pt(WaveParams P, int depth) {
                         uint32_t pixel = f_bits(P.B.radiance[slot].w), pass = f_bits(P.B.beta[slot].w);
                         key = media_key(P, pixel, pass, uint32_t(depth), 0);
                     }
-                    walk_init(P.S, W, f3(ro), f3(rd), 0.001f, 3.0e38f, key);
+                    walk_init(P.S, W, f3(ro), f3(rd), spawn_tmin(f3(ro), f3(rd)), 3.0e38f, key);
                     active = true;
                 } else {
                     exhausted = true;
@@ -481,8 +481,8 @@ __device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
                     terminate = true;
                 } else {
                     beta *= sr.attenuation;
-                    new_o = s.p;
                     new_d = sr.skip_dir;
+                    new_o = spawn_origin(s, new_d);
                     if (P.transparent_shadows && lets_shadows_through(S, mat) && P.has_lights && depth > 0 && !specular)
                         seen = true;
                     specular = true;
@@ -528,7 +528,8 @@ __device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
                             float w = last ? 1.0f : power_heuristic(lp, mis_pdf(to_light));
                             float3 c = beta * f * sky * (w / lp);
                             float3 sd = normalize(to_light);
-                            P.B.sh_o[slot] = make_float4(s.p.x, s.p.y, s.p.z, 0.0f);
+                            float3 so = spawn_origin(s, sd);
+                            P.B.sh_o[slot] = make_float4(so.x, so.y, so.z, 0.0f);
                             P.B.sh_d[slot] = make_float4(sd.x, sd.y, sd.z, 0.0f);
                             P.B.sh_c[slot] = make_float4(c.x, c.y, c.z, sky_only ? 1.0f : 0.0f);
                             P.B.shadow_queue[warp_push(sh_counter(P, depth))] = slot;
@@ -553,8 +554,8 @@ __device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
                         float3 factor = class_eval<C>(S, mat, d, s, dir) / spdf;
                         beta *= factor;
                         scatter_pdf = spdf;
-                        new_o = s.p;
                         new_d = dir;
+                        new_o = spawn_origin(s, new_d);
                         specular = false;
                         if constexpr (GUIDED && kGuidable<C>()) {
                             if (P.record && !vol && slot < P.rec_slots && depth < P.rec.depth) {
@@ -645,13 +646,13 @@ __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
             // sample already holds the sky's radiance (sc.w = 1).
             if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1);
-            if (!any_hit<VOX, WALK>(S, o, d, 0.001f, 3.0e38f, key))
+            if (!any_hit<VOX, WALK>(S, o, d, spawn_tmin(o, d), 3.0e38f, key))
                 emission = sc.w != 0.0f ? f3(1.0f) : escaped_radiance(S, d, false);
         } else
         for (int hop = 0; hop <= 16; hop++) {
             if (P.keyed)
                 key = media_key(P, pixel, pass, uint32_t(depth), 1 + 4 * hop);
-            HitInfo h = closest_hit<VOX, WALK>(S, o, d, 0.001f, 3.0e38f, key);
+            HitInfo h = closest_hit<VOX, WALK>(S, o, d, spawn_tmin(o, d), 3.0e38f, key);
             if (h.prim == kMiss) {
                 emission = escaped_radiance(S, d, false);
                 break;
@@ -665,7 +666,7 @@ __global__ void __launch_bounds__(256, 3) k_shadow(WaveParams P, int depth) {
             Surface s = make_surface(S, h, o, d);
             if (through_glass) {
                 through *= interior_transmittance(S, mat, h.t * length(d), s.front);
-                o = s.p;
+                o = spawn_origin(s, d);
                 continue;
             }
             emission = emitted(S, mat, d, s);
