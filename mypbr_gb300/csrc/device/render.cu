@@ -206,7 +206,61 @@ __global__ void k_next_bounce(WaveParams P, cudaGraphConditionalHandle loop) {
     cudaGraphSetConditional(loop, next < P.max_depth && *ext_counter(P, next) > 0 ? 1u : 0u);
 }
 
-__global__ void k_generate(WaveParams P) {
+// A job of a batch graph, before its loop: the first wave's state (passes
+// [0, min(per_wave, spp)), bounce 0, starting) and cleared queue counters.
+__global__ void k_job_begin(WaveParams P, int per_wave, int spp, int counter_words) {
+    if (threadIdx.x == 0) {
+        P.B.wave_state[0] = 0;
+        P.B.wave_state[1] = min(per_wave, spp);
+        P.B.wave_state[2] = 0;
+        P.B.wave_state[3] = 1;
+    }
+    for (int k = threadIdx.x; k < counter_words; k += blockDim.x)
+        P.B.counters[k] = 0;
+}
+
+// Ends one iteration of a job's loop in a batch graph (one bounce of one
+// wave): the next bounce of this wave while it is below max_depth and has
+// paths, else the next wave (counters cleared, camera rays generated by the
+// next iteration) while passes remain, else the job is done. Each iteration
+// advances the bounce or the pass range, so the loop ends after
+// waves x max_depth iterations at most.
+__global__ void k_job_step(WaveParams P, cudaGraphConditionalHandle loop, int per_wave, int spp, int counter_words) {
+    __shared__ int new_wave;
+    if (threadIdx.x == 0) {
+        int* ws = P.B.wave_state;
+        ws[3] = 0;
+        atomicAdd(&P.totals[2], 1ull);
+        int next = ws[2] + 1;
+        unsigned go = 1;
+        new_wave = 0;
+        if (next < P.max_depth && *ext_counter(P, next) > 0) {
+            ws[2] = next;
+        } else if (ws[0] + ws[1] < spp) {
+            int pass0 = ws[0] + ws[1];
+            ws[0] = pass0;
+            ws[1] = min(per_wave, spp - pass0);
+            ws[2] = 0;
+            ws[3] = 1;
+            new_wave = 1;
+        } else {
+            go = 0;
+        }
+        cudaGraphSetConditional(loop, go);
+    }
+    __syncthreads();
+    if (new_wave)
+        for (int k = threadIdx.x; k < counter_words; k += blockDim.x)
+            P.B.counters[k] = 0;
+}
+
+// gated: only when the wave state says a wave starts (a job's device-side
+// loop in a batch graph runs this kernel every iteration).
+MYPBR_DEV bool wave_starting(const WaveParams& P, int gated) { return !gated || P.B.wave_state[3] != 0; }
+
+__global__ void k_generate(WaveParams P, int gated) {
+    if (!wave_starting(P, gated))
+        return;
     const int2 wv = wave_of(P);
     size_t npix = size_t(P.cam.width) * P.band_rows;
     size_t n = npix * size_t(wv.y);
@@ -230,7 +284,9 @@ __global__ void k_generate(WaveParams P) {
 }
 
 // camera.h:253-277: albedo and normal of the first non-specular surface
-__global__ void k_features(WaveParams P) {
+__global__ void k_features(WaveParams P, int gated) {
+    if (!wave_starting(P, gated))
+        return;
     size_t n = size_t(P.cam.width) * P.band_rows * size_t(wave_of(P).y);
     size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
@@ -1043,10 +1099,10 @@ struct KernelTimer {
 // A wave's start: cleared queue counters, camera rays, feature guides.
 int run_prefix(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launches, KernelTimer& T) {
     MYPBR_CUDA(cudaMemsetAsync(P.B.counters, 0, sizeof(uint32_t) * counter_words(P.B.depth_slots), st));
-    TIMED(0, (k_generate<<<L.grid_stream, 256, 0, st>>>(P)));
+    TIMED(0, (k_generate<<<L.grid_stream, 256, 0, st>>>(P, 0)));
     launches++;
     if (P.collect_features) {
-        TIMED(4, (k_features<<<L.grid_shade, 256, 0, st>>>(P)));
+        TIMED(4, (k_features<<<L.grid_shade, 256, 0, st>>>(P, 0)));
         launches++;
     }
     return MYPBR_OK;
@@ -1558,6 +1614,133 @@ int job_start(mypbr_batch_job& jb, BatchJob& j) {
     return MYPBR_OK;
 }
 
+// ----------------------------------------------- a batch as one graph
+//
+// Every job of a batch of plain renders becomes one device-side loop: a
+// conditional WHILE node whose body is one bounce (camera rays and feature
+// guides are generated only in the iteration that starts a wave) ending in
+// k_job_step, which moves to the next bounce, the next wave or the end. The
+// jobs of one scene handle follow one another (they share its buffers);
+// jobs of different handles are independent branches of the same graph, so
+// the whole batch is one graph launch and the GPU schedules the branches.
+
+// Captures job `jb` at the end of the capture running on `st` (whose graph
+// is g); the loop body is captured on `side`.
+int capture_job(const mypbr_batch_job& jb, RenderSetup& R, cudaStream_t st, cudaStream_t side, cudaGraph_t g) {
+    WaveParams& P = R.P;
+    size_t full = size_t(P.cam.width) * P.cam.height;
+    MYPBR_CUDA(cudaMemsetAsync(P.totals, 0, 3 * sizeof(unsigned long long), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film, 0, 3 * full * sizeof(double), st));
+    MYPBR_CUDA(cudaMemsetAsync(P.B.film2, 0, 3 * full * sizeof(double), st));
+    if (P.collect_features)
+        MYPBR_CUDA(cudaMemsetAsync(P.B.feat, 0, 7 * full * sizeof(double), st));
+    const int words = int(counter_words(P.B.depth_slots));
+    k_job_begin<<<1, 256, 0, st>>>(P, R.per_wave, R.spp, words);
+    cudaGraphConditionalHandle loop;
+    MYPBR_CUDA(cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault));
+    cudaStreamCaptureStatus status;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    MYPBR_CUDA(cudaStreamGetCaptureInfo(st, &status, nullptr, nullptr, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    MYPBR_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+    MYPBR_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    MYPBR_CUDA(cudaStreamBeginCaptureToGraph(side, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal));
+    uint64_t n = 0;
+    KernelTimer off;  // no events inside a graph
+    off.st = side;
+    k_generate<<<R.L.grid_stream, 256, 0, side>>>(P, 1);
+    if (P.collect_features)
+        k_features<<<R.L.grid_shade, 256, 0, side>>>(P, 1);
+    int s = run_bounce(P, R.L, side, n, off, -1);
+    if (s == MYPBR_OK)
+        k_job_step<<<1, 256, 0, side>>>(P, loop, R.per_wave, R.spp, words);
+    cudaGraph_t body = nullptr;
+    cudaError_t e = cudaStreamEndCapture(side, &body);
+    if (s != MYPBR_OK)
+        return s;
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaStreamEndCapture (batch job body)");
+    k_resolve<<<R.L.grid_stream, 256, 0, st>>>(P, R.spp, jb.radiance, jb.albedo, jb.normal, jb.variance);
+    MYPBR_CUDA(cudaGetLastError());
+    return MYPBR_OK;
+}
+
+// The batch as one graph; MYPBR_OK when it ran (every job's status set).
+int batch_one_graph(mypbr_batch_job* jobs, int n, const std::vector<mypbr_gpu_scene*>& scenes,
+                    const std::vector<std::vector<int>>& order) {
+    const size_t count = size_t(n);
+    std::vector<RenderSetup> R(count);
+    std::vector<Totals> tot(count);
+    for (int i = 0; i < n; i++) {
+        if (!jobs[i].radiance)
+            return bad_arg("mypbr_gpu_render_batch: every job needs a radiance buffer");
+        int s = prepare(jobs[i].scene, jobs[i].camera, jobs[i].opts, 0, R[size_t(i)]);
+        if (s != MYPBR_OK)
+            return s;
+        MYPBR_CUDA(cudaMalloc(&tot[size_t(i)].d, 3 * sizeof(unsigned long long)));
+    }
+    for (int i = 0; i < n; i++) {  // the buffers as they are once every job has grown them
+        WaveParams& P = R[size_t(i)].P;
+        P.B = jobs[i].scene->rb;
+        P.totals = tot[size_t(i)].d;
+    }
+    struct Owned {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaStream_t side = nullptr;
+        ~Owned() {
+            if (exec)
+                cudaGraphExecDestroy(exec);
+            if (g)
+                cudaGraphDestroy(g);
+            if (side)
+                cudaStreamDestroy(side);
+        }
+    } o;
+    MYPBR_CUDA(cudaStreamCreateWithFlags(&o.side, cudaStreamNonBlocking));
+    MYPBR_CUDA(cudaGraphCreate(&o.g, 0));
+    for (size_t k = 0; k < scenes.size(); k++) {
+        cudaStream_t st = scenes[k]->stream;
+        MYPBR_CUDA(cudaStreamBeginCaptureToGraph(st, o.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        int s = MYPBR_OK;
+        for (int i : order[k]) {
+            s = capture_job(jobs[i], R[size_t(i)], st, o.side, o.g);
+            if (s != MYPBR_OK)
+                break;
+        }
+        cudaGraph_t captured = nullptr;
+        cudaError_t e = cudaStreamEndCapture(st, &captured);
+        if (s != MYPBR_OK)
+            return s;
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaStreamEndCapture (batch)");
+    }
+    MYPBR_CUDA(cudaGraphInstantiate(&o.exec, o.g, 0));
+    cudaStream_t st = scenes[0]->stream;
+    {
+        NvtxRange range("mypbr batch graph");
+        MYPBR_CUDA(cudaGraphLaunch(o.exec, st));
+        MYPBR_CUDA(cudaStreamSynchronize(st));
+    }
+    int first_error = MYPBR_OK;
+    for (mypbr_gpu_scene* G : scenes) {
+        int s = check_device_error(G);
+        for (int i = 0; i < n; i++)
+            if (jobs[i].scene == G)
+                jobs[i].status = s;
+        if (s != MYPBR_OK && first_error == MYPBR_OK)
+            first_error = s;
+    }
+    return first_error;
+}
+
 }  // namespace
 }  // namespace mypbr_dev
 
@@ -1579,6 +1762,24 @@ extern "C" int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n) {
             it = scenes.end() - 1;
         }
         order[size_t(it - scenes.begin())].push_back(i);
+    }
+    // plain jobs on capturable streams: the whole batch as one graph launch
+    bool one_graph = n > 0 && !scenes.empty();
+    for (int i = 0; i < n && one_graph; i++)
+        one_graph = jobs[i].scene && jobs[i].camera && jobs[i].opts && jobs[i].opts->guided == 0 &&
+                    jobs[i].opts->timing == 0;
+    for (mypbr_gpu_scene* G : scenes)
+        one_graph = one_graph && graphs_allowed(G->stream);
+    if (one_graph) {
+        int s = batch_one_graph(jobs, n, scenes, order);
+        for (int i = 0; i < n; i++)
+            if (s != MYPBR_OK && jobs[i].status == MYPBR_OK)
+                jobs[i].status = s;
+        if (s != MYPBR_OK)
+            for (int i = 0; i < n; i++)
+                if (jobs[i].status == MYPBR_ERR_INVALID_ARGUMENT && s != MYPBR_ERR_INVALID_ARGUMENT)
+                    jobs[i].status = s;
+        return s;
     }
     std::vector<size_t> next(scenes.size(), 0);
     int first_error = MYPBR_OK;
