@@ -510,9 +510,11 @@ int mypbr_gpu_render_noalloc(mypbr_gpu_scene* scene, const mypbr_camera* cam, co
  * t < 0.001): for n rays (n x 8 as for mypbr_gpu_trace) the closest hit, then
  * a reflected ray and a ray going on through the surface, both started as
  * the renderer starts them (hit point moved off the surface by its FP32
- * error bound). out (n x 4): kind of the first hit (-1 none), 1 where the
- * reflected / the continued ray met the surface it left, kind of the
- * reflected ray's hit (-1 none). */
+ * error bound). out (n x 8 words): kind of the first hit (-1 none), 1 where
+ * the reflected / the continued ray met the surface it left, kind of the
+ * reflected ray's hit (-1 none), then as float bits for the first spawned ray
+ * that met its surface (else the reflected one) its t, its origin's offset,
+ * the cosine of its direction to the normal and its walk's t_min. */
 int mypbr_gpu_test_spawn(mypbr_gpu_scene* scene, const float* rays, int64_t n, int32_t* out);
 
 /* Ray batch query: closest hit of n rays against the scene, the reference's

@@ -268,13 +268,16 @@ class GpuScene:
 
     def spawn_probe(self, rays):
         """Self-intersection probe (mypbr_gpu_test_spawn): for rays (n, 8)
-        float32, (n, 4) int32 [kind of the hit, reflected ray met its surface,
-        continued ray met its surface, kind of the reflected ray's hit]."""
+        float32, (flags (n, 4) int32 [kind of the hit, reflected ray met its
+        surface, continued ray met its surface, kind of the reflected ray's
+        hit], detail (n, 4) float32 [t, origin offset, cosine to the normal,
+        t_min] of the first spawned ray that met its surface, else the
+        reflected one)."""
         rays = np.ascontiguousarray(rays, dtype=np.float32)
-        out = np.zeros((rays.shape[0], 4), dtype=np.int32)
+        out = np.zeros((rays.shape[0], 8), dtype=np.int32)
         fp, ip = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)
         check(lib().mypbr_gpu_test_spawn(self._h, rays.ctypes.data_as(fp), rays.shape[0], out.ctypes.data_as(ip)))
-        return out
+        return out[:, :4].copy(), out[:, 4:].copy().view(np.float32)
 
     def bsdf_eval(self, material, rec, r_in, wi):
         """eval rgb and scatter pdf of material at records rec (n, 16)."""

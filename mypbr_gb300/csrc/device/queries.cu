@@ -67,21 +67,26 @@ __global__ void k_bsdf(DeviceScene S, int material, const float* rec, const floa
 // Self-intersection probe of the spawned rays: each ray's closest hit, then
 // from there a reflected ray (about the geometric normal) and a ray going on
 // through the surface, both from spawn_origin with spawn_tmin as the
-// renderer starts them. out (n x 4): kind of the first hit (-1: miss), then
-// per spawned ray whether it met the surface it left: the same primitive
-// within 1e-4 of the hit point's scale, or, for a planar one (quad,
-// triangle, ground), anywhere, or, for a voxel block, the same face plane;
-// last, the kind of the reflected ray's hit.
+// renderer starts them. out (n x 8, 32-bit words): kind of the first hit
+// (-1: miss); per spawned ray whether it met the surface it left (a planar
+// primitive, quad, triangle or ground, met again at all; a voxel block's face
+// on the same plane with the same orientation; a sphere within 1e-4 of the
+// hit point's scale); the kind of the reflected ray's hit; then, as float
+// bits, for the first spawned ray that met its surface (else the reflected
+// one): its t, the origin's offset from the hit point, the cosine of its
+// direction to the normal and the t_min of its walk.
 __global__ void k_spawn_probe(DeviceScene S, const float* rays, long long n, int* out) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         const float* r = rays + 8 * k;
         float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
         HitInfo h = closest_hit<true>(S, o, d, r[6], r[7], 0);
-        int* res = out + 4 * k;
+        int* res = out + 8 * k;
         res[0] = h.prim == kMiss ? -1 : int(h.prim >> kKindShift);
         res[1] = res[2] = 0;
         res[3] = -1;
+        for (int c = 4; c < 8; c++)
+            res[c] = 0;
         if (h.prim == kMiss)
             continue;
         Surface s = make_surface(S, h, o, d);
@@ -92,20 +97,31 @@ __global__ void k_spawn_probe(DeviceScene S, const float* rays, long long n, int
         const float scale = fmaxf(1.0f, fmaxf(fabsf(s.p.x), fmaxf(fabsf(s.p.y), fabsf(s.p.z))));
         float3 dn = normalize(d);
         float3 dirs[2] = {dn - 2.0f * dot(dn, s.ng) * s.ng, dn};
+        bool noted = false;
         for (int m = 0; m < 2; m++) {
             float3 w = dirs[m];
             float3 o2 = spawn_origin(s, w);
-            HitInfo h2 = closest_hit<true>(S, o2, w, spawn_tmin(o2, w), 3.0e38f, 0);
+            float tmin = spawn_tmin(o2, w);
+            HitInfo h2 = closest_hit<true>(S, o2, w, tmin, 3.0e38f, 0);
             if (m == 0)
                 res[3] = h2.prim == kMiss ? -1 : int(h2.prim >> kKindShift);
-            if (h2.prim != h.prim)
-                continue;
-            bool self = planar || h2.t * length(w) < 1e-4f * scale;
-            if (kind == kVoxel) {
-                Surface s2 = make_surface(S, h2, o2, w);
-                self = self || (h2.b2 == h.b2 && fabsf(dot(s2.p - s.p, s.ng)) < 1e-3f);
+            bool self = false;
+            if (h2.prim == h.prim) {
+                if (kind == kVoxel) {
+                    Surface s2 = make_surface(S, h2, o2, w);
+                    self = h2.b2 == h.b2 && fabsf(dot(s2.p - s.p, s.ng)) < 1e-3f;
+                } else {
+                    self = planar || h2.t * length(w) < 1e-4f * scale;
+                }
             }
             res[1 + m] = self ? 1 : 0;
+            if ((self && !noted) || m == 0) {
+                res[4] = __float_as_int(h2.prim == kMiss ? -1.0f : h2.t);
+                res[5] = __float_as_int(length(o2 - s.p));
+                res[6] = __float_as_int(dot(w, s.ng));
+                res[7] = __float_as_int(tmin);
+                noted = noted || self;
+            }
         }
     }
 }
@@ -188,11 +204,11 @@ extern "C" int mypbr_gpu_test_spawn(mypbr_gpu_scene* G, const float* rays, int64
     MYPBR_CUDA(cudaSetDevice(G->device));
     Buf dr, dout;
     MYPBR_CUDA(cudaMalloc(&dr.p, size_t(n) * 8 * sizeof(float)));
-    MYPBR_CUDA(cudaMalloc(&dout.p, size_t(n) * 4 * sizeof(int)));
+    MYPBR_CUDA(cudaMalloc(&dout.p, size_t(n) * 8 * sizeof(int)));
     MYPBR_CUDA(cudaMemcpy(dr.p, rays, size_t(n) * 8 * sizeof(float), cudaMemcpyHostToDevice));
     int blocks = int(std::min<int64_t>((n + 127) / 128, int64_t(G->sm_count) * 16));
     k_spawn_probe<<<blocks, 128>>>(G->dev, static_cast<float*>(dr.p), (long long)n, static_cast<int*>(dout.p));
     MYPBR_CUDA(cudaGetLastError());
-    MYPBR_CUDA(cudaMemcpy(out, dout.p, size_t(n) * 4 * sizeof(int), cudaMemcpyDeviceToHost));
+    MYPBR_CUDA(cudaMemcpy(out, dout.p, size_t(n) * 8 * sizeof(int), cudaMemcpyDeviceToHost));
     return check_device_error(G);
 }
