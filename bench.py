@@ -595,7 +595,43 @@ def render_rate(mp, scene, spp, steps, warmup, guided=0, block=0, traversal=0, t
             times.append(time.perf_counter() - t0)
     G.close()
     t = statistics.median(times)
-    return st["paths"] / t / 1e6, t, st
+    return st["paths"] / t / 1e6, t, st, img
+
+
+def relmse_against_reference(mp, scene, img, spp, ref_spp, row_stride):
+    """relMSE (epsilon 0.01) of img against a ref_spp render of every
+    row_stride-th row (every row for 1), made as two independent halves whose
+    difference removes the reference's own noise."""
+    cam = scene.camera
+    cam.guided = 0
+    G = mp.GpuScene(scene)
+    h = cam.height()
+    rows = list(range(row_stride // 2, h, row_stride))
+    halves = []
+    t0 = time.perf_counter()
+    for seed in (888001, 888002):
+        cam.samples_per_pixel = ref_spp // 2
+        cam.seed = seed
+        if row_stride == 1:
+            half, _, _ = mp.render_ex(cam, G)
+        else:
+            half = np.zeros((h, cam.image_width, 3))
+            for j in rows:
+                cam.first_row, cam.row_count = j, 1
+                band, _, _ = mp.render_ex(cam, G)
+                half[j] = band[j]
+            cam.first_row, cam.row_count = 0, 0
+        halves.append(half[rows])
+    G.close()
+    cam.samples_per_pixel = spp
+    ref = 0.5 * (halves[0] + halves[1])
+    raw = rel_mse(img[rows], ref)
+    noise = reference_noise(halves[0], halves[1])
+    return {"relmse": raw - noise, "relmse_raw": raw, "reference_noise": noise, "epsilon": 0.01,
+            "reference": f"{ref_spp} spp (two independent halves), FP64 film, "
+                         + ("every row" if row_stride == 1 else f"every {row_stride}th row ({len(rows)} of {h})")
+                         + f", {time.perf_counter() - t0:.1f} s after the timed renders",
+            "of": f"the last timed frame ({spp} spp)"}
 
 
 def equal_time_relmse(mp, scene, spp, args):
@@ -649,8 +685,8 @@ def run_simple(args, workload):
             spp, cfg = 64, {"workload": "triangle_room_2m", "width": 1920, "height": 1080, "spp": 64,
                             "max_depth": 12, "triangles": 1985856, "materials": "32 principled", "lights": 16}
     tune = {} if args.autotune else None
-    value, t, st = render_rate(mp, scene, spp, args.steps, args.warmup, block=args.block, traversal=args.traversal,
-                               tune=tune, wave_paths=args.wave_paths)
+    value, t, st, img = render_rate(mp, scene, spp, args.steps, args.warmup, block=args.block,
+                                    traversal=args.traversal, tune=tune, wave_paths=args.wave_paths)
     if tune:
         cfg = dict(cfg, launch=dict(tune, chosen_by="mypbr_gpu_autotune"))
     line = {"metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
@@ -660,11 +696,14 @@ def run_simple(args, workload):
                      "shadow_per_path": st["shadow_rays"] / st["paths"],
                      "mrays_per_s": (st["extension_rays"] + st["shadow_rays"]) / t / 1e6}}
     if workload == "triangle_room" and args.hidden:
-        gv, gt, _ = render_rate(mp, scene, spp, max(1, args.steps // 2), 1, guided=args.hidden,
-                                block=args.block, traversal=args.traversal)
+        gv, gt, _, _ = render_rate(mp, scene, spp, max(1, args.steps // 2), 1, guided=args.hidden,
+                                   block=args.block, traversal=args.traversal)
         line["guided"] = {"value": gv, "ms_per_step": gt * 1e3, "hidden_layers": args.hidden,
                           "note": "untrained network at the first render; later renders train further"}
         line["equal_time"] = equal_time_relmse(mp, scene, spp, args)
+    if args.headline_ref_spp > 0:
+        line["quality"] = relmse_against_reference(mp, scene, img, spp, args.headline_ref_spp,
+                                                   1 if workload == "cornell" else 16)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         h = scene.camera.height()
