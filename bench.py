@@ -818,6 +818,7 @@ def run_hall_render(args):
     cam.guided = args.hidden
     cam.samples_per_wave = args.per_wave
     cam.seed = 1
+    cam.timing = int(args.plain_launches)
     t0 = time.perf_counter()
     img, _, st = mp.render_ex(cam, G)
     t = time.perf_counter() - t0
@@ -845,6 +846,9 @@ def main():
                                           "hall_render"], default="sphere_field")
     p.add_argument("--hall-size", type=int, default=512)
     p.add_argument("--per-wave", type=int, default=0)
+    p.add_argument("--plain-launches", action="store_true",
+                   help="hall_render: every kernel launched on its own with events (profilers cannot look inside "
+                        "graphs with conditional nodes)")
     p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3, 4],
                    help="0: the scene's default; 1: extend lanes take new rays as theirs finish; 2: the 4-wide "
                         "tree; 3: postponed leaves; 4: the plain binary walk")

@@ -298,6 +298,14 @@ MYPBR_DEV bool alpha_covers(const DeviceScene& S, int i, float b1, float b2, uin
 // MASKED = false treats an alpha-masked triangle as solid (the light-sampling
 // density of a mesh light, which ignores holes as its power estimate does,
 // mesh.h:138).
+// gamma_n = n u / (1 - n u), u = 2^-24: a bound on the relative error of n
+// FP32 roundings (PBRT 3rd ed. section 3.9.1), taken at twice the IEEE
+// figure for fast-math reciprocals and square roots.
+MYPBR_DEV float err_gamma(int n) {
+    const float u = 5.9604645e-8f;
+    return 2.0f * float(n) * u / (1.0f - float(n) * u);
+}
+
 template <bool MASKED = true>
 MYPBR_DEV bool hit_triangle(const DeviceScene& S, int i, float3 o, const TriRay& R, float tmin, float tmax, float& t,
                             float& b1, float& b2, uint64_t key = 0) {
@@ -324,6 +332,23 @@ MYPBR_DEV bool hit_triangle(const DeviceScene& S, int i, float3 o, const TriRay&
     float tt = T * inv;
     if (!(tt > tmin && tt < tmax))
         return false;
+    {
+        // a hit only where t is surely positive: t above the bound on its
+        // own rounding error (PBRT 3rd ed. section 3.9.6), from the largest
+        // sheared vertex coordinates and edge functions. On long, thin
+        // triangles that error can exceed a spawned ray's offset from the
+        // surface it leaves, which is then met again just behind the origin.
+        float zt = fabsf(R.sz) * fmaxf(fabsf(Az), fmaxf(fabsf(Bz), fabsf(Cz)));
+        float xt = fmaxf(fabsf(Ax), fmaxf(fabsf(Bx), fabsf(Cx)));
+        float yt = fmaxf(fabsf(Ay), fmaxf(fabsf(By), fabsf(Cy)));
+        float dz = err_gamma(3) * zt;
+        float dx = err_gamma(5) * (xt + zt), dy = err_gamma(5) * (yt + zt);
+        float de = 2.0f * (err_gamma(2) * xt * yt + dy * xt + dx * yt);
+        float me = fmaxf(fabsf(U), fmaxf(fabsf(V), fabsf(W)));
+        float dt = 3.0f * (err_gamma(3) * me * zt + de * zt + dz * me) * fabsf(inv);
+        if (tt <= dt)
+            return false;
+    }
     // checked before the caller's closest hit changes (mesh.h:81-86)
     if (MASKED && S.has_alpha && !alpha_covers(S, i, V * inv, W * inv, key))
         return false;
@@ -1179,10 +1204,6 @@ struct Surface {
 // bound projected on the normal, then one float step further: the exact
 // surface is then behind the origin. The bounds below are taken at twice the
 // IEEE figure: fast-math reciprocals and square roots round less tightly.
-MYPBR_DEV float err_gamma(int n) {
-    const float u = 5.9604645e-8f;
-    return 2.0f * float(n) * u / (1.0f - float(n) * u);
-}
 MYPBR_DEV float3 abs3(float3 a) { return f3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
 
 // The error of X p (+ translation) for a point p with error e: the rounding

@@ -109,7 +109,8 @@ __global__ void k_spawn_probe(DeviceScene S, const float* rays, long long n, int
             if (h2.prim == h.prim) {
                 if (kind == kVoxel) {
                     Surface s2 = make_surface(S, h2, o2, w);
-                    self = h2.b2 == h.b2 && fabsf(dot(s2.p - s.p, s.ng)) < 1e-3f;
+                    // the face codes are integers held as float bits: compare the bits
+                    self = __float_as_int(h2.b2) == __float_as_int(h.b2) && fabsf(dot(s2.p - s.p, s.ng)) < 1e-3f;
                 } else {
                     self = planar || h2.t * length(w) < 1e-4f * scale;
                 }

@@ -15,6 +15,7 @@
 // Kernels are persistent-style (grid = SMs x resident blocks, grid-stride over
 // the queue length they read on the device).
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -1764,7 +1765,9 @@ extern "C" int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n) {
         order[size_t(it - scenes.begin())].push_back(i);
     }
     // plain jobs on capturable streams: the whole batch as one graph launch
-    bool one_graph = n > 0 && !scenes.empty();
+    // (MYPBR_BATCH_ONE_GRAPH=0 keeps the per-wave host loop, for comparison)
+    const char* env = std::getenv("MYPBR_BATCH_ONE_GRAPH");
+    bool one_graph = n > 0 && !scenes.empty() && !(env && env[0] == '0');
     for (int i = 0; i < n && one_graph; i++)
         one_graph = jobs[i].scene && jobs[i].camera && jobs[i].opts && jobs[i].opts->guided == 0 &&
                     jobs[i].opts->timing == 0;
