@@ -496,6 +496,8 @@ def run_voxel_hall(args):
         return max(raw - floor, 1e-12), raw
     Gg = mp.GpuScene(scene)
     render(Gg, 64, args.hidden, 7)  # warm-up: guiding buffers and network
+    mp.guide_configure(Gg, alpha=args.guide_alpha, depths=args.guide_depths)
+    mp.guide_schedule(Gg, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps)
     curves = {}
     for name, guided in (("plain", 0), ("guided", args.hidden)):
         pts = []
@@ -560,7 +562,11 @@ def run_voxel_hall(args):
                        "reference_noise_relmse": floor,
                        "relmse": "against the reference, minus the reference's own noise (two independent "
                                  "halves; relMSE_raw is uncorrected)",
-                       "guide_hidden_layers": args.hidden, "sky": "uniform 0.35 0.45 0.6",
+                       "guide_hidden_layers": args.hidden, "guide_alpha": args.guide_alpha,
+                       "guide_depths": args.guide_depths,
+                       "guide_schedule": {"steps_early": args.steps_early, "steps_late": args.steps_late,
+                                          "max_steps": args.max_steps},
+                       "sky": "uniform 0.35 0.45 0.6",
                        "sun": "elevation 40 azimuth 160 intensity 1000 angle 0.54"},
             "plain": curves["plain"], "guided": curves["guided"],
             "guided_speedup_vs_plain": curves["plain"]["time_to_target_s"] / curves["guided"]["time_to_target_s"],
@@ -866,6 +872,11 @@ def main():
                    help="voxel_hall: spp of the repeated renders that estimate each method's error constant")
     p.add_argument("--repeats", type=int, default=10, help="voxel_hall: renders per method at --repeat-spp")
     p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
+    p.add_argument("--guide-alpha", type=float, default=0.5, help="voxel_hall: probability of sampling the mixture")
+    p.add_argument("--guide-depths", type=int, default=4, help="voxel_hall: bounces that sample the mixture")
+    p.add_argument("--steps-early", type=int, default=16, help="voxel_hall: Adam steps after each early wave")
+    p.add_argument("--steps-late", type=int, default=4, help="voxel_hall: Adam steps after each later wave")
+    p.add_argument("--max-steps", type=int, default=1500, help="voxel_hall: training steps in all")
     args = p.parse_args()
     if args.workload != "sphere_field":
         sys.path.insert(0, os.path.join(ROOT, "oracle"))

@@ -739,6 +739,13 @@ int mypbr_guide_reset(mypbr_gpu_scene* scene);
  * setting applies from the next render. */
 int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths);
 
+/* How the guiding network of this scene handle trains (no counterpart in the
+ * reference): Adam steps after each of the first 8 waves of a guided render
+ * (small waves, every path recorded; default 16), after each later wave
+ * (default 4), and the total after which recording and training stop
+ * (default 1500). Applies from the next wave. */
+int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps);
+
 /* the network's encoded inputs (n x 128, BF16 values as floats) of n
  * vertices given by their 7 scalars in [0, 1] (n x 7). */
 int mypbr_guide_test_encode(const float* scalars, int64_t n, float* out);

@@ -60,6 +60,10 @@ struct GuideState {
     // at the kGuideRecordDepth vertices the network is trained on
     float alpha = 0.5f;
     int depths = 4;
+    // training schedule (mypbr_guide_schedule): Adam steps after each of the
+    // first recorded waves and after each later one, and the total after
+    // which recording and training stop
+    int steps_early = 16, steps_late = 4, max_steps = 1500;
     // recording buffers (slot-indexed, grown with the render buffers)
     GuideRecords rec{};
     size_t rec_slots = 0;

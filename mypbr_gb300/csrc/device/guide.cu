@@ -758,6 +758,21 @@ int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths) {
     return MYPBR_OK;
 }
 
+int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps) {
+    if (!scene) {
+        set_error_message("mypbr_guide_schedule: null scene");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    if (steps_early < 0 || steps_late < 0 || max_steps < 0 || steps_early > 4096 || steps_late > 4096) {
+        set_error_message("mypbr_guide_schedule: steps must lie in [0, 4096] and max_steps be non-negative");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
+    scene->guide.steps_early = steps_early;
+    scene->guide.steps_late = steps_late;
+    scene->guide.max_steps = max_steps;
+    return MYPBR_OK;
+}
+
 int mypbr_guide_test_forward(int hidden, const float* weights, const float* inputs, int64_t n, float* out) {
     if (!weights || !inputs || !out || n < 0)
         return MYPBR_ERR_INVALID_ARGUMENT;

@@ -1265,10 +1265,8 @@ struct RenderSetup {
 // Guided renders: the first waves are small and recorded, each followed by
 // Adam steps on their vertices; later waves keep training online, lightly.
 constexpr int kGuideTrainWaves = 8;
-constexpr int kGuideStepsEarly = 16, kGuideStepsLate = 4;
 constexpr int kGuideMinSteps = 16;    // steps before the mixture is sampled at all
 constexpr int kGuideBatchTilesPerSm = 2;  // 128-sample tiles per SM in one step (39K samples on 152 SMs)
-constexpr int kGuideMaxSteps = 1500;  // no recording or training past this
 constexpr float kGuideLr = 4e-3f;
 
 int prepare(mypbr_gpu_scene* G, const mypbr_camera* cam, const mypbr_render_opts* o, int save_every, RenderSetup& R) {
@@ -1370,7 +1368,7 @@ int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int sav
         P.guided = g.steps >= kGuideMinSteps;
         P.guide_alpha = P.guided ? g.alpha : 0.0f;
         P.guide_depths = std::min(g.depths, P.max_depth);
-        P.record = g.steps < kGuideMaxSteps;
+        P.record = g.steps < g.max_steps;
         if (P.record)
             MYPBR_CUDA(cudaMemsetAsync(P.rec.count, 0, sizeof(uint32_t), st));
     }
@@ -1393,11 +1391,13 @@ int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int sav
     if (R.guided && P.record) {
         if ((s = T.begin(4)) != MYPBR_OK)
             return s;
-        s = guide_train(G, train_wave ? kGuideStepsEarly : kGuideStepsLate, kGuideBatchTilesPerSm * G->sm_count,
+        const long long left = std::max(0LL, (long long)G->guide.max_steps - G->guide.steps);
+        const int steps = (int)std::min<long long>(train_wave ? G->guide.steps_early : G->guide.steps_late, left);
+        s = guide_train(G, steps, kGuideBatchTilesPerSm * G->sm_count,
                         kGuideLr, st);
         if (s != MYPBR_OK || (s = T.end()) != MYPBR_OK)
             return s;
-        launches += 3 * (train_wave ? kGuideStepsEarly : kGuideStepsLate);
+        launches += 3 * steps;
     }
     return MYPBR_OK;
 }
