@@ -770,11 +770,13 @@ def run_batch(args):
         t_render.append(t1 - t0)
     t = statistics.median(times)
     # one by one, for the batch's gain (render only)
-    t0 = time.perf_counter()
+    per_job = []
     for job in jobs:
+        t0 = time.perf_counter()
         mp.render_batch([job])
-    torch.cuda.synchronize()
-    t_serial = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        per_job.append(time.perf_counter() - t0)
+    t_serial = sum(per_job)
     # references: each scene at 4x the spp, another seed
     refs = []
     for (sc, G), cam in zip(scenes, cams):
@@ -802,6 +804,7 @@ def run_batch(args):
                        "step": "render with albedo/normal/variance guides + 5-iteration denoise of every frame"},
             "render_ms": statistics.median(t_render) * 1e3,
             "one_by_one_render_ms": t_serial * 1e3, "batch_speedup": t_serial / statistics.median(t_render),
+            "longest_job_alone_ms": max(per_job) * 1e3,
             "rel_mse": {"epsilon": 0.01, "reference": "same scene at 4x spp, another seed",
                         "noisy_median": statistics.median(noisy), "denoised_median": statistics.median(denoised),
                         "noisy": [round(x, 5) for x in noisy], "denoised": [round(x, 5) for x in denoised]}}

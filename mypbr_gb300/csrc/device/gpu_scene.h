@@ -12,6 +12,8 @@
 
 namespace mypbr_dev {
 
+struct BatchGraphCache;  // render.cu
+
 // Scratch memory of one render: path state in slots, queues of slot indices,
 // the FP64 film. Kept on the scene handle and grown on demand.
 struct RenderBuffers {
@@ -91,6 +93,9 @@ struct mypbr_gpu_scene {
     int tuned_traversal = 0;  // 0: the scene's default (3 or 4); 1: lanes take new rays (k_extend_pt);
                               // 2: the 4-wide tree; 3: postponed leaves; 4: the plain binary walk
     bool prefer_postponed = false;  // spheres fill fewer than half the leaves: traversal 0 means 3
+    // the instantiated graph of the last batch whose first job used this
+    // handle, replayed while a batch captures to the same launches
+    mypbr_dev::BatchGraphCache* batch_graph = nullptr;
 };
 
 namespace mypbr_dev {
@@ -109,6 +114,7 @@ int cuda_fail(cudaError_t e, const char* what);
 int release_buffers(RenderBuffers& rb);
 int check_device_error(mypbr_gpu_scene* G);
 int release_guide(GuideState& g);
+void release_batch_graph(mypbr_gpu_scene* G);
 // Creates the network (seeded initial weights) if the scene has none of this size.
 int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed);
 // Mixture buffers for `mix_slots` path slots, training records for the first `rec_slots`.

@@ -1673,61 +1673,110 @@ int capture_job(const mypbr_batch_job& jb, RenderSetup& R, cudaStream_t st, cuda
     return MYPBR_OK;
 }
 
+void append_bytes(std::vector<unsigned char>& k, const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    k.insert(k.end(), c, c + n);
+}
+
+}  // namespace
+
+// The instantiated graph of a batch and the key it was captured for: every
+// job's wave parameters (all device pointers, camera, options, buffers; the
+// totals pointer left out, it belongs to the cache), launch shapes, output
+// pointers, in capture order. A batch whose key equals it would capture the
+// same nodes with the same arguments, so the graph is launched again as it is.
+struct BatchGraphCache {
+    std::vector<unsigned char> key;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long* totals = nullptr;  // 3 per job
+    ~BatchGraphCache() {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (totals)
+            cudaFree(totals);
+    }
+};
+
+void release_batch_graph(mypbr_gpu_scene* G) {
+    delete G->batch_graph;
+    G->batch_graph = nullptr;
+}
+
+namespace {
+
 // The batch as one graph; MYPBR_OK when it ran (every job's status set).
+// The graph is kept on the first job's scene handle and replayed by the next
+// batch that would capture the same launches.
 int batch_one_graph(mypbr_batch_job* jobs, int n, const std::vector<mypbr_gpu_scene*>& scenes,
                     const std::vector<std::vector<int>>& order) {
     const size_t count = size_t(n);
     std::vector<RenderSetup> R(count);
-    std::vector<Totals> tot(count);
     for (int i = 0; i < n; i++) {
         if (!jobs[i].radiance)
             return bad_arg("mypbr_gpu_render_batch: every job needs a radiance buffer");
         int s = prepare(jobs[i].scene, jobs[i].camera, jobs[i].opts, 0, R[size_t(i)]);
         if (s != MYPBR_OK)
             return s;
-        MYPBR_CUDA(cudaMalloc(&tot[size_t(i)].d, 3 * sizeof(unsigned long long)));
     }
-    for (int i = 0; i < n; i++) {  // the buffers as they are once every job has grown them
-        WaveParams& P = R[size_t(i)].P;
-        P.B = jobs[i].scene->rb;
-        P.totals = tot[size_t(i)].d;
-    }
-    struct Owned {
-        cudaGraph_t g = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        cudaStream_t side = nullptr;
-        ~Owned() {
-            if (exec)
-                cudaGraphExecDestroy(exec);
-            if (g)
-                cudaGraphDestroy(g);
-            if (side)
-                cudaStreamDestroy(side);
-        }
-    } o;
-    MYPBR_CUDA(cudaStreamCreateWithFlags(&o.side, cudaStreamNonBlocking));
-    MYPBR_CUDA(cudaGraphCreate(&o.g, 0));
+    std::vector<unsigned char> key;
     for (size_t k = 0; k < scenes.size(); k++) {
-        cudaStream_t st = scenes[k]->stream;
-        MYPBR_CUDA(cudaStreamBeginCaptureToGraph(st, o.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        int s = MYPBR_OK;
+        uint32_t jobs_here = uint32_t(order[k].size());
+        append_bytes(key, &jobs_here, sizeof(jobs_here));
         for (int i : order[k]) {
-            s = capture_job(jobs[i], R[size_t(i)], st, o.side, o.g);
-            if (s != MYPBR_OK)
-                break;
+            RenderSetup& r = R[size_t(i)];
+            r.P.B = jobs[i].scene->rb;  // the buffers as they are once every job has grown them
+            r.P.totals = nullptr;
+            append_bytes(key, &r.P, sizeof(r.P));
+            append_bytes(key, &r.L, sizeof(r.L));
+            append_bytes(key, &r.spp, sizeof(r.spp));
+            append_bytes(key, &r.per_wave, sizeof(r.per_wave));
+            void* outs[4] = {jobs[i].radiance, jobs[i].albedo, jobs[i].normal, jobs[i].variance};
+            append_bytes(key, outs, sizeof(outs));
         }
-        cudaGraph_t captured = nullptr;
-        cudaError_t e = cudaStreamEndCapture(st, &captured);
-        if (s != MYPBR_OK)
-            return s;
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaStreamEndCapture (batch)");
     }
-    MYPBR_CUDA(cudaGraphInstantiate(&o.exec, o.g, 0));
-    cudaStream_t st = scenes[0]->stream;
+    mypbr_gpu_scene* owner = scenes[0];
+    cudaStream_t st = owner->stream;
+    if (!owner->batch_graph || owner->batch_graph->key != key) {
+        release_batch_graph(owner);
+        std::unique_ptr<BatchGraphCache> c(new BatchGraphCache());
+        c->key = std::move(key);
+        MYPBR_CUDA(cudaMalloc(&c->totals, 3 * count * sizeof(unsigned long long)));
+        for (int i = 0; i < n; i++)
+            R[size_t(i)].P.totals = c->totals + 3 * size_t(i);
+        struct Owned {
+            cudaGraph_t g = nullptr;
+            cudaStream_t side = nullptr;
+            ~Owned() {
+                if (g)
+                    cudaGraphDestroy(g);
+                if (side)
+                    cudaStreamDestroy(side);
+            }
+        } o;
+        MYPBR_CUDA(cudaStreamCreateWithFlags(&o.side, cudaStreamNonBlocking));
+        MYPBR_CUDA(cudaGraphCreate(&o.g, 0));
+        for (size_t k = 0; k < scenes.size(); k++) {
+            cudaStream_t sk = scenes[k]->stream;
+            MYPBR_CUDA(cudaStreamBeginCaptureToGraph(sk, o.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            int s = MYPBR_OK;
+            for (int i : order[k]) {
+                s = capture_job(jobs[i], R[size_t(i)], sk, o.side, o.g);
+                if (s != MYPBR_OK)
+                    break;
+            }
+            cudaGraph_t captured = nullptr;
+            cudaError_t e = cudaStreamEndCapture(sk, &captured);
+            if (s != MYPBR_OK)
+                return s;
+            if (e != cudaSuccess)
+                return cuda_fail(e, "cudaStreamEndCapture (batch)");
+        }
+        MYPBR_CUDA(cudaGraphInstantiate(&c->exec, o.g, 0));
+        owner->batch_graph = c.release();
+    }
     {
         NvtxRange range("mypbr batch graph");
-        MYPBR_CUDA(cudaGraphLaunch(o.exec, st));
+        MYPBR_CUDA(cudaGraphLaunch(owner->batch_graph->exec, st));
         MYPBR_CUDA(cudaStreamSynchronize(st));
     }
     int first_error = MYPBR_OK;

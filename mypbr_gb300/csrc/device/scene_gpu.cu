@@ -898,6 +898,7 @@ int check_device_error(mypbr_gpu_scene* G) {
 extern "C" void mypbr_gpu_scene_destroy(mypbr_gpu_scene* scene) {
     if (!scene)
         return;
+    mypbr_dev::release_batch_graph(scene);
     mypbr_dev::release_buffers(scene->rb);
     mypbr_dev::release_guide(scene->guide);
     for (void* p : scene->allocations)

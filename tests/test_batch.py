@@ -61,6 +61,24 @@ def test_batch_matches_single_renders():
     torch.cuda.synchronize()
     for buf, ref in zip(bufs, expect):
         np.testing.assert_allclose(buf.cpu().numpy(), ref, rtol=1e-12, atol=1e-14)
+    # the same batch again replays the graph kept on the first handle: the
+    # outputs are rewritten from cleared films
+    for buf in bufs:
+        buf.fill_(float("nan"))
+    assert mp.render_batch(jobs) == [0] * len(jobs)
+    torch.cuda.synchronize()
+    for buf, ref in zip(bufs, expect):
+        np.testing.assert_allclose(buf.cpu().numpy(), ref, rtol=1e-12, atol=1e-14)
+    # a changed job (another seed) is captured anew, not replayed
+    cam = setups[2][2]
+    cam.seed = 77
+    changed = cam.render(setups[2][1]).radiance
+    assert np.abs(changed - expect[2]).max() > 0
+    assert mp.render_batch(jobs) == [0] * len(jobs)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(bufs[2].cpu().numpy(), changed, rtol=1e-12, atol=1e-14)
+    for k in (0, 1, 3, 4, 5):
+        np.testing.assert_allclose(bufs[k].cpu().numpy(), expect[k], rtol=1e-12, atol=1e-14)
 
 
 def test_batch_reports_a_bad_job():
