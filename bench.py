@@ -566,7 +566,7 @@ def run_voxel_hall(args):
                        "guide_depths": args.guide_depths,
                        "guide_schedule": {"steps_early": args.steps_early, "steps_late": args.steps_late,
                                           "max_steps": args.max_steps},
-                       "sky": "uniform 0.35 0.45 0.6",
+                       "sky": "atmosphere (procedural, Earth densities, lit by the sun's settings)",
                        "sun": "elevation 40 azimuth 160 intensity 1000 angle 0.54"},
             "plain": curves["plain"], "guided": curves["guided"],
             "guided_speedup_vs_plain": curves["plain"]["time_to_target_s"] / curves["guided"]["time_to_target_s"],
@@ -822,6 +822,8 @@ def run_hall_render(args):
         scene = mp.load_scene(voxel_hall_scene(d, size=args.hall_size, width=w, height=w * 9 // 16, spp=args.spp))
     G = mp.GpuScene(scene)
     mp.set_launch(G, block=args.block, traversal=args.traversal)
+    mp.guide_configure(G, alpha=args.guide_alpha, depths=args.guide_depths)
+    mp.guide_schedule(G, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps)
     cam = scene.camera
     cam.samples_per_pixel = args.spp
     cam.guided = args.hidden

@@ -285,7 +285,7 @@ def voxel_hall_scene(directory, size=512, seed=5, spp=64, width=1920, height=108
              f"max_depth {depth}",
              f"camera lookfrom {eye[0]:.3f} {eye[1]:.3f} {eye[2]:.3f}  lookat {target[0]:.3f} {target[1]:.3f} "
              f"{target[2]:.3f}  vup 0 1 0  vfov 70",
-             "sky uniform 0.35 0.45 0.6",
+             "sky atmosphere",
              "sun elevation 40 azimuth 160 intensity 1000 angle 0.54",
              "vox hall.vox"]
     path = os.path.join(directory, "voxel_hall.scene")
