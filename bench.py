@@ -496,8 +496,9 @@ def run_voxel_hall(args):
         return max(raw - floor, 1e-12), raw
     Gg = mp.GpuScene(scene)
     render(Gg, 64, args.hidden, 7)  # warm-up: guiding buffers and network
-    mp.guide_configure(Gg, alpha=args.guide_alpha, depths=args.guide_depths)
-    mp.guide_schedule(Gg, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps)
+    mp.guide_configure(Gg, alpha=args.guide_alpha, depths=args.guide_depths, alpha_deep=args.guide_alpha_deep)
+    mp.guide_schedule(Gg, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps,
+                      use_after=args.use_after)
     curves = {}
     for name, guided in (("plain", 0), ("guided", args.hidden)):
         pts = []
@@ -563,9 +564,9 @@ def run_voxel_hall(args):
                        "relmse": "against the reference, minus the reference's own noise (two independent "
                                  "halves; relMSE_raw is uncorrected)",
                        "guide_hidden_layers": args.hidden, "guide_alpha": args.guide_alpha,
-                       "guide_depths": args.guide_depths,
+                       "guide_alpha_deep": args.guide_alpha_deep, "guide_depths": args.guide_depths,
                        "guide_schedule": {"steps_early": args.steps_early, "steps_late": args.steps_late,
-                                          "max_steps": args.max_steps},
+                                          "max_steps": args.max_steps, "use_after": args.use_after},
                        "sky": "atmosphere (procedural, Earth densities, lit by the sun's settings)",
                        "sun": "elevation 40 azimuth 160 intensity 1000 angle 0.54"},
             "plain": curves["plain"], "guided": curves["guided"],
@@ -739,8 +740,8 @@ def run_batch(args):
         cam = sc.camera
         cam.samples_per_pixel = spp
         cam.collect_features = 1
-        # about 2M paths in flight per job: 64 handles' path buffers stay near 30 GB
-        cam.samples_per_wave = max(1, (2 << 20) // (cam.height() * cam.image_width))
+        # --batch-wave-paths in flight per job (2M: 64 handles' path buffers stay near 30 GB)
+        cam.samples_per_wave = max(1, args.batch_wave_paths // (cam.height() * cam.image_width))
         scenes.append((sc, G))
         cams.append(cam)
         h, w = cam.height(), cam.image_width
@@ -798,6 +799,7 @@ def run_batch(args):
             "n_gpus": 1, "steps": args.steps, "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
             "ms_per_step": t * 1e3,
             "config": {"workload": "batch_64", "scenes": len(items), "paths": int(paths),
+                       "paths_in_flight_per_job": args.batch_wave_paths,
                        "triangles": "10k..1M log-uniform (a third of the scenes)",
                        "resolutions": "64^2..1024^2 log-uniform", "spp": "16..1024 log-uniform",
                        "media": "every other scene: fog 0.02, albedo 0.9, g 0.6",
@@ -822,8 +824,9 @@ def run_hall_render(args):
         scene = mp.load_scene(voxel_hall_scene(d, size=args.hall_size, width=w, height=w * 9 // 16, spp=args.spp))
     G = mp.GpuScene(scene)
     mp.set_launch(G, block=args.block, traversal=args.traversal)
-    mp.guide_configure(G, alpha=args.guide_alpha, depths=args.guide_depths)
-    mp.guide_schedule(G, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps)
+    mp.guide_configure(G, alpha=args.guide_alpha, depths=args.guide_depths, alpha_deep=args.guide_alpha_deep)
+    mp.guide_schedule(G, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps,
+                      use_after=args.use_after)
     cam = scene.camera
     cam.samples_per_pixel = args.spp
     cam.guided = args.hidden
@@ -867,6 +870,7 @@ def main():
     p.add_argument("--autotune", action="store_true", help="cornell / triangle_room: autotuned launch settings")
     p.add_argument("--wave-paths", type=int, default=0, help="cornell / triangle_room: paths per wave (0: default)")
     p.add_argument("--batch-count", type=int, default=64)
+    p.add_argument("--batch-wave-paths", type=int, default=2 << 20, help="batch: paths in flight per job")
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--no-curve", action="store_true",
                    help="voxel_hall: skip the doubling-spp curve (the repeated renders decide the time to target)")
@@ -879,6 +883,9 @@ def main():
     p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
     p.add_argument("--guide-alpha", type=float, default=0.5, help="voxel_hall: probability of sampling the mixture")
     p.add_argument("--guide-depths", type=int, default=4, help="voxel_hall: bounces that sample the mixture")
+    p.add_argument("--guide-alpha-deep", type=float, default=-1.0,
+                   help="voxel_hall: probability of sampling the mixture after the first bounce (below 0: alpha)")
+    p.add_argument("--use-after", type=int, default=128, help="voxel_hall: training steps before the mixture is used")
     p.add_argument("--steps-early", type=int, default=16, help="voxel_hall: Adam steps after each early wave")
     p.add_argument("--steps-late", type=int, default=4, help="voxel_hall: Adam steps after each later wave")
     p.add_argument("--max-steps", type=int, default=1500, help="voxel_hall: training steps in all")

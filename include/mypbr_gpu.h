@@ -732,19 +732,23 @@ int mypbr_guide_reset(mypbr_gpu_scene* scene);
 
 /* How guided renders of this scene handle sample: at the first `depths`
  * bounces of a path (1..4096; default 4), a direction comes from the learned
- * mixture with probability `alpha` (0 < alpha < 1; default 0.5), else from
- * the BSDF, and the density used is the mixture of both (one-sample MIS), so
- * the estimate stays unbiased whatever the network outputs: the BSDF
- * proposal keeps every direction the BSDF can scatter into reachable. The
- * setting applies from the next render. */
-int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths);
+ * mixture with probability `alpha` (0 < alpha < 1; default 0.5) at the first
+ * bounce and `alpha_deep` at the later ones (0 <= alpha_deep < 1, or below 0
+ * for alpha itself; default), else from the BSDF, and the density used is the
+ * mixture of both (one-sample MIS), so the estimate stays unbiased whatever
+ * the network outputs: the BSDF proposal keeps every direction the BSDF can
+ * scatter into reachable. The setting applies from the next render. */
+int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths, float alpha_deep);
 
 /* How the guiding network of this scene handle trains (no counterpart in the
  * reference): Adam steps after each of the first 8 waves of a guided render
  * (small waves, every path recorded; default 16), after each later wave
- * (default 4), and the total after which recording and training stop
- * (default 1500). Applies from the next wave. */
-int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps);
+ * (default 4), the total after which recording and training stop (default
+ * 1500), and the steps taken before the mixture is sampled at all (default
+ * 128, the end of the first recorded waves; until then guided renders sample
+ * as plain ones). Applies from the next wave. */
+int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps,
+                         int32_t use_after);
 
 /* the network's encoded inputs (n x 128, BF16 values as floats) of n
  * vertices given by their 7 scalars in [0, 1] (n x 7). */

@@ -164,8 +164,8 @@ def lib():
                                     ctypes.POINTER(ctypes.c_uint8), ctypes.c_int]
     L.mypbr_write_image.argtypes = [ctypes.c_char_p, dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), ctypes.c_int]
     L.mypbr_guide_reset.argtypes = [vp]
-    L.mypbr_guide_configure.argtypes = [vp, ctypes.c_float, i32]
-    L.mypbr_guide_schedule.argtypes = [vp, i32, i32, i32]
+    L.mypbr_guide_configure.argtypes = [vp, ctypes.c_float, i32, ctypes.c_float]
+    L.mypbr_guide_schedule.argtypes = [vp, i32, i32, i32, i32]
     L.mypbr_guide_test_encode.argtypes = [fp, i64, fp]
     L.mypbr_gpu_test_spawn.argtypes = [vp, fp, i64, ip]
     L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
@@ -578,17 +578,19 @@ def guide_reset(gpu_scene):
     check(lib().mypbr_guide_reset(gpu_scene.handle))
 
 
-def guide_configure(gpu_scene, alpha=0.5, depths=4):
+def guide_configure(gpu_scene, alpha=0.5, depths=4, alpha_deep=-1.0):
     """Guided sampling of the handle: the mixture drawn with probability alpha
-    (0 < alpha < 1, else the BSDF) at the first `depths` bounces of a path."""
+    (0 < alpha < 1, else the BSDF) at the first bounce and alpha_deep (below
+    0: alpha) at the later ones of the first `depths` bounces of a path."""
     check(lib().mypbr_guide_configure(gpu_scene.handle if gpu_scene is not None else None, float(alpha),
-                                      int(depths)))
+                                      int(depths), float(alpha_deep)))
 
 
-def guide_schedule(gpu_scene, steps_early=16, steps_late=4, max_steps=1500):
+def guide_schedule(gpu_scene, steps_early=16, steps_late=4, max_steps=1500, use_after=128):
     """The training schedule of the scene handle's guiding network
     (mypbr_guide_schedule)."""
-    check(lib().mypbr_guide_schedule(gpu_scene.handle, int(steps_early), int(steps_late), int(max_steps)))
+    check(lib().mypbr_guide_schedule(gpu_scene.handle, int(steps_early), int(steps_late), int(max_steps),
+                                     int(use_after)))
 
 
 def rebuild_bvh(gpu_scene):

@@ -51,7 +51,8 @@ struct GuideState {
     float* v = nullptr;
     float* grad = nullptr;
     float* stats = nullptr;          // [0] loss sum, [1] weight sum of the current batch
-    __nv_bfloat16* scratch = nullptr;  // per training CTA: transposed activations of one tile
+    __nv_bfloat16* scratch = nullptr;  // per training group: the layer inputs of its tile
+    float* partial = nullptr;          // per training group: its FP32 weight gradients
     int train_ctas = 0;
     long long steps = 0;             // Adam steps taken
     float3 box_lo{}, box_inv{};      // box of the position encoding: the scene's, then where paths go
@@ -61,11 +62,13 @@ struct GuideState {
     // the first `depths` bounces of a path (mypbr_guide_configure); by default
     // at the kGuideRecordDepth vertices the network is trained on
     float alpha = 0.5f;
+    float alpha_deep = -1.0f;  // alpha at bounces after the first (below 0: alpha)
     int depths = 4;
     // training schedule (mypbr_guide_schedule): Adam steps after each of the
     // first recorded waves and after each later one, and the total after
     // which recording and training stop
     int steps_early = 16, steps_late = 4, max_steps = 1500;
+    int use_after = 128;  // steps before the mixture is sampled at all
     // recording buffers (slot-indexed, grown with the render buffers)
     GuideRecords rec{};
     size_t rec_slots = 0;

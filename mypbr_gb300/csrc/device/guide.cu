@@ -3,17 +3,10 @@
 //
 // One training step: k_guide_prep sums the sample weights of a batch drawn
 // from the recorded vertices; k_guide_train runs forward and backward for
-// tiles of 128 samples (one CTA of 128 threads per tile, a thread per
-// sample) and adds the weight gradients into FP32 sums; k_guide_adam updates
-// the FP32 master weights and rewrites the BF16 copies the kernels read.
-//
-// Backward per matrix l with input H (batch x in) and output gradient dZ
-// (batch x 64), both BF16:
-//   dW^T = H^T dZ   (tcgen05.mma M = 128 (in, zero-padded), N = 64, K = 128 batch)
-//   dX   = dZ W     (M = 128 batch, N = 64 in, K = 64), masked by the ReLU of
-//                   the layer below to give that layer's dZ.
-// The transposed activations H^T of each layer are kept in a per-CTA scratch
-// area in global memory (L2 resident) between the forward and backward pass.
+// tiles of 128 samples (groups of 128 threads, a thread per sample, sharing
+// the CTA's resident weights) and adds the weight gradients into per-CTA
+// FP32 partial sums; k_guide_adam sums the partials, updates the FP32 master
+// weights and rewrites the BF16 copies the kernels read.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -26,8 +19,6 @@
 namespace mypbr_dev {
 
 namespace {
-
-constexpr size_t kTrainSmem = 32768 + 16384 + 32768 + 16384 + 64;
 
 MYPBR_DEV uint32_t hash_u32(uint32_t a, uint32_t b) {
     uint64_t z = mix64((uint64_t(a) << 32) ^ b ^ 0x5bd1e995ull);
@@ -137,40 +128,87 @@ MYPBR_DEV void store_col_bf16(__nv_bfloat16* tileT, int row, int features, const
         tileT[canon(f, row, 128)] = __float2bfloat16_rn(v[f]);
 }
 
+// Training CTA: kTrainGroups groups of 128 threads (a thread per sample row),
+// each group on its own tile of 128 samples, all sharing one resident copy
+// of the weights. Shared memory: the weights (canonical [64 out][in] per
+// matrix), then per group a 128 x 128 activation tile and a 128 x 64
+// output-gradient tile, then the groups' mbarriers and the TMEM address.
+constexpr int kTrainGroups = 2;
+// (16 KB of slack after the barriers: every operand an MMA addresses lies in
+// its tile, the slack keeps any layout misreading inside the allocation)
+MYPBR_HD size_t train_smem(int hidden) {
+    return size_t(guide_params(hidden)) * 2 + size_t(kTrainGroups) * (128 * 128 + 128 * 64) * 2 + 64 + 16384;
+}
+// Per group of a training CTA: the layer inputs of its current tile kept for
+// the backward pass (canonical K-major, the input encoding then each hidden
+// layer's activations), in global memory (L2 resident).
+MYPBR_HD size_t train_scratch_per_group(int hidden) { return size_t(128) * 128 + size_t(hidden) * 128 * 64; }
+MYPBR_HD size_t train_scratch_offset(int l) { return l == 0 ? 0 : size_t(128) * 128 + size_t(l - 1) * 128 * 64; }
+
+// Copies row `row` of a canonical K-major BF16 tile with K columns from src
+// to dst (K / 8 16-byte chunks, the row's own).
+MYPBR_DEV void copy_row_u4(__nv_bfloat16* dst, const __nv_bfloat16* src, int row, int K) {
+    for (int b = 0; b < K / 8; b++) {
+        const int e = canon(row, 8 * b, K);
+        *reinterpret_cast<uint4*>(dst + e) = *reinterpret_cast<const uint4*>(src + e);
+    }
+}
+
+// One training step's forward and backward passes. Per layer l with input H
+// (batch x in) and output gradient dZ (batch x 64), both BF16 in shared
+// memory:
+//   forward  Z = H W^T           (M = 128 batch, N = 64, K = in; A = H K-major,
+//                                 B = W K-major)
+//   dW^T = H^T dZ                (M = 128 in (rows past `in` unused), N = 64,
+//                                 K = 128 batch; A = the H tile read MN-major,
+//                                 B = the dZ tile read MN-major)
+//   dX   = dZ W                  (M = 128 batch, N = in, K = 64; A = dZ
+//                                 K-major, B = W read MN-major)
+// so no transposed copy of anything is made. Each group writes its tiles'
+// dW into its own FP32 partial ([out][in] per matrix; plain stores for its
+// first tile, additions by the same thread for later ones, zeros if it had
+// none); the Adam kernel sums the groups' partials.
 template <int HIDDEN, class Src>
-__global__ void __launch_bounds__(128) k_guide_train(GuideNetView net, Src src, long long rows,
-                                                     __nv_bfloat16* scratch, float* loss_sum) {
+__global__ void __launch_bounds__(128 * kTrainGroups) k_guide_train(GuideNetView net, Src src, long long rows,
+                                                                    __nv_bfloat16* scratch, float* partial,
+                                                                    float* loss_sum) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(smem);  // 128 x 128
-    __nv_bfloat16* Wb = A + 128 * 128;                            // 64 x 128
-    __nv_bfloat16* HT = Wb + 64 * 128;                            // 128 x 128
-    __nv_bfloat16* DZT = HT + 128 * 128;                          // 64 x 128
-    uint64_t* bar = reinterpret_cast<uint64_t*>(DZT + 64 * 128);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
-    __nv_bfloat16* scr = scratch + size_t(blockIdx.x) * (HIDDEN + 1) * 128 * 128;
-    const int row = threadIdx.x, warp = threadIdx.x >> 5;
-    // rows 64..127 of HT stay zero for the 64-wide layers (they pad M to 128)
-    for (int k = threadIdx.x; k < 64 * 128 / 8; k += blockDim.x)
-        reinterpret_cast<uint4*>(HT + 64 * 128)[k] = make_uint4(0, 0, 0, 0);
+    constexpr int P = kGuideWidth * kGuideIn + HIDDEN * kGuideWidth * kGuideWidth;
+    const int group = threadIdx.x >> 7, row = threadIdx.x & 127, warp = threadIdx.x >> 5;
+    __nv_bfloat16* W = reinterpret_cast<__nv_bfloat16*>(smem);
+    __nv_bfloat16* A = W + P + size_t(group) * (128 * 128 + 128 * 64);  // 128 x 128
+    __nv_bfloat16* DZ = A + 128 * 128;                                   // 128 x 64
+    uint64_t* bars = reinterpret_cast<uint64_t*>(W + P + size_t(kTrainGroups) * (128 * 128 + 128 * 64));
+    uint64_t* bar = bars + group;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kTrainGroups);
+    float* part = partial + (size_t(blockIdx.x) * kTrainGroups + group) * P;
+    __nv_bfloat16* scr = scratch + (size_t(blockIdx.x) * kTrainGroups + group) * train_scratch_per_group(HIDDEN);
+    {
+        const uint4* g = reinterpret_cast<const uint4*>(net.w);
+        uint4* w = reinterpret_cast<uint4*>(W);
+        for (int k = threadIdx.x; k < P / 8; k += blockDim.x)
+            w[k] = g[k];
+    }
     if (warp == 0)
-        tc::tmem_alloc(tmem_slot, 128);
-    if (threadIdx.x == 0)
+        tc::tmem_alloc(tmem_slot, 128 * kTrainGroups);
+    if (row == 0)
         tc::bar_init(bar, 1);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    const uint32_t tmem = *tmem_slot;
+    const uint32_t t_acc = *tmem_slot + uint32_t(128 * group), t_dw = t_acc + 64;
+    const int bar_id = 1 + group;  // named barrier 0 is __syncthreads
     uint32_t phase = 0;
-    const uint32_t idesc = tc::idesc_bf16(128, 64);
-    bool failed = false;
+    bool failed = false, first = true;
     float loss_acc = 0.0f;
-    long long tiles = (rows + 127) / 128;
-    // Issues the MMAs (thread 0), then every thread waits for them; false on a timeout.
+    const long long tiles = (rows + 127) / 128;
+    // Every thread of the group waits for the MMAs of the group's issuing
+    // thread; false (error recorded) on a timeout.
     auto wait_mma = [&]() {
         bool ok = tc::bar_wait(bar, phase);
         phase ^= 1;
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0)
+        if (tc::group_sync_or(bar_id, 128, !ok)) {
+            if (row == 0)
                 atomicCAS(net.error, 0, 3);
             tc::bar_wait(bar, phase ^ 1);  // once more, bounded, for the MMAs in flight
             return false;
@@ -178,36 +216,26 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideNetView net, Src src, 
         tc::fence_after();
         return true;
     };
-    for (long long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
-        long long i = tile * 128 + row;
-        long long src_i = i < rows ? i : -1;
+    for (long long tile = (long long)blockIdx.x * kTrainGroups + group; tile < tiles && !failed;
+         tile += (long long)gridDim.x * kTrainGroups) {
+        const long long i = tile * 128 + row;
+        const long long src_i = i < rows ? i : -1;
         src.fill(src_i, A, row);
-        {  // H_0^T: this row's 128 inputs, read back from the tile
-            float v[128];
-#pragma unroll
-            for (int b = 0; b < 16; b++) {
-                uint4 u = *reinterpret_cast<const uint4*>(A + canon(row, 8 * b, 128));
-                const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&u);
-#pragma unroll
-                for (int e = 0; e < 8; e++)
-                    v[8 * b + e] = __bfloat162float(h[e]);
-            }
-            store_col_bf16(scr, row, 128, v);
-        }
+        copy_row_u4(scr, A, row, kGuideIn);  // the encoding, for layer 0's weight gradient
         uint32_t mask[2 * HIDDEN + 2];
         float dz[64];
         // ---- forward
-#pragma unroll
+#pragma unroll 1
         for (int l = 0; l <= HIDDEN; l++) {
             const int K = guide_in(l);
-            copy_u4(Wb, net.w + guide_offset(l), 64 * K * 2);
             tc::fence_smem();
-            __syncthreads();
-            if (threadIdx.x == 0) {
+            tc::group_sync(bar_id, 128);
+            if (row == 0) {
                 tc::fence_after();
-                uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(Wb);
+                const uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(W + guide_offset(l));
+                const uint32_t idesc = tc::idesc_bf16(128, 64);
                 for (int s = 0; s < K / 16; s++)
-                    tc::mma(tmem, tc::desc(a0 + 256 * s, 128, K * 16), tc::desc(b0 + 256 * s, 128, K * 16), idesc,
+                    tc::mma(t_acc, tc::desc(a0 + 256 * s, 128, K * 16), tc::desc(b0 + 256 * s, 128, K * 16), idesc,
                             s > 0);
                 tc::commit(bar);
             }
@@ -216,28 +244,20 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideNetView net, Src src, 
                 break;
             }
             float v[64];
-            tc::tmem_row64(tmem, 0, v);
+            tc::tmem_row64(t_acc, 0, v);
             tc::fence_before();
             if (l < HIDDEN) {
                 uint32_t m0 = 0, m1 = 0;
 #pragma unroll
-                for (int k = 0; k < 64; k++) {
-                    bool on = v[k] > 0.0f;
-                    if (k < 32)
-                        m0 |= on ? (1u << k) : 0u;
-                    else
-                        m1 |= on ? (1u << (k - 32)) : 0u;
-                    v[k] = on ? v[k] : 0.0f;
+                for (int k = 0; k < 32; k++) {
+                    m0 |= v[k] > 0.0f ? (1u << k) : 0u;
+                    m1 |= v[k + 32] > 0.0f ? (1u << k) : 0u;
                 }
                 mask[2 * l] = m0;
                 mask[2 * l + 1] = m1;
-                store_row_bf16(A, row, kGuideWidth, 0, v);
-                // the stored BF16 values, transposed, for this layer's weight gradient
-                float r[64];
-#pragma unroll
-                for (int k = 0; k < 64; k++)
-                    r[k] = __bfloat162float(__float2bfloat16_rn(v[k]));
-                store_col_bf16(scr + size_t(l + 1) * 128 * 128, row, 64, r);
+                store_row_bf16_relu(A, row, v);  // the next layer's input, K = 64
+                if (l + 1 < HIDDEN)              // the last one stays in A for the backward pass
+                    copy_row_u4(scr + train_scratch_offset(l + 1), A, row, kGuideWidth);
             } else {
                 loss_acc += src.dout(src_i, v, dz);
             }
@@ -245,61 +265,82 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideNetView net, Src src, 
         if (failed)
             break;
         // ---- backward
-#pragma unroll
+        uint4 pre[8];  // the next layer's input row (its first 64 values), read while this layer's MMAs run
+#pragma unroll 1
         for (int l = HIDDEN; l >= 0; l--) {
             const int in = guide_in(l);
-            store_row_bf16(A, row, kGuideWidth, 0, dz);  // dZ [batch][64]
-            store_col_bf16(DZT, row, 64, dz);           // dZ^T [64][batch]
-            copy_u4(Wb, net.wt + guide_offset(l), in * 64 * 2);
-            copy_u4(HT, scr + size_t(l) * 128 * 128, in * 128 * 2);
+            store_row_bf16(DZ, row, kGuideWidth, 0, dz);
+            if (l < HIDDEN) {  // this layer's input, back from the scratch
+#pragma unroll
+                for (int b = 0; b < 8; b++)
+                    *reinterpret_cast<uint4*>(A + canon(row, 8 * b, in)) = pre[b];
+                for (int b = 8; b < in / 8; b++) {
+                    const int e = canon(row, 8 * b, in);
+                    *reinterpret_cast<uint4*>(A + e) =
+                        *reinterpret_cast<const uint4*>(scr + train_scratch_offset(l) + e);
+                }
+            }
             tc::fence_smem();
-            __syncthreads();
-            if (threadIdx.x == 0) {
+            tc::group_sync(bar_id, 128);
+            if (row == 0) {
                 tc::fence_after();
-                uint32_t h0 = tc::smem_u32(HT), z0 = tc::smem_u32(DZT);
+                const uint32_t h0 = tc::smem_u32(A), z0 = tc::smem_u32(DZ), w0 = tc::smem_u32(W + guide_offset(l));
+                // dW^T: K = batch in steps of 16 rows (two row groups of each tile)
+                const uint32_t id_w = tc::idesc_bf16_mn(128, 64, true, true);
                 for (int s = 0; s < 8; s++)
-                    tc::mma(tmem + 64, tc::desc(h0 + 256 * s, 128, 2048), tc::desc(z0 + 256 * s, 128, 2048), idesc,
-                            s > 0);
-                if (l > 0) {
-                    uint32_t a0 = tc::smem_u32(A), w0 = tc::smem_u32(Wb);
+                    tc::mma(t_dw, tc::desc(h0 + uint32_t(s) * 32u * uint32_t(in), uint32_t(in) * 16u, 128),
+                            tc::desc(z0 + uint32_t(s) * 2048u, 1024, 128), id_w, s > 0);
+                if (l > 0) {  // dX: K = the 64 outputs in steps of 16 (two row groups of W)
+                    const uint32_t id_x = tc::idesc_bf16_mn(128, 64, false, true);
                     for (int s = 0; s < 4; s++)
-                        tc::mma(tmem, tc::desc(a0 + 256 * s, 128, 1024), tc::desc(w0 + 256 * s, 128, 1024), idesc,
+                        tc::mma(t_acc, tc::desc(z0 + 256u * uint32_t(s), 128, 1024),
+                                tc::desc(w0 + uint32_t(s) * 32u * uint32_t(in), uint32_t(in) * 16u, 128), id_x,
                                 s > 0);
                 }
                 tc::commit(bar);
+            }
+            if (l > 0) {
+                const int nin = guide_in(l - 1);
+                const __nv_bfloat16* src_row = scr + train_scratch_offset(l - 1);
+#pragma unroll
+                for (int b = 0; b < 8; b++)
+                    pre[b] = *reinterpret_cast<const uint4*>(src_row + canon(row, 8 * b, nin));
             }
             if (!wait_mma()) {
                 failed = true;
                 break;
             }
             float gw[64];
-            tc::tmem_row64(tmem, 64, gw);  // row = input feature `row`
-            if (row < in) {
-                float* gbase = net.grad + guide_offset(l) + row;
-#pragma unroll 4
-                for (int j = 0; j < 64; j++)
-                    if (gw[j] != 0.0f)
-                        atomicAdd(gbase + j * in, gw[j]);
+            tc::tmem_row64(t_dw, 0, gw);  // lane = input feature `row`
+            if (row < in) {  // element (j, row) of the [out][in] matrix: a warp writes 32 neighbours
+                float* gp = part + guide_offset(l) + row;
+                if (first) {
+#pragma unroll 8
+                    for (int j = 0; j < 64; j++)
+                        gp[j * in] = gw[j];
+                } else {
+#pragma unroll 8
+                    for (int j = 0; j < 64; j++)
+                        gp[j * in] += gw[j];
+                }
             }
             if (l > 0) {
                 float dx[64];
-                tc::tmem_row64(tmem, 0, dx);
-                uint32_t m0 = mask[2 * (l - 1)], m1 = mask[2 * (l - 1) + 1];
+                tc::tmem_row64(t_acc, 0, dx);
+                const uint32_t m0 = mask[2 * (l - 1)], m1 = mask[2 * (l - 1) + 1];
 #pragma unroll
-                for (int k = 0; k < 64; k++) {
-                    bool on = k < 32 ? ((m0 >> k) & 1u) : ((m1 >> (k - 32)) & 1u);
-                    dz[k] = on ? dx[k] : 0.0f;
+                for (int k = 0; k < 32; k++) {
+                    dz[k] = (m0 >> k) & 1u ? dx[k] : 0.0f;
+                    dz[k + 32] = (m1 >> k) & 1u ? dx[k + 32] : 0.0f;
                 }
             }
             tc::fence_before();
-            if (l == 0) {  // layer 0 filled all of HT: clear the padding rows again
-                __syncthreads();
-                for (int k = threadIdx.x; k < 64 * 128 / 8; k += blockDim.x)
-                    reinterpret_cast<uint4*>(HT + 64 * 128)[k] = make_uint4(0, 0, 0, 0);
-            }
         }
+        first = false;
     }
-    // warp-reduced loss
+    if (first)  // no tile for this group: its partial is zero
+        for (int k = row; k < P / 4; k += 128)
+            reinterpret_cast<float4*>(part)[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int o = 16; o > 0; o >>= 1)
         loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
     if ((threadIdx.x & 31) == 0 && loss_sum && loss_acc != 0.0f)
@@ -308,7 +349,17 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideNetView net, Src src, 
     __syncthreads();
     if (warp == 0) {
         tc::fence_after();
-        tc::tmem_free(tmem, 128);
+        tc::tmem_free(*tmem_slot, 128 * kTrainGroups);
+    }
+}
+
+// Sums the training groups' partial gradients into grad (test entry points).
+__global__ void k_guide_sum_partials(const float* partial, int ctas, int params, float* grad) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < params; p += gridDim.x * blockDim.x) {
+        float acc = 0.0f;
+        for (int c = 0; c < ctas; c++)
+            acc += partial[size_t(c) * params + p];
+        grad[p] = acc;
     }
 }
 
@@ -342,13 +393,17 @@ MYPBR_DEV void param_coords(int p, int& l, int& j, int& t, int& in) {
 
 // Adam (Kingma and Ba 2015) on the FP32 masters, then the BF16 copies.
 // lr == 0 only republishes the copies.
-__global__ void k_guide_adam(float* master, float* m, float* v, float* grad, __nv_bfloat16* w,
+// The gradient is the sum of the training groups' partials.
+__global__ void k_guide_adam(float* master, float* m, float* v, const float* partial, int ctas, __nv_bfloat16* w,
                              __nv_bfloat16* wt, int params, float lr, float b1t, float b2t) {
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < params; p += gridDim.x * blockDim.x) {
         float x = master[p];
         if (lr > 0.0f) {
-            float g = grad[p];
+            float g = 0.0f;
+#pragma unroll 8
+            for (int c = 0; c < ctas; c++)
+                g += partial[size_t(c) * params + p];
             g = isfinite(g) ? g : 0.0f;
             float mm = b1 * m[p] + (1.0f - b1) * g;
             float vv = b2 * v[p] + (1.0f - b2) * g * g;
@@ -357,7 +412,6 @@ __global__ void k_guide_adam(float* master, float* m, float* v, float* grad, __n
             x -= lr * (mm / (1.0f - b1t)) / (sqrtf(vv / (1.0f - b2t)) + eps);
             master[p] = x;
         }
-        grad[p] = 0.0f;
         int l, j, t, in;
         param_coords(p, l, j, t, in);
         __nv_bfloat16 h = __float2bfloat16_rn(x);
@@ -400,24 +454,28 @@ int set_smem(Kernel k, size_t bytes) {
 }
 
 template <int H, class Src>
-int launch_train(GuideNetView net, Src src, long long rows, int ctas, __nv_bfloat16* scratch, float* loss,
-                 cudaStream_t st) {
+int launch_train(GuideNetView net, Src src, long long rows, int ctas, __nv_bfloat16* scratch, float* partial,
+                 float* loss, cudaStream_t st) {
     auto k = k_guide_train<H, Src>;
-    int rc = set_smem(k, kTrainSmem);
+    const size_t smem = train_smem(H);
+    int rc = set_smem(k, smem);
     if (rc != MYPBR_OK)
         return rc;
-    k<<<ctas, 128, kTrainSmem, st>>>(net, src, rows, scratch, loss);
+    k<<<ctas, 128 * kTrainGroups, smem, st>>>(net, src, rows, scratch, partial, loss);
     MYPBR_CUDA(cudaGetLastError());
     return MYPBR_OK;
 }
 
+// `ctas` training CTAs (each kTrainGroups tiles at a time); scratch holds
+// ctas * kTrainGroups * train_scratch_per_group(hidden) BF16 values and
+// partial ctas * kTrainGroups * params floats.
 template <class Src>
 int train_dispatch(int hidden, GuideNetView net, Src src, long long rows, int ctas, __nv_bfloat16* scratch,
-                   float* loss, cudaStream_t st) {
+                   float* partial, float* loss, cudaStream_t st) {
     switch (hidden) {
-        case 2: return launch_train<2>(net, src, rows, ctas, scratch, loss, st);
-        case 4: return launch_train<4>(net, src, rows, ctas, scratch, loss, st);
-        case 8: return launch_train<8>(net, src, rows, ctas, scratch, loss, st);
+        case 2: return launch_train<2>(net, src, rows, ctas, scratch, partial, loss, st);
+        case 4: return launch_train<4>(net, src, rows, ctas, scratch, partial, loss, st);
+        case 8: return launch_train<8>(net, src, rows, ctas, scratch, partial, loss, st);
         default:
             set_error_message("guiding networks have 2, 4 or 8 hidden layers");
             return MYPBR_ERR_UNSUPPORTED;
@@ -473,7 +531,7 @@ int temp_net(TempNet& T, int hidden, const float* weights) {
     MYPBR_CUDA(cudaMemcpy(g.master, weights, P * 4, cudaMemcpyHostToDevice));
     MYPBR_CUDA(cudaMemset(g.grad, 0, P * 4));
     MYPBR_CUDA(cudaMemset(T.err, 0, 4));
-    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
+    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, nullptr, 0, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
     MYPBR_CUDA(cudaGetLastError());
     return MYPBR_OK;
 }
@@ -505,7 +563,7 @@ __global__ void k_wait_probe(int* err) {
 }  // namespace
 
 int release_guide(GuideState& g) {
-    void* ptrs[] = {g.w, g.wt, g.master, g.m, g.v, g.grad, g.stats, g.scratch, g.rec.in0, g.rec.in1, g.rec.dir,
+    void* ptrs[] = {g.w, g.wt, g.master, g.m, g.v, g.grad, g.stats, g.scratch, g.partial, g.rec.in0, g.rec.in1, g.rec.dir,
                     g.rec.fac, g.rec.mark, g.rec.bnext, g.rec.fin, g.rec.list, g.rec.count, g.packed};
     for (void* p : ptrs)
         if (p)
@@ -644,14 +702,15 @@ int guide_ensure(mypbr_gpu_scene* G, int hidden, unsigned long long seed) {
     int rc;
     if ((rc = dalloc(g.w, P)) || (rc = dalloc(g.wt, P)) || (rc = dalloc(g.master, P)) || (rc = dalloc(g.m, P)) ||
         (rc = dalloc(g.v, P)) || (rc = dalloc(g.grad, P)) || (rc = dalloc(g.stats, 4)) ||
-        (rc = dalloc(g.scratch, size_t(g.train_ctas) * (hidden + 1) * 128 * 128)))
+        (rc = dalloc(g.scratch, size_t(g.train_ctas) * kTrainGroups * train_scratch_per_group(hidden))) ||
+        (rc = dalloc(g.partial, size_t(g.train_ctas) * kTrainGroups * P)))
         return rc;
     std::vector<float> w0 = initial_weights(hidden, seed);
     MYPBR_CUDA(cudaMemcpy(g.master, w0.data(), P * 4, cudaMemcpyHostToDevice));
     MYPBR_CUDA(cudaMemset(g.m, 0, P * 4));
     MYPBR_CUDA(cudaMemset(g.v, 0, P * 4));
     MYPBR_CUDA(cudaMemset(g.grad, 0, P * 4));
-    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
+    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, nullptr, 0, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
     MYPBR_CUDA(cudaGetLastError());
     g.steps = 0;
     set_scene_box(G);
@@ -704,12 +763,13 @@ int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaSt
         MYPBR_CUDA(cudaMemsetAsync(g.stats, 0, 4 * sizeof(float), st));
         k_guide_prep<<<G->sm_count * 2, 256, 0, st>>>(src, rows, g.stats);
         MYPBR_CUDA(cudaGetLastError());
-        int rc = train_dispatch(g.hidden, net, src, rows, g.train_ctas, g.scratch, g.stats, st);
+        int rc = train_dispatch(g.hidden, net, src, rows, g.train_ctas, g.scratch, g.partial, g.stats, st);
         if (rc != MYPBR_OK)
             return rc;
         g.steps++;
         float b1t = std::pow(0.9f, float(g.steps)), b2t = std::pow(0.99f, float(g.steps));
-        k_guide_adam<<<(g.params + 255) / 256, 256, 0, st>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, lr,
+        k_guide_adam<<<(g.params + 255) / 256, 256, 0, st>>>(g.master, g.m, g.v, g.partial,
+                                                            g.train_ctas * kTrainGroups, g.w, g.wt, g.params, lr,
                                                             b1t, b2t);
         MYPBR_CUDA(cudaGetLastError());
     }
@@ -736,7 +796,7 @@ int mypbr_guide_reset(mypbr_gpu_scene* scene) {
     MYPBR_CUDA(cudaMemset(g.m, 0, P * 4));
     MYPBR_CUDA(cudaMemset(g.v, 0, P * 4));
     MYPBR_CUDA(cudaMemset(g.grad, 0, P * 4));
-    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, g.grad, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
+    k_guide_adam<<<64, 256>>>(g.master, g.m, g.v, nullptr, 0, g.w, g.wt, g.params, 0.0f, 0.0f, 0.0f);
     MYPBR_CUDA(cudaGetLastError());
     MYPBR_CUDA(cudaDeviceSynchronize());
     g.steps = 0;
@@ -744,32 +804,38 @@ int mypbr_guide_reset(mypbr_gpu_scene* scene) {
     return MYPBR_OK;
 }
 
-int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths) {
+int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths, float alpha_deep) {
     if (!scene) {
         set_error_message("mypbr_guide_configure: null scene");
         return MYPBR_ERR_INVALID_ARGUMENT;
     }
-    if (!(alpha > 0.0f && alpha < 1.0f) || depths < 1 || depths > 4096) {
-        set_error_message("mypbr_guide_configure: alpha must lie in (0, 1) and depths in [1, 4096]");
+    if (!(alpha > 0.0f && alpha < 1.0f) || depths < 1 || depths > 4096 || !(alpha_deep < 1.0f)) {
+        set_error_message("mypbr_guide_configure: alpha must lie in (0, 1), alpha_deep below 1 and depths in "
+                          "[1, 4096]");
         return MYPBR_ERR_INVALID_ARGUMENT;
     }
     scene->guide.alpha = alpha;
+    scene->guide.alpha_deep = alpha_deep < 0.0f ? -1.0f : alpha_deep;
     scene->guide.depths = depths;
     return MYPBR_OK;
 }
 
-int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps) {
+int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps,
+                         int32_t use_after) {
     if (!scene) {
         set_error_message("mypbr_guide_schedule: null scene");
         return MYPBR_ERR_INVALID_ARGUMENT;
     }
-    if (steps_early < 0 || steps_late < 0 || max_steps < 0 || steps_early > 4096 || steps_late > 4096) {
-        set_error_message("mypbr_guide_schedule: steps must lie in [0, 4096] and max_steps be non-negative");
+    if (steps_early < 0 || steps_late < 0 || max_steps < 0 || steps_early > 4096 || steps_late > 4096 ||
+        use_after < 0) {
+        set_error_message("mypbr_guide_schedule: steps must lie in [0, 4096], max_steps and use_after be "
+                          "non-negative");
         return MYPBR_ERR_INVALID_ARGUMENT;
     }
     scene->guide.steps_early = steps_early;
     scene->guide.steps_late = steps_late;
     scene->guide.max_steps = max_steps;
+    scene->guide.use_after = use_after;
     return MYPBR_OK;
 }
 
@@ -815,20 +881,25 @@ int mypbr_guide_test_backward(int hidden, const float* weights, const float* inp
     int rc = temp_net(T, hidden, weights);
     if (rc != MYPBR_OK)
         return rc;
-    float *d_in = nullptr, *d_g = nullptr;
+    float *d_in = nullptr, *d_g = nullptr, *partial = nullptr;
     __nv_bfloat16* scratch = nullptr;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     long long tiles = (n + 127) / 128;
-    int ctas = int(std::min<long long>(std::max<long long>(tiles, 1), sms));
+    // fewer CTAs than tiles, so that groups also take several tiles in turn
+    int ctas = int(std::min<long long>(std::max<long long>((tiles + 2 * kTrainGroups - 1) / (2 * kTrainGroups), 1),
+                                       sms));
     if ((rc = dalloc(d_in, size_t(n) * kGuideIn + 1)) || (rc = dalloc(d_g, size_t(n) * kGuideOut + 1)) ||
-        (rc = dalloc(scratch, size_t(ctas) * (hidden + 1) * 128 * 128)))
+        (rc = dalloc(scratch, size_t(ctas) * kTrainGroups * train_scratch_per_group(hidden))) ||
+        (rc = dalloc(partial, size_t(ctas) * kTrainGroups * T.g.params)))
         return rc;
     cudaMemcpy(d_in, inputs, size_t(n) * kGuideIn * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(d_g, dout, size_t(n) * kGuideOut * 4, cudaMemcpyHostToDevice);
-    rc = train_dispatch(hidden, view_of(T.g, T.err), GivenSource{d_in, d_g}, n, ctas, scratch, nullptr, 0);
+    rc = train_dispatch(hidden, view_of(T.g, T.err), GivenSource{d_in, d_g}, n, ctas, scratch, partial, nullptr, 0);
     if (rc == MYPBR_OK) {
+        k_guide_sum_partials<<<(T.g.params + 255) / 256, 256>>>(partial, ctas * kTrainGroups, T.g.params,
+                                                                T.g.grad);
         cudaError_t e = cudaDeviceSynchronize();
         rc = e != cudaSuccess ? cuda_fail(e, "k_guide_train") : read_error(T.err);
     }
@@ -836,6 +907,7 @@ int mypbr_guide_test_backward(int hidden, const float* weights, const float* inp
         cudaMemcpy(grads, T.g.grad, size_t(T.g.params) * 4, cudaMemcpyDeviceToHost);
     cudaFree(d_in);
     cudaFree(d_g);
+    cudaFree(partial);
     cudaFree(scratch);
     return rc;
 }

@@ -225,6 +225,17 @@ MYPBR_HD uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
 }
 
+// The same with A (bit 15) and / or B (bit 16) read MN-major: the operand's
+// M (or N) index runs along the 16-byte rows of its core matrices. A tile
+// stored K-major as [rows][K] is, read MN-major, its own transpose. For the
+// no-swizzle MN-major layout the descriptor's leading byte offset is the
+// core-matrix stride along K and the stride byte offset the one along M/N:
+// element (mn, k) sits at (mn % 8) * 2 B + (mn / 8) * SBO + (k % 8) * 16 B +
+// (k / 8) * LBO.
+MYPBR_HD uint32_t idesc_bf16_mn(int M, int N, bool a_mn, bool b_mn) {
+    return idesc_bf16(M, N) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+
 MYPBR_DEV void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"

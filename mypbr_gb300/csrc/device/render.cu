@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -60,7 +61,8 @@ struct WaveParams {
     unsigned long long* totals;  // extension rays, shadow rays, bounces run by a replayed wave graph
     // path guiding
     int guided;                // mixtures were computed for this wave's guidable vertices
-    float guide_alpha;         // probability of sampling the mixture there (one-sample MIS)
+    float guide_alpha;         // probability of sampling the mixture there (one-sample MIS), first bounce
+    float guide_alpha_deep;    // the same at later bounces
     int guide_depths;          // bounces below this sample the mixture
     int record;                // write training records
     GuideRecords rec;          // slots below rec_slots record their first rec.depth vertices
@@ -556,16 +558,16 @@ __device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
                 // weight and throughput uses the combined density.
                 GuideMix gm;
                 bool use_guide = false;
+                const float ga = depth == 0 ? P.guide_alpha : P.guide_alpha_deep;
                 if constexpr (GUIDED && kGuidable<C>()) {
-                    if (P.guided && P.guide_alpha > 0.0f && !vol && depth < P.guide_depths) {
+                    if (P.guided && ga > 0.0f && !vol && depth < P.guide_depths) {
                         guide_unpack(P.guide_mix[slot], gm);
                         use_guide = true;
                     }
                 }
                 auto mis_pdf = [&](float3 dir) {
                     float pb = sr.pdf.value(dir);
-                    return use_guide ? P.guide_alpha * guide_pdf(gm, normalize(dir)) + (1.0f - P.guide_alpha) * pb
-                                     : pb;
+                    return use_guide ? ga * guide_pdf(gm, normalize(dir)) + (1.0f - ga) * pb : pb;
                 };
                 if (P.has_lights) {  // camera.h:466-506; the shadow ray is traced by k_shadow
                     // With the sky as the only light, the sample carries its own
@@ -598,7 +600,7 @@ __device__ __forceinline__ void shade_body(const WaveParams& P, int depth) {
                     terminate = true;
                 } else {
                     float3 dir;
-                    if (use_guide && g.next() < P.guide_alpha) {
+                    if (use_guide && g.next() < ga) {
                         float u0 = g.next(), u1 = g.next();
                         dir = guide_sample(gm, u0, u1, g.next());
                     } else {
@@ -991,8 +993,40 @@ const void* shadow_kernel(bool vox, int walk) {
     return vox ? (const void*)k_shadow<true, kWalkBinary> : (const void*)k_shadow<false, kWalkBinary>;
 }
 
+// The path kernels keep their data in L1 (tree nodes, voxel cells, material
+// records): they ask for the largest L1 share of each SM's on-chip memory.
+// Without the request an SM keeps the split of the kernel before, and after
+// the guiding network's kernels (213 KB of shared memory each) that leaves
+// the walks a small L1. Set once per device.
+void prefer_l1(int device) {
+    static std::atomic<uint64_t> done{0};
+    const uint64_t bit = uint64_t(1) << (device & 63);
+    if (done.load() & bit)
+        return;
+    const void* kernels[] = {
+        (const void*)k_generate, (const void*)k_features,
+        (const void*)k_extend<true, kWalkBinary>, (const void*)k_extend<false, kWalkBinary>,
+        (const void*)k_extend<true, kWalkWide>, (const void*)k_extend<false, kWalkWide>,
+        (const void*)k_extend<true, kWalkPostponed>, (const void*)k_extend<false, kWalkPostponed>,
+        (const void*)k_extend_pt<true>, (const void*)k_extend_pt<false>,
+        (const void*)k_shadow<true, kWalkBinary>, (const void*)k_shadow<false, kWalkBinary>,
+        (const void*)k_shadow<true, kWalkWide>, (const void*)k_shadow<false, kWalkWide>,
+        (const void*)k_shadow<true, kWalkPostponed>, (const void*)k_shadow<false, kWalkPostponed>,
+        (const void*)k_shade<kClassMiss>, (const void*)k_shade<kClassLambert>, (const void*)k_shade<kClassMetal>,
+        (const void*)k_shade<kClassDielectric>, (const void*)k_shade<kClassPrincipled>,
+        (const void*)k_shade<kClassGeneric>, (const void*)k_shade_guided<kClassMiss>,
+        (const void*)k_shade_guided<kClassLambert>, (const void*)k_shade_guided<kClassMetal>,
+        (const void*)k_shade_guided<kClassDielectric>, (const void*)k_shade_guided<kClassPrincipled>,
+        (const void*)k_shade_guided<kClassGeneric>};
+    for (const void* k : kernels)
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxL1));
+    cudaGetLastError();  // a hint: a driver that ignores it changes nothing
+    done.fetch_or(bit);
+}
+
 // Grids of `block` threads: SMs x resident blocks (persistent-style loops).
 Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
+    prefer_l1(G.device);
     Launch L{};
     // 128-thread blocks suit the postponed-leaf walk (6 % faster on the
     // 2 M-triangle room, 6 % on the guided voxel hall), 256 the rest
@@ -1218,7 +1252,9 @@ int launch_wave(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launc
     // the wave's launches depend on these; the kernels' parameters (captured
     // by value) on the mixing probability too
     int key = (P.guided ? 1 : 0) | (P.record ? 2 : 0) | (P.guide_alpha > 0.0f ? 4 : 0) |
-              (P.guided ? (std::min(P.guide_depths, 255) << 3) | (int(P.guide_alpha * 1000.0f + 0.5f) << 11) : 0);
+              (P.guided ? (std::min(P.guide_depths, 255) << 3) | (int(P.guide_alpha * 1000.0f + 0.5f) << 11) |
+                              (int(P.guide_alpha_deep * 1000.0f + 0.5f) << 21)
+                        : 0);
     if (!graph->exec || graph->key != key) {
         if (graph->exec) {
             cudaGraphExecDestroy(graph->exec);
@@ -1265,7 +1301,6 @@ struct RenderSetup {
 // Guided renders: the first waves are small and recorded, each followed by
 // Adam steps on their vertices; later waves keep training online, lightly.
 constexpr int kGuideTrainWaves = 8;
-constexpr int kGuideMinSteps = 16;    // steps before the mixture is sampled at all
 constexpr int kGuideBatchTilesPerSm = 2;  // 128-sample tiles per SM in one step (39K samples on 152 SMs)
 constexpr float kGuideLr = 4e-3f;
 
@@ -1365,8 +1400,9 @@ int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int sav
         P.npass = std::min(P.npass, save_every - pass0 % save_every);
     if (R.guided) {
         const GuideState& g = G->guide;
-        P.guided = g.steps >= kGuideMinSteps;
+        P.guided = g.steps >= g.use_after;
         P.guide_alpha = P.guided ? g.alpha : 0.0f;
+        P.guide_alpha_deep = P.guided ? (g.alpha_deep >= 0.0f ? g.alpha_deep : g.alpha) : 0.0f;
         P.guide_depths = std::min(g.depths, P.max_depth);
         P.record = g.steps < g.max_steps;
         if (P.record)

@@ -257,12 +257,15 @@ def test_guiding_gains_on_occluded_scene():
     sc = mp.load_scene(p)
     G = mp.GpuScene(sc)
     ref, _, _ = _render(sc, G, 16384, 0, 0, seed=99)
-    plain = np.mean([rel_mse(_render(sc, G, 256, 0, 0, seed=s)[0], ref) for s in (1, 2)])
+    seeds = range(1, 9)
+    plain = [rel_mse(_render(sc, G, 256, 0, 0, seed=s)[0], ref) for s in seeds]
     guided = []
-    for s in (1, 2):
+    for s in seeds:
         Gs = mp.GpuScene(sc)  # a fresh, untrained network each time
         guided.append(rel_mse(_render(sc, Gs, 256, 2, 8, seed=s)[0], ref))
         Gs.close()
-    guided = float(np.mean(guided))
-    print(f"relMSE at 256 spp: plain {plain:.4f}, guided {guided:.4f}")
+    # single renders of this scene are firefly-dominated (one render's relMSE
+    # swings by 10x or more either way), so the typical render decides
+    plain, guided = float(np.median(plain)), float(np.median(guided))
+    print(f"median relMSE over {len(seeds)} renders at 256 spp: plain {plain:.4f}, guided {guided:.4f}")
     assert guided < plain, (guided, plain)
