@@ -46,9 +46,10 @@ the oracle beside it; with --hidden H the triangle room also renders guided
 and compares plain and guided relMSE at equal time against --c3-ref-spp.
 batch: C4, 64 scenes in one mypbr_gpu_render_batch call with feature guides,
 every frame denoised, per-scene relMSE against 4x-spp renders.
---traversal 0..4 picks the walk (the scene's default: postponed leaves where
+--traversal 0..5 picks the walk (the scene's default: postponed leaves where
 triangles fill most leaves, else binary; lanes taking new rays; 4-wide tree;
-postponed leaves; plain binary), --block the threads per block.
+postponed leaves; plain binary; 8-wide tree with quantised boxes), --block
+the threads per block.
 
 --impl reference times the CPU implementation of the same path (the FP64
 restatement of the reference's camera::render in oracle/, on every host core)
@@ -740,7 +741,7 @@ def run_batch(args):
         cam = sc.camera
         cam.samples_per_pixel = spp
         cam.collect_features = 1
-        # --batch-wave-paths in flight per job (2M: 64 handles' path buffers stay near 30 GB)
+        # --batch-wave-paths in flight per job (8M: 64 handles' path buffers stay near 80 GB)
         cam.samples_per_wave = max(1, args.batch_wave_paths // (cam.height() * cam.image_width))
         scenes.append((sc, G))
         cams.append(cam)
@@ -863,14 +864,15 @@ def main():
     p.add_argument("--plain-launches", action="store_true",
                    help="hall_render: every kernel launched on its own with events (profilers cannot look inside "
                         "graphs with conditional nodes)")
-    p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3, 4],
+    p.add_argument("--traversal", type=int, default=0, choices=[0, 1, 2, 3, 4, 5],
                    help="0: the scene's default; 1: extend lanes take new rays as theirs finish; 2: the 4-wide "
-                        "tree; 3: postponed leaves; 4: the plain binary walk")
+                        "tree; 3: postponed leaves; 4: the plain binary walk; 5: the 8-wide tree with quantised "
+                        "boxes")
     p.add_argument("--block", type=int, default=0, choices=[0, 128, 256])
     p.add_argument("--autotune", action="store_true", help="cornell / triangle_room: autotuned launch settings")
     p.add_argument("--wave-paths", type=int, default=0, help="cornell / triangle_room: paths per wave (0: default)")
     p.add_argument("--batch-count", type=int, default=64)
-    p.add_argument("--batch-wave-paths", type=int, default=2 << 20, help="batch: paths in flight per job")
+    p.add_argument("--batch-wave-paths", type=int, default=8 << 20, help="batch: paths in flight per job")
     p.add_argument("--hall-width", type=int, default=480)
     p.add_argument("--no-curve", action="store_true",
                    help="voxel_hall: skip the doubling-spp curve (the repeated renders decide the time to target)")

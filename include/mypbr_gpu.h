@@ -523,7 +523,9 @@ int mypbr_gpu_test_spawn(mypbr_gpu_scene* scene, const float* rays, int64_t n, i
  * tmin tmax), device or host memory as `on_device` says. hits: n x 8 floats
  * (t, nx, ny, nz, u, v, front_face, material) and prim: n x 2 int32 (kind,
  * index; kind -1 on a miss; a voxel face reports its block; the ground plane
- * reports kind 5). */
+ * reports kind 5). The walk is the one the handle's traversal setting names
+ * (mypbr_gpu_set_launch: 2, 3 or 5 where the tree allows it), else the plain
+ * binary walk. */
 int mypbr_gpu_trace(mypbr_gpu_scene* scene, const float* rays, int64_t n, float* hits, int32_t* prim,
                     int on_device);
 
@@ -638,13 +640,15 @@ typedef struct mypbr_tune_result {
     int32_t traversal;
     int64_t wave_paths;
     double mpaths_per_s;
-    double trial_mpaths[32];
+    double trial_mpaths[40];  /* traversal 1..5 x block 128, 256 x 4, 8, 16, 32 M paths per wave */
 } mypbr_tune_result;
 
 /* Sets the launch settings the autotuner would set (0 keeps a setting's
- * default: block 256, 32M paths per wave, traversal 0). A traversal the
- * scene's tree does not allow (2 without a 4-wide tree, 3 with leaves of 16
- * or more references) walks the plain binary tree. */
+ * default: block 256, 32M paths per wave, traversal 0). Traversal: 0 the
+ * scene's default, 1 lanes that take new rays, 2 the 4-wide tree, 3 postponed
+ * leaves, 4 the plain binary walk, 5 the 8-wide tree with quantised boxes. A
+ * traversal the scene's tree does not allow (2 or 5 without that tree, 3 or
+ * 5 with leaves of 16 or more references) walks the plain binary tree. */
 int mypbr_gpu_set_launch(mypbr_gpu_scene* scene, int32_t block, int64_t wave_paths, int32_t traversal);
 
 /* Times short renders of the view with each setting and keeps the fastest on

@@ -95,7 +95,7 @@ class SkySettingsStruct(ctypes.Structure):
 
 class TuneResultStruct(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("traversal", ctypes.c_int32), ("wave_paths", ctypes.c_int64),
-                ("mpaths_per_s", ctypes.c_double), ("trial_mpaths", ctypes.c_double * 32)]
+                ("mpaths_per_s", ctypes.c_double), ("trial_mpaths", ctypes.c_double * 40)]
 
 
 class DisplayOptsStruct(ctypes.Structure):

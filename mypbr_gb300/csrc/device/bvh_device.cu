@@ -372,10 +372,21 @@ extern "C" int mypbr_gpu_scene_rebuild_bvh(mypbr_gpu_scene* G, int32_t method, m
         MYPBR_CUDA(cudaMemcpy(wide_p, wide.data(), wide.size() * sizeof(float4), cudaMemcpyHostToDevice));
         G->allocations.push_back(wide_p);
     }
+    // and its 8-wide quantised form, likewise
+    std::vector<uint4> wide8;
+    int depth8 = 0;
+    uint4* wide8_p = nullptr;
+    if (collapse_to_8q(after, wide8, depth8) && 7 * (depth8 + 1) <= kBvh8Stack) {
+        MYPBR_CUDA(cudaMalloc(&wide8_p, wide8.size() * sizeof(uint4)));
+        MYPBR_CUDA(cudaMemcpy(wide8_p, wide8.data(), wide8.size() * sizeof(uint4), cudaMemcpyHostToDevice));
+        G->allocations.push_back(wide8_p);
+    }
     D.bvh = nodes.p;
     D.leaf_refs = sorted_refs.p;
     D.bvh_node_count = n - 1;
     D.bvh4 = wide_p;
+    D.bvh8 = wide8_p;
+    D.bvh8_node_count = wide8_p ? int(wide8.size() / 6) : 0;
     D.postponed_ok = n < (1 << 26);  // one reference per leaf
     D.bvh4_node_count = wide_p ? int(wide.size() / 8) : 0;
     nodes.p = nullptr;

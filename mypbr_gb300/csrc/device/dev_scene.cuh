@@ -73,6 +73,8 @@ struct DeviceScene {
     const uint32_t* leaf_refs;
     const float4* bvh4;  // the same tree collapsed to 4 children per node (nullptr: not built)
     int bvh4_node_count;
+    const uint4* bvh8;   // collapsed to 8 children with quantised boxes (nullptr: not built)
+    int bvh8_node_count;
     int postponed_ok;    // leaves small enough to pack into walk_postponed's stack entries
     const float4* spheres;
     const int2* sphere_info;
@@ -632,7 +634,7 @@ MYPBR_DEV float safe_inv(float x) { return fabsf(x) > 1e-30f ? 1.0f / x : copysi
 // WALK: which walk. 0: the binary tree, leaves tested as soon as they are
 // met; 1: the 4-wide tree (S.bvh4); 2: the binary tree with leaves postponed
 // until every lane of the warp holds one (walk_postponed).
-enum : int { kWalkBinary = 0, kWalkWide = 1, kWalkPostponed = 2 };
+enum : int { kWalkBinary = 0, kWalkWide = 1, kWalkPostponed = 2, kWalkWide8 = 3 };
 template <bool ANY, bool VOX = true, int WALK = kWalkBinary>
 MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint64_t media_key);
 
@@ -1039,6 +1041,109 @@ MYPBR_DEV bool walk_postponed(const DeviceScene& S, float3 o, float3 d, float tm
     return false;
 }
 
+// The walk over the 8-wide tree with quantised boxes (96-byte nodes, the
+// layout collapse_to_8q writes). Per node the eight child planes are decoded
+// from bytes as t = q (s / d) + (p - o) / d per axis (one FMA each); leaves
+// among the children the ray meets are tested at once, the interior ones
+// still nearer than the closest hit are sorted near to far (a 19-comparator
+// network) and all but the nearest pushed. The host bounds the stack (seven
+// entries per level) before it enables this walk.
+constexpr int kBvh8Stack = 64;
+MYPBR_DEV float byte_at(uint32_t w, int c) { return float((w >> (8 * (c & 3))) & 0xffu); }
+template <bool ANY, bool VOX>
+MYPBR_DEV bool walk_tree8q(const DeviceScene& S, float3 o, float3 d, float tmin, uint64_t media_key, HitInfo& h) {
+    const float3 inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    const TriRay tr = make_tri_ray(d);
+    int stack[kBvh8Stack];
+    int sp = 0;
+    int node = 0;
+    int visits = 0;
+    while (true) {
+        if (++visits > S.bvh8_node_count + 1) {  // a tree walk enters each node at most once
+            atomicCAS(S.error, 0, 1);
+            return false;
+        }
+        const uint4* n = S.bvh8 + 6 * node;
+        const uint4 r0 = __ldg(n), rx = __ldg(n + 1), ry = __ldg(n + 2), rz = __ldg(n + 3), w03 = __ldg(n + 4),
+                    w47 = __ldg(n + 5);
+        const float sx = __uint_as_float((r0.w & 0xffu) << 23), sy = __uint_as_float(((r0.w >> 8) & 0xffu) << 23),
+                    sz = __uint_as_float(((r0.w >> 16) & 0xffu) << 23);
+        const float ax = sx * inv.x, ay = sy * inv.y, az = sz * inv.z;
+        const float bx = (__uint_as_float(r0.x) - o.x) * inv.x, by = (__uint_as_float(r0.y) - o.y) * inv.y,
+                    bz = (__uint_as_float(r0.z) - o.z) * inv.z;
+        float key[8];
+        int val[8];
+        unsigned leaves = 0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const uint32_t w = c < 4 ? (c == 0 ? w03.x : c == 1 ? w03.y : c == 2 ? w03.z : w03.w)
+                                     : (c == 4 ? w47.x : c == 5 ? w47.y : c == 6 ? w47.z : w47.w);
+            const uint32_t lxw = c < 4 ? rx.x : rx.y, hxw = c < 4 ? rx.z : rx.w;
+            const uint32_t lyw = c < 4 ? ry.x : ry.y, hyw = c < 4 ? ry.z : ry.w;
+            const uint32_t lzw = c < 4 ? rz.x : rz.y, hzw = c < 4 ? rz.z : rz.w;
+            const float lx = fmaf(byte_at(lxw, c), ax, bx), hx = fmaf(byte_at(hxw, c), ax, bx);
+            const float ly = fmaf(byte_at(lyw, c), ay, by), hy = fmaf(byte_at(hyw, c), ay, by);
+            const float lz = fmaf(byte_at(lzw, c), az, bz), hz = fmaf(byte_at(hzw, c), az, bz);
+            const float tn = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fmaxf(fminf(lz, hz), tmin));
+            const float tf = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fminf(fmaxf(lz, hz), h.t));
+            // a small relative widening keeps FP32 slab tests conservative
+            const bool met = w != 0xffffffffu && tn <= tf * 1.00000024f + 1e-30f;
+            const bool leaf = (w >> 31) != 0u;
+            leaves |= (met && leaf) ? 1u << c : 0u;
+            key[c] = (met && !leaf) ? tn : INFINITY;
+            val[c] = leaf ? int((w >> 4) & 0x7ffffffu) : int(w);
+            if (met && leaf)
+                key[c] = INFINITY;
+        }
+        for (unsigned m = leaves; m; m &= m - 1) {
+            const int c = __ffs(m) - 1;
+            const uint32_t w = c < 4 ? (c == 0 ? w03.x : c == 1 ? w03.y : c == 2 ? w03.z : w03.w)
+                                     : (c == 4 ? w47.x : c == 5 ? w47.y : c == 6 ? w47.z : w47.w);
+            if (test_leaf<ANY, VOX>(S, int((w >> 4) & 0x7ffffffu), int(w & 15u), o, d, tr, tmin, media_key, h))
+                return true;
+        }
+        // the interior children still nearer than the closest hit, nearest first
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            key[c] = key[c] <= h.t ? key[c] : INFINITY;
+        auto cswap = [&](int i, int j) {
+            if (key[j] < key[i]) {
+                const float tk = key[i];
+                key[i] = key[j];
+                key[j] = tk;
+                const int tv = val[i];
+                val[i] = val[j];
+                val[j] = tv;
+            }
+        };
+        cswap(0, 2); cswap(1, 3); cswap(4, 6); cswap(5, 7);
+        cswap(0, 4); cswap(1, 5); cswap(2, 6); cswap(3, 7);
+        cswap(0, 1); cswap(2, 3); cswap(4, 5); cswap(6, 7);
+        cswap(2, 4); cswap(3, 5);
+        cswap(1, 4); cswap(3, 6);
+        cswap(1, 2); cswap(3, 4); cswap(5, 6);
+        int pushes = 0;
+#pragma unroll
+        for (int c = 1; c < 8; c++)
+            pushes += key[c] < INFINITY;
+        if (sp + pushes > kBvh8Stack) {  // deeper than the host-checked bound: report, stop
+            atomicCAS(S.error, 0, 2);
+            return false;
+        }
+#pragma unroll
+        for (int c = 7; c >= 1; c--)
+            if (key[c] < INFINITY)
+                stack[sp++] = val[c];
+        if (key[0] < INFINITY) {
+            node = val[0];
+        } else {
+            if (sp == 0)
+                return false;
+            node = stack[--sp];
+        }
+    }
+}
+
 // The whole walk in one loop (the form the per-ray kernels use; walk_node
 // above is the same step, resumable, for k_extend_pt).
 template <bool ANY, bool VOX, int WALK>
@@ -1049,6 +1154,9 @@ MYPBR_DEV HitInfo walk(const DeviceScene& S, float3 o, float3 d, float tmin, flo
     h.b1 = h.b2 = 0.0f;
     if constexpr (WALK == kWalkWide) {
         if (S.has_bvh && walk_tree4<ANY, VOX>(S, o, d, tmin, media_key, h))
+            return h;
+    } else if constexpr (WALK == kWalkWide8) {
+        if (S.has_bvh && walk_tree8q<ANY, VOX>(S, o, d, tmin, media_key, h))
             return h;
     } else if constexpr (WALK == kWalkPostponed) {
         if (S.has_bvh && walk_postponed<ANY, VOX>(S, o, d, tmin, media_key, h))

@@ -130,6 +130,10 @@ int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaSt
 int guide_fit_box(mypbr_gpu_scene* G, cudaStream_t st);
 // The binary tree's device nodes collapsed to four children per node (walk_tree4's layout); depth: deepest level.
 void collapse_to_4(const std::vector<float4>& bin, std::vector<float4>& out, int& depth);
+// The binary tree collapsed to 8 children per node with quantised child boxes
+// (the layout walk_tree8q reads); false (out empty) when a leaf holds 16 or
+// more references or starts past 2^27.
+bool collapse_to_8q(const std::vector<float4>& bin, std::vector<uint4>& out, int& depth);
 // The environment's pdf table (p n per texel) and alias table (probability, alias index bits) from its
 // pixels (w x h x 3 floats): on the device (device pointers, env_dist.cu) or on the host (Vose's method).
 int build_env_distribution(const float* rgb, int w, int h, float* texel_pdf, float2* alias, cudaStream_t st);

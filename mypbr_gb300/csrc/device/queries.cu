@@ -9,12 +9,13 @@
 
 namespace mypbr_dev {
 
+template <int WALK>
 __global__ void k_trace(DeviceScene S, const float* rays, long long n, float* hits, int* prim) {
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         const float* r = rays + 8 * k;
         float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
-        HitInfo h = closest_hit<true>(S, o, d, r[6], r[7], 0);
+        HitInfo h = closest_hit<true, WALK>(S, o, d, r[6], r[7], 0);
         float* out = hits + 8 * k;
         if (h.prim == kMiss) {
             for (int c = 0; c < 8; c++)
@@ -145,6 +146,19 @@ int bad_arg(const std::string& m) {
 
 using namespace mypbr_dev;
 
+// The walk the handle's traversal setting names (mypbr_gpu_set_launch): 2 the
+// 4-wide tree, 3 postponed leaves, 5 the quantised 8-wide tree, where the
+// scene's tree allows it; the plain binary walk otherwise.
+static void (*trace_kernel(const mypbr_gpu_scene* G))(DeviceScene, const float*, long long, float*, int*) {
+    if (G->tuned_traversal == 2 && G->dev.bvh4)
+        return k_trace<kWalkWide>;
+    if (G->tuned_traversal == 3 && G->dev.postponed_ok)
+        return k_trace<kWalkPostponed>;
+    if (G->tuned_traversal == 5 && G->dev.bvh8)
+        return k_trace<kWalkWide8>;
+    return k_trace<kWalkBinary>;
+}
+
 extern "C" int mypbr_gpu_trace(mypbr_gpu_scene* G, const float* rays, int64_t n, float* hits, int32_t* prim,
                                int on_device) {
     if (!G || (n > 0 && (!rays || !hits || !prim)) || n < 0)
@@ -153,8 +167,9 @@ extern "C" int mypbr_gpu_trace(mypbr_gpu_scene* G, const float* rays, int64_t n,
         return MYPBR_OK;
     MYPBR_CUDA(cudaSetDevice(G->device));
     int blocks = int(std::min<int64_t>((n + 127) / 128, int64_t(G->sm_count) * 16));
+    auto k_trace_walk = trace_kernel(G);
     if (on_device) {
-        k_trace<<<blocks, 128>>>(G->dev, rays, (long long)n, hits, prim);
+        k_trace_walk<<<blocks, 128>>>(G->dev, rays, (long long)n, hits, prim);
         MYPBR_CUDA(cudaGetLastError());
         MYPBR_CUDA(cudaDeviceSynchronize());
         return check_device_error(G);
@@ -164,8 +179,8 @@ extern "C" int mypbr_gpu_trace(mypbr_gpu_scene* G, const float* rays, int64_t n,
     MYPBR_CUDA(cudaMalloc(&dh.p, size_t(n) * 8 * sizeof(float)));
     MYPBR_CUDA(cudaMalloc(&dp.p, size_t(n) * 2 * sizeof(int)));
     MYPBR_CUDA(cudaMemcpy(dr.p, rays, size_t(n) * 8 * sizeof(float), cudaMemcpyHostToDevice));
-    k_trace<<<blocks, 128>>>(G->dev, static_cast<float*>(dr.p), (long long)n, static_cast<float*>(dh.p),
-                             static_cast<int*>(dp.p));
+    k_trace_walk<<<blocks, 128>>>(G->dev, static_cast<float*>(dr.p), (long long)n, static_cast<float*>(dh.p),
+                                  static_cast<int*>(dp.p));
     MYPBR_CUDA(cudaGetLastError());
     MYPBR_CUDA(cudaMemcpy(hits, dh.p, size_t(n) * 8 * sizeof(float), cudaMemcpyDeviceToHost));
     MYPBR_CUDA(cudaMemcpy(prim, dp.p, size_t(n) * 2 * sizeof(int), cudaMemcpyDeviceToHost));

@@ -979,6 +979,8 @@ void launch_bounce_kernel(const void* fn, int grid, int block, cudaStream_t st, 
 
 // The extend and shadow kernels of a walk, with or without the voxel code.
 const void* extend_kernel(bool vox, int walk) {
+    if (walk == kWalkWide8)
+        return vox ? (const void*)k_extend<true, kWalkWide8> : (const void*)k_extend<false, kWalkWide8>;
     if (walk == kWalkWide)
         return vox ? (const void*)k_extend<true, kWalkWide> : (const void*)k_extend<false, kWalkWide>;
     if (walk == kWalkPostponed)
@@ -986,6 +988,8 @@ const void* extend_kernel(bool vox, int walk) {
     return vox ? (const void*)k_extend<true, kWalkBinary> : (const void*)k_extend<false, kWalkBinary>;
 }
 const void* shadow_kernel(bool vox, int walk) {
+    if (walk == kWalkWide8)
+        return vox ? (const void*)k_shadow<true, kWalkWide8> : (const void*)k_shadow<false, kWalkWide8>;
     if (walk == kWalkWide)
         return vox ? (const void*)k_shadow<true, kWalkWide> : (const void*)k_shadow<false, kWalkWide>;
     if (walk == kWalkPostponed)
@@ -1008,6 +1012,8 @@ void prefer_l1(int device) {
         (const void*)k_extend<true, kWalkBinary>, (const void*)k_extend<false, kWalkBinary>,
         (const void*)k_extend<true, kWalkWide>, (const void*)k_extend<false, kWalkWide>,
         (const void*)k_extend<true, kWalkPostponed>, (const void*)k_extend<false, kWalkPostponed>,
+        (const void*)k_extend<true, kWalkWide8>, (const void*)k_extend<false, kWalkWide8>,
+        (const void*)k_shadow<true, kWalkWide8>, (const void*)k_shadow<false, kWalkWide8>,
         (const void*)k_extend_pt<true>, (const void*)k_extend_pt<false>,
         (const void*)k_shadow<true, kWalkBinary>, (const void*)k_shadow<false, kWalkBinary>,
         (const void*)k_shadow<true, kWalkWide>, (const void*)k_shadow<false, kWalkWide>,
@@ -1042,6 +1048,8 @@ Launch launch_config(const mypbr_gpu_scene& G, int block = 0) {
         L.walk = kWalkWide;
     else if (trav == 3 && G.dev.postponed_ok)
         L.walk = kWalkPostponed;
+    else if (trav == 5 && G.dev.bvh8 != nullptr)
+        L.walk = kWalkWide8;
     int per_sm = 0;
     bool vox = G.dev.has_voxels;
     const void* extend = extend_kernel(vox, L.walk);
@@ -1956,9 +1964,10 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
     MYPBR_CUDA(cudaEventCreate(&e1));
     int status = MYPBR_OK;
     int trial = 0;
-    for (int trav = 1; trav <= 4; trav++)
+    for (int trav = 1; trav <= 5; trav++)
     for (int b : blocks) {
-        if ((trav == 2 && G->dev.bvh4 == nullptr) || (trav == 3 && !G->dev.postponed_ok)) {
+        if ((trav == 2 && G->dev.bvh4 == nullptr) || (trav == 3 && !G->dev.postponed_ok) ||
+            (trav == 5 && G->dev.bvh8 == nullptr)) {
             trial += 4;  // a walk this scene's tree does not allow: trials skipped
             continue;
         }
@@ -2004,8 +2013,8 @@ extern "C" int mypbr_gpu_autotune(mypbr_gpu_scene* G, const mypbr_camera* cam, c
 }
 
 extern "C" int mypbr_gpu_set_launch(mypbr_gpu_scene* G, int32_t block, int64_t wave_paths, int32_t traversal) {
-    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 4)
-        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0 to 4");
+    if (!G || (block != 0 && block != 128 && block != 256) || wave_paths < 0 || traversal < 0 || traversal > 5)
+        return bad_arg("mypbr_gpu_set_launch: block 0, 128 or 256; wave_paths >= 0; traversal 0 to 5");
     G->tuned_block = block;
     G->tuned_wave_paths = size_t(wave_paths);
     G->tuned_traversal = traversal;

@@ -413,6 +413,18 @@ int create_scene(const mypbr_flat_scene* Fp, mypbr_gpu_scene** out) {
         }
     }
     {
+        std::vector<uint4> nodes8;
+        int depth8 = 0;
+        // the 8-wide walk's stack takes at most seven entries per level
+        if (D.has_bvh && collapse_to_8q(nodes, nodes8, depth8) && 7 * (depth8 + 1) <= kBvh8Stack) {
+            PUT(nodes8, D.bvh8);
+            D.bvh8_node_count = int(nodes8.size() / 6);
+        } else {
+            D.bvh8 = nullptr;
+            D.bvh8_node_count = 0;
+        }
+    }
+    {
         std::vector<int> zero(1, 0);
         const int* err = nullptr;
         PUT(zero, err);
@@ -862,6 +874,155 @@ void collapse_to_4(const std::vector<float4>& bin, std::vector<float4>& out, int
         return me;
     };
     build(0, 0);
+}
+
+// The binary tree collapsed to eight children per node (the interior child of
+// largest surface area expanded first, as for four), each node 96 bytes:
+//   row 0      the origin p (3 floats, at least one quantum below the
+//              node's box) and, per axis, the biased exponent e of the
+//              quantum 2^(e - 127) (bytes 0-2)
+//   rows 1-3   per axis: the children's low planes as bytes (8), then their
+//              high planes (8); a plane is p + q 2^(e - 127)
+//   rows 4-5   per child a word: a node index, or 1 << 31 | first << 4 |
+//              count for a leaf of `count` references from `first`, or
+//              0xffffffff for an empty slot
+// Quantised boxes contain the child's box with one to two quanta to spare on
+// every side; the quantum is at least four float steps of the node's
+// coordinates.
+bool collapse_to_8q(const std::vector<float4>& bin, std::vector<uint4>& out, int& depth) {
+    struct Child {
+        float4 lo, hi;
+        int index() const { return float_bits(lo.w); }
+        int count() const { return float_bits(hi.w); }
+    };
+    auto children = [&](int i, Child* c) {
+        c[0] = {bin[size_t(i) * 4], bin[size_t(i) * 4 + 1]};
+        c[1] = {bin[size_t(i) * 4 + 2], bin[size_t(i) * 4 + 3]};
+    };
+    auto area = [](const Child& c) {
+        double x = double(c.hi.x) - c.lo.x, y = double(c.hi.y) - c.lo.y, z = double(c.hi.z) - c.lo.z;
+        if (!(x >= 0 && y >= 0 && z >= 0) || !std::isfinite(x + y + z))
+            return -1.0;
+        return x * y + y * z + z * x;
+    };
+    auto axis = [](const float4& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); };
+    out.clear();
+    depth = 0;
+    bool ok = true;
+    std::function<int(int, int)> build = [&](int i, int level) -> int {
+        depth = std::max(depth, level);
+        Child list[8];
+        children(i, list);
+        int n = 2;
+        while (n < 8) {
+            int best = -1;
+            double best_area = -2;
+            for (int k = 0; k < n; k++)
+                if (list[k].count() == 0 && area(list[k]) > best_area) {
+                    best = k;
+                    best_area = area(list[k]);
+                }
+            if (best < 0)
+                break;
+            Child sub[2];
+            children(list[best].index(), sub);
+            list[best] = sub[0];
+            list[n++] = sub[1];
+        }
+        // empty padding children (boxes at +infinity) take no slot
+        int m = 0;
+        for (int k = 0; k < n; k++)
+            if (std::isfinite(list[k].lo.x) || list[k].count() == 0)
+                list[m++] = list[k];
+        n = m;
+        const int me = int(out.size() / 6);
+        out.resize(out.size() + 6);
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; a++) {
+            lo[a] = INFINITY;
+            hi[a] = -INFINITY;
+            for (int k = 0; k < n; k++) {
+                lo[a] = std::min(lo[a], double(axis(list[k].lo, a)));
+                hi[a] = std::max(hi[a], double(axis(list[k].hi, a)));
+            }
+            if (!(lo[a] <= hi[a]))
+                lo[a] = hi[a] = 0.0;
+        }
+        // per axis: the quantum s = 2^e, at least four float steps of the
+        // coordinates, and the origin p one quantum or more below the box;
+        // every child plane then lies one to two quanta outside the child's
+        // own (low planes rounded down, high planes up, one more quantum
+        // each), so FP32 rounding of the slab distances cannot cut a child
+        uint32_t ebias[3];
+        double quantum[3], origin[3];
+        for (int a = 0; a < 3; a++) {
+            const double mag = std::max(std::fabs(lo[a]), std::fabs(hi[a])) + 1e-30;
+            const double extent = hi[a] - lo[a];
+            int e = std::max(std::ilogb(mag) - 21, -126);
+            if (extent > 0)
+                e = std::max(e, int(std::ceil(std::log2(extent / 250.0))));
+            for (;; e++) {
+                const double sq = std::ldexp(1.0, e);
+                const float pf = std::nextafter(float(lo[a] - sq), -INFINITY);  // at or below lo - s
+                if (e >= 127 || (std::ceil((hi[a] - double(pf)) / sq) + 1.0 <= 255.0 && double(pf) <= lo[a] - sq)) {
+                    origin[a] = double(pf);
+                    break;
+                }
+            }
+            ebias[a] = uint32_t(std::min(e, 127) + 127);
+            quantum[a] = std::ldexp(1.0, std::min(e, 127));
+        }
+        uint8_t qlo[3][8], qhi[3][8];
+        uint32_t word[8];
+        for (int k = 0; k < 8; k++) {
+            for (int a = 0; a < 3; a++) {
+                qlo[a][k] = 1;  // empty slots: an inverted box, and an empty word
+                qhi[a][k] = 0;
+            }
+            word[k] = 0xffffffffu;
+        }
+        for (int k = 0; k < n; k++) {
+            for (int a = 0; a < 3; a++) {
+                const double p = origin[a], sq = quantum[a];
+                const double cl = axis(list[k].lo, a), ch = axis(list[k].hi, a);
+                const double ql = std::floor((cl - p) / sq) - 1.0, qh = std::ceil((ch - p) / sq) + 1.0;
+                qlo[a][k] = uint8_t(std::min(std::max(ql, 0.0), 255.0));
+                qhi[a][k] = uint8_t(std::min(std::max(qh, 0.0), 255.0));
+            }
+        }
+        int child_node[8];
+        for (int k = 0; k < n; k++)
+            child_node[k] = list[k].count() == 0 ? build(list[k].index(), level + 1) : -1;
+        for (int k = 0; k < n; k++) {
+            if (list[k].count() == 0) {
+                word[k] = uint32_t(child_node[k]);
+            } else {
+                const int first = list[k].index(), count = list[k].count();
+                if (count >= 16 || first < 0 || first >= (1 << 27)) {
+                    ok = false;
+                    continue;
+                }
+                word[k] = 0x80000000u | (uint32_t(first) << 4) | uint32_t(count);
+            }
+        }
+        uint4* row = &out[size_t(me) * 6];
+        row[0] = make_uint4(uint32_t(float_bits(float(origin[0]))), uint32_t(float_bits(float(origin[1]))),
+                            uint32_t(float_bits(float(origin[2]))), ebias[0] | (ebias[1] << 8) | (ebias[2] << 16));
+        auto pack = [](const uint8_t* q, int from) {
+            return uint32_t(q[from]) | (uint32_t(q[from + 1]) << 8) | (uint32_t(q[from + 2]) << 16) |
+                   (uint32_t(q[from + 3]) << 24);
+        };
+        for (int a = 0; a < 3; a++)
+            row[1 + a] = make_uint4(pack(qlo[a], 0), pack(qlo[a], 4), pack(qhi[a], 0), pack(qhi[a], 4));
+        row[4] = make_uint4(word[0], word[1], word[2], word[3]);
+        row[5] = make_uint4(word[4], word[5], word[6], word[7]);
+        return me;
+    };
+    if (!bin.empty())
+        build(0, 0);
+    if (!ok)
+        out.clear();
+    return ok && !out.empty();
 }
 
 }  // namespace mypbr_dev

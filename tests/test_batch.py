@@ -101,7 +101,7 @@ def test_autotune_keeps_the_result():
     before = cam.render(G).radiance
     r = mp.autotune(cam, G)
     assert r["block"] in (128, 256) and r["wave_paths"] in (4 << 20, 8 << 20, 16 << 20, 32 << 20)
-    assert r["traversal"] in (1, 2, 3, 4) and len(r["trials"]) == 32
+    assert r["traversal"] in (1, 2, 3, 4, 5) and len(r["trials"]) == 40
     assert all(t > 0 for t in r["trials"]) and r["mpaths_per_s"] == max(r["trials"])
     after = cam.render(G).radiance
     np.testing.assert_allclose(after, before, rtol=1e-12, atol=1e-14)
@@ -125,11 +125,12 @@ def test_persistent_traversal_matches(name):
     np.testing.assert_allclose(c, a, rtol=1e-5, atol=1e-7)
 
 
-@pytest.mark.parametrize("traversal", [2, 3])
+@pytest.mark.parametrize("traversal", [2, 3, 5])
 @pytest.mark.parametrize("name", ["materials", "voxels", "fog_box", "gallery", "alpha_masks"])
 def test_other_walks_match(name, traversal):
-    """The walk over the tree collapsed to four children per node (2) and the
-    binary walk with postponed leaves (3) meet the same closest hits (and,
+    """The walk over the tree collapsed to four children per node (2), the
+    binary walk with postponed leaves (3) and the walk over the 8-wide tree
+    with quantised boxes (5) meet the same closest hits (and,
     for shadow rays, the same blockers) as the plain binary walk: equal to
     1e-5 (separately compiled kernels round media and fog distances in their
     own last bits)."""

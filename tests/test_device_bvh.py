@@ -77,10 +77,11 @@ def test_device_bvh_on_a_triangle_room():
     assert close.mean() > 0.999, close.mean()
 
 
-@pytest.mark.parametrize("traversal", [2, 3])
+@pytest.mark.parametrize("traversal", [2, 3, 5])
 def test_device_bvh_with_the_other_walks(traversal):
-    """After an LBVH rebuild the 4-wide tree is rebuilt from it and the
-    postponed-leaf walk stays allowed: both render what the binary walk does."""
+    """After an LBVH rebuild the 4-wide and the quantised 8-wide trees are
+    rebuilt from it and the postponed-leaf walk stays allowed: each renders
+    what the binary walk does."""
     sc = mp.load_scene(scene_path("materials.scene"))
     G = mp.GpuScene(sc)
     mp.rebuild_bvh(G)
