@@ -631,10 +631,12 @@ int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n);
  * new rays as theirs finish; 2: each lane walks its ray to the end over the
  * tree collapsed to 4 children per node; 3: the binary tree with leaves
  * postponed until the warp's lanes all hold one; 4: the plain binary walk;
- * 0, the default, is 4 for trees whose leaves are mostly spheres and 3
- * otherwise), with the Mpaths/s of each of the 32 trials (traversal 1 to 4;
- * within each, block 128 then 256; within each, 4M, 8M, 16M, 32M paths; 0
- * for trials skipped because the scene's tree does not allow that walk). */
+ * 5: each lane walks the tree collapsed to 8 children per node with
+ * quantised boxes; 0, the default, is 4 for trees whose leaves are mostly
+ * spheres and 3 otherwise), with the Mpaths/s of each of the 40 trials
+ * (traversal 1 to 5; within each, block 128 then 256; within each, 4M, 8M,
+ * 16M, 32M paths; 0 for trials skipped because the scene's tree does not
+ * allow that walk). */
 typedef struct mypbr_tune_result {
     int32_t block;
     int32_t traversal;
