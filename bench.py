@@ -81,8 +81,9 @@ WIDTH, HEIGHT = 1920, 1080
 # and the issue figures of bounces 0 and 1.
 EXTEND_PROFILE = {
     "profile": "profiles/k_extend_sphere_field_1080p.md",
-    "dram_bytes": 298.96e6 + 135.86e6, "rays": 8294400,
-    "issue_active_frac": [0.589, 0.611], "threads_per_instruction": [26.55, 12.88],
+    "commit": "c7bbfab",
+    "dram_bytes": 298.96e6 + 135.59e6, "rays": 8294400,
+    "issue_active_frac": [0.600, 0.620], "threads_per_instruction": [26.57, 12.92],
 }
 EXTEND_DRAM_BYTES_PER_RAY = EXTEND_PROFILE["dram_bytes"] / EXTEND_PROFILE["rays"]
 METRIC = "Mpaths/s at 1080p"
@@ -398,7 +399,8 @@ def run_ours(args):
                              "traffic": EXTEND_DRAM_BYTES_PER_RAY * ext_per_launch,
                              "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_extend on bounce "
                                                f"0 of a 4-spp frame ({EXTEND_PROFILE['dram_bytes'] / 1e6:.1f} MB for "
-                                               f"{EXTEND_PROFILE['rays']} camera rays, {EXTEND_PROFILE['profile']}), "
+                                               f"{EXTEND_PROFILE['rays']} camera rays, {EXTEND_PROFILE['profile']}, captured at commit "
+                                               f"{EXTEND_PROFILE['commit']}), "
                                                "scaled to the rays of an average launch",
                              "peak_source": peak_src, "bytes_per_ray": bytes_per_ray,
                              "avg_launch_ms": ms_ext, "rays_per_launch": ext_per_launch,
@@ -408,7 +410,8 @@ def run_ours(args):
                                        "threads_per_instruction": EXTEND_PROFILE["threads_per_instruction"],
                                        "source": "ncu smsp__issue_active and smsp__thread_inst_executed_per_"
                                                  "inst_executed of k_extend, bounces 0 and 1 of a 4-spp frame ("
-                                                 + EXTEND_PROFILE["profile"] + ")"}},
+                                                 + EXTEND_PROFILE["profile"] + ", captured at commit "
+                                                 + EXTEND_PROFILE["commit"] + ")"}},
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(w * h * 3 * 8)},
                 "clocks": clk}
