@@ -18,7 +18,7 @@ with host buffers: mypbr_gpu_scene_create (uploads the flat scene) +
 mypbr_gpu_render (renders, copies the FP64 frame back) + destroy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--spp S]
-  python bench.py --workload voxel_hall [--hall-width 480] [--ref-spp 65536]
+  python bench.py --workload voxel_hall [--hall-width 1920] [--ref-spp 65536] [--repeats 4] [--repeat-spp 1024]
   python bench.py --workload cornell | triangle_room | batch
   python bench.py --workload hall_render [--hall-size 128] [--hall-width 256] [--spp 96] [--hidden 8]
                   [--per-wave 8]      (one render; the profiling case of the guiding kernels)
@@ -32,9 +32,10 @@ noise (relMSE_raw in each point is the uncorrected value). The time to
 target comes from --repeats independent renders of each method at
 --repeat-spp (a fresh network for every guided one): their mean relMSE gives
 c in relMSE = c/spp, and the time is c/0.01 samples at their mean seconds
-per sample. Each method renders at doubling spp (a fresh, untrained
-network for every guided render, so training time is inside each timing)
-until relMSE <= 0.01 or --max-spp, reported as the curve (with the time to
+per sample. With --curve each method also renders at doubling spp (a
+fresh, untrained network for every guided render, so training time is
+inside each timing) until relMSE <= 0.01 or --max-spp, reported as the
+curve (with the time to
 target that curve alone gives: interpolated log-log between the bracketing
 renders, or extrapolated from the three highest-spp ones; single renders
 are dominated by a few fireflies). The oracle is the plain estimator
@@ -467,7 +468,7 @@ def spp_to_target(points, target):
 
 def run_voxel_hall(args):
     import mypbr_gb300 as mp
-    width = args.hall_width
+    width = args.hall_width or 1920
     height = width * 9 // 16
     target = 0.01
     with tempfile.TemporaryDirectory() as d:
@@ -507,7 +508,7 @@ def run_voxel_hall(args):
     for name, guided in (("plain", 0), ("guided", args.hidden)):
         pts = []
         spp = 16
-        while spp <= args.max_spp and not args.no_curve:
+        while spp <= args.max_spp and args.curve:
             if guided:  # an untrained network every time: training is inside each timing
                 mp.guide_reset(Gg)
             img, t = render(Gg if guided else G, spp, guided, 1 + spp)
@@ -824,7 +825,7 @@ def run_hall_render(args):
     per wave (0: automatic)."""
     import mypbr_gb300 as mp
     with tempfile.TemporaryDirectory() as d:
-        w = args.hall_width
+        w = args.hall_width or 256
         scene = mp.load_scene(voxel_hall_scene(d, size=args.hall_size, width=w, height=w * 9 // 16, spp=args.spp))
     G = mp.GpuScene(scene)
     mp.set_launch(G, block=args.block, traversal=args.traversal)
@@ -876,15 +877,18 @@ def main():
     p.add_argument("--wave-paths", type=int, default=0, help="cornell / triangle_room: paths per wave (0: default)")
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--batch-wave-paths", type=int, default=8 << 20, help="batch: paths in flight per job")
-    p.add_argument("--hall-width", type=int, default=480)
-    p.add_argument("--no-curve", action="store_true",
-                   help="voxel_hall: skip the doubling-spp curve (the repeated renders decide the time to target)")
+    p.add_argument("--hall-width", type=int, default=0,
+                   help="voxel_hall (default 1920, the configuration's width) / hall_render (default 256): pixels "
+                        "wide, 16:9")
+    p.add_argument("--curve", action="store_true",
+                   help="voxel_hall: also render the doubling-spp curve (the repeated renders decide the time to "
+                        "target)")
     p.add_argument("--ref-spp", type=int, default=65536)
     p.add_argument("--c3-ref-spp", type=int, default=1024, help="spp of the triangle room's reference render")
     p.add_argument("--max-spp", type=int, default=32768)
-    p.add_argument("--repeat-spp", type=int, default=8192,
+    p.add_argument("--repeat-spp", type=int, default=1024,
                    help="voxel_hall: spp of the repeated renders that estimate each method's error constant")
-    p.add_argument("--repeats", type=int, default=10, help="voxel_hall: renders per method at --repeat-spp")
+    p.add_argument("--repeats", type=int, default=4, help="voxel_hall: renders per method at --repeat-spp")
     p.add_argument("--hidden", type=int, default=8, help="hidden layers of the guiding network")
     p.add_argument("--guide-alpha", type=float, default=0.5, help="voxel_hall: probability of sampling the mixture")
     p.add_argument("--guide-depths", type=int, default=4, help="voxel_hall: bounces that sample the mixture")

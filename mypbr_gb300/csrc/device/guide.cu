@@ -80,7 +80,13 @@ struct RecordSource {
 struct GivenSource {
     const float* inputs;  // n x 128
     const float* grads;   // n x 64
+    struct Row {
+        long long i;
+    };
     MYPBR_DEV long long count(long long rows) const { return rows; }
+    MYPBR_DEV void load(long long i, Row& r) const { r.i = i; }
+    MYPBR_DEV void finish(Row&) const {}
+    MYPBR_DEV void encode(const Row& r, __nv_bfloat16* A, int row) const { fill(r.i, A, row); }
     MYPBR_DEV void fill(long long i, __nv_bfloat16* A, int row) const {
 #pragma unroll 1
         for (int b = 0; b < kGuideIn / 8; b++) {
@@ -106,7 +112,8 @@ struct GivenSource {
 
 struct RowSink {
     float* out;  // n x 64
-    MYPBR_DEV void put(long long i, const float* v) const {
+    template <class Row>
+    MYPBR_DEV void put(long long i, const Row&, const float* v) const {
         float4* o = reinterpret_cast<float4*>(out + i * kGuideOut);
 #pragma unroll
         for (int k = 0; k < kGuideOut / 4; k++)

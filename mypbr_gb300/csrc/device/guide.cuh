@@ -409,8 +409,12 @@ MYPBR_DEV void group_sync(int id, int count) { asm volatile("bar.sync %0, %1;" :
 // Batched MLP forward on the tensor cores: each CTA (kGuideGroups groups of
 // 128 threads, one thread per row) walks tiles of 128 rows, a tile per group
 // at a time. Src::count(rows) gives the number of rows (it may read a device
-// counter); Src::fill(i, tile, row) writes the encoded input row (BF16,
-// canonical, K = 128), i = -1 for padding rows; Sink::put(i, v) takes the 64
+// counter). A row is staged in three steps, so that the memory reads behind
+// the next tile's rows are in flight while the current tile's layers run:
+// Src::load(i, r) starts the reads of row i into the thread's Src::Row (i =
+// -1 for padding rows), Src::finish(r) completes the row's inputs two layers
+// later, Src::encode(r, tile, row) writes the encoded input row (BF16,
+// canonical, K = 128) when its tile begins. Sink::put(i, r, v) takes the 64
 // FP32 outputs of row i.
 template <class Src, class Sink>
 __global__ void __launch_bounds__(128 * kGuideGroups) k_guide_forward(GuideNetView net, Src src, Sink sink,
@@ -445,10 +449,18 @@ __global__ void __launch_bounds__(128 * kGuideGroups) k_guide_forward(GuideNetVi
     uint32_t phase = 0;
     const uint32_t idesc = tc::idesc_bf16(128, 64);
     bool failed = false;
-    for (long long tile = (long long)blockIdx.x * kGuideGroups + group; tile < tiles && !failed;
-         tile += (long long)gridDim.x * kGuideGroups) {
-        long long i = tile * 128 + row;
-        src.fill(i < rows ? i : -1, A, row);
+    const long long stride = (long long)gridDim.x * kGuideGroups;
+    auto row_of = [&](long long t) { return t < tiles && t * 128 + row < rows ? t * 128 + row : -1LL; };
+    // the layer at which the next tile's rows are completed (their reads were
+    // started at layer 0)
+    const int finish_at = net.hidden < 2 ? net.hidden : 2;
+    typename Src::Row cur, next;
+    src.load(row_of((long long)blockIdx.x * kGuideGroups + group), cur);
+    src.finish(cur);
+    for (long long tile = (long long)blockIdx.x * kGuideGroups + group; tile < tiles && !failed; tile += stride) {
+        const long long i = tile * 128 + row;
+        src.encode(cur, A, row);
+        const long long i_next = row_of(tile + stride);
         for (int l = 0; l <= net.hidden; l++) {
             int K = guide_in(l);
             tc::fence_smem();
@@ -461,6 +473,11 @@ __global__ void __launch_bounds__(128 * kGuideGroups) k_guide_forward(GuideNetVi
                             s > 0);
                 tc::commit(bar);
             }
+            // while the layer's MMAs run: the next tile's rows
+            if (l == 0)
+                src.load(i_next, next);
+            if (l == finish_at)
+                src.finish(next);
             bool ok = tc::bar_wait(bar, phase);
             phase ^= 1;
             if (tc::group_sync_or(bar_id, 128, !ok)) {
@@ -477,9 +494,10 @@ __global__ void __launch_bounds__(128 * kGuideGroups) k_guide_forward(GuideNetVi
             if (l < net.hidden) {
                 store_row_bf16_relu(A, row, v);
             } else if (i < rows) {
-                sink.put(i, v);
+                sink.put(i, cur, v);
             }
         }
+        cur = next;
     }
     tc::fence_before();
     __syncthreads();

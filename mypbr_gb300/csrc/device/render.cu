@@ -821,10 +821,18 @@ MYPBR_DEV uint32_t guided_slot(const WaveParams& P, int depth, long long i) {
 }
 
 // The guidable vertices of a bounce (depth -1: the bounce in device memory),
-// none past the guided depths.
+// none past the guided depths. A row is the vertex's path slot and, once
+// finished, its 7 network scalars; load starts the reads of the ray and hit
+// records, finish turns them into the surface point and its scalars.
 struct GuideQueueSource {
     WaveParams P;
     int depth;
+    struct Row {
+        float4 ro, rd, hb;
+        float s[kGuideScalars];
+        uint32_t slot;
+        bool valid;
+    };
     MYPBR_DEV long long count(long long) const {
         const int d = bounce_of(P, depth);
         if (d >= P.guide_depths)
@@ -835,33 +843,39 @@ struct GuideQueueSource {
             n += *class_counter(P, d, guided_class(c));
         return n;
     }
-    MYPBR_DEV void fill(long long i, __nv_bfloat16* A, int row) const {
-        if (i < 0) {
-            guide_encode_row(nullptr, A, row);
+    MYPBR_DEV void load(long long i, Row& r) const {
+        r.valid = i >= 0;
+        if (!r.valid)
+            return;
+        r.slot = guided_slot(P, bounce_of(P, depth), i);
+        r.ro = P.B.ray_o[r.slot];
+        r.rd = P.B.ray_d[r.slot];
+        r.hb = P.B.hit[r.slot];
+    }
+    MYPBR_DEV void finish(Row& r) const {
+        if (!r.valid) {  // a padding row: its outputs are never used
+#pragma unroll
+            for (int k = 0; k < kGuideScalars; k++)
+                r.s[k] = 0.0f;
             return;
         }
-        uint32_t slot = guided_slot(P, bounce_of(P, depth), i);
-        float4 ro = P.B.ray_o[slot], rd = P.B.ray_d[slot], hb = P.B.hit[slot];
         HitInfo h;
-        h.t = hb.x;
-        h.b1 = hb.y;
-        h.b2 = hb.z;
-        h.prim = __float_as_uint(hb.w);
-        Surface s = make_surface(P.S, h, f3(ro), f3(rd));
-        float sc[7];
-        guide_scalars(s.p, s.normal, normalize(-1.0f * f3(rd)), P.guide_lo, P.guide_inv, sc);
-        guide_encode_row(sc, A, row);
+        h.t = r.hb.x;
+        h.b1 = r.hb.y;
+        h.b2 = r.hb.z;
+        h.prim = __float_as_uint(r.hb.w);
+        Surface sf = make_surface(P.S, h, f3(r.ro), f3(r.rd));
+        guide_scalars(sf.p, sf.normal, normalize(-1.0f * f3(r.rd)), P.guide_lo, P.guide_inv, r.s);
     }
+    MYPBR_DEV void encode(const Row& r, __nv_bfloat16* A, int row) const { guide_encode_row(r.s, A, row); }
 };
 
 struct GuidePackSink {
     WaveParams P;
-    int depth;
-    MYPBR_DEV void put(long long i, const float* v) const {
-        uint32_t slot = guided_slot(P, bounce_of(P, depth), i);
+    MYPBR_DEV void put(long long, const GuideQueueSource::Row& r, const float* v) const {
         GuidePacked pk;
         guide_pack(v, pk);
-        P.guide_mix[slot] = pk;
+        P.guide_mix[r.slot] = pk;
     }
 };
 
@@ -1162,7 +1176,7 @@ int run_bounce(WaveParams& P, const Launch& L, cudaStream_t st, uint64_t& launch
         TIMED(1, (launch_bounce_kernel(extend_kernel(P.S.has_voxels, L.walk), L.grid_extend, L.block, st, P, depth)));
     if (P.guided && (depth < 0 || depth < P.guide_depths)) {  // the mixtures of this bounce's guidable vertices
         TIMED(4, (k_guide_forward<GuideQueueSource, GuidePackSink><<<L.grid_guide, 128 * kGuideGroups, L.guide_smem, st>>>(
-                     L.net, GuideQueueSource{P, depth}, GuidePackSink{P, depth}, 0)));
+                     L.net, GuideQueueSource{P, depth}, GuidePackSink{P}, 0)));
         launches++;
     }
     if (L.guided_kernels) {
