@@ -402,7 +402,7 @@ struct Pdf {
         return s;
     }
     MYPBR_DEV float3 generate(Rng& g) const {
-        float xi = g.next(), acc = 0.0f;
+        float xi = g.next();
         int pick = n - 1;
 #pragma unroll
         for (int k = 2; k >= 0; k--) {  // the first lobe whose running sum passes xi
@@ -413,7 +413,6 @@ struct Pdf {
             if (k < n - 1 && xi < upto)
                 pick = k;
         }
-        (void)acc;
         Lobe l = lobe[0];
 #pragma unroll
         for (int k = 1; k < 3; k++)

@@ -42,7 +42,6 @@ struct RecordSource {
     GuideRecords R;
     uint32_t step;
     const float* stats;  // [1]: sum of the batch's weights
-    MYPBR_DEV long long count(long long rows) const { return rows; }
     MYPBR_DEV bool pick(long long i, uint32_t& r) const {
         uint32_t n = *R.count;
         if (i < 0 || n == 0)
@@ -120,20 +119,6 @@ struct RowSink {
             o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
     }
 };
-
-MYPBR_DEV void copy_u4(void* dst, const void* src, int bytes) {
-    const uint4* s = reinterpret_cast<const uint4*>(src);
-    uint4* d = reinterpret_cast<uint4*>(dst);
-    for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x)
-        d[k] = s[k];
-}
-
-// Row `row` of a canonical K = 128 (batch) tile holding a transposed matrix:
-// writes value v of feature f at (f, row).
-MYPBR_DEV void store_col_bf16(__nv_bfloat16* tileT, int row, int features, const float* v) {
-    for (int f = 0; f < features; f++)
-        tileT[canon(f, row, 128)] = __float2bfloat16_rn(v[f]);
-}
 
 // Training CTA: kTrainGroups groups of 128 threads (a thread per sample row),
 // each group on its own tile of 128 samples, all sharing one resident copy

@@ -1873,7 +1873,6 @@ class Loader {
         if (at.material != default_material)
             return fail("vox models take their materials from the file's palette");
         const Xf& xform = at.xform;
-        const bool transformed = at.moved;
         VoxFile vox;
         std::string err;
         if (!read_vox(file, vox, err))
