@@ -1,8 +1,9 @@
 // Training of the guiding network on the tensor cores, its Adam optimiser,
 // and pointwise entry points that the tests compare with the CPU oracle.
 //
-// One training step: k_guide_prep sums the sample weights of a batch drawn
-// from the recorded vertices; k_guide_train runs forward and backward for
+// One training step: k_guide_prep, twice, sums the sample weights of a batch
+// drawn from the recorded vertices (their mean, then the sum with each weight
+// capped at a multiple of it); k_guide_train runs forward and backward for
 // tiles of 128 samples (groups of 128 threads, a thread per sample, sharing
 // the CTA's resident weights) and adds the weight gradients into per-CTA
 // FP32 partial sums; k_guide_adam sums the partials, updates the FP32 master
@@ -36,12 +37,22 @@ MYPBR_DEV float record_weight(const GuideRecords& R, uint32_t r, uint32_t slot) 
     return isfinite(c) ? fminf(fmaxf(c, 0.0f), 1e6f) : 0.0f;
 }
 
+// A training record's weight is capped at this multiple of the batch's mean
+// weight. A rare path that carries a very large contribution (a caustic, a
+// glint of the sun) would otherwise take most of a batch's loss and pull a
+// lobe toward its one direction. The cap shapes only what the network is
+// fitted to; the renderer's estimator stays unbiased whatever it learns.
+constexpr float kGuideWeightCap = 256.0f;
+
 // Training rows drawn from the recorded vertices (uniformly, by a hash of
 // the step and the row).
 struct RecordSource {
     GuideRecords R;
     uint32_t step;
-    const float* stats;  // [1]: sum of the batch's weights
+    const float* stats;  // [1]: sum of the batch's capped weights; [2]: the rows drawn; [3]: the uncapped sum
+    // The cap on one record's weight: kGuideWeightCap x the batch's mean
+    // uncapped weight.
+    MYPBR_DEV float weight_cap() const { return kGuideWeightCap * stats[3] / fmaxf(stats[2], 1.0f); }
     MYPBR_DEV bool pick(long long i, uint32_t& r) const {
         uint32_t n = *R.count;
         if (i < 0 || n == 0)
@@ -67,7 +78,7 @@ struct RecordSource {
         float total = stats[1];
         if (!pick(i, r) || !(total > 0.0f))
             return 0.0f;
-        float c = record_weight(R, r, r / uint32_t(R.depth)) / total;
+        float c = fminf(record_weight(R, r, r / uint32_t(R.depth)), weight_cap()) / total;
         if (c <= 0.0f)
             return 0.0f;
         float4 d = R.dir[r];
@@ -355,19 +366,31 @@ __global__ void k_guide_sum_partials(const float* partial, int ctas, int params,
     }
 }
 
-// Sum of the batch's weights (normalises the loss so the weights sum to 1).
-__global__ void k_guide_prep(RecordSource src, long long rows, float* stats) {
-    float acc = 0.0f;
+// The batch's weights: pass 0 sums them uncapped (stats[3]) and counts the
+// rows drawn (stats[2]); pass 1 sums them capped (stats[1], which normalises
+// the loss so the weights used sum to 1).
+__global__ void k_guide_prep(RecordSource src, long long rows, float* stats, int pass) {
+    const float cap = pass == 1 ? src.weight_cap() : 0.0f;
+    float acc = 0.0f, drawn = 0.0f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < rows;
          i += (long long)gridDim.x * blockDim.x) {
         uint32_t r;
-        if (src.pick(i, r))
-            acc += record_weight(src.R, r, r / uint32_t(src.R.depth));
+        if (src.pick(i, r)) {
+            const float w = record_weight(src.R, r, r / uint32_t(src.R.depth));
+            acc += pass == 1 ? fminf(w, cap) : w;
+            drawn += 1.0f;
+        }
     }
-    for (int o = 16; o > 0; o >>= 1)
+    for (int o = 16; o > 0; o >>= 1) {
         acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0 && acc != 0.0f)
-        atomicAdd(stats + 1, acc);
+        drawn += __shfl_xor_sync(0xffffffffu, drawn, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (acc != 0.0f)
+            atomicAdd(stats + (pass == 1 ? 1 : 3), acc);
+        if (pass == 0 && drawn != 0.0f)
+            atomicAdd(stats + 2, drawn);
+    }
 }
 
 MYPBR_DEV void param_coords(int p, int& l, int& j, int& t, int& in) {
@@ -753,7 +776,8 @@ int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaSt
     for (int s = 0; s < steps; s++) {
         RecordSource src{g.rec, uint32_t(g.steps * 7919 + 17), g.stats};
         MYPBR_CUDA(cudaMemsetAsync(g.stats, 0, 4 * sizeof(float), st));
-        k_guide_prep<<<G->sm_count * 2, 256, 0, st>>>(src, rows, g.stats);
+        k_guide_prep<<<G->sm_count * 2, 256, 0, st>>>(src, rows, g.stats, 0);
+        k_guide_prep<<<G->sm_count * 2, 256, 0, st>>>(src, rows, g.stats, 1);
         MYPBR_CUDA(cudaGetLastError());
         int rc = train_dispatch(g.hidden, net, src, rows, g.train_ctas, g.scratch, g.partial, g.stats, st);
         if (rc != MYPBR_OK)

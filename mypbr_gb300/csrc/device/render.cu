@@ -1455,7 +1455,7 @@ int render_wave(mypbr_gpu_scene* G, RenderSetup& R, int wave, int pass0, int sav
                         kGuideLr, st);
         if (s != MYPBR_OK || (s = T.end()) != MYPBR_OK)
             return s;
-        launches += 3 * steps;
+        launches += 4 * steps;  // two weight passes, the step, Adam
     }
     return MYPBR_OK;
 }
