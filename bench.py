@@ -503,7 +503,7 @@ def run_voxel_hall(args):
     render(Gg, 64, args.hidden, 7)  # warm-up: guiding buffers and network
     mp.guide_configure(Gg, alpha=args.guide_alpha, depths=args.guide_depths, alpha_deep=args.guide_alpha_deep)
     mp.guide_schedule(Gg, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps,
-                      use_after=args.use_after)
+                      use_after=args.use_after, weight_cap=args.weight_cap)
     curves = {}
     for name, guided in (("plain", 0), ("guided", args.hidden)):
         pts = []
@@ -571,6 +571,7 @@ def run_voxel_hall(args):
                        "guide_hidden_layers": args.hidden, "guide_alpha": args.guide_alpha,
                        "guide_alpha_deep": args.guide_alpha_deep, "guide_depths": args.guide_depths,
                        "guide_schedule": {"steps_early": args.steps_early, "steps_late": args.steps_late,
+                                          "weight_cap": args.weight_cap,
                                           "max_steps": args.max_steps, "use_after": args.use_after},
                        "sky": "atmosphere (procedural, Earth densities, lit by the sun's settings)",
                        "sun": "elevation 40 azimuth 160 intensity 1000 angle 0.54"},
@@ -831,7 +832,7 @@ def run_hall_render(args):
     mp.set_launch(G, block=args.block, traversal=args.traversal)
     mp.guide_configure(G, alpha=args.guide_alpha, depths=args.guide_depths, alpha_deep=args.guide_alpha_deep)
     mp.guide_schedule(G, steps_early=args.steps_early, steps_late=args.steps_late, max_steps=args.max_steps,
-                      use_after=args.use_after)
+                      use_after=args.use_after, weight_cap=args.weight_cap)
     cam = scene.camera
     cam.samples_per_pixel = args.spp
     cam.guided = args.hidden
@@ -898,6 +899,8 @@ def main():
     p.add_argument("--steps-early", type=int, default=16, help="voxel_hall: Adam steps after each early wave")
     p.add_argument("--steps-late", type=int, default=4, help="voxel_hall: Adam steps after each later wave")
     p.add_argument("--max-steps", type=int, default=1500, help="voxel_hall: training steps in all")
+    p.add_argument("--weight-cap", type=float, default=256.0,
+                   help="voxel_hall: a training record's weight at most this x its batch's mean (0: no cap)")
     args = p.parse_args()
     if args.workload != "sphere_field":
         sys.path.insert(0, os.path.join(ROOT, "oracle"))

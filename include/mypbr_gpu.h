@@ -750,11 +750,14 @@ int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths, f
  * reference): Adam steps after each of the first 8 waves of a guided render
  * (small waves, every path recorded; default 16), after each later wave
  * (default 4), the total after which recording and training stop (default
- * 1500), and the steps taken before the mixture is sampled at all (default
+ * 1500), the steps taken before the mixture is sampled at all (default
  * 128, the end of the first recorded waves; until then guided renders sample
- * as plain ones). Applies from the next wave. */
+ * as plain ones), and the cap on one training record's weight as a multiple
+ * of its batch's mean weight (default 256; 0 for no cap, else 1 to 1e6), so
+ * that a few very bright paths cannot take over the fit. Applies from the
+ * next wave. */
 int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps,
-                         int32_t use_after);
+                         int32_t use_after, float weight_cap);
 
 /* the network's encoded inputs (n x 128, BF16 values as floats) of n
  * vertices given by their 7 scalars in [0, 1] (n x 7). */

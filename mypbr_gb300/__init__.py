@@ -165,7 +165,7 @@ def lib():
     L.mypbr_write_image.argtypes = [ctypes.c_char_p, dp, i32, i32, ctypes.POINTER(DisplayOptsStruct), ctypes.c_int]
     L.mypbr_guide_reset.argtypes = [vp]
     L.mypbr_guide_configure.argtypes = [vp, ctypes.c_float, i32, ctypes.c_float]
-    L.mypbr_guide_schedule.argtypes = [vp, i32, i32, i32, i32]
+    L.mypbr_guide_schedule.argtypes = [vp, i32, i32, i32, i32, ctypes.c_float]
     L.mypbr_guide_test_encode.argtypes = [fp, i64, fp]
     L.mypbr_gpu_test_spawn.argtypes = [vp, fp, i64, ip]
     L.mypbr_guide_test_forward.argtypes = [ctypes.c_int, fp, fp, i64, fp]
@@ -586,11 +586,11 @@ def guide_configure(gpu_scene, alpha=0.5, depths=4, alpha_deep=-1.0):
                                       int(depths), float(alpha_deep)))
 
 
-def guide_schedule(gpu_scene, steps_early=16, steps_late=4, max_steps=1500, use_after=128):
+def guide_schedule(gpu_scene, steps_early=16, steps_late=4, max_steps=1500, use_after=128, weight_cap=256.0):
     """The training schedule of the scene handle's guiding network
     (mypbr_guide_schedule)."""
     check(lib().mypbr_guide_schedule(gpu_scene.handle, int(steps_early), int(steps_late), int(max_steps),
-                                     int(use_after)))
+                                     int(use_after), float(weight_cap)))
 
 
 def rebuild_bvh(gpu_scene):

@@ -69,6 +69,7 @@ struct GuideState {
     // which recording and training stop
     int steps_early = 16, steps_late = 4, max_steps = 1500;
     int use_after = 128;  // steps before the mixture is sampled at all
+    float weight_cap = 256.0f;  // a record's training weight at most this x the batch's mean (0: no cap)
     // recording buffers (slot-indexed, grown with the render buffers)
     GuideRecords rec{};
     size_t rec_slots = 0;

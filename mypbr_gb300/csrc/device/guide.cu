@@ -37,22 +37,21 @@ MYPBR_DEV float record_weight(const GuideRecords& R, uint32_t r, uint32_t slot) 
     return isfinite(c) ? fminf(fmaxf(c, 0.0f), 1e6f) : 0.0f;
 }
 
-// A training record's weight is capped at this multiple of the batch's mean
-// weight. A rare path that carries a very large contribution (a caustic, a
-// glint of the sun) would otherwise take most of a batch's loss and pull a
-// lobe toward its one direction. The cap shapes only what the network is
-// fitted to; the renderer's estimator stays unbiased whatever it learns.
-constexpr float kGuideWeightCap = 256.0f;
-
 // Training rows drawn from the recorded vertices (uniformly, by a hash of
 // the step and the row).
+// A training record's weight can be capped at a multiple of the batch's mean
+// weight (mypbr_guide_schedule's weight_cap). A rare path that carries a very
+// large contribution (a caustic, a glint of the sun) would otherwise take
+// most of a batch's loss and pull a lobe toward its one direction. The cap
+// shapes only what the network is fitted to; the renderer's estimator stays
+// unbiased whatever it learns.
 struct RecordSource {
     GuideRecords R;
     uint32_t step;
     const float* stats;  // [1]: sum of the batch's capped weights; [2]: the rows drawn; [3]: the uncapped sum
-    // The cap on one record's weight: kGuideWeightCap x the batch's mean
-    // uncapped weight.
-    MYPBR_DEV float weight_cap() const { return kGuideWeightCap * stats[3] / fmaxf(stats[2], 1.0f); }
+    float cap;           // the cap as a multiple of the batch's mean weight; 0: none
+    // The cap on one record's weight: `cap` x the batch's mean uncapped weight.
+    MYPBR_DEV float weight_cap() const { return cap > 0.0f ? cap * stats[3] / fmaxf(stats[2], 1.0f) : 3.0e38f; }
     MYPBR_DEV bool pick(long long i, uint32_t& r) const {
         uint32_t n = *R.count;
         if (i < 0 || n == 0)
@@ -774,7 +773,7 @@ int guide_train(mypbr_gpu_scene* G, int steps, int batch_tiles, float lr, cudaSt
     long long rows = (long long)batch_tiles * 128;
     GuideNetView net = view_of(g, G->dev.error);
     for (int s = 0; s < steps; s++) {
-        RecordSource src{g.rec, uint32_t(g.steps * 7919 + 17), g.stats};
+        RecordSource src{g.rec, uint32_t(g.steps * 7919 + 17), g.stats, g.weight_cap};
         MYPBR_CUDA(cudaMemsetAsync(g.stats, 0, 4 * sizeof(float), st));
         k_guide_prep<<<G->sm_count * 2, 256, 0, st>>>(src, rows, g.stats, 0);
         k_guide_prep<<<G->sm_count * 2, 256, 0, st>>>(src, rows, g.stats, 1);
@@ -837,7 +836,7 @@ int mypbr_guide_configure(mypbr_gpu_scene* scene, float alpha, int32_t depths, f
 }
 
 int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t steps_late, int32_t max_steps,
-                         int32_t use_after) {
+                         int32_t use_after, float weight_cap) {
     if (!scene) {
         set_error_message("mypbr_guide_schedule: null scene");
         return MYPBR_ERR_INVALID_ARGUMENT;
@@ -848,10 +847,15 @@ int mypbr_guide_schedule(mypbr_gpu_scene* scene, int32_t steps_early, int32_t st
                           "non-negative");
         return MYPBR_ERR_INVALID_ARGUMENT;
     }
+    if (!(weight_cap == 0.0f || (weight_cap >= 1.0f && weight_cap <= 1.0e6f))) {
+        set_error_message("mypbr_guide_schedule: weight_cap must be 0 (no cap) or lie in [1, 1e6]");
+        return MYPBR_ERR_INVALID_ARGUMENT;
+    }
     scene->guide.steps_early = steps_early;
     scene->guide.steps_late = steps_late;
     scene->guide.max_steps = max_steps;
     scene->guide.use_after = use_after;
+    scene->guide.weight_cap = weight_cap;
     return MYPBR_OK;
 }
 

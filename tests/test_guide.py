@@ -238,6 +238,18 @@ def test_guided_settings_stay_unbiased(alpha, depths):
         mp.guide_configure(G, alpha=0.5, depths=0)
 
 
+@pytest.mark.gpu
+def test_guide_schedule_checks_the_weight_cap():
+    sc = mp.load_scene(scene_path("cornell_c1.scene"))
+    G = mp.GpuScene(sc)
+    mp.guide_schedule(G, weight_cap=0.0)  # no cap
+    mp.guide_schedule(G, weight_cap=64.0)
+    for bad in (0.5, -1.0, 2.0e6, float("nan")):
+        with pytest.raises(mp.MypbrError, match="weight_cap"):
+            mp.guide_schedule(G, weight_cap=bad)
+    G.close()
+
+
 def test_guide_configure_checks_its_handle():
     with pytest.raises(mp.MypbrError, match="null scene"):
         mp.guide_configure(None)
