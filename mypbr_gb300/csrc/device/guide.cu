@@ -38,13 +38,12 @@ MYPBR_DEV float record_weight(const GuideRecords& R, uint32_t r, uint32_t slot) 
 }
 
 // Training rows drawn from the recorded vertices (uniformly, by a hash of
-// the step and the row).
-// A training record's weight can be capped at a multiple of the batch's mean
-// weight (mypbr_guide_schedule's weight_cap). A rare path that carries a very
-// large contribution (a caustic, a glint of the sun) would otherwise take
-// most of a batch's loss and pull a lobe toward its one direction. The cap
-// shapes only what the network is fitted to; the renderer's estimator stays
-// unbiased whatever it learns.
+// the step and the row). A record's weight can be capped at a multiple of
+// the batch's mean weight (mypbr_guide_schedule's weight_cap): a rare path
+// that carries a very large contribution (a caustic, a glint of the sun)
+// would otherwise take most of a batch's loss and pull a lobe toward its one
+// direction. The cap shapes only what the network is fitted to; the
+// renderer's estimator stays unbiased whatever it learns.
 struct RecordSource {
     GuideRecords R;
     uint32_t step;
