@@ -651,7 +651,7 @@ int guide_fit_box(mypbr_gpu_scene* G, cudaStream_t st) {
         for (int k = 0; k < kBoxBins; k++)
             total += H[k];
         if (total < 1024)
-            return MYPBR_OK;  // too few vertices to judge: the scene box stays
+            return MYPBR_OK;  // too few vertices to go by: the scene box stays
         uint64_t run = 0;
         int lo = 0, hi = kBoxBins - 1;
         for (int k = 0; k < kBoxBins; k++) {
