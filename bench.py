@@ -260,7 +260,7 @@ def run_ours(args):
     cam.samples_per_pixel = args.spp
     cam.seed = 1000 + rank  # independent samples per rank
     gpu = mp.GpuScene(scene)
-    mp.set_launch(gpu, block=args.block, traversal=args.traversal)
+    mp.set_launch(gpu, block=args.block, traversal=args.traversal, wave_paths=args.wave_paths)
     L = mp.lib()
     c, o = cam.structs()
     w, h = c.image_width, c.image_height
@@ -327,7 +327,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         g2 = mp.GpuScene(scene)
-        mp.set_launch(g2, block=args.block, traversal=args.traversal)
+        mp.set_launch(g2, block=args.block, traversal=args.traversal, wave_paths=args.wave_paths)
         mp.check(L.mypbr_gpu_render(g2.handle, ctypes.byref(c), ctypes.byref(o), ctypes.c_void_p(host.ctypes.data),
                                     None, None, None, 0, mp.PASS_CALLBACK(), None))
         g2.close()
@@ -388,7 +388,7 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
                 "config": dict(WORKLOAD, spp=args.spp, parallelism=f"samples x{world}", traversal=args.traversal,
-                               block=args.block or 256),
+                               block=args.block or 256, wave_paths=args.wave_paths or "default"),
                 "gpu_launches": int(launches),
                 "rays": {"extension_per_path": totals["ext"] / (paths_per_step * args.steps),
                          "shadow_per_path": totals["sh"] / (paths_per_step * args.steps),
@@ -875,7 +875,8 @@ def main():
                         "boxes")
     p.add_argument("--block", type=int, default=0, choices=[0, 128, 256])
     p.add_argument("--autotune", action="store_true", help="cornell / triangle_room: autotuned launch settings")
-    p.add_argument("--wave-paths", type=int, default=0, help="cornell / triangle_room: paths per wave (0: default)")
+    p.add_argument("--wave-paths", type=int, default=0,
+                   help="sphere_field / cornell / triangle_room: paths per wave (0: the library's default)")
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--batch-wave-paths", type=int, default=8 << 20, help="batch: paths in flight per job")
     p.add_argument("--hall-width", type=int, default=0,

@@ -634,19 +634,20 @@ int mypbr_gpu_render_batch(mypbr_batch_job* jobs, int32_t n);
  * 5: each lane walks the tree collapsed to 8 children per node with
  * quantised boxes; 0, the default, is 4 for trees whose leaves are mostly
  * spheres and 3 otherwise), with the Mpaths/s of each of the 40 trials
- * (traversal 1 to 5; within each, block 128 then 256; within each, 4M, 8M,
- * 16M, 32M paths; 0 for trials skipped because the scene's tree does not
- * allow that walk). */
+ * (traversal 1 to 5; within each, block 128 then 256; within each, 16M,
+ * 32M, 64M, 128M paths; 0 for trials skipped because the scene's tree does
+ * not allow that walk). */
 typedef struct mypbr_tune_result {
     int32_t block;
     int32_t traversal;
     int64_t wave_paths;
     double mpaths_per_s;
-    double trial_mpaths[40];  /* traversal 1..5 x block 128, 256 x 4, 8, 16, 32 M paths per wave */
+    double trial_mpaths[40];  /* traversal 1..5 x block 128, 256 x 16, 32, 64, 128 M paths per wave */
 } mypbr_tune_result;
 
 /* Sets the launch settings the autotuner would set (0 keeps a setting's
- * default: block 256, 32M paths per wave, traversal 0). Traversal: 0 the
+ * default: block 256, 128M paths per wave for plain renders and 32M for
+ * guided ones, traversal 0). Traversal: 0 the
  * scene's default, 1 lanes that take new rays, 2 the 4-wide tree, 3 postponed
  * leaves, 4 the plain binary walk, 5 the 8-wide tree with quantised boxes. A
  * traversal the scene's tree does not allow (2 or 5 without that tree, 3 or

@@ -100,7 +100,7 @@ def test_autotune_keeps_the_result():
     cam = camera_of(sc, 64, 32)
     before = cam.render(G).radiance
     r = mp.autotune(cam, G)
-    assert r["block"] in (128, 256) and r["wave_paths"] in (4 << 20, 8 << 20, 16 << 20, 32 << 20)
+    assert r["block"] in (128, 256) and r["wave_paths"] in (16 << 20, 32 << 20, 64 << 20, 128 << 20)
     assert r["traversal"] in (1, 2, 3, 4, 5) and len(r["trials"]) == 40
     assert all(t > 0 for t in r["trials"]) and r["mpaths_per_s"] == max(r["trials"])
     after = cam.render(G).radiance
